@@ -1,0 +1,192 @@
+/*
+ * hybird_gpu.h -- C-ABI of the GB300 (sm_103a) time-step library for hybird.
+ *
+ * One opaque context owns every device buffer of one simulation on one GPU.  The
+ * reference's per-step class methods become forwarders into these calls (see
+ * INTEGRATION.md); every call returns an int status (HB_OK == 0) instead of calling
+ * exit() as the reference does (macros.h:8, LB.cpp:1057, LB.cpp:1460).
+ *
+ * Units: every quantity crossing this boundary is in the reference's lattice units
+ * with unitLength = unitTime = unitDensity = 1 (LB.cpp:93-98); hb_create rejects other
+ * unit values.  Lattice arrays are indexed like the reference, i = x + y*X + z*X*Y
+ * (LB.cpp:2314-2370); per-direction and per-component arrays are structure-of-arrays,
+ * component-major: f[j*N + i], u[c*N + i].
+ */
+#ifndef HYBIRD_GPU_H
+#define HYBIRD_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define HB_OK               0
+#define HB_ERR_ARG          1   /* bad argument, NULL pointer, size mismatch          */
+#define HB_ERR_UNSUPPORTED  2   /* feature outside the implemented path               */
+#define HB_ERR_CUDA         3   /* CUDA runtime error (message via hb_last_error)      */
+#define HB_ERR_NOMEM        4   /* device allocation failed                            */
+#define HB_ERR_CAPACITY     5   /* a fixed-capacity device list overflowed             */
+#define HB_ERR_STATE        6   /* call out of order (e.g. step before upload)         */
+#define HB_ERR_NUMERIC      7   /* NaN/Inf detected in density or velocity             */
+
+/* ---- enumerations ------------------------------------------------------------------ */
+#define HB_FP64   0   /* populations stored and computed in FP64                           */
+#define HB_FP32   1   /* populations stored as f_i - w_i*rho0 in FP32, FP32 compute        */
+#define HB_FP16S  2   /* populations stored as scaled FP16 deviations, FP32 compute        */
+
+#define HB_BGK    0   /* single relaxation time, node.cpp:158-165                          */
+#define HB_TRT    1   /* two relaxation times (magic parameter), not in the reference      */
+
+#define HB_LINEAR   0 /* ContactModel LINEAR  (elmt.h:137)                                 */
+#define HB_HERTZIAN 1 /* ContactModel HERTZIAN (elmt.h:137)                                */
+
+/* node type codes, identical to nodeType::t (node.h:75-86) */
+#define HB_T_FLUID     0
+#define HB_T_GAS       2
+#define HB_T_INTERFACE 3
+#define HB_T_PERIODIC  4
+#define HB_T_STATWALL  7
+#define HB_T_DYNWALL   8
+
+/* ---- parameters -------------------------------------------------------------------- */
+/* Mirrors the cfg keys parsed by LB::latticeBoltzmannGet (LB.cpp:85-188),
+ * DEM::discreteElementGet (DEM.cpp:13-183) and parseConfigFile (hybird.cpp:132-223). */
+typedef struct hb_params {
+    int32_t lb_size[3];        /* lbSizeX/Y/Z: nodes incl. the two boundary layers          */
+    int32_t boundary[6];       /* boundary0..5 (x-,x+,y-,y+,z-,z+): 4, 7 or 8               */
+    double  units[3];          /* unitLength, unitTime, unitDensity: must be 1.0            */
+    double  init_visc;         /* initVisc (kinematic, lattice units): tau = 0.5 + 3 nu     */
+    double  init_velocity[3];  /* initVelocityX/Y/Z                                          */
+    double  lbF[3];            /* lbFX/Y/Z body force (also DEM gravity, DEM.cpp:194)        */
+    int32_t force_field;       /* forceFieldSolve: 0 zeroes lbF in collision (LB.cpp:1074)   */
+    int32_t non_newtonian;     /* nonNewtonianSolve (Bingham)                                */
+    double  plastic_visc;      /* plasticVisc                                                */
+    double  yield_stress;      /* yieldStress                                                */
+    int32_t turbulence;        /* turbulenceSolve (Smagorinsky)                              */
+    double  turb_const;        /* turbConst = Cs^2                                           */
+    int32_t free_surface;      /* freeSurfaceSolve                                           */
+    int32_t collision;         /* HB_BGK | HB_TRT                                            */
+    double  trt_magic;         /* TRT magic parameter Lambda (e.g. 3/16)                     */
+    int32_t precision;         /* HB_FP64 | HB_FP32 | HB_FP16S                               */
+    double  gas_box[2];        /* dam-break column: gas where x >= gx*X or z >= gz*Z;
+                                  {0,0} disables (interface init as LB.cpp:787-814)          */
+    int32_t lb_solve;          /* lbSolve: 0 runs DEM only (hybird.cpp:49-64)                */
+    /* DEM (DEM.cpp:13-183) */
+    int32_t dem_solve;         /* demSolve                                                   */
+    int32_t multi_step;        /* multiStep (>= 1): DEM substeps per LB step                 */
+    int32_t contact_model;     /* HB_LINEAR | HB_HERTZIAN                                    */
+    double  density;           /* particle density                                           */
+    double  linear_stiff;      /* linearStiff                                                */
+    double  young_mod;         /* youngMod  (HERTZIAN)                                       */
+    double  poisson;           /* poisson   (HERTZIAN)                                       */
+    double  restitution;       /* restitution                                                */
+    double  visc_tang;         /* viscTang                                                   */
+    double  friction_part;     /* frictionCoefPart                                           */
+    double  friction_wall;     /* frictionCoefWall                                           */
+    double  num_visc;          /* numVisc                                                    */
+    /* capacities of the fixed-size device lists (0 = library default) */
+    int64_t cap_pairs;         /* DEM candidate pairs                                        */
+    int64_t cap_interface;     /* interface cells                                            */
+} hb_params;
+
+/* Spheres: one element per particle (elmt size 1, DEM.cpp:81-127 particle file row). */
+typedef struct hb_elements {
+    int32_t count;
+    const double* radius;      /* [count]                                                    */
+    const double* x0;          /* [3*count] centre, component-major                          */
+    const double* x1;          /* [3*count] velocity                                         */
+    const double* w0;          /* [3*count] angular velocity                                 */
+    const double* q0;          /* [4*count] orientation quaternion (p,q,r,s); NULL = (1,0,0,0) */
+} hb_elements;
+
+/* Fixed spherical objects (DEM.cpp:129-173 object file row); they become static-wall
+ * lattice nodes (LB.cpp:535-550) and DEM contact partners (DEM.cpp:2060-2136). */
+typedef struct hb_objects {
+    int32_t count;
+    const double* radius;      /* [count]   */
+    const double* x0;          /* [3*count] */
+    const double* x1;          /* [3*count] velocity (contact only) */
+} hb_objects;
+
+/* Device-side status word, read back at output steps (all counters since the last read). */
+typedef struct hb_status {
+    int32_t numeric_error;     /* NaN/Inf seen in rho or u                                   */
+    int32_t capacity_error;    /* a device list overflowed                                   */
+    int32_t wait_timeout;      /* a bounded device wait gave up                              */
+    int32_t reserved;
+    int64_t interface_cells;   /* current interface count                                    */
+    int64_t active_nodes;      /* fluid + interface nodes (activeNodes.size())               */
+    int64_t pairs;             /* DEM candidate pairs (neighborTable.size()/2)               */
+    int64_t contacts;          /* overlapping pairs in the last DEM substep                  */
+    double  mass_surplus;      /* FP64 free-surface ledger of the last step                  */
+    double  total_mass;        /* FP64 sum of mass over active non-particle nodes            */
+} hb_status;
+
+typedef struct hb_ctx hb_ctx;
+
+/* ---- lifecycle ------------------------------------------------------------------- */
+/* Replaces the LB/DEM constructors + LB::latticeDefinition (LB.cpp:42-83) and
+ * DEM::discreteElementInit parameter setup (DEM.cpp:185-297).  Allocates all device
+ * memory once; nothing is allocated per step. */
+int hb_create(const hb_params* params, hb_ctx** out);
+int hb_destroy(hb_ctx* ctx);
+const char* hb_last_error(void);
+
+/* Builds the initial state on the device, as LB::latticeBolzmannInit does
+ * (LB.cpp:190-219): lattice boundaries, walls (DEM.cpp:435-633), particle flags
+ * (LB.cpp:475-495), objects (LB.cpp:535-550), interface (LB.cpp:787-814), hydrostatic
+ * variables (LB.cpp:909-944), wall nodes (LB.cpp:946-996) and f = f_eq.
+ * elements/objects may be NULL. */
+int hb_init(hb_ctx* ctx, const hb_elements* elements, const hb_objects* objects);
+
+/* Overwrites the lattice state with a host-built one (the reference's own init, or a
+ * checkpoint).  N = X*Y*Z.  type[N] node codes, inside[N] particle flags, solid[N]
+ * solid indices, f[19*N] (NULL: f = f_eq(n,u) as node::initialize, node.cpp:26-61),
+ * n[N], u[3*N], mass[N], visc[N] (NULL: init_visc). */
+int hb_upload_lattice(hb_ctx* ctx, const uint8_t* type, const uint8_t* inside,
+                      const uint32_t* solid, const double* f, const double* n,
+                      const double* u, const double* mass, const double* visc);
+
+/* ---- time step (goCycle order, hybird.cpp:35-66) ----------------------------------- */
+int hb_dem_step(hb_ctx* ctx);        /* DEM::discreteElementStep        DEM.cpp:331-376  */
+int hb_fs_step(hb_ctx* ctx);         /* LB::latticeBoltzmannFreeSurfaceStep LB.cpp:235-245 */
+int hb_coupling_step(hb_ctx* ctx);   /* LB::latticeBoltzmannCouplingStep LB.cpp:247-280  */
+int hb_lb_step(hb_ctx* ctx);         /* LB::latticeBolzmannStep         LB.cpp:221-233  */
+/* nsteps whole cycles (DEM, free surface, coupling, LB) replayed from one CUDA graph. */
+int hb_cycle(hb_ctx* ctx, int32_t nsteps);
+int hb_synchronize(hb_ctx* ctx);
+
+/* ---- download (output steps and tests) --------------------------------------------- */
+/* Any pointer may be NULL.  f is the post-streaming population (the reference's
+ * node::f between steps); n,u are the values of the last reconstruction (with u
+ * shifted by half the force, as the reference leaves them after collision). */
+int hb_download_lattice(hb_ctx* ctx, uint8_t* type, uint8_t* inside, uint32_t* solid,
+                        double* f, double* n, double* u, double* mass, double* visc,
+                        double* hydro_force);
+/* Element state (component-major [3*count]); FHydro/MHydro as last computed by the
+ * coupling (LB.cpp:1851-1919), FParticle/FWall/MParticle/MWall of the last substep. */
+int hb_download_elements(hb_ctx* ctx, double* x0, double* x1, double* w, double* q0,
+                         double* fhydro, double* mhydro, double* fparticle, double* fwall,
+                         double* mparticle, double* mwall, double* fluid_volume);
+/* Candidate pair list as sorted (min,max) pairs, like DEM::neighborTable
+ * (DEM.cpp:1369-1494) after normalisation.  *count receives the pair count. */
+int hb_download_pairs(hb_ctx* ctx, uint32_t* pairs, int64_t capacity, int64_t* count);
+/* Interface cells, ascending node index.  *count receives the count. */
+int hb_download_interface(hb_ctx* ctx, uint32_t* cells, int64_t capacity, int64_t* count);
+/* Per-wall hydrodynamic force (walls[].FHydro, LB.cpp:1334) [3*nwalls]; *nwalls = count. */
+int hb_download_walls(hb_ctx* ctx, double* fhydro, double* fparticle, int32_t* nwalls);
+int hb_get_status(hb_ctx* ctx, hb_status* status);
+
+/* ---- measurement ------------------------------------------------------------------- */
+/* Runs nsteps cycles on the context's stream bracketed by CUDA events and returns the
+ * elapsed device time of the whole cycles and of the stream-collide kernel alone. */
+int hb_time_cycles(hb_ctx* ctx, int32_t nsteps, float* ms_total, float* ms_lb_kernel,
+                   int32_t* kernels_per_cycle);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HYBIRD_GPU_H */

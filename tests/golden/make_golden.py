@@ -1,0 +1,228 @@
+"""Generate the parity fixtures in this folder from the reference hybird code itself.
+
+Test infrastructure only.  For every case below this script writes a .cfg file (the
+reference's own GetPot format) plus particle/object files, runs ``oracle/_ref/ref_dump``
+(the unmodified reference sources, built by ``make -C oracle ref``) with
+OMP_NUM_THREADS=1 -- coupled force sums in the reference are thread-order dependent
+(LB.cpp:1897) -- and stores the reference's FP64 state at the listed step counts as a
+compressed ``<case>.npz``.
+
+Run in a container that has the reference tree:
+
+    make -C oracle ref && python tests/golden/make_golden.py
+
+The fixtures are committed; the GPU host never runs this script.
+"""
+import json
+import os
+import random
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF_DUMP = os.path.join(REPO, "oracle", "_ref", "ref_dump")
+
+# ----------------------------------------------------------------------------------
+# cases
+# ----------------------------------------------------------------------------------
+
+BASE = dict(
+    problemName="NONE", demSolve=1, lbSolve=1, freeSurfaceSolve=0, forceFieldSolve=1,
+    nonNewtonianSolve=0, turbulenceSolve=0, unitLength=1.0, unitTime=1.0, unitDensity=1.0,
+    initVisc=0.1, plasticVisc=0.0, yieldStress=0.0, turbConst=0.0, slipCoefficient=0.0,
+    initVelocityX=0.0, initVelocityY=0.0, initVelocityZ=0.0,
+    lbFX=0.0, lbFY=0.0, lbFZ=0.0, maxTime=1e9, maximumTimeSteps=0, screenExpTime=0.0,
+    fluidExpTime=0.0, partExpTime=0.0, objectExpTime=0.0, recycleExpTime=0.0, saveCount=0,
+    demInitialRepeat=0.0, lbmInitialRepeat=0, density=2.5, contactModel="LINEAR",
+    youngMod=1.0, poisson=0.3, linearStiff=1e3, restitution=0.8, viscTang=0.5,
+    frictionCoefPart=0.5, frictionCoefWall=0.5, numVisc=0.0, multiStep=1, criticalRatio=0.1,
+    scale=1.0, translateX=0.0, translateY=0.0, translateZ=0.0,
+)
+
+
+def rsa_spheres(seed, n, rmin, rmax, lo, hi, gap=0.0):
+    """Seeded random sequential addition of non-overlapping spheres inside [lo+r, hi-r]^3."""
+    rng = random.Random(seed)
+    out = []
+    tries = 0
+    while len(out) < n and tries < 200000:
+        tries += 1
+        r = rng.uniform(rmin, rmax)
+        c = [rng.uniform(lo[k] + r, hi[k] - r) for k in range(3)]
+        ok = True
+        for (q, rq) in out:
+            d2 = sum((c[k] - q[k]) ** 2 for k in range(3))
+            if d2 < (r + rq + gap) ** 2:
+                ok = False
+                break
+        if ok:
+            out.append((c, r))
+    return out
+
+
+CASES = {
+    # periodic-x/z channel with walls at y=0/Ly-1 (BASELINE config 1 shape, shrunk)
+    "channel_bgk": dict(
+        cfg=dict(lbSizeX=12, lbSizeY=8, lbSizeZ=6, lbFX=2e-5, initVisc=0.1,
+                 boundary0=4, boundary1=4, boundary2=7, boundary3=7, boundary4=4, boundary5=4),
+        spheres=[], objects=[], steps=[0, 1, 5, 40], full=[0, 1, 40]),
+    # moving-wall bounce-back at y+ (type 8; the reference's walls have zero speed) and
+    # static wall at y-, non-zero initial velocity so the wall force is exercised
+    "channel_movwall": dict(
+        cfg=dict(lbSizeX=10, lbSizeY=8, lbSizeZ=6, lbFX=1e-5, lbFZ=-3e-6, initVisc=0.05,
+                 initVelocityX=0.01, initVelocityZ=0.004,
+                 boundary0=4, boundary1=4, boundary2=7, boundary3=8, boundary4=4, boundary5=4),
+        spheres=[], objects=[], steps=[0, 1, 12], full=[0, 1, 12]),
+    # Bingham + Smagorinsky inline viscosity (node.cpp:103-145)
+    "channel_bingham_smag": dict(
+        cfg=dict(lbSizeX=10, lbSizeY=8, lbSizeZ=6, lbFX=4e-5, initVisc=0.1,
+                 nonNewtonianSolve=1, plasticVisc=1.0 / 30.0, yieldStress=3e-6,
+                 turbulenceSolve=1, turbConst=0.01,
+                 boundary0=4, boundary1=4, boundary2=7, boundary3=7, boundary4=4, boundary5=4),
+        spheres=[], objects=[], steps=[0, 1, 10], full=[0, 1, 10]),
+    # closed box with a few spheres: DEM + direct-forcing coupling (LB.cpp:1851-2033)
+    "box_spheres": dict(
+        cfg=dict(lbSizeX=16, lbSizeY=14, lbSizeZ=16, lbFZ=-2e-4, initVisc=0.1, multiStep=3,
+                 boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
+        spheres=("rsa", 11, 7, 2.2, 3.2), objects=[], steps=[0, 1, 2, 10, 30], full=[1, 30]),
+    # DEM only (no LB): spheres against walls and fixed objects (DEM.cpp:1668-2136)
+    "dem_objects": dict(
+        # particles stay > nebrRange from the side walls: the reference keeps only the
+        # first wall in range per particle (DEM.cpp:1502-1511) and would let corner
+        # particles fall through the floor
+        cfg=dict(lbSizeX=32, lbSizeY=32, lbSizeZ=32, lbSolve=0, lbFZ=-1e-3, multiStep=20,
+                 boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
+        spheres=("rsa", 5, 14, 1.6, 2.6, (9.5, 9.5, 6.0), (22.5, 22.5, 28.0)),
+        objects=[(13.0, 14.0, 4.0, 3.0), (19.0, 17.0, 3.5, 2.5)],
+        steps=[0, 1, 50, 100, 150], full=[]),
+    # free-surface dam break (LB.cpp:1492-1804), column x < 0.4 Lx, z < 0.6 Lz
+    "dambreak_fs": dict(
+        cfg=dict(lbSizeX=20, lbSizeY=8, lbSizeZ=12, lbFZ=-5e-4, initVisc=0.05, freeSurfaceSolve=1,
+                 boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
+        spheres=[], objects=[], gasbox=(0.4, 0.6), steps=[0, 1, 2, 5, 20, 60, 150], full=[0, 1, 20, 150]),
+}
+
+
+def write_cfg(path, cfg):
+    with open(path, "w") as fh:
+        for k, v in cfg.items():
+            fh.write(f"{k} = {v}\n")
+
+
+def write_particles(path, spheres):
+    with open(path, "w") as fh:
+        fh.write(f"{len(spheres)}\n")
+        for i, (c, r) in enumerate(spheres):
+            vals = [i, 1, repr(r), repr(c[0]), repr(c[1]), repr(c[2]), 0.0, 0.0, 0.0,
+                    0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0]
+            fh.write(" ".join(str(v) for v in vals) + "\n")
+
+
+def write_objects(path, objects):
+    with open(path, "w") as fh:
+        fh.write(f"{len(objects)}\n")
+        for i, (x, y, z, r) in enumerate(objects):
+            vals = [i, 1, r, x, y, z, 0.0, 0.0, 0.0] + [0.0] * 11
+            fh.write(" ".join(str(v) for v in vals) + "\n")
+
+
+def parse_dump(path):
+    """Return a list of dicts, one per dumped step."""
+    dt = {0: np.float64, 1: np.uint32, 2: np.uint8, 3: np.int64}
+    snaps = []
+    with open(path, "rb") as fh:
+        data = fh.read()
+    off = 0
+    cur = None
+    while off < len(data):
+        name = data[off:off + 32].split(b"\0")[0].decode()
+        code, cnt = struct.unpack_from("<IQ", data, off + 32)
+        off += 44
+        arr = np.frombuffer(data, dtype=dt[code], count=cnt, offset=off).copy()
+        off += cnt * np.dtype(dt[code]).itemsize
+        if name == "header":
+            cur = {}
+            snaps.append(cur)
+        cur[name] = arr
+    return snaps
+
+
+def run_case(name, spec):
+    cfg = dict(BASE)
+    cfg.update(spec["cfg"])
+    sizes = (cfg["lbSizeX"], cfg["lbSizeY"], cfg["lbSizeZ"])
+    if spec["spheres"]:
+        seed, n, rmin, rmax = spec["spheres"][1:5]
+        lo, hi = (1.5, 1.5, 1.5), (sizes[0] - 2.5, sizes[1] - 2.5, sizes[2] - 2.5)
+        if len(spec["spheres"]) > 5:
+            lo, hi = spec["spheres"][5], spec["spheres"][6]
+        spheres = rsa_spheres(seed, n, rmin, rmax, lo, hi, gap=0.3)
+    else:
+        spheres = []
+    with tempfile.TemporaryDirectory() as tmp:
+        cfg["particleFile"] = os.path.join(tmp, "particles.dat")
+        cfg["objectFile"] = os.path.join(tmp, "objects.dat")
+        write_particles(cfg["particleFile"], spheres)
+        write_objects(cfg["objectFile"], spec["objects"])
+        cpath = os.path.join(tmp, "case.cfg")
+        write_cfg(cpath, cfg)
+        out = os.path.join(tmp, "out.bin")
+        cmd = [REF_DUMP, cpath, os.path.join(tmp, "work"), out] + [str(s) for s in spec["steps"]]
+        if spec.get("gasbox"):
+            cmd += ["--gasbox", str(spec["gasbox"][0]), str(spec["gasbox"][1])]
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        subprocess.run(cmd, check=True, cwd=tmp, env=env, stdout=subprocess.DEVNULL, timeout=120)
+        snaps = parse_dump(out)
+
+    store = {}
+    params = {k: v for k, v in cfg.items() if k not in ("particleFile", "objectFile")}
+    store["params_json"] = np.frombuffer(json.dumps(params).encode(), dtype=np.uint8)
+    store["spheres"] = np.array([[c[0], c[1], c[2], r] for (c, r) in spheres], dtype=np.float64).reshape(-1, 4)
+    store["objects"] = np.array(spec["objects"], dtype=np.float64).reshape(-1, 4)
+    store["steps"] = np.array(spec["steps"], dtype=np.int64)
+    lattice = cfg.get("lbSolve", 1) == 1
+    for s in snaps:
+        step = int(s["header"][0])
+        p = f"s{step}_"
+        store[p + "header"] = s["header"]
+        if lattice:
+            store[p + "type"] = s["type"]
+            store[p + "inside"] = s["inside"]
+            store[p + "solid"] = s["solid"]
+            store[p + "has_node"] = s["has_node"]
+            store[p + "n"] = s["n"]
+            store[p + "u"] = s["u"]
+            store[p + "mass"] = s["mass"]
+            store[p + "visc"] = s["visc"]
+            store[p + "interfaceNodes"] = s["interfaceNodes"]
+            store[p + "particleNodes"] = s["particleNodes"]
+            store[p + "totalMass"] = s["totalMass"]
+            store[p + "w_FHydro"] = s["w_FHydro"]
+            if step in spec["full"]:
+                store[p + "f"] = s["f"]
+                store[p + "hydroForce"] = s["hydroForce"]
+        for k in ("e_x0", "e_x1", "e_x2", "e_w", "e_q0", "e_FHydro", "e_MHydro", "e_FParticle",
+                  "e_FWall", "e_MParticle", "e_MWall", "e_fluidVolume", "e_m", "e_I",
+                  "neighborTable", "nearWallTable", "nearObjectTable", "w_FParticle",
+                  "dem_scalars"):
+            store[p + k] = s[k]
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **store)
+    return len(snaps)
+
+
+def main(argv):
+    if not os.path.exists(REF_DUMP):
+        sys.exit("build the reference first: make -C oracle ref")
+    names = argv[1:] or list(CASES)
+    for name in names:
+        n = run_case(name, CASES[name])
+        print(f"{name}: {n} snapshots")
+
+
+if __name__ == "__main__":
+    main(sys.argv)

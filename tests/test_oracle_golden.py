@@ -1,0 +1,70 @@
+"""Pins the CPU oracle (oracle/hb_oracle.cpp) to the reference itself: every fixture in
+tests/golden/ was produced by the unmodified reference sources (make_golden.py).
+
+Single-phase, coupled and free-surface lattice fields must match the reference
+bit-for-bit or to FP64 rounding (1e-13 relative); integer artefacts (node types,
+particle flags, solid indices, interface sets, DEM pair sets) must be identical.
+"""
+import numpy as np
+import pytest
+
+from oracle_port import OracleSim, golden_gasbox, golden_params, load_golden, rel_linf
+
+LATTICE_CASES = ["channel_bgk", "channel_movwall", "channel_bingham_smag", "box_spheres",
+                 "dambreak_fs"]
+TOL = 1e-13
+
+
+def _run(name):
+    d = load_golden(name)
+    p = golden_params(d, gas_box=golden_gasbox(name))
+    sim = OracleSim(p, d["spheres"], d["objects"])
+    return d, sim
+
+
+@pytest.mark.parametrize("name", LATTICE_CASES)
+def test_lattice_matches_reference(name):
+    d, sim = _run(name)
+    done = 0
+    for step in d["steps"]:
+        sim.cycle(int(step) - done)
+        done = int(step)
+        g = {k[len(f"s{step}_"):]: d[k] for k in d.files if k.startswith(f"s{step}_")}
+        o = sim.lattice()
+        np.testing.assert_array_equal(o["type"], g["type"], err_msg=f"{name} step {step} type")
+        np.testing.assert_array_equal(o["inside"], g["inside"], err_msg=f"{name} step {step} inside")
+        act = (g["type"] == 0) | (g["type"] == 3)
+        np.testing.assert_array_equal(o["solid"][act | (g["type"] >= 7)], g["solid"][act | (g["type"] >= 7)])
+        assert rel_linf(o["n"], g["n"], act) <= TOL, (name, step, "n")
+        assert rel_linf(o["u"].reshape(3, -1), g["u"].reshape(3, -1), act) <= TOL, (name, step, "u")
+        assert rel_linf(o["mass"], g["mass"], act) <= TOL, (name, step, "mass")
+        assert rel_linf(o["visc"], g["visc"], act) <= TOL, (name, step, "visc")
+        if "f" in g:
+            assert rel_linf(o["f"].reshape(19, -1), g["f"].reshape(19, -1), act) <= TOL, (name, step, "f")
+            assert rel_linf(o["hydroForce"].reshape(3, -1), g["hydroForce"].reshape(3, -1), act) <= TOL or \
+                np.abs(g["hydroForce"]).max() == 0.0
+        np.testing.assert_array_equal(np.sort(sim.interface()), np.sort(g["interfaceNodes"]))
+        fh, _ = sim.walls()
+        if len(g["w_FHydro"]):
+            assert np.allclose(fh, g["w_FHydro"], rtol=1e-12, atol=1e-15), (name, step, fh, g["w_FHydro"])
+
+
+@pytest.mark.parametrize("name", ["box_spheres", "dem_objects"])
+def test_dem_matches_reference(name):
+    d, sim = _run(name)
+    done = 0
+    for step in d["steps"]:
+        sim.cycle(int(step) - done)
+        done = int(step)
+        pre = f"s{step}_"
+        e = sim.elements()
+        for k, gk in (("x0", "e_x0"), ("x1", "e_x1"), ("w", "e_w"), ("FHydro", "e_FHydro"),
+                      ("MHydro", "e_MHydro"), ("FParticle", "e_FParticle"), ("FWall", "e_FWall")):
+            g = d[pre + gk].reshape(-1, 3).T.reshape(-1)
+            if np.abs(g).max() == 0:
+                assert np.abs(e[k]).max() == 0, (name, step, k)
+            else:
+                assert rel_linf(e[k], g) <= 1e-12, (name, step, k, rel_linf(e[k], g))
+        pairs = sim.pairs().reshape(-1, 2)
+        gp = d[pre + "neighborTable"].reshape(-1, 2)
+        np.testing.assert_array_equal(pairs, gp)  # same sweep order as the reference
