@@ -1,0 +1,296 @@
+"""Benchmark of the coupled LBM-DEM time step (one GB300, replicas for N>1).
+
+Workload (default): coupled sedimentation, 128^3 D3Q19 TRT in a no-slip box, seeded
+non-overlapping spheres r ~ U[4,6] (random sequential addition from seed 2 until it
+jams; the achieved count is reported), density ratio 2.5, gravity 1e-5, linear
+spring-dashpot contacts (kn=1e3, e=0.8, mu=0.5), multiStep 3, populations FP32
+(deviation storage) with FP64 DEM.  A "step" is one whole cycle: DEM substeps, coupling
+masks, fused collide+stream, element force reduction.
+
+value      MLUPS over the active nodes (inside-particle nodes included, as the
+           reference counts activeNodes), device-resident, graph-replayed cycles.
+e2e        same metric through the C-ABI per step with host buffers: hb_cycle(1) plus
+           the host<->device copies a host driver makes every step (body force in,
+           element state and hydrodynamic forces out).
+roofline   the fused collide+stream kernel: algorithmic bytes per launch / its
+           CUDA-event duration, against the measured HBM copy bandwidth.
+cpu_baseline  the CPU oracle (this repository's C++ restatement of the reference, the
+           reference itself cannot be built on the aarch64 GPU host) on a bounded
+           sample of the same workload.
+
+Multi-GPU: the path does not shard on one box; --gpus N runs N independent replicas
+(one per rank, no collective), value = sum over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+B_LU = {0: 2 * 19 * 8 + 1, 1: 2 * 19 * 4 + 1, 2: 2 * 19 * 2 + 1}  # bytes per lattice update
+DTYPE = {0: "f64", 1: "f32", 2: "f16-storage/f32-compute"}
+
+
+def rsa_spheres(seed, target, rmin, rmax, lo, hi, tries=400000, batch=4096):
+    """Seeded random sequential addition of non-overlapping spheres (vectorised in
+    batches; each candidate is accepted only if it overlaps no earlier sphere)."""
+    rng = np.random.default_rng(seed)
+    placed = np.zeros((0, 4))
+    done = 0
+    while done < tries and len(placed) < target:
+        r = rng.uniform(rmin, rmax, batch)
+        c = np.stack([rng.uniform(lo + r, hi - r) for _ in range(3)], axis=1)
+        done += batch
+        if len(placed):
+            d2 = ((c[:, None, :] - placed[None, :, :3]) ** 2).sum(-1)
+            ok = (d2 >= (r[:, None] + placed[None, :, 3]) ** 2).all(axis=1)
+        else:
+            ok = np.ones(batch, bool)
+        acc = []
+        for k in np.nonzero(ok)[0]:
+            good = True
+            for a in acc:
+                if ((c[k] - c[a]) ** 2).sum() < (r[k] + r[a]) ** 2:
+                    good = False
+                    break
+            if good:
+                acc.append(k)
+                if len(placed) + len(acc) >= target:
+                    break
+        if acc:
+            placed = np.vstack([placed, np.c_[c[acc], r[acc]]])
+    return placed
+
+
+def workload(precision):
+    from hybird_gb300 import abi
+    L = 128
+    spheres = rsa_spheres(2, 2000, 4.0, 6.0, 0.5, L - 1.5)
+    p = abi.make_params((L, L, L), (7,) * 6, init_visc=(0.8 - 0.5) / 3.0, lbF=(0.0, 0.0, -1e-5),
+                        collision=abi.HB_TRT, trt_magic=3.0 / 16.0, precision=precision,
+                        multi_step=3, density=2.5, linear_stiff=1e3, restitution=0.8,
+                        friction_part=0.5, friction_wall=0.5, visc_tang=0.5)
+    return p, spheres
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", f"--id={self.index}",
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([s.strip() for s in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx = float(s[1])
+                for k, nm in enumerate(names):
+                    if s[3 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_sample(params, spheres, steps, threads):
+    """CPU oracle on a bounded sample of the workload: `steps` whole cycles."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from oracle_port import OracleSim
+    o = OracleSim(params, spheres, threads=threads)
+    active = int(o.lib.hbo_active(o.h))
+    o.cycle(1)  # first cycle includes the neighbour rebuild; not timed
+    t0 = time.perf_counter()
+    o.cycle(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return active * steps / dt / 1e6, dt
+
+
+def run_reference(args, rank):
+    """The reference arm: the reference's CPU algorithm (the oracle port; the reference
+    sources do not travel to the GPU host) on this machine's host cores."""
+    from hybird_gb300 import abi
+    if rank != 0:
+        return
+    p, spheres = workload(abi.HB_FP64)
+    threads = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 4))
+    vals = []
+    for _ in range(max(1, args.warmup and 1)):
+        pass
+    v, dt = cpu_sample(p, spheres, steps, threads)
+    vals.append(v)
+    line = {"impl": "reference", "metric": "MLUPS (coupled LBM-DEM step)", "value": round(v, 3),
+            "unit": "MLUPS", "n_gpus": args.gpus, "steps": steps, "warmup": 1,
+            "ms_per_step": round(dt / steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "coupled sedimentation 128^3 D3Q19, %d spheres r~U[4,6], multiStep 3"
+                       % len(spheres), "lattice": [128, 128, 128], "spheres": len(spheres)},
+            "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+                             "sample": f"{steps} whole cycles after 1 untimed cycle"},
+            "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "fp16s"])
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist = dist_mod
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference(args, rank)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import ctypes as C
+    from hybird_gb300 import abi
+    from hybird_gb300.gpu import GpuSim, check, lib
+
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    prec = {"fp64": abi.HB_FP64, "fp32": abi.HB_FP32, "fp16s": abi.HB_FP16S}[args.precision]
+    p, spheres = workload(prec)
+    g = GpuSim(p, spheres)
+    st = g.status()
+    L = lib()
+    # active nodes and inside-particle nodes from the device state
+    gl = g.lattice()
+    act = (gl["type"] == 0) | (gl["type"] == 3)
+    A = int(act.sum())
+    A_in = int((act & (gl["inside"] == 1)).sum())
+    del gl
+    # warm-up
+    for _ in range(args.warmup):
+        check(L.hb_cycle(g.h, 1))
+    check(L.hb_synchronize(g.h))
+    if dist:
+        dist.barrier()
+    # device-resident timed region (inputs larger than L2: 2 x 19 x 2.1M x 4 B = 319 MB)
+    with Clocks(local) as clk:
+        ms_tot, ms_lb, kpc = g.time_cycles(args.steps)
+    check(L.hb_synchronize(g.h))
+    ms_step = ms_tot / args.steps
+    if dist:
+        import torch
+        t = torch.tensor([ms_step], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = A * world / (ms_step * 1e-3) / 1e6
+    # end-to-end through the C-ABI with host buffers
+    E = g.E
+    pin = {k: np.zeros(3 * E) for k in ("x0", "x1", "FHydro", "MHydro")}
+    force = np.array(p.lbF[:], dtype=np.float64)
+    e2e_steps = max(3, args.steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        check(L.hb_set_body_force(g.h, force.ctypes.data_as(C.c_void_p)))
+        check(L.hb_cycle(g.h, 1))
+        check(L.hb_download_elements(g.h, pin["x0"].ctypes.data_as(C.c_void_p),
+                                     pin["x1"].ctypes.data_as(C.c_void_p), None, None,
+                                     pin["FHydro"].ctypes.data_as(C.c_void_p),
+                                     pin["MHydro"].ctypes.data_as(C.c_void_p), None, None, None, None, None))
+    e2e_dt = time.perf_counter() - t0
+    e2e = A * world * e2e_steps / e2e_dt / 1e6
+    # roofline of the fused kernel
+    peak, peak_kind = measured_peak()
+    bytes_launch = A * B_LU[prec] + A_in * (4 + 3 * (8 if prec == abi.HB_FP64 else 4))
+    achieved = bytes_launch / (ms_lb * 1e-3) / 1e9 if ms_lb > 0 else None
+    st = g.status()
+    g.close()
+    line = {
+        "metric": "MLUPS (coupled LBM-DEM step)", "value": round(value, 2), "unit": "MLUPS",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": DTYPE[prec], "data": "synthetic",
+        "config": {"workload": "coupled sedimentation 128^3 D3Q19 TRT, %d spheres r~U[4,6], multiStep 3, "
+                               "populations %s, DEM f64" % (E, args.precision),
+                   "lattice": [128, 128, 128], "active_nodes": A, "inside_nodes": A_in, "spheres": E,
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (319 MB populations per step)",
+                   "kernels_per_cycle": kpc},
+        "gpu_launches": kpc * args.steps,
+        "e2e": {"value": round(e2e, 2), "unit": "MLUPS", "h2d_bytes_per_step": 24,
+                "d2h_bytes_per_step": 4 * 3 * E * 8},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
+                     "traffic": None, "kernel": "k_collide_stream", "kernel_ms": round(ms_lb, 5),
+                     "peak_kind": peak_kind, "bytes_per_launch": bytes_launch},
+        "clocks": clk.summary(),
+        "dem": {"contacts_last_substep": st.contacts, "candidate_pairs": st.pairs},
+    }
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        try:
+            p64, sph = workload(abi.HB_FP64)
+            v, dt = cpu_sample(p64, sph, args.cpu_steps, threads)
+            line["cpu_baseline"] = {"value": round(v, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+                                    "sample": f"{args.cpu_steps} whole cycles of the same workload in FP64 "
+                                              f"after one untimed cycle ({dt:.1f} s)"}
+        except Exception as exc:  # noqa: BLE001
+            line["cpu_baseline"] = {"value": None, "error": str(exc)[:200]}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,606 @@
+// hb_api.cu -- the C-ABI (include/hybird_gpu.h): context lifecycle, initial state,
+// whole-cycle CUDA graph, downloads, status and timing.
+//
+// One cycle is the reference's goCycle (hybird.cpp:35-66) minus output:
+//   DEM substeps -> free-surface step -> coupling masks -> collide+stream -> element
+//   hydrodynamic force reduction -> parity flip.
+// It is captured once into a CUDA graph and replayed; all device memory is allocated in
+// hb_create/hb_init, nothing per step.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hb_common.cuh"
+#include "hb_ctx.h"
+
+namespace {
+thread_local std::string g_err;
+
+int seterr(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                      \
+    do {                                                                              \
+        cudaError_t _e = (call);                                                      \
+        if (_e != cudaSuccess)                                                        \
+            return seterr(HB_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(_e), \
+                          __FILE__, __LINE__);                                        \
+    } while (0)
+
+template <class T>
+int dalloc(T** p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+    if (e != cudaSuccess) return seterr(HB_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", sizeof(T) * count, cudaGetErrorString(e));
+    return HB_OK;
+}
+
+int check_params(const hb_params* p) {
+    for (int k = 0; k < 3; ++k)
+        if (p->lb_size[k] < 3) return seterr(HB_ERR_ARG, "lb_size[%d] = %d < 3", k, p->lb_size[k]);
+    for (int k = 0; k < 3; ++k)
+        if (p->units[k] != 1.0) return seterr(HB_ERR_UNSUPPORTED, "units must be 1 (lattice units)");
+    for (int k = 0; k < 6; ++k) {
+        const int b = p->boundary[k];
+        if (b != HB_T_PERIODIC && b != HB_T_STATWALL && b != HB_T_DYNWALL)
+            return seterr(HB_ERR_UNSUPPORTED, "boundary%d = %d: only 4 (periodic), 7, 8 are implemented", k, b);
+    }
+    if (!(p->init_visc > 0.0)) return seterr(HB_ERR_ARG, "init_visc must be > 0");
+    if (p->precision < HB_FP64 || p->precision > HB_FP16S) return seterr(HB_ERR_ARG, "precision");
+    if (p->collision != HB_BGK && p->collision != HB_TRT) return seterr(HB_ERR_ARG, "collision");
+    if (p->dem_solve && p->multi_step < 1) return seterr(HB_ERR_ARG, "multi_step must be >= 1");
+    return HB_OK;
+}
+}  // namespace
+
+namespace hb {
+
+int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
+    hb_dem_dev& d = c->d;
+    const hb_params& P = c->P;
+    // walls from the boundary codes (DEM.cpp:435-633)
+    const double ps[6][3] = {{0.5, 0, 0}, {c->X - 1.5, 0, 0}, {0, 0.5, 0}, {0, c->Y - 1.5, 0}, {0, 0, 0.5}, {0, 0, c->Z - 1.5}};
+    const double ns[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+    d.nw = 0;
+    for (int k = 0; k < 6; ++k) {
+        const int b = P.boundary[k];
+        if (b == HB_T_STATWALL || b == HB_T_DYNWALL) {
+            for (int q = 0; q < 3; ++q) { d.wall_p[d.nw][q] = ps[k][q]; d.wall_n[d.nw][q] = ns[k][q]; }
+            d.wall_moving[d.nw] = b == HB_T_DYNWALL;
+            ++d.nw;
+        }
+    }
+    const double re = P.restitution;
+    d.dampCoeff = -1.0 * std::sqrt(2.0) * std::log(re) / std::sqrt((std::log(re) * std::log(re) + M_PI));
+    d.knConst = 2.0 / 3.0 * P.young_mod / (1 - P.poisson * P.poisson);
+    d.ksConst = 2.0 * P.young_mod / (2.0 - P.poisson) / (1.0 + P.poisson);
+    // objects
+    d.O = o ? o->count : 0;
+    if (d.O > 0) {
+        int rc;
+        if ((rc = dalloc(&d.obj_x0, 3 * d.O)) || (rc = dalloc(&d.obj_x1, 3 * d.O)) || (rc = dalloc(&d.obj_r, d.O))) return rc;
+        CK(cudaMemcpy(d.obj_x0, o->x0, sizeof(double) * 3 * d.O, cudaMemcpyHostToDevice));
+        std::vector<double> z(3 * d.O, 0.0);
+        CK(cudaMemcpy(d.obj_x1, o->x1 ? o->x1 : z.data(), sizeof(double) * 3 * d.O, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.obj_r, o->radius, sizeof(double) * d.O, cudaMemcpyHostToDevice));
+    }
+    const int E = (P.dem_solve && e) ? e->count : 0;
+    d.E = E;
+    d.multi = E ? P.multi_step : 1;
+    d.dt = E ? 1.0 / double(P.multi_step) : 1.0;
+    if (E == 0) return HB_OK;
+    for (int k = 0; k < 6; ++k)
+        if (P.boundary[k] == HB_T_PERIODIC)
+            return seterr(HB_ERR_UNSUPPORTED, "moving particles with periodic boundaries (ghost particles) are not implemented");
+    // element fields, one allocation (elmt.h:53-135)
+    const int nfields = 6 * 3 * 4 + 6 * 4 * 2 + 4 * 3 + 6 * 3 + 1 + 1 + 3 + 1;
+    int rc;
+    if ((rc = dalloc(&d.base, (size_t)nfields * E))) return rc;
+    CK(cudaMemset(d.base, 0, sizeof(double) * nfields * E));
+    double* p = d.base;
+    auto take = [&](int comps) { double* r = p; p += (size_t)comps * E; return r; };
+    for (int k = 0; k < 6; ++k) d.x[k] = take(3);
+    for (int k = 0; k < 6; ++k) d.xp[k] = take(3);
+    for (int k = 0; k < 6; ++k) d.w[k] = take(3);
+    for (int k = 0; k < 6; ++k) d.wp[k] = take(3);
+    for (int k = 0; k < 6; ++k) d.q[k] = take(4);
+    for (int k = 0; k < 6; ++k) d.qp[k] = take(4);
+    d.wG = take(3); d.wL = take(3); d.wpG = take(3); d.wpL = take(3);
+    d.FH = take(3); d.MH = take(3); d.FP = take(3); d.FW = take(3); d.MP = take(3); d.MW = take(3);
+    d.fvol = take(1); d.m = take(1); d.I = take(3); d.rad = take(1);
+    // host-side element init (elmt.cpp:13-61)
+    std::vector<double> m(E), I(3 * E), q0(4 * E), w0(3 * E, 0.0), x1(3 * E, 0.0);
+    double maxRad = 0.0;
+    for (int k = 0; k < E; ++k) {
+        const double r = e->radius[k];
+        maxRad = std::max(maxRad, r);
+        const double sm = 4.0 / 3.0 * P.density * M_PI * r * r * r;
+        m[k] = 1 * sm;
+        const double iv = 1 * 2.0 / 5.0 * sm * r * r;
+        for (int q = 0; q < 3; ++q) I[q * E + k] = iv * 1.0 + sm * r * r * 0.0;
+        if (e->q0) for (int q = 0; q < 4; ++q) q0[q * E + k] = e->q0[q * E + k];
+        else { q0[k] = 1.0; q0[E + k] = q0[2 * E + k] = q0[3 * E + k] = 0.0; }
+        if (e->w0) for (int q = 0; q < 3; ++q) w0[q * E + k] = e->w0[q * E + k];
+        if (e->x1) for (int q = 0; q < 3; ++q) x1[q * E + k] = e->x1[q * E + k];
+    }
+    CK(cudaMemcpy(d.x[0], e->x0, sizeof(double) * 3 * E, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.xp[0], e->x0, sizeof(double) * 3 * E, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.x[1], x1.data(), sizeof(double) * 3 * E, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.xp[1], x1.data(), sizeof(double) * 3 * E, cudaMemcpyHostToDevice));
+    for (double* dst : {d.w[0], d.wG, d.wL, d.wpG, d.wpL})
+        CK(cudaMemcpy(dst, w0.data(), sizeof(double) * 3 * E, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.q[0], q0.data(), sizeof(double) * 4 * E, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.qp[0], q0.data(), sizeof(double) * 4 * E, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.m, m.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.I, I.data(), sizeof(double) * 3 * E, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.rad, e->radius, sizeof(double) * E, cudaMemcpyHostToDevice));
+    // neighbour-list parameters (DEM.cpp:1270-1312)
+    const double demSize[3] = {(double)c->X, (double)c->Y, (double)c->Z};
+    for (int k = 0; k < 3; ++k) {
+        d.cellWidth[k] = std::min(maxRad * 5.0, demSize[k]);
+        d.nCells[k] = (int)std::ceil(demSize[k] / d.cellWidth[k]);
+        d.cellWidth[k] = demSize[k] / double(d.nCells[k]);
+        d.nCells[k] += 2;
+    }
+    d.nebrRange = std::max(maxRad * 3.0, 0.5 * std::min(d.cellWidth[0], std::min(d.cellWidth[1], d.cellWidth[2])));
+    d.trigger = 0.25 * d.nebrRange;
+    d.ncells = d.nCells[0] * d.nCells[1] * d.nCells[2];
+    if ((rc = dalloc(&d.cell_of, E)) || (rc = dalloc(&d.cell_cnt, d.ncells)) || (rc = dalloc(&d.cell_start, d.ncells + 1)) ||
+        (rc = dalloc(&d.cell_fill, d.ncells)) || (rc = dalloc(&d.cell_items, E)) ||
+        (rc = dalloc(&d.nbr, (size_t)E * NBR_CAP)) || (rc = dalloc(&d.nbr_cnt, E)) || (rc = dalloc(&d.wall_of, E)) ||
+        (rc = dalloc(&d.obj, (size_t)E * OBJ_CAP)) || (rc = dalloc(&d.obj_cnt, E)) || (rc = dalloc(&d.scal, 8)) ||
+        (rc = dalloc(&d.contacts, 1)) || (rc = dalloc(&d.partial, ceil_div(E, 256) + 1)) || (rc = dalloc(&d.done, 1)))
+        return rc;
+    const double scal0[8] = {0.5 * d.nebrRange, 1.0, 0, 0, 0, 0, 0, 0};  // maxDisp, rebuild
+    CK(cudaMemcpy(d.scal, scal0, sizeof(scal0), cudaMemcpyHostToDevice));
+    CK(cudaMemset(d.contacts, 0, sizeof(int)));
+    CK(cudaMemset(d.done, 0, sizeof(unsigned int)));
+    CK(cudaMemset(d.nbr_cnt, 0, sizeof(int) * E));
+    CK(cudaMemset(d.obj_cnt, 0, sizeof(int) * E));
+    return HB_OK;
+}
+
+}  // namespace hb
+
+using namespace hb;
+
+static int build_graph(hb_ctx* c);
+
+extern "C" {
+
+const char* hb_last_error(void) { return g_err.c_str(); }
+
+int hb_create(const hb_params* params, hb_ctx** out) {
+    if (!params || !out) return seterr(HB_ERR_ARG, "null argument");
+    int rc = check_params(params);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return seterr(HB_ERR_CUDA, "no CUDA device");
+    hb_ctx* c = new hb_ctx();
+    c->P = *params;
+    c->X = params->lb_size[0];
+    c->Y = params->lb_size[1];
+    c->Z = params->lb_size[2];
+    c->N = (long long)c->X * c->Y * c->Z;
+    CK(cudaGetDevice(&c->dev));
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    const long long N = c->N;
+    c->sz = params->precision == HB_FP64 ? 8 : (params->precision == HB_FP32 ? 4 : 2);
+    const size_t tsz = params->precision == HB_FP64 ? 8 : 4;
+    if ((rc = dalloc(&c->ntype, N)) || (rc = dalloc(&c->solid, N)) || (rc = dalloc((uint8_t**)&c->fA, 19 * N * c->sz)) ||
+        (rc = dalloc((uint8_t**)&c->fB, 19 * N * c->sz)) || (rc = dalloc(&c->parity, 1)) || (rc = dalloc(&c->mode, 1)) ||
+        (rc = dalloc(&c->rho, N)) || (rc = dalloc(&c->u, 3 * N)) || (rc = dalloc(&c->hf, 3 * N)) ||
+        (rc = dalloc(&c->mass, N)) || (rc = dalloc(&c->status, STATUS_WORDS)) ||
+        (rc = dalloc(&c->wall_force, MAX_WALLS * 3 + 1))) {
+        hb_destroy(c);
+        return rc;
+    }
+    if (params->non_newtonian || params->turbulence)
+        if ((rc = dalloc((uint8_t**)&c->visc, N * tsz))) { hb_destroy(c); return rc; }
+    CK(cudaMemset(c->parity, 0, sizeof(int)));
+    CK(cudaMemset(c->mode, 0, sizeof(int)));
+    CK(cudaMemset(c->status, 0, sizeof(int) * STATUS_WORDS));
+    CK(cudaMemset(c->wall_force, 0, sizeof(double) * (MAX_WALLS * 3 + 1)));
+    CK(cudaEventCreate(&c->ev0));
+    CK(cudaEventCreate(&c->ev1));
+    *out = c;
+    return HB_OK;
+}
+
+int hb_destroy(hb_ctx* c) {
+    if (!c) return HB_OK;
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    void* ptrs[] = {c->ntype, c->solid, c->fA, c->fB, c->parity, c->mode, c->rho, c->u, c->hf, c->mass,
+                    c->visc, c->dv, c->claim, c->status, c->wall_part, c->wall_force, c->fs_force, c->if_list,
+                    c->if_count, c->fs_scal, c->fs_flag, c->fs_parent, c->fs_part, c->lb_force,
+                    c->d.base, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
+                    c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
+                    c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return HB_OK;
+}
+
+int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
+    if (!c) return seterr(HB_ERR_ARG, "null ctx");
+    int rc = dem_init(c, e, o);
+    if (rc) return rc;
+    const long long N = c->N;
+    const size_t tsz = c->P.precision == HB_FP64 ? 8 : 4;
+    if (c->d.E > 0) {
+        if (!c->dv && (rc = dalloc((uint8_t**)&c->dv, 3 * N * tsz))) return rc;
+        if (!c->claim && (rc = dalloc(&c->claim, N))) return rc;
+        CK(cudaMemset(c->claim, 0xFF, sizeof(unsigned long long) * N));
+    }
+    if (!c->wall_part) {
+        const long long grid = (long long)ceil_div(c->X, c->X <= 64 ? 64 : (c->X <= 128 ? 128 : 256)) * (c->Y - 2) * (c->Z - 2);
+        if ((rc = dalloc(&c->wall_part, (size_t)grid * (MAX_WALLS * 3 + 1)))) return rc;
+    }
+    if (!c->fs_force) {
+        if ((rc = dalloc(&c->fs_force, 3))) return rc;
+    }
+    if (!c->lb_force) {
+        if ((rc = dalloc(&c->lb_force, 3))) return rc;
+    }
+    CK(cudaMemcpy(c->fs_force, c->P.lbF, sizeof(double) * 3, cudaMemcpyHostToDevice));
+    {
+        const double z[3] = {0.0, 0.0, 0.0};
+        CK(cudaMemcpy(c->lb_force, c->P.force_field ? c->P.lbF : z, sizeof(double) * 3, cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemset(c->parity, 0, sizeof(int)));
+    c->h_parity = 0;
+    c->steps = 0;
+    if (launch_init_lattice(c, e && c->d.E ? c->d.x[0] : nullptr, c->d.E ? c->d.rad : nullptr, c->d.E,
+                            c->d.obj_x0, c->d.obj_r, c->d.O))
+        return seterr(HB_ERR_CUDA, "lattice init: %s", cudaGetErrorString(cudaGetLastError()));
+    // count dynamic-wall nodes
+    {
+        std::vector<uint8_t> t(N);
+        CK(cudaMemcpy(t.data(), c->ntype, N, cudaMemcpyDeviceToHost));
+        c->has_dynwall = false;
+        for (long long i = 0; i < N; ++i)
+            if ((t[i] & HB_TYPE_MASK) == HB_T_DYNWALL) { c->has_dynwall = true; break; }
+    }
+    if (c->P.free_surface) {
+        if ((rc = fs_init(c))) return rc;
+    }
+    // the reference builds the neighbour table at init (DEM.cpp:253-257) and, because
+    // maxDisp starts at 0.5 nebrRange, again at the first substep; only the second is
+    // ever used, so the first trigger evaluation sets the rebuild flag here
+    if (c->d.E > 0) launch_dem_first_predict(c);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    c->initialized = true;
+    if ((rc = build_graph(c))) return rc;
+    return HB_OK;
+}
+
+int hb_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside, const uint32_t* solid,
+                      const double* f, const double* n, const double* u, const double* mass, const double* visc) {
+    if (!c || !type || !inside || !solid || !n || !u || !mass) return seterr(HB_ERR_ARG, "null argument");
+    if (!c->initialized) return seterr(HB_ERR_STATE, "hb_init must run first");
+    if (launch_upload_lattice(c, type, inside, solid, f, n, u, mass, visc))
+        return seterr(HB_ERR_CUDA, "upload: %s", cudaGetErrorString(cudaGetLastError()));
+    return HB_OK;
+}
+
+}  // extern "C"
+
+// one whole cycle on the context stream
+static void enqueue_cycle(hb_ctx* c) {
+    const bool dem = c->P.dem_solve && c->d.E > 0;
+    if (dem)
+        for (int s = 0; s < c->d.multi; ++s) launch_dem_substep(c);
+    if (!c->P.lb_solve) return;
+    if (c->P.free_surface) launch_fs_step(c);
+    if (dem) launch_couple_masks(c);
+    launch_lb_step(c);
+    if (c->has_dynwall) launch_lb_wallforce(c);
+    if (dem) launch_couple_reduce(c);
+    launch_flip(c);
+    if (!c->P.force_field) cudaMemsetAsync(c->fs_force, 0, sizeof(double) * 3, c->stream);
+}
+
+static int build_graph(hb_ctx* c) {
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+    if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_cycle(c);
+    CK(cudaStreamEndCapture(c->stream, &c->graph));
+    CK(cudaGraphInstantiate(&c->gexec, c->graph, 0));
+    size_t nn = 0;
+    CK(cudaGraphGetNodes(c->graph, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    CK(cudaGraphGetNodes(c->graph, nodes.data(), &nn));
+    int k = 0;
+    for (auto& nd : nodes) {
+        cudaGraphNodeType t;
+        cudaGraphNodeGetType(nd, &t);
+        if (t == cudaGraphNodeTypeKernel) ++k;
+    }
+    c->kernels_per_cycle = k;
+    return HB_OK;
+}
+
+static int run_cycles(hb_ctx* c, int n, bool last_mirror) {
+    for (int s = 0; s < n; ++s) {
+        const int m = (last_mirror && s == n - 1) ? 1 : 0;
+        CK(cudaMemsetAsync(c->mode, m, sizeof(int), c->stream));
+        CK(cudaGraphLaunch(c->gexec, c->stream));
+        if (c->P.lb_solve) c->h_parity ^= 1;
+        ++c->steps;
+    }
+    return HB_OK;
+}
+
+extern "C" {
+
+int hb_dem_step(hb_ctx* c) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    if (c->P.dem_solve && c->d.E > 0)
+        for (int s = 0; s < c->d.multi; ++s) launch_dem_substep(c);
+    CK(cudaGetLastError());
+    return HB_OK;
+}
+
+int hb_fs_step(hb_ctx* c) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    if (c->P.free_surface) launch_fs_step(c);
+    CK(cudaGetLastError());
+    return HB_OK;
+}
+
+int hb_coupling_step(hb_ctx* c) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    if (c->P.dem_solve && c->d.E > 0) launch_couple_masks(c);
+    CK(cudaGetLastError());
+    return HB_OK;
+}
+
+int hb_lb_step(hb_ctx* c) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    CK(cudaMemsetAsync(c->mode, 1, sizeof(int), c->stream));
+    launch_lb_step(c);
+    if (c->has_dynwall) launch_lb_wallforce(c);
+    if (c->P.dem_solve && c->d.E > 0) launch_couple_reduce(c);
+    launch_flip(c);
+    if (!c->P.force_field) CK(cudaMemsetAsync(c->fs_force, 0, sizeof(double) * 3, c->stream));
+    c->h_parity ^= 1;
+    ++c->steps;
+    CK(cudaGetLastError());
+    return HB_OK;
+}
+
+int hb_cycle(hb_ctx* c, int32_t nsteps) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    if (nsteps < 0) return seterr(HB_ERR_ARG, "nsteps < 0");
+    int rc = run_cycles(c, nsteps, true);
+    if (rc) return rc;
+    CK(cudaGetLastError());
+    return HB_OK;
+}
+
+int hb_set_body_force(hb_ctx* c, const double* force) {
+    if (!c || !force || !c->initialized) return seterr(HB_ERR_ARG, "null argument or not initialised");
+    for (int k = 0; k < 3; ++k) c->P.lbF[k] = force[k];
+    if (c->P.force_field) CK(cudaMemcpyAsync(c->lb_force, force, sizeof(double) * 3, cudaMemcpyHostToDevice, c->stream));
+    return HB_OK;
+}
+
+int hb_synchronize(hb_ctx* c) {
+    if (!c) return seterr(HB_ERR_ARG, "null ctx");
+    CK(cudaStreamSynchronize(c->stream));
+    int st[STATUS_WORDS];
+    CK(cudaMemcpy(st, c->status, sizeof(st), cudaMemcpyDeviceToHost));
+    if (st[1]) return seterr(HB_ERR_UNSUPPORTED, "TYPE ERROR: an active node links to an unsupported node type");
+    if (st[2]) return seterr(HB_ERR_CAPACITY, "device list capacity exceeded (code %d)", st[2]);
+    return HB_OK;
+}
+
+int hb_download_lattice(hb_ctx* c, uint8_t* type, uint8_t* inside, uint32_t* solid, double* f, double* n,
+                        double* u, double* mass, double* visc, double* hydro_force) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    CK(cudaStreamSynchronize(c->stream));
+    const long long N = c->N;
+    if (type || inside) {
+        std::vector<uint8_t> t(N);
+        CK(cudaMemcpy(t.data(), c->ntype, N, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < N; ++i) {
+            if (type) type[i] = t[i] & HB_TYPE_MASK;
+            if (inside) inside[i] = (t[i] & HB_INSIDE) ? 1 : 0;
+        }
+    }
+    if (solid) CK(cudaMemcpy(solid, c->solid, sizeof(uint32_t) * N, cudaMemcpyDeviceToHost));
+    if (f) {
+        double* df = nullptr;
+        int rc = dalloc(&df, 19 * N);
+        if (rc) return rc;
+        launch_download_lattice(c, df, c->h_parity);
+        CK(cudaStreamSynchronize(c->stream));
+        CK(cudaMemcpy(f, df, sizeof(double) * 19 * N, cudaMemcpyDeviceToHost));
+        cudaFree(df);
+    }
+    if (n) CK(cudaMemcpy(n, c->rho, sizeof(double) * N, cudaMemcpyDeviceToHost));
+    if (u) CK(cudaMemcpy(u, c->u, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost));
+    if (mass) CK(cudaMemcpy(mass, c->mass, sizeof(double) * N, cudaMemcpyDeviceToHost));
+    if (hydro_force) CK(cudaMemcpy(hydro_force, c->hf, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost));
+    if (visc) {
+        if (!c->visc) {
+            for (long long i = 0; i < N; ++i) visc[i] = c->P.init_visc;
+        } else if (c->P.precision == HB_FP64) {
+            CK(cudaMemcpy(visc, c->visc, sizeof(double) * N, cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> v(N);
+            CK(cudaMemcpy(v.data(), c->visc, sizeof(float) * N, cudaMemcpyDeviceToHost));
+            for (long long i = 0; i < N; ++i) visc[i] = v[i];
+        }
+    }
+    return HB_OK;
+}
+
+int hb_download_elements(hb_ctx* c, double* x0, double* x1, double* w, double* q0, double* fhydro, double* mhydro,
+                         double* fparticle, double* fwall, double* mparticle, double* mwall, double* fluid_volume) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    CK(cudaStreamSynchronize(c->stream));
+    const int E = c->d.E;
+    if (E == 0) return HB_OK;
+    struct { double* dst; double* src; int comps; } items[] = {
+        {x0, c->d.x[0], 3}, {x1, c->d.x[1], 3}, {w, c->d.wG, 3}, {q0, c->d.q[0], 4}, {fhydro, c->d.FH, 3},
+        {mhydro, c->d.MH, 3}, {fparticle, c->d.FP, 3}, {fwall, c->d.FW, 3}, {mparticle, c->d.MP, 3},
+        {mwall, c->d.MW, 3}, {fluid_volume, c->d.fvol, 1}};
+    for (auto& it : items)
+        if (it.dst) CK(cudaMemcpy(it.dst, it.src, sizeof(double) * it.comps * E, cudaMemcpyDeviceToHost));
+    return HB_OK;
+}
+
+int hb_download_pairs(hb_ctx* c, uint32_t* pairs, int64_t capacity, int64_t* count) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    CK(cudaStreamSynchronize(c->stream));
+    const int E = c->d.E;
+    std::vector<uint32_t> out;
+    if (E > 0) {
+        std::vector<int> nb((size_t)E * NBR_CAP), cnt(E);
+        CK(cudaMemcpy(nb.data(), c->d.nbr, sizeof(int) * nb.size(), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(cnt.data(), c->d.nbr_cnt, sizeof(int) * E, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < E; ++i) {
+            std::vector<int> js(nb.begin() + (size_t)i * NBR_CAP, nb.begin() + (size_t)i * NBR_CAP + cnt[i]);
+            std::sort(js.begin(), js.end());
+            for (int j : js)
+                if (j > i) { out.push_back((uint32_t)i); out.push_back((uint32_t)j); }
+        }
+    }
+    const int64_t np = (int64_t)out.size() / 2;
+    if (count) *count = np;
+    if (pairs) memcpy(pairs, out.data(), sizeof(uint32_t) * 2 * std::min(np, capacity));
+    return HB_OK;
+}
+
+int hb_download_interface(hb_ctx* c, uint32_t* cells, int64_t capacity, int64_t* count) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    CK(cudaStreamSynchronize(c->stream));
+    const long long N = c->N;
+    std::vector<uint8_t> t(N);
+    CK(cudaMemcpy(t.data(), c->ntype, N, cudaMemcpyDeviceToHost));
+    int64_t k = 0;
+    for (long long i = 0; i < N; ++i)
+        if ((t[i] & HB_TYPE_MASK) == HB_T_INTERFACE) {
+            if (cells && k < capacity) cells[k] = (uint32_t)i;
+            ++k;
+        }
+    if (count) *count = k;
+    return HB_OK;
+}
+
+int hb_download_walls(hb_ctx* c, double* fhydro, double* fparticle, int32_t* nwalls) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    CK(cudaStreamSynchronize(c->stream));
+    if (nwalls) *nwalls = c->d.nw;
+    double wf[MAX_WALLS * 3 + 1];
+    CK(cudaMemcpy(wf, c->wall_force, sizeof(wf), cudaMemcpyDeviceToHost));
+    for (int w = 0; w < c->d.nw; ++w)
+        for (int k = 0; k < 3; ++k) {
+            if (fhydro) fhydro[3 * w + k] = wf[3 * w + k];
+            if (fparticle) fparticle[3 * w + k] = 0.0;
+        }
+    return HB_OK;
+}
+
+int hb_get_status(hb_ctx* c, hb_status* s) {
+    if (!c || !s) return seterr(HB_ERR_ARG, "null argument");
+    CK(cudaStreamSynchronize(c->stream));
+    int st[STATUS_WORDS];
+    CK(cudaMemcpy(st, c->status, sizeof(st), cudaMemcpyDeviceToHost));
+    memset(s, 0, sizeof(*s));
+    s->numeric_error = st[0];
+    s->capacity_error = st[2];
+    s->wait_timeout = st[3];
+    if (c->d.E > 0) {
+        int k = 0;
+        CK(cudaMemcpy(&k, c->d.contacts, sizeof(int), cudaMemcpyDeviceToHost));
+        s->contacts = k;
+        std::vector<int> cnt(c->d.E);
+        CK(cudaMemcpy(cnt.data(), c->d.nbr_cnt, sizeof(int) * c->d.E, cudaMemcpyDeviceToHost));
+        int64_t tot = 0;
+        for (int v : cnt) tot += v;
+        s->pairs = tot / 2;
+    }
+    if (c->if_count) {
+        int k = 0;
+        CK(cudaMemcpy(&k, c->if_count, sizeof(int), cudaMemcpyDeviceToHost));
+        s->interface_cells = k;
+        double sc[2];
+        CK(cudaMemcpy(sc, c->fs_scal, sizeof(sc), cudaMemcpyDeviceToHost));
+        s->mass_surplus = sc[0];
+    }
+    return HB_OK;
+}
+
+int hb_time_cycles(hb_ctx* c, int32_t nsteps, float* ms_total, float* ms_lb_kernel, int32_t* kernels_per_cycle) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    if (nsteps <= 0) return seterr(HB_ERR_ARG, "nsteps <= 0");
+    CK(cudaStreamSynchronize(c->stream));
+    // whole cycles replayed from the graph
+    CK(cudaMemsetAsync(c->mode, 0, sizeof(int), c->stream));
+    CK(cudaEventRecord(c->ev0, c->stream));
+    for (int s = 0; s < nsteps; ++s) {
+        CK(cudaGraphLaunch(c->gexec, c->stream));
+        if (c->P.lb_solve) c->h_parity ^= 1;
+        ++c->steps;
+    }
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaEventSynchronize(c->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    if (ms_total) *ms_total = ms;
+    if (kernels_per_cycle) *kernels_per_cycle = c->kernels_per_cycle;
+    // the stream-collide kernel alone, bracketed by events on its own stream, inside the
+    // same cycles launched one kernel at a time
+    if (ms_lb_kernel && c->P.lb_solve) {
+        std::vector<cudaEvent_t> ev(2 * nsteps);
+        for (auto& e : ev) CK(cudaEventCreate(&e));
+        const bool dem = c->P.dem_solve && c->d.E > 0;
+        for (int s = 0; s < nsteps; ++s) {
+            if (dem)
+                for (int k = 0; k < c->d.multi; ++k) launch_dem_substep(c);
+            if (c->P.free_surface) launch_fs_step(c);
+            if (dem) launch_couple_masks(c);
+            CK(cudaEventRecord(ev[2 * s], c->stream));
+            launch_lb_step(c);
+            CK(cudaEventRecord(ev[2 * s + 1], c->stream));
+            if (c->has_dynwall) launch_lb_wallforce(c);
+            if (dem) launch_couple_reduce(c);
+            launch_flip(c);
+            c->h_parity ^= 1;
+            ++c->steps;
+        }
+        CK(cudaStreamSynchronize(c->stream));
+        double tot = 0.0;
+        for (int s = 0; s < nsteps; ++s) {
+            float m = 0.f;
+            CK(cudaEventElapsedTime(&m, ev[2 * s], ev[2 * s + 1]));
+            tot += m;
+        }
+        *ms_lb_kernel = (float)(tot / nsteps);
+        for (auto& e : ev) cudaEventDestroy(e);
+    }
+    CK(cudaGetLastError());
+    return HB_OK;
+}
+
+}  // extern "C"

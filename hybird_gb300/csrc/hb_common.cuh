@@ -1,0 +1,131 @@
+// hb_common.cuh -- shared device definitions of the sm_103a time-step library.
+//
+// Data layout in HBM (one context, one GPU):
+//   node byte  ntype[N]      : type code (node.h:75-86) | HB_INSIDE (particle flag) |
+//                              HB_BULK (all 18 links lead to active nodes)
+//   solid[N]   uint32        : particle index for inside nodes, wall/object index for walls
+//   fA/fB      S[19*N]       : populations, structure-of-arrays f[j*N+i], ping-pong
+//   rho[N], u[3N], hf[3N], mass[N] : FP64 node macros, written where a later phase
+//                              (free surface, coupling, downloads) reads them
+//   visc[N]    T             : persistent viscosity, only with Bingham/Smagorinsky
+//   dv[3N]     T             : direct-forcing term per inside-particle node
+// Index i = x + X*(y + Y*z), exactly the reference's (LB.cpp:2314-2370).
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "../../include/hybird_gpu.h"
+
+#define HB_TYPE_MASK 0x0F
+#define HB_INSIDE 0x10
+#define HB_BULK 0x20
+
+namespace hb {
+
+constexpr int Q = 19;
+constexpr int MAX_WALLS = 6;
+constexpr int NBR_CAP = 48;      // candidate neighbours kept per particle
+constexpr int OBJ_CAP = 16;      // objects in range kept per particle
+constexpr int STATUS_WORDS = 8;  // device status words (numeric, capacity, wait, ...)
+
+// D3Q19 velocity set in the reference's order O,x,y,z,xy,yz,zx (lattice.h:36-60)
+__host__ __device__ constexpr int cx(int j) {
+    return j == 1 || j == 7 || j == 10 || j == 15 || j == 17 ? 1
+         : (j == 2 || j == 8 || j == 9 || j == 16 || j == 18 ? -1 : 0);
+}
+__host__ __device__ constexpr int cy(int j) {
+    return j == 3 || j == 7 || j == 9 || j == 11 || j == 14 ? 1
+         : (j == 4 || j == 8 || j == 10 || j == 12 || j == 13 ? -1 : 0);
+}
+__host__ __device__ constexpr int cz(int j) {
+    return j == 5 || j == 11 || j == 13 || j == 15 || j == 18 ? 1
+         : (j == 6 || j == 12 || j == 14 || j == 16 || j == 17 ? -1 : 0);
+}
+__host__ __device__ constexpr int opp(int j) { return j == 0 ? 0 : ((j & 1) ? j + 1 : j - 1); }
+__host__ __device__ constexpr double wgt(int j) {
+    return j == 0 ? 12.0 / 36.0 : (j <= 6 ? 2.0 / 36.0 : 1.0 / 36.0);
+}
+
+__device__ __forceinline__ bool is_active(uint8_t t) {
+    const uint8_t c = t & HB_TYPE_MASK;
+    return c == HB_T_FLUID || c == HB_T_INTERFACE;
+}
+
+// ---- storage precision policies ------------------------------------------------------
+// FP64: full populations in double, compute in double (the reference's arithmetic).
+// FP32: deviations g = f - w*rho0 in float, compute in float.
+// FP16S: deviations scaled by 2^SHIFT in half, compute in float.
+struct PolF64 {
+    using S = double;
+    using T = double;
+    static constexpr bool DEV = false;
+    __device__ static __forceinline__ T load(const S* p) { return __ldcs(p); }
+    __device__ static __forceinline__ void store(S* p, T v) { __stcs(p, v); }
+    __device__ static __forceinline__ S enc(T v) { return v; }
+};
+struct PolF32 {
+    using S = float;
+    using T = float;
+    static constexpr bool DEV = true;
+    __device__ static __forceinline__ T load(const S* p) { return __ldcs(p); }
+    __device__ static __forceinline__ void store(S* p, T v) { __stcs(p, v); }
+    __device__ static __forceinline__ S enc(T v) { return v; }
+};
+struct PolF16 {
+    using S = __half;
+    using T = float;
+    static constexpr bool DEV = true;
+    static constexpr float SCALE = 32768.0f;
+    static constexpr float INV = 1.0f / 32768.0f;
+    __device__ static __forceinline__ T load(const S* p) {
+        const unsigned short b = __ldcs(reinterpret_cast<const unsigned short*>(p));
+        return __half2float(__ushort_as_half(b)) * INV;
+    }
+    __device__ static __forceinline__ void store(S* p, T v) {
+        __stcs(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(v * SCALE)));
+    }
+};
+
+// ---- device-side views of the context ----------------------------------------------
+struct Particles {          // DEM elements as the coupling sees them (FP64)
+    int count;
+    const double* x0;       // [3*E] particle centre (corrected)
+    const double* x1;       // [3*E] velocity
+    const double* w;        // [3*E] wGlobal
+    const double* radius;   // [E]
+};
+
+struct LBArgs {
+    int X, Y, Z;
+    long long N;
+    int per[6];             // face periodic flags (boundary code 4), x-,x+,y-,y+,z-,z+
+    uint8_t* ntype;
+    uint32_t* solid;
+    void* fA;
+    void* fB;
+    const int* parity;      // device step parity: 0 reads fA writes fB, 1 the reverse
+    const int* mode;        // bit0: write all node macros (downloads)
+    double* rho;
+    double* u;              // [3N]
+    double* hf;             // [3N]
+    double* mass;
+    void* visc;             // T[N] when viscosity is persistent
+    void* dv;               // T[3N] direct-forcing term of inside nodes
+    const double* F;        // device body force [3] (zero when forceFieldSolve = 0)
+    double init_visc;
+    int collision;
+    double trt_magic;
+    int visc_model;         // bit0 Bingham, bit1 Smagorinsky
+    double plastic_visc, yield_stress, turb_const;
+    int free_surface;
+    int couple;
+    Particles parts;
+    int* status;            // [STATUS_WORDS]
+    double* wall_part;      // [grid * (MAX_WALLS*3 + 1)] per-CTA moving-wall partials
+    int nwalls;
+};
+
+inline int ceil_div(long long a, int b) { return (int)((a + b - 1) / b); }
+
+}  // namespace hb

@@ -1,0 +1,119 @@
+// hb_ctx.h -- host-side context of one simulation (device pointers, sizes, graph).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "hb_common.cuh"
+
+struct hb_dem_dev {             // element state, FP64, component-major [3E] / [4E]
+    int E = 0;
+    double* base = nullptr;     // one allocation holding every field below
+    double *x[6], *xp[6], *w[6], *wp[6];
+    double *q[6], *qp[6];
+    double *wG, *wL, *wpG, *wpL;
+    double *FH, *MH, *FP, *FW, *MP, *MW;
+    double *fvol, *m, *I, *rad;
+    // neighbour structures
+    int* cell_of = nullptr;     // [E]
+    int* cell_cnt = nullptr;    // [nc]
+    int* cell_start = nullptr;  // [nc+1]
+    int* cell_fill = nullptr;   // [nc]
+    int* cell_items = nullptr;  // [E]
+    int* nbr = nullptr;         // [E*NBR_CAP]
+    int* nbr_cnt = nullptr;     // [E]
+    int* wall_of = nullptr;     // [E] first wall in range or -1
+    int* obj = nullptr;         // [E*OBJ_CAP]
+    int* obj_cnt = nullptr;     // [E]
+    double* scal = nullptr;     // device scalars: [0]=maxDisp [1]=rebuild flag [2]=contacts
+    int* contacts = nullptr;    // overlapping pairs counter of the last substep
+    double* partial = nullptr;  // per-block maxima for the displacement trigger
+    unsigned int* done = nullptr;  // last-block counter
+    int ncells = 0;
+    int nCells[3] = {0, 0, 0};
+    double cellWidth[3] = {0, 0, 0};
+    double nebrRange = 0.0, trigger = 0.0;
+    double dt = 1.0;
+    int multi = 1;
+    double dampCoeff = 0, knConst = 0, ksConst = 0;
+    // objects
+    int O = 0;
+    double* obj_x0 = nullptr;   // [3*O]
+    double* obj_x1 = nullptr;   // [3*O]
+    double* obj_r = nullptr;    // [O]
+    // walls (boundary planes, DEM.cpp:435-633)
+    int nw = 0;
+    double wall_p[hb::MAX_WALLS][3], wall_n[hb::MAX_WALLS][3];
+    int wall_moving[hb::MAX_WALLS];
+};
+
+struct hb_ctx {
+    hb_params P;
+    int X = 0, Y = 0, Z = 0;
+    long long N = 0;
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    size_t sz = 8;              // bytes per stored population
+    // lattice
+    uint8_t* ntype = nullptr;
+    uint32_t* solid = nullptr;
+    void* fA = nullptr;
+    void* fB = nullptr;
+    int* parity = nullptr;      // device
+    int* mode = nullptr;        // device
+    int h_parity = 0;
+    double* rho = nullptr;
+    double* u = nullptr;
+    double* hf = nullptr;
+    double* mass = nullptr;
+    void* visc = nullptr;
+    void* dv = nullptr;
+    unsigned long long* claim = nullptr;
+    int* status = nullptr;      // [STATUS_WORDS]
+    double* wall_part = nullptr;
+    double* wall_force = nullptr;   // [MAX_WALLS*3 + 1]
+    int lb_grid = 0, lb_block = 256;
+    bool has_dynwall = false;
+    bool initialized = false;
+    long long steps = 0;
+    double* fs_force = nullptr; // device lbF seen by the free-surface init of new cells
+    double* lb_force = nullptr; // device lbF seen by the collision (zero without forceField)
+    // free surface
+    uint32_t* if_list = nullptr;    // compacted interface list
+    int* if_count = nullptr;
+    double* fs_scal = nullptr;      // [0]=surplus [1]=interface count as double
+    long long cap_if = 0;
+    int* fs_flag = nullptr;         // per-node conversion flags
+    uint32_t* fs_parent = nullptr;  // per-node parent key for new interface cells
+    double* fs_part = nullptr;      // per-block FP64 partials for the surplus ledger
+    // DEM
+    hb_dem_dev d;
+    // graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int kernels_per_cycle = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+// launchers implemented in the .cu files (all enqueue on ctx->stream)
+namespace hb {
+int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int E,
+                        const double* ob_x0, const double* ob_r, int O);
+void launch_refresh_bulk(hb_ctx* c);
+void launch_lb_step(hb_ctx* c);
+void launch_lb_wallforce(hb_ctx* c);
+void launch_flip(hb_ctx* c);
+int launch_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside,
+                          const uint32_t* solid, const double* f, const double* n, const double* u,
+                          const double* mass, const double* visc);
+int launch_download_lattice(hb_ctx* c, double* f_dev, int which_parity);
+void launch_dem_substep(hb_ctx* c);
+void launch_dem_first_predict(hb_ctx* c);
+void launch_couple_masks(hb_ctx* c);
+void launch_couple_reduce(hb_ctx* c);
+void launch_fs_step(hb_ctx* c);
+int fs_init(hb_ctx* c);
+int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o);
+}  // namespace hb

@@ -1,0 +1,683 @@
+// hb_dem.cu -- DEM substep kernels (FP64) and LB-DEM coupling kernels.
+//
+// DEM::discreteElementStep (DEM.cpp:331-376) runs multiStep substeps of
+//   [neighbour rebuild if maxDisp > 0.25 nebrRange] predict -> forces -> correct.
+// Here one substep is: k_nl_cells + k_nl_build (both return at once unless the device
+// rebuild flag is set), k_dem_forces, k_dem_correct.  The corrector also updates the
+// displacement trigger (a deterministic max over elements) and runs the NEXT substep's
+// predictor, which depends only on the element's own corrected state (elmt.cpp:139-177).
+//
+// Contacts: every particle owns its candidate list (both directions).  A pair is always
+// evaluated with I = min index, J = max index, so both owners compute bit-identical
+// pair forces; each sums its own side in list order.  No floating-point atomics.
+//
+// Coupling (LB.cpp:1851-2033): one CTA per particle sweeps the particle's bounding box.
+#include <cstdio>
+
+#include "hb_common.cuh"
+#include "hb_ctx.h"
+
+namespace hb {
+
+struct DemArgs {
+    int E;
+    double *x0, *x1, *x2, *x3, *x4, *x5;
+    double *xp0, *xp1, *xp2, *xp3, *xp4, *xp5;
+    double *w0, *w1, *w2, *w3, *w4, *w5;
+    double *wp0, *wp1, *wp2, *wp3, *wp4, *wp5;
+    double *q0, *q1, *q2, *q3, *q4, *q5;
+    double *qp0, *qp1, *qp2, *qp3, *qp4, *qp5;
+    double *wG, *wL, *wpG, *wpL;
+    double *FH, *MH, *FP, *FW, *MP, *MW;
+    double *fvol, *m, *I, *rad;
+    int *cell_of, *cell_cnt, *cell_start, *cell_fill, *cell_items;
+    int *nbr, *nbr_cnt, *wall_of, *obj, *obj_cnt;
+    double* scal;
+    int* contacts;
+    double* partial;
+    unsigned int* done;
+    int ncells, nC0, nC1, nC2;
+    double cw0, cw1, cw2, nebrRange, trigger, dt;
+    int nw;
+    double wp[MAX_WALLS][3], wn[MAX_WALLS][3];
+    int O;
+    const double *ox0, *ox1, *orad;
+    int model;
+    double kn, damp, knConst, ksConst, viscTang, muPart, muWall, numVisc, demF[3];
+    int* status;
+    unsigned long long* total_contacts;
+};
+
+struct V {
+    double x, y, z;
+};
+__device__ __forceinline__ V ld3(const double* a, int E, int i) { return V{a[i], a[E + i], a[2 * E + i]}; }
+__device__ __forceinline__ void st3(double* a, int E, int i, V v) {
+    a[i] = v.x; a[E + i] = v.y; a[2 * E + i] = v.z;
+}
+__device__ __forceinline__ V add(V a, V b) { return V{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V sub(V a, V b) { return V{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V mul(double s, V a) { return V{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ V divs(V a, double s) { return V{a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ double dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ double nrm2(V a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+__device__ __forceinline__ V cross(V a, V b) {
+    return V{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+struct Qt {
+    double a, b, c, d;
+};
+__device__ __forceinline__ Qt ldq(const double* q, int E, int i) { return Qt{q[i], q[E + i], q[2 * E + i], q[3 * E + i]}; }
+__device__ __forceinline__ void stq(double* q, int E, int i, Qt v) {
+    q[i] = v.a; q[E + i] = v.b; q[2 * E + i] = v.c; q[3 * E + i] = v.d;
+}
+__device__ __forceinline__ Qt qmul(Qt p, Qt q) {  // vector.cpp:222-228, p.multiply(q)
+    return Qt{q.a * p.a - q.b * p.b - q.c * p.c - q.d * p.d, q.a * p.b + q.b * p.a - q.c * p.d + q.d * p.c,
+              q.a * p.c + q.b * p.d + q.c * p.a - q.d * p.b, q.a * p.d - q.b * p.c + q.c * p.b + q.d * p.a};
+}
+__device__ __forceinline__ Qt qadj(Qt p) { return Qt{p.a, -p.b, -p.c, -p.d}; }
+__device__ __forceinline__ V project(V v, Qt q) {  // vector.cpp:364-370
+    Qt r = qmul(qmul(q, Qt{0.0, v.x, v.y, v.z}), qadj(q));
+    return V{r.b, r.c, r.d};
+}
+__device__ __forceinline__ Qt qaxpy(Qt a, Qt b, double s) { return Qt{a.a + b.a * s, a.b + b.b * s, a.c + b.c * s, a.d + b.d * s}; }
+
+__device__ double normal_contact(const DemArgs& a, double overlap, double vn, double effRad, double effMass) {
+    if (a.model == HB_HERTZIAN) {  // DEM.cpp:2142-2152
+        const double kn = a.knConst * sqrt(effRad) * sqrt(overlap);
+        const double gn = 2.0 * a.damp * sqrt(kn * effMass);
+        return fmax(kn * overlap + (-gn * vn), 0.0);
+    }
+    const double el = a.kn * overlap;  // DEM.cpp:2153-2160
+    const double gn = 2.0 * a.damp * sqrt(a.kn * effMass);
+    return fmax(el + (-gn * vn), 0.0);
+}
+__device__ double tangential_contact(const DemArgs& a, double vt, double fn, double effRad, double effMass,
+                                     double mu) {  // DEM.cpp:2176-2222
+    const double ks = a.model == HB_HERTZIAN ? a.ksConst * sqrt(effRad) * pow(fabs(fn), 1.0 / 3.0) : a.kn;
+    const double gs = 2.0 * a.viscTang * sqrt(effMass * ks);
+    return fmin(gs * vt, mu * fn);
+}
+
+// ---- neighbour rebuild (DEM.cpp:1326-1533) -------------------------------------------
+
+// single CTA: cell of every particle (linearizePosition, vector.cpp:147-149), counting
+// sort into cells, then ascending order inside each cell
+__global__ void __launch_bounds__(1024) k_nl_cells(DemArgs a) {
+    if (a.scal[1] == 0.0) return;
+    const int E = a.E, nc = a.ncells;
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) { a.cell_cnt[c] = 0; a.cell_fill[c] = 0; }
+    __syncthreads();
+    for (int i = threadIdx.x; i < E; i += blockDim.x) {
+        const V x = ld3(a.x0, E, i);
+        const int c0 = (int)floor(x.x / a.cw0) + 1, c1 = (int)floor(x.y / a.cw1) + 2, c2 = (int)floor(x.z / a.cw2);
+        int c = -1;
+        if (c0 >= 0 && c0 < a.nC0 && c1 >= 0 && c1 < a.nC1 && c2 >= 0 && c2 < a.nC2) c = c0 + a.nC0 * (c1 + a.nC1 * c2);
+        else atomicOr(a.status + 2, 2);  // particle outside the box
+        a.cell_of[i] = c;
+        if (c >= 0) atomicAdd(a.cell_cnt + c, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // exclusive scan (ncells is small: a few thousand)
+        int s = 0;
+        for (int c = 0; c < nc; ++c) { a.cell_start[c] = s; s += a.cell_cnt[c]; }
+        a.cell_start[nc] = s;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < E; i += blockDim.x) {
+        const int c = a.cell_of[i];
+        if (c >= 0) a.cell_items[a.cell_start[c] + atomicAdd(a.cell_fill + c, 1)] = i;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {  // insertion sort per cell
+        const int s = a.cell_start[c], e = a.cell_start[c + 1];
+        for (int k = s + 1; k < e; ++k) {
+            const int v = a.cell_items[k];
+            int m = k - 1;
+            while (m >= s && a.cell_items[m] > v) { a.cell_items[m + 1] = a.cell_items[m]; --m; }
+            a.cell_items[m + 1] = v;
+        }
+    }
+}
+
+// candidate list of every particle: all others within nebrRange in the 27 adjacent
+// cells; first wall within range (DEM.cpp:1502-1511); objects within range
+__global__ void k_nl_build(DemArgs a) {
+    if (a.scal[1] == 0.0) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.E) return;
+    const int E = a.E;
+    const V xi = ld3(a.x0, E, i);
+    const double r2 = a.nebrRange * a.nebrRange;
+    int cnt = 0;
+    const int c = a.cell_of[i];
+    if (c >= 0) {
+        const int c0 = c % a.nC0, c1 = (c / a.nC0) % a.nC1, c2 = c / (a.nC0 * a.nC1);
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int n0 = c0 + dx, n1 = c1 + dy, n2 = c2 + dz;
+                    if (n0 < 0 || n1 < 0 || n2 < 0 || n0 >= a.nC0 || n1 >= a.nC1 || n2 >= a.nC2) continue;
+                    const int cc = n0 + a.nC0 * (n1 + a.nC1 * n2);
+                    for (int k = a.cell_start[cc]; k < a.cell_start[cc + 1]; ++k) {
+                        const int j = a.cell_items[k];
+                        if (j == i) continue;
+                        const V d = sub(ld3(a.x0, E, j), xi);
+                        if (nrm2(d) < r2) {
+                            if (cnt < NBR_CAP) a.nbr[(long long)i * NBR_CAP + cnt] = j;
+                            ++cnt;
+                        }
+                    }
+                }
+    }
+    if (cnt > NBR_CAP) { atomicOr(a.status + 2, 1); cnt = NBR_CAP; }
+    a.nbr_cnt[i] = cnt;
+    int wo = -1;
+    for (int w = 0; w < a.nw; ++w) {
+        const double d = a.wn[w][0] * (xi.x - a.wp[w][0]) + a.wn[w][1] * (xi.y - a.wp[w][1]) +
+                         a.wn[w][2] * (xi.z - a.wp[w][2]);
+        if (d < a.nebrRange) { wo = w; break; }
+    }
+    a.wall_of[i] = wo;
+    int oc = 0;
+    for (int o = 0; o < a.O; ++o) {
+        const V d = sub(xi, V{a.ox0[o], a.ox0[a.O + o], a.ox0[2 * a.O + o]});
+        if (nrm2(d) < r2) {
+            if (oc < OBJ_CAP) a.obj[(long long)i * OBJ_CAP + oc] = o;
+            ++oc;
+        }
+    }
+    if (oc > OBJ_CAP) { atomicOr(a.status + 2, 4); oc = OBJ_CAP; }
+    a.obj_cnt[i] = oc;
+}
+
+// ---- forces (DEM.cpp:1114-1182, 1801-2136) --------------------------------------------
+__global__ void k_dem_forces(DemArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int E = a.E;
+    int ncont = 0;
+    if (i < E) {
+        const V xpi = ld3(a.xp0, E, i);
+        V FP{0, 0, 0}, MP{0, 0, 0}, FW{0, 0, 0}, MW{0, 0, 0};
+        const int cnt = a.nbr_cnt[i];
+        for (int k = 0; k < cnt; ++k) {
+            const int j = a.nbr[(long long)i * NBR_CAP + k];
+            const int I = min(i, j), J = max(i, j);
+            const double rI = a.rad[I], rJ = a.rad[J];
+            const double sig = rI + rJ;
+            const V vd = sub(ld3(a.xp0, E, J), ld3(a.xp0, E, I));
+            if (!(nrm2(vd) < sig * sig)) continue;
+            if (i < j) ++ncont;
+            // particleParticleCollision with I = lower index (DEM.cpp:1801-1900)
+            const double dist = sqrt(nrm2(vd));
+            const double overlap = rI + rJ - dist;
+            const V relVel = sub(ld3(a.xp1, E, J), ld3(a.xp1, E, I));
+            const V en = divs(vd, dist);
+            const double vn = dot(relVel, en);
+            const V nrv = mul(vn, en);
+            const double mI = a.m[I], mJ = a.m[J];
+            const double effMass = mI * mJ / (mI + mJ);
+            const double effRad = rI * rJ / (rI + rJ);
+            const double fn = normal_contact(a, overlap, vn, effRad, effMass);
+            const V nf = mul(fn, en);
+            const V vrI = mul(rI, en), vrJ = mul(-rJ, en);
+            const V rvc = add(sub(relVel, cross(ld3(a.wpG, E, I), vrI)), cross(ld3(a.wpG, E, J), vrJ));
+            const V tang = sub(rvc, nrv);
+            const double nt = sqrt(nrm2(tang));
+            V tf{0, 0, 0};
+            const bool hasT = nt != 0.0;
+            if (hasT) {
+                const double ft = tangential_contact(a, nt, fn, effRad, effMass, a.muPart);
+                tf = mul(ft, divs(tang, nt));
+            }
+            if (i == I) {
+                FP = sub(FP, nf);
+                if (hasT) { MP = add(MP, cross(vrI, tf)); FP = add(FP, tf); }
+            } else {
+                FP = add(FP, nf);
+                if (hasT) { MP = sub(MP, cross(vrJ, tf)); FP = sub(FP, tf); }
+            }
+        }
+        const double ri = a.rad[i], mi = a.m[i];
+        const V xpv = ld3(a.xp1, E, i);
+        const V wpg = ld3(a.wpG, E, i);
+        const int w = a.wall_of[i];
+        if (w >= 0) {  // wallParticleCollision (DEM.cpp:1902-1982), static walls
+            const V wn{a.wn[w][0], a.wn[w][1], a.wn[w][2]};
+            const double dist = dot(wn, sub(xpi, V{a.wp[w][0], a.wp[w][1], a.wp[w][2]}));
+            const double overlap = ri - dist;
+            if (overlap > 0.0) {
+                const V relVel = sub(xpv, V{0, 0, 0});
+                const double vn = dot(relVel, wn);
+                const V nrv = mul(vn, wn);
+                const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
+                const V nf = mul(fn, wn);
+                const V vrJ = mul(-ri, wn);
+                FW = add(FW, nf);
+                const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
+                const double nt = sqrt(nrm2(tang));
+                if (nt != 0.0) {
+                    const double ft = tangential_contact(a, nt, fn, ri, mi, a.muWall);
+                    const V tfw = mul(ft, divs(tang, nt));
+                    MW = sub(MW, cross(vrJ, tfw));
+                    FW = sub(FW, tfw);
+                }
+            }
+        }
+        const int oc = a.obj_cnt[i];
+        for (int k = 0; k < oc; ++k) {  // objectParticleCollision (DEM.cpp:2060-2136)
+            const int o = a.obj[(long long)i * OBJ_CAP + k];
+            const V vd = sub(xpi, V{a.ox0[o], a.ox0[a.O + o], a.ox0[2 * a.O + o]});
+            const double dist = sqrt(nrm2(vd));
+            const double overlap = ri + a.orad[o] - dist;
+            if (!(overlap > 0.0)) continue;
+            const V en = mul(1.0 / dist, vd);
+            const V relVel = sub(xpv, V{a.ox1[o], a.ox1[a.O + o], a.ox1[2 * a.O + o]});
+            const double vn = dot(relVel, en);
+            const V nrv = mul(vn, en);
+            const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
+            const V nf = mul(fn, en);
+            const V vrJ = mul(-ri, en);
+            const V cJ = add(vrJ, V{0, 0, 0});
+            FW = add(FW, nf);
+            const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
+            const double nt = sqrt(nrm2(tang));
+            if (nt != 0.0) {
+                const double ft = tangential_contact(a, nt, fn, ri, mi, a.muPart);
+                const V tfo = mul(ft, divs(tang, nt));
+                MW = sub(MW, cross(cJ, tfo));
+                FW = sub(FW, tfo);
+            }
+        }
+        st3(a.FP, E, i, FP);
+        st3(a.MP, E, i, MP);
+        st3(a.FW, E, i, FW);
+        st3(a.MW, E, i, MW);
+        // Newton (DEM.cpp:1149-1181)
+        const double nv = a.numVisc;
+        const V FVisc = mul(-6.0 * M_PI * nv * ri, xpv);
+        const V MVisc = mul(-8.0 * M_PI * nv * ri * ri * ri, wpg);
+        const V x2 = add(divs(add(add(add(FVisc, ld3(a.FH, E, i)), FP), FW), mi), V{a.demF[0], a.demF[1], a.demF[2]});
+        st3(a.x2, E, i, x2);
+        const V mom = add(add(add(MVisc, ld3(a.MH, E, i)), MP), MW);
+        const Qt qp0 = ldq(a.qp0, E, i);
+        const V mBf = project(mom, qadj(qp0));
+        const V Iv = ld3(a.I, E, i);
+        const V wl = ld3(a.wpL, E, i);
+        const V waBf{(mBf.x + (Iv.y - Iv.z) * wl.y * wl.z) / Iv.x, (mBf.y + (Iv.z - Iv.x) * wl.z * wl.x) / Iv.y,
+                     (mBf.z + (Iv.x - Iv.y) * wl.x * wl.y) / Iv.z};
+        st3(a.w1, E, i, project(waBf, qp0));
+    }
+    // overlapping-pair counter: integer atomics, deterministic
+    for (int off = 16; off > 0; off >>= 1) ncont += __shfl_down_sync(0xffffffffu, ncont, off);
+    if ((threadIdx.x & 31) == 0 && ncont) {
+        atomicAdd(a.contacts, ncont);
+        atomicAdd(a.total_contacts, (unsigned long long)ncont);
+    }
+}
+
+__device__ void predict_one(const DemArgs& a, int i) {  // elmt.cpp:139-177
+    const int E = a.E;
+    const double dt = a.dt;
+    const double c[5] = {dt, dt * dt / 2.0, dt * dt * dt / 6.0, dt * dt * dt * dt / 24.0, dt * dt * dt * dt * dt / 120.0};
+    const V x0 = ld3(a.x0, E, i), x1 = ld3(a.x1, E, i), x2 = ld3(a.x2, E, i), x3 = ld3(a.x3, E, i),
+            x4 = ld3(a.x4, E, i), x5 = ld3(a.x5, E, i);
+    st3(a.xp0, E, i, add(add(add(add(add(x0, mul(c[0], x1)), mul(c[1], x2)), mul(c[2], x3)), mul(c[3], x4)), mul(c[4], x5)));
+    st3(a.xp1, E, i, add(add(add(add(x1, mul(c[0], x2)), mul(c[1], x3)), mul(c[2], x4)), mul(c[3], x5)));
+    st3(a.xp2, E, i, add(add(add(x2, mul(c[0], x3)), mul(c[1], x4)), mul(c[2], x5)));
+    st3(a.xp3, E, i, add(add(x3, mul(c[0], x4)), mul(c[1], x5)));
+    st3(a.xp4, E, i, add(x4, mul(c[0], x5)));
+    st3(a.xp5, E, i, x5);
+    const Qt q0 = ldq(a.q0, E, i), q1 = ldq(a.q1, E, i), q2 = ldq(a.q2, E, i), q3 = ldq(a.q3, E, i),
+             q4 = ldq(a.q4, E, i), q5 = ldq(a.q5, E, i);
+    Qt qp0 = qaxpy(qaxpy(qaxpy(qaxpy(qaxpy(q0, q1, c[0]), q2, c[1]), q3, c[2]), q4, c[3]), q5, c[4]);
+    const double qn = sqrt(qp0.a * qp0.a + qp0.b * qp0.b + qp0.c * qp0.c + qp0.d * qp0.d);
+    qp0 = Qt{qp0.a / qn, qp0.b / qn, qp0.c / qn, qp0.d / qn};
+    stq(a.qp0, E, i, qp0);
+    stq(a.qp1, E, i, qaxpy(qaxpy(qaxpy(qaxpy(q1, q2, c[0]), q3, c[1]), q4, c[2]), q5, c[3]));
+    stq(a.qp2, E, i, qaxpy(qaxpy(qaxpy(q2, q3, c[0]), q4, c[1]), q5, c[2]));
+    stq(a.qp3, E, i, qaxpy(qaxpy(q3, q4, c[0]), q5, c[1]));
+    stq(a.qp4, E, i, qaxpy(q4, q5, c[0]));
+    stq(a.qp5, E, i, q5);
+    const V w0 = ld3(a.w0, E, i), w1 = ld3(a.w1, E, i), w2 = ld3(a.w2, E, i), w3 = ld3(a.w3, E, i),
+            w4 = ld3(a.w4, E, i), w5 = ld3(a.w5, E, i);
+    const V wp0 = add(add(add(add(add(w0, mul(c[0], w1)), mul(c[1], w2)), mul(c[2], w3)), mul(c[3], w4)), mul(c[4], w5));
+    st3(a.wp0, E, i, wp0);
+    st3(a.wp1, E, i, add(add(add(add(w1, mul(c[0], w2)), mul(c[1], w3)), mul(c[2], w4)), mul(c[3], w5)));
+    st3(a.wp2, E, i, add(add(add(w2, mul(c[0], w3)), mul(c[1], w4)), mul(c[2], w5)));
+    st3(a.wp3, E, i, add(add(w3, mul(c[0], w4)), mul(c[1], w5)));
+    st3(a.wp4, E, i, add(w4, mul(c[0], w5)));
+    st3(a.wp5, E, i, w5);
+    st3(a.wpG, E, i, wp0);
+    st3(a.wpL, E, i, project(wp0, qadj(qp0)));
+}
+
+// displacement trigger (DEM.cpp:1314-1324, 334-347): block maxima, the last block folds
+// them and sets the rebuild flag for the next substep
+__device__ void trigger_update(const DemArgs& a, double v2) {
+    __shared__ double sh[256];
+    __shared__ bool last;
+    sh[threadIdx.x] = v2;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        a.partial[blockIdx.x] = sh[0];
+        __threadfence();
+        last = atomicAdd(a.done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double mx = 0.0;
+        for (int b = 0; b < (int)gridDim.x; ++b) mx = fmax(mx, ((volatile double*)a.partial)[b]);
+        double md = a.scal[0] + sqrt(mx) * a.dt;
+        double flag = 0.0;
+        if (md > a.trigger) { md = 0.0; flag = 1.0; }
+        a.scal[0] = md;
+        a.scal[1] = flag;
+        *a.done = 0u;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_dem_correct(DemArgs a) {  // elmt.cpp:179-254
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int E = a.E;
+    double v2 = 0.0;
+    if (i < E) {
+        const double dt = a.dt;
+        const double c[5] = {dt, dt * dt / 2.0, dt * dt * dt / 6.0, dt * dt * dt * dt / 24.0, dt * dt * dt * dt * dt / 120.0};
+        const double g1[6] = {95.0 / 288.0, 1.0, 25.0 / 24.0, 35.0 / 72.0, 5.0 / 48.0, 1.0 / 120.0};
+        const double g2[6] = {3.0 / 16.0, 251.0 / 360.0, 1.0, 11.0 / 18.0, 1.0 / 6.0, 1.0 / 60.0};
+        const double c1o[6] = {g1[0] * c[0], g1[1] * c[0] / c[0], g1[2] * c[0] / c[1], g1[3] * c[0] / c[2],
+                               g1[4] * c[0] / c[3], g1[5] * c[0] / c[4]};
+        const double c2o[6] = {g2[0] * c[1], g2[1] * c[1] / c[0], g2[2] * c[1] / c[1], g2[3] * c[1] / c[2],
+                               g2[4] * c[1] / c[3], g2[5] * c[1] / c[4]};
+        const V x2 = ld3(a.x2, E, i);
+        const V x2c = sub(x2, ld3(a.xp2, E, i));
+        const V x0 = add(ld3(a.xp0, E, i), mul(c2o[0], x2c));
+        const V x1 = add(ld3(a.xp1, E, i), mul(c2o[1], x2c));
+        st3(a.x0, E, i, x0);
+        st3(a.x1, E, i, x1);
+        st3(a.x3, E, i, add(ld3(a.xp3, E, i), mul(c2o[3], x2c)));
+        st3(a.x4, E, i, add(ld3(a.xp4, E, i), mul(c2o[4], x2c)));
+        st3(a.x5, E, i, add(ld3(a.xp5, E, i), mul(c2o[5], x2c)));
+        const V w1 = ld3(a.w1, E, i);
+        const V w1c = sub(w1, ld3(a.wp1, E, i));
+        const V w0 = add(ld3(a.wp0, E, i), mul(c1o[0], w1c));
+        st3(a.w0, E, i, w0);
+        st3(a.w2, E, i, add(ld3(a.wp2, E, i), mul(c1o[2], w1c)));
+        st3(a.w3, E, i, add(ld3(a.wp3, E, i), mul(c1o[3], w1c)));
+        st3(a.w4, E, i, add(ld3(a.wp4, E, i), mul(c1o[4], w1c)));
+        st3(a.w5, E, i, add(ld3(a.wp5, E, i), mul(c1o[5], w1c)));
+        const Qt q2 = ldq(a.q2, E, i);
+        const Qt qp2 = ldq(a.qp2, E, i);
+        const Qt q2c = Qt{q2.a - qp2.a, q2.b - qp2.b, q2.c - qp2.c, q2.d - qp2.d};
+        Qt q0 = qaxpy(ldq(a.qp0, E, i), q2c, c2o[0]);
+        stq(a.q1, E, i, qaxpy(ldq(a.qp1, E, i), q2c, c2o[1]));
+        stq(a.q3, E, i, qaxpy(ldq(a.qp3, E, i), q2c, c2o[3]));
+        stq(a.q4, E, i, qaxpy(ldq(a.qp4, E, i), q2c, c2o[4]));
+        stq(a.q5, E, i, qaxpy(ldq(a.qp5, E, i), q2c, c2o[5]));
+        const double qn = sqrt(q0.a * q0.a + q0.b * q0.b + q0.c * q0.c + q0.d * q0.d);
+        q0 = Qt{q0.a / qn, q0.b / qn, q0.c / qn, q0.d / qn};
+        stq(a.q0, E, i, q0);
+        st3(a.wG, E, i, w0);
+        st3(a.wL, E, i, project(w0, qadj(q0)));
+        v2 = nrm2(x1);
+    }
+    trigger_update(a, v2);
+    if (i < E) predict_one(a, i);  // next substep's predictor
+}
+
+// first substep after init: trigger from the initial velocities, then predict
+__global__ void __launch_bounds__(256) k_dem_first(DemArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v2 = 0.0;
+    if (i < a.E) v2 = nrm2(ld3(a.x1, a.E, i));
+    trigger_update(a, v2);
+    if (i < a.E) predict_one(a, i);
+}
+
+// ---- coupling -----------------------------------------------------------------------
+struct CoupleArgs {
+    int X, Y, Z;
+    long long N;
+    int per[6];
+    uint8_t* ntype;
+    uint32_t* solid;
+    unsigned long long* claim;
+    const double *x0, *rad;
+    int E;
+    const void* dv;
+    int dv_f64;
+    const double* mass;
+    int free_surface;
+    double *FH, *MH, *fvol;
+};
+
+struct Box {
+    int x0, y0, z0, nx, ny, nz;
+};
+__device__ __forceinline__ Box pbox(const CoupleArgs& a, int p, int margin) {
+    const int E = a.E;
+    const double cx_ = a.x0[p], cy_ = a.x0[E + p], cz_ = a.x0[2 * E + p], r = a.rad[p];
+    Box b;
+    b.x0 = max(0, (int)floor(cx_ - r) - margin);
+    b.y0 = max(0, (int)floor(cy_ - r) - margin);
+    b.z0 = max(0, (int)floor(cz_ - r) - margin);
+    const int x1 = min(a.X - 1, (int)ceil(cx_ + r) + margin);
+    const int y1 = min(a.Y - 1, (int)ceil(cy_ + r) + margin);
+    const int z1 = min(a.Z - 1, (int)ceil(cz_ + r) + margin);
+    b.nx = max(0, x1 - b.x0 + 1);
+    b.ny = max(0, y1 - b.y0 + 1);
+    b.nz = max(0, z1 - b.z0 + 1);
+    return b;
+}
+__device__ __forceinline__ bool in_sphere(const CoupleArgs& a, int p, int x, int y, int z) {
+    const int E = a.E;
+    const double dx = x - a.x0[p], dy = y - a.x0[E + p], dz = z - a.x0[2 * E + p];
+    return dx * dx + dy * dy + dz * dz < a.rad[p] * a.rad[p];  // insideSphere, vector.cpp:153-158
+}
+
+// findNewActive (LB.cpp:1921-1967): uncovered nodes leave the particle
+__global__ void k_couple_pop(CoupleArgs a) {
+    const int p = blockIdx.x;
+    const Box b = pbox(a, p, 2);
+    for (int k = threadIdx.x; k < b.nx * b.ny * b.nz; k += blockDim.x) {
+        const int x = b.x0 + k % b.nx, y = b.y0 + (k / b.nx) % b.ny, z = b.z0 + k / (b.nx * b.ny);
+        const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
+        const uint8_t t = a.ntype[i];
+        if ((t & HB_INSIDE) && a.solid[i] == (uint32_t)p && !in_sphere(a, p, x, y, z)) a.ntype[i] = t & ~HB_INSIDE;
+    }
+}
+
+// findNewSolid (LB.cpp:1969-2033): a node covered by particle p and 6-linked from a
+// node of p becomes a particle node; the source node with the lowest index wins, which
+// is the reference's first-in-particleNodes-order rule (the list is sorted there)
+__global__ void k_couple_claim(CoupleArgs a) {
+    const int p = blockIdx.x;
+    const Box b = pbox(a, p, 1);
+    for (int k = threadIdx.x; k < b.nx * b.ny * b.nz; k += blockDim.x) {
+        const int x = b.x0 + k % b.nx, y = b.y0 + (k / b.nx) % b.ny, z = b.z0 + k / (b.nx * b.ny);
+        const long long l = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
+        if (a.ntype[l] & HB_INSIDE) continue;
+        if (!in_sphere(a, p, x, y, z)) continue;
+        unsigned long long best = ~0ull;
+        for (int kk = 1; kk <= 6; ++kk) {  // source m with link d[m][kk] == l
+            int mx = x - cx(kk), my = y - cy(kk), mz = z - cz(kk);
+            if (mx == 0 && a.per[1]) mx = a.X - 2; else if (mx == a.X - 1 && a.per[0]) mx = 1;
+            if (my == 0 && a.per[3]) my = a.Y - 2; else if (my == a.Y - 1 && a.per[2]) my = 1;
+            if (mz == 0 && a.per[5]) mz = a.Z - 2; else if (mz == a.Z - 1 && a.per[4]) mz = 1;
+            if (mx < 0 || my < 0 || mz < 0 || mx >= a.X || my >= a.Y || mz >= a.Z) continue;
+            const long long m = (long long)mx + (long long)a.X * ((long long)my + (long long)a.Y * mz);
+            const uint8_t tm = a.ntype[m];
+            if (!(tm & HB_INSIDE) || a.solid[m] != (uint32_t)p) continue;
+            // the reference's link table: interior nodes link arithmetically (with the
+            // periodic remap), boundary nodes link to themselves
+            const bool interior = mx > 0 && my > 0 && mz > 0 && mx < a.X - 1 && my < a.Y - 1 && mz < a.Z - 1;
+            if (!interior) continue;
+            int lx = mx + cx(kk), ly = my + cy(kk), lz = mz + cz(kk);
+            if (lx == 0 && a.per[0]) lx = a.X - 2; else if (lx == a.X - 1 && a.per[1]) lx = 1;
+            if (ly == 0 && a.per[2]) ly = a.Y - 2; else if (ly == a.Y - 1 && a.per[3]) ly = 1;
+            if (lz == 0 && a.per[4]) lz = a.Z - 2; else if (lz == a.Z - 1 && a.per[5]) lz = 1;
+            if (lx != x || ly != y || lz != z) continue;
+            const unsigned long long key = ((unsigned long long)m << 32) | (unsigned)p;
+            if (key < best) best = key;
+        }
+        if (best != ~0ull) atomicMin(a.claim + l, best);
+    }
+}
+
+__global__ void k_couple_commit(CoupleArgs a) {
+    const int p = blockIdx.x;
+    const Box b = pbox(a, p, 1);
+    for (int k = threadIdx.x; k < b.nx * b.ny * b.nz; k += blockDim.x) {
+        const int x = b.x0 + k % b.nx, y = b.y0 + (k / b.nx) % b.ny, z = b.z0 + k / (b.nx * b.ny);
+        const long long l = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
+        const unsigned long long c = a.claim[l];
+        if (c == ~0ull || (uint32_t)(c & 0xffffffffu) != (uint32_t)p) continue;
+        a.ntype[l] = a.ntype[l] | HB_INSIDE;
+        a.solid[l] = (uint32_t)p;
+        a.claim[l] = ~0ull;
+    }
+}
+
+// element hydrodynamic force, torque and entrained fluid (LB.cpp:1853-1918): fixed
+// thread-to-node assignment and a fixed-order tree, so the sum is reproducible
+__global__ void __launch_bounds__(256) k_couple_reduce(CoupleArgs a) {
+    __shared__ double sh[7][256];
+    const int p = blockIdx.x;
+    const int E = a.E;
+    const Box b = pbox(a, p, 1);
+    const double px = a.x0[p], py = a.x0[E + p], pz = a.x0[2 * E + p];
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int k = threadIdx.x; k < b.nx * b.ny * b.nz; k += blockDim.x) {
+        const int x = b.x0 + k % b.nx, y = b.y0 + (k / b.nx) % b.ny, z = b.z0 + k / (b.nx * b.ny);
+        const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
+        const uint8_t t = a.ntype[i];
+        if (!(t & HB_INSIDE) || !is_active(t) || a.solid[i] != (uint32_t)p) continue;
+        double dvx, dvy, dvz;
+        if (a.dv_f64) {
+            const double* d = reinterpret_cast<const double*>(a.dv);
+            dvx = d[i]; dvy = d[a.N + i]; dvz = d[2 * a.N + i];
+        } else {
+            const float* d = reinterpret_cast<const float*>(a.dv);
+            dvx = d[i]; dvy = d[a.N + i]; dvz = d[2 * a.N + i];
+        }
+        const double rx = (x - px) + 0.0, ry = (y - py) + 0.0, rz = (z - pz) + 0.0;
+        acc[0] += dvx; acc[1] += dvy; acc[2] += dvz;
+        acc[3] += ry * dvz - rz * dvy;
+        acc[4] += rz * dvx - rx * dvz;
+        acc[5] += rx * dvy - ry * dvx;
+        acc[6] += a.free_surface ? a.mass[i] : 1.0;
+    }
+    for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] = acc[c];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s)
+            for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        a.FH[p] = sh[0][0]; a.FH[E + p] = sh[1][0]; a.FH[2 * E + p] = sh[2][0];
+        a.MH[p] = sh[3][0]; a.MH[E + p] = sh[4][0]; a.MH[2 * E + p] = sh[5][0];
+        a.fvol[p] = sh[6][0];
+    }
+}
+
+// ---- host side ------------------------------------------------------------------------
+
+static DemArgs dem_args(hb_ctx* c) {
+    hb_dem_dev& d = c->d;
+    DemArgs a;
+    a.E = d.E;
+    a.x0 = d.x[0]; a.x1 = d.x[1]; a.x2 = d.x[2]; a.x3 = d.x[3]; a.x4 = d.x[4]; a.x5 = d.x[5];
+    a.xp0 = d.xp[0]; a.xp1 = d.xp[1]; a.xp2 = d.xp[2]; a.xp3 = d.xp[3]; a.xp4 = d.xp[4]; a.xp5 = d.xp[5];
+    a.w0 = d.w[0]; a.w1 = d.w[1]; a.w2 = d.w[2]; a.w3 = d.w[3]; a.w4 = d.w[4]; a.w5 = d.w[5];
+    a.wp0 = d.wp[0]; a.wp1 = d.wp[1]; a.wp2 = d.wp[2]; a.wp3 = d.wp[3]; a.wp4 = d.wp[4]; a.wp5 = d.wp[5];
+    a.q0 = d.q[0]; a.q1 = d.q[1]; a.q2 = d.q[2]; a.q3 = d.q[3]; a.q4 = d.q[4]; a.q5 = d.q[5];
+    a.qp0 = d.qp[0]; a.qp1 = d.qp[1]; a.qp2 = d.qp[2]; a.qp3 = d.qp[3]; a.qp4 = d.qp[4]; a.qp5 = d.qp[5];
+    a.wG = d.wG; a.wL = d.wL; a.wpG = d.wpG; a.wpL = d.wpL;
+    a.FH = d.FH; a.MH = d.MH; a.FP = d.FP; a.FW = d.FW; a.MP = d.MP; a.MW = d.MW;
+    a.fvol = d.fvol; a.m = d.m; a.I = d.I; a.rad = d.rad;
+    a.cell_of = d.cell_of; a.cell_cnt = d.cell_cnt; a.cell_start = d.cell_start;
+    a.cell_fill = d.cell_fill; a.cell_items = d.cell_items;
+    a.nbr = d.nbr; a.nbr_cnt = d.nbr_cnt; a.wall_of = d.wall_of; a.obj = d.obj; a.obj_cnt = d.obj_cnt;
+    a.scal = d.scal; a.contacts = d.contacts; a.partial = d.partial; a.done = d.done;
+    a.ncells = d.ncells; a.nC0 = d.nCells[0]; a.nC1 = d.nCells[1]; a.nC2 = d.nCells[2];
+    a.cw0 = d.cellWidth[0]; a.cw1 = d.cellWidth[1]; a.cw2 = d.cellWidth[2];
+    a.nebrRange = d.nebrRange; a.trigger = d.trigger; a.dt = d.dt;
+    a.nw = d.nw;
+    for (int w = 0; w < MAX_WALLS; ++w)
+        for (int k = 0; k < 3; ++k) {
+            a.wp[w][k] = d.wall_p[w][k];
+            a.wn[w][k] = d.wall_n[w][k];
+        }
+    a.O = d.O; a.ox0 = d.obj_x0; a.ox1 = d.obj_x1; a.orad = d.obj_r;
+    a.model = c->P.contact_model;
+    a.kn = c->P.linear_stiff;
+    a.damp = d.dampCoeff;
+    a.knConst = d.knConst;
+    a.ksConst = d.ksConst;
+    a.viscTang = c->P.visc_tang;
+    a.muPart = c->P.friction_part;
+    a.muWall = c->P.friction_wall;
+    a.numVisc = c->P.num_visc;
+    for (int k = 0; k < 3; ++k) a.demF[k] = c->P.lbF[k];  // DEM.cpp:194
+    a.status = c->status;
+    a.total_contacts = reinterpret_cast<unsigned long long*>(d.scal + 4);
+    return a;
+}
+
+void launch_dem_first_predict(hb_ctx* c) {
+    if (c->d.E == 0) return;
+    DemArgs a = dem_args(c);
+    k_dem_first<<<ceil_div(c->d.E, 256), 256, 0, c->stream>>>(a);
+}
+
+void launch_dem_substep(hb_ctx* c) {
+    if (c->d.E == 0) return;
+    DemArgs a = dem_args(c);
+    const int G = ceil_div(c->d.E, 256);
+    k_nl_cells<<<1, 1024, 0, c->stream>>>(a);
+    k_nl_build<<<ceil_div(c->d.E, 128), 128, 0, c->stream>>>(a);
+    cudaMemsetAsync(c->d.contacts, 0, sizeof(int), c->stream);
+    k_dem_forces<<<ceil_div(c->d.E, 128), 128, 0, c->stream>>>(a);
+    k_dem_correct<<<G, 256, 0, c->stream>>>(a);
+}
+
+static CoupleArgs couple_args(hb_ctx* c) {
+    CoupleArgs a;
+    a.X = c->X; a.Y = c->Y; a.Z = c->Z; a.N = c->N;
+    for (int k = 0; k < 6; ++k) a.per[k] = c->P.boundary[k] == HB_T_PERIODIC;
+    a.ntype = c->ntype;
+    a.solid = c->solid;
+    a.claim = c->claim;
+    a.x0 = c->d.x[0];
+    a.rad = c->d.rad;
+    a.E = c->d.E;
+    a.dv = c->dv;
+    a.dv_f64 = c->P.precision == HB_FP64;
+    a.mass = c->mass;
+    a.free_surface = c->P.free_surface;
+    a.FH = c->d.FH; a.MH = c->d.MH; a.fvol = c->d.fvol;
+    return a;
+}
+
+void launch_couple_masks(hb_ctx* c) {
+    if (c->d.E == 0) return;
+    CoupleArgs a = couple_args(c);
+    k_couple_pop<<<c->d.E, 128, 0, c->stream>>>(a);
+    k_couple_claim<<<c->d.E, 128, 0, c->stream>>>(a);
+    k_couple_commit<<<c->d.E, 128, 0, c->stream>>>(a);
+}
+
+void launch_couple_reduce(hb_ctx* c) {
+    if (c->d.E == 0) return;
+    CoupleArgs a = couple_args(c);
+    k_couple_reduce<<<c->d.E, 256, 0, c->stream>>>(a);
+}
+
+}  // namespace hb

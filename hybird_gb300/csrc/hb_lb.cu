@@ -1,0 +1,722 @@
+// hb_lb.cu -- fused D3Q19 collide+stream kernel, lattice init and lattice up/download.
+//
+// The reference updates each active node as reconstruct -> hydro force -> collide ->
+// store -> pull-stream (LB.cpp:221-233, 1062-1488).  Here one kernel does all of it in
+// PUSH form: the node reads its own 19 post-streaming populations (coalesced SoA loads),
+// collides in registers and scatters the post-collision values to the neighbours that
+// pull them in the reference.  Links to non-active neighbours are resolved by the node
+// itself, exactly as the reference's pull rules: static wall -> bounce-back
+// (LB.cpp:1344-1356), moving wall -> bounce-back with 6 n w (u_w.c) (LB.cpp:1321-1341),
+// gas -> constant-pressure reconstruction (LB.cpp:1237-1246).  Every population of
+// every active node is written exactly once per step, so the state between steps is the
+// reference's node::f after streaming, and the free-surface and coupling phases, which
+// the reference runs between streaming and the next collision, see the same data.
+//
+// Roofline: per lattice update the kernel reads 19 and writes 19 stored populations
+// plus the one-byte node type: 2*19*s + 1 bytes (s = 8, 4, 2 for FP64, FP32, FP16S).
+#include <cstdio>
+
+#include "hb_common.cuh"
+#include "hb_ctx.h"
+
+namespace hb {
+
+__device__ __forceinline__ void flag_status(int* status, int word) {
+    atomicOr(status + word, 1);
+}
+
+// neighbour of interior node (x,y,z) along direction j with the reference's periodic
+// remap (LB.cpp:437-472): a link crossing a periodic face re-enters on the opposite side
+__device__ __forceinline__ long long link_index(const LBArgs& a, int x, int y, int z, int j) {
+    int xn = x + cx(j), yn = y + cy(j), zn = z + cz(j);
+    if (xn == 0 && a.per[0]) xn = a.X - 2;
+    else if (xn == a.X - 1 && a.per[1]) xn = 1;
+    if (yn == 0 && a.per[2]) yn = a.Y - 2;
+    else if (yn == a.Y - 1 && a.per[3]) yn = 1;
+    if (zn == 0 && a.per[4]) zn = a.Z - 2;
+    else if (zn == a.Z - 1 && a.per[5]) zn = 1;
+    return (long long)xn + (long long)a.X * ((long long)yn + (long long)a.Y * zn);
+}
+
+template <class P>
+__global__ void __launch_bounds__(256) k_collide_stream(LBArgs a) {
+    using T = typename P::T;
+    using S = typename P::S;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y + 1;
+    const int z = blockIdx.z + 1;
+    if (x < 1 || x > a.X - 2) return;
+    const long long N = a.N;
+    const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
+    const uint8_t t = a.ntype[i];
+    if (!is_active(t)) return;
+    const int par = *a.parity;
+    const int mode = *a.mode;
+    const S* fin = reinterpret_cast<const S*>(par ? a.fB : a.fA);
+    S* fout = reinterpret_cast<S*>(par ? a.fA : a.fB);
+    const uint8_t code = t & HB_TYPE_MASK;
+
+    T f[Q];
+#pragma unroll
+    for (int j = 0; j < Q; ++j) f[j] = P::load(fin + (long long)j * N + i);
+
+    // ---- reconstruct (node.cpp:63-83); deviation forms keep rho-1 to preserve digits
+    T n, dn;
+    {
+        T s = T(0);
+#pragma unroll
+        for (int j = 0; j < Q; ++j) s += f[j];
+        if constexpr (P::DEV) { dn = s; n = T(1) + s; }
+        else { n = s; dn = s - T(1); }
+    }
+    T mx = T(0), my = T(0), mz = T(0);
+#pragma unroll
+    for (int j = 0; j < Q; ++j) {
+        if (cx(j) > 0) mx += f[j]; else if (cx(j) < 0) mx += -f[j];
+        if (cy(j) > 0) my += f[j]; else if (cy(j) < 0) my += -f[j];
+        if (cz(j) > 0) mz += f[j]; else if (cz(j) < 0) mz += -f[j];
+    }
+    T ux = mx / n, uy = my / n, uz = mz / n;
+    if (!(n > T(0)) || ux != ux || uy != uy || uz != uz) flag_status(a.status, 0);
+
+    // ---- direct-forcing coupling (LB.cpp:1863-1904): node force -eps (u - u_p)
+    T hx = T(0), hy = T(0), hz = T(0);
+    const double m_i = a.free_surface ? a.mass[i] : 1.0;
+    if (a.couple && (t & HB_INSIDE)) {
+        const int p = (int)a.solid[i];
+        const int E = a.parts.count;
+        const double rx = (double)x - a.parts.x0[p];
+        const double ry = (double)y - a.parts.x0[E + p];
+        const double rz = (double)z - a.parts.x0[2 * E + p];
+        const double wx = a.parts.w[p], wy = a.parts.w[E + p], wz = a.parts.w[2 * E + p];
+        const double lvx = a.parts.x1[p] + (wy * rz - wz * ry);
+        const double lvy = a.parts.x1[E + p] + (wz * rx - wx * rz);
+        const double lvz = a.parts.x1[2 * E + p] + (wx * ry - wy * rx);
+        const T lf = T(m_i / (double)n);
+        const T dvx = lf * (ux - T(lvx)), dvy = lf * (uy - T(lvy)), dvz = lf * (uz - T(lvz));
+        hx = T(0) + T(-1) * dvx;
+        hy = T(0) + T(-1) * dvy;
+        hz = T(0) + T(-1) * dvz;
+        T* dv = reinterpret_cast<T*>(a.dv);
+        dv[i] = dvx;
+        dv[N + i] = dvy;
+        dv[2 * N + i] = dvz;
+    }
+
+    // ---- collision (LB.cpp:1094-1111, node.cpp:85-184)
+    const T Fx = T(a.F[0]) + hx, Fy = T(a.F[1]) + hy, Fz = T(a.F[2]) + hz;
+    ux = ux + (T(0.5) * Fx) / n;  // shiftVelocity
+    uy = uy + (T(0.5) * Fy) / n;
+    uz = uz + (T(0.5) * Fz) / n;
+    const T usq = ux * ux + uy * uy + uz * uz;
+    T feq[Q];  // FP64: f_eq; deviation forms: f_eq - w
+#pragma unroll
+    for (int j = 0; j < Q; ++j) {
+        T vu = T(0);
+        if (cx(j) > 0) vu += ux; else if (cx(j) < 0) vu += -ux;
+        if (cy(j) > 0) vu += uy; else if (cy(j) < 0) vu += -uy;
+        if (cz(j) > 0) vu += uz; else if (cz(j) < 0) vu += -uz;
+        const T w = T(wgt(j));
+        if constexpr (P::DEV)
+            feq[j] = w * (dn + n * (T(3) * vu + T(4.5) * vu * vu - T(1.5) * usq));
+        else
+            feq[j] = w * n * (T(1) + T(3) * vu + T(4.5) * vu * vu - T(1.5) * usq);
+    }
+    T visc;
+    if (a.visc_model) {  // computeShearRate (node.cpp:103-145)
+        T* vp = reinterpret_cast<T*>(a.visc);
+        const T vold = vp[i];
+        const T tau = T(0.5) + T(3) * vold;
+        T gxx = 0, gyy = 0, gzz = 0, gxy = 0, gxz = 0, gyz = 0;
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const T d = f[j] - feq[j];
+            if (cx(j)) gxx += d;
+            if (cy(j)) gyy += d;
+            if (cz(j)) gzz += d;
+            if (cx(j) * cy(j) > 0) gxy += d; else if (cx(j) * cy(j) < 0) gxy += -d;
+            if (cx(j) * cz(j) > 0) gxz += d; else if (cx(j) * cz(j) < 0) gxz += -d;
+            if (cy(j) * cz(j) > 0) gyz += d; else if (cy(j) * cz(j) < 0) gyz += -d;
+        }
+        const T sc = T(1.5) / (tau * n);
+        gxx *= sc; gyy *= sc; gzz *= sc; gxy *= sc; gxz *= sc; gyz *= sc;
+        const T shear = sqrt(T(0.5) * (gxx * gxx + gyy * gyy + gzz * gzz +
+                                       T(2) * (gxy * gxy + gxz * gxz + gyz * gyz)));
+        const T nuTurb = (a.visc_model & 2) ? T(a.turb_const) * shear : T(0);
+        const T nuApp = (a.visc_model & 1) ? T(a.plastic_visc) + T(a.yield_stress) / (n * T(2) * shear) : vold;
+        const T minV = T((0.501 - 0.5) / 3.0), maxV = T((1.8 - 0.5) / 3.0);
+        visc = fmax(minV, fmin(maxV, nuApp + nuTurb));  // NaN -> maxV like std::min/max
+        vp[i] = visc;
+    } else {
+        visc = T(a.init_visc);
+    }
+    T fs[Q];
+    if (a.collision == HB_TRT) {
+        const T tp = T(0.5) + T(3) * visc;
+        const T tm = T(a.trt_magic) / (tp - T(0.5)) + T(0.5);
+        const T wp = T(1) / tp, wm = T(1) / tm;
+        const T ap = T(1) - T(0.5) * wp, am = T(1) - T(0.5) * wm;
+        T Fi[Q];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const T vu = T(cx(j)) * ux + T(cy(j)) * uy + T(cz(j)) * uz;
+            const T fpx = T(9) * vu * T(cx(j)) + T(3) * (T(cx(j)) - ux);
+            const T fpy = T(9) * vu * T(cy(j)) + T(3) * (T(cy(j)) - uy);
+            const T fpz = T(9) * vu * T(cz(j)) + T(3) * (T(cz(j)) - uz);
+            Fi[j] = T(wgt(j)) * (fpx * Fx + fpy * Fy + fpz * Fz);
+        }
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const int o = opp(j);
+            const T fp = T(0.5) * (f[j] + f[o]), fm = T(0.5) * (f[j] - f[o]);
+            const T ep = T(0.5) * (feq[j] + feq[o]), em = T(0.5) * (feq[j] - feq[o]);
+            fs[j] = f[j] - wp * (fp - ep) - wm * (fm - em) + ap * T(0.5) * (Fi[j] + Fi[o]) +
+                    am * T(0.5) * (Fi[j] - Fi[o]);
+        }
+    } else {
+        const T omega = T(1) / (T(0.5) + T(3) * visc);
+        const T omegaf = T(1) - T(1) / (T(1) + T(6) * visc);
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            T v = f[j] + omega * (feq[j] - f[j]);  // solveCollision
+            T vu = T(0);
+            if (cx(j) > 0) vu += ux; else if (cx(j) < 0) vu += -ux;
+            if (cy(j) > 0) vu += uy; else if (cy(j) < 0) vu += -uy;
+            if (cz(j) > 0) vu += uz; else if (cz(j) < 0) vu += -uz;
+            const T fpx = T(9) * vu * T(cx(j)) + T(3) * (T(cx(j)) - ux);  // addForce
+            const T fpy = T(9) * vu * T(cy(j)) + T(3) * (T(cy(j)) - uy);
+            const T fpz = T(9) * vu * T(cz(j)) + T(3) * (T(cz(j)) - uz);
+            v += T(1) * omegaf * T(wgt(j)) * (fpx * Fx + fpy * Fy + fpz * Fz);
+            fs[j] = v;
+        }
+    }
+
+    // ---- node macros needed by later phases (free surface, downloads, wall force)
+    const bool all = (mode & 1) != 0;
+    if (all || a.free_surface || !(t & HB_BULK)) a.rho[i] = (double)n;
+    if (a.free_surface && code == HB_T_FLUID) a.mass[i] = (double)n;
+    if (all || code == HB_T_INTERFACE) {
+        a.u[i] = (double)ux; a.u[N + i] = (double)uy; a.u[2 * N + i] = (double)uz;
+        a.hf[i] = (double)hx; a.hf[N + i] = (double)hy; a.hf[2 * N + i] = (double)hz;
+    }
+
+    // ---- streaming (push form of LB.cpp:1216-1463)
+    P::store(fout + i, fs[0]);
+    if (t & HB_BULK) {
+#pragma unroll
+        for (int j = 1; j < Q; ++j) P::store(fout + (long long)j * N + link_index(a, x, y, z, j), fs[j]);
+        return;
+    }
+#pragma unroll
+    for (int j = 1; j < Q; ++j) {
+        const long long l = link_index(a, x, y, z, j);
+        const uint8_t lc = a.ntype[l] & HB_TYPE_MASK;
+        const int o = opp(j);
+        if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
+            P::store(fout + (long long)j * N + l, fs[j]);
+        } else if (lc == HB_T_GAS) {
+            T vu = T(0);
+            if (cx(j) > 0) vu += ux; else if (cx(j) < 0) vu += -ux;
+            if (cy(j) > 0) vu += uy; else if (cy(j) < 0) vu += -uy;
+            if (cz(j) > 0) vu += uz; else if (cz(j) < 0) vu += -uz;
+            const T w = T(wgt(j));
+            T v;
+            if constexpr (P::DEV) v = -fs[j] + w * (T(9) * (vu * vu) - T(3) * usq);
+            else v = -fs[j] + w * T(1) * (T(2) + T(9) * (vu * vu) - T(3) * usq);
+            P::store(fout + (long long)o * N + i, v);
+        } else if (lc == HB_T_DYNWALL) {
+            const double uw = a.u[l] * cx(j) + a.u[N + l] * cy(j) + a.u[2 * N + l] * cz(j);
+            const T BBi = T(6.0 * (double)n * wgt(j) * uw);
+            P::store(fout + (long long)o * N + i, fs[j] - BBi);
+        } else if (lc == HB_T_STATWALL) {
+            P::store(fout + (long long)o * N + i, fs[j]);
+        } else {
+            flag_status(a.status, 1);  // TYPE ERROR (LB.cpp:1458-1461)
+        }
+    }
+}
+
+// Moving-wall momentum exchange and extra mass (LB.cpp:1321-1341): recomputed from the
+// post-streaming populations, f_out[opp j] = fs[j] - BBi, so the hot kernel stays free
+// of reductions.  One FP64 partial per CTA and wall, summed in CTA order afterwards.
+template <class P>
+__global__ void __launch_bounds__(256) k_wallforce(LBArgs a) {
+    using S = typename P::S;
+    __shared__ double sh[256];
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y + 1, z = blockIdx.z + 1;
+    const long long N = a.N;
+    double acc[MAX_WALLS * 3 + 1];
+#pragma unroll
+    for (int k = 0; k < MAX_WALLS * 3 + 1; ++k) acc[k] = 0.0;
+    if (x >= 1 && x <= a.X - 2) {
+        const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
+        const uint8_t t = a.ntype[i];
+        if (is_active(t) && !(t & HB_BULK)) {
+            const S* fcur = reinterpret_cast<const S*>(*a.parity ? a.fA : a.fB);
+            for (int j = 1; j < Q; ++j) {
+                const long long l = link_index(a, x, y, z, j);
+                if ((a.ntype[l] & HB_TYPE_MASK) != HB_T_DYNWALL) continue;
+                const double uw = a.u[l] * cx(j) + a.u[N + l] * cy(j) + a.u[2 * N + l] * cz(j);
+                const double BBi = 6.0 * a.rho[i] * wgt(j) * uw;
+                double fo = (double)P::load(fcur + (long long)opp(j) * N + i);
+                if (P::DEV) fo += wgt(j);
+                const double fsj = fo + BBi;
+                const double sc = (2.0 * (fsj - 1.0 * wgt(j)) - BBi) * 1.0;
+                const int w = (int)a.solid[l];
+                if (w >= 0 && w < MAX_WALLS) {
+                    acc[3 * w] += sc * cx(j);
+                    acc[3 * w + 1] += sc * cy(j);
+                    acc[3 * w + 2] += sc * cz(j);
+                }
+                acc[MAX_WALLS * 3] += BBi * a.mass[i];
+            }
+        }
+    }
+    const int nb = gridDim.x * gridDim.y * gridDim.z;
+    const int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    for (int k = 0; k < MAX_WALLS * 3 + 1; ++k) {
+        sh[threadIdx.x] = acc[k];
+        __syncthreads();
+        for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+            if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) a.wall_part[(long long)k * nb + b] = sh[0];
+        __syncthreads();
+    }
+}
+
+__global__ void k_wallforce_final(const double* part, int nb, double* out) {
+    const int k = threadIdx.x;
+    if (k >= MAX_WALLS * 3 + 1) return;
+    double s = 0.0;
+    for (int b = 0; b < nb; ++b) s += part[(long long)k * nb + b];
+    out[k] = s;
+}
+
+__global__ void k_flip(int* parity) { *parity ^= 1; }
+
+// ---- initialisation ------------------------------------------------------------------
+
+struct InitArgs {
+    int X, Y, Z;
+    long long N;
+    int boundary[6];
+    int nw;
+    double wp[MAX_WALLS][3], wn[MAX_WALLS][3];
+    int wmov[MAX_WALLS];
+    double gas_x, gas_z;
+};
+
+// lattice boundary codes (LB.cpp:393-432), DEM walls (LB.cpp:497-533)
+__global__ void k_init_types(InitArgs a, uint8_t* ntype, uint32_t* solid) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
+    auto wall = [](int c) { return c >= 5 && c <= 9; };
+    int t = HB_T_FLUID;
+    if (x == 0 && !wall(t)) t = a.boundary[0];
+    else if (x == a.X - 1 && !wall(t)) t = a.boundary[1];
+    if (y == 0 && !wall(t)) t = a.boundary[2];
+    else if (y == a.Y - 1 && !wall(t)) t = a.boundary[3];
+    if (z == 0 && !wall(t)) t = a.boundary[4];
+    else if (z == a.Z - 1 && !wall(t)) t = a.boundary[5];
+    uint32_t s = 0;
+    for (int w = 0; w < a.nw; ++w) {
+        const double d = a.wn[w][0] * ((double)x - a.wp[w][0]) + a.wn[w][1] * ((double)y - a.wp[w][1]) +
+                         a.wn[w][2] * ((double)z - a.wp[w][2]);
+        if (d < 0.0) {
+            s = (uint32_t)w;
+            t = a.wmov[w] ? HB_T_DYNWALL : HB_T_STATWALL;
+        }
+    }
+    ntype[i] = (uint8_t)t;
+    solid[i] = s;
+}
+
+// particle flags, last particle in list order wins (LB.cpp:475-495)
+__global__ void k_init_particles(InitArgs a, const double* x0, const double* r, int E,
+                                 const uint8_t* ntype, int* owner) {
+    const int p = blockIdx.x;
+    const double cxp = x0[p], cyp = x0[E + p], czp = x0[2 * E + p], rr = r[p];
+    const int x0i = max(0, (int)floor(cxp - rr) - 1), x1i = min(a.X - 1, (int)ceil(cxp + rr) + 1);
+    const int y0i = max(0, (int)floor(cyp - rr) - 1), y1i = min(a.Y - 1, (int)ceil(cyp + rr) + 1);
+    const int z0i = max(0, (int)floor(czp - rr) - 1), z1i = min(a.Z - 1, (int)ceil(czp + rr) + 1);
+    const int nx = x1i - x0i + 1, ny = y1i - y0i + 1, nz = z1i - z0i + 1;
+    for (int k = threadIdx.x; k < nx * ny * nz; k += blockDim.x) {
+        const int x = x0i + k % nx, y = y0i + (k / nx) % ny, z = z0i + k / (nx * ny);
+        const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
+        if (!is_active(ntype[i])) continue;
+        const double dx = x - cxp, dy = y - cyp, dz = z - czp;
+        if (dx * dx + dy * dy + dz * dz < rr * rr) atomicMax(owner + i, p);
+    }
+}
+
+// objects become static wall nodes, last object wins (LB.cpp:535-550); particle owner
+// commits the inside flag (set before objects in the reference, so it survives them)
+__global__ void k_init_objects(InitArgs a, const double* ox, const double* orad, int O,
+                               const int* owner, uint8_t* ntype, uint32_t* solid) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
+    uint8_t t = ntype[i];
+    uint32_t s = solid[i];
+    if (owner && owner[i] >= 0) {
+        t |= HB_INSIDE;
+        s = (uint32_t)owner[i];
+    }
+    for (int o = 0; o < O; ++o) {
+        const double dx = x - ox[o], dy = y - ox[O + o], dz = z - ox[2 * O + o];
+        if (dx * dx + dy * dy + dz * dz < orad[o] * orad[o]) {
+            s = (uint32_t)o;
+            t = (t & HB_INSIDE) | HB_T_STATWALL;
+        }
+    }
+    // dam-break column: gas outside x < gx*X, z < gz*Z
+    if ((t & HB_TYPE_MASK) == HB_T_FLUID && (a.gas_x > 0.0 || a.gas_z > 0.0)) {
+        if ((double)x >= a.gas_x * a.X || (double)z >= a.gas_z * a.Z) t = (t & HB_INSIDE) | HB_T_GAS;
+    }
+    ntype[i] = t;
+    solid[i] = s;
+}
+
+__device__ __forceinline__ long long init_link(const InitArgs& a, const int* per, long long i, int j) {
+    const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
+    int xn = x + cx(j), yn = y + cy(j), zn = z + cz(j);
+    if (xn == 0 && per[0]) xn = a.X - 2; else if (xn == a.X - 1 && per[1]) xn = 1;
+    if (yn == 0 && per[2]) yn = a.Y - 2; else if (yn == a.Y - 1 && per[3]) yn = 1;
+    if (zn == 0 && per[4]) zn = a.Z - 2; else if (zn == a.Z - 1 && per[5]) zn = 1;
+    return (long long)xn + (long long)a.X * ((long long)yn + (long long)a.Y * zn);
+}
+
+struct PerFaces { int v[6]; };
+
+// interface = fluid with a gas link (LB.cpp:788-797)
+__global__ void k_init_interface(InitArgs a, PerFaces pf, uint8_t* ntype) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
+    if (x < 1 || y < 1 || z < 1 || x > a.X - 2 || y > a.Y - 2 || z > a.Z - 2) return;
+    const uint8_t t = ntype[i];
+    if ((t & HB_TYPE_MASK) != HB_T_FLUID) return;
+    for (int j = 1; j < Q; ++j)
+        if ((ntype[init_link(a, pf.v, i, j)] & HB_TYPE_MASK) == HB_T_GAS) {
+            ntype[i] = (t & ~HB_TYPE_MASK) | HB_T_INTERFACE;
+            return;
+        }
+}
+
+// isolated interface (no fluid link) -> gas (LB.cpp:800-814)
+__global__ void k_init_isolated(InitArgs a, PerFaces pf, uint8_t* ntype) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    const uint8_t t = ntype[i];
+    if ((t & HB_TYPE_MASK) != HB_T_INTERFACE) return;
+    for (int j = 1; j < Q; ++j)
+        if ((ntype[init_link(a, pf.v, i, j)] & HB_TYPE_MASK) == HB_T_FLUID) return;
+    ntype[i] = (t & ~HB_TYPE_MASK) | HB_T_GAS;
+}
+
+__global__ void k_active_max(InitArgs a, const uint8_t* ntype, int* mx) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    if (!is_active(ntype[i])) return;
+    atomicMax(mx + 0, (int)(i % a.X));
+    atomicMax(mx + 1, (int)((i / a.X) % a.Y));
+    atomicMax(mx + 2, (int)(i / ((long long)a.X * a.Y)));
+}
+
+// hydrostatic variables + f = f_eq (LB.cpp:909-944, node.cpp:26-61) and wall nodes
+template <class P>
+__global__ void k_init_vars(InitArgs a, LBArgs b, const int* mx, double Fx, double Fy, double Fz,
+                            double ivx, double ivy, double ivz, double visc0) {
+    using T = typename P::T;
+    using S = typename P::S;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    const long long N = a.N;
+    const uint8_t t = b.ntype[i];
+    const uint8_t code = t & HB_TYPE_MASK;
+    const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
+    double n = 1.0, mass = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+    bool node = false;
+    if (code == HB_T_FLUID) {
+        const double dhx = (double)x - mx[0], dhy = (double)y - mx[1], dhz = (double)z - mx[2];
+        n = 1.0 + 3.0 * 1.0 * 1.0 * 1.0 * (dhx * Fx + dhy * Fy + dhz * Fz);
+        mass = 1.0;
+        vx = ivx; vy = ivy; vz = ivz;
+        node = true;
+    } else if (code == HB_T_INTERFACE) {
+        n = 1.0;
+        mass = 0.5 * 1.0;
+        vx = ivx; vy = ivy; vz = ivz;
+        node = true;
+    }
+    double ux = 0.0, uy = 0.0, uz = 0.0;
+    if (node) {
+        ux = 1.0 * Fx / 2.0 / n + vx;
+        uy = 1.0 * Fy / 2.0 / n + vy;
+        uz = 1.0 * Fz / 2.0 / n + vz;
+    }
+    b.rho[i] = n;
+    b.u[i] = ux; b.u[N + i] = uy; b.u[2 * N + i] = uz;
+    b.hf[i] = 0.0; b.hf[N + i] = 0.0; b.hf[2 * N + i] = 0.0;
+    b.mass[i] = mass;
+    if (b.visc_model) reinterpret_cast<T*>(b.visc)[i] = node ? T(visc0) : T(0);
+    S* f = reinterpret_cast<S*>(b.fA);
+    const double usq = ux * ux + uy * uy + uz * uz;
+    for (int j = 0; j < Q; ++j) {
+        const double vu = ux * cx(j) + uy * cy(j) + uz * cz(j);
+        double fe = node ? wgt(j) * n * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq) : wgt(j);
+        if (P::DEV) fe -= wgt(j);
+        P::store(f + (long long)j * N + i, (T)fe);
+        P::store(reinterpret_cast<S*>(b.fB) + (long long)j * N + i, (T)(P::DEV ? 0.0 : wgt(j)));
+    }
+}
+
+// HB_BULK: node active and all 18 links lead to active nodes
+__global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    uint8_t t = ntype[i];
+    bool bulk = is_active(t);
+    if (bulk) {
+        const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
+        if (x < 1 || y < 1 || z < 1 || x > a.X - 2 || y > a.Y - 2 || z > a.Z - 2) bulk = false;
+        for (int j = 1; j < Q && bulk; ++j)
+            if (!is_active(ntype[init_link(a, pf.v, i, j)])) bulk = false;
+    }
+    const uint8_t nt = bulk ? (t | HB_BULK) : (t & ~HB_BULK);
+    if (nt != t) ntype[i] = nt;
+}
+
+// ---- upload / download ---------------------------------------------------------------
+
+template <class P>
+__global__ void k_upload_f(const double* f, long long N, void* dst) {
+    using S = typename P::S;
+    using T = typename P::T;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    for (int j = 0; j < Q; ++j) {
+        double v = f[(long long)j * N + i];
+        if (P::DEV) v -= wgt(j);
+        P::store(reinterpret_cast<S*>(dst) + (long long)j * N + i, (T)v);
+    }
+}
+
+template <class P>
+__global__ void k_download_f(const void* src, long long N, double* f) {
+    using S = typename P::S;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    for (int j = 0; j < Q; ++j) {
+        double v = (double)P::load(reinterpret_cast<const S*>(src) + (long long)j * N + i);
+        if (P::DEV) v += wgt(j);
+        f[(long long)j * N + i] = v;
+    }
+}
+
+__global__ void k_pack_types(const uint8_t* type, const uint8_t* inside, uint8_t* ntype, long long N) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    ntype[i] = (uint8_t)((type[i] & HB_TYPE_MASK) | (inside[i] ? HB_INSIDE : 0));
+}
+
+// ---- host launchers ------------------------------------------------------------------
+
+static InitArgs init_args(hb_ctx* c) {
+    InitArgs a;
+    a.X = c->X; a.Y = c->Y; a.Z = c->Z; a.N = c->N;
+    for (int k = 0; k < 6; ++k) a.boundary[k] = c->P.boundary[k];
+    a.nw = c->d.nw;
+    for (int w = 0; w < MAX_WALLS; ++w) {
+        for (int k = 0; k < 3; ++k) {
+            a.wp[w][k] = w < c->d.nw ? c->d.wall_p[w][k] : 0.0;
+            a.wn[w][k] = w < c->d.nw ? c->d.wall_n[w][k] : 0.0;
+        }
+        a.wmov[w] = w < c->d.nw ? c->d.wall_moving[w] : 0;
+    }
+    a.gas_x = c->P.gas_box[0];
+    a.gas_z = c->P.gas_box[1];
+    return a;
+}
+
+static PerFaces per_faces(hb_ctx* c) {
+    PerFaces p;
+    for (int k = 0; k < 6; ++k) p.v[k] = c->P.boundary[k] == HB_T_PERIODIC;
+    return p;
+}
+
+LBArgs lb_args(hb_ctx* c) {
+    LBArgs a;
+    a.X = c->X; a.Y = c->Y; a.Z = c->Z; a.N = c->N;
+    for (int k = 0; k < 6; ++k) a.per[k] = c->P.boundary[k] == HB_T_PERIODIC;
+    a.ntype = c->ntype;
+    a.solid = c->solid;
+    a.fA = c->fA;
+    a.fB = c->fB;
+    a.parity = c->parity;
+    a.mode = c->mode;
+    a.rho = c->rho;
+    a.u = c->u;
+    a.hf = c->hf;
+    a.mass = c->mass;
+    a.visc = c->visc;
+    a.dv = c->dv;
+    a.F = c->lb_force;
+    a.init_visc = c->P.init_visc;
+    a.collision = c->P.collision;
+    a.trt_magic = c->P.trt_magic;
+    a.visc_model = (c->P.non_newtonian ? 1 : 0) | (c->P.turbulence ? 2 : 0);
+    a.plastic_visc = c->P.plastic_visc;
+    a.yield_stress = c->P.yield_stress;
+    a.turb_const = c->P.turb_const;
+    a.free_surface = c->P.free_surface;
+    a.couple = (c->P.dem_solve && c->d.E > 0) ? 1 : 0;
+    a.parts.count = c->d.E;
+    a.parts.x0 = c->d.E ? c->d.x[0] : nullptr;
+    a.parts.x1 = c->d.E ? c->d.x[1] : nullptr;
+    a.parts.w = c->d.E ? c->d.wG : nullptr;
+    a.parts.radius = c->d.E ? c->d.rad : nullptr;
+    a.status = c->status;
+    a.wall_part = c->wall_part;
+    a.nwalls = c->d.nw;
+    return a;
+}
+
+static dim3 lb_grid(hb_ctx* c, int& block) {
+    block = c->X <= 64 ? 64 : (c->X <= 128 ? 128 : 256);
+    return dim3((unsigned)ceil_div(c->X, block), (unsigned)(c->Y - 2), (unsigned)(c->Z - 2));
+}
+
+int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int E,
+                        const double* ob_x0, const double* ob_r, int O) {
+    InitArgs a = init_args(c);
+    const int B = 256;
+    const int G = ceil_div(c->N, B);
+    k_init_types<<<G, B, 0, c->stream>>>(a, c->ntype, c->solid);
+    int* owner = nullptr;
+    if (E > 0) {
+        cudaMalloc(&owner, sizeof(int) * c->N);
+        cudaMemsetAsync(owner, 0xFF, sizeof(int) * c->N, c->stream);
+        k_init_particles<<<E, 256, 0, c->stream>>>(a, el_x0, el_r, E, c->ntype, owner);
+    }
+    k_init_objects<<<G, B, 0, c->stream>>>(a, ob_x0, ob_r, O, owner, c->ntype, c->solid);
+    PerFaces pf = per_faces(c);
+    k_init_interface<<<G, B, 0, c->stream>>>(a, pf, c->ntype);
+    k_init_isolated<<<G, B, 0, c->stream>>>(a, pf, c->ntype);
+    int* mx = nullptr;
+    cudaMalloc(&mx, 3 * sizeof(int));
+    cudaMemsetAsync(mx, 0, 3 * sizeof(int), c->stream);
+    k_active_max<<<G, B, 0, c->stream>>>(a, c->ntype, mx);
+    LBArgs b = lb_args(c);
+    const double* F = c->P.lbF;  // initialisation always uses lbF (LB.cpp:935)
+    const double* iv = c->P.init_velocity;
+    if (c->P.precision == HB_FP64)
+        k_init_vars<PolF64><<<G, B, 0, c->stream>>>(a, b, mx, F[0], F[1], F[2], iv[0], iv[1], iv[2], c->P.init_visc);
+    else if (c->P.precision == HB_FP32)
+        k_init_vars<PolF32><<<G, B, 0, c->stream>>>(a, b, mx, F[0], F[1], F[2], iv[0], iv[1], iv[2], c->P.init_visc);
+    else
+        k_init_vars<PolF16><<<G, B, 0, c->stream>>>(a, b, mx, F[0], F[1], F[2], iv[0], iv[1], iv[2], c->P.init_visc);
+    k_bulk<<<G, B, 0, c->stream>>>(a, pf, c->ntype);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (owner) cudaFree(owner);
+    cudaFree(mx);
+    return e == cudaSuccess ? 0 : -1;
+}
+
+void launch_refresh_bulk(hb_ctx* c) {
+    InitArgs a = init_args(c);
+    k_bulk<<<ceil_div(c->N, 256), 256, 0, c->stream>>>(a, per_faces(c), c->ntype);
+}
+
+void launch_lb_step(hb_ctx* c) {
+    LBArgs a = lb_args(c);
+    int block;
+    dim3 g = lb_grid(c, block);
+    if (c->P.precision == HB_FP64) k_collide_stream<PolF64><<<g, block, 0, c->stream>>>(a);
+    else if (c->P.precision == HB_FP32) k_collide_stream<PolF32><<<g, block, 0, c->stream>>>(a);
+    else k_collide_stream<PolF16><<<g, block, 0, c->stream>>>(a);
+}
+
+void launch_lb_wallforce(hb_ctx* c) {
+    LBArgs a = lb_args(c);
+    int block;
+    dim3 g = lb_grid(c, block);
+    if (c->P.precision == HB_FP64) k_wallforce<PolF64><<<g, block, 0, c->stream>>>(a);
+    else if (c->P.precision == HB_FP32) k_wallforce<PolF32><<<g, block, 0, c->stream>>>(a);
+    else k_wallforce<PolF16><<<g, block, 0, c->stream>>>(a);
+    k_wallforce_final<<<1, 32, 0, c->stream>>>(c->wall_part, (int)(g.x * g.y * g.z), c->wall_force);
+}
+
+void launch_flip(hb_ctx* c) { k_flip<<<1, 1, 0, c->stream>>>(c->parity); }
+
+int launch_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside,
+                          const uint32_t* solid, const double* f, const double* n, const double* u,
+                          const double* mass, const double* visc) {
+    const long long N = c->N;
+    const int B = 256, G = ceil_div(N, B);
+    uint8_t *dt = nullptr, *di = nullptr;
+    cudaMalloc(&dt, N);
+    cudaMalloc(&di, N);
+    cudaMemcpyAsync(dt, type, N, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(di, inside, N, cudaMemcpyHostToDevice, c->stream);
+    k_pack_types<<<G, B, 0, c->stream>>>(dt, di, c->ntype, N);
+    cudaMemcpyAsync(c->solid, solid, sizeof(uint32_t) * N, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->rho, n, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->u, u, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->mass, mass, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream);
+    double* df = nullptr;
+    cudaMalloc(&df, sizeof(double) * 19 * N);
+    if (f) {
+        cudaMemcpyAsync(df, f, sizeof(double) * 19 * N, cudaMemcpyHostToDevice, c->stream);
+    }
+    cudaStreamSynchronize(c->stream);
+    cudaFree(dt);
+    cudaFree(di);
+    // f given: encode; otherwise f_eq(n,u) as node::initialize does (node.cpp:26-61)
+    if (!f) {
+        std::vector<double> hf((size_t)19 * N);
+        for (long long i = 0; i < N; ++i) {
+            const double ux = u[i], uy = u[N + i], uz = u[2 * N + i];
+            const double usq = ux * ux + uy * uy + uz * uz;
+            for (int j = 0; j < Q; ++j) {
+                const double vu = ux * cx(j) + uy * cy(j) + uz * cz(j);
+                hf[(size_t)j * N + i] = wgt(j) * n[i] * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
+            }
+        }
+        cudaMemcpy(df, hf.data(), sizeof(double) * 19 * N, cudaMemcpyHostToDevice);
+    }
+    void* dst = c->h_parity ? c->fB : c->fA;
+    if (c->P.precision == HB_FP64) k_upload_f<PolF64><<<G, B, 0, c->stream>>>(df, N, dst);
+    else if (c->P.precision == HB_FP32) k_upload_f<PolF32><<<G, B, 0, c->stream>>>(df, N, dst);
+    else k_upload_f<PolF16><<<G, B, 0, c->stream>>>(df, N, dst);
+    if (c->visc && visc) {
+        if (c->P.precision == HB_FP64) {
+            cudaMemcpyAsync(c->visc, visc, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream);
+        } else {
+            std::vector<float> vf(N);
+            for (long long i = 0; i < N; ++i) vf[i] = (float)visc[i];
+            cudaMemcpyAsync(c->visc, vf.data(), sizeof(float) * N, cudaMemcpyHostToDevice, c->stream);
+            cudaStreamSynchronize(c->stream);
+        }
+    }
+    launch_refresh_bulk(c);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFree(df);
+    return e == cudaSuccess ? 0 : -1;
+}
+
+int launch_download_lattice(hb_ctx* c, double* f_dev, int which) {
+    const long long N = c->N;
+    const void* src = which ? c->fB : c->fA;
+    const int B = 256, G = ceil_div(N, B);
+    if (c->P.precision == HB_FP64) k_download_f<PolF64><<<G, B, 0, c->stream>>>(src, N, f_dev);
+    else if (c->P.precision == HB_FP32) k_download_f<PolF32><<<G, B, 0, c->stream>>>(src, N, f_dev);
+    else k_download_f<PolF16><<<G, B, 0, c->stream>>>(src, N, f_dev);
+    return 0;
+}
+
+}  // namespace hb

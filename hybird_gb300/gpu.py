@@ -1,0 +1,136 @@
+"""Python handle on the CUDA library through its C-ABI (include/hybird_gpu.h).
+
+Every call goes through ``_lib/libhybird_gpu.so``; there is no CPU fallback: loading
+fails loudly when the library is missing.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_lib = None
+
+
+class HbError(RuntimeError):
+    pass
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(abi.LIB_PATH):
+        raise HbError(f"CUDA library not built: {abi.LIB_PATH} (run __graft_entry__.build())")
+    L = C.CDLL(abi.LIB_PATH)
+    vp, P = C.c_void_p, C.POINTER
+    L.hb_last_error.restype = C.c_char_p
+    L.hb_create.argtypes = [P(abi.HbParams), P(vp)]
+    L.hb_destroy.argtypes = [vp]
+    L.hb_init.argtypes = [vp, P(abi.HbElements), P(abi.HbObjects)]
+    L.hb_upload_lattice.argtypes = [vp] + [vp] * 8
+    for name in ("hb_dem_step", "hb_fs_step", "hb_coupling_step", "hb_lb_step", "hb_synchronize"):
+        getattr(L, name).argtypes = [vp]
+    L.hb_cycle.argtypes = [vp, C.c_int32]
+    L.hb_set_body_force.argtypes = [vp, vp]
+    L.hb_download_lattice.argtypes = [vp] + [vp] * 9
+    L.hb_download_elements.argtypes = [vp] + [vp] * 11
+    L.hb_download_pairs.argtypes = [vp, vp, C.c_int64, P(C.c_int64)]
+    L.hb_download_interface.argtypes = [vp, vp, C.c_int64, P(C.c_int64)]
+    L.hb_download_walls.argtypes = [vp, vp, vp, P(C.c_int32)]
+    L.hb_get_status.argtypes = [vp, P(abi.HbStatus)]
+    L.hb_time_cycles.argtypes = [vp, C.c_int32, P(C.c_float), P(C.c_float), P(C.c_int32)]
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def check(rc):
+    if rc != abi.HB_OK:
+        raise HbError(f"{abi.STATUS_NAMES.get(rc, rc)}: {lib().hb_last_error().decode()}")
+
+
+class GpuSim:
+    """One simulation context on the current CUDA device."""
+
+    def __init__(self, params, spheres=None, objects=None):
+        self.L = lib()
+        self.params = params
+        self.arrays = abi.ElementArrays(spheres, objects)
+        h = C.c_void_p()
+        check(self.L.hb_create(C.byref(params), C.byref(h)))
+        self.h = h
+        check(self.L.hb_init(self.h, self.arrays.el_ptr(), self.arrays.ob_ptr()))
+        X, Y, Z = params.lb_size
+        self.N = X * Y * Z
+        self.E = 0 if self.arrays.el is None else self.arrays.el.count
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def cycle(self, n=1):
+        check(self.L.hb_cycle(self.h, n))
+        check(self.L.hb_synchronize(self.h))
+
+    def lattice(self):
+        N = self.N
+        out = dict(type=np.zeros(N, np.uint8), inside=np.zeros(N, np.uint8),
+                   solid=np.zeros(N, np.uint32), f=np.zeros(19 * N), n=np.zeros(N),
+                   u=np.zeros(3 * N), mass=np.zeros(N), visc=np.zeros(N),
+                   hydroForce=np.zeros(3 * N))
+        check(self.L.hb_download_lattice(self.h, *[_p(out[k]) for k in
+                                                   ("type", "inside", "solid", "f", "n", "u",
+                                                    "mass", "visc", "hydroForce")]))
+        return out
+
+    def upload(self, type, inside, solid, f, n, u, mass, visc=None):
+        check(self.L.hb_upload_lattice(self.h, _p(type), _p(inside), _p(solid), _p(f), _p(n),
+                                       _p(u), _p(mass), _p(visc)))
+
+    def elements(self):
+        E = self.E
+        keys = ("x0", "x1", "w", "q0", "FHydro", "MHydro", "FParticle", "FWall", "MParticle",
+                "MWall", "fluidVolume")
+        out = {k: np.zeros((4 if k == "q0" else 1 if k == "fluidVolume" else 3) * E) for k in keys}
+        check(self.L.hb_download_elements(self.h, *[_p(out[k]) for k in keys]))
+        return out
+
+    def pairs(self):
+        n = C.c_int64(0)
+        check(self.L.hb_download_pairs(self.h, None, 0, C.byref(n)))
+        buf = np.zeros(2 * max(n.value, 1), np.uint32)
+        check(self.L.hb_download_pairs(self.h, _p(buf), n.value, C.byref(n)))
+        return buf[:2 * n.value]
+
+    def interface(self):
+        n = C.c_int64(0)
+        check(self.L.hb_download_interface(self.h, None, 0, C.byref(n)))
+        buf = np.zeros(max(n.value, 1), np.uint32)
+        check(self.L.hb_download_interface(self.h, _p(buf), n.value, C.byref(n)))
+        return buf[:n.value]
+
+    def walls(self):
+        nw = C.c_int32(0)
+        fh = np.zeros(18)
+        fp = np.zeros(18)
+        check(self.L.hb_download_walls(self.h, _p(fh), _p(fp), C.byref(nw)))
+        return fh[:3 * nw.value], fp[:3 * nw.value]
+
+    def status(self):
+        s = abi.HbStatus()
+        check(self.L.hb_get_status(self.h, C.byref(s)))
+        return s
+
+    def time_cycles(self, n):
+        tot, lbk, kpc = C.c_float(0), C.c_float(0), C.c_int32(0)
+        check(self.L.hb_time_cycles(self.h, n, C.byref(tot), C.byref(lbk), C.byref(kpc)))
+        return tot.value, lbk.value, kpc.value

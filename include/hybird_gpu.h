@@ -157,6 +157,9 @@ int hb_coupling_step(hb_ctx* ctx);   /* LB::latticeBoltzmannCouplingStep LB.cpp:
 int hb_lb_step(hb_ctx* ctx);         /* LB::latticeBolzmannStep         LB.cpp:221-233  */
 /* nsteps whole cycles (DEM, free surface, coupling, LB) replayed from one CUDA graph. */
 int hb_cycle(hb_ctx* ctx, int32_t nsteps);
+/* Changes the body force lbF used by the collision from the next step on (the reference
+ * reads lb.lbF every collision, LB.cpp:1098-1111; problem code may change it). */
+int hb_set_body_force(hb_ctx* ctx, const double* force /* [3] */);
 int hb_synchronize(hb_ctx* ctx);
 
 /* ---- download (output steps and tests) --------------------------------------------- */

@@ -1,0 +1,63 @@
+"""CPU-only checks of the C-ABI boundary: the shared library loads without a GPU, exports
+every entry point declared in include/hybird_gpu.h, and rejects bad parameters before
+touching the device (the reference would exit(); here an error code comes back)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from hybird_gb300 import abi
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _ensure_built():
+    if not os.path.exists(abi.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+
+
+def declared_symbols():
+    syms = []
+    for hdr in os.listdir(os.path.join(REPO, "include")):
+        if hdr.endswith(".h"):
+            text = open(os.path.join(REPO, "include", hdr)).read()
+            syms += re.findall(r"^\s*(?:int|const char\*|void)\s+\**(hb_\w+)\s*\(", text, re.M)
+    return sorted(set(syms))
+
+
+def test_library_exports_every_declared_symbol():
+    _ensure_built()
+    lib = C.CDLL(abi.LIB_PATH)
+    syms = declared_symbols()
+    assert len(syms) >= 15, syms
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_params_struct_matches_header_field_order():
+    text = open(os.path.join(REPO, "include", "hybird_gpu.h")).read()
+    body = text[text.index("typedef struct hb_params {"):text.index("} hb_params;")]
+    fields = re.findall(r"^\s*(?:int32_t|int64_t|double)\s+(\w+)", body, re.M)
+    assert fields == [f[0] for f in abi.HbParams._fields_]
+
+
+@pytest.mark.parametrize("field,value,code", [
+    ("boundary", (5, 7, 7, 7, 7, 7), abi.STATUS_NAMES and 2),   # slip walls: unsupported
+    ("init_visc", 0.0, 1),
+    ("precision", 7, 1),
+])
+def test_create_rejects_bad_parameters_without_gpu(field, value, code):
+    _ensure_built()
+    lib = C.CDLL(abi.LIB_PATH)
+    lib.hb_last_error.restype = C.c_char_p
+    p = abi.make_params((8, 8, 8), (7,) * 6)
+    if field == "boundary":
+        p.boundary[:] = list(value)
+    else:
+        setattr(p, field, value)
+    h = C.c_void_p()
+    rc = lib.hb_create(C.byref(p), C.byref(h))
+    assert rc == code, (rc, lib.hb_last_error())
+    assert not h.value

@@ -1,0 +1,157 @@
+"""Parity of the CUDA library (through its C-ABI) with the reference fixtures and with the
+CPU oracle.  Tolerances: FP64 fields 1e-12 relative L-inf; integer artefacts exact;
+FP32 velocity relative L2 <= 1e-5 against the FP64 oracle."""
+import numpy as np
+import pytest
+
+from hybird_gb300 import abi
+from oracle_port import OracleSim, golden_gasbox, golden_params, load_golden, rel_linf
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+
+
+def _gpu():
+    from hybird_gb300.gpu import GpuSim
+    return GpuSim
+
+
+@pytest.mark.parametrize("name", ["channel_bgk", "channel_movwall", "channel_bingham_smag", "box_spheres"])
+def test_fp64_matches_reference_fixture(name):
+    d = load_golden(name)
+    p = golden_params(d, gas_box=golden_gasbox(name))
+    g = _gpu()(p, d["spheres"], d["objects"])
+    done = 0
+    for step in d["steps"]:
+        if step > done:
+            g.cycle(int(step) - done)
+            done = int(step)
+        pre = f"s{step}_"
+        gl = g.lattice()
+        np.testing.assert_array_equal(gl["type"], d[pre + "type"])
+        np.testing.assert_array_equal(gl["inside"], d[pre + "inside"])
+        act = (d[pre + "type"] == 0) | (d[pre + "type"] == 3)
+        if step == 0:
+            continue  # macros of step 0 are the init values; f checked below
+        assert rel_linf(gl["n"], d[pre + "n"], act) <= FP64_TOL, (name, step, "n")
+        assert rel_linf(gl["u"].reshape(3, -1), d[pre + "u"].reshape(3, -1), act) <= FP64_TOL, (name, step, "u")
+        if pre + "f" in d.files:
+            assert rel_linf(gl["f"].reshape(19, -1), d[pre + "f"].reshape(19, -1), act) <= FP64_TOL, (name, step, "f")
+        if pre + "w_FHydro" in d.files and len(d[pre + "w_FHydro"]):
+            fh, _ = g.walls()
+            ref = d[pre + "w_FHydro"]
+            assert np.allclose(fh, ref, rtol=1e-10, atol=1e-14 * max(1.0, np.abs(ref).max())), (fh, ref)
+        if d["spheres"].shape[0]:
+            ge = g.elements()
+            for k, gk in (("x0", "e_x0"), ("x1", "e_x1"), ("FHydro", "e_FHydro"), ("MHydro", "e_MHydro")):
+                ref = d[pre + gk].reshape(-1, 3).T.reshape(-1)
+                assert rel_linf(ge[k], ref) <= 1e-11, (name, step, k, rel_linf(ge[k], ref))
+    g.close()
+
+
+def test_init_matches_reference_fixture():
+    d = load_golden("box_spheres")
+    p = golden_params(d)
+    g = _gpu()(p, d["spheres"], d["objects"])
+    gl = g.lattice()
+    np.testing.assert_array_equal(gl["type"], d["s0_type"])
+    np.testing.assert_array_equal(gl["inside"], d["s0_inside"])
+    act = (d["s0_type"] == 0) | (d["s0_type"] == 3)
+    np.testing.assert_array_equal(gl["solid"][act], d["s0_solid"][act])
+    g.close()
+
+
+def test_dem_matches_reference_fixture():
+    d = load_golden("dem_objects")
+    p = golden_params(d)
+    g = _gpu()(p, d["spheres"], d["objects"])
+    done = 0
+    for step in d["steps"]:
+        if step > done:
+            g.cycle(int(step) - done)
+            done = int(step)
+        pre = f"s{step}_"
+        ge = g.elements()
+        for k, gk, tol in (("x0", "e_x0", 1e-10), ("x1", "e_x1", 1e-8)):
+            ref = d[pre + gk].reshape(-1, 3).T.reshape(-1)
+            assert rel_linf(ge[k], ref) <= tol, (step, k, rel_linf(ge[k], ref))
+        # candidate pair set, normalised to sorted (min,max) pairs, must be identical
+        gp = g.pairs().reshape(-1, 2)
+        rp = np.sort(d[pre + "neighborTable"].reshape(-1, 2), axis=1)
+        rp = rp[np.lexsort((rp[:, 1], rp[:, 0]))]
+        if step > 0:
+            np.testing.assert_array_equal(gp, rp)
+    g.close()
+
+
+def _channel(shape=(64, 32, 32), precision=abi.HB_FP64, collision=abi.HB_BGK, tau=0.8, magic=3 / 16):
+    return abi.make_params(shape, (4, 4, 7, 7, 4, 4), init_visc=(tau - 0.5) / 3.0, lbF=(1e-6, 0, 0),
+                           precision=precision, collision=collision, trt_magic=magic)
+
+
+def test_config1_fp64_vs_oracle_100_steps():
+    p = _channel()
+    g = _gpu()(p)
+    o = OracleSim(p, threads=4)
+    g.cycle(100)
+    o.cycle(100)
+    gl, ol = g.lattice(), o.lattice()
+    act = ol["type"] == 0
+    for k, comps in (("f", 19), ("n", 1), ("u", 3)):
+        e = rel_linf(gl[k].reshape(comps, -1), ol[k].reshape(comps, -1), act)
+        assert e <= FP64_TOL, (k, e)
+
+
+@pytest.mark.parametrize("prec,tol", [(abi.HB_FP32, 1e-5), (abi.HB_FP16S, 5e-2)])
+def test_reduced_precision_error_vs_fp64_oracle(prec, tol):
+    p64 = _channel()
+    p = _channel(precision=prec)
+    g = _gpu()(p)
+    o = OracleSim(p64, threads=4)
+    g.cycle(200)
+    o.cycle(200)
+    gl, ol = g.lattice(), o.lattice()
+    act = ol["type"] == 0
+    du = gl["u"].reshape(3, -1)[:, act] - ol["u"].reshape(3, -1)[:, act]
+    l2 = np.sqrt((du ** 2).sum() / (ol["u"].reshape(3, -1)[:, act] ** 2).sum())
+    assert l2 <= tol, l2
+    dn = np.abs(gl["n"][act] - ol["n"][act]).max()
+    assert dn <= 1e-6 if prec == abi.HB_FP32 else dn <= 1e-3
+
+
+def test_trt_fp64_vs_oracle():
+    p = _channel(shape=(24, 16, 12), collision=abi.HB_TRT, tau=0.7)
+    g = _gpu()(p)
+    o = OracleSim(p)
+    g.cycle(50)
+    o.cycle(50)
+    gl, ol = g.lattice(), o.lattice()
+    act = ol["type"] == 0
+    assert rel_linf(gl["f"].reshape(19, -1), ol["f"].reshape(19, -1), act) <= FP64_TOL
+    assert rel_linf(gl["u"].reshape(3, -1), ol["u"].reshape(3, -1), act) <= FP64_TOL
+
+
+def test_coupled_box_fp64_vs_oracle():
+    rng = np.random.default_rng(3)
+    spheres = []
+    while len(spheres) < 12:
+        r = rng.uniform(2.5, 3.5)
+        c = rng.uniform(2 + r, 30 - r, size=3)
+        if all(np.linalg.norm(c - s[:3]) > r + s[3] + 0.4 for s in spheres):
+            spheres.append(np.r_[c, r])
+    spheres = np.array(spheres)
+    p = abi.make_params((32, 32, 32), (7,) * 6, init_visc=0.1, lbF=(0, 0, -1e-4), multi_step=3,
+                        collision=abi.HB_BGK)
+    g = _gpu()(p, spheres)
+    o = OracleSim(p, spheres, threads=4)
+    for _ in range(4):
+        g.cycle(10)
+        o.cycle(10)
+    gl, ol = g.lattice(), o.lattice()
+    np.testing.assert_array_equal(gl["inside"], ol["inside"])
+    act = (ol["type"] == 0) | (ol["type"] == 3)
+    assert rel_linf(gl["f"].reshape(19, -1), ol["f"].reshape(19, -1), act) <= FP64_TOL
+    ge, oe = g.elements(), o.elements()
+    for k in ("x0", "x1", "FHydro", "MHydro"):
+        assert rel_linf(ge[k], oe[k]) <= 1e-10, (k, rel_linf(ge[k], oe[k]))
