@@ -3,7 +3,8 @@
 //
 // One cycle is the reference's goCycle (hybird.cpp:35-66) minus output:
 //   DEM substeps -> free-surface step -> coupling masks -> collide+stream -> element
-//   hydrodynamic force reduction -> parity flip.
+//   (element forces of the previous step, DEM substeps and coupling masks in one
+//   cooperative kernel) -> free surface -> collide+stream.
 // It is captured once into a CUDA graph and replayed; all device memory is allocated in
 // hb_create/hb_init, nothing per step.
 #include <algorithm>
@@ -145,6 +146,17 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     CK(cudaMemcpy(d.m, m.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(d.I, I.data(), sizeof(double) * 3 * E, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(d.rad, e->radius, sizeof(double) * E, cudaMemcpyHostToDevice));
+    {  // FP32 copy read by the reduced-precision lattice kernel
+        std::vector<float> pf(9 * (size_t)E);
+        for (int k = 0; k < E; ++k)
+            for (int q = 0; q < 3; ++q) {
+                pf[(size_t)q * E + k] = (float)e->x0[q * E + k];
+                pf[(size_t)(3 + q) * E + k] = (float)x1[q * E + k];
+                pf[(size_t)(6 + q) * E + k] = (float)w0[q * E + k];
+            }
+        if ((rc = dalloc(&d.pf, 9 * (size_t)E))) return rc;
+        CK(cudaMemcpy(d.pf, pf.data(), sizeof(float) * pf.size(), cudaMemcpyHostToDevice));
+    }
     // neighbour-list parameters (DEM.cpp:1270-1312)
     const double demSize[3] = {(double)c->X, (double)c->Y, (double)c->Z};
     for (int k = 0; k < 3; ++k) {
@@ -199,7 +211,7 @@ int hb_create(const hb_params* params, hb_ctx** out) {
     c->sz = params->precision == HB_FP64 ? 8 : (params->precision == HB_FP32 ? 4 : 2);
     const size_t tsz = params->precision == HB_FP64 ? 8 : 4;
     if ((rc = dalloc(&c->ntype, N)) || (rc = dalloc(&c->solid, N)) || (rc = dalloc((uint8_t**)&c->fA, 19 * N * c->sz)) ||
-        (rc = dalloc((uint8_t**)&c->fB, 19 * N * c->sz)) || (rc = dalloc(&c->parity, 1)) || (rc = dalloc(&c->mode, 1)) ||
+        (rc = dalloc((uint8_t**)&c->fB, 19 * N * c->sz)) || (rc = dalloc(&c->mode, 1)) ||
         (rc = dalloc(&c->rho, N)) || (rc = dalloc(&c->u, 3 * N)) || (rc = dalloc(&c->hf, 3 * N)) ||
         (rc = dalloc(&c->mass, N)) || (rc = dalloc(&c->status, STATUS_WORDS)) ||
         (rc = dalloc(&c->wall_force, MAX_WALLS * 3 + 1))) {
@@ -208,7 +220,6 @@ int hb_create(const hb_params* params, hb_ctx** out) {
     }
     if (params->non_newtonian || params->turbulence)
         if ((rc = dalloc((uint8_t**)&c->visc, N * tsz))) { hb_destroy(c); return rc; }
-    CK(cudaMemset(c->parity, 0, sizeof(int)));
     CK(cudaMemset(c->mode, 0, sizeof(int)));
     CK(cudaMemset(c->status, 0, sizeof(int) * STATUS_WORDS));
     CK(cudaMemset(c->wall_force, 0, sizeof(double) * (MAX_WALLS * 3 + 1)));
@@ -220,11 +231,13 @@ int hb_create(const hb_params* params, hb_ctx** out) {
 
 int hb_destroy(hb_ctx* c) {
     if (!c) return HB_OK;
-    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    for (int k = 0; k < 2; ++k)
+        if (c->gexec[k]) cudaGraphExecDestroy(c->gexec[k]);
     if (c->graph) cudaGraphDestroy(c->graph);
-    void* ptrs[] = {c->ntype, c->solid, c->fA, c->fB, c->parity, c->mode, c->rho, c->u, c->hf, c->mass,
+    if (c->graph2) cudaGraphDestroy(c->graph2);
+    void* ptrs[] = {c->ntype, c->solid, c->fA, c->fB, c->mode, c->rho, c->u, c->hf, c->mass,
                     c->visc, c->dv, c->claim, c->status, c->wall_part, c->wall_force, c->fs_force, c->if_list,
-                    c->if_count, c->fs_scal, c->fs_flag, c->fs_parent, c->fs_part, c->lb_force,
+                    c->if_count, c->fs_scal, c->fs_flag, c->fs_parent, c->fs_part, c->lb_force, c->lb_force_f, c->d.pf,
                     c->d.base, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r};
@@ -258,13 +271,21 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     if (!c->lb_force) {
         if ((rc = dalloc(&c->lb_force, 3))) return rc;
     }
+    if (!c->lb_force_f) {
+        if ((rc = dalloc(&c->lb_force_f, 3))) return rc;
+    }
+    {
+        const float ff[3] = {c->P.force_field ? (float)c->P.lbF[0] : 0.f, c->P.force_field ? (float)c->P.lbF[1] : 0.f,
+                             c->P.force_field ? (float)c->P.lbF[2] : 0.f};
+        CK(cudaMemcpy(c->lb_force_f, ff, sizeof(ff), cudaMemcpyHostToDevice));
+    }
     CK(cudaMemcpy(c->fs_force, c->P.lbF, sizeof(double) * 3, cudaMemcpyHostToDevice));
     {
         const double z[3] = {0.0, 0.0, 0.0};
         CK(cudaMemcpy(c->lb_force, c->P.force_field ? c->P.lbF : z, sizeof(double) * 3, cudaMemcpyHostToDevice));
     }
-    CK(cudaMemset(c->parity, 0, sizeof(int)));
-    c->h_parity = 0;
+    c->cur = 0;
+    c->reduce_pending = false;
     c->steps = 0;
     if (launch_init_lattice(c, e && c->d.E ? c->d.x[0] : nullptr, c->d.E ? c->d.rad : nullptr, c->d.E,
                             c->d.obj_x0, c->d.obj_r, c->d.O))
@@ -302,28 +323,35 @@ int hb_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside, con
 
 }  // extern "C"
 
-// one whole cycle on the context stream
-static void enqueue_cycle(hb_ctx* c) {
+// one whole cycle on the context stream, starting from population buffer `cur`
+static int enqueue_cycle(hb_ctx* c, int cur) {
     const bool dem = c->P.dem_solve && c->d.E > 0;
-    if (dem)
-        for (int s = 0; s < c->d.multi; ++s) launch_dem_substep(c);
-    if (!c->P.lb_solve) return;
-    if (c->P.free_surface) launch_fs_step(c);
-    if (dem) launch_couple_masks(c);
-    launch_lb_step(c);
-    if (c->has_dynwall) launch_lb_wallforce(c);
-    if (dem) launch_couple_reduce(c);
-    launch_flip(c);
+    // R (element forces of the previous lattice step) + DEM substeps + coupling masks
+    if (dem && launch_cycle_coop(c, 1, 1, c->P.lb_solve ? 1 : 0)) return -1;
+    if (!c->P.lb_solve) return 0;
+    if (c->P.free_surface) launch_fs_step(c, cur);
+    launch_lb_step(c, cur);
+    if (c->has_dynwall) launch_lb_wallforce(c, cur);
     if (!c->P.force_field) cudaMemsetAsync(c->fs_force, 0, sizeof(double) * 3, c->stream);
+    return 0;
 }
 
 static int build_graph(hb_ctx* c) {
-    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+    for (int k = 0; k < 2; ++k) {
+        if (c->gexec[k]) { cudaGraphExecDestroy(c->gexec[k]); c->gexec[k] = nullptr; }
+    }
     if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
-    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_cycle(c);
-    CK(cudaStreamEndCapture(c->stream, &c->graph));
-    CK(cudaGraphInstantiate(&c->gexec, c->graph, 0));
+    if (c->graph2) { cudaGraphDestroy(c->graph2); c->graph2 = nullptr; }
+    for (int k = 0; k < 2; ++k) {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_cycle(c, k);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (rc || e != cudaSuccess)
+            return seterr(HB_ERR_CUDA, "cycle capture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : cudaGetLastError()));
+        CK(cudaGraphInstantiate(&c->gexec[k], g, 0));
+        if (k == 0) c->graph = g; else c->graph2 = g;
+    }
     size_t nn = 0;
     CK(cudaGraphGetNodes(c->graph, nullptr, &nn));
     std::vector<cudaGraphNode_t> nodes(nn);
@@ -342,8 +370,11 @@ static int run_cycles(hb_ctx* c, int n, bool last_mirror) {
     for (int s = 0; s < n; ++s) {
         const int m = (last_mirror && s == n - 1) ? 1 : 0;
         CK(cudaMemsetAsync(c->mode, m, sizeof(int), c->stream));
-        CK(cudaGraphLaunch(c->gexec, c->stream));
-        if (c->P.lb_solve) c->h_parity ^= 1;
+        CK(cudaGraphLaunch(c->gexec[c->cur], c->stream));
+        if (c->P.lb_solve) {
+            c->cur ^= 1;
+            c->reduce_pending = true;
+        }
         ++c->steps;
     }
     return HB_OK;
@@ -353,22 +384,26 @@ extern "C" {
 
 int hb_dem_step(hb_ctx* c) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
-    if (c->P.dem_solve && c->d.E > 0)
-        for (int s = 0; s < c->d.multi; ++s) launch_dem_substep(c);
+    if (c->P.dem_solve && c->d.E > 0) {
+        if (launch_cycle_coop(c, 1, 1, 0)) return seterr(HB_ERR_CUDA, "DEM launch: %s", cudaGetErrorString(cudaGetLastError()));
+        c->reduce_pending = false;
+    }
     CK(cudaGetLastError());
     return HB_OK;
 }
 
 int hb_fs_step(hb_ctx* c) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
-    if (c->P.free_surface) launch_fs_step(c);
+    if (c->P.free_surface) launch_fs_step(c, c->cur);
     CK(cudaGetLastError());
     return HB_OK;
 }
 
 int hb_coupling_step(hb_ctx* c) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
-    if (c->P.dem_solve && c->d.E > 0) launch_couple_masks(c);
+    if (c->P.dem_solve && c->d.E > 0) {
+        if (launch_cycle_coop(c, 0, 0, 1)) return seterr(HB_ERR_CUDA, "coupling launch: %s", cudaGetErrorString(cudaGetLastError()));
+    }
     CK(cudaGetLastError());
     return HB_OK;
 }
@@ -376,12 +411,11 @@ int hb_coupling_step(hb_ctx* c) {
 int hb_lb_step(hb_ctx* c) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
     CK(cudaMemsetAsync(c->mode, 1, sizeof(int), c->stream));
-    launch_lb_step(c);
-    if (c->has_dynwall) launch_lb_wallforce(c);
-    if (c->P.dem_solve && c->d.E > 0) launch_couple_reduce(c);
-    launch_flip(c);
+    launch_lb_step(c, c->cur);
+    if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
     if (!c->P.force_field) CK(cudaMemsetAsync(c->fs_force, 0, sizeof(double) * 3, c->stream));
-    c->h_parity ^= 1;
+    c->cur ^= 1;
+    c->reduce_pending = true;
     ++c->steps;
     CK(cudaGetLastError());
     return HB_OK;
@@ -399,7 +433,13 @@ int hb_cycle(hb_ctx* c, int32_t nsteps) {
 int hb_set_body_force(hb_ctx* c, const double* force) {
     if (!c || !force || !c->initialized) return seterr(HB_ERR_ARG, "null argument or not initialised");
     for (int k = 0; k < 3; ++k) c->P.lbF[k] = force[k];
-    if (c->P.force_field) CK(cudaMemcpyAsync(c->lb_force, force, sizeof(double) * 3, cudaMemcpyHostToDevice, c->stream));
+    if (c->P.force_field) {
+        c->h_force_f[0] = (float)force[0];
+        c->h_force_f[1] = (float)force[1];
+        c->h_force_f[2] = (float)force[2];
+        CK(cudaMemcpyAsync(c->lb_force, force, sizeof(double) * 3, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->lb_force_f, c->h_force_f, sizeof(float) * 3, cudaMemcpyHostToDevice, c->stream));
+    }
     return HB_OK;
 }
 
@@ -431,7 +471,7 @@ int hb_download_lattice(hb_ctx* c, uint8_t* type, uint8_t* inside, uint32_t* sol
         double* df = nullptr;
         int rc = dalloc(&df, 19 * N);
         if (rc) return rc;
-        launch_download_lattice(c, df, c->h_parity);
+        launch_download_lattice(c, df, c->cur);
         CK(cudaStreamSynchronize(c->stream));
         CK(cudaMemcpy(f, df, sizeof(double) * 19 * N, cudaMemcpyDeviceToHost));
         cudaFree(df);
@@ -460,6 +500,10 @@ int hb_download_elements(hb_ctx* c, double* x0, double* x1, double* w, double* q
     CK(cudaStreamSynchronize(c->stream));
     const int E = c->d.E;
     if (E == 0) return HB_OK;
+    if (c->reduce_pending) {  // the element forces of the last lattice step (LB.cpp:1851-1919)
+        launch_couple_reduce(c);
+        CK(cudaStreamSynchronize(c->stream));
+    }
     struct { double* dst; double* src; int comps; } items[] = {
         {x0, c->d.x[0], 3}, {x1, c->d.x[1], 3}, {w, c->d.wG, 3}, {q0, c->d.q[0], 4}, {fhydro, c->d.FH, 3},
         {mhydro, c->d.MH, 3}, {fparticle, c->d.FP, 3}, {fwall, c->d.FW, 3}, {mparticle, c->d.MP, 3},
@@ -551,16 +595,47 @@ int hb_get_status(hb_ctx* c, hb_status* s) {
     return HB_OK;
 }
 
+int hb_profile_phases(hb_ctx* c, int32_t nsteps, double* us, int32_t* nphases) {
+    if (!c || !c->initialized || !us || !nphases) return seterr(HB_ERR_ARG, "null argument or not initialised");
+    if (!(c->P.dem_solve && c->d.E > 0)) { *nphases = 0; return HB_OK; }
+    const int np = 1 + 2 * c->d.multi + 3 + 1;
+    unsigned long long* ts = nullptr;
+    int rc = dalloc(&ts, (size_t)np * nsteps);
+    if (rc) return rc;
+    CK(cudaMemset(ts, 0, sizeof(unsigned long long) * np * nsteps));
+    for (int s = 0; s < nsteps; ++s) {
+        if (launch_cycle_coop(c, 1, 1, 1, ts + (size_t)s * np)) { cudaFree(ts); return seterr(HB_ERR_CUDA, "cycle launch failed"); }
+        if (c->P.free_surface) launch_fs_step(c, c->cur);
+        launch_lb_step(c, c->cur);
+        if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
+        c->cur ^= 1;
+        c->reduce_pending = true;
+        ++c->steps;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<unsigned long long> h((size_t)np * nsteps);
+    CK(cudaMemcpy(h.data(), ts, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost));
+    cudaFree(ts);
+    const int nint = np - 1;  // intervals between the recorded barriers
+    for (int k = 0; k < nint; ++k) {
+        double acc = 0.0;
+        for (int s = 0; s < nsteps; ++s) acc += (double)(h[(size_t)s * np + k + 1] - h[(size_t)s * np + k]) * 1e-3;
+        us[k] = acc / nsteps;
+    }
+    *nphases = nint;
+    return HB_OK;
+}
+
 int hb_time_cycles(hb_ctx* c, int32_t nsteps, float* ms_total, float* ms_lb_kernel, int32_t* kernels_per_cycle) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
     if (nsteps <= 0) return seterr(HB_ERR_ARG, "nsteps <= 0");
     CK(cudaStreamSynchronize(c->stream));
-    // whole cycles replayed from the graph
+    // whole cycles replayed from the graphs
     CK(cudaMemsetAsync(c->mode, 0, sizeof(int), c->stream));
     CK(cudaEventRecord(c->ev0, c->stream));
     for (int s = 0; s < nsteps; ++s) {
-        CK(cudaGraphLaunch(c->gexec, c->stream));
-        if (c->P.lb_solve) c->h_parity ^= 1;
+        CK(cudaGraphLaunch(c->gexec[c->cur], c->stream));
+        if (c->P.lb_solve) { c->cur ^= 1; c->reduce_pending = true; }
         ++c->steps;
     }
     CK(cudaEventRecord(c->ev1, c->stream));
@@ -569,24 +644,21 @@ int hb_time_cycles(hb_ctx* c, int32_t nsteps, float* ms_total, float* ms_lb_kern
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     if (ms_total) *ms_total = ms;
     if (kernels_per_cycle) *kernels_per_cycle = c->kernels_per_cycle;
-    // the stream-collide kernel alone, bracketed by events on its own stream, inside the
-    // same cycles launched one kernel at a time
+    // the collide+stream kernel alone, bracketed by events on its own stream inside the
+    // same cycles launched kernel by kernel
     if (ms_lb_kernel && c->P.lb_solve) {
         std::vector<cudaEvent_t> ev(2 * nsteps);
         for (auto& e : ev) CK(cudaEventCreate(&e));
         const bool dem = c->P.dem_solve && c->d.E > 0;
         for (int s = 0; s < nsteps; ++s) {
-            if (dem)
-                for (int k = 0; k < c->d.multi; ++k) launch_dem_substep(c);
-            if (c->P.free_surface) launch_fs_step(c);
-            if (dem) launch_couple_masks(c);
+            if (dem && launch_cycle_coop(c, 1, 1, 1)) return seterr(HB_ERR_CUDA, "cycle launch failed");
+            if (c->P.free_surface) launch_fs_step(c, c->cur);
             CK(cudaEventRecord(ev[2 * s], c->stream));
-            launch_lb_step(c);
+            launch_lb_step(c, c->cur);
             CK(cudaEventRecord(ev[2 * s + 1], c->stream));
-            if (c->has_dynwall) launch_lb_wallforce(c);
-            if (dem) launch_couple_reduce(c);
-            launch_flip(c);
-            c->h_parity ^= 1;
+            if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
+            c->cur ^= 1;
+            c->reduce_pending = true;
             ++c->steps;
         }
         CK(cudaStreamSynchronize(c->stream));

@@ -20,6 +20,7 @@
 #define HB_TYPE_MASK 0x0F
 #define HB_INSIDE 0x10
 #define HB_BULK 0x20
+#define HB_PWRAP 0x40   // some link of this node crosses a periodic face
 
 namespace hb {
 
@@ -52,6 +53,19 @@ __device__ __forceinline__ bool is_active(uint8_t t) {
     return c == HB_T_FLUID || c == HB_T_INTERFACE;
 }
 
+// ---- population load/store cache policy ----------------------------------------------
+// HB_CACHE_HINT 1: streaming (evict-first) loads and stores; 0: default caching.
+#ifndef HB_CACHE_HINT
+#define HB_CACHE_HINT 0
+#endif
+#if HB_CACHE_HINT
+#define HB_LD(p) __ldcs(p)
+#define HB_ST(p, v) __stcs(p, v)
+#else
+#define HB_LD(p) (*(p))
+#define HB_ST(p, v) (*(p) = (v))
+#endif
+
 // ---- storage precision policies ------------------------------------------------------
 // FP64: full populations in double, compute in double (the reference's arithmetic).
 // FP32: deviations g = f - w*rho0 in float, compute in float.
@@ -60,16 +74,16 @@ struct PolF64 {
     using S = double;
     using T = double;
     static constexpr bool DEV = false;
-    __device__ static __forceinline__ T load(const S* p) { return __ldcs(p); }
-    __device__ static __forceinline__ void store(S* p, T v) { __stcs(p, v); }
+    __device__ static __forceinline__ T load(const S* p) { return HB_LD(p); }
+    __device__ static __forceinline__ void store(S* p, T v) { HB_ST(p, v); }
     __device__ static __forceinline__ S enc(T v) { return v; }
 };
 struct PolF32 {
     using S = float;
     using T = float;
     static constexpr bool DEV = true;
-    __device__ static __forceinline__ T load(const S* p) { return __ldcs(p); }
-    __device__ static __forceinline__ void store(S* p, T v) { __stcs(p, v); }
+    __device__ static __forceinline__ T load(const S* p) { return HB_LD(p); }
+    __device__ static __forceinline__ void store(S* p, T v) { HB_ST(p, v); }
     __device__ static __forceinline__ S enc(T v) { return v; }
 };
 struct PolF16 {
@@ -79,11 +93,11 @@ struct PolF16 {
     static constexpr float SCALE = 32768.0f;
     static constexpr float INV = 1.0f / 32768.0f;
     __device__ static __forceinline__ T load(const S* p) {
-        const unsigned short b = __ldcs(reinterpret_cast<const unsigned short*>(p));
+        const unsigned short b = HB_LD(reinterpret_cast<const unsigned short*>(p));
         return __half2float(__ushort_as_half(b)) * INV;
     }
     __device__ static __forceinline__ void store(S* p, T v) {
-        __stcs(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(v * SCALE)));
+        HB_ST(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(v * SCALE)));
     }
 };
 
@@ -94,6 +108,7 @@ struct Particles {          // DEM elements as the coupling sees them (FP64)
     const double* x1;       // [3*E] velocity
     const double* w;        // [3*E] wGlobal
     const double* radius;   // [E]
+    const float* pf;        // [9*E] FP32 copy: centre, velocity, wGlobal (component-major)
 };
 
 struct LBArgs {
@@ -102,10 +117,9 @@ struct LBArgs {
     int per[6];             // face periodic flags (boundary code 4), x-,x+,y-,y+,z-,z+
     uint8_t* ntype;
     uint32_t* solid;
-    void* fA;
-    void* fB;
-    const int* parity;      // device step parity: 0 reads fA writes fB, 1 the reverse
-    const int* mode;        // bit0: write all node macros (downloads)
+    const void* fin;        // populations after the previous streaming (read)
+    void* fout;             // populations after this step's streaming (written)
+    const int* mode;       // bit0: write all node macros (downloads)
     double* rho;
     double* u;              // [3N]
     double* hf;             // [3N]
@@ -113,6 +127,9 @@ struct LBArgs {
     void* visc;             // T[N] when viscosity is persistent
     void* dv;               // T[3N] direct-forcing term of inside nodes
     const double* F;        // device body force [3] (zero when forceFieldSolve = 0)
+    const float* Ff;        // the same force in FP32 for the reduced-precision kernels
+    int ne[Q];              // index offset of link j for nodes whose links do not wrap
+    float init_visc_f, trt_magic_f, plastic_visc_f, yield_stress_f, turb_const_f;
     double init_visc;
     int collision;
     double trt_magic;
@@ -127,5 +144,7 @@ struct LBArgs {
 };
 
 inline int ceil_div(long long a, int b) { return (int)((a + b - 1) / b); }
+
+__device__ __forceinline__ void flag_status(int* status, int word) { atomicOr(status + word, 1); }
 
 }  // namespace hb

@@ -16,6 +16,7 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     double *wG, *wL, *wpG, *wpL;
     double *FH, *MH, *FP, *FW, *MP, *MW;
     double *fvol, *m, *I, *rad;
+    float* pf = nullptr;        // [9E] FP32 centre/velocity/wGlobal for the FP32 lattice kernel
     // neighbour structures
     int* cell_of = nullptr;     // [E]
     int* cell_cnt = nullptr;    // [nc]
@@ -61,9 +62,8 @@ struct hb_ctx {
     uint32_t* solid = nullptr;
     void* fA = nullptr;
     void* fB = nullptr;
-    int* parity = nullptr;      // device
+    int cur = 0;                // population buffer holding the current state (0: fA, 1: fB)
     int* mode = nullptr;        // device
-    int h_parity = 0;
     double* rho = nullptr;
     double* u = nullptr;
     double* hf = nullptr;
@@ -80,6 +80,8 @@ struct hb_ctx {
     long long steps = 0;
     double* fs_force = nullptr; // device lbF seen by the free-surface init of new cells
     double* lb_force = nullptr; // device lbF seen by the collision (zero without forceField)
+    float* lb_force_f = nullptr;    // FP32 copy of lb_force
+    float h_force_f[3] = {0.f, 0.f, 0.f};  // host staging of the FP32 force (kept alive for async copies)
     // free surface
     uint32_t* if_list = nullptr;    // compacted interface list
     int* if_count = nullptr;
@@ -92,7 +94,9 @@ struct hb_ctx {
     hb_dem_dev d;
     // graph
     cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // cycle graphs starting from fA / fB
+    cudaGraph_t graph2 = nullptr;
+    bool reduce_pending = false; // element forces lag the last lattice step
     int kernels_per_cycle = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
@@ -102,18 +106,17 @@ namespace hb {
 int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int E,
                         const double* ob_x0, const double* ob_r, int O);
 void launch_refresh_bulk(hb_ctx* c);
-void launch_lb_step(hb_ctx* c);
-void launch_lb_wallforce(hb_ctx* c);
-void launch_flip(hb_ctx* c);
+void launch_lb_step(hb_ctx* c, int cur);
+void launch_lb_step_dev(hb_ctx* c, const LBArgs& a);
+void launch_lb_wallforce(hb_ctx* c, int cur);
 int launch_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside,
                           const uint32_t* solid, const double* f, const double* n, const double* u,
                           const double* mass, const double* visc);
 int launch_download_lattice(hb_ctx* c, double* f_dev, int which_parity);
-void launch_dem_substep(hb_ctx* c);
+int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_couple, unsigned long long* ts = nullptr);
 void launch_dem_first_predict(hb_ctx* c);
-void launch_couple_masks(hb_ctx* c);
 void launch_couple_reduce(hb_ctx* c);
-void launch_fs_step(hb_ctx* c);
+void launch_fs_step(hb_ctx* c, int cur);
 int fs_init(hb_ctx* c);
 int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o);
 }  // namespace hb

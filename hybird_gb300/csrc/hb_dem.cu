@@ -1,21 +1,27 @@
-// hb_dem.cu -- DEM substep kernels (FP64) and LB-DEM coupling kernels.
+// hb_dem.cu -- DEM (FP64) and LB-DEM coupling: one cooperative kernel per cycle.
 //
 // DEM::discreteElementStep (DEM.cpp:331-376) runs multiStep substeps of
 //   [neighbour rebuild if maxDisp > 0.25 nebrRange] predict -> forces -> correct.
-// Here one substep is: k_nl_cells + k_nl_build (both return at once unless the device
-// rebuild flag is set), k_dem_forces, k_dem_correct.  The corrector also updates the
-// displacement trigger (a deterministic max over elements) and runs the NEXT substep's
-// predictor, which depends only on the element's own corrected state (elmt.cpp:139-177).
+// Here every substep is "forces | correct + the NEXT substep's predictor" (the predictor
+// depends only on the element's own corrected state, elmt.cpp:139-177), with the
+// rebuild (cell sort in one block, candidate lists per particle) only when the device
+// displacement trigger fired.  The element hydrodynamic-force reduction of the previous
+// lattice step runs first and the coupling masks (LB.cpp:1921-2033) last, all in one
+// cooperative launch separated by grid barriers: two kernels per cycle in total (this
+// one and the lattice kernel) instead of one per phase.
 //
 // Contacts: every particle owns its candidate list (both directions).  A pair is always
 // evaluated with I = min index, J = max index, so both owners compute bit-identical
 // pair forces; each sums its own side in list order.  No floating-point atomics.
 //
-// Coupling (LB.cpp:1851-2033): one CTA per particle sweeps the particle's bounding box.
+// Coupling: one CTA per particle (grid-stride) sweeps the particle's bounding box.
+#include <cooperative_groups.h>
 #include <cstdio>
 
 #include "hb_common.cuh"
 #include "hb_ctx.h"
+
+namespace cg = cooperative_groups;
 
 namespace hb {
 
@@ -30,6 +36,7 @@ struct DemArgs {
     double *wG, *wL, *wpG, *wpL;
     double *FH, *MH, *FP, *FW, *MP, *MW;
     double *fvol, *m, *I, *rad;
+    float* pf;
     int *cell_of, *cell_cnt, *cell_start, *cell_fill, *cell_items;
     int *nbr, *nbr_cnt, *wall_of, *obj, *obj_cnt;
     double* scal;
@@ -103,8 +110,7 @@ __device__ double tangential_contact(const DemArgs& a, double vt, double fn, dou
 
 // single CTA: cell of every particle (linearizePosition, vector.cpp:147-149), counting
 // sort into cells, then ascending order inside each cell
-__global__ void __launch_bounds__(1024) k_nl_cells(DemArgs a) {
-    if (a.scal[1] == 0.0) return;
+__device__ void nl_cells_block(const DemArgs& a) {
     const int E = a.E, nc = a.ncells;
     for (int c = threadIdx.x; c < nc; c += blockDim.x) { a.cell_cnt[c] = 0; a.cell_fill[c] = 0; }
     __syncthreads();
@@ -142,10 +148,7 @@ __global__ void __launch_bounds__(1024) k_nl_cells(DemArgs a) {
 
 // candidate list of every particle: all others within nebrRange in the 27 adjacent
 // cells; first wall within range (DEM.cpp:1502-1511); objects within range
-__global__ void k_nl_build(DemArgs a) {
-    if (a.scal[1] == 0.0) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.E) return;
+__device__ void nl_build_one(const DemArgs& a, int i) {
     const int E = a.E;
     const V xi = ld3(a.x0, E, i);
     const double r2 = a.nebrRange * a.nebrRange;
@@ -192,11 +195,9 @@ __global__ void k_nl_build(DemArgs a) {
 }
 
 // ---- forces (DEM.cpp:1114-1182, 1801-2136) --------------------------------------------
-__global__ void k_dem_forces(DemArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ void forces_one(const DemArgs& a, int i, int& ncont) {
     const int E = a.E;
-    int ncont = 0;
-    if (i < E) {
+    {
         const V xpi = ld3(a.xp0, E, i);
         V FP{0, 0, 0}, MP{0, 0, 0}, FW{0, 0, 0}, MW{0, 0, 0};
         const int cnt = a.nbr_cnt[i];
@@ -308,12 +309,6 @@ __global__ void k_dem_forces(DemArgs a) {
                      (mBf.z + (Iv.x - Iv.y) * wl.x * wl.y) / Iv.z};
         st3(a.w1, E, i, project(waBf, qp0));
     }
-    // overlapping-pair counter: integer atomics, deterministic
-    for (int off = 16; off > 0; off >>= 1) ncont += __shfl_down_sync(0xffffffffu, ncont, off);
-    if ((threadIdx.x & 31) == 0 && ncont) {
-        atomicAdd(a.contacts, ncont);
-        atomicAdd(a.total_contacts, (unsigned long long)ncont);
-    }
 }
 
 __device__ void predict_one(const DemArgs& a, int i) {  // elmt.cpp:139-177
@@ -382,11 +377,10 @@ __device__ void trigger_update(const DemArgs& a, double v2) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_dem_correct(DemArgs a) {  // elmt.cpp:179-254
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ double correct_one(const DemArgs& a, int i) {  // elmt.cpp:179-254
     const int E = a.E;
     double v2 = 0.0;
-    if (i < E) {
+    {
         const double dt = a.dt;
         const double c[5] = {dt, dt * dt / 2.0, dt * dt * dt / 6.0, dt * dt * dt * dt / 24.0, dt * dt * dt * dt * dt / 120.0};
         const double g1[6] = {95.0 / 288.0, 1.0, 25.0 / 24.0, 35.0 / 72.0, 5.0 / 48.0, 1.0 / 120.0};
@@ -426,9 +420,11 @@ __global__ void __launch_bounds__(256) k_dem_correct(DemArgs a) {  // elmt.cpp:1
         st3(a.wG, E, i, w0);
         st3(a.wL, E, i, project(w0, qadj(q0)));
         v2 = nrm2(x1);
+        a.pf[i] = (float)x0.x; a.pf[E + i] = (float)x0.y; a.pf[2 * E + i] = (float)x0.z;
+        a.pf[3 * E + i] = (float)x1.x; a.pf[4 * E + i] = (float)x1.y; a.pf[5 * E + i] = (float)x1.z;
+        a.pf[6 * E + i] = (float)w0.x; a.pf[7 * E + i] = (float)w0.y; a.pf[8 * E + i] = (float)w0.z;
     }
-    trigger_update(a, v2);
-    if (i < E) predict_one(a, i);  // next substep's predictor
+    return v2;
 }
 
 // first substep after init: trigger from the initial velocities, then predict
@@ -475,35 +471,53 @@ __device__ __forceinline__ Box pbox(const CoupleArgs& a, int p, int margin) {
     b.nz = max(0, z1 - b.z0 + 1);
     return b;
 }
-__device__ __forceinline__ bool in_sphere(const CoupleArgs& a, int p, int x, int y, int z) {
+// insideSphere (vector.cpp:153-158) is decided in FP64 with the reference's expression;
+// an FP32 screen settles the nodes far from the surface, because the FP64 pipe of this
+// part is narrow (relative screen margin 1e-3, FP32 error below 1e-5 for boxes <= 256)
+struct Sph {
+    double cx, cy, cz, r2;
+    float fx, fy, fz, r2f;
+};
+__device__ __forceinline__ Sph load_sph(const CoupleArgs& a, int p) {
     const int E = a.E;
-    const double dx = x - a.x0[p], dy = y - a.x0[E + p], dz = z - a.x0[2 * E + p];
-    return dx * dx + dy * dy + dz * dz < a.rad[p] * a.rad[p];  // insideSphere, vector.cpp:153-158
+    Sph s;
+    s.cx = a.x0[p]; s.cy = a.x0[E + p]; s.cz = a.x0[2 * E + p];
+    s.r2 = a.rad[p] * a.rad[p];
+    s.fx = (float)s.cx; s.fy = (float)s.cy; s.fz = (float)s.cz; s.r2f = (float)s.r2;
+    return s;
+}
+__device__ __forceinline__ bool in_sph(const Sph& s, int x, int y, int z) {
+    const float dxf = float(x) - s.fx, dyf = float(y) - s.fy, dzf = float(z) - s.fz;
+    const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
+    if (d2f < 0.999f * s.r2f) return true;
+    if (d2f > 1.001f * s.r2f) return false;
+    const double dx = x - s.cx, dy = y - s.cy, dz = z - s.cz;
+    return dx * dx + dy * dy + dz * dz < s.r2;
 }
 
 // findNewActive (LB.cpp:1921-1967): uncovered nodes leave the particle
-__global__ void k_couple_pop(CoupleArgs a) {
-    const int p = blockIdx.x;
+__device__ void pop_block(const CoupleArgs& a, int p) {
     const Box b = pbox(a, p, 2);
+    const Sph s = load_sph(a, p);
     for (int k = threadIdx.x; k < b.nx * b.ny * b.nz; k += blockDim.x) {
         const int x = b.x0 + k % b.nx, y = b.y0 + (k / b.nx) % b.ny, z = b.z0 + k / (b.nx * b.ny);
         const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
         const uint8_t t = a.ntype[i];
-        if ((t & HB_INSIDE) && a.solid[i] == (uint32_t)p && !in_sphere(a, p, x, y, z)) a.ntype[i] = t & ~HB_INSIDE;
+        if ((t & HB_INSIDE) && a.solid[i] == (uint32_t)p && !in_sph(s, x, y, z)) a.ntype[i] = t & ~HB_INSIDE;
     }
 }
 
 // findNewSolid (LB.cpp:1969-2033): a node covered by particle p and 6-linked from a
 // node of p becomes a particle node; the source node with the lowest index wins, which
 // is the reference's first-in-particleNodes-order rule (the list is sorted there)
-__global__ void k_couple_claim(CoupleArgs a) {
-    const int p = blockIdx.x;
+__device__ void claim_block(const CoupleArgs& a, int p) {
     const Box b = pbox(a, p, 1);
+    const Sph s = load_sph(a, p);
     for (int k = threadIdx.x; k < b.nx * b.ny * b.nz; k += blockDim.x) {
         const int x = b.x0 + k % b.nx, y = b.y0 + (k / b.nx) % b.ny, z = b.z0 + k / (b.nx * b.ny);
         const long long l = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
         if (a.ntype[l] & HB_INSIDE) continue;
-        if (!in_sphere(a, p, x, y, z)) continue;
+        if (!in_sph(s, x, y, z)) continue;
         unsigned long long best = ~0ull;
         for (int kk = 1; kk <= 6; ++kk) {  // source m with link d[m][kk] == l
             int mx = x - cx(kk), my = y - cy(kk), mz = z - cz(kk);
@@ -530,8 +544,7 @@ __global__ void k_couple_claim(CoupleArgs a) {
     }
 }
 
-__global__ void k_couple_commit(CoupleArgs a) {
-    const int p = blockIdx.x;
+__device__ void commit_block(const CoupleArgs& a, int p) {
     const Box b = pbox(a, p, 1);
     for (int k = threadIdx.x; k < b.nx * b.ny * b.nz; k += blockDim.x) {
         const int x = b.x0 + k % b.nx, y = b.y0 + (k / b.nx) % b.ny, z = b.z0 + k / (b.nx * b.ny);
@@ -546,9 +559,7 @@ __global__ void k_couple_commit(CoupleArgs a) {
 
 // element hydrodynamic force, torque and entrained fluid (LB.cpp:1853-1918): fixed
 // thread-to-node assignment and a fixed-order tree, so the sum is reproducible
-__global__ void __launch_bounds__(256) k_couple_reduce(CoupleArgs a) {
-    __shared__ double sh[7][256];
-    const int p = blockIdx.x;
+__device__ void reduce_block(const CoupleArgs& a, int p, double (*sh)[256]) {
     const int E = a.E;
     const Box b = pbox(a, p, 1);
     const double px = a.x0[p], py = a.x0[E + p], pz = a.x0[2 * E + p];
@@ -573,6 +584,7 @@ __global__ void __launch_bounds__(256) k_couple_reduce(CoupleArgs a) {
         acc[5] += rx * dvy - ry * dvx;
         acc[6] += a.free_surface ? a.mass[i] : 1.0;
     }
+    __syncthreads();
     for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] = acc[c];
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
@@ -584,6 +596,108 @@ __global__ void __launch_bounds__(256) k_couple_reduce(CoupleArgs a) {
         a.FH[p] = sh[0][0]; a.FH[E + p] = sh[1][0]; a.FH[2 * E + p] = sh[2][0];
         a.MH[p] = sh[3][0]; a.MH[E + p] = sh[4][0]; a.MH[2 * E + p] = sh[5][0];
         a.fvol[p] = sh[6][0];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_couple_reduce(CoupleArgs a) {
+    __shared__ double sh[7][256];
+    reduce_block(a, blockIdx.x, sh);
+}
+
+// ---- one cooperative kernel per cycle --------------------------------------------------
+// phases, separated by grid-wide barriers (the launch is cooperative, so every block is
+// resident and the barrier cannot stall):
+//   R  hydrodynamic force of every element from the previous lattice step
+//   D  multiStep DEM substeps: [neighbour rebuild] forces | correct + next predict +
+//      displacement trigger
+//   C  coupling masks: pop | claim | commit
+struct CycleArgs {
+    DemArgs d;
+    CoupleArgs c;
+    int do_reduce, do_dem, do_couple, multi;
+    unsigned long long* ts;  // optional phase timestamps (ns), written by block 0 after each barrier
+};
+
+__device__ __forceinline__ void stamp(const CycleArgs& A, int k) {
+    if (A.ts && blockIdx.x == 0 && threadIdx.x == 0) {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        A.ts[k] = t;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_cycle(CycleArgs A) {
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double sh[7][256];
+    const int E = A.d.E;
+    // element loops spread consecutive elements over different blocks, so the FP64 work
+    // (narrow pipe on this part) lands on every SM instead of the first few
+    const int gt = blockIdx.x + gridDim.x * threadIdx.x;
+    const int gs = gridDim.x * blockDim.x;
+    stamp(A, 0);
+    if (A.do_reduce)
+        for (int p = blockIdx.x; p < E; p += gridDim.x) reduce_block(A.c, p, sh);
+    int k = 1;
+    if (A.do_dem) {
+        double maxDisp = A.d.scal[0];
+        bool rebuild = A.d.scal[1] != 0.0;
+        if (blockIdx.x == 0 && threadIdx.x == 0) *A.d.contacts = 0;
+        grid.sync();
+        stamp(A, k++);
+        for (int s = 0; s < A.multi; ++s) {
+            if (rebuild) {
+                if (blockIdx.x == 0) nl_cells_block(A.d);
+                grid.sync();
+                for (int i = gt; i < E; i += gs) nl_build_one(A.d, i);
+            }
+            int ncont = 0;
+            for (int i = gt; i < E; i += gs) forces_one(A.d, i, ncont);
+            if (s == A.multi - 1) {  // overlapping pairs of the last substep (integer atomics)
+                for (int off = 16; off > 0; off >>= 1) ncont += __shfl_down_sync(0xffffffffu, ncont, off);
+                if ((threadIdx.x & 31) == 0 && ncont) {
+                    atomicAdd(A.d.contacts, ncont);
+                    atomicAdd(A.d.total_contacts, (unsigned long long)ncont);
+                }
+            }
+            grid.sync();
+            stamp(A, k++);
+            double v2 = 0.0;
+            for (int i = gt; i < E; i += gs) {
+                v2 = fmax(v2, correct_one(A.d, i));
+                predict_one(A.d, i);  // next substep's predictor (own state only)
+            }
+            sh[0][threadIdx.x] = v2;
+            __syncthreads();
+            for (int q = blockDim.x / 2; q > 0; q >>= 1) {
+                if ((int)threadIdx.x < q) sh[0][threadIdx.x] = fmax(sh[0][threadIdx.x], sh[0][threadIdx.x + q]);
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) A.d.partial[blockIdx.x] = sh[0][0];
+            grid.sync();
+            stamp(A, k++);
+            double mx = 0.0;  // DEM.cpp:1314-1324, 334-347 (every thread folds the same maxima)
+            for (int b = 0; b < (int)gridDim.x; ++b) mx = fmax(mx, ((volatile double*)A.d.partial)[b]);
+            maxDisp += sqrt(mx) * A.d.dt;
+            rebuild = maxDisp > A.d.trigger;
+            if (rebuild) maxDisp = 0.0;
+            __syncthreads();
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            A.d.scal[0] = maxDisp;
+            A.d.scal[1] = rebuild ? 1.0 : 0.0;
+        }
+    }
+    if (A.do_couple) {
+        grid.sync();
+        for (int p = blockIdx.x; p < E; p += gridDim.x) pop_block(A.c, p);
+        grid.sync();
+        stamp(A, k++);
+        for (int p = blockIdx.x; p < E; p += gridDim.x) claim_block(A.c, p);
+        grid.sync();
+        stamp(A, k++);
+        for (int p = blockIdx.x; p < E; p += gridDim.x) commit_block(A.c, p);
+        grid.sync();
+        stamp(A, k++);
     }
 }
 
@@ -602,6 +716,7 @@ static DemArgs dem_args(hb_ctx* c) {
     a.wG = d.wG; a.wL = d.wL; a.wpG = d.wpG; a.wpL = d.wpL;
     a.FH = d.FH; a.MH = d.MH; a.FP = d.FP; a.FW = d.FW; a.MP = d.MP; a.MW = d.MW;
     a.fvol = d.fvol; a.m = d.m; a.I = d.I; a.rad = d.rad;
+    a.pf = d.pf;
     a.cell_of = d.cell_of; a.cell_cnt = d.cell_cnt; a.cell_start = d.cell_start;
     a.cell_fill = d.cell_fill; a.cell_items = d.cell_items;
     a.nbr = d.nbr; a.nbr_cnt = d.nbr_cnt; a.wall_of = d.wall_of; a.obj = d.obj; a.obj_cnt = d.obj_cnt;
@@ -637,17 +752,6 @@ void launch_dem_first_predict(hb_ctx* c) {
     k_dem_first<<<ceil_div(c->d.E, 256), 256, 0, c->stream>>>(a);
 }
 
-void launch_dem_substep(hb_ctx* c) {
-    if (c->d.E == 0) return;
-    DemArgs a = dem_args(c);
-    const int G = ceil_div(c->d.E, 256);
-    k_nl_cells<<<1, 1024, 0, c->stream>>>(a);
-    k_nl_build<<<ceil_div(c->d.E, 128), 128, 0, c->stream>>>(a);
-    cudaMemsetAsync(c->d.contacts, 0, sizeof(int), c->stream);
-    k_dem_forces<<<ceil_div(c->d.E, 128), 128, 0, c->stream>>>(a);
-    k_dem_correct<<<G, 256, 0, c->stream>>>(a);
-}
-
 static CoupleArgs couple_args(hb_ctx* c) {
     CoupleArgs a;
     a.X = c->X; a.Y = c->Y; a.Z = c->Z; a.N = c->N;
@@ -666,12 +770,39 @@ static CoupleArgs couple_args(hb_ctx* c) {
     return a;
 }
 
-void launch_couple_masks(hb_ctx* c) {
-    if (c->d.E == 0) return;
-    CoupleArgs a = couple_args(c);
-    k_couple_pop<<<c->d.E, 128, 0, c->stream>>>(a);
-    k_couple_claim<<<c->d.E, 128, 0, c->stream>>>(a);
-    k_couple_commit<<<c->d.E, 128, 0, c->stream>>>(a);
+int coop_grid(hb_ctx* c) {
+    static int cached = 0;
+    if (cached) return cached;
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cycle, 256, 0);
+    occ = occ < 1 ? 1 : (occ > 4 ? 4 : occ);
+    cached = sms * occ;
+    return cached;
+}
+
+int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_couple, unsigned long long* ts) {
+    if (c->d.E == 0) return 0;
+    CycleArgs A;
+    A.ts = ts;
+    A.d = dem_args(c);
+    A.c = couple_args(c);
+    A.do_reduce = do_reduce;
+    A.do_dem = do_dem;
+    A.do_couple = do_couple;
+    A.multi = c->d.multi;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)coop_grid(c));
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = c->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_cycle, A) == cudaSuccess ? 0 : -1;
 }
 
 void launch_couple_reduce(hb_ctx* c) {

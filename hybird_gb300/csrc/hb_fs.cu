@@ -4,5 +4,5 @@
 
 namespace hb {
 int fs_init(hb_ctx* c) { (void)c; return HB_ERR_UNSUPPORTED; }
-void launch_fs_step(hb_ctx* c) { (void)c; }
+void launch_fs_step(hb_ctx* c, int cur) { (void)c; (void)cur; }
 }  // namespace hb

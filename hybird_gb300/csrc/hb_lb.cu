@@ -12,6 +12,10 @@
 // reference's node::f after streaming, and the free-surface and coupling phases, which
 // the reference runs between streaming and the next collision, see the same data.
 //
+// This file holds the FP64 form, which follows the reference's arithmetic order and is
+// compiled without FMA contraction (as the reference's x86 build computes), plus lattice
+// init and up/download; the FP32 / FP16-storage form is in hb_lb32.cu.
+//
 // Roofline: per lattice update the kernel reads 19 and writes 19 stored populations
 // plus the one-byte node type: 2*19*s + 1 bytes (s = 8, 4, 2 for FP64, FP32, FP16S).
 #include <cstdio>
@@ -21,9 +25,6 @@
 
 namespace hb {
 
-__device__ __forceinline__ void flag_status(int* status, int word) {
-    atomicOr(status + word, 1);
-}
 
 // neighbour of interior node (x,y,z) along direction j with the reference's periodic
 // remap (LB.cpp:437-472): a link crossing a periodic face re-enters on the opposite side
@@ -50,10 +51,9 @@ __global__ void __launch_bounds__(256) k_collide_stream(LBArgs a) {
     const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
     const uint8_t t = a.ntype[i];
     if (!is_active(t)) return;
-    const int par = *a.parity;
     const int mode = *a.mode;
-    const S* fin = reinterpret_cast<const S*>(par ? a.fB : a.fA);
-    S* fout = reinterpret_cast<S*>(par ? a.fA : a.fB);
+    const S* fin = reinterpret_cast<const S*>(a.fin);
+    S* fout = reinterpret_cast<S*>(a.fout);
     const uint8_t code = t & HB_TYPE_MASK;
 
     T f[Q];
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(256) k_wallforce(LBArgs a) {
         const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
         const uint8_t t = a.ntype[i];
         if (is_active(t) && !(t & HB_BULK)) {
-            const S* fcur = reinterpret_cast<const S*>(*a.parity ? a.fA : a.fB);
+            const S* fcur = reinterpret_cast<const S*>(a.fout);
             for (int j = 1; j < Q; ++j) {
                 const long long l = link_index(a, x, y, z, j);
                 if ((a.ntype[l] & HB_TYPE_MASK) != HB_T_DYNWALL) continue;
@@ -295,7 +295,6 @@ __global__ void k_wallforce_final(const double* part, int nb, double* out) {
     out[k] = s;
 }
 
-__global__ void k_flip(int* parity) { *parity ^= 1; }
 
 // ---- initialisation ------------------------------------------------------------------
 
@@ -464,14 +463,14 @@ __global__ void k_init_vars(InitArgs a, LBArgs b, const int* mx, double Fx, doub
     b.hf[i] = 0.0; b.hf[N + i] = 0.0; b.hf[2 * N + i] = 0.0;
     b.mass[i] = mass;
     if (b.visc_model) reinterpret_cast<T*>(b.visc)[i] = node ? T(visc0) : T(0);
-    S* f = reinterpret_cast<S*>(b.fA);
+    S* f = reinterpret_cast<S*>(b.fout);
     const double usq = ux * ux + uy * uy + uz * uz;
     for (int j = 0; j < Q; ++j) {
         const double vu = ux * cx(j) + uy * cy(j) + uz * cz(j);
         double fe = node ? wgt(j) * n * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq) : wgt(j);
         if (P::DEV) fe -= wgt(j);
         P::store(f + (long long)j * N + i, (T)fe);
-        P::store(reinterpret_cast<S*>(b.fB) + (long long)j * N + i, (T)(P::DEV ? 0.0 : wgt(j)));
+        P::store(reinterpret_cast<S*>(const_cast<void*>(b.fin)) + (long long)j * N + i, (T)(P::DEV ? 0.0 : wgt(j)));
     }
 }
 
@@ -481,13 +480,18 @@ __global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype) {
     if (i >= a.N) return;
     uint8_t t = ntype[i];
     bool bulk = is_active(t);
+    bool wrap = false;
     if (bulk) {
         const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
         if (x < 1 || y < 1 || z < 1 || x > a.X - 2 || y > a.Y - 2 || z > a.Z - 2) bulk = false;
-        for (int j = 1; j < Q && bulk; ++j)
-            if (!is_active(ntype[init_link(a, pf.v, i, j)])) bulk = false;
+        for (int j = 1; j < Q && bulk; ++j) {
+            const long long l = init_link(a, pf.v, i, j);
+            if (!is_active(ntype[l])) bulk = false;
+            if (l != i + cx(j) + (long long)a.X * (cy(j) + (long long)a.Y * cz(j))) wrap = true;
+        }
     }
-    const uint8_t nt = bulk ? (t | HB_BULK) : (t & ~HB_BULK);
+    uint8_t nt = bulk ? (t | HB_BULK) : (t & ~HB_BULK);
+    nt = wrap ? (nt | HB_PWRAP) : (nt & ~HB_PWRAP);
     if (nt != t) ntype[i] = nt;
 }
 
@@ -549,15 +553,14 @@ static PerFaces per_faces(hb_ctx* c) {
     return p;
 }
 
-LBArgs lb_args(hb_ctx* c) {
+LBArgs lb_args(hb_ctx* c, int cur) {
     LBArgs a;
     a.X = c->X; a.Y = c->Y; a.Z = c->Z; a.N = c->N;
     for (int k = 0; k < 6; ++k) a.per[k] = c->P.boundary[k] == HB_T_PERIODIC;
     a.ntype = c->ntype;
     a.solid = c->solid;
-    a.fA = c->fA;
-    a.fB = c->fB;
-    a.parity = c->parity;
+    a.fin = cur ? c->fB : c->fA;
+    a.fout = cur ? c->fA : c->fB;
     a.mode = c->mode;
     a.rho = c->rho;
     a.u = c->u;
@@ -566,6 +569,13 @@ LBArgs lb_args(hb_ctx* c) {
     a.visc = c->visc;
     a.dv = c->dv;
     a.F = c->lb_force;
+    a.Ff = c->lb_force_f;
+    for (int j = 0; j < Q; ++j) a.ne[j] = cx(j) + c->X * (cy(j) + c->Y * cz(j));
+    a.init_visc_f = (float)c->P.init_visc;
+    a.trt_magic_f = (float)c->P.trt_magic;
+    a.plastic_visc_f = (float)c->P.plastic_visc;
+    a.yield_stress_f = (float)c->P.yield_stress;
+    a.turb_const_f = (float)c->P.turb_const;
     a.init_visc = c->P.init_visc;
     a.collision = c->P.collision;
     a.trt_magic = c->P.trt_magic;
@@ -580,6 +590,7 @@ LBArgs lb_args(hb_ctx* c) {
     a.parts.x1 = c->d.E ? c->d.x[1] : nullptr;
     a.parts.w = c->d.E ? c->d.wG : nullptr;
     a.parts.radius = c->d.E ? c->d.rad : nullptr;
+    a.parts.pf = c->d.E ? c->d.pf : nullptr;
     a.status = c->status;
     a.wall_part = c->wall_part;
     a.nwalls = c->d.nw;
@@ -611,7 +622,7 @@ int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int 
     cudaMalloc(&mx, 3 * sizeof(int));
     cudaMemsetAsync(mx, 0, 3 * sizeof(int), c->stream);
     k_active_max<<<G, B, 0, c->stream>>>(a, c->ntype, mx);
-    LBArgs b = lb_args(c);
+    LBArgs b = lb_args(c, 1);  // fout = fA: the initial state lives in buffer 0
     const double* F = c->P.lbF;  // initialisation always uses lbF (LB.cpp:935)
     const double* iv = c->P.init_velocity;
     if (c->P.precision == HB_FP64)
@@ -632,17 +643,19 @@ void launch_refresh_bulk(hb_ctx* c) {
     k_bulk<<<ceil_div(c->N, 256), 256, 0, c->stream>>>(a, per_faces(c), c->ntype);
 }
 
-void launch_lb_step(hb_ctx* c) {
-    LBArgs a = lb_args(c);
+void launch_lb_step(hb_ctx* c, int cur) {
+    LBArgs a = lb_args(c, cur);
     int block;
     dim3 g = lb_grid(c, block);
-    if (c->P.precision == HB_FP64) k_collide_stream<PolF64><<<g, block, 0, c->stream>>>(a);
-    else if (c->P.precision == HB_FP32) k_collide_stream<PolF32><<<g, block, 0, c->stream>>>(a);
-    else k_collide_stream<PolF16><<<g, block, 0, c->stream>>>(a);
+    if (c->P.precision == HB_FP64) {
+        k_collide_stream<PolF64><<<g, block, 0, c->stream>>>(a);
+        return;
+    }
+    launch_lb_step_dev(c, a);
 }
 
-void launch_lb_wallforce(hb_ctx* c) {
-    LBArgs a = lb_args(c);
+void launch_lb_wallforce(hb_ctx* c, int cur) {
+    LBArgs a = lb_args(c, cur);
     int block;
     dim3 g = lb_grid(c, block);
     if (c->P.precision == HB_FP64) k_wallforce<PolF64><<<g, block, 0, c->stream>>>(a);
@@ -651,7 +664,6 @@ void launch_lb_wallforce(hb_ctx* c) {
     k_wallforce_final<<<1, 32, 0, c->stream>>>(c->wall_part, (int)(g.x * g.y * g.z), c->wall_force);
 }
 
-void launch_flip(hb_ctx* c) { k_flip<<<1, 1, 0, c->stream>>>(c->parity); }
 
 int launch_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside,
                           const uint32_t* solid, const double* f, const double* n, const double* u,
@@ -689,7 +701,7 @@ int launch_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside,
         }
         cudaMemcpy(df, hf.data(), sizeof(double) * 19 * N, cudaMemcpyHostToDevice);
     }
-    void* dst = c->h_parity ? c->fB : c->fA;
+    void* dst = c->cur ? c->fB : c->fA;
     if (c->P.precision == HB_FP64) k_upload_f<PolF64><<<G, B, 0, c->stream>>>(df, N, dst);
     else if (c->P.precision == HB_FP32) k_upload_f<PolF32><<<G, B, 0, c->stream>>>(df, N, dst);
     else k_upload_f<PolF16><<<G, B, 0, c->stream>>>(df, N, dst);

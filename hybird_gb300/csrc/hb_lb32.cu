@@ -1,0 +1,196 @@
+// hb_lb32.cu -- the reduced-precision fused collide+stream kernel (FP32 deviations or
+// scaled FP16 deviations in HBM, FP32 arithmetic), compiled with FMA contraction.
+#include <cstdio>
+
+#include "hb_common.cuh"
+#include "hb_ctx.h"
+
+namespace hb {
+
+// ---- reduced-precision kernel (FP32 / FP16 storage, FP32 compute) ---------------------
+// Populations are deviations g = f - w (rho0 = 1).  The collision is written on the
+// symmetric / antisymmetric parts of each direction pair (j, opp j):
+//   g'_j   = sym + anti,   g'_opp = sym - anti,
+//   sym  = fp - w+ (fp - ep) + (1 - w+/2) Fs,   anti = fm - w- (fm - em) + (1 - w-/2) Fa
+// with fp, fm (ep, em; Fs, Fa) the halves of g_j +/- g_opp (of the equilibrium and of the
+// Guo term).  BGK is the case w- = w+ = 1/tau: then g'_j = g_j + w (geq_j - g_j) + (1 - w/2)
+// F_j, which is node::solveCollision + node::addForce (node.cpp:158-184).
+// 32-bit indices; nodes whose links neither wrap nor touch a non-active node stream with
+// fixed offsets ne[j].  Threads of wall nodes at the ends of an active row write their own
+// (never read) entries so each row is written as whole 64-byte chunks by one block.
+
+__device__ __forceinline__ int link32(const LBArgs& a, int x, int y, int z, int j) {
+    int xn = x + cx(j), yn = y + cy(j), zn = z + cz(j);
+    if (xn == 0 && a.per[0]) xn = a.X - 2;
+    else if (xn == a.X - 1 && a.per[1]) xn = 1;
+    if (yn == 0 && a.per[2]) yn = a.Y - 2;
+    else if (yn == a.Y - 1 && a.per[3]) yn = 1;
+    if (zn == 0 && a.per[4]) zn = a.Z - 2;
+    else if (zn == a.Z - 1 && a.per[5]) zn = 1;
+    return xn + a.X * (yn + a.Y * zn);
+}
+
+// one post-collision population of a node with non-trivial links (pull rules of
+// LB.cpp:1231-1356 seen from the sending node)
+template <class P>
+__device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fout, int N, int x, int y, int z,
+                                             int i, int j, float g, float n, float ux, float uy, float uz,
+                                             float usq) {
+    const int l = link32(a, x, y, z, j);
+    const uint8_t lc = a.ntype[l] & HB_TYPE_MASK;
+    const int o = opp(j);
+    if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
+        P::store(fout + j * N + l, g);
+    } else if (lc == HB_T_STATWALL) {
+        P::store(fout + o * N + i, g);
+    } else if (lc == HB_T_GAS) {
+        const float vu = float(cx(j)) * ux + float(cy(j)) * uy + float(cz(j)) * uz;
+        const float w = float(wgt(j));
+        P::store(fout + o * N + i, -g + w * (9.0f * vu * vu - 3.0f * usq));
+    } else if (lc == HB_T_DYNWALL) {
+        const float uw = float(a.u[l] * cx(j) + a.u[a.N + l] * cy(j) + a.u[2 * a.N + l] * cz(j));
+        P::store(fout + o * N + i, g - 6.0f * n * float(wgt(j)) * uw);
+    } else {
+        flag_status(a.status, 1);
+    }
+}
+
+template <class P>
+__global__ void __launch_bounds__(128, 8) k_collide_stream_dev(LBArgs a) {
+    using S = typename P::S;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y + 1;
+    const int z = blockIdx.z + 1;
+    if (x >= a.X) return;
+    const int N = (int)a.N;
+    const int i = x + a.X * (y + a.Y * z);
+    const S* fin = reinterpret_cast<const S*>(a.fin);
+    S* fout = reinterpret_cast<S*>(a.fout);
+    const uint8_t t = a.ntype[i];
+    if (!is_active(t)) {
+        if (x == 0 || x == a.X - 1) {
+#pragma unroll
+            for (int j = 0; j < Q; ++j) P::store(fout + j * N + i, 0.0f);
+        }
+        return;
+    }
+    const int mode = *a.mode;
+    const uint8_t code = t & HB_TYPE_MASK;
+    float f[Q];
+#pragma unroll
+    for (int j = 0; j < Q; ++j) f[j] = P::load(fin + j * N + i);
+
+    float dn = 0.0f, mx = 0.0f, my = 0.0f, mz = 0.0f;
+#pragma unroll
+    for (int j = 0; j < Q; ++j) {
+        dn += f[j];
+        if (cx(j)) mx += cx(j) > 0 ? f[j] : -f[j];
+        if (cy(j)) my += cy(j) > 0 ? f[j] : -f[j];
+        if (cz(j)) mz += cz(j) > 0 ? f[j] : -f[j];
+    }
+    const float n = 1.0f + dn;
+    const float inv = 1.0f / n;
+    float ux = mx * inv, uy = my * inv, uz = mz * inv;
+    if (!(n > 0.0f) || ux != ux || uy != uy || uz != uz) flag_status(a.status, 0);
+
+    float hx = 0.0f, hy = 0.0f, hz = 0.0f;
+    if (a.couple && (t & HB_INSIDE)) {  // LB.cpp:1863-1904 with FP32 particle copies
+        const int p = (int)a.solid[i];
+        const int E = a.parts.count;
+        const float* pf = a.parts.pf;
+        const float rx = float(x) - pf[p], ry = float(y) - pf[E + p], rz = float(z) - pf[2 * E + p];
+        const float wx = pf[6 * E + p], wy = pf[7 * E + p], wz = pf[8 * E + p];
+        const float lvx = pf[3 * E + p] + (wy * rz - wz * ry);
+        const float lvy = pf[4 * E + p] + (wz * rx - wx * rz);
+        const float lvz = pf[5 * E + p] + (wx * ry - wy * rx);
+        const float lf = (a.free_surface ? float(a.mass[i]) : 1.0f) * inv;
+        const float dvx = lf * (ux - lvx), dvy = lf * (uy - lvy), dvz = lf * (uz - lvz);
+        hx = -dvx; hy = -dvy; hz = -dvz;
+        float* dv = reinterpret_cast<float*>(a.dv);
+        dv[i] = dvx; dv[N + i] = dvy; dv[2 * N + i] = dvz;
+    }
+    const float Fx = a.Ff[0] + hx, Fy = a.Ff[1] + hy, Fz = a.Ff[2] + hz;
+    ux += 0.5f * Fx * inv;  // shiftVelocity
+    uy += 0.5f * Fy * inv;
+    uz += 0.5f * Fz * inv;
+    const float usq = ux * ux + uy * uy + uz * uz;
+    const float uF = ux * Fx + uy * Fy + uz * Fz;
+
+    float visc = a.init_visc_f;
+    if (a.visc_model) {  // computeShearRate (node.cpp:103-145) on the symmetric parts
+        float* vp = reinterpret_cast<float*>(a.visc);
+        const float vold = vp[i];
+        float pxx = 0, pyy = 0, pzz = 0, pxy = 0, pxz = 0, pyz = 0;
+#pragma unroll
+        for (int j = 1; j < Q; j += 2) {
+            const int o = j + 1;
+            const float vu = float(cx(j)) * ux + float(cy(j)) * uy + float(cz(j)) * uz;
+            const float w = float(wgt(j));
+            const float ep = w * (dn + n * (4.5f * vu * vu - 1.5f * usq));
+            const float d = (f[j] + f[o]) - 2.0f * ep;
+            if (cx(j)) pxx += d;
+            if (cy(j)) pyy += d;
+            if (cz(j)) pzz += d;
+            if (cx(j) * cy(j)) pxy += cx(j) * cy(j) > 0 ? d : -d;
+            if (cx(j) * cz(j)) pxz += cx(j) * cz(j) > 0 ? d : -d;
+            if (cy(j) * cz(j)) pyz += cy(j) * cz(j) > 0 ? d : -d;
+        }
+        const float tau = 0.5f + 3.0f * vold;
+        const float sc = 1.5f / (tau * n);
+        pxx *= sc; pyy *= sc; pzz *= sc; pxy *= sc; pxz *= sc; pyz *= sc;
+        const float shear = sqrtf(0.5f * (pxx * pxx + pyy * pyy + pzz * pzz + 2.0f * (pxy * pxy + pxz * pxz + pyz * pyz)));
+        const float nuTurb = (a.visc_model & 2) ? a.turb_const_f * shear : 0.0f;
+        const float nuApp = (a.visc_model & 1) ? a.plastic_visc_f + a.yield_stress_f / (n * 2.0f * shear) : vold;
+        visc = fmaxf(float((0.501 - 0.5) / 3.0), fminf(float((1.8 - 0.5) / 3.0), nuApp + nuTurb));
+        vp[i] = visc;
+    }
+    const float tp = 0.5f + 3.0f * visc;
+    const float wp = 1.0f / tp;
+    const float wm = a.collision == HB_TRT ? 1.0f / (a.trt_magic_f / (tp - 0.5f) + 0.5f) : wp;
+    const float ap = 1.0f - 0.5f * wp, am = 1.0f - 0.5f * wm;
+
+    const bool all = (mode & 1) != 0;
+    if (all || a.free_surface || !(t & HB_BULK)) a.rho[i] = (double)n;
+    if (a.free_surface && code == HB_T_FLUID) a.mass[i] = (double)n;
+    if (all || code == HB_T_INTERFACE) {
+        a.u[i] = (double)ux; a.u[a.N + i] = (double)uy; a.u[2 * a.N + i] = (double)uz;
+        a.hf[i] = (double)hx; a.hf[a.N + i] = (double)hy; a.hf[2 * a.N + i] = (double)hz;
+    }
+    const bool fast = (t & (HB_BULK | HB_PWRAP)) == HB_BULK;
+
+    {  // rest population
+        const float w0 = float(wgt(0));
+        const float e0 = w0 * (dn + n * (-1.5f * usq));
+        P::store(fout + i, f[0] - wp * (f[0] - e0) + ap * (w0 * (-3.0f * uF)));
+    }
+#pragma unroll
+    for (int j = 1; j < Q; j += 2) {
+        const int o = j + 1;
+        const float w = float(wgt(j));
+        const float vu = float(cx(j)) * ux + float(cy(j)) * uy + float(cz(j)) * uz;
+        const float cF = float(cx(j)) * Fx + float(cy(j)) * Fy + float(cz(j)) * Fz;
+        const float ep = w * (dn + n * (4.5f * vu * vu - 1.5f * usq));
+        const float em = 3.0f * w * n * vu;
+        const float fp = 0.5f * (f[j] + f[o]), fm = 0.5f * (f[j] - f[o]);
+        const float Fs = w * (9.0f * vu * cF - 3.0f * uF), Fa = 3.0f * w * cF;
+        const float sym = fp - wp * (fp - ep) + ap * Fs;
+        const float anti = fm - wm * (fm - em) + am * Fa;
+        const float gj = sym + anti, go = sym - anti;
+        if (fast) {
+            P::store(fout + j * N + i + a.ne[j], gj);
+            P::store(fout + o * N + i + a.ne[o], go);
+        } else {
+            push_general<P>(a, fout, N, x, y, z, i, j, gj, n, ux, uy, uz, usq);
+            push_general<P>(a, fout, N, x, y, z, i, o, go, n, ux, uy, uz, usq);
+        }
+    }
+}
+
+void launch_lb_step_dev(hb_ctx* c, const LBArgs& a) {
+    const int b2 = c->X <= 64 ? 64 : 128;
+    dim3 g2((unsigned)ceil_div(c->X, b2), (unsigned)(c->Y - 2), (unsigned)(c->Z - 2));
+    if (c->P.precision == HB_FP32) k_collide_stream_dev<PolF32><<<g2, b2, 0, c->stream>>>(a);
+    else k_collide_stream_dev<PolF16><<<g2, b2, 0, c->stream>>>(a);
+}
+
+}  // namespace hb

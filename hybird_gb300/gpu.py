@@ -21,9 +21,10 @@ def lib():
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(abi.LIB_PATH):
-        raise HbError(f"CUDA library not built: {abi.LIB_PATH} (run __graft_entry__.build())")
-    L = C.CDLL(abi.LIB_PATH)
+    path = os.environ.get("HB_LIB_PATH", abi.LIB_PATH)  # an alternate build of the same ABI
+    if not os.path.exists(path):
+        raise HbError(f"CUDA library not built: {path} (run __graft_entry__.build())")
+    L = C.CDLL(path)
     vp, P = C.c_void_p, C.POINTER
     L.hb_last_error.restype = C.c_char_p
     L.hb_create.argtypes = [P(abi.HbParams), P(vp)]
@@ -41,6 +42,7 @@ def lib():
     L.hb_download_walls.argtypes = [vp, vp, vp, P(C.c_int32)]
     L.hb_get_status.argtypes = [vp, P(abi.HbStatus)]
     L.hb_time_cycles.argtypes = [vp, C.c_int32, P(C.c_float), P(C.c_float), P(C.c_int32)]
+    L.hb_profile_phases.argtypes = [vp, C.c_int32, vp, P(C.c_int32)]
     _lib = L
     return L
 
@@ -129,6 +131,12 @@ class GpuSim:
         s = abi.HbStatus()
         check(self.L.hb_get_status(self.h, C.byref(s)))
         return s
+
+    def profile_phases(self, n):
+        us = np.zeros(64)
+        k = C.c_int32(0)
+        check(self.L.hb_profile_phases(self.h, n, _p(us), C.byref(k)))
+        return us[:k.value]
 
     def time_cycles(self, n):
         tot, lbk, kpc = C.c_float(0), C.c_float(0), C.c_int32(0)

@@ -188,6 +188,11 @@ int hb_get_status(hb_ctx* ctx, hb_status* status);
  * elapsed device time of the whole cycles and of the stream-collide kernel alone. */
 int hb_time_cycles(hb_ctx* ctx, int32_t nsteps, float* ms_total, float* ms_lb_kernel,
                    int32_t* kernels_per_cycle);
+/* Runs nsteps cycles with device timestamps at the grid barriers of the DEM/coupling
+ * kernel and returns the mean duration (microseconds) of each phase in order:
+ * element-force reduction, then (forces, correct+predict) per DEM substep, then the
+ * three coupling-mask passes.  us must hold 4 + 2*multiStep values. */
+int hb_profile_phases(hb_ctx* ctx, int32_t nsteps, double* us, int32_t* nphases);
 
 #ifdef __cplusplus
 }
