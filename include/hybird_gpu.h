@@ -194,6 +194,28 @@ int hb_time_cycles(hb_ctx* ctx, int32_t nsteps, float* ms_total, float* ms_lb_ke
  * three coupling-mask passes.  us must hold 4 + 2*multiStep values. */
 int hb_profile_phases(hb_ctx* ctx, int32_t nsteps, double* us, int32_t* nphases);
 
+/* ---- allocation-free entry point ----------------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device memory:
+ * host drivers that run each solver step inside a CUDA stream capture, where
+ * cudaMalloc is not allowed, and integrations confined to a device-memory budget fixed
+ * by the embedding application.  Computes the moving-wall momentum exchange of one
+ * streamed state (the quantity hb_download_walls reports, LB.cpp:1321-1341) from caller
+ * device buffers and allocates nothing: its scratch is a fixed 152 KiB device array
+ * inside the library, kept by every GPU that loads it until the process exits.
+ *   f          [19*N] FP64 populations after streaming, component-major
+ *   type       [N] node type codes (0..9), solid [N] wall index of wall nodes
+ *   rho, mass  [N]; u [3*N] (wall-node velocities are read from u)
+ *   wall_force [3*6+1] device output: per wall (Fx,Fy,Fz) in wall order, then the
+ *              extra mass; stream: cudaStream_t or NULL for the default stream.
+ * The first call on a device resolves the scratch address for that device: make it
+ * before any stream capture.  Calls that overlap on the GPU share the scratch and race;
+ * the caller serialises them.  Lattices above HB_NOALLOC_MAX_NODES give HB_ERR_ARG. */
+#define HB_NOALLOC_MAX_NODES (1LL << 28)
+int hb_wall_force_noalloc(const double* f, const uint8_t* type, const uint32_t* solid,
+                          const double* rho, const double* u, const double* mass,
+                          const int32_t* lb_size, const int32_t* boundary,
+                          double* wall_force, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
