@@ -155,6 +155,13 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
                 pf[(size_t)(6 + q) * E + k] = (float)w0[q * E + k];
             }
         if ((rc = dalloc(&d.pf, 9 * (size_t)E))) return rc;
+        std::vector<int> plain(E);
+        for (int k = 0; k < E; ++k) {
+            const bool ident = q0[k] == 1.0 && q0[E + k] == 0.0 && q0[2 * E + k] == 0.0 && q0[3 * E + k] == 0.0;
+            plain[k] = ident ? 1 : 0;  // q1 (quaternion rate) is zero for every uploaded element
+        }
+        if ((rc = dalloc(&d.plain, E))) return rc;
+        CK(cudaMemcpy(d.plain, plain.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(d.pf, pf.data(), sizeof(float) * pf.size(), cudaMemcpyHostToDevice));
     }
     // neighbour-list parameters (DEM.cpp:1270-1312)
@@ -172,7 +179,7 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         (rc = dalloc(&d.cell_fill, d.ncells)) || (rc = dalloc(&d.cell_items, E)) ||
         (rc = dalloc(&d.nbr, (size_t)E * NBR_CAP)) || (rc = dalloc(&d.nbr_cnt, E)) || (rc = dalloc(&d.wall_of, E)) ||
         (rc = dalloc(&d.obj, (size_t)E * OBJ_CAP)) || (rc = dalloc(&d.obj_cnt, E)) || (rc = dalloc(&d.scal, 8)) ||
-        (rc = dalloc(&d.contacts, 1)) || (rc = dalloc(&d.partial, ceil_div(E, 256) + 1)) || (rc = dalloc(&d.done, 1)))
+        (rc = dalloc(&d.contacts, 1)) || (rc = dalloc(&d.partial, hb::PARTIAL_CAP)) || (rc = dalloc(&d.done, 1)))
         return rc;
     const double scal0[8] = {0.5 * d.nebrRange, 1.0, 0, 0, 0, 0, 0, 0};  // maxDisp, rebuild
     CK(cudaMemcpy(d.scal, scal0, sizeof(scal0), cudaMemcpyHostToDevice));
@@ -237,7 +244,7 @@ int hb_destroy(hb_ctx* c) {
     if (c->graph2) cudaGraphDestroy(c->graph2);
     void* ptrs[] = {c->ntype, c->solid, c->fA, c->fB, c->mode, c->rho, c->u, c->hf, c->mass,
                     c->visc, c->dv, c->claim, c->status, c->wall_part, c->wall_force, c->fs_force, c->if_list,
-                    c->if_count, c->fs_scal, c->fs_flag, c->fs_parent, c->fs_part, c->lb_force, c->lb_force_f, c->d.pf,
+                    c->if_count, c->fs_scal, c->fs_flag, c->fs_parent, c->fs_part, c->lb_force, c->lb_force_f, c->d.pf, c->d.plain,
                     c->d.base, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r};

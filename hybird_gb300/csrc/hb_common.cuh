@@ -29,6 +29,7 @@ constexpr int MAX_WALLS = 6;
 constexpr int NBR_CAP = 48;      // candidate neighbours kept per particle
 constexpr int OBJ_CAP = 16;      // objects in range kept per particle
 constexpr int STATUS_WORDS = 8;  // device status words (numeric, capacity, wait, ...)
+constexpr int PARTIAL_CAP = 4096;  // per-block partials of grid-wide reductions (>= any grid used)
 
 // D3Q19 velocity set in the reference's order O,x,y,z,xy,yz,zx (lattice.h:36-60)
 __host__ __device__ constexpr int cx(int j) {

@@ -37,6 +37,7 @@ struct DemArgs {
     double *FH, *MH, *FP, *FW, *MP, *MW;
     double *fvol, *m, *I, *rad;
     float* pf;
+    const int* plain;  // 1: orientation fixed at identity (no quaternion rates)
     int *cell_of, *cell_cnt, *cell_start, *cell_fill, *cell_items;
     int *nbr, *nbr_cnt, *wall_of, *obj, *obj_cnt;
     double* scal;
@@ -311,6 +312,129 @@ __device__ void forces_one(const DemArgs& a, int i, int& ncont) {
     }
 }
 
+// contacts of particle i by one warp: lanes take candidates (and objects) in list
+// order, the sums use a fixed xor-shuffle tree, so the result is reproducible
+__device__ void forces_warp(const DemArgs& a, int i, int lane, int& ncont) {
+    const int E = a.E;
+    const V xpi = ld3(a.xp0, E, i);
+    V FP{0, 0, 0}, MP{0, 0, 0}, FW{0, 0, 0}, MW{0, 0, 0};
+    const int cnt = a.nbr_cnt[i];
+    for (int k = lane; k < cnt; k += 32) {
+        const int j = a.nbr[(long long)i * NBR_CAP + k];
+        const int I = min(i, j), J = max(i, j);
+        const double rI = a.rad[I], rJ = a.rad[J];
+        const double sig = rI + rJ;
+        const V vd = sub(ld3(a.xp0, E, J), ld3(a.xp0, E, I));
+        if (!(nrm2(vd) < sig * sig)) continue;
+        if (i < j) ++ncont;
+        // particleParticleCollision with I = lower index (DEM.cpp:1801-1900)
+        const double dist = sqrt(nrm2(vd));
+        const double overlap = rI + rJ - dist;
+        const V relVel = sub(ld3(a.xp1, E, J), ld3(a.xp1, E, I));
+        const V en = divs(vd, dist);
+        const double vn = dot(relVel, en);
+        const V nrv = mul(vn, en);
+        const double mI = a.m[I], mJ = a.m[J];
+        const double effMass = mI * mJ / (mI + mJ);
+        const double effRad = rI * rJ / (rI + rJ);
+        const double fn = normal_contact(a, overlap, vn, effRad, effMass);
+        const V nf = mul(fn, en);
+        const V vrI = mul(rI, en), vrJ = mul(-rJ, en);
+        const V rvc = add(sub(relVel, cross(ld3(a.wpG, E, I), vrI)), cross(ld3(a.wpG, E, J), vrJ));
+        const V tang = sub(rvc, nrv);
+        const double nt = sqrt(nrm2(tang));
+        V tf{0, 0, 0};
+        const bool hasT = nt != 0.0;
+        if (hasT) {
+            const double ft = tangential_contact(a, nt, fn, effRad, effMass, a.muPart);
+            tf = mul(ft, divs(tang, nt));
+        }
+        if (i == I) {
+            FP = sub(FP, nf);
+            if (hasT) { MP = add(MP, cross(vrI, tf)); FP = add(FP, tf); }
+        } else {
+            FP = add(FP, nf);
+            if (hasT) { MP = sub(MP, cross(vrJ, tf)); FP = sub(FP, tf); }
+        }
+    }
+    const double ri = a.rad[i], mi = a.m[i];
+    const V xpv = ld3(a.xp1, E, i);
+    const V wpg = ld3(a.wpG, E, i);
+    const int w = a.wall_of[i];
+    if (lane == 0 && w >= 0) {  // wallParticleCollision (DEM.cpp:1902-1982), static walls
+        const V wn{a.wn[w][0], a.wn[w][1], a.wn[w][2]};
+        const double dist = dot(wn, sub(xpi, V{a.wp[w][0], a.wp[w][1], a.wp[w][2]}));
+        const double overlap = ri - dist;
+        if (overlap > 0.0) {
+            const V relVel = sub(xpv, V{0, 0, 0});
+            const double vn = dot(relVel, wn);
+            const V nrv = mul(vn, wn);
+            const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
+            const V nf = mul(fn, wn);
+            const V vrJ = mul(-ri, wn);
+            FW = add(FW, nf);
+            const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
+            const double nt = sqrt(nrm2(tang));
+            if (nt != 0.0) {
+                const double ft = tangential_contact(a, nt, fn, ri, mi, a.muWall);
+                const V tfw = mul(ft, divs(tang, nt));
+                MW = sub(MW, cross(vrJ, tfw));
+                FW = sub(FW, tfw);
+            }
+        }
+    }
+    const int oc = a.obj_cnt[i];
+    for (int k = lane; k < oc; k += 32) {  // objectParticleCollision (DEM.cpp:2060-2136)
+        const int o = a.obj[(long long)i * OBJ_CAP + k];
+        const V vd = sub(xpi, V{a.ox0[o], a.ox0[a.O + o], a.ox0[2 * a.O + o]});
+        const double dist = sqrt(nrm2(vd));
+        const double overlap = ri + a.orad[o] - dist;
+        if (!(overlap > 0.0)) continue;
+        const V en = mul(1.0 / dist, vd);
+        const V relVel = sub(xpv, V{a.ox1[o], a.ox1[a.O + o], a.ox1[2 * a.O + o]});
+        const double vn = dot(relVel, en);
+        const V nrv = mul(vn, en);
+        const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
+        const V nf = mul(fn, en);
+        const V vrJ = mul(-ri, en);
+        const V cJ = add(vrJ, V{0, 0, 0});
+        FW = add(FW, nf);
+        const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
+        const double nt = sqrt(nrm2(tang));
+        if (nt != 0.0) {
+            const double ft = tangential_contact(a, nt, fn, ri, mi, a.muPart);
+            const V tfo = mul(ft, divs(tang, nt));
+            MW = sub(MW, cross(cJ, tfo));
+            FW = sub(FW, tfo);
+        }
+    }
+    double v[12] = {FP.x, FP.y, FP.z, MP.x, MP.y, MP.z, FW.x, FW.y, FW.z, MW.x, MW.y, MW.z};
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int c = 0; c < 12; ++c) v[c] += __shfl_xor_sync(0xffffffffu, v[c], off);
+    if (lane != 0) return;
+    FP = V{v[0], v[1], v[2]}; MP = V{v[3], v[4], v[5]}; FW = V{v[6], v[7], v[8]}; MW = V{v[9], v[10], v[11]};
+    st3(a.FP, E, i, FP);
+    st3(a.MP, E, i, MP);
+    st3(a.FW, E, i, FW);
+    st3(a.MW, E, i, MW);
+    // Newton (DEM.cpp:1149-1181)
+    const double nv = a.numVisc;
+    const V FVisc = mul(-6.0 * M_PI * nv * ri, xpv);
+    const V MVisc = mul(-8.0 * M_PI * nv * ri * ri * ri, wpg);
+    const V x2 = add(divs(add(add(add(FVisc, ld3(a.FH, E, i)), FP), FW), mi), V{a.demF[0], a.demF[1], a.demF[2]});
+    st3(a.x2, E, i, x2);
+    const V mom = add(add(add(MVisc, ld3(a.MH, E, i)), MP), MW);
+    const Qt qp0 = ldq(a.qp0, E, i);
+    const V mBf = project(mom, qadj(qp0));
+    const V Iv = ld3(a.I, E, i);
+    const V wl = ld3(a.wpL, E, i);
+    const V waBf{(mBf.x + (Iv.y - Iv.z) * wl.y * wl.z) / Iv.x, (mBf.y + (Iv.z - Iv.x) * wl.z * wl.x) / Iv.y,
+                 (mBf.z + (Iv.x - Iv.y) * wl.x * wl.y) / Iv.z};
+    st3(a.w1, E, i, project(waBf, qp0));
+}
+
 __device__ void predict_one(const DemArgs& a, int i) {  // elmt.cpp:139-177
     const int E = a.E;
     const double dt = a.dt;
@@ -428,6 +552,142 @@ __device__ double correct_one(const DemArgs& a, int i) {  // elmt.cpp:179-254
 }
 
 // first substep after init: trigger from the initial velocities, then predict
+// corrector (elmt.cpp:179-254) followed by the next substep's predictor
+// (elmt.cpp:139-177) on registers: every input is loaded before the first store, so the
+// element's loads overlap instead of waiting on each other
+__device__ double correct_predict_one(const DemArgs& a, int i) {
+    const int E = a.E;
+    const double dt = a.dt;
+    const double c[5] = {dt, dt * dt / 2.0, dt * dt * dt / 6.0, dt * dt * dt * dt / 24.0, dt * dt * dt * dt * dt / 120.0};
+    const double g1[6] = {95.0 / 288.0, 1.0, 25.0 / 24.0, 35.0 / 72.0, 5.0 / 48.0, 1.0 / 120.0};
+    const double g2[6] = {3.0 / 16.0, 251.0 / 360.0, 1.0, 11.0 / 18.0, 1.0 / 6.0, 1.0 / 60.0};
+    const double c1o[6] = {g1[0] * c[0], g1[1] * c[0] / c[0], g1[2] * c[0] / c[1], g1[3] * c[0] / c[2],
+                           g1[4] * c[0] / c[3], g1[5] * c[0] / c[4]};
+    const double c2o[6] = {g2[0] * c[1], g2[1] * c[1] / c[0], g2[2] * c[1] / c[1], g2[3] * c[1] / c[2],
+                           g2[4] * c[1] / c[3], g2[5] * c[1] / c[4]};
+    // loads
+    const V x2 = ld3(a.x2, E, i), xp0 = ld3(a.xp0, E, i), xp1 = ld3(a.xp1, E, i), xp2 = ld3(a.xp2, E, i),
+            xp3 = ld3(a.xp3, E, i), xp4 = ld3(a.xp4, E, i), xp5 = ld3(a.xp5, E, i);
+    const V w1 = ld3(a.w1, E, i), wp0 = ld3(a.wp0, E, i), wp1 = ld3(a.wp1, E, i), wp2 = ld3(a.wp2, E, i),
+            wp3 = ld3(a.wp3, E, i), wp4 = ld3(a.wp4, E, i), wp5 = ld3(a.wp5, E, i);
+    const Qt q2 = ldq(a.q2, E, i), qp0 = ldq(a.qp0, E, i), qp1 = ldq(a.qp1, E, i), qp2 = ldq(a.qp2, E, i),
+             qp3 = ldq(a.qp3, E, i), qp4 = ldq(a.qp4, E, i), qp5 = ldq(a.qp5, E, i);
+    // corrector
+    const V x2c = sub(x2, xp2);
+    const V x0 = add(xp0, mul(c2o[0], x2c));
+    const V x1 = add(xp1, mul(c2o[1], x2c));
+    const V x3 = add(xp3, mul(c2o[3], x2c));
+    const V x4 = add(xp4, mul(c2o[4], x2c));
+    const V x5 = add(xp5, mul(c2o[5], x2c));
+    const V w1c = sub(w1, wp1);
+    const V w0 = add(wp0, mul(c1o[0], w1c));
+    const V w2 = add(wp2, mul(c1o[2], w1c));
+    const V w3 = add(wp3, mul(c1o[3], w1c));
+    const V w4 = add(wp4, mul(c1o[4], w1c));
+    const V w5 = add(wp5, mul(c1o[5], w1c));
+    const Qt q2c = Qt{q2.a - qp2.a, q2.b - qp2.b, q2.c - qp2.c, q2.d - qp2.d};
+    Qt q0 = qaxpy(qp0, q2c, c2o[0]);
+    const Qt q1 = qaxpy(qp1, q2c, c2o[1]);
+    const Qt q3 = qaxpy(qp3, q2c, c2o[3]);
+    const Qt q4 = qaxpy(qp4, q2c, c2o[4]);
+    const Qt q5 = qaxpy(qp5, q2c, c2o[5]);
+    const double qn = sqrt(q0.a * q0.a + q0.b * q0.b + q0.c * q0.c + q0.d * q0.d);
+    q0 = Qt{q0.a / qn, q0.b / qn, q0.c / qn, q0.d / qn};
+    const V wL = project(w0, qadj(q0));
+    // predictor for the next substep
+    const V nxp0 = add(add(add(add(add(x0, mul(c[0], x1)), mul(c[1], x2)), mul(c[2], x3)), mul(c[3], x4)), mul(c[4], x5));
+    const V nxp1 = add(add(add(add(x1, mul(c[0], x2)), mul(c[1], x3)), mul(c[2], x4)), mul(c[3], x5));
+    const V nxp2 = add(add(add(x2, mul(c[0], x3)), mul(c[1], x4)), mul(c[2], x5));
+    const V nxp3 = add(add(x3, mul(c[0], x4)), mul(c[1], x5));
+    const V nxp4 = add(x4, mul(c[0], x5));
+    Qt nqp0 = qaxpy(qaxpy(qaxpy(qaxpy(qaxpy(q0, q1, c[0]), q2, c[1]), q3, c[2]), q4, c[3]), q5, c[4]);
+    const double pn = sqrt(nqp0.a * nqp0.a + nqp0.b * nqp0.b + nqp0.c * nqp0.c + nqp0.d * nqp0.d);
+    nqp0 = Qt{nqp0.a / pn, nqp0.b / pn, nqp0.c / pn, nqp0.d / pn};
+    const Qt nqp1 = qaxpy(qaxpy(qaxpy(qaxpy(q1, q2, c[0]), q3, c[1]), q4, c[2]), q5, c[3]);
+    const Qt nqp2 = qaxpy(qaxpy(qaxpy(q2, q3, c[0]), q4, c[1]), q5, c[2]);
+    const Qt nqp3 = qaxpy(qaxpy(q3, q4, c[0]), q5, c[1]);
+    const Qt nqp4 = qaxpy(q4, q5, c[0]);
+    const V nwp0 = add(add(add(add(add(w0, mul(c[0], w1)), mul(c[1], w2)), mul(c[2], w3)), mul(c[3], w4)), mul(c[4], w5));
+    const V nwp1 = add(add(add(add(w1, mul(c[0], w2)), mul(c[1], w3)), mul(c[2], w4)), mul(c[3], w5));
+    const V nwp2 = add(add(add(w2, mul(c[0], w3)), mul(c[1], w4)), mul(c[2], w5));
+    const V nwp3 = add(add(w3, mul(c[0], w4)), mul(c[1], w5));
+    const V nwp4 = add(w4, mul(c[0], w5));
+    const V nwpL = project(nwp0, qadj(nqp0));
+    // stores
+    st3(a.x0, E, i, x0); st3(a.x1, E, i, x1); st3(a.x3, E, i, x3); st3(a.x4, E, i, x4); st3(a.x5, E, i, x5);
+    st3(a.w0, E, i, w0); st3(a.w2, E, i, w2); st3(a.w3, E, i, w3); st3(a.w4, E, i, w4); st3(a.w5, E, i, w5);
+    stq(a.q0, E, i, q0); stq(a.q1, E, i, q1); stq(a.q3, E, i, q3); stq(a.q4, E, i, q4); stq(a.q5, E, i, q5);
+    st3(a.wG, E, i, w0);
+    st3(a.wL, E, i, wL);
+    a.pf[i] = (float)x0.x; a.pf[E + i] = (float)x0.y; a.pf[2 * E + i] = (float)x0.z;
+    a.pf[3 * E + i] = (float)x1.x; a.pf[4 * E + i] = (float)x1.y; a.pf[5 * E + i] = (float)x1.z;
+    a.pf[6 * E + i] = (float)w0.x; a.pf[7 * E + i] = (float)w0.y; a.pf[8 * E + i] = (float)w0.z;
+    st3(a.xp0, E, i, nxp0); st3(a.xp1, E, i, nxp1); st3(a.xp2, E, i, nxp2); st3(a.xp3, E, i, nxp3);
+    st3(a.xp4, E, i, nxp4); st3(a.xp5, E, i, x5);
+    stq(a.qp0, E, i, nqp0); stq(a.qp1, E, i, nqp1); stq(a.qp2, E, i, nqp2); stq(a.qp3, E, i, nqp3);
+    stq(a.qp4, E, i, nqp4); stq(a.qp5, E, i, q5);
+    st3(a.wp0, E, i, nwp0); st3(a.wp1, E, i, nwp1); st3(a.wp2, E, i, nwp2); st3(a.wp3, E, i, nwp3);
+    st3(a.wp4, E, i, nwp4); st3(a.wp5, E, i, w5);
+    st3(a.wpG, E, i, nwp0);
+    st3(a.wpL, E, i, nwpL);
+    return nrm2(x1);
+}
+
+// Elements whose orientation stays the identity (single spheres with q0 = (1,0,0,0) and
+// no quaternion rates: their q2 is never set, elmt.cpp:139-254 keeps q exactly) need no
+// quaternion algebra, and the projections to the body frame are the identity; their
+// Gear corrector+predictor splits into independent Cartesian components.  Six lanes
+// per element: lanes 0-2 take x, y, z of the position chain, lanes 3-5 of the spin
+// chain.  Same arithmetic per component as correct_predict_one.
+__device__ double correct_predict_plain(const DemArgs& a, int i, int c) {
+    const int E = a.E;
+    const double dt = a.dt;
+    const double cc[5] = {dt, dt * dt / 2.0, dt * dt * dt / 6.0, dt * dt * dt * dt / 24.0, dt * dt * dt * dt * dt / 120.0};
+    const long long o = (long long)(c % 3) * E + i;
+    if (c < 3) {
+        const double g2[6] = {3.0 / 16.0, 251.0 / 360.0, 1.0, 11.0 / 18.0, 1.0 / 6.0, 1.0 / 60.0};
+        const double c2o[6] = {g2[0] * cc[1], g2[1] * cc[1] / cc[0], g2[2] * cc[1] / cc[1], g2[3] * cc[1] / cc[2],
+                               g2[4] * cc[1] / cc[3], g2[5] * cc[1] / cc[4]};
+        const double x2 = a.x2[o], p0 = a.xp0[o], p1 = a.xp1[o], p2 = a.xp2[o], p3 = a.xp3[o], p4 = a.xp4[o],
+                     p5 = a.xp5[o];
+        const double d = x2 - p2;
+        const double x0 = p0 + d * c2o[0], x1 = p1 + d * c2o[1], x3 = p3 + d * c2o[3], x4 = p4 + d * c2o[4],
+                     x5 = p5 + d * c2o[5];
+        a.x0[o] = x0; a.x1[o] = x1; a.x3[o] = x3; a.x4[o] = x4; a.x5[o] = x5;
+        a.xp0[o] = x0 + x1 * cc[0] + x2 * cc[1] + x3 * cc[2] + x4 * cc[3] + x5 * cc[4];
+        a.xp1[o] = x1 + x2 * cc[0] + x3 * cc[1] + x4 * cc[2] + x5 * cc[3];
+        a.xp2[o] = x2 + x3 * cc[0] + x4 * cc[1] + x5 * cc[2];
+        a.xp3[o] = x3 + x4 * cc[0] + x5 * cc[1];
+        a.xp4[o] = x4 + x5 * cc[0];
+        a.xp5[o] = x5;
+        a.pf[c * E + i] = (float)x0;
+        a.pf[(3 + c) * E + i] = (float)x1;
+        return x1;
+    }
+    const double g1[6] = {95.0 / 288.0, 1.0, 25.0 / 24.0, 35.0 / 72.0, 5.0 / 48.0, 1.0 / 120.0};
+    const double c1o[6] = {g1[0] * cc[0], g1[1] * cc[0] / cc[0], g1[2] * cc[0] / cc[1], g1[3] * cc[0] / cc[2],
+                           g1[4] * cc[0] / cc[3], g1[5] * cc[0] / cc[4]};
+    const double w1 = a.w1[o], p0 = a.wp0[o], p1 = a.wp1[o], p2 = a.wp2[o], p3 = a.wp3[o], p4 = a.wp4[o],
+                 p5 = a.wp5[o];
+    const double d = w1 - p1;
+    const double w0 = p0 + d * c1o[0], w2 = p2 + d * c1o[2], w3 = p3 + d * c1o[3], w4 = p4 + d * c1o[4],
+                 w5 = p5 + d * c1o[5];
+    a.w0[o] = w0; a.w2[o] = w2; a.w3[o] = w3; a.w4[o] = w4; a.w5[o] = w5;
+    a.wG[o] = w0;
+    a.wL[o] = w0;
+    const double n0 = w0 + w1 * cc[0] + w2 * cc[1] + w3 * cc[2] + w4 * cc[3] + w5 * cc[4];
+    a.wp0[o] = n0;
+    a.wp1[o] = w1 + w2 * cc[0] + w3 * cc[1] + w4 * cc[2] + w5 * cc[3];
+    a.wp2[o] = w2 + w3 * cc[0] + w4 * cc[1] + w5 * cc[2];
+    a.wp3[o] = w3 + w4 * cc[0] + w5 * cc[1];
+    a.wp4[o] = w4 + w5 * cc[0];
+    a.wp5[o] = w5;
+    a.wpG[o] = n0;
+    a.wpL[o] = n0;
+    a.pf[(6 + (c - 3)) * E + i] = (float)w0;
+    return 0.0;
+}
+
 __global__ void __launch_bounds__(256) k_dem_first(DemArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v2 = 0.0;
@@ -495,15 +755,28 @@ __device__ __forceinline__ bool in_sph(const Sph& s, int x, int y, int z) {
     return dx * dx + dy * dy + dz * dz < s.r2;
 }
 
+// The coupling passes give each thread whole rows (fixed y, z) of a particle's box: one
+// row of node bytes is one or two cache lines, so a thread pays one memory latency per
+// row instead of one per node.
+
 // findNewActive (LB.cpp:1921-1967): uncovered nodes leave the particle
 __device__ void pop_block(const CoupleArgs& a, int p) {
     const Box b = pbox(a, p, 2);
     const Sph s = load_sph(a, p);
-    for (int k = threadIdx.x; k < b.nx * b.ny * b.nz; k += blockDim.x) {
-        const int x = b.x0 + k % b.nx, y = b.y0 + (k / b.nx) % b.ny, z = b.z0 + k / (b.nx * b.ny);
-        const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
-        const uint8_t t = a.ntype[i];
-        if ((t & HB_INSIDE) && a.solid[i] == (uint32_t)p && !in_sph(s, x, y, z)) a.ntype[i] = t & ~HB_INSIDE;
+    for (int r = threadIdx.x; r < b.ny * b.nz; r += blockDim.x) {
+        const int y = b.y0 + r % b.ny, z = b.z0 + r / b.ny;
+        const long long base = (long long)a.X * ((long long)y + (long long)a.Y * z);
+        for (int xc = b.x0; xc < b.x0 + b.nx; xc += 8) {  // 8 loads in flight per chunk
+            uint8_t t8[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) t8[k] = xc + k < b.x0 + b.nx ? a.ntype[base + xc + k] : 0;
+            uint32_t s8[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) s8[k] = (t8[k] & HB_INSIDE) ? a.solid[base + xc + k] : 0xffffffffu;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (s8[k] == (uint32_t)p && !in_sph(s, xc + k, y, z)) a.ntype[base + xc + k] = t8[k] & ~HB_INSIDE;
+        }
     }
 }
 
@@ -513,76 +786,101 @@ __device__ void pop_block(const CoupleArgs& a, int p) {
 __device__ void claim_block(const CoupleArgs& a, int p) {
     const Box b = pbox(a, p, 1);
     const Sph s = load_sph(a, p);
-    for (int k = threadIdx.x; k < b.nx * b.ny * b.nz; k += blockDim.x) {
-        const int x = b.x0 + k % b.nx, y = b.y0 + (k / b.nx) % b.ny, z = b.z0 + k / (b.nx * b.ny);
-        const long long l = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
-        if (a.ntype[l] & HB_INSIDE) continue;
-        if (!in_sph(s, x, y, z)) continue;
-        unsigned long long best = ~0ull;
-        for (int kk = 1; kk <= 6; ++kk) {  // source m with link d[m][kk] == l
-            int mx = x - cx(kk), my = y - cy(kk), mz = z - cz(kk);
-            if (mx == 0 && a.per[1]) mx = a.X - 2; else if (mx == a.X - 1 && a.per[0]) mx = 1;
-            if (my == 0 && a.per[3]) my = a.Y - 2; else if (my == a.Y - 1 && a.per[2]) my = 1;
-            if (mz == 0 && a.per[5]) mz = a.Z - 2; else if (mz == a.Z - 1 && a.per[4]) mz = 1;
-            if (mx < 0 || my < 0 || mz < 0 || mx >= a.X || my >= a.Y || mz >= a.Z) continue;
-            const long long m = (long long)mx + (long long)a.X * ((long long)my + (long long)a.Y * mz);
-            const uint8_t tm = a.ntype[m];
-            if (!(tm & HB_INSIDE) || a.solid[m] != (uint32_t)p) continue;
-            // the reference's link table: interior nodes link arithmetically (with the
-            // periodic remap), boundary nodes link to themselves
-            const bool interior = mx > 0 && my > 0 && mz > 0 && mx < a.X - 1 && my < a.Y - 1 && mz < a.Z - 1;
-            if (!interior) continue;
-            int lx = mx + cx(kk), ly = my + cy(kk), lz = mz + cz(kk);
-            if (lx == 0 && a.per[0]) lx = a.X - 2; else if (lx == a.X - 1 && a.per[1]) lx = 1;
-            if (ly == 0 && a.per[2]) ly = a.Y - 2; else if (ly == a.Y - 1 && a.per[3]) ly = 1;
-            if (lz == 0 && a.per[4]) lz = a.Z - 2; else if (lz == a.Z - 1 && a.per[5]) lz = 1;
-            if (lx != x || ly != y || lz != z) continue;
-            const unsigned long long key = ((unsigned long long)m << 32) | (unsigned)p;
-            if (key < best) best = key;
+    for (int r = threadIdx.x; r < b.ny * b.nz; r += blockDim.x) {
+        const int y = b.y0 + r % b.ny, z = b.z0 + r / b.ny;
+        const long long base = (long long)a.X * ((long long)y + (long long)a.Y * z);
+        for (int x = b.x0; x < b.x0 + b.nx; ++x) {
+            const long long l = base + x;
+            if (a.ntype[l] & HB_INSIDE) continue;
+            if (!in_sph(s, x, y, z)) continue;
+            unsigned long long best = ~0ull;
+            for (int kk = 1; kk <= 6; ++kk) {  // source m with link d[m][kk] == l
+                int mx = x - cx(kk), my = y - cy(kk), mz = z - cz(kk);
+                if (mx == 0 && a.per[1]) mx = a.X - 2; else if (mx == a.X - 1 && a.per[0]) mx = 1;
+                if (my == 0 && a.per[3]) my = a.Y - 2; else if (my == a.Y - 1 && a.per[2]) my = 1;
+                if (mz == 0 && a.per[5]) mz = a.Z - 2; else if (mz == a.Z - 1 && a.per[4]) mz = 1;
+                if (mx < 0 || my < 0 || mz < 0 || mx >= a.X || my >= a.Y || mz >= a.Z) continue;
+                const long long m = (long long)mx + (long long)a.X * ((long long)my + (long long)a.Y * mz);
+                const uint8_t tm = a.ntype[m];
+                if (!(tm & HB_INSIDE) || a.solid[m] != (uint32_t)p) continue;
+                // the reference's link table: interior nodes link arithmetically (with the
+                // periodic remap), boundary nodes link to themselves
+                const bool interior = mx > 0 && my > 0 && mz > 0 && mx < a.X - 1 && my < a.Y - 1 && mz < a.Z - 1;
+                if (!interior) continue;
+                int lx = mx + cx(kk), ly = my + cy(kk), lz = mz + cz(kk);
+                if (lx == 0 && a.per[0]) lx = a.X - 2; else if (lx == a.X - 1 && a.per[1]) lx = 1;
+                if (ly == 0 && a.per[2]) ly = a.Y - 2; else if (ly == a.Y - 1 && a.per[3]) ly = 1;
+                if (lz == 0 && a.per[4]) lz = a.Z - 2; else if (lz == a.Z - 1 && a.per[5]) lz = 1;
+                if (lx != x || ly != y || lz != z) continue;
+                const unsigned long long key = ((unsigned long long)m << 32) | (unsigned)p;
+                if (key < best) best = key;
+            }
+            if (best != ~0ull) atomicMin(a.claim + l, best);
         }
-        if (best != ~0ull) atomicMin(a.claim + l, best);
     }
 }
 
 __device__ void commit_block(const CoupleArgs& a, int p) {
     const Box b = pbox(a, p, 1);
-    for (int k = threadIdx.x; k < b.nx * b.ny * b.nz; k += blockDim.x) {
-        const int x = b.x0 + k % b.nx, y = b.y0 + (k / b.nx) % b.ny, z = b.z0 + k / (b.nx * b.ny);
-        const long long l = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
-        const unsigned long long c = a.claim[l];
-        if (c == ~0ull || (uint32_t)(c & 0xffffffffu) != (uint32_t)p) continue;
-        a.ntype[l] = a.ntype[l] | HB_INSIDE;
-        a.solid[l] = (uint32_t)p;
-        a.claim[l] = ~0ull;
+    for (int r = threadIdx.x; r < b.ny * b.nz; r += blockDim.x) {
+        const int y = b.y0 + r % b.ny, z = b.z0 + r / b.ny;
+        const long long base = (long long)a.X * ((long long)y + (long long)a.Y * z);
+        for (int xc = b.x0; xc < b.x0 + b.nx; xc += 8) {  // 8 loads in flight per chunk
+            unsigned long long c8[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) c8[k] = xc + k < b.x0 + b.nx ? a.claim[base + xc + k] : ~0ull;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const unsigned long long c = c8[k];
+                if (c == ~0ull || (uint32_t)(c & 0xffffffffu) != (uint32_t)p) continue;
+                const long long l = base + xc + k;
+                a.ntype[l] = a.ntype[l] | HB_INSIDE;
+                a.solid[l] = (uint32_t)p;
+                a.claim[l] = ~0ull;
+            }
+        }
     }
 }
 
 // element hydrodynamic force, torque and entrained fluid (LB.cpp:1853-1918): fixed
-// thread-to-node assignment and a fixed-order tree, so the sum is reproducible
+// thread-to-row assignment and a fixed-order tree, so the sum is reproducible
 __device__ void reduce_block(const CoupleArgs& a, int p, double (*sh)[256]) {
     const int E = a.E;
     const Box b = pbox(a, p, 1);
     const double px = a.x0[p], py = a.x0[E + p], pz = a.x0[2 * E + p];
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-    for (int k = threadIdx.x; k < b.nx * b.ny * b.nz; k += blockDim.x) {
-        const int x = b.x0 + k % b.nx, y = b.y0 + (k / b.nx) % b.ny, z = b.z0 + k / (b.nx * b.ny);
-        const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
-        const uint8_t t = a.ntype[i];
-        if (!(t & HB_INSIDE) || !is_active(t) || a.solid[i] != (uint32_t)p) continue;
-        double dvx, dvy, dvz;
-        if (a.dv_f64) {
-            const double* d = reinterpret_cast<const double*>(a.dv);
-            dvx = d[i]; dvy = d[a.N + i]; dvz = d[2 * a.N + i];
-        } else {
-            const float* d = reinterpret_cast<const float*>(a.dv);
-            dvx = d[i]; dvy = d[a.N + i]; dvz = d[2 * a.N + i];
+    for (int r = threadIdx.x; r < b.ny * b.nz; r += blockDim.x) {
+        const int y = b.y0 + r % b.ny, z = b.z0 + r / b.ny;
+        const long long base = (long long)a.X * ((long long)y + (long long)a.Y * z);
+        for (int xc = b.x0; xc < b.x0 + b.nx; xc += 8) {  // 8 loads in flight per chunk
+            uint8_t t8[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) t8[k] = xc + k < b.x0 + b.nx ? a.ntype[base + xc + k] : 0;
+            bool in8[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                in8[k] = (t8[k] & HB_INSIDE) && is_active(t8[k]) && a.solid[base + xc + k] == (uint32_t)p;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (!in8[k]) continue;
+                const long long i = base + xc + k;
+                const int x = xc + k;
+                double dvx, dvy, dvz;
+                if (a.dv_f64) {
+                    const double* d = reinterpret_cast<const double*>(a.dv);
+                    dvx = d[i]; dvy = d[a.N + i]; dvz = d[2 * a.N + i];
+                } else {
+                    const float* d = reinterpret_cast<const float*>(a.dv);
+                    dvx = d[i]; dvy = d[a.N + i]; dvz = d[2 * a.N + i];
+                }
+                const double rx = (x - px) + 0.0, ry = (y - py) + 0.0, rz = (z - pz) + 0.0;
+                acc[0] += dvx; acc[1] += dvy; acc[2] += dvz;
+                acc[3] += ry * dvz - rz * dvy;
+                acc[4] += rz * dvx - rx * dvz;
+                acc[5] += rx * dvy - ry * dvx;
+                acc[6] += a.free_surface ? a.mass[i] : 1.0;
+            }
         }
-        const double rx = (x - px) + 0.0, ry = (y - py) + 0.0, rz = (z - pz) + 0.0;
-        acc[0] += dvx; acc[1] += dvy; acc[2] += dvz;
-        acc[3] += ry * dvz - rz * dvy;
-        acc[4] += rz * dvx - rx * dvz;
-        acc[5] += rx * dvy - ry * dvx;
-        acc[6] += a.free_surface ? a.mass[i] : 1.0;
     }
     __syncthreads();
     for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] = acc[c];
@@ -626,7 +924,7 @@ __device__ __forceinline__ void stamp(const CycleArgs& A, int k) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_cycle(CycleArgs A) {
+__global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
     cg::grid_group grid = cg::this_grid();
     __shared__ double sh[7][256];
     const int E = A.d.E;
@@ -634,6 +932,9 @@ __global__ void __launch_bounds__(256) k_cycle(CycleArgs A) {
     // (narrow pipe on this part) lands on every SM instead of the first few
     const int gt = blockIdx.x + gridDim.x * threadIdx.x;
     const int gs = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x + gridDim.x * (threadIdx.x >> 5);  // one warp per particle
+    const int nw = gridDim.x * (blockDim.x >> 5);
     stamp(A, 0);
     if (A.do_reduce)
         for (int p = blockIdx.x; p < E; p += gridDim.x) reduce_block(A.c, p, sh);
@@ -649,9 +950,10 @@ __global__ void __launch_bounds__(256) k_cycle(CycleArgs A) {
                 if (blockIdx.x == 0) nl_cells_block(A.d);
                 grid.sync();
                 for (int i = gt; i < E; i += gs) nl_build_one(A.d, i);
+                grid.sync();  // the contact warps read other threads' candidate lists
             }
             int ncont = 0;
-            for (int i = gt; i < E; i += gs) forces_one(A.d, i, ncont);
+            for (int i = gw; i < E; i += nw) forces_warp(A.d, i, lane, ncont);
             if (s == A.multi - 1) {  // overlapping pairs of the last substep (integer atomics)
                 for (int off = 16; off > 0; off >>= 1) ncont += __shfl_down_sync(0xffffffffu, ncont, off);
                 if ((threadIdx.x & 31) == 0 && ncont) {
@@ -662,9 +964,22 @@ __global__ void __launch_bounds__(256) k_cycle(CycleArgs A) {
             grid.sync();
             stamp(A, k++);
             double v2 = 0.0;
-            for (int i = gt; i < E; i += gs) {
-                v2 = fmax(v2, correct_one(A.d, i));
-                predict_one(A.d, i);  // next substep's predictor (own state only)
+            {  // six lanes per element (five elements per warp, lanes 30-31 idle)
+                const int grp = lane / 6, c = lane - 6 * grp;
+                const int wglob = blockIdx.x + gridDim.x * (threadIdx.x >> 5);
+                const int ngroups = 5 * nw;
+                for (int base = 5 * wglob; base < E; base += ngroups) {
+                    const int i = base + grp;
+                    const bool on = grp < 5 && i < E;
+                    const bool plain = on && A.d.plain[i];
+                    double x1c = 0.0;
+                    if (plain) x1c = correct_predict_plain(A.d, i, c);
+                    else if (on && c == 0) v2 = fmax(v2, correct_predict_one(A.d, i));
+                    // |x1|^2 in the reference's order (x*x + y*y) + z*z, gathered at lane c = 0
+                    const double y1 = __shfl_down_sync(0xffffffffu, x1c, 1);
+                    const double z1 = __shfl_down_sync(0xffffffffu, x1c, 2);
+                    if (plain && c == 0) v2 = fmax(v2, x1c * x1c + y1 * y1 + z1 * z1);
+                }
             }
             sh[0][threadIdx.x] = v2;
             __syncthreads();
@@ -675,8 +990,11 @@ __global__ void __launch_bounds__(256) k_cycle(CycleArgs A) {
             if (threadIdx.x == 0) A.d.partial[blockIdx.x] = sh[0][0];
             grid.sync();
             stamp(A, k++);
-            double mx = 0.0;  // DEM.cpp:1314-1324, 334-347 (every thread folds the same maxima)
-            for (int b = 0; b < (int)gridDim.x; ++b) mx = fmax(mx, ((volatile double*)A.d.partial)[b]);
+            // DEM.cpp:1314-1324, 334-347: every warp folds the block maxima with its lanes
+            // in parallel (max is order-independent), so all threads agree on the flag
+            double mx = 0.0;
+            for (int b = lane; b < (int)gridDim.x; b += 32) mx = fmax(mx, ((volatile double*)A.d.partial)[b]);
+            for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
             maxDisp += sqrt(mx) * A.d.dt;
             rebuild = maxDisp > A.d.trigger;
             if (rebuild) maxDisp = 0.0;
@@ -717,6 +1035,7 @@ static DemArgs dem_args(hb_ctx* c) {
     a.FH = d.FH; a.MH = d.MH; a.FP = d.FP; a.FW = d.FW; a.MP = d.MP; a.MW = d.MW;
     a.fvol = d.fvol; a.m = d.m; a.I = d.I; a.rad = d.rad;
     a.pf = d.pf;
+    a.plain = d.plain;
     a.cell_of = d.cell_of; a.cell_cnt = d.cell_cnt; a.cell_start = d.cell_start;
     a.cell_fill = d.cell_fill; a.cell_items = d.cell_items;
     a.nbr = d.nbr; a.nbr_cnt = d.nbr_cnt; a.wall_of = d.wall_of; a.obj = d.obj; a.obj_cnt = d.obj_cnt;
@@ -779,6 +1098,7 @@ int coop_grid(hb_ctx* c) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cycle, 256, 0);
     occ = occ < 1 ? 1 : (occ > 4 ? 4 : occ);
     cached = sms * occ;
+    if (cached > PARTIAL_CAP) cached = PARTIAL_CAP;  // one trigger partial per block
     return cached;
 }
 
