@@ -243,8 +243,8 @@ int hb_destroy(hb_ctx* c) {
     if (c->graph) cudaGraphDestroy(c->graph);
     if (c->graph2) cudaGraphDestroy(c->graph2);
     void* ptrs[] = {c->ntype, c->solid, c->fA, c->fB, c->mode, c->rho, c->u, c->hf, c->mass,
-                    c->visc, c->dv, c->claim, c->status, c->wall_part, c->wall_force, c->fs_force, c->if_list,
-                    c->if_count, c->fs_scal, c->fs_flag, c->fs_parent, c->fs_part, c->lb_force, c->lb_force_f, c->d.pf, c->d.plain,
+                    c->visc, c->dv, c->claim, c->status, c->wall_part, c->wall_force, c->fs_force, c->fs_mass2,
+                    c->fs_cnt, c->fs_scal, c->fs_flag, c->fs_first, c->fs_part, c->lb_force, c->lb_force_f, c->d.pf, c->d.plain,
                     c->d.base, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r};
@@ -591,13 +591,11 @@ int hb_get_status(hb_ctx* c, hb_status* s) {
         for (int v : cnt) tot += v;
         s->pairs = tot / 2;
     }
-    if (c->if_count) {
-        int k = 0;
-        CK(cudaMemcpy(&k, c->if_count, sizeof(int), cudaMemcpyDeviceToHost));
-        s->interface_cells = k;
+    if (c->fs_scal) {
         double sc[2];
         CK(cudaMemcpy(sc, c->fs_scal, sizeof(sc), cudaMemcpyDeviceToHost));
         s->mass_surplus = sc[0];
+        s->interface_cells = (int64_t)sc[1];
     }
     return HB_OK;
 }

@@ -84,13 +84,12 @@ struct hb_ctx {
     float* lb_force_f = nullptr;    // FP32 copy of lb_force
     float h_force_f[3] = {0.f, 0.f, 0.f};  // host staging of the FP32 force (kept alive for async copies)
     // free surface
-    uint32_t* if_list = nullptr;    // compacted interface list
-    int* if_count = nullptr;
     double* fs_scal = nullptr;      // [0]=surplus [1]=interface count as double
-    long long cap_if = 0;
-    int* fs_flag = nullptr;         // per-node conversion flags
-    uint32_t* fs_parent = nullptr;  // per-node parent key for new interface cells
+    uint8_t* fs_flag = nullptr;     // per-node conversion flags of the current step
+    double* fs_mass2 = nullptr;     // new interface masses (updateMass reads the old ones)
     double* fs_part = nullptr;      // per-block FP64 partials for the surplus ledger
+    int* fs_cnt = nullptr;          // per-block interface counts
+    int* fs_first = nullptr;        // 1 until the first free-surface step has run
     // DEM
     hb_dem_dev d;
     // graph

@@ -194,7 +194,6 @@ __global__ void __launch_bounds__(256) k_collide_stream(LBArgs a) {
     // ---- node macros needed by later phases (free surface, downloads, wall force)
     const bool all = (mode & 1) != 0;
     if (all || a.free_surface || !(t & HB_BULK)) a.rho[i] = (double)n;
-    if (a.free_surface && code == HB_T_FLUID) a.mass[i] = (double)n;
     if (all || code == HB_T_INTERFACE) {
         a.u[i] = (double)ux; a.u[N + i] = (double)uy; a.u[2 * N + i] = (double)uz;
         a.hf[i] = (double)hx; a.hf[N + i] = (double)hy; a.hf[2 * N + i] = (double)hz;

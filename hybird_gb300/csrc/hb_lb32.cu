@@ -145,7 +145,6 @@ __global__ void __launch_bounds__(128, 8) k_collide_stream_dev(LBArgs a) {
 
     const bool all = (mode & 1) != 0;
     if (all || a.free_surface || !(t & HB_BULK)) a.rho[i] = (double)n;
-    if (a.free_surface && code == HB_T_FLUID) a.mass[i] = (double)n;
     if (all || code == HB_T_INTERFACE) {
         a.u[i] = (double)ux; a.u[a.N + i] = (double)uy; a.u[2 * a.N + i] = (double)uz;
         a.hf[i] = (double)hx; a.hf[a.N + i] = (double)hy; a.hf[2 * a.N + i] = (double)hz;
