@@ -77,6 +77,12 @@ class HbStatus(C.Structure):
                 ("mass_surplus", C.c_double), ("total_mass", C.c_double)]
 
 
+class HbAdjointCfg(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("checkpoint_every", C.c_int32), ("precision", C.c_int32),
+                ("drag_axis", C.c_int32), ("tau", C.c_double), ("body_force", C.c_double * 3),
+                ("inlet_velocity", C.POINTER(C.c_double))]
+
+
 def dptr(a):
     """double* of a C-contiguous float64 array (or NULL for None)."""
     if a is None:

@@ -238,6 +238,7 @@ int hb_create(const hb_params* params, hb_ctx** out) {
 
 int hb_destroy(hb_ctx* c) {
     if (!c) return HB_OK;
+    hb::adjoint_free(c);
     for (int k = 0; k < 2; ++k)
         if (c->gexec[k]) cudaGraphExecDestroy(c->gexec[k]);
     if (c->graph) cudaGraphDestroy(c->graph);
@@ -677,6 +678,31 @@ int hb_time_cycles(hb_ctx* c, int32_t nsteps, float* ms_total, float* ms_lb_kern
         for (auto& e : ev) cudaEventDestroy(e);
     }
     CK(cudaGetLastError());
+    return HB_OK;
+}
+
+// ---- reverse (adjoint) ---------------------------------------------------------------
+
+int hb_adjoint_forward(hb_ctx* c, const hb_adjoint_cfg* cfg, double* J) {
+    if (!c) return seterr(HB_ERR_ARG, "ctx is NULL");
+    std::string e;
+    const int rc = hb::adjoint_run(c, cfg, false, J, nullptr, nullptr, nullptr, e);
+    return rc ? seterr(rc, "%s", e.c_str()) : HB_OK;
+}
+
+int hb_adjoint_drag(hb_ctx* c, const hb_adjoint_cfg* cfg, double* J, double* dJ_dF, double* dJ_dtau,
+                    double* dJ_dUin) {
+    if (!c) return seterr(HB_ERR_ARG, "ctx is NULL");
+    std::string e;
+    const int rc = hb::adjoint_run(c, cfg, true, J, dJ_dF, dJ_dtau, dJ_dUin, e);
+    return rc ? seterr(rc, "%s", e.c_str()) : HB_OK;
+}
+
+int hb_adjoint_timing(hb_ctx* c, float* ms_forward, float* ms_reverse, int64_t* forward_steps,
+                      int64_t* reverse_steps) {
+    if (!c) return seterr(HB_ERR_ARG, "ctx is NULL");
+    if (hb::adjoint_timing(c, ms_forward, ms_reverse, forward_steps, reverse_steps))
+        return seterr(HB_ERR_STATE, "no adjoint call has run on this context");
     return HB_OK;
 }
 

@@ -51,6 +51,8 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     int wall_moving[hb::MAX_WALLS];
 };
 
+namespace hb { struct hb_adj; }
+
 struct hb_ctx {
     hb_params P;
     int X = 0, Y = 0, Z = 0;
@@ -99,6 +101,7 @@ struct hb_ctx {
     bool reduce_pending = false; // element forces lag the last lattice step
     int kernels_per_cycle = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    hb::hb_adj* adj = nullptr;  // adjoint buffers (checkpoints, tape), allocated on first use
 };
 
 // launchers implemented in the .cu files (all enqueue on ctx->stream)
@@ -119,4 +122,8 @@ void launch_couple_reduce(hb_ctx* c);
 void launch_fs_step(hb_ctx* c, int cur);
 int fs_init(hb_ctx* c);
 int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o);
+int adjoint_run(hb_ctx* c, const hb_adjoint_cfg* cfg, bool reverse, double* J, double* dF, double* dtau,
+                double* duin, std::string& err);
+int adjoint_timing(hb_ctx* c, float* ms_forward, float* ms_reverse, int64_t* fwd_steps, int64_t* rev_steps);
+void adjoint_free(hb_ctx* c);
 }  // namespace hb

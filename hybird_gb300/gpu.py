@@ -43,6 +43,9 @@ def lib():
     L.hb_get_status.argtypes = [vp, P(abi.HbStatus)]
     L.hb_time_cycles.argtypes = [vp, C.c_int32, P(C.c_float), P(C.c_float), P(C.c_int32)]
     L.hb_profile_phases.argtypes = [vp, C.c_int32, vp, P(C.c_int32)]
+    L.hb_adjoint_forward.argtypes = [vp, P(abi.HbAdjointCfg), vp]
+    L.hb_adjoint_drag.argtypes = [vp, P(abi.HbAdjointCfg), vp, vp, vp, vp]
+    L.hb_adjoint_timing.argtypes = [vp, P(C.c_float), P(C.c_float), P(C.c_int64), P(C.c_int64)]
     _lib = L
     return L
 
@@ -142,3 +145,36 @@ class GpuSim:
         tot, lbk, kpc = C.c_float(0), C.c_float(0), C.c_int32(0)
         check(self.L.hb_time_cycles(self.h, n, C.byref(tot), C.byref(lbk), C.byref(kpc)))
         return tot.value, lbk.value, kpc.value
+
+    # ---- adjoint (reverse) entry points -------------------------------------------------
+    def _adjoint_cfg(self, steps, checkpoint_every, precision, tau, force, inlet, axis):
+        Y, Z = self.params.lb_size[1], self.params.lb_size[2]
+        self._inlet = None if inlet is None else np.ascontiguousarray(inlet, dtype=np.float64).reshape(-1)
+        if self._inlet is not None and self._inlet.size != Y * Z:
+            raise ValueError(f"inlet field must hold Y*Z = {Y * Z} values")
+        cfg = abi.HbAdjointCfg()
+        cfg.steps, cfg.checkpoint_every, cfg.precision, cfg.drag_axis = steps, checkpoint_every, precision, axis
+        cfg.tau = tau
+        cfg.body_force[:] = list(force)
+        cfg.inlet_velocity = abi.dptr(self._inlet)
+        return cfg
+
+    def adjoint_forward(self, steps, tau, force, inlet=None, precision=abi.HB_FP64, checkpoint_every=100, axis=0):
+        """Object drag J after `steps` steps from the current state."""
+        cfg = self._adjoint_cfg(steps, checkpoint_every, precision, tau, force, inlet, axis)
+        J = np.zeros(1)
+        check(self.L.hb_adjoint_forward(self.h, C.byref(cfg), _p(J)))
+        return float(J[0])
+
+    def adjoint_drag(self, steps, tau, force, inlet=None, precision=abi.HB_FP64, checkpoint_every=100, axis=0):
+        """J and (dJ/dF[3], dJ/dtau, dJ/du_in[Y*Z]) by the reverse kernel."""
+        cfg = self._adjoint_cfg(steps, checkpoint_every, precision, tau, force, inlet, axis)
+        Y, Z = self.params.lb_size[1], self.params.lb_size[2]
+        J, dF, dtau, duin = np.zeros(1), np.zeros(3), np.zeros(1), np.zeros(Y * Z)
+        check(self.L.hb_adjoint_drag(self.h, C.byref(cfg), _p(J), _p(dF), _p(dtau), _p(duin)))
+        return float(J[0]), dF, float(dtau[0]), duin
+
+    def adjoint_timing(self):
+        f, r, nf, nr = C.c_float(0), C.c_float(0), C.c_int64(0), C.c_int64(0)
+        check(self.L.hb_adjoint_timing(self.h, C.byref(f), C.byref(r), C.byref(nf), C.byref(nr)))
+        return f.value, r.value, nf.value, nr.value

@@ -194,6 +194,39 @@ int hb_time_cycles(hb_ctx* ctx, int32_t nsteps, float* ms_total, float* ms_lb_ke
  * three coupling-mask passes.  us must hold 4 + 2*multiStep values. */
 int hb_profile_phases(hb_ctx* ctx, int32_t nsteps, double* us, int32_t* nphases);
 
+/* ---- reverse (adjoint) ------------------------------------------------------------- */
+/* No counterpart in the reference (it has no derivative code).  Objective: J = total
+ * drag on the context's objects (fixed spheres, which the lattice holds as static wall
+ * nodes, LB.cpp:535-550) along drag_axis, measured in the last of `steps` single-phase
+ * steps: the sum over fluid->object links of 2 (fs_j - w_j rho0) c_j, the reference's
+ * node::bounceBackForce (node.cpp:283-291) with BBi = 0.  The run starts from the
+ * context's current populations (not changed by the call) and uses, instead of the
+ * context's values, the relaxation time tau (TRT magic parameter and collision kind from
+ * hb_params), the uniform body force F and the inlet field: moving-wall nodes (code 8)
+ * on the planes x = 0 and x = X-1 move with velocity (u_in[y + Y*z], 0, 0); other
+ * moving walls keep their node velocity.  Single-phase lattices only: no free surface,
+ * no Bingham/Smagorinsky viscosity, no DEM elements (HB_ERR_UNSUPPORTED otherwise).
+ * The gradient is taken by a hand-written reverse kernel with checkpoints of the state
+ * every checkpoint_every steps in device memory and recomputation of each segment. */
+typedef struct hb_adjoint_cfg {
+    int32_t steps;             /* T >= 1                                                    */
+    int32_t checkpoint_every;  /* K >= 1                                                    */
+    int32_t precision;         /* HB_FP32 or HB_FP64: storage and arithmetic of the run     */
+    int32_t drag_axis;         /* 0, 1, 2                                                   */
+    double  tau;               /* relaxation time (> 0.5)                                   */
+    double  body_force[3];     /* lbF                                                       */
+    const double* inlet_velocity; /* host [Y*Z], index y + Y*z, or NULL for zero            */
+} hb_adjoint_cfg;
+/* Forward only: J (used for finite differences). */
+int hb_adjoint_forward(hb_ctx* ctx, const hb_adjoint_cfg* cfg, double* J);
+/* J and its gradient: dJ_dF[3], dJ_dtau[1], dJ_dUin[Y*Z] (host; any may be NULL). */
+int hb_adjoint_drag(hb_ctx* ctx, const hb_adjoint_cfg* cfg, double* J, double* dJ_dF,
+                    double* dJ_dtau, double* dJ_dUin);
+/* Device time of the last adjoint call: the first forward pass, and the reverse pass
+ * (segment recomputation + reverse steps); step counts of each. */
+int hb_adjoint_timing(hb_ctx* ctx, float* ms_forward, float* ms_reverse,
+                      int64_t* forward_steps, int64_t* reverse_steps);
+
 /* ---- allocation-free entry point ----------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory:
  * host drivers that run each solver step inside a CUDA stream capture, where

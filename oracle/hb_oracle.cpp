@@ -1216,4 +1216,28 @@ int hbo_dem_scalars(const hbo_sim* s, double* out) {
     return 0;
 }
 
+// Drag on the objects along one axis from the post-collision populations of the last
+// step: node::bounceBackForce (node.cpp:283-291) with BBi = 0, (2 (fs_j - w_j rho0)) c_j,
+// summed over every link from an active node to a static wall node inside an object
+// sphere (the node set LB.cpp:535-550 turns into walls), in node order.
+double hbo_object_drag(const hbo_sim* s, int axis) {
+    std::vector<uint8_t> isObj(s->N, 0);
+    for (size_t i = 0; i < s->N; ++i) {
+        if (s->type[i] != 7) continue;
+        for (const Object& ob : s->obj)
+            if (norm2(sub(s->pos(i), ob.x0)) < ob.r * ob.r) { isObj[i] = 1; break; }
+    }
+    double J = 0.0;
+    for (size_t i = 0; i < s->N; ++i) {
+        if (!s->isActive(i)) continue;
+        for (int j = 1; j < Q; ++j) {
+            if (!isObj[s->nb[i * Q + j]]) continue;
+            const V3 c = cvec(j);
+            const double ca = axis == 0 ? c.x : (axis == 1 ? c.y : c.z);
+            J += 2.0 * (s->fs[i * Q + j] - W[j] * 1.0) * ca;
+        }
+    }
+    return J;
+}
+
 }  // extern "C"

@@ -47,6 +47,8 @@ int64_t hbo_get_interface(const hbo_sim* s, uint32_t* cells, int64_t capacity);
 int hbo_get_walls(const hbo_sim* s, double* fhydro, double* fparticle, int32_t* nwalls);
 double hbo_total_mass(const hbo_sim* s);
 int hbo_dem_scalars(const hbo_sim* s, double* out /* demTime,maxDisp,nebrRange,deltat */);
+/* drag on the objects along axis from the last step's post-collision populations */
+double hbo_object_drag(const hbo_sim* s, int axis);
 
 #ifdef __cplusplus
 }

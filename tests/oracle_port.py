@@ -51,6 +51,8 @@ def oracle_lib():
     lib.hbo_total_mass.argtypes = [C.c_void_p]
     lib.hbo_dem_scalars.argtypes = [C.c_void_p, C.c_void_p]
     lib.hbo_set_threads.argtypes = [C.c_int]
+    lib.hbo_object_drag.restype = C.c_double
+    lib.hbo_object_drag.argtypes = [C.c_void_p, C.c_int]
     _lib = lib
     return lib
 
@@ -99,6 +101,24 @@ class OracleSim:
 
     def set_lattice(self, f=None, n=None, u=None, mass=None, visc=None):
         self.lib.hbo_set_lattice(self.h, _p(f), _p(n), _p(u), _p(mass), _p(visc))
+
+    def object_drag(self, axis=0):
+        return self.lib.hbo_object_drag(self.h, axis)
+
+    def set_inlet(self, inlet):
+        """Moving-wall nodes of the planes x = 0 and x = X-1 move along x with
+        inlet[y + Y*z] (the node velocity the moving-wall bounce-back reads)."""
+        X, Y, Z = self.params.lb_size
+        lat = self.lattice()
+        u = lat["u"].reshape(3, Z, Y, X).copy()
+        t = lat["type"].reshape(Z, Y, X)
+        uin = np.asarray(inlet, dtype=np.float64).reshape(Z, Y)
+        for xp in (0, X - 1):
+            m = t[:, :, xp] == 8
+            u[0, :, :, xp][m] = uin[m]
+            u[1, :, :, xp][m] = 0.0
+            u[2, :, :, xp][m] = 0.0
+        self.set_lattice(u=np.ascontiguousarray(u.reshape(-1)))
 
     def elements(self):
         E = self.E
