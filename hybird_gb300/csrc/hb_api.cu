@@ -244,11 +244,12 @@ int hb_destroy(hb_ctx* c) {
     if (c->graph) cudaGraphDestroy(c->graph);
     if (c->graph2) cudaGraphDestroy(c->graph2);
     void* ptrs[] = {c->ntype, c->solid, c->fA, c->fB, c->mode, c->rho, c->u, c->hf, c->mass,
-                    c->visc, c->dv, c->claim, c->status, c->wall_part, c->wall_force, c->fs_force, c->fs_mass2,
+                    c->visc, c->dv, c->hacc, c->status, c->wall_part, c->wall_force, c->fs_force, c->fs_mass2,
                     c->fs_cnt, c->fs_scal, c->fs_flag, c->fs_first, c->fs_part, c->lb_force, c->lb_force_f, c->d.pf, c->d.plain,
                     c->d.base, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
-                    c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r};
+                    c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
+                    c->d.claim_list, c->d.claim_cnt, c->d.boxes};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -265,9 +266,16 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     const long long N = c->N;
     const size_t tsz = c->P.precision == HB_FP64 ? 8 : 4;
     if (c->d.E > 0) {
-        if (!c->dv && (rc = dalloc((uint8_t**)&c->dv, 3 * N * tsz))) return rc;
-        if (!c->claim && (rc = dalloc(&c->claim, N))) return rc;
-        CK(cudaMemset(c->claim, 0xFF, sizeof(unsigned long long) * N));
+        if (c->P.precision == HB_FP64) {
+            if (!c->dv && (rc = dalloc((uint8_t**)&c->dv, 3 * N * tsz))) return rc;
+        } else {
+            if (!c->hacc && (rc = dalloc(&c->hacc, 7 * (size_t)c->d.E))) return rc;
+            CK(cudaMemset(c->hacc, 0, sizeof(unsigned long long) * 7 * c->d.E));
+        }
+        if (!c->d.claim_list && (rc = dalloc(&c->d.claim_list, 2 * N))) return rc;
+        if (!c->d.claim_cnt && (rc = dalloc(&c->d.claim_cnt, 1))) return rc;
+        if (!c->d.boxes && (rc = dalloc((uint8_t**)&c->d.boxes, (size_t)c->d.E * 128))) return rc;
+        CK(cudaMemset(c->d.claim_cnt, 0, sizeof(int)));
     }
     if (!c->wall_part) {
         const long long grid = (long long)ceil_div(c->X, c->X <= 64 ? 64 : (c->X <= 128 ? 128 : 256)) * (c->Y - 2) * (c->Z - 2);
@@ -337,6 +345,7 @@ static int enqueue_cycle(hb_ctx* c, int cur) {
     // R (element forces of the previous lattice step) + DEM substeps + coupling masks
     if (dem && launch_cycle_coop(c, 1, 1, c->P.lb_solve ? 1 : 0)) return -1;
     if (!c->P.lb_solve) return 0;
+    if (dem) launch_couple(c, false);
     if (c->P.free_surface) launch_fs_step(c, cur);
     launch_lb_step(c, cur);
     if (c->has_dynwall) launch_lb_wallforce(c, cur);
@@ -410,7 +419,7 @@ int hb_fs_step(hb_ctx* c) {
 int hb_coupling_step(hb_ctx* c) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
     if (c->P.dem_solve && c->d.E > 0) {
-        if (launch_cycle_coop(c, 0, 0, 1)) return seterr(HB_ERR_CUDA, "coupling launch: %s", cudaGetErrorString(cudaGetLastError()));
+        launch_couple(c, true);
     }
     CK(cudaGetLastError());
     return HB_OK;
@@ -604,13 +613,16 @@ int hb_get_status(hb_ctx* c, hb_status* s) {
 int hb_profile_phases(hb_ctx* c, int32_t nsteps, double* us, int32_t* nphases) {
     if (!c || !c->initialized || !us || !nphases) return seterr(HB_ERR_ARG, "null argument or not initialised");
     if (!(c->P.dem_solve && c->d.E > 0)) { *nphases = 0; return HB_OK; }
-    const int np = 1 + 2 * c->d.multi + 3 + 1;
+    const int np = 2 + 2 * c->d.multi;  // barrier stamps of the cooperative kernel
     unsigned long long* ts = nullptr;
     int rc = dalloc(&ts, (size_t)np * nsteps);
     if (rc) return rc;
     CK(cudaMemset(ts, 0, sizeof(unsigned long long) * np * nsteps));
+    std::vector<cudaEvent_t> ev(4 * (size_t)nsteps);
+    for (auto& e : ev) CK(cudaEventCreate(&e));
     for (int s = 0; s < nsteps; ++s) {
         if (launch_cycle_coop(c, 1, 1, 1, ts + (size_t)s * np)) { cudaFree(ts); return seterr(HB_ERR_CUDA, "cycle launch failed"); }
+        launch_couple(c, false, ev.data() + 4 * (size_t)s);
         if (c->P.free_surface) launch_fs_step(c, c->cur);
         launch_lb_step(c, c->cur);
         if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
@@ -628,7 +640,17 @@ int hb_profile_phases(hb_ctx* c, int32_t nsteps, double* us, int32_t* nphases) {
         for (int s = 0; s < nsteps; ++s) acc += (double)(h[(size_t)s * np + k + 1] - h[(size_t)s * np + k]) * 1e-3;
         us[k] = acc / nsteps;
     }
-    *nphases = nint;
+    for (int k = 0; k < 3; ++k) {  // coupling: list reset, mask pass (pop + claim), commit
+        double acc = 0.0;
+        for (int s = 0; s < nsteps; ++s) {
+            float m = 0.f;
+            CK(cudaEventElapsedTime(&m, ev[4 * (size_t)s + k], ev[4 * (size_t)s + k + 1]));
+            acc += m * 1e3;
+        }
+        us[nint + k] = acc / nsteps;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    *nphases = nint + 3;
     return HB_OK;
 }
 
@@ -658,6 +680,7 @@ int hb_time_cycles(hb_ctx* c, int32_t nsteps, float* ms_total, float* ms_lb_kern
         const bool dem = c->P.dem_solve && c->d.E > 0;
         for (int s = 0; s < nsteps; ++s) {
             if (dem && launch_cycle_coop(c, 1, 1, 1)) return seterr(HB_ERR_CUDA, "cycle launch failed");
+            if (dem) launch_couple(c, false);
             if (c->P.free_surface) launch_fs_step(c, c->cur);
             CK(cudaEventRecord(ev[2 * s], c->stream));
             launch_lb_step(c, c->cur);

@@ -30,6 +30,11 @@ constexpr int NBR_CAP = 48;      // candidate neighbours kept per particle
 constexpr int OBJ_CAP = 16;      // objects in range kept per particle
 constexpr int STATUS_WORDS = 8;  // device status words (numeric, capacity, wait, ...)
 constexpr int PARTIAL_CAP = 4096;  // per-block partials of grid-wide reductions (>= any grid used)
+// fixed-point scale of the element force/torque/volume sums of the reduced-precision
+// lattice kernels: 64-bit integer sums are exact and order-free, so the atomics that
+// build them give the same bits on every run
+constexpr double HACC_SCALE = 274877906944.0;  // 2^38
+constexpr double HACC_INV = 1.0 / 274877906944.0;
 
 // D3Q19 velocity set in the reference's order O,x,y,z,xy,yz,zx (lattice.h:36-60)
 __host__ __device__ constexpr int cx(int j) {
@@ -126,7 +131,8 @@ struct LBArgs {
     double* hf;             // [3N]
     double* mass;
     void* visc;             // T[N] when viscosity is persistent
-    void* dv;               // T[3N] direct-forcing term of inside nodes
+    void* dv;               // T[3N] direct-forcing term of inside nodes (FP64 kernel)
+    unsigned long long* hacc;  // [7E] fixed-point F, M, fluid volume per element (FP32/FP16 kernels)
     const double* F;        // device body force [3] (zero when forceFieldSolve = 0)
     const float* Ff;        // the same force in FP32 for the reduced-precision kernels
     int ne[Q];              // index offset of link j for nodes whose links do not wrap

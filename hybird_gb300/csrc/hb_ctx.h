@@ -29,6 +29,9 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     int* wall_of = nullptr;     // [E] first wall in range or -1
     int* obj = nullptr;         // [E*OBJ_CAP]
     int* obj_cnt = nullptr;     // [E]
+    uint32_t* claim_list = nullptr;  // [2N] (node, particle) pairs joined by the coupling in this step
+    int* claim_cnt = nullptr;
+    void* boxes = nullptr;      // [E] per-particle spheres of the current step (coupling masks)
     double* scal = nullptr;     // device scalars: [0]=maxDisp [1]=rebuild flag [2]=contacts
     int* contacts = nullptr;    // overlapping pairs counter of the last substep
     double* partial = nullptr;  // per-block maxima for the displacement trigger
@@ -73,7 +76,7 @@ struct hb_ctx {
     double* mass = nullptr;
     void* visc = nullptr;
     void* dv = nullptr;
-    unsigned long long* claim = nullptr;
+    unsigned long long* hacc = nullptr;  // [7E] fixed-point element sums of the FP32/FP16 kernels
     int* status = nullptr;      // [STATUS_WORDS]
     double* wall_part = nullptr;
     double* wall_force = nullptr;   // [MAX_WALLS*3 + 1]
@@ -116,7 +119,8 @@ int launch_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside,
                           const uint32_t* solid, const double* f, const double* n, const double* u,
                           const double* mass, const double* visc);
 int launch_download_lattice(hb_ctx* c, double* f_dev, int which_parity);
-int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_couple, unsigned long long* ts = nullptr);
+int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsigned long long* ts = nullptr);
+void launch_couple(hb_ctx* c, bool build_boxes, cudaEvent_t* ev = nullptr);
 void launch_dem_first_predict(hb_ctx* c);
 void launch_couple_reduce(hb_ctx* c);
 void launch_fs_step(hb_ctx* c, int cur);

@@ -196,128 +196,13 @@ __device__ void nl_build_one(const DemArgs& a, int i) {
 }
 
 // ---- forces (DEM.cpp:1114-1182, 1801-2136) --------------------------------------------
-__device__ void forces_one(const DemArgs& a, int i, int& ncont) {
-    const int E = a.E;
-    {
-        const V xpi = ld3(a.xp0, E, i);
-        V FP{0, 0, 0}, MP{0, 0, 0}, FW{0, 0, 0}, MW{0, 0, 0};
-        const int cnt = a.nbr_cnt[i];
-        for (int k = 0; k < cnt; ++k) {
-            const int j = a.nbr[(long long)i * NBR_CAP + k];
-            const int I = min(i, j), J = max(i, j);
-            const double rI = a.rad[I], rJ = a.rad[J];
-            const double sig = rI + rJ;
-            const V vd = sub(ld3(a.xp0, E, J), ld3(a.xp0, E, I));
-            if (!(nrm2(vd) < sig * sig)) continue;
-            if (i < j) ++ncont;
-            // particleParticleCollision with I = lower index (DEM.cpp:1801-1900)
-            const double dist = sqrt(nrm2(vd));
-            const double overlap = rI + rJ - dist;
-            const V relVel = sub(ld3(a.xp1, E, J), ld3(a.xp1, E, I));
-            const V en = divs(vd, dist);
-            const double vn = dot(relVel, en);
-            const V nrv = mul(vn, en);
-            const double mI = a.m[I], mJ = a.m[J];
-            const double effMass = mI * mJ / (mI + mJ);
-            const double effRad = rI * rJ / (rI + rJ);
-            const double fn = normal_contact(a, overlap, vn, effRad, effMass);
-            const V nf = mul(fn, en);
-            const V vrI = mul(rI, en), vrJ = mul(-rJ, en);
-            const V rvc = add(sub(relVel, cross(ld3(a.wpG, E, I), vrI)), cross(ld3(a.wpG, E, J), vrJ));
-            const V tang = sub(rvc, nrv);
-            const double nt = sqrt(nrm2(tang));
-            V tf{0, 0, 0};
-            const bool hasT = nt != 0.0;
-            if (hasT) {
-                const double ft = tangential_contact(a, nt, fn, effRad, effMass, a.muPart);
-                tf = mul(ft, divs(tang, nt));
-            }
-            if (i == I) {
-                FP = sub(FP, nf);
-                if (hasT) { MP = add(MP, cross(vrI, tf)); FP = add(FP, tf); }
-            } else {
-                FP = add(FP, nf);
-                if (hasT) { MP = sub(MP, cross(vrJ, tf)); FP = sub(FP, tf); }
-            }
-        }
-        const double ri = a.rad[i], mi = a.m[i];
-        const V xpv = ld3(a.xp1, E, i);
-        const V wpg = ld3(a.wpG, E, i);
-        const int w = a.wall_of[i];
-        if (w >= 0) {  // wallParticleCollision (DEM.cpp:1902-1982), static walls
-            const V wn{a.wn[w][0], a.wn[w][1], a.wn[w][2]};
-            const double dist = dot(wn, sub(xpi, V{a.wp[w][0], a.wp[w][1], a.wp[w][2]}));
-            const double overlap = ri - dist;
-            if (overlap > 0.0) {
-                const V relVel = sub(xpv, V{0, 0, 0});
-                const double vn = dot(relVel, wn);
-                const V nrv = mul(vn, wn);
-                const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
-                const V nf = mul(fn, wn);
-                const V vrJ = mul(-ri, wn);
-                FW = add(FW, nf);
-                const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
-                const double nt = sqrt(nrm2(tang));
-                if (nt != 0.0) {
-                    const double ft = tangential_contact(a, nt, fn, ri, mi, a.muWall);
-                    const V tfw = mul(ft, divs(tang, nt));
-                    MW = sub(MW, cross(vrJ, tfw));
-                    FW = sub(FW, tfw);
-                }
-            }
-        }
-        const int oc = a.obj_cnt[i];
-        for (int k = 0; k < oc; ++k) {  // objectParticleCollision (DEM.cpp:2060-2136)
-            const int o = a.obj[(long long)i * OBJ_CAP + k];
-            const V vd = sub(xpi, V{a.ox0[o], a.ox0[a.O + o], a.ox0[2 * a.O + o]});
-            const double dist = sqrt(nrm2(vd));
-            const double overlap = ri + a.orad[o] - dist;
-            if (!(overlap > 0.0)) continue;
-            const V en = mul(1.0 / dist, vd);
-            const V relVel = sub(xpv, V{a.ox1[o], a.ox1[a.O + o], a.ox1[2 * a.O + o]});
-            const double vn = dot(relVel, en);
-            const V nrv = mul(vn, en);
-            const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
-            const V nf = mul(fn, en);
-            const V vrJ = mul(-ri, en);
-            const V cJ = add(vrJ, V{0, 0, 0});
-            FW = add(FW, nf);
-            const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
-            const double nt = sqrt(nrm2(tang));
-            if (nt != 0.0) {
-                const double ft = tangential_contact(a, nt, fn, ri, mi, a.muPart);
-                const V tfo = mul(ft, divs(tang, nt));
-                MW = sub(MW, cross(cJ, tfo));
-                FW = sub(FW, tfo);
-            }
-        }
-        st3(a.FP, E, i, FP);
-        st3(a.MP, E, i, MP);
-        st3(a.FW, E, i, FW);
-        st3(a.MW, E, i, MW);
-        // Newton (DEM.cpp:1149-1181)
-        const double nv = a.numVisc;
-        const V FVisc = mul(-6.0 * M_PI * nv * ri, xpv);
-        const V MVisc = mul(-8.0 * M_PI * nv * ri * ri * ri, wpg);
-        const V x2 = add(divs(add(add(add(FVisc, ld3(a.FH, E, i)), FP), FW), mi), V{a.demF[0], a.demF[1], a.demF[2]});
-        st3(a.x2, E, i, x2);
-        const V mom = add(add(add(MVisc, ld3(a.MH, E, i)), MP), MW);
-        const Qt qp0 = ldq(a.qp0, E, i);
-        const V mBf = project(mom, qadj(qp0));
-        const V Iv = ld3(a.I, E, i);
-        const V wl = ld3(a.wpL, E, i);
-        const V waBf{(mBf.x + (Iv.y - Iv.z) * wl.y * wl.z) / Iv.x, (mBf.y + (Iv.z - Iv.x) * wl.z * wl.x) / Iv.y,
-                     (mBf.z + (Iv.x - Iv.y) * wl.x * wl.y) / Iv.z};
-        st3(a.w1, E, i, project(waBf, qp0));
-    }
-}
-
 // contacts of particle i by one warp: lanes take candidates (and objects) in list
 // order, the sums use a fixed xor-shuffle tree, so the result is reproducible
 __device__ void forces_warp(const DemArgs& a, int i, int lane, int& ncont) {
     const int E = a.E;
     const V xpi = ld3(a.xp0, E, i);
     V FP{0, 0, 0}, MP{0, 0, 0}, FW{0, 0, 0}, MW{0, 0, 0};
+    bool contrib = false;  // this lane added a contact, wall or object force
     const int cnt = a.nbr_cnt[i];
     for (int k = lane; k < cnt; k += 32) {
         const int j = a.nbr[(long long)i * NBR_CAP + k];
@@ -327,6 +212,7 @@ __device__ void forces_warp(const DemArgs& a, int i, int lane, int& ncont) {
         const V vd = sub(ld3(a.xp0, E, J), ld3(a.xp0, E, I));
         if (!(nrm2(vd) < sig * sig)) continue;
         if (i < j) ++ncont;
+        contrib = true;
         // particleParticleCollision with I = lower index (DEM.cpp:1801-1900)
         const double dist = sqrt(nrm2(vd));
         const double overlap = rI + rJ - dist;
@@ -366,6 +252,7 @@ __device__ void forces_warp(const DemArgs& a, int i, int lane, int& ncont) {
         const double dist = dot(wn, sub(xpi, V{a.wp[w][0], a.wp[w][1], a.wp[w][2]}));
         const double overlap = ri - dist;
         if (overlap > 0.0) {
+            contrib = true;
             const V relVel = sub(xpv, V{0, 0, 0});
             const double vn = dot(relVel, wn);
             const V nrv = mul(vn, wn);
@@ -390,6 +277,7 @@ __device__ void forces_warp(const DemArgs& a, int i, int lane, int& ncont) {
         const double dist = sqrt(nrm2(vd));
         const double overlap = ri + a.orad[o] - dist;
         if (!(overlap > 0.0)) continue;
+        contrib = true;
         const V en = mul(1.0 / dist, vd);
         const V relVel = sub(xpv, V{a.ox1[o], a.ox1[a.O + o], a.ox1[2 * a.O + o]});
         const double vn = dot(relVel, en);
@@ -408,24 +296,36 @@ __device__ void forces_warp(const DemArgs& a, int i, int lane, int& ncont) {
             FW = sub(FW, tfo);
         }
     }
+    // fixed xor-shuffle tree over the lanes; when at most lane 0 holds a force the tree
+    // would only add zeros to it, so it is skipped
+    const unsigned who = __ballot_sync(0xffffffffu, contrib);
     double v[12] = {FP.x, FP.y, FP.z, MP.x, MP.y, MP.z, FW.x, FW.y, FW.z, MW.x, MW.y, MW.z};
+    if (who & ~1u) {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
+        for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
-        for (int c = 0; c < 12; ++c) v[c] += __shfl_xor_sync(0xffffffffu, v[c], off);
+            for (int c = 0; c < 12; ++c) v[c] += __shfl_xor_sync(0xffffffffu, v[c], off);
+    }
     if (lane != 0) return;
-    FP = V{v[0], v[1], v[2]}; MP = V{v[3], v[4], v[5]}; FW = V{v[6], v[7], v[8]}; MW = V{v[9], v[10], v[11]};
-    st3(a.FP, E, i, FP);
-    st3(a.MP, E, i, MP);
-    st3(a.FW, E, i, FW);
-    st3(a.MW, E, i, MW);
-    // Newton (DEM.cpp:1149-1181)
+    st3(a.FP, E, i, V{v[0], v[1], v[2]});
+    st3(a.MP, E, i, V{v[3], v[4], v[5]});
+    st3(a.FW, E, i, V{v[6], v[7], v[8]});
+    st3(a.MW, E, i, V{v[9], v[10], v[11]});
+}
+
+// Newton (DEM.cpp:1149-1181): accelerations from the forces of this substep
+__device__ void newton_one(const DemArgs& a, int i) {
+    const int E = a.E;
+    const double ri = a.rad[i], mi = a.m[i];
+    const V xpv = ld3(a.xp1, E, i);
+    const V wpg = ld3(a.wpG, E, i);
     const double nv = a.numVisc;
     const V FVisc = mul(-6.0 * M_PI * nv * ri, xpv);
     const V MVisc = mul(-8.0 * M_PI * nv * ri * ri * ri, wpg);
-    const V x2 = add(divs(add(add(add(FVisc, ld3(a.FH, E, i)), FP), FW), mi), V{a.demF[0], a.demF[1], a.demF[2]});
+    const V x2 = add(divs(add(add(add(FVisc, ld3(a.FH, E, i)), ld3(a.FP, E, i)), ld3(a.FW, E, i)), mi),
+                     V{a.demF[0], a.demF[1], a.demF[2]});
     st3(a.x2, E, i, x2);
-    const V mom = add(add(add(MVisc, ld3(a.MH, E, i)), MP), MW);
+    const V mom = add(add(add(MVisc, ld3(a.MH, E, i)), ld3(a.MP, E, i)), ld3(a.MW, E, i));
     const Qt qp0 = ldq(a.qp0, E, i);
     const V mBf = project(mom, qadj(qp0));
     const V Iv = ld3(a.I, E, i);
@@ -433,6 +333,29 @@ __device__ void forces_warp(const DemArgs& a, int i, int lane, int& ncont) {
     const V waBf{(mBf.x + (Iv.y - Iv.z) * wl.y * wl.z) / Iv.x, (mBf.y + (Iv.z - Iv.x) * wl.z * wl.x) / Iv.y,
                  (mBf.z + (Iv.x - Iv.y) * wl.x * wl.y) / Iv.z};
     st3(a.w1, E, i, project(waBf, qp0));
+}
+
+// The same for one Cartesian component of an identity-orientation element (lane c of
+// its six: 0-2 linear, 3-5 angular).  With qp0 = identity both projections return their
+// argument, so the arithmetic per component is that of newton_one.
+__device__ double newton_plain(const DemArgs& a, int i, int c) {
+    const int E = a.E;
+    const double ri = a.rad[i];
+    const double nv = a.numVisc;
+    if (c < 3) {
+        const long long o = (long long)c * E + i;
+        const double fv = a.xp1[o] * (-6.0 * M_PI * nv * ri);
+        return (((fv + a.FH[o]) + a.FP[o]) + a.FW[o]) / a.m[i] + a.demF[c];
+    }
+    const int k = c - 3;
+    const long long o = (long long)k * E + i;
+    const double mv = a.wpG[o] * (-8.0 * M_PI * nv * ri * ri * ri);
+    const double mom = ((mv + a.MH[o]) + a.MP[o]) + a.MW[o];
+    const double Ix = a.I[i], Iy = a.I[E + i], Iz = a.I[2 * E + i];
+    const double wx = a.wpL[i], wy = a.wpL[E + i], wz = a.wpL[2 * E + i];
+    if (k == 0) return (mom + (Iy - Iz) * wy * wz) / Ix;
+    if (k == 1) return (mom + (Iz - Ix) * wz * wx) / Iy;
+    return (mom + (Ix - Iy) * wx * wy) / Iz;
 }
 
 __device__ void predict_one(const DemArgs& a, int i) {  // elmt.cpp:139-177
@@ -565,6 +488,7 @@ __device__ double correct_predict_one(const DemArgs& a, int i) {
                            g1[4] * c[0] / c[3], g1[5] * c[0] / c[4]};
     const double c2o[6] = {g2[0] * c[1], g2[1] * c[1] / c[0], g2[2] * c[1] / c[1], g2[3] * c[1] / c[2],
                            g2[4] * c[1] / c[3], g2[5] * c[1] / c[4]};
+    newton_one(a, i);
     // loads
     const V x2 = ld3(a.x2, E, i), xp0 = ld3(a.xp0, E, i), xp1 = ld3(a.xp1, E, i), xp2 = ld3(a.xp2, E, i),
             xp3 = ld3(a.xp3, E, i), xp4 = ld3(a.xp4, E, i), xp5 = ld3(a.xp5, E, i);
@@ -639,7 +563,7 @@ __device__ double correct_predict_one(const DemArgs& a, int i) {
 // Gear corrector+predictor splits into independent Cartesian components.  Six lanes
 // per element: lanes 0-2 take x, y, z of the position chain, lanes 3-5 of the spin
 // chain.  Same arithmetic per component as correct_predict_one.
-__device__ double correct_predict_plain(const DemArgs& a, int i, int c) {
+__device__ double correct_predict_plain(const DemArgs& a, int i, int c, double acc) {
     const int E = a.E;
     const double dt = a.dt;
     const double cc[5] = {dt, dt * dt / 2.0, dt * dt * dt / 6.0, dt * dt * dt * dt / 24.0, dt * dt * dt * dt * dt / 120.0};
@@ -648,12 +572,12 @@ __device__ double correct_predict_plain(const DemArgs& a, int i, int c) {
         const double g2[6] = {3.0 / 16.0, 251.0 / 360.0, 1.0, 11.0 / 18.0, 1.0 / 6.0, 1.0 / 60.0};
         const double c2o[6] = {g2[0] * cc[1], g2[1] * cc[1] / cc[0], g2[2] * cc[1] / cc[1], g2[3] * cc[1] / cc[2],
                                g2[4] * cc[1] / cc[3], g2[5] * cc[1] / cc[4]};
-        const double x2 = a.x2[o], p0 = a.xp0[o], p1 = a.xp1[o], p2 = a.xp2[o], p3 = a.xp3[o], p4 = a.xp4[o],
+        const double x2 = acc, p0 = a.xp0[o], p1 = a.xp1[o], p2 = a.xp2[o], p3 = a.xp3[o], p4 = a.xp4[o],
                      p5 = a.xp5[o];
         const double d = x2 - p2;
         const double x0 = p0 + d * c2o[0], x1 = p1 + d * c2o[1], x3 = p3 + d * c2o[3], x4 = p4 + d * c2o[4],
                      x5 = p5 + d * c2o[5];
-        a.x0[o] = x0; a.x1[o] = x1; a.x3[o] = x3; a.x4[o] = x4; a.x5[o] = x5;
+        a.x0[o] = x0; a.x1[o] = x1; a.x2[o] = x2; a.x3[o] = x3; a.x4[o] = x4; a.x5[o] = x5;
         a.xp0[o] = x0 + x1 * cc[0] + x2 * cc[1] + x3 * cc[2] + x4 * cc[3] + x5 * cc[4];
         a.xp1[o] = x1 + x2 * cc[0] + x3 * cc[1] + x4 * cc[2] + x5 * cc[3];
         a.xp2[o] = x2 + x3 * cc[0] + x4 * cc[1] + x5 * cc[2];
@@ -667,12 +591,12 @@ __device__ double correct_predict_plain(const DemArgs& a, int i, int c) {
     const double g1[6] = {95.0 / 288.0, 1.0, 25.0 / 24.0, 35.0 / 72.0, 5.0 / 48.0, 1.0 / 120.0};
     const double c1o[6] = {g1[0] * cc[0], g1[1] * cc[0] / cc[0], g1[2] * cc[0] / cc[1], g1[3] * cc[0] / cc[2],
                            g1[4] * cc[0] / cc[3], g1[5] * cc[0] / cc[4]};
-    const double w1 = a.w1[o], p0 = a.wp0[o], p1 = a.wp1[o], p2 = a.wp2[o], p3 = a.wp3[o], p4 = a.wp4[o],
+    const double w1 = acc, p0 = a.wp0[o], p1 = a.wp1[o], p2 = a.wp2[o], p3 = a.wp3[o], p4 = a.wp4[o],
                  p5 = a.wp5[o];
     const double d = w1 - p1;
     const double w0 = p0 + d * c1o[0], w2 = p2 + d * c1o[2], w3 = p3 + d * c1o[3], w4 = p4 + d * c1o[4],
                  w5 = p5 + d * c1o[5];
-    a.w0[o] = w0; a.w2[o] = w2; a.w3[o] = w3; a.w4[o] = w4; a.w5[o] = w5;
+    a.w0[o] = w0; a.w1[o] = w1; a.w2[o] = w2; a.w3[o] = w3; a.w4[o] = w4; a.w5[o] = w5;
     a.wG[o] = w0;
     a.wL[o] = w0;
     const double n0 = w0 + w1 * cc[0] + w2 * cc[1] + w3 * cc[2] + w4 * cc[3] + w5 * cc[4];
@@ -703,11 +627,14 @@ struct CoupleArgs {
     int per[6];
     uint8_t* ntype;
     uint32_t* solid;
-    unsigned long long* claim;
     const double *x0, *rad;
     int E;
     const void* dv;
     int dv_f64;
+    const unsigned long long* hacc;  // fixed-point element sums (FP32/FP16 lattice kernels)
+    uint32_t* claim_list;       // [2N] (node, particle) joined in this step
+    int* claim_cnt;
+    struct PartBox* tab;        // [E] spheres of the current step
     const double* mass;
     int free_surface;
     double *FH, *MH, *fvol;
@@ -732,113 +659,174 @@ __device__ __forceinline__ Box pbox(const CoupleArgs& a, int p, int margin) {
     return b;
 }
 // insideSphere (vector.cpp:153-158) is decided in FP64 with the reference's expression;
-// an FP32 screen settles the nodes far from the surface, because the FP64 pipe of this
-// part is narrow (relative screen margin 1e-3, FP32 error below 1e-5 for boxes <= 256)
+// an FP32 screen settles every node whose FP32 distance is farther from the sphere
+// surface than a rigorous bound of its own rounding error, because the FP64 pipe of this
+// part is narrow.  The centre is kept as integer + fraction, so the screen's error does
+// not grow with the lattice size:
+//   dx_f = f32(x - ix) - f32(cx - ix): |dx_f - dx| <= u (1 + |dx|),  u = 2^-24,
+//   |d2_f - d2| <= 3 u (1 + B)(2B + 1) + 12 u B^2  for |dx|, |dy|, |dz| <= B = 2r,
+// and nodes farther than 2r are far outside whatever the rounding.  The window
+// [lo, hi] = r^2 -/+ (that bound + 1e-9) is rounded outwards.
 struct Sph {
     double cx, cy, cz, r2;
-    float fx, fy, fz, r2f;
+    int ix, iy, iz;
+    float fx, fy, fz, lo, hi;
 };
 __device__ __forceinline__ Sph load_sph(const CoupleArgs& a, int p) {
     const int E = a.E;
     Sph s;
     s.cx = a.x0[p]; s.cy = a.x0[E + p]; s.cz = a.x0[2 * E + p];
-    s.r2 = a.rad[p] * a.rad[p];
-    s.fx = (float)s.cx; s.fy = (float)s.cy; s.fz = (float)s.cz; s.r2f = (float)s.r2;
+    const double r = a.rad[p];
+    s.r2 = r * r;
+    s.ix = (int)floor(s.cx); s.iy = (int)floor(s.cy); s.iz = (int)floor(s.cz);
+    s.fx = (float)(s.cx - s.ix); s.fy = (float)(s.cy - s.iy); s.fz = (float)(s.cz - s.iz);
+    const double u = 5.9604644775390625e-8, B = 2.0 * r;
+    const double M = 3.0 * u * (1.0 + B) * (2.0 * B + 1.0) + 12.0 * u * B * B + 1e-9;
+    s.lo = __double2float_rd(s.r2 - M);
+    s.hi = __double2float_ru(s.r2 + M);
     return s;
 }
+// exact int -> float for |v| < 2^22 on the FP32 pipe: the bits of 1.5 * 2^23 + v, minus 1.5 * 2^23
+__device__ __forceinline__ float i2f_small(int v) { return __int_as_float(0x4B400000 + v) - 12582912.0f; }
+
 __device__ __forceinline__ bool in_sph(const Sph& s, int x, int y, int z) {
-    const float dxf = float(x) - s.fx, dyf = float(y) - s.fy, dzf = float(z) - s.fz;
+    const float dxf = i2f_small(x - s.ix) - s.fx, dyf = i2f_small(y - s.iy) - s.fy, dzf = i2f_small(z - s.iz) - s.fz;
     const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
-    if (d2f < 0.999f * s.r2f) return true;
-    if (d2f > 1.001f * s.r2f) return false;
+    if (d2f < s.lo) return true;
+    if (d2f > s.hi) return false;
     const double dx = x - s.cx, dy = y - s.cy, dz = z - s.cz;
     return dx * dx + dy * dy + dz * dz < s.r2;
 }
 
-// The coupling passes give each thread whole rows (fixed y, z) of a particle's box: one
-// row of node bytes is one or two cache lines, so a thread pays one memory latency per
-// row instead of one per node.
+// Sphere of every particle for the current step, built once per particle (FP64 is
+// narrow on this part; the mask kernel only reads the table).
+struct PartBox {
+    Sph s;
+};
+static_assert(sizeof(PartBox) <= 128, "the context allocates 128 bytes per particle");
 
-// findNewActive (LB.cpp:1921-1967): uncovered nodes leave the particle
-__device__ void pop_block(const CoupleArgs& a, int p) {
-    const Box b = pbox(a, p, 2);
-    const Sph s = load_sph(a, p);
-    for (int r = threadIdx.x; r < b.ny * b.nz; r += blockDim.x) {
-        const int y = b.y0 + r % b.ny, z = b.z0 + r / b.ny;
-        const long long base = (long long)a.X * ((long long)y + (long long)a.Y * z);
-        for (int xc = b.x0; xc < b.x0 + b.nx; xc += 8) {  // 8 loads in flight per chunk
-            uint8_t t8[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) t8[k] = xc + k < b.x0 + b.nx ? a.ntype[base + xc + k] : 0;
-            uint32_t s8[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) s8[k] = (t8[k] & HB_INSIDE) ? a.solid[base + xc + k] : 0xffffffffu;
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-                if (s8[k] == (uint32_t)p && !in_sph(s, xc + k, y, z)) a.ntype[base + xc + k] = t8[k] & ~HB_INSIDE;
-        }
-    }
+__device__ __forceinline__ void build_box(const CoupleArgs& a, int p) { a.tab[p].s = load_sph(a, p); }
+
+// Coupling masks, node-parallel (one thread per lattice node, coalesced):
+//  findNewActive (LB.cpp:1921-1967): a particle node no longer covered by its particle
+//    leaves it;
+//  findNewSolid (LB.cpp:1969-2033): a node that is not a particle node after that and is
+//    covered by particle q of one of its 6-linked source nodes m (a particle node that
+//    stays) joins q; among several sources the lowest node index m wins, the
+//    reference's first-in-particleNodes-order rule (that list is sorted).  Nodes that
+//    the reference would add through a source added in the same pass (a displacement
+//    above half a lattice unit per step) join in the next step.
+// Each node decides only for itself.  A source's own flag may be read before or after
+// its own pop; both give the same decision because a source must also still be covered
+// (in_sph).  New members are listed and joined by k_commit, so no node added in this
+// pass acts as a source in it.
+__device__ __forceinline__ void claim_push(const CoupleArgs& a, long long l, unsigned long long best) {
+    const int slot = atomicAdd(a.claim_cnt, 1);
+    a.claim_list[2 * slot] = (uint32_t)l;
+    a.claim_list[2 * slot + 1] = (uint32_t)(best & 0xffffffffu);
 }
 
-// findNewSolid (LB.cpp:1969-2033): a node covered by particle p and 6-linked from a
-// node of p becomes a particle node; the source node with the lowest index wins, which
-// is the reference's first-in-particleNodes-order rule (the list is sorted there)
-__device__ void claim_block(const CoupleArgs& a, int p) {
-    const Box b = pbox(a, p, 1);
-    const Sph s = load_sph(a, p);
-    for (int r = threadIdx.x; r < b.ny * b.nz; r += blockDim.x) {
-        const int y = b.y0 + r % b.ny, z = b.z0 + r / b.ny;
-        const long long base = (long long)a.X * ((long long)y + (long long)a.Y * z);
-        for (int x = b.x0; x < b.x0 + b.nx; ++x) {
-            const long long l = base + x;
-            if (a.ntype[l] & HB_INSIDE) continue;
-            if (!in_sph(s, x, y, z)) continue;
-            unsigned long long best = ~0ull;
-            for (int kk = 1; kk <= 6; ++kk) {  // source m with link d[m][kk] == l
-                int mx = x - cx(kk), my = y - cy(kk), mz = z - cz(kk);
-                if (mx == 0 && a.per[1]) mx = a.X - 2; else if (mx == a.X - 1 && a.per[0]) mx = 1;
-                if (my == 0 && a.per[3]) my = a.Y - 2; else if (my == a.Y - 1 && a.per[2]) my = 1;
-                if (mz == 0 && a.per[5]) mz = a.Z - 2; else if (mz == a.Z - 1 && a.per[4]) mz = 1;
-                if (mx < 0 || my < 0 || mz < 0 || mx >= a.X || my >= a.Y || mz >= a.Z) continue;
-                const long long m = (long long)mx + (long long)a.X * ((long long)my + (long long)a.Y * mz);
-                const uint8_t tm = a.ntype[m];
-                if (!(tm & HB_INSIDE) || a.solid[m] != (uint32_t)p) continue;
-                // the reference's link table: interior nodes link arithmetically (with the
-                // periodic remap), boundary nodes link to themselves
-                const bool interior = mx > 0 && my > 0 && mz > 0 && mx < a.X - 1 && my < a.Y - 1 && mz < a.Z - 1;
-                if (!interior) continue;
-                int lx = mx + cx(kk), ly = my + cy(kk), lz = mz + cz(kk);
-                if (lx == 0 && a.per[0]) lx = a.X - 2; else if (lx == a.X - 1 && a.per[1]) lx = 1;
-                if (ly == 0 && a.per[2]) ly = a.Y - 2; else if (ly == a.Y - 1 && a.per[3]) ly = 1;
-                if (lz == 0 && a.per[4]) lz = a.Z - 2; else if (lz == a.Z - 1 && a.per[5]) lz = 1;
-                if (lx != x || ly != y || lz != z) continue;
-                const unsigned long long key = ((unsigned long long)m << 32) | (unsigned)p;
-                if (key < best) best = key;
-            }
-            if (best != ~0ull) atomicMin(a.claim + l, best);
-        }
+// one node with the reference's full link rules (periodic remap, self-linked boundary)
+__device__ __noinline__ void mask_node_general(const CoupleArgs& a, int x, int y, int z) {
+    const long long l = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
+    const uint8_t t = a.ntype[l];
+    if (t & HB_INSIDE) {
+        const uint32_t q = a.solid[l];
+        if (in_sph(a.tab[q].s, x, y, z)) return;  // stays
+        a.ntype[l] = t & ~HB_INSIDE;              // pop
     }
+    unsigned long long best = ~0ull;
+    for (int kk = 1; kk <= 6; ++kk) {  // source m with link d[m][kk] == l
+        int mx = x - cx(kk), my = y - cy(kk), mz = z - cz(kk);
+        if (mx == 0 && a.per[1]) mx = a.X - 2; else if (mx == a.X - 1 && a.per[0]) mx = 1;
+        if (my == 0 && a.per[3]) my = a.Y - 2; else if (my == a.Y - 1 && a.per[2]) my = 1;
+        if (mz == 0 && a.per[5]) mz = a.Z - 2; else if (mz == a.Z - 1 && a.per[4]) mz = 1;
+        // the reference's link table: interior nodes link arithmetically (with the
+        // periodic remap), boundary nodes link to themselves
+        if (!(mx > 0 && my > 0 && mz > 0 && mx < a.X - 1 && my < a.Y - 1 && mz < a.Z - 1)) continue;
+        const long long m = (long long)mx + (long long)a.X * ((long long)my + (long long)a.Y * mz);
+        if (!(a.ntype[m] & HB_INSIDE)) continue;
+        int lx = mx + cx(kk), ly = my + cy(kk), lz = mz + cz(kk);
+        if (lx == 0 && a.per[0]) lx = a.X - 2; else if (lx == a.X - 1 && a.per[1]) lx = 1;
+        if (ly == 0 && a.per[2]) ly = a.Y - 2; else if (ly == a.Y - 1 && a.per[3]) ly = 1;
+        if (lz == 0 && a.per[4]) lz = a.Z - 2; else if (lz == a.Z - 1 && a.per[5]) lz = 1;
+        if (lx != x || ly != y || lz != z) continue;
+        const uint32_t q = a.solid[m];
+        const Sph& sq = a.tab[q].s;
+        if (!in_sph(sq, mx, my, mz) || !in_sph(sq, x, y, z)) continue;
+        const unsigned long long key = ((unsigned long long)m << 32) | q;
+        if (key < best) best = key;
+    }
+    if (best != ~0ull) claim_push(a, l, best);
 }
 
-__device__ void commit_block(const CoupleArgs& a, int p) {
-    const Box b = pbox(a, p, 1);
-    for (int r = threadIdx.x; r < b.ny * b.nz; r += blockDim.x) {
-        const int y = b.y0 + r % b.ny, z = b.z0 + r / b.ny;
-        const long long base = (long long)a.X * ((long long)y + (long long)a.Y * z);
-        for (int xc = b.x0; xc < b.x0 + b.nx; xc += 8) {  // 8 loads in flight per chunk
-            unsigned long long c8[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) c8[k] = xc + k < b.x0 + b.nx ? a.claim[base + xc + k] : ~0ull;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const unsigned long long c = c8[k];
-                if (c == ~0ull || (uint32_t)(c & 0xffffffffu) != (uint32_t)p) continue;
-                const long long l = base + xc + k;
-                a.ntype[l] = a.ntype[l] | HB_INSIDE;
-                a.solid[l] = (uint32_t)p;
-                a.claim[l] = ~0ull;
-            }
+__device__ __forceinline__ uint8_t byte_of(uint32_t w, int k) { return (uint8_t)(w >> (8 * k)); }
+
+// Four consecutive nodes of a row per thread, 4-byte loads of the node bytes of the row
+// and of the four neighbouring rows, so a thread's loads are in flight together.  Rows
+// near a periodic face, or of a length that is not a multiple of 4, take the general
+// per-node rules.
+__global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
+    const int x0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
+    if (x0 >= a.X || y >= a.Y) return;
+    const bool pnear = ((a.per[0] | a.per[1]) && (x0 < 2 || x0 + 3 > a.X - 3)) ||
+                       ((a.per[2] | a.per[3]) && (y < 2 || y > a.Y - 3)) ||
+                       ((a.per[4] | a.per[5]) && (z < 2 || z > a.Z - 3));
+    if ((a.X & 3) || pnear) {
+        for (int k = 0; k < 4 && x0 + k < a.X; ++k) mask_node_general(a, x0 + k, y, z);
+        return;
+    }
+    // without a periodic face nearby every link is plain arithmetic: a source is the
+    // interior node one step back, and its forward link lands here
+    const long long sy = a.X, sz = (long long)a.X * a.Y;
+    const long long l0 = (long long)x0 + sy * y + sz * z;
+    const bool iy = y >= 1 && y <= a.Y - 2, iz = z >= 1 && z <= a.Z - 2;
+    const uint32_t* w32 = reinterpret_cast<const uint32_t*>(a.ntype);
+    const uint32_t tw = w32[l0 >> 2];
+    const uint32_t wym = (y - 1 >= 1 && iz) ? w32[(l0 - sy) >> 2] : 0u;
+    const uint32_t wyp = (y + 1 <= a.Y - 2 && iz) ? w32[(l0 + sy) >> 2] : 0u;
+    const uint32_t wzm = (z - 1 >= 1 && iy) ? w32[(l0 - sz) >> 2] : 0u;
+    const uint32_t wzp = (z + 1 <= a.Z - 2 && iy) ? w32[(l0 + sz) >> 2] : 0u;
+    const uint8_t tl = (x0 - 1 >= 1 && iy && iz) ? a.ntype[l0 - 1] : (uint8_t)0;
+    const uint8_t tr = (x0 + 4 <= a.X - 2 && iy && iz) ? a.ntype[l0 + 4] : (uint8_t)0;
+    uint32_t sl[4] = {0u, 0u, 0u, 0u};
+    if (tw & 0x10101010u) {  // HB_INSIDE in any of the four bytes
+        const uint4 v = *reinterpret_cast<const uint4*>(a.solid + l0);
+        sl[0] = v.x; sl[1] = v.y; sl[2] = v.z; sl[3] = v.w;
+    }
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+        const int x = x0 + k;
+        const long long l = l0 + k;
+        const uint8_t t = byte_of(tw, k);
+        if (t & HB_INSIDE) {
+            if (in_sph(a.tab[sl[k]].s, x, y, z)) continue;  // stays
+            a.ntype[l] = t & ~HB_INSIDE;                     // pop
         }
+        const bool ix = x >= 1 && x <= a.X - 2;
+        // source flags in kk order: x-1, x+1, y-1, y+1, z-1, z+1 (pre- or post-pop)
+        uint8_t tm[6];
+        tm[0] = (x - 1 >= 1 && iy && iz) ? (k > 0 ? byte_of(tw, k - 1) : tl) : (uint8_t)0;
+        tm[1] = (x + 1 <= a.X - 2 && iy && iz) ? (k < 3 ? byte_of(tw, k + 1) : tr) : (uint8_t)0;
+        tm[2] = ix ? byte_of(wym, k) : (uint8_t)0;
+        tm[3] = ix ? byte_of(wyp, k) : (uint8_t)0;
+        tm[4] = ix ? byte_of(wzm, k) : (uint8_t)0;
+        tm[5] = ix ? byte_of(wzp, k) : (uint8_t)0;
+        if (!((tm[0] | tm[1] | tm[2] | tm[3] | tm[4] | tm[5]) & HB_INSIDE)) continue;
+        const long long ms[6] = {l - 1, l + 1, l - sy, l + sy, l - sz, l + sz};
+        unsigned long long best = ~0ull;
+#pragma unroll
+        for (int kk = 0; kk < 6; ++kk) {
+            if (!(tm[kk] & HB_INSIDE)) continue;
+            const long long m = ms[kk];
+            const uint32_t q = a.solid[m];
+            const Sph& sq = a.tab[q].s;
+            if (!in_sph(sq, x - cx(kk + 1), y - cy(kk + 1), z - cz(kk + 1)) || !in_sph(sq, x, y, z)) continue;
+            const unsigned long long key = ((unsigned long long)m << 32) | q;
+            if (key < best) best = key;
+        }
+        if (best != ~0ull) claim_push(a, l, best);
     }
 }
 
@@ -897,9 +885,26 @@ __device__ void reduce_block(const CoupleArgs& a, int p, double (*sh)[256]) {
     }
 }
 
+// the reduced-precision lattice kernels leave the same seven sums as 64-bit fixed-point
+// integers; converting them is the whole reduction
+__device__ __forceinline__ void convert_sums(const CoupleArgs& a, int p) {
+    const int E = a.E;
+    double v[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) v[k] = (double)(long long)a.hacc[(long long)k * E + p] * HACC_INV;
+    a.FH[p] = v[0]; a.FH[E + p] = v[1]; a.FH[2 * E + p] = v[2];
+    a.MH[p] = v[3]; a.MH[E + p] = v[4]; a.MH[2 * E + p] = v[5];
+    a.fvol[p] = v[6];
+}
+
 __global__ void __launch_bounds__(256) k_couple_reduce(CoupleArgs a) {
     __shared__ double sh[7][256];
     reduce_block(a, blockIdx.x, sh);
+}
+
+__global__ void k_convert_sums(CoupleArgs a) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < a.E) convert_sums(a, p);
 }
 
 // ---- one cooperative kernel per cycle --------------------------------------------------
@@ -908,11 +913,10 @@ __global__ void __launch_bounds__(256) k_couple_reduce(CoupleArgs a) {
 //   R  hydrodynamic force of every element from the previous lattice step
 //   D  multiStep DEM substeps: [neighbour rebuild] forces | correct + next predict +
 //      displacement trigger
-//   C  coupling masks: pop | claim | commit
 struct CycleArgs {
     DemArgs d;
     CoupleArgs c;
-    int do_reduce, do_dem, do_couple, multi;
+    int do_reduce, do_dem, do_boxes, multi;
     unsigned long long* ts;  // optional phase timestamps (ns), written by block 0 after each barrier
 };
 
@@ -936,8 +940,13 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
     const int gw = blockIdx.x + gridDim.x * (threadIdx.x >> 5);  // one warp per particle
     const int nw = gridDim.x * (blockDim.x >> 5);
     stamp(A, 0);
-    if (A.do_reduce)
-        for (int p = blockIdx.x; p < E; p += gridDim.x) reduce_block(A.c, p, sh);
+    if (A.do_reduce) {
+        if (A.c.hacc) {
+            for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) convert_sums(A.c, p);
+        } else {
+            for (int p = blockIdx.x; p < E; p += gridDim.x) reduce_block(A.c, p, sh);
+        }
+    }
     int k = 1;
     if (A.do_dem) {
         double maxDisp = A.d.scal[0];
@@ -973,7 +982,7 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
                     const bool on = grp < 5 && i < E;
                     const bool plain = on && A.d.plain[i];
                     double x1c = 0.0;
-                    if (plain) x1c = correct_predict_plain(A.d, i, c);
+                    if (plain) x1c = correct_predict_plain(A.d, i, c, newton_plain(A.d, i, c));
                     else if (on && c == 0) v2 = fmax(v2, correct_predict_one(A.d, i));
                     // |x1|^2 in the reference's order (x*x + y*y) + z*z, gathered at lane c = 0
                     const double y1 = __shfl_down_sync(0xffffffffu, x1c, 1);
@@ -1000,22 +1009,27 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
             if (rebuild) maxDisp = 0.0;
             __syncthreads();
         }
+        if (A.do_boxes)  // positions are final: boxes for the coupling passes
+            for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) build_box(A.c, p);
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             A.d.scal[0] = maxDisp;
             A.d.scal[1] = rebuild ? 1.0 : 0.0;
         }
     }
-    if (A.do_couple) {
-        grid.sync();
-        for (int p = blockIdx.x; p < E; p += gridDim.x) pop_block(A.c, p);
-        grid.sync();
-        stamp(A, k++);
-        for (int p = blockIdx.x; p < E; p += gridDim.x) claim_block(A.c, p);
-        grid.sync();
-        stamp(A, k++);
-        for (int p = blockIdx.x; p < E; p += gridDim.x) commit_block(A.c, p);
-        grid.sync();
-        stamp(A, k++);
+}
+
+// ---- coupling masks: separate full-occupancy kernels, one thread per (particle, row) --
+__global__ void __launch_bounds__(256) k_build_boxes(CoupleArgs a) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < a.E) build_box(a, p);
+}
+
+__global__ void __launch_bounds__(256) k_commit(CoupleArgs a) {
+    const int n = *a.claim_cnt;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const uint32_t l = a.claim_list[2 * q], p = a.claim_list[2 * q + 1];
+        a.ntype[l] = a.ntype[l] | HB_INSIDE;
+        a.solid[l] = p;
     }
 }
 
@@ -1077,12 +1091,15 @@ static CoupleArgs couple_args(hb_ctx* c) {
     for (int k = 0; k < 6; ++k) a.per[k] = c->P.boundary[k] == HB_T_PERIODIC;
     a.ntype = c->ntype;
     a.solid = c->solid;
-    a.claim = c->claim;
     a.x0 = c->d.x[0];
     a.rad = c->d.rad;
     a.E = c->d.E;
     a.dv = c->dv;
     a.dv_f64 = c->P.precision == HB_FP64;
+    a.hacc = c->P.precision == HB_FP64 ? nullptr : c->hacc;
+    a.claim_list = c->d.claim_list;
+    a.claim_cnt = c->d.claim_cnt;
+    a.tab = reinterpret_cast<PartBox*>(c->d.boxes);
     a.mass = c->mass;
     a.free_surface = c->P.free_surface;
     a.FH = c->d.FH; a.MH = c->d.MH; a.fvol = c->d.fvol;
@@ -1102,7 +1119,7 @@ int coop_grid(hb_ctx* c) {
     return cached;
 }
 
-int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_couple, unsigned long long* ts) {
+int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsigned long long* ts) {
     if (c->d.E == 0) return 0;
     CycleArgs A;
     A.ts = ts;
@@ -1110,7 +1127,7 @@ int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_couple, unsig
     A.c = couple_args(c);
     A.do_reduce = do_reduce;
     A.do_dem = do_dem;
-    A.do_couple = do_couple;
+    A.do_boxes = do_boxes;
     A.multi = c->d.multi;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)coop_grid(c));
@@ -1125,10 +1142,28 @@ int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_couple, unsig
     return cudaLaunchKernelEx(&cfg, k_cycle, A) == cudaSuccess ? 0 : -1;
 }
 
+// findNewActive + findNewSolid (LB.cpp:247-280); boxes come from the cooperative kernel
+// when it ran the DEM substeps of this cycle (build == false), else are built here.
+// ev (optional, 4 events) brackets the three passes for the phase profiler.
+void launch_couple(hb_ctx* c, bool build, cudaEvent_t* ev) {
+    if (c->d.E == 0) return;
+    CoupleArgs a = couple_args(c);
+    if (build) k_build_boxes<<<ceil_div(c->d.E, 256), 256, 0, c->stream>>>(a);
+    if (ev) cudaEventRecord(ev[0], c->stream);
+    cudaMemsetAsync(a.claim_cnt, 0, sizeof(int), c->stream);
+    if (ev) cudaEventRecord(ev[1], c->stream);
+    k_mask<<<dim3((unsigned)ceil_div(ceil_div(c->X, 4), 32), (unsigned)ceil_div(c->Y, 4), (unsigned)c->Z), dim3(32, 4),
+             0, c->stream>>>(a);
+    if (ev) cudaEventRecord(ev[2], c->stream);
+    k_commit<<<152, 256, 0, c->stream>>>(a);
+    if (ev) cudaEventRecord(ev[3], c->stream);
+}
+
 void launch_couple_reduce(hb_ctx* c) {
     if (c->d.E == 0) return;
     CoupleArgs a = couple_args(c);
-    k_couple_reduce<<<c->d.E, 256, 0, c->stream>>>(a);
+    if (a.hacc) k_convert_sums<<<ceil_div(c->d.E, 128), 128, 0, c->stream>>>(a);
+    else k_couple_reduce<<<c->d.E, 256, 0, c->stream>>>(a);
 }
 
 }  // namespace hb

@@ -567,6 +567,7 @@ LBArgs lb_args(hb_ctx* c, int cur) {
     a.mass = c->mass;
     a.visc = c->visc;
     a.dv = c->dv;
+    a.hacc = c->hacc;
     a.F = c->lb_force;
     a.Ff = c->lb_force_f;
     for (int j = 0; j < Q; ++j) a.ne[j] = cx(j) + c->X * (cy(j) + c->Y * cz(j));
@@ -650,6 +651,7 @@ void launch_lb_step(hb_ctx* c, int cur) {
         k_collide_stream<PolF64><<<g, block, 0, c->stream>>>(a);
         return;
     }
+    if (a.couple) cudaMemsetAsync(c->hacc, 0, sizeof(unsigned long long) * 7 * c->d.E, c->stream);
     launch_lb_step_dev(c, a);
 }
 

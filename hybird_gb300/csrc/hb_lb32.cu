@@ -55,24 +55,55 @@ __device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fou
     }
 }
 
+// Element sums of the coupling (LB.cpp:1853-1918) folded into the lattice step: the
+// nodes of one particle form runs of consecutive lanes along x; a segmented suffix sum
+// over each run (fixed shuffle pattern) leaves the run total in its first lane, which
+// adds it to the element's 64-bit fixed-point accumulators.  Integer sums do not depend
+// on the order of the atomics, so the result is reproducible bit for bit.
+__device__ __forceinline__ void element_sums_warp(unsigned long long* hacc, int E, int key, float* v) {
+    const unsigned full = 0xffffffffu;
+    if (!__any_sync(full, key >= 0)) return;
+    const int lane = threadIdx.x & 31;
+    const int knext = __shfl_down_sync(full, key, 1);
+    const int kprev = __shfl_up_sync(full, key, 1);
+    const unsigned ends = __ballot_sync(full, lane == 31 || knext != key);
+    const int tail = lane + __ffs(ends >> lane) - 1;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            const float o = __shfl_down_sync(full, v[k], off);
+            if (lane + off <= tail) v[k] += o;
+        }
+    }
+    if (key >= 0 && (lane == 0 || kprev != key)) {
+#pragma unroll
+        for (int k = 0; k < 7; ++k)
+            atomicAdd(hacc + (long long)k * E + key,
+                      (unsigned long long)__float2ll_rn(v[k] * float(HACC_SCALE)));
+    }
+}
+
 template <class P>
 __global__ void __launch_bounds__(128, 8) k_collide_stream_dev(LBArgs a) {
     using S = typename P::S;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y + 1;
     const int z = blockIdx.z + 1;
-    if (x >= a.X) return;
     const int N = (int)a.N;
     const int i = x + a.X * (y + a.Y * z);
     const S* fin = reinterpret_cast<const S*>(a.fin);
     S* fout = reinterpret_cast<S*>(a.fout);
-    const uint8_t t = a.ntype[i];
-    if (!is_active(t)) return;
+    // whole warps leave together so that the element sums below can use full-warp
+    // shuffles; single lanes leave after them
+    const uint8_t t = x < a.X ? a.ntype[i] : (uint8_t)HB_T_STATWALL;
+    const bool act = is_active(t);
+    if (!__any_sync(0xffffffffu, act)) return;
     const int mode = *a.mode;
     const uint8_t code = t & HB_TYPE_MASK;
     float f[Q];
 #pragma unroll
-    for (int j = 0; j < Q; ++j) f[j] = P::load(fin + j * N + i);
+    for (int j = 0; j < Q; ++j) f[j] = act ? P::load(fin + j * N + i) : 0.0f;
 
     float dn = 0.0f, mx = 0.0f, my = 0.0f, mz = 0.0f;
 #pragma unroll
@@ -88,21 +119,32 @@ __global__ void __launch_bounds__(128, 8) k_collide_stream_dev(LBArgs a) {
     if (!(n > 0.0f) || ux != ux || uy != uy || uz != uz) flag_status(a.status, 0);
 
     float hx = 0.0f, hy = 0.0f, hz = 0.0f;
-    if (a.couple && (t & HB_INSIDE)) {  // LB.cpp:1863-1904 with FP32 particle copies
-        const int p = (int)a.solid[i];
-        const int E = a.parts.count;
-        const float* pf = a.parts.pf;
-        const float rx = float(x) - pf[p], ry = float(y) - pf[E + p], rz = float(z) - pf[2 * E + p];
-        const float wx = pf[6 * E + p], wy = pf[7 * E + p], wz = pf[8 * E + p];
-        const float lvx = pf[3 * E + p] + (wy * rz - wz * ry);
-        const float lvy = pf[4 * E + p] + (wz * rx - wx * rz);
-        const float lvz = pf[5 * E + p] + (wx * ry - wy * rx);
-        const float lf = (a.free_surface ? float(a.mass[i]) : 1.0f) * inv;
-        const float dvx = lf * (ux - lvx), dvy = lf * (uy - lvy), dvz = lf * (uz - lvz);
-        hx = -dvx; hy = -dvy; hz = -dvz;
-        float* dv = reinterpret_cast<float*>(a.dv);
-        dv[i] = dvx; dv[N + i] = dvy; dv[2 * N + i] = dvz;
+    if (a.couple) {
+        int key = -1;
+        float v[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (act && (t & HB_INSIDE)) {  // LB.cpp:1863-1904 with FP32 particle copies
+            const int p = (int)a.solid[i];
+            const int E = a.parts.count;
+            const float* pf = a.parts.pf;
+            const float rx = float(x) - pf[p], ry = float(y) - pf[E + p], rz = float(z) - pf[2 * E + p];
+            const float wx = pf[6 * E + p], wy = pf[7 * E + p], wz = pf[8 * E + p];
+            const float lvx = pf[3 * E + p] + (wy * rz - wz * ry);
+            const float lvy = pf[4 * E + p] + (wz * rx - wx * rz);
+            const float lvz = pf[5 * E + p] + (wx * ry - wy * rx);
+            const float m = a.free_surface ? float(a.mass[i]) : 1.0f;
+            const float lf = m * inv;
+            const float dvx = lf * (ux - lvx), dvy = lf * (uy - lvy), dvz = lf * (uz - lvz);
+            hx = -dvx; hy = -dvy; hz = -dvz;
+            key = p;
+            v[0] = dvx; v[1] = dvy; v[2] = dvz;  // element F, M, fluidVolume (LB.cpp:1893-1899)
+            v[3] = ry * dvz - rz * dvy;
+            v[4] = rz * dvx - rx * dvz;
+            v[5] = rx * dvy - ry * dvx;
+            v[6] = m;
+        }
+        element_sums_warp(a.hacc, a.parts.count, key, v);
     }
+    if (!act) return;
     const float Fx = a.Ff[0] + hx, Fy = a.Ff[1] + hy, Fz = a.Ff[2] + hz;
     ux += 0.5f * Fx * inv;  // shiftVelocity
     uy += 0.5f * Fy * inv;
