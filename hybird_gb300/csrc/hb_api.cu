@@ -61,6 +61,9 @@ int check_params(const hb_params* p) {
     if (p->precision < HB_FP64 || p->precision > HB_FP16S) return seterr(HB_ERR_ARG, "precision");
     if (p->collision != HB_BGK && p->collision != HB_TRT) return seterr(HB_ERR_ARG, "collision");
     if (p->dem_solve && p->multi_step < 1) return seterr(HB_ERR_ARG, "multi_step must be >= 1");
+    const long long N = (long long)p->lb_size[0] * p->lb_size[1] * p->lb_size[2];
+    if (p->precision != HB_FP64 && 19LL * N >= (1LL << 31))  // 32-bit population offsets
+        return seterr(HB_ERR_UNSUPPORTED, "FP32/FP16 lattices are limited to 19 * nodes < 2^31 (%lld nodes)", N);
     return HB_OK;
 }
 }  // namespace

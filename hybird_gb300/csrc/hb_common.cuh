@@ -83,6 +83,7 @@ struct PolF64 {
     __device__ static __forceinline__ T load(const S* p) { return HB_LD(p); }
     __device__ static __forceinline__ void store(S* p, T v) { HB_ST(p, v); }
     __device__ static __forceinline__ S enc(T v) { return v; }
+    __device__ static __forceinline__ S enc_store(T v) { return v; }
 };
 struct PolF32 {
     using S = float;
@@ -91,6 +92,7 @@ struct PolF32 {
     __device__ static __forceinline__ T load(const S* p) { return HB_LD(p); }
     __device__ static __forceinline__ void store(S* p, T v) { HB_ST(p, v); }
     __device__ static __forceinline__ S enc(T v) { return v; }
+    __device__ static __forceinline__ S enc_store(T v) { return v; }
 };
 struct PolF16 {
     using S = __half;
@@ -105,6 +107,7 @@ struct PolF16 {
     __device__ static __forceinline__ void store(S* p, T v) {
         HB_ST(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(v * SCALE)));
     }
+    __device__ static __forceinline__ S enc_store(T v) { return __float2half_rn(v * SCALE); }
 };
 
 // ---- device-side views of the context ----------------------------------------------
@@ -136,6 +139,8 @@ struct LBArgs {
     const double* F;        // device body force [3] (zero when forceFieldSolve = 0)
     const float* Ff;        // the same force in FP32 for the reduced-precision kernels
     int ne[Q];              // index offset of link j for nodes whose links do not wrap
+    int jn[Q];              // j * N: start of direction j in a population array
+    int so[Q];              // j * N + ne[j]: push target of direction j from node 0
     float init_visc_f, trt_magic_f, plastic_visc_f, yield_stress_f, turb_const_f;
     double init_visc;
     int collision;

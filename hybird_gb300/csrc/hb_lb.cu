@@ -479,15 +479,16 @@ __global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype) {
     if (i >= a.N) return;
     uint8_t t = ntype[i];
     bool bulk = is_active(t);
-    bool wrap = false;
+    bool wrap = false;  // some link crosses a periodic face (checked over all 18 links)
     if (bulk) {
         const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
         if (x < 1 || y < 1 || z < 1 || x > a.X - 2 || y > a.Y - 2 || z > a.Z - 2) bulk = false;
-        for (int j = 1; j < Q && bulk; ++j) {
-            const long long l = init_link(a, pf.v, i, j);
-            if (!is_active(ntype[l])) bulk = false;
-            if (l != i + cx(j) + (long long)a.X * (cy(j) + (long long)a.Y * cz(j))) wrap = true;
-        }
+        else
+            for (int j = 1; j < Q; ++j) {
+                const long long l = init_link(a, pf.v, i, j);
+                if (!is_active(ntype[l])) bulk = false;
+                if (l != i + cx(j) + (long long)a.X * (cy(j) + (long long)a.Y * cz(j))) wrap = true;
+            }
     }
     uint8_t nt = bulk ? (t | HB_BULK) : (t & ~HB_BULK);
     nt = wrap ? (nt | HB_PWRAP) : (nt & ~HB_PWRAP);
@@ -570,7 +571,11 @@ LBArgs lb_args(hb_ctx* c, int cur) {
     a.hacc = c->hacc;
     a.F = c->lb_force;
     a.Ff = c->lb_force_f;
-    for (int j = 0; j < Q; ++j) a.ne[j] = cx(j) + c->X * (cy(j) + c->Y * cz(j));
+    for (int j = 0; j < Q; ++j) {
+        a.ne[j] = cx(j) + c->X * (cy(j) + c->Y * cz(j));
+        a.jn[j] = (int)(j * c->N);
+        a.so[j] = (int)(j * c->N) + a.ne[j];
+    }
     a.init_visc_f = (float)c->P.init_visc;
     a.trt_magic_f = (float)c->P.trt_magic;
     a.plastic_visc_f = (float)c->P.plastic_visc;

@@ -30,21 +30,40 @@ __device__ __forceinline__ int link32(const LBArgs& a, int x, int y, int z, int 
     return xn + a.X * (yn + a.Y * zn);
 }
 
-// one post-collision population of a node with non-trivial links (pull rules of
-// LB.cpp:1231-1356 seen from the sending node)
+// c_j . v with the zero components of c_j left out: without fast-math the compiler keeps
+// every 0 * v product, so the sums are spelled out per direction (all branches fold)
+__device__ __forceinline__ float cdot(int j, float vx, float vy, float vz) {
+    float r;
+    if (cx(j) != 0) {
+        r = cx(j) > 0 ? vx : -vx;
+        if (cy(j) != 0) r = cy(j) > 0 ? r + vy : r - vy;
+        if (cz(j) != 0) r = cz(j) > 0 ? r + vz : r - vz;
+    } else if (cy(j) != 0) {
+        r = cy(j) > 0 ? vy : -vy;
+        if (cz(j) != 0) r = cz(j) > 0 ? r + vz : r - vz;
+    } else {
+        r = cz(j) > 0 ? vz : -vz;
+    }
+    return r;
+}
+
+// One post-collision population of a node with non-trivial links, the pull rules of
+// LB.cpp:1231-1356 seen from the sending node.  (A form with selected target index and
+// value, keeping the lanes of a warp converged, measured slower on GB300 than this
+// branch chain.)
 template <class P>
-__device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fout, int N, int x, int y, int z,
-                                             int i, int j, float g, float n, float ux, float uy, float uz,
-                                             float usq) {
+__device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fout, int x, int y, int z, int i,
+                                             int j, float g, float n, float ux, float uy, float uz, float usq) {
     const int l = link32(a, x, y, z, j);
     const uint8_t lc = a.ntype[l] & HB_TYPE_MASK;
     const int o = opp(j);
+    const int N = (int)a.N;
     if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
         P::store(fout + j * N + l, g);
     } else if (lc == HB_T_STATWALL) {
         P::store(fout + o * N + i, g);
     } else if (lc == HB_T_GAS) {
-        const float vu = float(cx(j)) * ux + float(cy(j)) * uy + float(cz(j)) * uz;
+        const float vu = cdot(j, ux, uy, uz);
         const float w = float(wgt(j));
         P::store(fout + o * N + i, -g + w * (9.0f * vu * vu - 3.0f * usq));
     } else if (lc == HB_T_DYNWALL) {
@@ -84,26 +103,17 @@ __device__ __forceinline__ void element_sums_warp(unsigned long long* hacc, int 
     }
 }
 
+// The update of one node from its 19 post-streaming deviations f: moments, coupling,
+// collision, push.  Every lane of a warp calls it (act false for lanes without an active
+// node), because the element sums use full-warp shuffles.
 template <class P>
-__global__ void __launch_bounds__(128, 8) k_collide_stream_dev(LBArgs a) {
+__device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, int i, uint8_t t, bool act,
+                                        float* f) {
     using S = typename P::S;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y + 1;
-    const int z = blockIdx.z + 1;
     const int N = (int)a.N;
-    const int i = x + a.X * (y + a.Y * z);
-    const S* fin = reinterpret_cast<const S*>(a.fin);
     S* fout = reinterpret_cast<S*>(a.fout);
-    // whole warps leave together so that the element sums below can use full-warp
-    // shuffles; single lanes leave after them
-    const uint8_t t = x < a.X ? a.ntype[i] : (uint8_t)HB_T_STATWALL;
-    const bool act = is_active(t);
-    if (!__any_sync(0xffffffffu, act)) return;
     const int mode = *a.mode;
     const uint8_t code = t & HB_TYPE_MASK;
-    float f[Q];
-#pragma unroll
-    for (int j = 0; j < Q; ++j) f[j] = act ? P::load(fin + j * N + i) : 0.0f;
 
     float dn = 0.0f, mx = 0.0f, my = 0.0f, mz = 0.0f;
 #pragma unroll
@@ -144,6 +154,8 @@ __global__ void __launch_bounds__(128, 8) k_collide_stream_dev(LBArgs a) {
         }
         element_sums_warp(a.hacc, a.parts.count, key, v);
     }
+    // every link of this node is plain (no wall, no periodic wrap): fixed push offsets
+    const bool fast = (t & (HB_BULK | HB_PWRAP)) == HB_BULK;
     if (!act) return;
     const float Fx = a.Ff[0] + hx, Fy = a.Ff[1] + hy, Fz = a.Ff[2] + hz;
     ux += 0.5f * Fx * inv;  // shiftVelocity
@@ -160,7 +172,7 @@ __global__ void __launch_bounds__(128, 8) k_collide_stream_dev(LBArgs a) {
 #pragma unroll
         for (int j = 1; j < Q; j += 2) {
             const int o = j + 1;
-            const float vu = float(cx(j)) * ux + float(cy(j)) * uy + float(cz(j)) * uz;
+            const float vu = cdot(j, ux, uy, uz);
             const float w = float(wgt(j));
             const float ep = w * (dn + n * (4.5f * vu * vu - 1.5f * usq));
             const float d = (f[j] + f[o]) - 2.0f * ep;
@@ -191,34 +203,62 @@ __global__ void __launch_bounds__(128, 8) k_collide_stream_dev(LBArgs a) {
         a.u[i] = (double)ux; a.u[a.N + i] = (double)uy; a.u[2 * a.N + i] = (double)uz;
         a.hf[i] = (double)hx; a.hf[a.N + i] = (double)hy; a.hf[2 * a.N + i] = (double)hz;
     }
-    const bool fast = (t & (HB_BULK | HB_PWRAP)) == HB_BULK;
 
-    {  // rest population
-        const float w0 = float(wgt(0));
-        const float e0 = w0 * (dn + n * (-1.5f * usq));
-        P::store(fout + i, f[0] - wp * (f[0] - e0) + ap * (w0 * (-3.0f * uF)));
+    // Pairwise collision with per-node coefficients for the two link weights (w = 1/18 on
+    // the axes, 1/36 on the diagonals), S = g_j + g_o, D = g_j - g_o, base = dn - 1.5 n u^2:
+    //   sym  = (1 - w+) S/2 + w+ w (base + 4.5 n vu^2) + a+ w (9 vu cF - 3 uF)
+    //   anti = (1 - w-) D/2 + w- 3 w n vu + a- 3 w cF
+    const float base = dn - 1.5f * n * usq;
+    const float c1 = 0.5f * (1.0f - wp), c2 = 0.5f * (1.0f - wm);
+    const float kb = wp * base - 3.0f * ap * uF;
+    float K0[2], Kq[2], Kc[2], Lu[2], Lf[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const float w = q == 0 ? float(1.0 / 18.0) : float(1.0 / 36.0);
+        K0[q] = w * kb;
+        Kq[q] = 4.5f * wp * w * n;
+        Kc[q] = 9.0f * ap * w;
+        Lu[q] = 3.0f * wm * w * n;
+        Lf[q] = 3.0f * am * w;
     }
+    S* fo = fout + i;
+    fo[0] = P::enc_store(2.0f * c1 * f[0] + float(wgt(0)) * kb);  // rest population
 #pragma unroll
     for (int j = 1; j < Q; j += 2) {
         const int o = j + 1;
-        const float w = float(wgt(j));
-        const float vu = float(cx(j)) * ux + float(cy(j)) * uy + float(cz(j)) * uz;
-        const float cF = float(cx(j)) * Fx + float(cy(j)) * Fy + float(cz(j)) * Fz;
-        const float ep = w * (dn + n * (4.5f * vu * vu - 1.5f * usq));
-        const float em = 3.0f * w * n * vu;
-        const float fp = 0.5f * (f[j] + f[o]), fm = 0.5f * (f[j] - f[o]);
-        const float Fs = w * (9.0f * vu * cF - 3.0f * uF), Fa = 3.0f * w * cF;
-        const float sym = fp - wp * (fp - ep) + ap * Fs;
-        const float anti = fm - wm * (fm - em) + am * Fa;
+        const int q = j <= 6 ? 0 : 1;
+        const float vu = cdot(j, ux, uy, uz);
+        const float cF = cdot(j, Fx, Fy, Fz);
+        const float sym = fmaf(c1, f[j] + f[o], fmaf(Kq[q], vu * vu, fmaf(Kc[q] * vu, cF, K0[q])));
+        const float anti = fmaf(c2, f[j] - f[o], fmaf(Lu[q], vu, Lf[q] * cF));
         const float gj = sym + anti, go = sym - anti;
         if (fast) {
-            P::store(fout + j * N + i + a.ne[j], gj);
-            P::store(fout + o * N + i + a.ne[o], go);
+            fo[a.so[j]] = P::enc_store(gj);
+            fo[a.so[o]] = P::enc_store(go);
         } else {
-            push_general<P>(a, fout, N, x, y, z, i, j, gj, n, ux, uy, uz, usq);
-            push_general<P>(a, fout, N, x, y, z, i, o, go, n, ux, uy, uz, usq);
+            push_general<P>(a, fout, x, y, z, i, j, gj, n, ux, uy, uz, usq);
+            push_general<P>(a, fout, x, y, z, i, o, go, n, ux, uy, uz, usq);
         }
     }
+}
+
+// One thread per node, populations loaded straight from HBM.
+template <class P>
+__global__ void __launch_bounds__(128, 8) k_collide_stream_dev(LBArgs a) {
+    using S = typename P::S;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y + 1;
+    const int z = blockIdx.z + 1;
+    const int i = x + a.X * (y + a.Y * z);
+    const S* fin = reinterpret_cast<const S*>(a.fin);
+    // whole warps leave together so that the element sums can use full-warp shuffles
+    const uint8_t t = x < a.X ? a.ntype[i] : (uint8_t)HB_T_STATWALL;
+    const bool act = is_active(t);
+    if (!__any_sync(0xffffffffu, act)) return;
+    float f[Q];
+#pragma unroll
+    for (int j = 0; j < Q; ++j) f[j] = act ? P::load(fin + a.jn[j] + i) : 0.0f;
+    lb_node<P>(a, x, y, z, i, t, act, f);
 }
 
 void launch_lb_step_dev(hb_ctx* c, const LBArgs& a) {
