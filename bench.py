@@ -17,6 +17,12 @@ roofline   the fused collide+stream kernel: algorithmic bytes per launch / its
 cpu_baseline  the CPU oracle (this repository's C++ restatement of the reference, the
            reference itself cannot be built on the aarch64 GPU host) on a bounded
            sample of the same workload.
+fp64_form  the same workload with FP64 populations: step time, FP32 speed-up, and the
+           FP32 form's velocity (relative L2, L-inf) and density error against it after
+           --compare-steps cycles from the same initial state.
+adjoint    drag adjoint on the 96^3 channel with 64 fixed spheres (FP32, 2000 steps,
+           checkpoints every 100): device time per step of forward + reverse, and dJ/dtau
+           against central differences of the FP64 forward.
 
 Multi-GPU: the path does not shard on one box; --gpus N runs N independent replicas
 (one per rank, no collective), value = sum over ranks.
@@ -149,30 +155,102 @@ def cpu_sample(params, spheres, steps, threads):
     return active * steps / dt / 1e6, dt
 
 
+def fp64_compare(p32, spheres, steps):
+    """The FP64 form of the same workload: its step time, and the FP32 form's velocity and
+    density error against it after `steps` cycles from the same initial state."""
+    from hybird_gb300 import abi
+    from hybird_gb300.gpu import GpuSim
+    p64 = abi.HbParams.from_buffer_copy(p32)
+    p64.precision = abi.HB_FP64
+    out = {"steps": steps}
+    lat = {}
+    for name, p in (("f64", p64), ("f32", p32)):
+        g = GpuSim(p, spheres)
+        if name == "f64":
+            g.cycle(3)
+            ms, _, _ = g.time_cycles(10)
+            out["ms_per_step_f64"] = ms / 10
+            g.close()
+            g = GpuSim(p, spheres)
+        g.cycle(steps)
+        l = g.lattice()
+        lat[name] = {k: l[k] for k in ("type", "n", "u")}
+        g.close()
+    act = (lat["f64"]["type"] == 0) | (lat["f64"]["type"] == 3)
+    u64 = lat["f64"]["u"].reshape(3, -1)[:, act]
+    du = lat["f32"]["u"].reshape(3, -1)[:, act] - u64
+    out["u_rel_l2"] = float(np.sqrt((du ** 2).sum() / (u64 ** 2).sum()))
+    out["u_rel_linf"] = float(np.abs(du).max() / np.abs(u64).max())
+    out["rho_abs_linf"] = float(np.abs(lat["f32"]["n"][act] - lat["f64"]["n"][act]).max())
+    return out
+
+
+def adjoint_measure(steps):
+    """Drag adjoint on 96^3 (64 fixed spheres r=6, TRT tau 0.7, FP32, body force 2e-6,
+    inlet/outlet planes): device time per step of forward + reverse (checkpoints every
+    100 steps, segments recomputed), and dJ/dtau against central differences of the FP64
+    forward (relative step 1e-4)."""
+    from hybird_gb300 import abi
+    from hybird_gb300.gpu import GpuSim
+    from hybird_gb300.workloads import adjoint_channel
+    p, obj, uin = adjoint_channel(precision=abi.HB_FP32)
+    g = GpuSim(p, None, obj)
+    F = tuple(p.lbF)
+    g.adjoint_drag(steps, 0.7, F, uin, abi.HB_FP32, 100)  # allocation and warm-up
+    J, dF, dtau, duin = g.adjoint_drag(steps, 0.7, F, uin, abi.HB_FP32, 100)
+    ms_f, ms_r, nf, nr = g.adjoint_timing()
+    h = 1e-4 * 0.7
+    fd = (g.adjoint_forward(steps, 0.7 + h, F, uin, abi.HB_FP64, 100)
+          - g.adjoint_forward(steps, 0.7 - h, F, uin, abi.HB_FP64, 100)) / (2 * h)
+    g.close()
+    return {"workload": "96^3 channel, 64 fixed spheres r=6, TRT tau 0.7, F=2e-6, inlet/outlet u0=0.02, FP32",
+            "steps": steps, "checkpoint_every": 100, "ms_forward": round(ms_f, 3), "ms_reverse": round(ms_r, 3),
+            "ms_per_step": round((ms_f + ms_r) / steps, 5), "forward_steps": nf, "reverse_steps": nr,
+            "J": J, "dJ_dtau": dtau, "dJ_dtau_fd_fp64": fd, "dJ_dtau_rel_err": abs(dtau - fd) / abs(fd)}
+
+
 def run_reference(args, rank):
     """The reference arm: the reference's CPU algorithm (the oracle port; the reference
-    sources do not travel to the GPU host) on this machine's host cores."""
+    sources do not travel to the GPU host) on this machine's host cores, on the same workload,
+    metric and unit: min(W, 3) untimed cycles, then min(K, 200) timed cycles."""
     from hybird_gb300 import abi
     if rank != 0:
         return
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from oracle_port import OracleSim
     p, spheres = workload(abi.HB_FP64)
     threads = os.cpu_count() or 1
-    steps = max(1, min(args.steps, 4))
-    vals = []
-    for _ in range(max(1, args.warmup and 1)):
-        pass
-    v, dt = cpu_sample(p, spheres, steps, threads)
-    vals.append(v)
+    steps = max(1, min(args.steps, 200))
+    warm = max(1, min(args.warmup, 3))
+    o = OracleSim(p, spheres, threads=threads)
+    active = int(o.lib.hbo_active(o.h))
+    o.cycle(warm)
+    t0 = time.perf_counter()
+    o.cycle(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    v = active * steps / dt / 1e6
     line = {"impl": "reference", "metric": "MLUPS (coupled LBM-DEM step)", "value": round(v, 3),
-            "unit": "MLUPS", "n_gpus": args.gpus, "steps": steps, "warmup": 1,
+            "unit": "MLUPS", "n_gpus": args.gpus, "steps": steps, "warmup": warm,
             "ms_per_step": round(dt / steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "coupled sedimentation 128^3 D3Q19, %d spheres r~U[4,6], multiStep 3"
+            "config": {"workload": "coupled sedimentation 128^3 D3Q19 TRT, %d spheres r~U[4,6], multiStep 3"
                        % len(spheres), "lattice": [128, 128, 128], "spheres": len(spheres)},
             "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
-                             "sample": f"{steps} whole cycles after 1 untimed cycle"},
+                             "sample": f"{steps} whole cycles after {warm} untimed cycles ({dt:.1f} s)"},
             "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def lattice_traffic(prec):
+    """DRAM bytes per launch of the lattice kernel from the committed ncu capture of this
+    workload (profiles/), or None."""
+    try:
+        with open(os.path.join(REPO, "profiles", "lattice_kernel_traffic.json")) as fh:
+            d = json.load(fh)
+        return d["dram_bytes_per_launch"].get(DTYPE[prec])
+    except (OSError, KeyError, ValueError):
+        return None
 
 
 def main():
@@ -182,7 +260,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "fp16s"])
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=100, help="0 skips the CPU baseline")
+    ap.add_argument("--compare-steps", type=int, default=100,
+                    help="cycles of the FP64 form run beside the FP32 one (speed-up and error)")
+    ap.add_argument("--adjoint-steps", type=int, default=2000, help="0 skips the adjoint measurement")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -255,6 +336,8 @@ def main():
     achieved = bytes_launch / (ms_lb * 1e-3) / 1e9 if ms_lb > 0 else None
     st = g.status()
     g.close()
+    fp64 = fp64_compare(p, spheres, args.compare_steps) if args.compare_steps > 0 and prec != abi.HB_FP64 else None
+    adj = adjoint_measure(args.adjoint_steps) if args.adjoint_steps > 0 else None
     line = {
         "metric": "MLUPS (coupled LBM-DEM step)", "value": round(value, 2), "unit": "MLUPS",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
@@ -271,12 +354,17 @@ def main():
                 "d2h_bytes_per_step": 4 * 3 * E * 8},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
-                     "traffic": None, "kernel": "k_collide_stream", "kernel_ms": round(ms_lb, 5),
+                     "traffic": lattice_traffic(prec), "kernel": "k_collide_stream_dev" if prec != abi.HB_FP64 else "k_collide_stream", "kernel_ms": round(ms_lb, 5),
                      "peak_kind": peak_kind, "bytes_per_launch": bytes_launch},
         "clocks": clk.summary(),
         "dem": {"contacts_last_substep": st.contacts, "candidate_pairs": st.pairs},
     }
-    if rank == 0:
+    if fp64:
+        fp64["fp32_speedup"] = round(fp64.pop("ms_per_step_f64") / ms_step, 2)
+        line["fp64_form"] = fp64
+    if adj:
+        line["adjoint"] = adj
+    if rank == 0 and args.cpu_steps > 0:
         threads = os.cpu_count() or 1
         try:
             p64, sph = workload(abi.HB_FP64)
@@ -286,6 +374,7 @@ def main():
                                               f"after one untimed cycle ({dt:.1f} s)"}
         except Exception as exc:  # noqa: BLE001
             line["cpu_baseline"] = {"value": None, "error": str(exc)[:200]}
+    if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

@@ -689,13 +689,18 @@ __device__ __forceinline__ Sph load_sph(const CoupleArgs& a, int p) {
 // exact int -> float for |v| < 2^22 on the FP32 pipe: the bits of 1.5 * 2^23 + v, minus 1.5 * 2^23
 __device__ __forceinline__ float i2f_small(int v) { return __int_as_float(0x4B400000 + v) - 12582912.0f; }
 
+// the FP64 decision, not inlined so that the compiler cannot execute it speculatively
+__device__ __noinline__ bool in_sph_exact(const Sph& s, int x, int y, int z) {
+    const double dx = x - s.cx, dy = y - s.cy, dz = z - s.cz;
+    return dx * dx + dy * dy + dz * dz < s.r2;
+}
+
 __device__ __forceinline__ bool in_sph(const Sph& s, int x, int y, int z) {
     const float dxf = i2f_small(x - s.ix) - s.fx, dyf = i2f_small(y - s.iy) - s.fy, dzf = i2f_small(z - s.iz) - s.fz;
     const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
     if (d2f < s.lo) return true;
     if (d2f > s.hi) return false;
-    const double dx = x - s.cx, dy = y - s.cy, dz = z - s.cz;
-    return dx * dx + dy * dy + dz * dz < s.r2;
+    return in_sph_exact(s, x, y, z);
 }
 
 // Sphere of every particle for the current step, built once per particle (FP64 is

@@ -74,6 +74,28 @@ __device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fou
     }
 }
 
+// v * 2^38 rounded to a 64-bit integer, from 32-bit conversions only (a 64-bit float to
+// integer conversion issues on the narrow FP64 pipe of this part): a = |v| * 2^6 splits
+// into floor(a) (the high word) and the exact fraction times 2^32 (the low word,
+// < 2^32); the sign is applied to the 64-bit result.
+__device__ __forceinline__ unsigned long long to_fixed(float v) {
+    const float a = fabsf(v) * 64.0f;
+    const float h = floorf(a);
+    const unsigned long long m =
+        ((unsigned long long)__float2uint_rn(h) << 32) + __float2uint_rn((a - h) * 4294967296.0f);
+    return v < 0.0f ? 0ull - m : m;
+}
+
+// FP64 node fields (read by the free surface, the wall force and downloads) are written
+// by separate non-inlined stores: inlined, their float -> double conversions would be
+// executed for every node and occupy the narrow FP64 pipe.
+__device__ __noinline__ void write_rho(double* rho, int i, float n) { rho[i] = (double)n; }
+__device__ __noinline__ void write_u_hf(double* u, double* hf, long long N, int i, float ux, float uy, float uz,
+                                        float hx, float hy, float hz) {
+    u[i] = (double)ux; u[N + i] = (double)uy; u[2 * N + i] = (double)uz;
+    hf[i] = (double)hx; hf[N + i] = (double)hy; hf[2 * N + i] = (double)hz;
+}
+
 // Element sums of the coupling (LB.cpp:1853-1918) folded into the lattice step: the
 // nodes of one particle form runs of consecutive lanes along x; a segmented suffix sum
 // over each run (fixed shuffle pattern) leaves the run total in its first lane, which
@@ -97,9 +119,7 @@ __device__ __forceinline__ void element_sums_warp(unsigned long long* hacc, int 
     }
     if (key >= 0 && (lane == 0 || kprev != key)) {
 #pragma unroll
-        for (int k = 0; k < 7; ++k)
-            atomicAdd(hacc + (long long)k * E + key,
-                      (unsigned long long)__float2ll_rn(v[k] * float(HACC_SCALE)));
+        for (int k = 0; k < 7; ++k) atomicAdd(hacc + (long long)k * E + key, to_fixed(v[k]));
     }
 }
 
@@ -198,11 +218,8 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
     const float ap = 1.0f - 0.5f * wp, am = 1.0f - 0.5f * wm;
 
     const bool all = (mode & 1) != 0;
-    if (all || a.free_surface || !(t & HB_BULK)) a.rho[i] = (double)n;
-    if (all || code == HB_T_INTERFACE) {
-        a.u[i] = (double)ux; a.u[a.N + i] = (double)uy; a.u[2 * a.N + i] = (double)uz;
-        a.hf[i] = (double)hx; a.hf[a.N + i] = (double)hy; a.hf[2 * a.N + i] = (double)hz;
-    }
+    if (all || a.free_surface || !(t & HB_BULK)) write_rho(a.rho, i, n);
+    if (all || code == HB_T_INTERFACE) write_u_hf(a.u, a.hf, a.N, i, ux, uy, uz, hx, hy, hz);
 
     // Pairwise collision with per-node coefficients for the two link weights (w = 1/18 on
     // the axes, 1/36 on the diagonals), S = g_j + g_o, D = g_j - g_o, base = dn - 1.5 n u^2:
