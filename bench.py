@@ -267,19 +267,12 @@ def main():
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist_mod
-        dist = dist_mod
-        dist.init_process_group("gloo")
+    from hybird_gb300.replicas import Replicas
+    rep = Replicas()
+    rank, world, local = rep.rank, rep.world, rep.local
     if args.impl == "reference":
         run_reference(args, rank)
-        if dist:
-            dist.barrier()
-            dist.destroy_process_group()
+        rep.close()
         return
 
     import ctypes as C
@@ -302,19 +295,13 @@ def main():
     for _ in range(args.warmup):
         check(L.hb_cycle(g.h, 1))
     check(L.hb_synchronize(g.h))
-    if dist:
-        dist.barrier()
+    rep.barrier()
     # device-resident timed region (inputs larger than L2: 2 x 19 x 2.1M x 4 B = 319 MB)
     with Clocks(local) as clk:
         ms_tot, ms_lb, kpc = g.time_cycles(args.steps)
     check(L.hb_synchronize(g.h))
-    ms_step = ms_tot / args.steps
-    if dist:
-        import torch
-        t = torch.tensor([ms_step], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = A * world / (ms_step * 1e-3) / 1e6
+    ms_step = rep.max(ms_tot / args.steps)
+    value = rep.aggregate_rate(A, ms_step * 1e-3) / 1e6
     # end-to-end through the C-ABI with host buffers
     E = g.E
     pin = {k: np.zeros(3 * E) for k in ("x0", "x1", "FHydro", "MHydro")}
@@ -328,8 +315,8 @@ def main():
                                      pin["x1"].ctypes.data_as(C.c_void_p), None, None,
                                      pin["FHydro"].ctypes.data_as(C.c_void_p),
                                      pin["MHydro"].ctypes.data_as(C.c_void_p), None, None, None, None, None))
-    e2e_dt = time.perf_counter() - t0
-    e2e = A * world * e2e_steps / e2e_dt / 1e6
+    e2e_dt = rep.max(time.perf_counter() - t0)
+    e2e = rep.aggregate_rate(A * e2e_steps, e2e_dt) / 1e6
     # roofline of the fused kernel
     peak, peak_kind = measured_peak()
     bytes_launch = A * B_LU[prec] + A_in * (4 + 3 * (8 if prec == abi.HB_FP64 else 4))
@@ -376,9 +363,7 @@ def main():
             line["cpu_baseline"] = {"value": None, "error": str(exc)[:200]}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
+    rep.close()
 
 
 if __name__ == "__main__":
