@@ -226,3 +226,81 @@ def test_coupled_box_fp32_vs_fp64_oracle_and_reproducible():
     assert rel_linf(ge["FHydro"], oe["FHydro"]) <= 2e-3, rel_linf(ge["FHydro"], oe["FHydro"])
     assert rel_linf(ge["MHydro"], oe["MHydro"]) <= 2e-2, rel_linf(ge["MHydro"], oe["MHydro"])
     assert rel_linf(ge["x0"], oe["x0"]) <= 1e-6, rel_linf(ge["x0"], oe["x0"])
+
+
+def test_coupled_box_fp64_vs_oracle_200_step_horizon():
+    """Coupled runs are compared over a 200-step horizon (elements and lattice)."""
+    p, spheres = _coupled_box(abi.HB_FP64)
+    g = _gpu()(p, spheres)
+    o = OracleSim(p, spheres, threads=4)
+    g.cycle(200)
+    o.cycle(200)
+    gl, ol = g.lattice(), o.lattice()
+    np.testing.assert_array_equal(gl["inside"], ol["inside"])
+    act = (ol["type"] == 0) | (ol["type"] == 3)
+    assert rel_linf(gl["f"].reshape(19, -1), ol["f"].reshape(19, -1), act) <= 1e-10
+    ge, oe = g.elements(), o.elements()
+    for k in ("x0", "x1", "FHydro"):
+        assert rel_linf(ge[k], oe[k]) <= 1e-8, (k, rel_linf(ge[k], oe[k]))
+    g.close()
+
+
+def _stats(sim, steps, every):
+    """Per-sample mean particle z-velocity, mean z hydrodynamic force and the fluid mass
+    (sum of density over active non-particle nodes)."""
+    vz, fz, mass = [], [], []
+    for _ in range(steps // every):
+        sim.cycle(every)
+        e = sim.elements()
+        E = len(e["x1"]) // 3
+        vz.append(e["x1"][2 * E:].mean())
+        fz.append(e["FHydro"][2 * E:].mean())
+        lat = sim.lattice()
+        fl = ((lat["type"] == 0) | (lat["type"] == 3)) & (lat["inside"] == 0)
+        mass.append(lat["n"][fl].sum())
+    return np.array(vz), np.array(fz), np.array(mass)
+
+
+def test_coupled_long_run_statistics_fp32_vs_fp64_oracle():
+    """Long-run statistics of the coupled FP32 form against the FP64 oracle: settling
+    velocity and mean drag over the second half of 600 steps, and the drift of the fluid
+    mass (the closed box conserves it up to the nodes the particles cover and uncover)."""
+    p32, spheres = _coupled_box(abi.HB_FP32)
+    p64, _ = _coupled_box(abi.HB_FP64)
+    g = _gpu()(p32, spheres)
+    o = OracleSim(p64, spheres, threads=4)
+    vg, fg, mg = _stats(g, 600, 50)
+    vo, fo, mo = _stats(o, 600, 50)
+    half = len(vg) // 2
+    sv_g, sv_o = vg[half:].mean(), vo[half:].mean()
+    fd_g, fd_o = fg[half:].mean(), fo[half:].mean()
+    print("settling", sv_g, sv_o, "drag", fd_g, fd_o, "mass drift", mg[-1] - mg[0], mo[-1] - mo[0])
+    assert abs(sv_g - sv_o) <= 1e-3 * abs(sv_o), (sv_g, sv_o)
+    assert abs(fd_g - fd_o) <= 1e-3 * abs(fd_o), (fd_g, fd_o)
+    assert abs((mg[-1] - mg[0]) - (mo[-1] - mo[0])) <= 1e-4 * mo[0]
+    g.close()
+
+
+def test_free_surface_bingham_smagorinsky_spheres_fp64_vs_oracle():
+    """Every feature of the dam-break configuration at once on a small lattice: free
+    surface, Bingham plastic with Smagorinsky, and particles in the liquid column."""
+    spheres = np.array([[8.3, 7.1, 7.6, 3.0], [8.8, 15.7, 8.2, 3.0], [9.6, 11.2, 14.9, 2.6]])
+    p = abi.make_params((40, 24, 28), (7,) * 6, init_visc=1.0 / 30.0, lbF=(0.0, 0.0, -1e-4),
+                        non_newtonian=1, plastic_visc=1.0 / 30.0, yield_stress=5e-6, turbulence=1,
+                        turb_const=0.01, free_surface=1, gas_box=(0.4, 0.6), multi_step=3, collision=abi.HB_BGK)
+    g = _gpu()(p, spheres)
+    o = OracleSim(p, spheres, threads=4)
+    for _ in range(4):
+        g.cycle(10)
+        o.cycle(10)
+        gl, ol = g.lattice(), o.lattice()
+        np.testing.assert_array_equal(gl["type"], ol["type"])
+        np.testing.assert_array_equal(gl["inside"], ol["inside"])
+        np.testing.assert_array_equal(g.interface(), np.sort(o.interface()))
+        act = (ol["type"] == 0) | (ol["type"] == 3)
+        assert rel_linf(gl["mass"], ol["mass"], act) <= 1e-11
+        assert rel_linf(gl["f"].reshape(19, -1), ol["f"].reshape(19, -1), act) <= 1e-11
+    ge, oe = g.elements(), o.elements()
+    for k in ("x0", "FHydro"):
+        assert rel_linf(ge[k], oe[k]) <= 1e-9, (k, rel_linf(ge[k], oe[k]))
+    g.close()
