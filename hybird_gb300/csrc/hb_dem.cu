@@ -46,6 +46,10 @@ struct DemArgs {
     unsigned int* done;
     int ncells, nC0, nC1, nC2;
     double cw0, cw1, cw2, nebrRange, trigger, dt;
+    // Gear coefficients (elmt.cpp:139-254): c_k = dt^k / k!, and the corrector weights of
+    // the position/orientation (2nd order) and spin (1st order) chains, computed once on
+    // the host with the same expressions (FP64 divisions are costly on this part's pipe)
+    double gc[5], gc1[6], gc2[6];
     int nw;
     double wp[MAX_WALLS][3], wn[MAX_WALLS][3];
     int O;
@@ -361,7 +365,7 @@ __device__ double newton_plain(const DemArgs& a, int i, int c) {
 __device__ void predict_one(const DemArgs& a, int i) {  // elmt.cpp:139-177
     const int E = a.E;
     const double dt = a.dt;
-    const double c[5] = {dt, dt * dt / 2.0, dt * dt * dt / 6.0, dt * dt * dt * dt / 24.0, dt * dt * dt * dt * dt / 120.0};
+    const double* c = a.gc;
     const V x0 = ld3(a.x0, E, i), x1 = ld3(a.x1, E, i), x2 = ld3(a.x2, E, i), x3 = ld3(a.x3, E, i),
             x4 = ld3(a.x4, E, i), x5 = ld3(a.x5, E, i);
     st3(a.xp0, E, i, add(add(add(add(add(x0, mul(c[0], x1)), mul(c[1], x2)), mul(c[2], x3)), mul(c[3], x4)), mul(c[4], x5)));
@@ -429,13 +433,9 @@ __device__ double correct_one(const DemArgs& a, int i) {  // elmt.cpp:179-254
     double v2 = 0.0;
     {
         const double dt = a.dt;
-        const double c[5] = {dt, dt * dt / 2.0, dt * dt * dt / 6.0, dt * dt * dt * dt / 24.0, dt * dt * dt * dt * dt / 120.0};
-        const double g1[6] = {95.0 / 288.0, 1.0, 25.0 / 24.0, 35.0 / 72.0, 5.0 / 48.0, 1.0 / 120.0};
-        const double g2[6] = {3.0 / 16.0, 251.0 / 360.0, 1.0, 11.0 / 18.0, 1.0 / 6.0, 1.0 / 60.0};
-        const double c1o[6] = {g1[0] * c[0], g1[1] * c[0] / c[0], g1[2] * c[0] / c[1], g1[3] * c[0] / c[2],
-                               g1[4] * c[0] / c[3], g1[5] * c[0] / c[4]};
-        const double c2o[6] = {g2[0] * c[1], g2[1] * c[1] / c[0], g2[2] * c[1] / c[1], g2[3] * c[1] / c[2],
-                               g2[4] * c[1] / c[3], g2[5] * c[1] / c[4]};
+        const double* c = a.gc;
+        const double* c1o = a.gc1;
+        const double* c2o = a.gc2;
         const V x2 = ld3(a.x2, E, i);
         const V x2c = sub(x2, ld3(a.xp2, E, i));
         const V x0 = add(ld3(a.xp0, E, i), mul(c2o[0], x2c));
@@ -481,13 +481,9 @@ __device__ double correct_one(const DemArgs& a, int i) {  // elmt.cpp:179-254
 __device__ double correct_predict_one(const DemArgs& a, int i) {
     const int E = a.E;
     const double dt = a.dt;
-    const double c[5] = {dt, dt * dt / 2.0, dt * dt * dt / 6.0, dt * dt * dt * dt / 24.0, dt * dt * dt * dt * dt / 120.0};
-    const double g1[6] = {95.0 / 288.0, 1.0, 25.0 / 24.0, 35.0 / 72.0, 5.0 / 48.0, 1.0 / 120.0};
-    const double g2[6] = {3.0 / 16.0, 251.0 / 360.0, 1.0, 11.0 / 18.0, 1.0 / 6.0, 1.0 / 60.0};
-    const double c1o[6] = {g1[0] * c[0], g1[1] * c[0] / c[0], g1[2] * c[0] / c[1], g1[3] * c[0] / c[2],
-                           g1[4] * c[0] / c[3], g1[5] * c[0] / c[4]};
-    const double c2o[6] = {g2[0] * c[1], g2[1] * c[1] / c[0], g2[2] * c[1] / c[1], g2[3] * c[1] / c[2],
-                           g2[4] * c[1] / c[3], g2[5] * c[1] / c[4]};
+    const double* c = a.gc;
+    const double* c1o = a.gc1;
+    const double* c2o = a.gc2;
     newton_one(a, i);
     // loads
     const V x2 = ld3(a.x2, E, i), xp0 = ld3(a.xp0, E, i), xp1 = ld3(a.xp1, E, i), xp2 = ld3(a.xp2, E, i),
@@ -566,12 +562,10 @@ __device__ double correct_predict_one(const DemArgs& a, int i) {
 __device__ double correct_predict_plain(const DemArgs& a, int i, int c, double acc) {
     const int E = a.E;
     const double dt = a.dt;
-    const double cc[5] = {dt, dt * dt / 2.0, dt * dt * dt / 6.0, dt * dt * dt * dt / 24.0, dt * dt * dt * dt * dt / 120.0};
+    const double* cc = a.gc;
     const long long o = (long long)(c % 3) * E + i;
     if (c < 3) {
-        const double g2[6] = {3.0 / 16.0, 251.0 / 360.0, 1.0, 11.0 / 18.0, 1.0 / 6.0, 1.0 / 60.0};
-        const double c2o[6] = {g2[0] * cc[1], g2[1] * cc[1] / cc[0], g2[2] * cc[1] / cc[1], g2[3] * cc[1] / cc[2],
-                               g2[4] * cc[1] / cc[3], g2[5] * cc[1] / cc[4]};
+        const double* c2o = a.gc2;
         const double x2 = acc, p0 = a.xp0[o], p1 = a.xp1[o], p2 = a.xp2[o], p3 = a.xp3[o], p4 = a.xp4[o],
                      p5 = a.xp5[o];
         const double d = x2 - p2;
@@ -588,9 +582,7 @@ __device__ double correct_predict_plain(const DemArgs& a, int i, int c, double a
         a.pf[(3 + c) * E + i] = (float)x1;
         return x1;
     }
-    const double g1[6] = {95.0 / 288.0, 1.0, 25.0 / 24.0, 35.0 / 72.0, 5.0 / 48.0, 1.0 / 120.0};
-    const double c1o[6] = {g1[0] * cc[0], g1[1] * cc[0] / cc[0], g1[2] * cc[0] / cc[1], g1[3] * cc[0] / cc[2],
-                           g1[4] * cc[0] / cc[3], g1[5] * cc[0] / cc[4]};
+    const double* c1o = a.gc1;
     const double w1 = acc, p0 = a.wp0[o], p1 = a.wp1[o], p2 = a.wp2[o], p3 = a.wp3[o], p4 = a.wp4[o],
                  p5 = a.wp5[o];
     const double d = w1 - p1;
@@ -933,17 +925,33 @@ __device__ __forceinline__ void stamp(const CycleArgs& A, int k) {
     }
 }
 
+// Warp-sized tasks (a particle's contacts, a group of five elements' corrector) are laid
+// out so that consecutive tasks land on different SMs first and on different warp
+// schedulers (warp index mod 4) second: an FP64 warp instruction costs the same narrow-
+// pipe time whatever its active lanes, so the schedulers' FP64 pipes, not the lanes, are
+// the resource.  With the grid as H = 2 blocks per SM slot: task p runs on block
+// (p mod S) + S * h and warp k mod W, where k = (p / S) mod (W * H), h = k / W.
+__device__ __forceinline__ void warp_tasks(int& first, int& stride) {
+    const int B = gridDim.x, W = blockDim.x >> 5;
+    const int H = (B & 1) ? 1 : 2, S = B / H;
+    const int b = blockIdx.x, w = threadIdx.x >> 5;
+    first = (b % S) + S * (w + W * (b / S));
+    stride = B * W;
+}
+
 __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
     cg::grid_group grid = cg::this_grid();
     __shared__ double sh[7][256];
+    __shared__ double s_maxdisp;
+    __shared__ int s_rebuild;
     const int E = A.d.E;
     // element loops spread consecutive elements over different blocks, so the FP64 work
     // (narrow pipe on this part) lands on every SM instead of the first few
     const int gt = blockIdx.x + gridDim.x * threadIdx.x;
     const int gs = gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
-    const int gw = blockIdx.x + gridDim.x * (threadIdx.x >> 5);  // one warp per particle
-    const int nw = gridDim.x * (blockDim.x >> 5);
+    int gw, nw;  // this warp's first task and the task stride (one warp per particle / group)
+    warp_tasks(gw, nw);
     stamp(A, 0);
     if (A.do_reduce) {
         if (A.c.hacc) {
@@ -980,9 +988,8 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
             double v2 = 0.0;
             {  // six lanes per element (five elements per warp, lanes 30-31 idle)
                 const int grp = lane / 6, c = lane - 6 * grp;
-                const int wglob = blockIdx.x + gridDim.x * (threadIdx.x >> 5);
                 const int ngroups = 5 * nw;
-                for (int base = 5 * wglob; base < E; base += ngroups) {
+                for (int base = 5 * gw; base < E; base += ngroups) {
                     const int i = base + grp;
                     const bool on = grp < 5 && i < E;
                     const bool plain = on && A.d.plain[i];
@@ -1004,15 +1011,24 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
             if (threadIdx.x == 0) A.d.partial[blockIdx.x] = sh[0][0];
             grid.sync();
             stamp(A, k++);
-            // DEM.cpp:1314-1324, 334-347: every warp folds the block maxima with its lanes
-            // in parallel (max is order-independent), so all threads agree on the flag
-            double mx = 0.0;
-            for (int b = lane; b < (int)gridDim.x; b += 32) mx = fmax(mx, ((volatile double*)A.d.partial)[b]);
-            for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-            maxDisp += sqrt(mx) * A.d.dt;
-            rebuild = maxDisp > A.d.trigger;
-            if (rebuild) maxDisp = 0.0;
+            // DEM.cpp:1314-1324, 334-347: warp 0 of every block folds the block maxima with
+            // its lanes (max is order-independent, so every block gets the same flag) and
+            // hands the result to the rest of the block through shared memory
+            if (threadIdx.x < 32) {
+                double mx = 0.0;
+                for (int b = lane; b < (int)gridDim.x; b += 32) mx = fmax(mx, ((volatile double*)A.d.partial)[b]);
+                for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+                if (lane == 0) {
+                    double md = maxDisp + sqrt(mx) * A.d.dt;
+                    const bool rb = md > A.d.trigger;
+                    if (rb) md = 0.0;
+                    s_maxdisp = md;
+                    s_rebuild = rb ? 1 : 0;
+                }
+            }
             __syncthreads();
+            maxDisp = s_maxdisp;
+            rebuild = s_rebuild != 0;
         }
         if (A.do_boxes)  // positions are final: boxes for the coupling passes
             for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) build_box(A.c, p);
@@ -1062,6 +1078,19 @@ static DemArgs dem_args(hb_ctx* c) {
     a.ncells = d.ncells; a.nC0 = d.nCells[0]; a.nC1 = d.nCells[1]; a.nC2 = d.nCells[2];
     a.cw0 = d.cellWidth[0]; a.cw1 = d.cellWidth[1]; a.cw2 = d.cellWidth[2];
     a.nebrRange = d.nebrRange; a.trigger = d.trigger; a.dt = d.dt;
+    {
+        const double dt = d.dt;
+        const double c[5] = {dt, dt * dt / 2.0, dt * dt * dt / 6.0, dt * dt * dt * dt / 24.0, dt * dt * dt * dt * dt / 120.0};
+        const double g1[6] = {95.0 / 288.0, 1.0, 25.0 / 24.0, 35.0 / 72.0, 5.0 / 48.0, 1.0 / 120.0};
+        const double g2[6] = {3.0 / 16.0, 251.0 / 360.0, 1.0, 11.0 / 18.0, 1.0 / 6.0, 1.0 / 60.0};
+        for (int k = 0; k < 5; ++k) a.gc[k] = c[k];
+        a.gc1[0] = g1[0] * c[0];
+        a.gc2[0] = g2[0] * c[1];
+        for (int k = 1; k < 6; ++k) {
+            a.gc1[k] = g1[k] * c[0] / c[k - 1];
+            a.gc2[k] = g2[k] * c[1] / c[k - 1];
+        }
+    }
     a.nw = d.nw;
     for (int w = 0; w < MAX_WALLS; ++w)
         for (int k = 0; k < 3; ++k) {
