@@ -230,6 +230,8 @@ int hb_create(const hb_params* params, hb_ctx** out) {
     }
     if (params->non_newtonian || params->turbulence)
         if ((rc = dalloc((uint8_t**)&c->visc, N * tsz))) { hb_destroy(c); return rc; }
+    if (params->precision != HB_FP64)
+        if ((rc = dalloc(&c->lmask, N))) { hb_destroy(c); return rc; }
     CK(cudaMemset(c->mode, 0, sizeof(int)));
     CK(cudaMemset(c->status, 0, sizeof(int) * STATUS_WORDS));
     CK(cudaMemset(c->wall_force, 0, sizeof(double) * (MAX_WALLS * 3 + 1)));
@@ -246,7 +248,7 @@ int hb_destroy(hb_ctx* c) {
         if (c->gexec[k]) cudaGraphExecDestroy(c->gexec[k]);
     if (c->graph) cudaGraphDestroy(c->graph);
     if (c->graph2) cudaGraphDestroy(c->graph2);
-    void* ptrs[] = {c->ntype, c->solid, c->fA, c->fB, c->mode, c->rho, c->u, c->hf, c->mass,
+    void* ptrs[] = {c->ntype, c->lmask, c->solid, c->fA, c->fB, c->mode, c->rho, c->u, c->hf, c->mass,
                     c->visc, c->dv, c->hacc, c->status, c->wall_part, c->wall_force, c->fs_force, c->fs_mass2,
                     c->fs_cnt, c->fs_scal, c->fs_flag, c->fs_first, c->fs_part, c->lb_force, c->lb_force_f, c->d.pf, c->d.plain,
                     c->d.base, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,

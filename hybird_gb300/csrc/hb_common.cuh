@@ -136,6 +136,7 @@ struct LBArgs {
     void* visc;             // T[N] when viscosity is persistent
     void* dv;               // T[3N] direct-forcing term of inside nodes (FP64 kernel)
     unsigned long long* hacc;  // [7E] fixed-point F, M, fluid volume per element (FP32/FP16 kernels)
+    const uint32_t* lmask;  // [N] links of a non-bulk active node that need the general push
     const double* F;        // device body force [3] (zero when forceFieldSolve = 0)
     const float* Ff;        // the same force in FP32 for the reduced-precision kernels
     int ne[Q];              // index offset of link j for nodes whose links do not wrap

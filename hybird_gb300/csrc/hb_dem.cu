@@ -813,13 +813,19 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
         if (!((tm[0] | tm[1] | tm[2] | tm[3] | tm[4] | tm[5]) & HB_INSIDE)) continue;
         const long long ms[6] = {l - 1, l + 1, l - sy, l + sy, l - sz, l + sz};
         unsigned long long best = ~0ull;
+        uint32_t qlast = 0xffffffffu;  // particle whose cover of this node was last decided
+        bool covered = false;
 #pragma unroll
         for (int kk = 0; kk < 6; ++kk) {
             if (!(tm[kk] & HB_INSIDE)) continue;
             const long long m = ms[kk];
             const uint32_t q = a.solid[m];
             const Sph& sq = a.tab[q].s;
-            if (!in_sph(sq, x - cx(kk + 1), y - cy(kk + 1), z - cz(kk + 1)) || !in_sph(sq, x, y, z)) continue;
+            if (q != qlast) {  // this node covered by q? (usually not: it lies just outside)
+                covered = in_sph(sq, x, y, z);
+                qlast = q;
+            }
+            if (!covered || !in_sph(sq, x - cx(kk + 1), y - cy(kk + 1), z - cz(kk + 1))) continue;
             const unsigned long long key = ((unsigned long long)m << 32) | q;
             if (key < best) best = key;
         }

@@ -474,25 +474,35 @@ __global__ void k_init_vars(InitArgs a, LBArgs b, const int* mx, double Fx, doub
 }
 
 // HB_BULK: node active and all 18 links lead to active nodes
-__global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype) {
+// HB_BULK / HB_PWRAP flags and, for active nodes, the mask of links that are not plain
+// (bit j: the neighbour along j is not active, or the link crosses a periodic face); the
+// reduced-precision lattice kernel sends only those links through the general push.
+__global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, uint32_t* lmask) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= a.N) return;
     uint8_t t = ntype[i];
     bool bulk = is_active(t);
     bool wrap = false;  // some link crosses a periodic face (checked over all 18 links)
+    uint32_t mask = 0;
     if (bulk) {
         const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
-        if (x < 1 || y < 1 || z < 1 || x > a.X - 2 || y > a.Y - 2 || z > a.Z - 2) bulk = false;
-        else
+        if (x < 1 || y < 1 || z < 1 || x > a.X - 2 || y > a.Y - 2 || z > a.Z - 2) {
+            bulk = false;
+            mask = 0x7FFFEu;
+        } else {
             for (int j = 1; j < Q; ++j) {
                 const long long l = init_link(a, pf.v, i, j);
+                const bool wj = l != i + cx(j) + (long long)a.X * (cy(j) + (long long)a.Y * cz(j));
+                if (!is_active(ntype[l]) || wj) mask |= 1u << j;
                 if (!is_active(ntype[l])) bulk = false;
-                if (l != i + cx(j) + (long long)a.X * (cy(j) + (long long)a.Y * cz(j))) wrap = true;
+                if (wj) wrap = true;
             }
+        }
     }
     uint8_t nt = bulk ? (t | HB_BULK) : (t & ~HB_BULK);
     nt = wrap ? (nt | HB_PWRAP) : (nt & ~HB_PWRAP);
     if (nt != t) ntype[i] = nt;
+    if (lmask) lmask[i] = mask;
 }
 
 // ---- upload / download ---------------------------------------------------------------
@@ -569,6 +579,7 @@ LBArgs lb_args(hb_ctx* c, int cur) {
     a.visc = c->visc;
     a.dv = c->dv;
     a.hacc = c->hacc;
+    a.lmask = c->lmask;
     a.F = c->lb_force;
     a.Ff = c->lb_force_f;
     for (int j = 0; j < Q; ++j) {
@@ -636,7 +647,7 @@ int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int 
         k_init_vars<PolF32><<<G, B, 0, c->stream>>>(a, b, mx, F[0], F[1], F[2], iv[0], iv[1], iv[2], c->P.init_visc);
     else
         k_init_vars<PolF16><<<G, B, 0, c->stream>>>(a, b, mx, F[0], F[1], F[2], iv[0], iv[1], iv[2], c->P.init_visc);
-    k_bulk<<<G, B, 0, c->stream>>>(a, pf, c->ntype);
+    k_bulk<<<G, B, 0, c->stream>>>(a, pf, c->ntype, c->lmask);
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (owner) cudaFree(owner);
     cudaFree(mx);
@@ -645,7 +656,7 @@ int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int 
 
 void launch_refresh_bulk(hb_ctx* c) {
     InitArgs a = init_args(c);
-    k_bulk<<<ceil_div(c->N, 256), 256, 0, c->stream>>>(a, per_faces(c), c->ntype);
+    k_bulk<<<ceil_div(c->N, 256), 256, 0, c->stream>>>(a, per_faces(c), c->ntype, c->lmask);
 }
 
 void launch_lb_step(hb_ctx* c, int cur) {

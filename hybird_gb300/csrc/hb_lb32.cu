@@ -174,8 +174,9 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
         }
         element_sums_warp(a.hacc, a.parts.count, key, v);
     }
-    // every link of this node is plain (no wall, no periodic wrap): fixed push offsets
+    // links that need the general push (none for bulk nodes: fixed push offsets)
     const bool fast = (t & (HB_BULK | HB_PWRAP)) == HB_BULK;
+    const uint32_t special = fast ? 0u : a.lmask[i];
     if (!act) return;
     const float Fx = a.Ff[0] + hx, Fy = a.Ff[1] + hy, Fz = a.Ff[2] + hz;
     ux += 0.5f * Fx * inv;  // shiftVelocity
@@ -249,13 +250,10 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
         const float sym = fmaf(c1, f[j] + f[o], fmaf(Kq[q], vu * vu, fmaf(Kc[q] * vu, cF, K0[q])));
         const float anti = fmaf(c2, f[j] - f[o], fmaf(Lu[q], vu, Lf[q] * cF));
         const float gj = sym + anti, go = sym - anti;
-        if (fast) {
-            fo[a.so[j]] = P::enc_store(gj);
-            fo[a.so[o]] = P::enc_store(go);
-        } else {
-            push_general<P>(a, fout, x, y, z, i, j, gj, n, ux, uy, uz, usq);
-            push_general<P>(a, fout, x, y, z, i, o, go, n, ux, uy, uz, usq);
-        }
+        if (special & (1u << j)) push_general<P>(a, fout, x, y, z, i, j, gj, n, ux, uy, uz, usq);
+        else fo[a.so[j]] = P::enc_store(gj);
+        if (special & (1u << o)) push_general<P>(a, fout, x, y, z, i, o, go, n, ux, uy, uz, usq);
+        else fo[a.so[o]] = P::enc_store(go);
     }
 }
 
