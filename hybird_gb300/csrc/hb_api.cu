@@ -254,7 +254,7 @@ int hb_destroy(hb_ctx* c) {
                     c->d.base, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
-                    c->d.claim_list, c->d.claim_cnt, c->d.boxes};
+                    c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -328,6 +328,7 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     if (c->d.E > 0) launch_dem_first_predict(c);
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaGetLastError());
+    if (dem_args_upload(c)) return seterr(HB_ERR_CUDA, "DEM parameter upload: %s", cudaGetErrorString(cudaGetLastError()));
     c->initialized = true;
     if ((rc = build_graph(c))) return rc;
     return HB_OK;

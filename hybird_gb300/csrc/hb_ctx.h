@@ -32,6 +32,7 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     uint32_t* claim_list = nullptr;  // [2N] (node, particle) pairs joined by the coupling in this step
     int* claim_cnt = nullptr;
     void* boxes = nullptr;      // [E] per-particle spheres of the current step (coupling masks)
+    void* gargs = nullptr;      // device copy of the DEM/coupling parameter blocks
     double* scal = nullptr;     // device scalars: [0]=maxDisp [1]=rebuild flag [2]=contacts
     int* contacts = nullptr;    // overlapping pairs counter of the last substep
     double* partial = nullptr;  // per-block maxima for the displacement trigger
@@ -127,6 +128,7 @@ void launch_couple_reduce(hb_ctx* c);
 void launch_fs_step(hb_ctx* c, int cur);
 int fs_init(hb_ctx* c);
 int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o);
+int dem_args_upload(hb_ctx* c);
 int adjoint_run(hb_ctx* c, const hb_adjoint_cfg* cfg, bool reverse, double* J, double* dF, double* dtau,
                 double* duin, std::string& err);
 int adjoint_timing(hb_ctx* c, float* ms_forward, float* ms_reverse, int64_t* fwd_steps, int64_t* rev_steps);

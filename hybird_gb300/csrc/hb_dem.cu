@@ -115,7 +115,7 @@ __device__ double tangential_contact(const DemArgs& a, double vt, double fn, dou
 
 // single CTA: cell of every particle (linearizePosition, vector.cpp:147-149), counting
 // sort into cells, then ascending order inside each cell
-__device__ void nl_cells_block(const DemArgs& a) {
+__device__ __noinline__ void nl_cells_block(const DemArgs& a) {
     const int E = a.E, nc = a.ncells;
     for (int c = threadIdx.x; c < nc; c += blockDim.x) { a.cell_cnt[c] = 0; a.cell_fill[c] = 0; }
     __syncthreads();
@@ -153,7 +153,7 @@ __device__ void nl_cells_block(const DemArgs& a) {
 
 // candidate list of every particle: all others within nebrRange in the 27 adjacent
 // cells; first wall within range (DEM.cpp:1502-1511); objects within range
-__device__ void nl_build_one(const DemArgs& a, int i) {
+__device__ __noinline__ void nl_build_one(const DemArgs& a, int i) {
     const int E = a.E;
     const V xi = ld3(a.x0, E, i);
     const double r2 = a.nebrRange * a.nebrRange;
@@ -200,9 +200,97 @@ __device__ void nl_build_one(const DemArgs& a, int i) {
 }
 
 // ---- forces (DEM.cpp:1114-1182, 1801-2136) --------------------------------------------
+// Contact forces are rare (a handful of overlapping pairs among ~10^4 candidates), so
+// their arithmetic is kept out of line: inlined, it sets the register budget of the whole
+// cooperative kernel and makes every phase spill.  Each takes the running sums and
+// returns them updated, in the reference's order of operations.
+struct FM {
+    V f, m;
+};
+
+// particleParticleCollision with I = lower index (DEM.cpp:1801-1900), seen by particle i
+__device__ __noinline__ FM pp_contact(const DemArgs& a, int i, int I, int J, V vd, double rI, double rJ, V FP,
+                                      V MP) {
+    const int E = a.E;
+    const double dist = sqrt(nrm2(vd));
+    const double overlap = rI + rJ - dist;
+    const V relVel = sub(ld3(a.xp1, E, J), ld3(a.xp1, E, I));
+    const V en = divs(vd, dist);
+    const double vn = dot(relVel, en);
+    const V nrv = mul(vn, en);
+    const double mI = a.m[I], mJ = a.m[J];
+    const double effMass = mI * mJ / (mI + mJ);
+    const double effRad = rI * rJ / (rI + rJ);
+    const double fn = normal_contact(a, overlap, vn, effRad, effMass);
+    const V nf = mul(fn, en);
+    const V vrI = mul(rI, en), vrJ = mul(-rJ, en);
+    const V rvc = add(sub(relVel, cross(ld3(a.wpG, E, I), vrI)), cross(ld3(a.wpG, E, J), vrJ));
+    const V tang = sub(rvc, nrv);
+    const double nt = sqrt(nrm2(tang));
+    V tf{0, 0, 0};
+    const bool hasT = nt != 0.0;
+    if (hasT) {
+        const double ft = tangential_contact(a, nt, fn, effRad, effMass, a.muPart);
+        tf = mul(ft, divs(tang, nt));
+    }
+    if (i == I) {
+        FP = sub(FP, nf);
+        if (hasT) { MP = add(MP, cross(vrI, tf)); FP = add(FP, tf); }
+    } else {
+        FP = add(FP, nf);
+        if (hasT) { MP = sub(MP, cross(vrJ, tf)); FP = sub(FP, tf); }
+    }
+    return FM{FP, MP};
+}
+
+// wallParticleCollision (DEM.cpp:1902-1982), static walls, effective overlap 2x
+__device__ __noinline__ FM wall_contact(const DemArgs& a, V wn, double overlap, V xpv, V wpg, double ri, double mi,
+                                        V FW, V MW) {
+    const V relVel = sub(xpv, V{0, 0, 0});
+    const double vn = dot(relVel, wn);
+    const V nrv = mul(vn, wn);
+    const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
+    const V nf = mul(fn, wn);
+    const V vrJ = mul(-ri, wn);
+    FW = add(FW, nf);
+    const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
+    const double nt = sqrt(nrm2(tang));
+    if (nt != 0.0) {
+        const double ft = tangential_contact(a, nt, fn, ri, mi, a.muWall);
+        const V tfw = mul(ft, divs(tang, nt));
+        MW = sub(MW, cross(vrJ, tfw));
+        FW = sub(FW, tfw);
+    }
+    return FM{FW, MW};
+}
+
+// objectParticleCollision (DEM.cpp:2060-2136), effective overlap 2x, particle friction
+__device__ __noinline__ FM object_contact(const DemArgs& a, int o, V vd, double dist, double overlap, V xpv, V wpg,
+                                          double ri, double mi, V FW, V MW) {
+    const V en = mul(1.0 / dist, vd);
+    const V relVel = sub(xpv, V{a.ox1[o], a.ox1[a.O + o], a.ox1[2 * a.O + o]});
+    const double vn = dot(relVel, en);
+    const V nrv = mul(vn, en);
+    const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
+    const V nf = mul(fn, en);
+    const V vrJ = mul(-ri, en);
+    const V cJ = add(vrJ, V{0, 0, 0});
+    FW = add(FW, nf);
+    const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
+    const double nt = sqrt(nrm2(tang));
+    if (nt != 0.0) {
+        const double ft = tangential_contact(a, nt, fn, ri, mi, a.muPart);
+        const V tfo = mul(ft, divs(tang, nt));
+        MW = sub(MW, cross(cJ, tfo));
+        FW = sub(FW, tfo);
+    }
+    return FM{FW, MW};
+}
+
 // contacts of particle i by one warp: lanes take candidates (and objects) in list
 // order, the sums use a fixed xor-shuffle tree, so the result is reproducible
-__device__ void forces_warp(const DemArgs& a, int i, int lane, int& ncont) {
+// a: the kernel's parameter block; ga: its device-memory copy for the out-of-line calls
+__device__ void forces_warp(const DemArgs& a, const DemArgs& ga, int i, int lane, int& ncont) {
     const int E = a.E;
     const V xpi = ld3(a.xp0, E, i);
     V FP{0, 0, 0}, MP{0, 0, 0}, FW{0, 0, 0}, MW{0, 0, 0};
@@ -217,35 +305,9 @@ __device__ void forces_warp(const DemArgs& a, int i, int lane, int& ncont) {
         if (!(nrm2(vd) < sig * sig)) continue;
         if (i < j) ++ncont;
         contrib = true;
-        // particleParticleCollision with I = lower index (DEM.cpp:1801-1900)
-        const double dist = sqrt(nrm2(vd));
-        const double overlap = rI + rJ - dist;
-        const V relVel = sub(ld3(a.xp1, E, J), ld3(a.xp1, E, I));
-        const V en = divs(vd, dist);
-        const double vn = dot(relVel, en);
-        const V nrv = mul(vn, en);
-        const double mI = a.m[I], mJ = a.m[J];
-        const double effMass = mI * mJ / (mI + mJ);
-        const double effRad = rI * rJ / (rI + rJ);
-        const double fn = normal_contact(a, overlap, vn, effRad, effMass);
-        const V nf = mul(fn, en);
-        const V vrI = mul(rI, en), vrJ = mul(-rJ, en);
-        const V rvc = add(sub(relVel, cross(ld3(a.wpG, E, I), vrI)), cross(ld3(a.wpG, E, J), vrJ));
-        const V tang = sub(rvc, nrv);
-        const double nt = sqrt(nrm2(tang));
-        V tf{0, 0, 0};
-        const bool hasT = nt != 0.0;
-        if (hasT) {
-            const double ft = tangential_contact(a, nt, fn, effRad, effMass, a.muPart);
-            tf = mul(ft, divs(tang, nt));
-        }
-        if (i == I) {
-            FP = sub(FP, nf);
-            if (hasT) { MP = add(MP, cross(vrI, tf)); FP = add(FP, tf); }
-        } else {
-            FP = add(FP, nf);
-            if (hasT) { MP = sub(MP, cross(vrJ, tf)); FP = sub(FP, tf); }
-        }
+        const FM r = pp_contact(ga, i, I, J, vd, rI, rJ, FP, MP);
+        FP = r.f;
+        MP = r.m;
     }
     const double ri = a.rad[i], mi = a.m[i];
     const V xpv = ld3(a.xp1, E, i);
@@ -257,21 +319,9 @@ __device__ void forces_warp(const DemArgs& a, int i, int lane, int& ncont) {
         const double overlap = ri - dist;
         if (overlap > 0.0) {
             contrib = true;
-            const V relVel = sub(xpv, V{0, 0, 0});
-            const double vn = dot(relVel, wn);
-            const V nrv = mul(vn, wn);
-            const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
-            const V nf = mul(fn, wn);
-            const V vrJ = mul(-ri, wn);
-            FW = add(FW, nf);
-            const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
-            const double nt = sqrt(nrm2(tang));
-            if (nt != 0.0) {
-                const double ft = tangential_contact(a, nt, fn, ri, mi, a.muWall);
-                const V tfw = mul(ft, divs(tang, nt));
-                MW = sub(MW, cross(vrJ, tfw));
-                FW = sub(FW, tfw);
-            }
+            const FM r = wall_contact(ga, wn, overlap, xpv, wpg, ri, mi, FW, MW);
+            FW = r.f;
+            MW = r.m;
         }
     }
     const int oc = a.obj_cnt[i];
@@ -282,23 +332,9 @@ __device__ void forces_warp(const DemArgs& a, int i, int lane, int& ncont) {
         const double overlap = ri + a.orad[o] - dist;
         if (!(overlap > 0.0)) continue;
         contrib = true;
-        const V en = mul(1.0 / dist, vd);
-        const V relVel = sub(xpv, V{a.ox1[o], a.ox1[a.O + o], a.ox1[2 * a.O + o]});
-        const double vn = dot(relVel, en);
-        const V nrv = mul(vn, en);
-        const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
-        const V nf = mul(fn, en);
-        const V vrJ = mul(-ri, en);
-        const V cJ = add(vrJ, V{0, 0, 0});
-        FW = add(FW, nf);
-        const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
-        const double nt = sqrt(nrm2(tang));
-        if (nt != 0.0) {
-            const double ft = tangential_contact(a, nt, fn, ri, mi, a.muPart);
-            const V tfo = mul(ft, divs(tang, nt));
-            MW = sub(MW, cross(cJ, tfo));
-            FW = sub(FW, tfo);
-        }
+        const FM r = object_contact(ga, o, vd, dist, overlap, xpv, wpg, ri, mi, FW, MW);
+        FW = r.f;
+        MW = r.m;
     }
     // fixed xor-shuffle tree over the lanes; when at most lane 0 holds a force the tree
     // would only add zeros to it, so it is skipped
@@ -478,7 +514,7 @@ __device__ double correct_one(const DemArgs& a, int i) {  // elmt.cpp:179-254
 // corrector (elmt.cpp:179-254) followed by the next substep's predictor
 // (elmt.cpp:139-177) on registers: every input is loaded before the first store, so the
 // element's loads overlap instead of waiting on each other
-__device__ double correct_predict_one(const DemArgs& a, int i) {
+__device__ __noinline__ double correct_predict_one(const DemArgs& a, int i) {
     const int E = a.E;
     const double dt = a.dt;
     const double* c = a.gc;
@@ -798,7 +834,8 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
         const long long l = l0 + k;
         const uint8_t t = byte_of(tw, k);
         if (t & HB_INSIDE) {
-            if (in_sph(a.tab[sl[k]].s, x, y, z)) continue;  // stays
+            const uint32_t sk = k == 0 ? sl[0] : (k == 1 ? sl[1] : (k == 2 ? sl[2] : sl[3]));  // registers
+            if (in_sph(a.tab[sk].s, x, y, z)) continue;  // stays
             a.ntype[l] = t & ~HB_INSIDE;                     // pop
         }
         const bool ix = x >= 1 && x <= a.X - 2;
@@ -812,21 +849,30 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
         tm[5] = ix ? byte_of(wzp, k) : (uint8_t)0;
         if (!((tm[0] | tm[1] | tm[2] | tm[3] | tm[4] | tm[5]) & HB_INSIDE)) continue;
         const long long ms[6] = {l - 1, l + 1, l - sy, l + sy, l - sz, l + sz};
+        // the six sources' particles in one round of independent loads (own index for
+        // non-sources, a valid address); usually every flagged source has the same one
+        uint32_t qs[6];
+#pragma unroll
+        for (int kk = 0; kk < 6; ++kk) qs[kk] = a.solid[(tm[kk] & HB_INSIDE) ? ms[kk] : l];
+        uint32_t q0 = 0xffffffffu;
+        bool several = false;
+#pragma unroll
+        for (int kk = 0; kk < 6; ++kk)
+            if (tm[kk] & HB_INSIDE) {
+                if (q0 == 0xffffffffu) q0 = qs[kk];
+                else if (qs[kk] != q0) several = true;
+            }
+        const bool cov0 = in_sph(a.tab[q0].s, x, y, z);
+        if (!cov0 && !several) continue;  // just outside its particle: the common case
         unsigned long long best = ~0ull;
-        uint32_t qlast = 0xffffffffu;  // particle whose cover of this node was last decided
-        bool covered = false;
 #pragma unroll
         for (int kk = 0; kk < 6; ++kk) {
             if (!(tm[kk] & HB_INSIDE)) continue;
-            const long long m = ms[kk];
-            const uint32_t q = a.solid[m];
+            const uint32_t q = qs[kk];
             const Sph& sq = a.tab[q].s;
-            if (q != qlast) {  // this node covered by q? (usually not: it lies just outside)
-                covered = in_sph(sq, x, y, z);
-                qlast = q;
-            }
+            const bool covered = q == q0 ? cov0 : in_sph(sq, x, y, z);
             if (!covered || !in_sph(sq, x - cx(kk + 1), y - cy(kk + 1), z - cz(kk + 1))) continue;
-            const unsigned long long key = ((unsigned long long)m << 32) | q;
+            const unsigned long long key = ((unsigned long long)ms[kk] << 32) | q;
             if (key < best) best = key;
         }
         if (best != ~0ull) claim_push(a, l, best);
@@ -835,7 +881,7 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
 
 // element hydrodynamic force, torque and entrained fluid (LB.cpp:1853-1918): fixed
 // thread-to-row assignment and a fixed-order tree, so the sum is reproducible
-__device__ void reduce_block(const CoupleArgs& a, int p, double (*sh)[256]) {
+__device__ __noinline__ void reduce_block(const CoupleArgs& a, int p, double (*sh)[256]) {
     const int E = a.E;
     const Box b = pbox(a, p, 1);
     const double px = a.x0[p], py = a.x0[E + p], pz = a.x0[2 * E + p];
@@ -916,9 +962,17 @@ __global__ void k_convert_sums(CoupleArgs a) {
 //   R  hydrodynamic force of every element from the previous lattice step
 //   D  multiStep DEM substeps: [neighbour rebuild] forces | correct + next predict +
 //      displacement trigger
+constexpr size_t GARGS_COUPLE = 2048;  // byte offset of the CoupleArgs copy in the parameter buffer
+constexpr size_t GARGS_BYTES = 4096;
+
 struct CycleArgs {
     DemArgs d;
     CoupleArgs c;
+    // the same two blocks in device memory, for the out-of-line (rarely taken) paths: a
+    // kernel parameter passed by reference to a non-inlined function would be copied to
+    // every thread's local memory
+    const DemArgs* gd;
+    const CoupleArgs* gc;
     int do_reduce, do_dem, do_boxes, multi;
     unsigned long long* ts;  // optional phase timestamps (ns), written by block 0 after each barrier
 };
@@ -963,7 +1017,7 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
         if (A.c.hacc) {
             for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) convert_sums(A.c, p);
         } else {
-            for (int p = blockIdx.x; p < E; p += gridDim.x) reduce_block(A.c, p, sh);
+            for (int p = blockIdx.x; p < E; p += gridDim.x) reduce_block(*A.gc, p, sh);
         }
     }
     int k = 1;
@@ -975,13 +1029,13 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
         stamp(A, k++);
         for (int s = 0; s < A.multi; ++s) {
             if (rebuild) {
-                if (blockIdx.x == 0) nl_cells_block(A.d);
+                if (blockIdx.x == 0) nl_cells_block(*A.gd);
                 grid.sync();
-                for (int i = gt; i < E; i += gs) nl_build_one(A.d, i);
+                for (int i = gt; i < E; i += gs) nl_build_one(*A.gd, i);
                 grid.sync();  // the contact warps read other threads' candidate lists
             }
             int ncont = 0;
-            for (int i = gw; i < E; i += nw) forces_warp(A.d, i, lane, ncont);
+            for (int i = gw; i < E; i += nw) forces_warp(A.d, *A.gd, i, lane, ncont);
             if (s == A.multi - 1) {  // overlapping pairs of the last substep (integer atomics)
                 for (int off = 16; off > 0; off >>= 1) ncont += __shfl_down_sync(0xffffffffu, ncont, off);
                 if ((threadIdx.x & 31) == 0 && ncont) {
@@ -1001,7 +1055,7 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
                     const bool plain = on && A.d.plain[i];
                     double x1c = 0.0;
                     if (plain) x1c = correct_predict_plain(A.d, i, c, newton_plain(A.d, i, c));
-                    else if (on && c == 0) v2 = fmax(v2, correct_predict_one(A.d, i));
+                    else if (on && c == 0) v2 = fmax(v2, correct_predict_one(*A.gd, i));
                     // |x1|^2 in the reference's order (x*x + y*y) + z*z, gathered at lane c = 0
                     const double y1 = __shfl_down_sync(0xffffffffu, x1c, 1);
                     const double z1 = __shfl_down_sync(0xffffffffu, x1c, 2);
@@ -1146,6 +1200,21 @@ static CoupleArgs couple_args(hb_ctx* c) {
     return a;
 }
 
+// the device copy of the DEM and coupling parameter blocks (constant after init)
+int dem_args_upload(hb_ctx* c) {
+    if (c->d.E == 0) return 0;
+    static_assert(sizeof(DemArgs) <= GARGS_COUPLE, "DemArgs larger than its slot");
+    static_assert(GARGS_COUPLE + sizeof(CoupleArgs) <= GARGS_BYTES, "parameter blocks larger than their buffer");
+    if (!c->d.gargs && cudaMalloc(&c->d.gargs, GARGS_BYTES) != cudaSuccess) return -1;
+    const DemArgs d = dem_args(c);
+    const CoupleArgs cp = couple_args(c);
+    if (cudaMemcpy(c->d.gargs, &d, sizeof(d), cudaMemcpyHostToDevice) != cudaSuccess) return -1;
+    if (cudaMemcpy(reinterpret_cast<char*>(c->d.gargs) + GARGS_COUPLE, &cp, sizeof(cp), cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+        return -1;
+    return 0;
+}
+
 int coop_grid(hb_ctx* c) {
     static int cached = 0;
     if (cached) return cached;
@@ -1165,6 +1234,8 @@ int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsign
     A.ts = ts;
     A.d = dem_args(c);
     A.c = couple_args(c);
+    A.gd = reinterpret_cast<const DemArgs*>(c->d.gargs);
+    A.gc = reinterpret_cast<const CoupleArgs*>(reinterpret_cast<const char*>(c->d.gargs) + GARGS_COUPLE);
     A.do_reduce = do_reduce;
     A.do_dem = do_dem;
     A.do_boxes = do_boxes;
