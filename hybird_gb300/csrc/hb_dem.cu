@@ -596,47 +596,55 @@ __device__ __noinline__ double correct_predict_one(const DemArgs& a, int i) {
 // per element: lanes 0-2 take x, y, z of the position chain, lanes 3-5 of the spin
 // chain.  Same arithmetic per component as correct_predict_one.
 __device__ double correct_predict_plain(const DemArgs& a, int i, int c, double acc) {
+    // Lanes 0-2 run the position chain (2nd order: the corrected derivative is x2, weights
+    // gc2), lanes 3-5 the spin chain (1st order: w1, weights gc1).  Both have the same
+    // shape, so one instruction stream with selected arrays and weights serves the whole
+    // warp (an FP64 warp instruction costs the same whatever its active lanes); the
+    // arithmetic per component is exactly that of each chain.
     const int E = a.E;
-    const double dt = a.dt;
     const double* cc = a.gc;
-    const long long o = (long long)(c % 3) * E + i;
-    if (c < 3) {
-        const double* c2o = a.gc2;
-        const double x2 = acc, p0 = a.xp0[o], p1 = a.xp1[o], p2 = a.xp2[o], p3 = a.xp3[o], p4 = a.xp4[o],
-                     p5 = a.xp5[o];
-        const double d = x2 - p2;
-        const double x0 = p0 + d * c2o[0], x1 = p1 + d * c2o[1], x3 = p3 + d * c2o[3], x4 = p4 + d * c2o[4],
-                     x5 = p5 + d * c2o[5];
-        a.x0[o] = x0; a.x1[o] = x1; a.x2[o] = x2; a.x3[o] = x3; a.x4[o] = x4; a.x5[o] = x5;
-        a.xp0[o] = x0 + x1 * cc[0] + x2 * cc[1] + x3 * cc[2] + x4 * cc[3] + x5 * cc[4];
-        a.xp1[o] = x1 + x2 * cc[0] + x3 * cc[1] + x4 * cc[2] + x5 * cc[3];
-        a.xp2[o] = x2 + x3 * cc[0] + x4 * cc[1] + x5 * cc[2];
-        a.xp3[o] = x3 + x4 * cc[0] + x5 * cc[1];
-        a.xp4[o] = x4 + x5 * cc[0];
-        a.xp5[o] = x5;
-        a.pf[c * E + i] = (float)x0;
-        a.pf[(3 + c) * E + i] = (float)x1;
-        return x1;
+    const bool lin = c < 3;
+    const long long o = (long long)(lin ? c : c - 3) * E + i;
+    double* const v0a = lin ? a.x0 : a.w0;
+    double* const v1a = lin ? a.x1 : a.w1;
+    double* const v2a = lin ? a.x2 : a.w2;
+    double* const v3a = lin ? a.x3 : a.w3;
+    double* const v4a = lin ? a.x4 : a.w4;
+    double* const v5a = lin ? a.x5 : a.w5;
+    double* const n0a = lin ? a.xp0 : a.wp0;
+    double* const n1a = lin ? a.xp1 : a.wp1;
+    double* const n2a = lin ? a.xp2 : a.wp2;
+    double* const n3a = lin ? a.xp3 : a.wp3;
+    double* const n4a = lin ? a.xp4 : a.wp4;
+    double* const n5a = lin ? a.xp5 : a.wp5;
+    double co[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) co[k] = lin ? a.gc2[k] : a.gc1[k];
+    const double p0 = n0a[o], p1 = n1a[o], p2 = n2a[o], p3 = n3a[o], p4 = n4a[o], p5 = n5a[o];
+    const double d = acc - (lin ? p2 : p1);
+    double v0 = p0 + d * co[0], v1 = p1 + d * co[1], v2 = p2 + d * co[2], v3 = p3 + d * co[3],
+           v4 = p4 + d * co[4], v5 = p5 + d * co[5];
+    if (lin) v2 = acc;
+    else v1 = acc;
+    v0a[o] = v0; v1a[o] = v1; v2a[o] = v2; v3a[o] = v3; v4a[o] = v4; v5a[o] = v5;
+    const double n0 = v0 + v1 * cc[0] + v2 * cc[1] + v3 * cc[2] + v4 * cc[3] + v5 * cc[4];
+    n0a[o] = n0;
+    n1a[o] = v1 + v2 * cc[0] + v3 * cc[1] + v4 * cc[2] + v5 * cc[3];
+    n2a[o] = v2 + v3 * cc[0] + v4 * cc[1] + v5 * cc[2];
+    n3a[o] = v3 + v4 * cc[0] + v5 * cc[1];
+    n4a[o] = v4 + v5 * cc[0];
+    n5a[o] = v5;
+    const float f0 = (float)v0, f1 = (float)v1;
+    if (lin) {
+        a.pf[c * E + i] = f0;
+        a.pf[(3 + c) * E + i] = f1;
+        return v1;
     }
-    const double* c1o = a.gc1;
-    const double w1 = acc, p0 = a.wp0[o], p1 = a.wp1[o], p2 = a.wp2[o], p3 = a.wp3[o], p4 = a.wp4[o],
-                 p5 = a.wp5[o];
-    const double d = w1 - p1;
-    const double w0 = p0 + d * c1o[0], w2 = p2 + d * c1o[2], w3 = p3 + d * c1o[3], w4 = p4 + d * c1o[4],
-                 w5 = p5 + d * c1o[5];
-    a.w0[o] = w0; a.w1[o] = w1; a.w2[o] = w2; a.w3[o] = w3; a.w4[o] = w4; a.w5[o] = w5;
-    a.wG[o] = w0;
-    a.wL[o] = w0;
-    const double n0 = w0 + w1 * cc[0] + w2 * cc[1] + w3 * cc[2] + w4 * cc[3] + w5 * cc[4];
-    a.wp0[o] = n0;
-    a.wp1[o] = w1 + w2 * cc[0] + w3 * cc[1] + w4 * cc[2] + w5 * cc[3];
-    a.wp2[o] = w2 + w3 * cc[0] + w4 * cc[1] + w5 * cc[2];
-    a.wp3[o] = w3 + w4 * cc[0] + w5 * cc[1];
-    a.wp4[o] = w4 + w5 * cc[0];
-    a.wp5[o] = w5;
+    a.wG[o] = v0;
+    a.wL[o] = v0;
     a.wpG[o] = n0;
     a.wpL[o] = n0;
-    a.pf[(6 + (c - 3)) * E + i] = (float)w0;
+    a.pf[(6 + (c - 3)) * E + i] = f0;
     return 0.0;
 }
 
