@@ -86,15 +86,16 @@ class GpuSim:
         check(self.L.hb_cycle(self.h, n))
         check(self.L.hb_synchronize(self.h))
 
-    def lattice(self):
+    def lattice(self, fields=None):
+        """Node fields after the last step; `fields` limits the download (e.g. ("type", "n", "u"))."""
         N = self.N
-        out = dict(type=np.zeros(N, np.uint8), inside=np.zeros(N, np.uint8),
-                   solid=np.zeros(N, np.uint32), f=np.zeros(19 * N), n=np.zeros(N),
-                   u=np.zeros(3 * N), mass=np.zeros(N), visc=np.zeros(N),
-                   hydroForce=np.zeros(3 * N))
-        check(self.L.hb_download_lattice(self.h, *[_p(out[k]) for k in
-                                                   ("type", "inside", "solid", "f", "n", "u",
-                                                    "mass", "visc", "hydroForce")]))
+        sizes = dict(type=(N, np.uint8), inside=(N, np.uint8), solid=(N, np.uint32), f=(19 * N, np.float64),
+                     n=(N, np.float64), u=(3 * N, np.float64), mass=(N, np.float64), visc=(N, np.float64),
+                     hydroForce=(3 * N, np.float64))
+        keys = ("type", "inside", "solid", "f", "n", "u", "mass", "visc", "hydroForce")
+        want = keys if fields is None else tuple(fields)
+        out = {k: np.zeros(sizes[k][0], sizes[k][1]) for k in want}
+        check(self.L.hb_download_lattice(self.h, *[_p(out.get(k)) for k in keys]))
         return out
 
     def upload(self, type, inside, solid, f, n, u, mass, visc=None):
