@@ -113,7 +113,7 @@ struct hb_ctx {
 namespace hb {
 int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int E,
                         const double* ob_x0, const double* ob_r, int O);
-void launch_refresh_bulk(hb_ctx* c);
+void launch_refresh_bulk(hb_ctx* c, int* changed = nullptr);
 void launch_lb_step(hb_ctx* c, int cur);
 void launch_lb_step_dev(hb_ctx* c, const LBArgs& a);
 void launch_lb_wallforce(hb_ctx* c, int cur);

@@ -32,6 +32,7 @@ namespace hb {
 
 enum : uint8_t { FS_FILLED = 1, FS_EMPTIED = 2, FS_NEW_A = 4, FS_NEW_B = 8 };
 constexpr int FS_PARTS = 4;  // ledger partials: K3, K4, K5, K6
+constexpr int FS_BLOCK = 128;  // threads per block along x
 
 struct FsArgs {
     int X, Y, Z;
@@ -53,20 +54,58 @@ struct FsArgs {
     const double* force;    // lbF as the free surface sees it (zeroed after the first step
                             // when forceFieldSolve = 0)
     int* first;             // device flag: 1 until the first free-surface step has run
+    int* nconv;             // [3] cells filled / emptied by this step's classify; cells whose
+                            // activity changed (gas <-> interface) in this step
     int blocks;
 };
 
-__device__ __forceinline__ long long fs_link(const FsArgs& a, long long i, int j) {
-    const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
-    int xn = x + cx(j), yn = y + cy(j), zn = z + cz(j);
+// Every pass runs on a 3D grid (x from the thread, y and z from the block), so a node's
+// coordinates come without divisions; neighbours follow the reference's periodic remap.
+struct Node {
+    int x, y, z;
+    long long i;
+    bool ok;
+};
+__device__ __forceinline__ Node node_of(const FsArgs& a) {
+    Node n;
+    n.x = blockIdx.x * blockDim.x + threadIdx.x;
+    n.y = blockIdx.y;
+    n.z = blockIdx.z;
+    n.ok = n.x < a.X;
+    n.i = (long long)n.x + (long long)a.X * ((long long)n.y + (long long)a.Y * n.z);
+    return n;
+}
+// linear block index of the 3D grid (ledger partial slot)
+__device__ __forceinline__ int block_id() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
+
+__device__ __forceinline__ void fs_link3(const FsArgs& a, int x, int y, int z, int j, int& xn, int& yn, int& zn) {
+    xn = x + cx(j); yn = y + cy(j); zn = z + cz(j);
     if (xn == 0 && a.per[0]) xn = a.X - 2; else if (xn == a.X - 1 && a.per[1]) xn = 1;
     if (yn == 0 && a.per[2]) yn = a.Y - 2; else if (yn == a.Y - 1 && a.per[3]) yn = 1;
     if (zn == 0 && a.per[4]) zn = a.Z - 2; else if (zn == a.Z - 1 && a.per[5]) zn = 1;
-    return (long long)xn + (long long)a.X * ((long long)yn + (long long)a.Y * zn);
 }
-__device__ __forceinline__ bool interior(const FsArgs& a, long long i) {
-    const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
+__device__ __forceinline__ long long lin(const FsArgs& a, int x, int y, int z) {
+    return (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
+}
+__device__ __forceinline__ long long fs_link(const FsArgs& a, const Node& n, int j) {
+    int xn, yn, zn;
+    fs_link3(a, n.x, n.y, n.z, j, xn, yn, zn);
+    return lin(a, xn, yn, zn);
+}
+__device__ __forceinline__ bool interior3(const FsArgs& a, int x, int y, int z) {
     return x > 0 && y > 0 && z > 0 && x < a.X - 1 && y < a.Y - 1 && z < a.Z - 1;
+}
+// the interior cell m with link d[m][opp(k)] == n, if any (the reference's neighbour table:
+// interior nodes link arithmetically with the periodic remap, boundary nodes to themselves)
+__device__ __forceinline__ bool source_of(const FsArgs& a, const Node& n, int k, long long& m) {
+    int xm, ym, zm;
+    fs_link3(a, n.x, n.y, n.z, k, xm, ym, zm);
+    if (!interior3(a, xm, ym, zm)) return false;
+    int xb, yb, zb;
+    fs_link3(a, xm, ym, zm, opp(k), xb, yb, zb);
+    if (xb != n.x || yb != n.y || zb != n.z) return false;
+    m = lin(a, xm, ym, zm);
+    return true;
 }
 __device__ __forceinline__ uint8_t code_of(const FsArgs& a, long long i) { return a.ntype[i] & HB_TYPE_MASK; }
 
@@ -79,50 +118,66 @@ __device__ __forceinline__ double fval(const FsArgs& a, int j, long long i) {
 
 // block-sum of one FP64 value into part[k*blocks + block] (fixed-order tree)
 __device__ void block_ledger(const FsArgs& a, int k, double v) {
-    __shared__ double sh[256];
+    __shared__ double sh[FS_BLOCK];
+    // most blocks convert nothing: their partial is 0 without FP64 work (narrow pipe)
+    if (!__syncthreads_or(__double_as_longlong(v) != 0)) {
+        if (threadIdx.x == 0) a.part[(long long)k * a.blocks + block_id()] = 0.0;
+        return;
+    }
     sh[threadIdx.x] = v;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) a.part[(long long)k * a.blocks + blockIdx.x] = sh[0];
+    if (threadIdx.x == 0) a.part[(long long)k * a.blocks + block_id()] = sh[0];
     __syncthreads();
 }
 
 // K1 updateMass (LB.cpp:1492-1590): newMass = mass + sum_j a_j (f[opp j] - fs[j])
 template <class P>
-__global__ void k_fs_mass(FsArgs a) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= a.N) return;
+__global__ void __launch_bounds__(FS_BLOCK) k_fs_mass(FsArgs a) {
+    const Node nd = node_of(a);
+    if (!nd.ok) return;
+    const long long i = nd.i;
     if (code_of(a, i) != HB_T_INTERFACE) return;
     const bool first = *a.first != 0;
     const double mi = a.mass[i];
     double dm = 0.0;
     for (int j = 1; j < Q; ++j) {
-        const long long l = fs_link(a, i, j);
+        const long long l = fs_link(a, nd, j);
         const uint8_t t = code_of(a, l);
         double av = 0.0;
         if (t == HB_T_INTERFACE) av = 0.5 * (a.mass[l] + mi);
         else if (t == HB_T_FLUID) av = 1.0;
         else if (t == HB_T_DYNWALL) av = 1.0 * mi;
         else continue;  // gas, static wall: averageMass 0
-        const double fin = fval<P>(a, opp(j), i);
-        double fs;
-        if (first) fs = fval<P>(a, j, i);  // f = fs = f_eq at initialisation
-        else if (t == HB_T_DYNWALL) {
+        if (t == HB_T_DYNWALL) {  // f[opp j] = fs[j] - BBi: the difference is -BBi
+            const double fin = fval<P>(a, opp(j), i);
             const double uw = a.u[l] * cx(j) + a.u[a.N + l] * cy(j) + a.u[2 * a.N + l] * cz(j);
-            fs = fin + 6.0 * a.rho[i] * wgt(j) * uw;  // f[opp j] = fs[j] - BBi
-        } else fs = fval<P>(a, j, l);              // pushed to the active neighbour
-        dm += 1.0 * av * (fin - fs);
+            const double fs = first ? fval<P>(a, j, i) : fin + 6.0 * a.rho[i] * wgt(j) * uw;
+            dm += 1.0 * av * (fin - fs);
+            continue;
+        }
+        const long long src = first ? i : l;  // fs[j]: f = fs = f_eq at initialisation, else
+                                               // pushed to the active neighbour
+        if (P::DEV) {  // deviations: their FP32 difference is the difference of the populations
+            using S = typename P::S;
+            const S* fp = reinterpret_cast<const S*>(a.f);
+            const float d = P::load(fp + (long long)opp(j) * a.N + i) - P::load(fp + (long long)j * a.N + src);
+            dm += 1.0 * av * (double)d;
+        } else {
+            dm += 1.0 * av * (fval<P>(a, opp(j), i) - fval<P>(a, j, src));
+        }
     }
     a.mass2[i] = mi + dm;
 }
 
 // K2 findInterfaceMutants (LB.cpp:1620-1650)
-__global__ void k_fs_classify(FsArgs a) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= a.N) return;
+__global__ void __launch_bounds__(FS_BLOCK) k_fs_classify(FsArgs a) {
+    const Node nd = node_of(a);
+    if (!nd.ok) return;
+    const long long i = nd.i;
     const uint8_t t = a.ntype[i];
     uint8_t fl = 0;
     if ((t & HB_TYPE_MASK) == HB_T_FLUID) a.mass[i] = a.rho[i];  // fluid mass = n (LB.cpp:1582-1585)
@@ -132,9 +187,12 @@ __global__ void k_fs_classify(FsArgs a) {
         if (m > a.rho[i]) {
             fl = FS_FILLED;
             a.ntype[i] = (t & ~HB_TYPE_MASK) | HB_T_FLUID;
+            atomicAdd(a.nconv, 1);
         } else if (m < 0.0) {
             fl = FS_EMPTIED;
             a.ntype[i] = (t & ~HB_TYPE_MASK) | HB_T_GAS;
+            atomicAdd(a.nconv + 1, 1);
+            atomicAdd(a.nconv + 2, 1);
         }
     }
     a.flag[i] = fl;
@@ -142,15 +200,16 @@ __global__ void k_fs_classify(FsArgs a) {
 
 // K3 smoothenInterface, gas neighbours of filled cells (LB.cpp:1657-1677)
 template <class P>
-__global__ void k_fs_new_from_filled(FsArgs a) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(FS_BLOCK) k_fs_new_from_filled(FsArgs a) {
+    const Node nd = node_of(a);
+    const long long i = nd.i;
     double contrib = 0.0;
-    if (i < a.N && code_of(a, i) == HB_T_GAS && interior(a, i)) {
+    // nothing filled in this step (the usual case): no cell changes, the partial is 0
+    if (a.nconv[0] != 0 && nd.ok && code_of(a, i) == HB_T_GAS && interior3(a, nd.x, nd.y, nd.z)) {
         long long parent = -1;
-        for (int k = 1; k < Q; ++k) {  // filled cell m with link d[m][j] == i
-            const long long m = fs_link(a, i, k);
-            if (!(a.flag[m] & FS_FILLED) || !interior(a, m)) continue;
-            if (fs_link(a, m, opp(k)) != i) continue;
+        for (int k = 1; k < Q; ++k) {  // filled cell m with link d[m][opp k] == i
+            long long m;
+            if (!source_of(a, nd, k, m) || !(a.flag[m] & FS_FILLED)) continue;
             if (m > parent) parent = m;
         }
         if (parent >= 0) {
@@ -178,6 +237,7 @@ __global__ void k_fs_new_from_filled(FsArgs a) {
             }
             a.ntype[i] = (a.ntype[i] & ~HB_TYPE_MASK) | HB_T_INTERFACE;
             a.flag[i] |= FS_NEW_A;
+            atomicAdd(a.nconv + 2, 1);
             contrib = -0.01 * 1.0;
         }
     }
@@ -185,15 +245,15 @@ __global__ void k_fs_new_from_filled(FsArgs a) {
 }
 
 // K4 smoothenInterface, fluid neighbours of emptied cells (LB.cpp:1679-1700)
-__global__ void k_fs_new_from_emptied(FsArgs a) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(FS_BLOCK) k_fs_new_from_emptied(FsArgs a) {
+    const Node nd = node_of(a);
+    const long long i = nd.i;
     double contrib = 0.0;
-    if (i < a.N && code_of(a, i) == HB_T_FLUID && interior(a, i)) {
+    if (a.nconv[1] != 0 && nd.ok && code_of(a, i) == HB_T_FLUID && interior3(a, nd.x, nd.y, nd.z)) {
         bool hit = false;
         for (int k = 1; k < Q && !hit; ++k) {
-            const long long m = fs_link(a, i, k);
-            if (!(a.flag[m] & FS_EMPTIED) || !interior(a, m)) continue;
-            if (fs_link(a, m, opp(k)) == i) hit = true;
+            long long m;
+            if (source_of(a, nd, k, m) && (a.flag[m] & FS_EMPTIED)) hit = true;
         }
         if (hit) {
             const double n = a.rho[i];
@@ -207,10 +267,11 @@ __global__ void k_fs_new_from_emptied(FsArgs a) {
 }
 
 // K5 updateMutants (LB.cpp:1703-1742) and removeIsolated, first pass (LB.cpp:1749-1769)
-__global__ void k_fs_mutants_to_fluid(FsArgs a) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(FS_BLOCK) k_fs_mutants_to_fluid(FsArgs a) {
+    const Node nd = node_of(a);
+    const long long i = nd.i;
     double contrib = 0.0;
-    if (i < a.N) {
+    if (nd.ok) {
         const uint8_t fl = a.flag[i];
         const uint8_t t = code_of(a, i);
         if ((fl & FS_EMPTIED) && !(fl & FS_NEW_A)) {
@@ -222,7 +283,7 @@ __global__ void k_fs_mutants_to_fluid(FsArgs a) {
         if (t == HB_T_INTERFACE) {
             bool gas = false;
             for (int j = 1; j < Q && !gas; ++j)
-                if (code_of(a, fs_link(a, i, j)) == HB_T_GAS) gas = true;
+                if (code_of(a, fs_link(a, nd, j)) == HB_T_GAS) gas = true;
             if (!gas) {
                 contrib += a.mass[i] - a.rho[i];
                 a.mass[i] = a.rho[i];
@@ -234,40 +295,51 @@ __global__ void k_fs_mutants_to_fluid(FsArgs a) {
 }
 
 // K6 removeIsolated, second pass (LB.cpp:1771-1793)
-__global__ void k_fs_isolated_gas(FsArgs a) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(FS_BLOCK) k_fs_isolated_gas(FsArgs a) {
+    const Node nd = node_of(a);
+    const long long i = nd.i;
     double contrib = 0.0;
     int count = 0;
-    if (i < a.N && code_of(a, i) == HB_T_INTERFACE) {
+    if (nd.ok && code_of(a, i) == HB_T_INTERFACE) {
         bool fluid = false;
         for (int j = 1; j < Q && !fluid; ++j)
-            if (code_of(a, fs_link(a, i, j)) == HB_T_FLUID) fluid = true;
+            if (code_of(a, fs_link(a, nd, j)) == HB_T_FLUID) fluid = true;
         if (!fluid) {
             contrib = a.mass[i];
             a.ntype[i] = (a.ntype[i] & ~HB_TYPE_MASK) | HB_T_GAS;
+            atomicAdd(a.nconv + 2, 1);
         } else {
             count = 1;
         }
     }
     block_ledger(a, 3, contrib);
-    __shared__ int shc[256];
+    __shared__ int shc[FS_BLOCK];
     shc[threadIdx.x] = count;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if ((int)threadIdx.x < s) shc[threadIdx.x] += shc[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) a.cnt_part[blockIdx.x] = shc[0];
+    if (threadIdx.x == 0) a.cnt_part[block_id()] = shc[0];
 }
 
-// ledger total (fixed order over kernels and blocks) and interface count
-__global__ void k_fs_ledger(FsArgs a) {
+// ledger total and interface count: k_fs_ledger_part sums fixed chunks of the block
+// partials (one block per chunk, fixed-order tree), k_fs_ledger the chunk sums; zero
+// partials are skipped by an integer test of their bits
+constexpr int FS_LEDGER_CHUNKS = 256;
+
+__global__ void k_fs_ledger_part(FsArgs a, double* csum, long long* ccnt) {
     __shared__ double shs[256];
     __shared__ long long shc[256];
+    const int per = (a.blocks + FS_LEDGER_CHUNKS - 1) / FS_LEDGER_CHUNKS;
+    const int b0 = blockIdx.x * per, b1 = min(a.blocks, b0 + per);
     double s = 0.0;
     long long c = 0;
-    for (int b = threadIdx.x; b < a.blocks; b += blockDim.x) {
-        for (int k = 0; k < FS_PARTS; ++k) s += a.part[(long long)k * a.blocks + b];
+    for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+        for (int k = 0; k < FS_PARTS; ++k) {
+            const double v = a.part[(long long)k * a.blocks + b];
+            if (__double_as_longlong(v) != 0) s += v;
+        }
         c += a.cnt_part[b];
     }
     shs[threadIdx.x] = s;
@@ -275,7 +347,26 @@ __global__ void k_fs_ledger(FsArgs a) {
     __syncthreads();
     for (int k = blockDim.x / 2; k > 0; k >>= 1) {
         if ((int)threadIdx.x < k) {
-            shs[threadIdx.x] += shs[threadIdx.x + k];
+            if (__double_as_longlong(shs[threadIdx.x + k]) != 0) shs[threadIdx.x] += shs[threadIdx.x + k];
+            shc[threadIdx.x] += shc[threadIdx.x + k];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        csum[blockIdx.x] = shs[0];
+        ccnt[blockIdx.x] = shc[0];
+    }
+}
+
+__global__ void k_fs_ledger(FsArgs a, const double* csum, const long long* ccnt) {
+    __shared__ double shs[FS_LEDGER_CHUNKS];
+    __shared__ long long shc[FS_LEDGER_CHUNKS];
+    shs[threadIdx.x] = csum[threadIdx.x];
+    shc[threadIdx.x] = ccnt[threadIdx.x];
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) {
+            if (__double_as_longlong(shs[threadIdx.x + k]) != 0) shs[threadIdx.x] += shs[threadIdx.x + k];
             shc[threadIdx.x] += shc[threadIdx.x + k];
         }
         __syncthreads();
@@ -284,13 +375,16 @@ __global__ void k_fs_ledger(FsArgs a) {
         a.scal[0] = shs[0];
         a.scal[1] = (double)shc[0];
         *a.first = 0;
+        a.nconv[0] = 0;  // counts of the next step's classify
+        a.nconv[1] = 0;
     }
 }
 
 // K7 redistributeMass (LB.cpp:1796-1804)
-__global__ void k_fs_redistribute(FsArgs a) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= a.N || code_of(a, i) != HB_T_INTERFACE) return;
+__global__ void __launch_bounds__(FS_BLOCK) k_fs_redistribute(FsArgs a) {
+    const Node nd = node_of(a);
+    const long long i = nd.i;
+    if (!nd.ok || code_of(a, i) != HB_T_INTERFACE) return;
     a.mass[i] += a.scal[0] / a.scal[1];
 }
 
@@ -315,29 +409,31 @@ static FsArgs fs_args(hb_ctx* c, int cur) {
     a.scal = c->fs_scal;
     a.force = c->fs_force;
     a.first = c->fs_first;
-    a.blocks = ceil_div(c->N, 256);
+    a.nconv = c->fs_first + 1;
+    a.blocks = ceil_div(c->X, FS_BLOCK) * c->Y * c->Z;
     return a;
 }
 
 int fs_init(hb_ctx* c) {
     const long long N = c->N;
-    const int blocks = ceil_div(N, 256);
+    const int blocks = ceil_div(c->X, FS_BLOCK) * c->Y * c->Z;
     if (cudaMalloc(&c->fs_flag, N) != cudaSuccess || cudaMalloc(&c->fs_mass2, sizeof(double) * N) != cudaSuccess ||
-        cudaMalloc(&c->fs_part, sizeof(double) * FS_PARTS * blocks) != cudaSuccess ||
+        cudaMalloc(&c->fs_part, sizeof(double) * (FS_PARTS * blocks + 2 * FS_LEDGER_CHUNKS)) != cudaSuccess ||
         cudaMalloc(&c->fs_cnt, sizeof(int) * blocks) != cudaSuccess ||
         cudaMalloc(&c->fs_scal, sizeof(double) * 2) != cudaSuccess ||
-        cudaMalloc(&c->fs_first, sizeof(int)) != cudaSuccess)
+        cudaMalloc(&c->fs_first, 4 * sizeof(int)) != cudaSuccess)
         return HB_ERR_NOMEM;
     cudaMemset(c->fs_flag, 0, N);
     cudaMemset(c->fs_scal, 0, sizeof(double) * 2);
-    const int one = 1;
-    cudaMemcpy(c->fs_first, &one, sizeof(int), cudaMemcpyHostToDevice);
+    const int init[4] = {1, 0, 0, 0};  // first step; filled / emptied / activity-change counts
+    cudaMemcpy(c->fs_first, init, sizeof(init), cudaMemcpyHostToDevice);
     return cudaGetLastError() == cudaSuccess ? HB_OK : HB_ERR_CUDA;
 }
 
 void launch_fs_step(hb_ctx* c, int cur) {
     FsArgs a = fs_args(c, cur);
-    const int G = a.blocks, B = 256;
+    const dim3 G((unsigned)ceil_div(c->X, FS_BLOCK), (unsigned)c->Y, (unsigned)c->Z);
+    const int B = FS_BLOCK;
     cudaStream_t s = c->stream;
     if (c->P.precision == HB_FP64) k_fs_mass<PolF64><<<G, B, 0, s>>>(a);
     else if (c->P.precision == HB_FP32) k_fs_mass<PolF32><<<G, B, 0, s>>>(a);
@@ -349,9 +445,12 @@ void launch_fs_step(hb_ctx* c, int cur) {
     k_fs_new_from_emptied<<<G, B, 0, s>>>(a);
     k_fs_mutants_to_fluid<<<G, B, 0, s>>>(a);
     k_fs_isolated_gas<<<G, B, 0, s>>>(a);
-    k_fs_ledger<<<1, 256, 0, s>>>(a);
+    double* csum = reinterpret_cast<double*>(c->fs_part + (size_t)FS_PARTS * a.blocks);
+    long long* ccnt = reinterpret_cast<long long*>(csum + FS_LEDGER_CHUNKS);
+    k_fs_ledger_part<<<FS_LEDGER_CHUNKS, 256, 0, s>>>(a, csum, ccnt);
+    k_fs_ledger<<<1, FS_LEDGER_CHUNKS, 0, s>>>(a, csum, ccnt);
     k_fs_redistribute<<<G, B, 0, s>>>(a);
-    launch_refresh_bulk(c);  // node types changed
+    launch_refresh_bulk(c, c->fs_first + 3);  // only when a cell's activity changed
 }
 
 }  // namespace hb

@@ -477,24 +477,33 @@ __global__ void k_init_vars(InitArgs a, LBArgs b, const int* mx, double Fx, doub
 // HB_BULK / HB_PWRAP flags and, for active nodes, the mask of links that are not plain
 // (bit j: the neighbour along j is not active, or the link crosses a periodic face); the
 // reduced-precision lattice kernel sends only those links through the general push.
-__global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, uint32_t* lmask) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= a.N) return;
+// 3D grid (x from the thread, y and z from the block).  With `changed` set, the pass
+// runs only when that counter is non-zero (the free surface changed some cell between
+// gas and interface) and resets it.
+__global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, uint32_t* lmask, int* changed) {
+    if (changed && *changed == 0) return;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= a.X) return;
+    const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
     uint8_t t = ntype[i];
     bool bulk = is_active(t);
     bool wrap = false;  // some link crosses a periodic face (checked over all 18 links)
     uint32_t mask = 0;
     if (bulk) {
-        const int x = (int)(i % a.X), y = (int)((i / a.X) % a.Y), z = (int)(i / ((long long)a.X * a.Y));
         if (x < 1 || y < 1 || z < 1 || x > a.X - 2 || y > a.Y - 2 || z > a.Z - 2) {
             bulk = false;
             mask = 0x7FFFEu;
         } else {
             for (int j = 1; j < Q; ++j) {
-                const long long l = init_link(a, pf.v, i, j);
-                const bool wj = l != i + cx(j) + (long long)a.X * (cy(j) + (long long)a.Y * cz(j));
-                if (!is_active(ntype[l]) || wj) mask |= 1u << j;
-                if (!is_active(ntype[l])) bulk = false;
+                int xn = x + cx(j), yn = y + cy(j), zn = z + cz(j);
+                if (xn == 0 && pf.v[0]) xn = a.X - 2; else if (xn == a.X - 1 && pf.v[1]) xn = 1;
+                if (yn == 0 && pf.v[2]) yn = a.Y - 2; else if (yn == a.Y - 1 && pf.v[3]) yn = 1;
+                if (zn == 0 && pf.v[4]) zn = a.Z - 2; else if (zn == a.Z - 1 && pf.v[5]) zn = 1;
+                const bool wj = xn != x + cx(j) || yn != y + cy(j) || zn != z + cz(j);
+                const long long l = (long long)xn + (long long)a.X * ((long long)yn + (long long)a.Y * zn);
+                const bool act = is_active(ntype[l]);
+                if (!act || wj) mask |= 1u << j;
+                if (!act) bulk = false;
                 if (wj) wrap = true;
             }
         }
@@ -504,6 +513,9 @@ __global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, uint32_t* lmask)
     if (nt != t) ntype[i] = nt;
     if (lmask) lmask[i] = mask;
 }
+
+// resets the activity-change counter after the (conditional) refresh has run
+__global__ void k_bulk_done(int* changed) { *changed = 0; }
 
 // ---- upload / download ---------------------------------------------------------------
 
@@ -647,16 +659,19 @@ int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int 
         k_init_vars<PolF32><<<G, B, 0, c->stream>>>(a, b, mx, F[0], F[1], F[2], iv[0], iv[1], iv[2], c->P.init_visc);
     else
         k_init_vars<PolF16><<<G, B, 0, c->stream>>>(a, b, mx, F[0], F[1], F[2], iv[0], iv[1], iv[2], c->P.init_visc);
-    k_bulk<<<G, B, 0, c->stream>>>(a, pf, c->ntype, c->lmask);
+    k_bulk<<<dim3((unsigned)ceil_div(c->X, 128), (unsigned)c->Y, (unsigned)c->Z), 128, 0, c->stream>>>(
+        a, pf, c->ntype, c->lmask, nullptr);
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (owner) cudaFree(owner);
     cudaFree(mx);
     return e == cudaSuccess ? 0 : -1;
 }
 
-void launch_refresh_bulk(hb_ctx* c) {
+void launch_refresh_bulk(hb_ctx* c, int* changed) {
     InitArgs a = init_args(c);
-    k_bulk<<<ceil_div(c->N, 256), 256, 0, c->stream>>>(a, per_faces(c), c->ntype, c->lmask);
+    k_bulk<<<dim3((unsigned)ceil_div(c->X, 128), (unsigned)c->Y, (unsigned)c->Z), 128, 0, c->stream>>>(
+        a, per_faces(c), c->ntype, c->lmask, changed);
+    if (changed) k_bulk_done<<<1, 1, 0, c->stream>>>(changed);
 }
 
 void launch_lb_step(hb_ctx* c, int cur) {
