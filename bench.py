@@ -23,6 +23,8 @@ fp64_form  the same workload with FP64 populations: step time, FP32 speed-up, an
 adjoint    drag adjoint on the 96^3 channel with 64 fixed spheres (FP32, 2000 steps,
            checkpoints every 100): device time per step of forward + reverse, and dJ/dtau
            against central differences of the FP64 forward.
+configs    MLUPS of configurations 1, 3 and 4 (channel FP64; dam break FP32; 256^3 with
+           16000 spheres in FP32 and FP16 storage).
 
 Multi-GPU: the path does not shard on one box; --gpus N runs N independent replicas
 (one per rank, no collective), value = sum over ranks.
@@ -185,6 +187,32 @@ def fp64_compare(p32, spheres, steps):
     return out
 
 
+def config_rates(steps):
+    """MLUPS of the other configurations (graph-replayed cycles, active nodes at the start):
+    1 = 64x32x32 periodic channel, BGK FP64; 3 = dam break 256x128x128 with free surface,
+    Bingham, Smagorinsky and 500 spheres (FP32); 4 = 256^3 with 16000 spheres (FP32 and
+    FP16-storage)."""
+    from hybird_gb300 import abi
+    from hybird_gb300.gpu import GpuSim
+    from hybird_gb300.workloads import channel, dam_break, precision_box
+    out = {}
+    cases = [("c1_channel_64x32x32_bgk_f64", channel(precision=abi.HB_FP64), None),
+             ("c3_dambreak_256x128x128_f32", *dam_break(abi.HB_FP32)),
+             ("c4_256cube_16000_spheres_f32", *precision_box(abi.HB_FP32)),
+             ("c4_256cube_16000_spheres_f16s", *precision_box(abi.HB_FP16S))]
+    for name, p, spheres in cases:
+        g = GpuSim(p, spheres)
+        t = g.lattice(("type",))["type"]
+        A = int(((t == 0) | (t == 3)).sum())
+        g.cycle(5)
+        ms, ms_lb, _ = g.time_cycles(steps)
+        g.close()
+        out[name] = {"mlups": round(A / (ms / steps * 1e-3) / 1e6, 1), "ms_per_step": round(ms / steps, 4),
+                     "lattice_kernel_ms": round(ms_lb, 4), "active_nodes": A,
+                     "spheres": 0 if spheres is None else len(spheres)}
+    return out
+
+
 def adjoint_measure(steps):
     """Drag adjoint on 96^3 (64 fixed spheres r=6, TRT tau 0.7, FP32, body force 2e-6,
     inlet/outlet planes): device time per step of forward + reverse (checkpoints every
@@ -264,6 +292,8 @@ def main():
     ap.add_argument("--compare-steps", type=int, default=100,
                     help="cycles of the FP64 form run beside the FP32 one (speed-up and error)")
     ap.add_argument("--adjoint-steps", type=int, default=2000, help="0 skips the adjoint measurement")
+    ap.add_argument("--config-steps", type=int, default=50,
+                    help="timed cycles of configurations 1, 3 and 4 (0 skips them)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -325,6 +355,7 @@ def main():
     g.close()
     fp64 = fp64_compare(p, spheres, args.compare_steps) if args.compare_steps > 0 and prec != abi.HB_FP64 else None
     adj = adjoint_measure(args.adjoint_steps) if args.adjoint_steps > 0 else None
+    cfgs = config_rates(args.config_steps) if args.config_steps > 0 else None
     line = {
         "metric": "MLUPS (coupled LBM-DEM step)", "value": round(value, 2), "unit": "MLUPS",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
@@ -351,6 +382,8 @@ def main():
         line["fp64_form"] = fp64
     if adj:
         line["adjoint"] = adj
+    if cfgs:
+        line["configs"] = cfgs
     if rank == 0 and args.cpu_steps > 0:
         threads = os.cpu_count() or 1
         try:

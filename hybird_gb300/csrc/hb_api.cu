@@ -150,14 +150,14 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     CK(cudaMemcpy(d.I, I.data(), sizeof(double) * 3 * E, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(d.rad, e->radius, sizeof(double) * E, cudaMemcpyHostToDevice));
     {  // FP32 copy read by the reduced-precision lattice kernel
-        std::vector<float> pf(9 * (size_t)E);
+        std::vector<float> pf(12 * (size_t)E, 0.0f);  // per particle: centre, velocity, spin, pad
         for (int k = 0; k < E; ++k)
             for (int q = 0; q < 3; ++q) {
-                pf[(size_t)q * E + k] = (float)e->x0[q * E + k];
-                pf[(size_t)(3 + q) * E + k] = (float)x1[q * E + k];
-                pf[(size_t)(6 + q) * E + k] = (float)w0[q * E + k];
+                pf[12 * (size_t)k + q] = (float)e->x0[q * E + k];
+                pf[12 * (size_t)k + 3 + q] = (float)x1[q * E + k];
+                pf[12 * (size_t)k + 6 + q] = (float)w0[q * E + k];
             }
-        if ((rc = dalloc(&d.pf, 9 * (size_t)E))) return rc;
+        if ((rc = dalloc(&d.pf, 12 * (size_t)E))) return rc;
         std::vector<int> plain(E);
         for (int k = 0; k < E; ++k) {
             const bool ident = q0[k] == 1.0 && q0[E + k] == 0.0 && q0[2 * E + k] == 0.0 && q0[3 * E + k] == 0.0;

@@ -117,7 +117,7 @@ struct Particles {          // DEM elements as the coupling sees them (FP64)
     const double* x1;       // [3*E] velocity
     const double* w;        // [3*E] wGlobal
     const double* radius;   // [E]
-    const float* pf;        // [9*E] FP32 copy: centre, velocity, wGlobal (component-major)
+    const float* pf;        // [12*E] FP32 copy per particle: centre, velocity, wGlobal, pad
 };
 
 struct LBArgs {

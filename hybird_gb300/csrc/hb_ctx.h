@@ -16,7 +16,7 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     double *wG, *wL, *wpG, *wpL;
     double *FH, *MH, *FP, *FW, *MP, *MW;
     double *fvol, *m, *I, *rad;
-    float* pf = nullptr;        // [9E] FP32 centre/velocity/wGlobal for the FP32 lattice kernel
+    float* pf = nullptr;        // [12E] FP32 centre/velocity/wGlobal(+pad) per particle for the FP32 lattice kernel
     int* plain = nullptr;       // [E] 1: orientation stays the identity (component-parallel Gear)
     // neighbour structures
     int* cell_of = nullptr;     // [E]

@@ -36,7 +36,7 @@ struct DemArgs {
     double *wG, *wL, *wpG, *wpL;
     double *FH, *MH, *FP, *FW, *MP, *MW;
     double *fvol, *m, *I, *rad;
-    float* pf;
+    float* pf;         // [12E] FP32 centre, velocity, spin (+ pad) per particle
     const int* plain;  // 1: orientation fixed at identity (no quaternion rates)
     int *cell_of, *cell_cnt, *cell_start, *cell_fill, *cell_items;
     int *nbr, *nbr_cnt, *wall_of, *obj, *obj_cnt;
@@ -503,9 +503,10 @@ __device__ double correct_one(const DemArgs& a, int i) {  // elmt.cpp:179-254
         st3(a.wG, E, i, w0);
         st3(a.wL, E, i, project(w0, qadj(q0)));
         v2 = nrm2(x1);
-        a.pf[i] = (float)x0.x; a.pf[E + i] = (float)x0.y; a.pf[2 * E + i] = (float)x0.z;
-        a.pf[3 * E + i] = (float)x1.x; a.pf[4 * E + i] = (float)x1.y; a.pf[5 * E + i] = (float)x1.z;
-        a.pf[6 * E + i] = (float)w0.x; a.pf[7 * E + i] = (float)w0.y; a.pf[8 * E + i] = (float)w0.z;
+        float* pq = a.pf + 12 * (size_t)i;
+        pq[0] = (float)x0.x; pq[1] = (float)x0.y; pq[2] = (float)x0.z;
+        pq[3] = (float)x1.x; pq[4] = (float)x1.y; pq[5] = (float)x1.z;
+        pq[6] = (float)w0.x; pq[7] = (float)w0.y; pq[8] = (float)w0.z;
     }
     return v2;
 }
@@ -575,9 +576,10 @@ __device__ __noinline__ double correct_predict_one(const DemArgs& a, int i) {
     stq(a.q0, E, i, q0); stq(a.q1, E, i, q1); stq(a.q3, E, i, q3); stq(a.q4, E, i, q4); stq(a.q5, E, i, q5);
     st3(a.wG, E, i, w0);
     st3(a.wL, E, i, wL);
-    a.pf[i] = (float)x0.x; a.pf[E + i] = (float)x0.y; a.pf[2 * E + i] = (float)x0.z;
-    a.pf[3 * E + i] = (float)x1.x; a.pf[4 * E + i] = (float)x1.y; a.pf[5 * E + i] = (float)x1.z;
-    a.pf[6 * E + i] = (float)w0.x; a.pf[7 * E + i] = (float)w0.y; a.pf[8 * E + i] = (float)w0.z;
+    float* pq = a.pf + 12 * (size_t)i;
+    pq[0] = (float)x0.x; pq[1] = (float)x0.y; pq[2] = (float)x0.z;
+    pq[3] = (float)x1.x; pq[4] = (float)x1.y; pq[5] = (float)x1.z;
+    pq[6] = (float)w0.x; pq[7] = (float)w0.y; pq[8] = (float)w0.z;
     st3(a.xp0, E, i, nxp0); st3(a.xp1, E, i, nxp1); st3(a.xp2, E, i, nxp2); st3(a.xp3, E, i, nxp3);
     st3(a.xp4, E, i, nxp4); st3(a.xp5, E, i, x5);
     stq(a.qp0, E, i, nqp0); stq(a.qp1, E, i, nqp1); stq(a.qp2, E, i, nqp2); stq(a.qp3, E, i, nqp3);
@@ -636,15 +638,15 @@ __device__ double correct_predict_plain(const DemArgs& a, int i, int c, double a
     n5a[o] = v5;
     const float f0 = (float)v0, f1 = (float)v1;
     if (lin) {
-        a.pf[c * E + i] = f0;
-        a.pf[(3 + c) * E + i] = f1;
+        a.pf[12 * (size_t)i + c] = f0;
+        a.pf[12 * (size_t)i + 3 + c] = f1;
         return v1;
     }
     a.wG[o] = v0;
     a.wL[o] = v0;
     a.wpG[o] = n0;
     a.wpL[o] = n0;
-    a.pf[(6 + (c - 3)) * E + i] = f0;
+    a.pf[12 * (size_t)i + 6 + (c - 3)] = f0;
     return 0.0;
 }
 

@@ -154,13 +154,13 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
         float v[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (act && (t & HB_INSIDE)) {  // LB.cpp:1863-1904 with FP32 particle copies
             const int p = (int)a.solid[i];
-            const int E = a.parts.count;
-            const float* pf = a.parts.pf;
-            const float rx = float(x) - pf[p], ry = float(y) - pf[E + p], rz = float(z) - pf[2 * E + p];
-            const float wx = pf[6 * E + p], wy = pf[7 * E + p], wz = pf[8 * E + p];
-            const float lvx = pf[3 * E + p] + (wy * rz - wz * ry);
-            const float lvy = pf[4 * E + p] + (wz * rx - wx * rz);
-            const float lvz = pf[5 * E + p] + (wx * ry - wy * rx);
+            const float4* pf4 = reinterpret_cast<const float4*>(a.parts.pf) + 3 * (size_t)p;
+            const float4 q0 = pf4[0], q1 = pf4[1], q2 = pf4[2];  // centre, velocity, spin
+            const float rx = float(x) - q0.x, ry = float(y) - q0.y, rz = float(z) - q0.z;
+            const float wx = q1.z, wy = q1.w, wz = q2.x;
+            const float lvx = q0.w + (wy * rz - wz * ry);
+            const float lvy = q1.x + (wz * rx - wx * rz);
+            const float lvz = q1.y + (wx * ry - wy * rx);
             const float m = a.free_surface ? float(a.mass[i]) : 1.0f;
             const float lf = m * inv;
             const float dvx = lf * (ux - lvx), dvy = lf * (uy - lvy), dvz = lf * (uz - lvz);
