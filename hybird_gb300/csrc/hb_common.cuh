@@ -136,7 +136,8 @@ struct LBArgs {
     void* visc;             // T[N] when viscosity is persistent
     void* dv;               // T[3N] direct-forcing term of inside nodes (FP64 kernel)
     unsigned long long* hacc;  // [7E] fixed-point F, M, fluid volume per element (FP32/FP16 kernels)
-    const uint32_t* lmask;  // [N] links of a non-bulk active node that need the general push
+    const unsigned long long* lmask;  // [N] non-bulk active node: bits 0-18 links that need the general
+                                      // push, bits 32-50 links ending on a static wall
     const double* F;        // device body force [3] (zero when forceFieldSolve = 0)
     const float* Ff;        // the same force in FP32 for the reduced-precision kernels
     int ne[Q];              // index offset of link j for nodes whose links do not wrap

@@ -66,7 +66,7 @@ struct hb_ctx {
     size_t sz = 8;              // bytes per stored population
     // lattice
     uint8_t* ntype = nullptr;
-    uint32_t* lmask = nullptr;  // [N] non-plain links of non-bulk active nodes (reduced-precision kernel)
+    unsigned long long* lmask = nullptr;  // [N] general / static-wall links of non-bulk active nodes (FP32/FP16 kernel)
     uint32_t* solid = nullptr;
     void* fA = nullptr;
     void* fB = nullptr;

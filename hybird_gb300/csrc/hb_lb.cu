@@ -480,7 +480,7 @@ __global__ void k_init_vars(InitArgs a, LBArgs b, const int* mx, double Fx, doub
 // 3D grid (x from the thread, y and z from the block).  With `changed` set, the pass
 // runs only when that counter is non-zero (the free surface changed some cell between
 // gas and interface) and resets it.
-__global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, uint32_t* lmask, int* changed) {
+__global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, unsigned long long* lmask, int* changed) {
     if (changed && *changed == 0) return;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     if (x >= a.X) return;
@@ -488,7 +488,8 @@ __global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, uint32_t* lmask,
     uint8_t t = ntype[i];
     bool bulk = is_active(t);
     bool wrap = false;  // some link crosses a periodic face (checked over all 18 links)
-    uint32_t mask = 0;
+    uint32_t mask = 0;  // links that need the general push
+    uint32_t bb = 0;    // links that end on a static wall: plain bounce-back into the node itself
     if (bulk) {
         if (x < 1 || y < 1 || z < 1 || x > a.X - 2 || y > a.Y - 2 || z > a.Z - 2) {
             bulk = false;
@@ -501,8 +502,10 @@ __global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, uint32_t* lmask,
                 if (zn == 0 && pf.v[4]) zn = a.Z - 2; else if (zn == a.Z - 1 && pf.v[5]) zn = 1;
                 const bool wj = xn != x + cx(j) || yn != y + cy(j) || zn != z + cz(j);
                 const long long l = (long long)xn + (long long)a.X * ((long long)yn + (long long)a.Y * zn);
-                const bool act = is_active(ntype[l]);
-                if (!act || wj) mask |= 1u << j;
+                const uint8_t tl = ntype[l];
+                const bool act = is_active(tl);
+                if ((tl & HB_TYPE_MASK) == HB_T_STATWALL) bb |= 1u << j;
+                else if (!act || wj) mask |= 1u << j;
                 if (!act) bulk = false;
                 if (wj) wrap = true;
             }
@@ -511,7 +514,7 @@ __global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, uint32_t* lmask,
     uint8_t nt = bulk ? (t | HB_BULK) : (t & ~HB_BULK);
     nt = wrap ? (nt | HB_PWRAP) : (nt & ~HB_PWRAP);
     if (nt != t) ntype[i] = nt;
-    if (lmask) lmask[i] = mask;
+    if (lmask) lmask[i] = (unsigned long long)mask | ((unsigned long long)bb << 32);
 }
 
 // resets the activity-change counter after the (conditional) refresh has run

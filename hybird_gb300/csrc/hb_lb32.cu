@@ -174,9 +174,11 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
         }
         element_sums_warp(a.hacc, a.parts.count, key, v);
     }
-    // links that need the general push (none for bulk nodes: fixed push offsets)
+    // links that need the general push and links that end on a static wall (none for bulk
+    // nodes: fixed push offsets)
     const bool fast = (t & (HB_BULK | HB_PWRAP)) == HB_BULK;
-    const uint32_t special = fast ? 0u : a.lmask[i];
+    const unsigned long long lm = fast ? 0ull : a.lmask[i];
+    const uint32_t special = (uint32_t)lm, bb = (uint32_t)(lm >> 32);
     if (!act) return;
     const float Fx = a.Ff[0] + hx, Fy = a.Ff[1] + hy, Fz = a.Ff[2] + hz;
     ux += 0.5f * Fx * inv;  // shiftVelocity
@@ -242,18 +244,33 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
     S* fo = fout + i;
     fo[0] = P::enc_store(2.0f * c1 * f[0] + float(wgt(0)) * kb);  // rest population
 #pragma unroll
-    for (int j = 1; j < Q; j += 2) {
+    for (int j = 1; j < Q; j += 2) {  // post-collision values replace f in place
         const int o = j + 1;
         const int q = j <= 6 ? 0 : 1;
         const float vu = cdot(j, ux, uy, uz);
         const float cF = cdot(j, Fx, Fy, Fz);
         const float sym = fmaf(c1, f[j] + f[o], fmaf(Kq[q], vu * vu, fmaf(Kc[q] * vu, cF, K0[q])));
         const float anti = fmaf(c2, f[j] - f[o], fmaf(Lu[q], vu, Lf[q] * cF));
-        const float gj = sym + anti, go = sym - anti;
-        if (special & (1u << j)) push_general<P>(a, fout, x, y, z, i, j, gj, n, ux, uy, uz, usq);
-        else fo[a.so[j]] = P::enc_store(gj);
-        if (special & (1u << o)) push_general<P>(a, fout, x, y, z, i, o, go, n, ux, uy, uz, usq);
-        else fo[a.so[o]] = P::enc_store(go);
+        f[j] = sym + anti;
+        f[o] = sym - anti;
+    }
+    // Push.  The choice among the three forms is made per warp (all lanes that reach this
+    // point), so that a warp of bulk nodes runs only plain stores and a warp next to a
+    // static wall only the selected-offset stores; each form is exact for every lane.
+    const unsigned warp = __activemask();
+    if (__all_sync(warp, lm == 0ull)) {
+#pragma unroll
+        for (int j = 1; j < Q; ++j) fo[a.so[j]] = P::enc_store(f[j]);
+    } else if (__all_sync(warp, special == 0u)) {
+        // a static wall returns the population into the node's own opposite slot
+#pragma unroll
+        for (int j = 1; j < Q; ++j) fo[(bb & (1u << j)) ? opp(j) * N : a.so[j]] = P::enc_store(f[j]);
+    } else {
+#pragma unroll
+        for (int j = 1; j < Q; ++j) {
+            if (special & (1u << j)) push_general<P>(a, fout, x, y, z, i, j, f[j], n, ux, uy, uz, usq);
+            else fo[(bb & (1u << j)) ? opp(j) * N : a.so[j]] = P::enc_store(f[j]);
+        }
     }
 }
 
