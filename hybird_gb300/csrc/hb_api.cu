@@ -250,13 +250,14 @@ int hb_destroy(hb_ctx* c) {
     if (c->graph2) cudaGraphDestroy(c->graph2);
     void* ptrs[] = {c->ntype, c->lmask, c->solid, c->fA, c->fB, c->mode, c->rho, c->u, c->hf, c->mass,
                     c->visc, c->dv, c->hacc, c->status, c->wall_part, c->wall_force, c->fs_force, c->fs_mass2,
-                    c->fs_cnt, c->fs_scal, c->fs_flag, c->fs_first, c->fs_part, c->lb_force, c->lb_force_f, c->d.pf, c->d.plain,
+                    c->fs_cnt, c->fs_scal, c->fs_flag, c->fs_first, c->fs_part, c->lb_force, c->d_stage, c->d.pf, c->d.plain,
                     c->d.base, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
                     c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -290,10 +291,8 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         if ((rc = dalloc(&c->fs_force, 3))) return rc;
     }
     if (!c->lb_force) {
-        if ((rc = dalloc(&c->lb_force, 3))) return rc;
-    }
-    if (!c->lb_force_f) {
-        if ((rc = dalloc(&c->lb_force_f, 3))) return rc;
+        if ((rc = dalloc(&c->lb_force, 5))) return rc;
+        c->lb_force_f = reinterpret_cast<float*>(c->lb_force + 3);
     }
     {
         const float ff[3] = {c->P.force_field ? (float)c->P.lbF[0] : 0.f, c->P.force_field ? (float)c->P.lbF[1] : 0.f,
@@ -389,6 +388,24 @@ static int build_graph(hb_ctx* c) {
     return HB_OK;
 }
 
+namespace hb {
+// concatenation of up to 11 element fields into one staging block (one copy to the host)
+constexpr int STAGE_DOUBLES_PER_ELEMENT = 35;
+struct GatherArgs {
+    const double* src[11];
+    long long off[12];
+    int n;
+};
+
+__global__ void k_gather(GatherArgs g, double* dst) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= g.off[g.n]) return;
+    int k = 0;
+    while (k + 1 < g.n && t >= g.off[k + 1]) ++k;
+    dst[t] = g.src[k][t - g.off[k]];
+}
+}  // namespace hb
+
 static int run_cycles(hb_ctx* c, int n, bool last_mirror) {
     for (int s = 0; s < n; ++s) {
         const int m = (last_mirror && s == n - 1) ? 1 : 0;
@@ -457,11 +474,13 @@ int hb_set_body_force(hb_ctx* c, const double* force) {
     if (!c || !force || !c->initialized) return seterr(HB_ERR_ARG, "null argument or not initialised");
     for (int k = 0; k < 3; ++k) c->P.lbF[k] = force[k];
     if (c->P.force_field) {
-        c->h_force_f[0] = (float)force[0];
-        c->h_force_f[1] = (float)force[1];
-        c->h_force_f[2] = (float)force[2];
-        CK(cudaMemcpyAsync(c->lb_force, force, sizeof(double) * 3, cudaMemcpyHostToDevice, c->stream));
-        CK(cudaMemcpyAsync(c->lb_force_f, c->h_force_f, sizeof(float) * 3, cudaMemcpyHostToDevice, c->stream));
+        // one copy of the FP64 force and its FP32 copy; a copy from pageable memory is
+        // staged before cudaMemcpyAsync returns, so the local block may go out of scope
+        double blk[5];
+        float* ff = reinterpret_cast<float*>(blk + 3);
+        for (int k = 0; k < 3; ++k) { blk[k] = force[k]; ff[k] = (float)force[k]; }
+        ff[3] = 0.0f;
+        CK(cudaMemcpyAsync(c->lb_force, blk, sizeof(blk), cudaMemcpyHostToDevice, c->stream));
     }
     return HB_OK;
 }
@@ -520,19 +539,39 @@ int hb_download_lattice(hb_ctx* c, uint8_t* type, uint8_t* inside, uint32_t* sol
 int hb_download_elements(hb_ctx* c, double* x0, double* x1, double* w, double* q0, double* fhydro, double* mhydro,
                          double* fparticle, double* fwall, double* mparticle, double* mwall, double* fluid_volume) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
-    CK(cudaStreamSynchronize(c->stream));
     const int E = c->d.E;
     if (E == 0) return HB_OK;
-    if (c->reduce_pending) {  // the element forces of the last lattice step (LB.cpp:1851-1919)
-        launch_couple_reduce(c);
-        CK(cudaStreamSynchronize(c->stream));
-    }
+    // Everything is queued on the context stream behind the steps already issued: the
+    // element-force conversion of the last lattice step (LB.cpp:1851-1919), one gather of
+    // the requested fields into a device staging block, one copy into pinned host memory.
+    if (c->reduce_pending) launch_couple_reduce(c);
     struct { double* dst; double* src; int comps; } items[] = {
         {x0, c->d.x[0], 3}, {x1, c->d.x[1], 3}, {w, c->d.wG, 3}, {q0, c->d.q[0], 4}, {fhydro, c->d.FH, 3},
         {mhydro, c->d.MH, 3}, {fparticle, c->d.FP, 3}, {fwall, c->d.FW, 3}, {mparticle, c->d.MP, 3},
         {mwall, c->d.MW, 3}, {fluid_volume, c->d.fvol, 1}};
+    if (!c->d_stage) {
+        int rc = dalloc(&c->d_stage, (size_t)hb::STAGE_DOUBLES_PER_ELEMENT * E);
+        if (rc) return rc;
+        CK(cudaMallocHost((void**)&c->h_stage, sizeof(double) * hb::STAGE_DOUBLES_PER_ELEMENT * E));
+    }
+    hb::GatherArgs g = {};
     for (auto& it : items)
-        if (it.dst) CK(cudaMemcpy(it.dst, it.src, sizeof(double) * it.comps * E, cudaMemcpyDeviceToHost));
+        if (it.dst) {
+            g.src[g.n] = it.src;
+            g.off[g.n + 1] = g.off[g.n] + (long long)it.comps * E;
+            ++g.n;
+        }
+    if (g.n == 0) return HB_OK;
+    const long long total = g.off[g.n];
+    hb::k_gather<<<(unsigned)ceil_div(total, 256), 256, 0, c->stream>>>(g, c->d_stage);
+    CK(cudaMemcpyAsync(c->h_stage, c->d_stage, sizeof(double) * total, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int k = 0;
+    for (auto& it : items)
+        if (it.dst) {
+            memcpy(it.dst, c->h_stage + g.off[k], sizeof(double) * (g.off[k + 1] - g.off[k]));
+            ++k;
+        }
     return HB_OK;
 }
 

@@ -87,9 +87,11 @@ struct hb_ctx {
     bool initialized = false;
     long long steps = 0;
     double* fs_force = nullptr; // device lbF seen by the free-surface init of new cells
-    double* lb_force = nullptr; // device lbF seen by the collision (zero without forceField)
-    float* lb_force_f = nullptr;    // FP32 copy of lb_force
-    float h_force_f[3] = {0.f, 0.f, 0.f};  // host staging of the FP32 force (kept alive for async copies)
+    double* lb_force = nullptr; // device lbF seen by the collision (zero without forceField), 5 doubles:
+                                // the FP64 force and, from byte 24, its FP32 copy
+    float* lb_force_f = nullptr;    // = (float*)(lb_force + 3), not a separate allocation
+    double* d_stage = nullptr;      // device staging of element downloads (35 E doubles)
+    double* h_stage = nullptr;      // pinned host staging of element downloads (35 E doubles)
     // free surface
     double* fs_scal = nullptr;      // [0]=surplus [1]=interface count as double
     uint8_t* fs_flag = nullptr;     // per-node conversion flags of the current step
