@@ -77,6 +77,17 @@ class HbStatus(C.Structure):
                 ("mass_surplus", C.c_double), ("total_mass", C.c_double)]
 
 
+class HbExport(C.Structure):
+    _fields_ = [("max_fluid_speed", C.c_double), ("total_fluid_mass", C.c_double),
+                ("plastic_percent", C.c_double), ("active_nodes", C.c_int64),
+                ("plastic_nodes", C.c_int64), ("max_particle_speed", C.c_double),
+                ("max_particle_spin", C.c_double), ("collision_force", C.c_double),
+                ("hydraulic_force", C.c_double), ("particle_mass", C.c_double),
+                ("object_force", C.c_double * 3), ("energy_kin", C.c_double),
+                ("energy_rot_kin", C.c_double), ("energy_tr_kin", C.c_double),
+                ("energy_grav", C.c_double), ("energy_total", C.c_double)]
+
+
 class HbAdjointCfg(C.Structure):
     _fields_ = [("steps", C.c_int32), ("checkpoint_every", C.c_int32), ("precision", C.c_int32),
                 ("drag_axis", C.c_int32), ("tau", C.c_double), ("body_force", C.c_double * 3),

@@ -12,7 +12,11 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <locale>
+#include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "hb_common.cuh"
@@ -182,8 +186,13 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         (rc = dalloc(&d.cell_fill, d.ncells)) || (rc = dalloc(&d.cell_items, E)) ||
         (rc = dalloc(&d.nbr, (size_t)E * NBR_CAP)) || (rc = dalloc(&d.nbr_cnt, E)) || (rc = dalloc(&d.wall_of, E)) ||
         (rc = dalloc(&d.obj, (size_t)E * OBJ_CAP)) || (rc = dalloc(&d.obj_cnt, E)) || (rc = dalloc(&d.scal, 8)) ||
-        (rc = dalloc(&d.contacts, 1)) || (rc = dalloc(&d.partial, hb::PARTIAL_CAP)) || (rc = dalloc(&d.done, 1)))
+        (rc = dalloc(&d.contacts, 1)) || (rc = dalloc(&d.partial, hb::PARTIAL_CAP)) || (rc = dalloc(&d.done, 1)) ||
+        (rc = dalloc(&d.wrec, (size_t)7 * E)) || (rc = dalloc(&d.orec, (size_t)7 * E * OBJ_CAP)) ||
+        (rc = dalloc(&d.react, (size_t)3 * (MAX_WALLS + d.O))))
         return rc;
+    CK(cudaMemset(d.react, 0, sizeof(double) * 3 * (MAX_WALLS + d.O)));
+    CK(cudaMemset(d.wrec, 0, sizeof(double) * 7 * E));
+    CK(cudaMemset(d.orec, 0, sizeof(double) * 7 * E * OBJ_CAP));
     const double scal0[8] = {0.5 * d.nebrRange, 1.0, 0, 0, 0, 0, 0, 0};  // maxDisp, rebuild
     CK(cudaMemcpy(d.scal, scal0, sizeof(scal0), cudaMemcpyHostToDevice));
     CK(cudaMemset(d.contacts, 0, sizeof(int)));
@@ -254,7 +263,8 @@ int hb_destroy(hb_ctx* c) {
                     c->d.base, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
-                    c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs};
+                    c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
+                    c->io_linked, c->io_part};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -307,6 +317,7 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     c->cur = 0;
     c->reduce_pending = false;
     c->steps = 0;
+    c->dem_stepped = false;
     if (launch_init_lattice(c, e && c->d.E ? c->d.x[0] : nullptr, c->d.E ? c->d.rad : nullptr, c->d.E,
                             c->d.obj_x0, c->d.obj_r, c->d.O))
         return seterr(HB_ERR_CUDA, "lattice init: %s", cudaGetErrorString(cudaGetLastError()));
@@ -411,6 +422,7 @@ static int run_cycles(hb_ctx* c, int n, bool last_mirror) {
         const int m = (last_mirror && s == n - 1) ? 1 : 0;
         CK(cudaMemsetAsync(c->mode, m, sizeof(int), c->stream));
         CK(cudaGraphLaunch(c->gexec[c->cur], c->stream));
+        if (c->P.dem_solve && c->d.E > 0) c->dem_stepped = true;
         if (c->P.lb_solve) {
             c->cur ^= 1;
             c->reduce_pending = true;
@@ -427,6 +439,7 @@ int hb_dem_step(hb_ctx* c) {
     if (c->P.dem_solve && c->d.E > 0) {
         if (launch_cycle_coop(c, 1, 1, 0)) return seterr(HB_ERR_CUDA, "DEM launch: %s", cudaGetErrorString(cudaGetLastError()));
         c->reduce_pending = false;
+        c->dem_stepped = true;
     }
     CK(cudaGetLastError());
     return HB_OK;
@@ -615,15 +628,35 @@ int hb_download_interface(hb_ctx* c, uint32_t* cells, int64_t capacity, int64_t*
 
 int hb_download_walls(hb_ctx* c, double* fhydro, double* fparticle, int32_t* nwalls) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
-    CK(cudaStreamSynchronize(c->stream));
     if (nwalls) *nwalls = c->d.nw;
+    double wr[3 * MAX_WALLS] = {};
+    if (fparticle && c->d.react) {
+        launch_reactions(c);
+        CK(cudaMemcpyAsync(wr, c->d.react, sizeof(wr), cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
     double wf[MAX_WALLS * 3 + 1];
     CK(cudaMemcpy(wf, c->wall_force, sizeof(wf), cudaMemcpyDeviceToHost));
     for (int w = 0; w < c->d.nw; ++w)
         for (int k = 0; k < 3; ++k) {
             if (fhydro) fhydro[3 * w + k] = wf[3 * w + k];
-            if (fparticle) fparticle[3 * w + k] = 0.0;
+            if (fparticle) fparticle[3 * w + k] = wr[3 * w + k];
         }
+    return HB_OK;
+}
+
+int hb_download_objects(hb_ctx* c, double* fparticle, int32_t* nobjects) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    if (nobjects) *nobjects = c->d.O;
+    if (!fparticle || c->d.O == 0) return HB_OK;
+    if (!c->d.react) {  // no moving elements: nothing touches the objects
+        memset(fparticle, 0, sizeof(double) * 3 * c->d.O);
+        return HB_OK;
+    }
+    launch_reactions(c);
+    CK(cudaMemcpyAsync(fparticle, c->d.react + 3 * MAX_WALLS, sizeof(double) * 3 * c->d.O, cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return HB_OK;
 }
 
@@ -652,6 +685,155 @@ int hb_get_status(hb_ctx* c, hb_status* s) {
         s->mass_surplus = sc[0];
         s->interface_cells = (int64_t)sc[1];
     }
+    if (c->P.lb_solve) {
+        hb_export ex;
+        const int rc = hb_export_values(c, &ex);
+        if (rc) return rc;
+        s->active_nodes = ex.active_nodes;
+        s->total_mass = ex.total_fluid_mass;
+    }
+    return HB_OK;
+}
+
+int hb_export_values(hb_ctx* c, hb_export* out) {
+    if (!c || !out || !c->initialized) return seterr(HB_ERR_ARG, "null argument or not initialised");
+    if (hb::io_prepare(c)) return seterr(HB_ERR_CUDA, "output mirror: %s", cudaGetErrorString(cudaGetLastError()));
+    if (c->reduce_pending) launch_couple_reduce(c);      // FHydro of the last lattice step (LB.cpp:1851-1919)
+    if (c->d.E > 0 && c->d.react) hb::launch_reactions(c);  // objects' FParticle of the last substep
+    const double* dev = hb::launch_io_export(c);
+    double v[32];
+    const int ns = hb::io_slot_count();
+    CK(cudaMemcpyAsync(v, dev, sizeof(double) * ns, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    memset(out, 0, sizeof(*out));
+    // slot order of hb_io.cu (IoSlot)
+    out->max_fluid_speed = sqrt(v[0]);
+    out->total_fluid_mass = v[1];
+    out->active_nodes = (int64_t)v[2];
+    out->plastic_nodes = (int64_t)v[3];
+    out->plastic_percent = out->active_nodes ? 100.0 * double(out->plastic_nodes) / double(out->active_nodes) : 0.0;
+    out->max_particle_speed = sqrt(v[4]);
+    out->max_particle_spin = sqrt(v[5]);
+    out->collision_force = v[6];
+    out->hydraulic_force = v[7];
+    out->particle_mass = v[8];
+    out->object_force[0] = v[9]; out->object_force[1] = v[10]; out->object_force[2] = v[11];
+    // DEM::updateEnergy runs at the end of each substep; before the first, zeros
+    if (c->dem_stepped || (c->steps > 0 && c->P.dem_solve && c->d.E > 0)) {
+        out->energy_tr_kin = v[12];
+        out->energy_rot_kin = v[13];
+        out->energy_grav = v[14];
+    }
+    out->energy_kin = out->energy_rot_kin + out->energy_tr_kin;  // energy::updateTotal (utils.cpp:324-327)
+    out->energy_total = out->energy_rot_kin + out->energy_tr_kin + out->energy_grav + 0.0;
+    return HB_OK;
+}
+
+int hb_vtk_fluid_fields(hb_ctx* c, int8_t* type, double* v, double* pressure, double* dyn_visc, double* mass,
+                        uint32_t* solid_index) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    if (!c->P.lb_solve) return seterr(HB_ERR_STATE, "no lattice (lbSolve = 0)");
+    if (hb::io_prepare(c)) return seterr(HB_ERR_CUDA, "output mirror: %s", cudaGetErrorString(cudaGetLastError()));
+    const long long N = c->N;
+    // one device block for the requested arrays, one copy per array
+    const size_t bytes = (type ? N : 0) + (solid_index ? 4 * N : 0) + 8 * N * ((v ? 3 : 0) + (pressure ? 1 : 0) +
+                         (dyn_visc ? 1 : 0) + (mass ? 1 : 0));
+    if (bytes == 0) return HB_OK;
+    uint8_t* blk = nullptr;
+    int rc = dalloc(&blk, bytes + 64);
+    if (rc) return rc;
+    uint8_t* p = blk;
+    auto take = [&](size_t b) { uint8_t* r = p; p += (b + 7) & ~(size_t)7; return r; };
+    double* dv = v ? reinterpret_cast<double*>(take(24 * N)) : nullptr;
+    double* dp = pressure ? reinterpret_cast<double*>(take(8 * N)) : nullptr;
+    double* dvi = dyn_visc ? reinterpret_cast<double*>(take(8 * N)) : nullptr;
+    double* dm = mass ? reinterpret_cast<double*>(take(8 * N)) : nullptr;
+    uint32_t* ds = solid_index ? reinterpret_cast<uint32_t*>(take(4 * N)) : nullptr;
+    int8_t* dt = type ? reinterpret_cast<int8_t*>(take(N)) : nullptr;
+    hb::launch_io_pack(c, dt, dv, dp, dvi, dm, ds);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess && v) e = cudaMemcpy(v, dv, 24 * N, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && pressure) e = cudaMemcpy(pressure, dp, 8 * N, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && dyn_visc) e = cudaMemcpy(dyn_visc, dvi, 8 * N, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && mass) e = cudaMemcpy(mass, dm, 8 * N, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && solid_index) e = cudaMemcpy(solid_index, ds, 4 * N, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && type) e = cudaMemcpy(type, dt, N, cudaMemcpyDeviceToHost);
+    cudaFree(blk);
+    if (e != cudaSuccess) return seterr(HB_ERR_CUDA, "output mirror copy: %s", cudaGetErrorString(e));
+    return HB_OK;
+}
+
+int hb_write_vtk_fluid(hb_ctx* c, const char* path) {
+    if (!c || !path || !c->initialized) return seterr(HB_ERR_ARG, "null argument or not initialised");
+    const long long N = c->N;
+    const bool vis = c->P.non_newtonian != 0, fs = c->P.free_surface != 0, dem = c->P.dem_solve != 0;
+    std::vector<int8_t> type(N);
+    std::vector<double> v(3 * N), pr(N), vi(vis ? N : 0), ms(fs ? N : 0);
+    std::vector<uint32_t> so(dem ? N : 0);
+    int rc = hb_vtk_fluid_fields(c, type.data(), v.data(), pr.data(), vis ? vi.data() : nullptr,
+                                 fs ? ms.data() : nullptr, dem ? so.data() : nullptr);
+    if (rc) return rc;
+    // IO::exportParaviewFluidOld (IO.cpp:698-831): ASCII image data, default stream
+    // formatting; the node loops are formatted in parallel chunks and written in order
+    const int nth = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    auto section = [&](auto&& one) {
+        std::vector<std::string> parts(nth);
+        std::vector<std::thread> th;
+        for (int t = 0; t < nth; ++t)
+            th.emplace_back([&, t] {
+                std::ostringstream os;
+                os.imbue(std::locale::classic());
+                const long long i0 = N * t / nth, i1 = N * (t + 1) / nth;
+                for (long long i = i0; i < i1; ++i) one(os, i);
+                parts[t] = os.str();
+            });
+        for (auto& x : th) x.join();
+        std::string all;
+        for (auto& x : parts) all += x;
+        return all;
+    };
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return seterr(HB_ERR_ARG, "cannot open %s", path);
+    f.imbue(std::locale::classic());
+    const double L = 1.0;
+    f << "<VTKFile type=\"ImageData\" version=\"0.1\">\n";
+    f << " <ImageData WholeExtent=\"0 " << c->X - 1 << " 0 " << c->Y - 1 << " 0 " << c->Z - 1 << "\" "
+      << "Origin=\"0.0 0.0 0.0\" Spacing=\"" << L << " " << L << " " << L << "\">\n";
+    f << "  <Piece Extent=\"0 " << c->X - 1 << " 0 " << c->Y - 1 << " 0 " << c->Z - 1 << "\">\n";
+    f << "   <PointData>\n";
+    f << "    <DataArray type=\"Int8\" Name=\"type\" format=\"ascii\" RangeMin=\"0\" RangeMax=\"8\">\n";
+    f << section([&](std::ostringstream& os, long long i) { os << (int)type[i] << " "; });
+    f << "    </DataArray>\n";
+    f << "    <DataArray type=\"Float64\" Name=\"v\" NumberOfComponents=\"3\" format=\"ascii\">\n";
+    f << section([&](std::ostringstream& os, long long i) {
+        os << v[3 * i] << " " << v[3 * i + 1] << " " << v[3 * i + 2] << " ";
+    });
+    f << "    </DataArray>\n";
+    f << "    <DataArray type=\"Float64\" Name=\"pressure\" format=\"ascii\" RangeMin=\"0\" RangeMax=\"2\">\n";
+    f << section([&](std::ostringstream& os, long long i) { os << pr[i] << " "; });
+    f << "    </DataArray>\n";
+    if (vis) {
+        f << "    <DataArray type=\"Float64\" Name=\"dynVisc\" format=\"ascii\" RangeMin=\"0\" RangeMax=\"2\">\n";
+        f << section([&](std::ostringstream& os, long long i) { os << vi[i] << " "; });
+        f << "    </DataArray>\n";
+    }
+    if (fs) {
+        f << "    <DataArray type=\"Float64\" Name=\"AAAmass\" format=\"ascii\" RangeMin=\"0\" RangeMax=\"2\">\n";
+        f << section([&](std::ostringstream& os, long long i) { os << ms[i] << " "; });
+        f << "    </DataArray>\n";
+    }
+    if (dem) {
+        f << "    <DataArray type=\"Int16\" Name=\"solidIndex\" format=\"ascii\" RangeMin=\"0\" RangeMax=\"8\">\n";
+        f << section([&](std::ostringstream& os, long long i) { os << so[i] << " "; });
+        f << "    </DataArray>\n";
+    }
+    f << "   </PointData>\n";
+    f << "   <CellData>\n";
+    f << "   </CellData>\n";
+    f << "  </Piece>\n";
+    f << " </ImageData>\n";
+    f << "</VTKFile>\n";
+    if (!f) return seterr(HB_ERR_ARG, "write failed: %s", path);
     return HB_OK;
 }
 

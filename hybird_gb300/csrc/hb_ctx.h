@@ -29,6 +29,9 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     int* wall_of = nullptr;     // [E] first wall in range or -1
     int* obj = nullptr;         // [E*OBJ_CAP]
     int* obj_cnt = nullptr;     // [E]
+    double* wrec = nullptr;     // [7E] last substep's wall contact per element: flag, normal, tangential force
+    double* orec = nullptr;     // [7E*OBJ_CAP] the same per (element, object slot)
+    double* react = nullptr;    // [3*(MAX_WALLS + O)] wall and object FParticle (ordered sums of the records)
     uint32_t* claim_list = nullptr;  // [2N] (node, particle) pairs joined by the coupling in this step
     int* claim_cnt = nullptr;
     void* boxes = nullptr;      // [E] per-particle spheres of the current step (coupling masks)
@@ -86,10 +89,13 @@ struct hb_ctx {
     bool has_dynwall = false;
     bool initialized = false;
     long long steps = 0;
+    bool dem_stepped = false;   // a DEM substep has run (particle energies exist)
     double* fs_force = nullptr; // device lbF seen by the free-surface init of new cells
     double* lb_force = nullptr; // device lbF seen by the collision (zero without forceField), 5 doubles:
                                 // the FP64 force and, from byte 24, its FP32 copy
     float* lb_force_f = nullptr;    // = (float*)(lb_force + 3), not a separate allocation
+    uint8_t* io_linked = nullptr;   // [N] output mirror: wall nodes that own a node object
+    void* io_part = nullptr;        // output mirror: per-block partials + result block
     double* d_stage = nullptr;      // device staging of element downloads (35 E doubles)
     double* h_stage = nullptr;      // pinned host staging of element downloads (35 E doubles)
     // free surface
@@ -127,6 +133,13 @@ int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsign
 void launch_couple(hb_ctx* c, bool build_boxes, cudaEvent_t* ev = nullptr);
 void launch_dem_first_predict(hb_ctx* c);
 void launch_couple_reduce(hb_ctx* c);
+void launch_reactions(hb_ctx* c);
+// output mirror (hb_io.cu)
+int io_prepare(hb_ctx* c);
+void launch_io_pack(hb_ctx* c, int8_t* type, double* v, double* pressure, double* visc, double* mass,
+                    uint32_t* solid);
+double* launch_io_export(hb_ctx* c);
+int io_slot_count();  // wall / object FParticle of the last substep into d.react
 void launch_fs_step(hb_ctx* c, int cur);
 int fs_init(hb_ctx* c);
 int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o);

@@ -40,6 +40,7 @@ struct DemArgs {
     const int* plain;  // 1: orientation fixed at identity (no quaternion rates)
     int *cell_of, *cell_cnt, *cell_start, *cell_fill, *cell_items;
     int *nbr, *nbr_cnt, *wall_of, *obj, *obj_cnt;
+    double *wrec, *orec;  // wall / object contact records of the current substep (7 doubles each)
     double* scal;
     int* contacts;
     double* partial;
@@ -243,9 +244,18 @@ __device__ __noinline__ FM pp_contact(const DemArgs& a, int i, int I, int J, V v
     return FM{FP, MP};
 }
 
+// Contact record for the reaction on the wall or object (its FParticle): the normal force
+// it loses and the tangential force it gains, in the order the reference applies them.
+// flag 0: no contact, 1: normal force only, 2: normal and tangential.
+__device__ __forceinline__ void put_rec(double* rec, double flag, V nf, V tf) {
+    rec[0] = flag;
+    rec[1] = nf.x; rec[2] = nf.y; rec[3] = nf.z;
+    rec[4] = tf.x; rec[5] = tf.y; rec[6] = tf.z;
+}
+
 // wallParticleCollision (DEM.cpp:1902-1982), static walls, effective overlap 2x
 __device__ __noinline__ FM wall_contact(const DemArgs& a, V wn, double overlap, V xpv, V wpg, double ri, double mi,
-                                        V FW, V MW) {
+                                        V FW, V MW, double* rec) {
     const V relVel = sub(xpv, V{0, 0, 0});
     const double vn = dot(relVel, wn);
     const V nrv = mul(vn, wn);
@@ -255,18 +265,20 @@ __device__ __noinline__ FM wall_contact(const DemArgs& a, V wn, double overlap, 
     FW = add(FW, nf);
     const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
     const double nt = sqrt(nrm2(tang));
+    V tfw{0, 0, 0};
     if (nt != 0.0) {
         const double ft = tangential_contact(a, nt, fn, ri, mi, a.muWall);
-        const V tfw = mul(ft, divs(tang, nt));
+        tfw = mul(ft, divs(tang, nt));
         MW = sub(MW, cross(vrJ, tfw));
         FW = sub(FW, tfw);
     }
+    put_rec(rec, nt != 0.0 ? 2.0 : 1.0, nf, tfw);  // wallI->FParticle (DEM.cpp:1946, 1977)
     return FM{FW, MW};
 }
 
 // objectParticleCollision (DEM.cpp:2060-2136), effective overlap 2x, particle friction
 __device__ __noinline__ FM object_contact(const DemArgs& a, int o, V vd, double dist, double overlap, V xpv, V wpg,
-                                          double ri, double mi, V FW, V MW) {
+                                          double ri, double mi, V FW, V MW, double* rec) {
     const V en = mul(1.0 / dist, vd);
     const V relVel = sub(xpv, V{a.ox1[o], a.ox1[a.O + o], a.ox1[2 * a.O + o]});
     const double vn = dot(relVel, en);
@@ -278,12 +290,14 @@ __device__ __noinline__ FM object_contact(const DemArgs& a, int o, V vd, double 
     FW = add(FW, nf);
     const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
     const double nt = sqrt(nrm2(tang));
+    V tfo{0, 0, 0};
     if (nt != 0.0) {
         const double ft = tangential_contact(a, nt, fn, ri, mi, a.muPart);
-        const V tfo = mul(ft, divs(tang, nt));
+        tfo = mul(ft, divs(tang, nt));
         MW = sub(MW, cross(cJ, tfo));
         FW = sub(FW, tfo);
     }
+    put_rec(rec, nt != 0.0 ? 2.0 : 1.0, nf, tfo);  // objectI->FParticle (DEM.cpp:2103, 2132)
     return FM{FW, MW};
 }
 
@@ -313,16 +327,20 @@ __device__ void forces_warp(const DemArgs& a, const DemArgs& ga, int i, int lane
     const V xpv = ld3(a.xp1, E, i);
     const V wpg = ld3(a.wpG, E, i);
     const int w = a.wall_of[i];
-    if (lane == 0 && w >= 0) {  // wallParticleCollision (DEM.cpp:1902-1982), static walls
-        const V wn{a.wn[w][0], a.wn[w][1], a.wn[w][2]};
-        const double dist = dot(wn, sub(xpi, V{a.wp[w][0], a.wp[w][1], a.wp[w][2]}));
-        const double overlap = ri - dist;
-        if (overlap > 0.0) {
-            contrib = true;
-            const FM r = wall_contact(ga, wn, overlap, xpv, wpg, ri, mi, FW, MW);
-            FW = r.f;
-            MW = r.m;
+    if (lane == 0) {  // wallParticleCollision (DEM.cpp:1902-1982), static walls
+        bool hit = false;
+        if (w >= 0) {
+            const V wn{a.wn[w][0], a.wn[w][1], a.wn[w][2]};
+            const double dist = dot(wn, sub(xpi, V{a.wp[w][0], a.wp[w][1], a.wp[w][2]}));
+            const double overlap = ri - dist;
+            if (overlap > 0.0) {
+                contrib = hit = true;
+                const FM r = wall_contact(ga, wn, overlap, xpv, wpg, ri, mi, FW, MW, a.wrec + 7 * (long long)i);
+                FW = r.f;
+                MW = r.m;
+            }
         }
+        if (!hit) a.wrec[7 * (long long)i] = 0.0;
     }
     const int oc = a.obj_cnt[i];
     for (int k = lane; k < oc; k += 32) {  // objectParticleCollision (DEM.cpp:2060-2136)
@@ -330,9 +348,13 @@ __device__ void forces_warp(const DemArgs& a, const DemArgs& ga, int i, int lane
         const V vd = sub(xpi, V{a.ox0[o], a.ox0[a.O + o], a.ox0[2 * a.O + o]});
         const double dist = sqrt(nrm2(vd));
         const double overlap = ri + a.orad[o] - dist;
-        if (!(overlap > 0.0)) continue;
+        double* rec = a.orec + 7 * ((long long)i * OBJ_CAP + k);
+        if (!(overlap > 0.0)) {
+            rec[0] = 0.0;
+            continue;
+        }
         contrib = true;
-        const FM r = object_contact(ga, o, vd, dist, overlap, xpv, wpg, ri, mi, FW, MW);
+        const FM r = object_contact(ga, o, vd, dist, overlap, xpv, wpg, ri, mi, FW, MW, rec);
         FW = r.f;
         MW = r.m;
     }
@@ -1144,6 +1166,7 @@ static DemArgs dem_args(hb_ctx* c) {
     a.cell_of = d.cell_of; a.cell_cnt = d.cell_cnt; a.cell_start = d.cell_start;
     a.cell_fill = d.cell_fill; a.cell_items = d.cell_items;
     a.nbr = d.nbr; a.nbr_cnt = d.nbr_cnt; a.wall_of = d.wall_of; a.obj = d.obj; a.obj_cnt = d.obj_cnt;
+    a.wrec = d.wrec; a.orec = d.orec;
     a.scal = d.scal; a.contacts = d.contacts; a.partial = d.partial; a.done = d.done;
     a.ncells = d.ncells; a.nC0 = d.nCells[0]; a.nC1 = d.nCells[1]; a.nC2 = d.nCells[2];
     a.cw0 = d.cellWidth[0]; a.cw1 = d.cellWidth[1]; a.cw2 = d.cellWidth[2];
@@ -1278,6 +1301,46 @@ void launch_couple(hb_ctx* c, bool build, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[2], c->stream);
     k_commit<<<152, 256, 0, c->stream>>>(a);
     if (ev) cudaEventRecord(ev[3], c->stream);
+}
+
+// Wall and object FParticle (DEM.cpp:1123-1129, 1946, 1977, 2103, 2132): reset at every
+// force evaluation, then each contact of the last substep subtracts its normal force and
+// adds its tangential force, in the reference's table order (particles in index order,
+// objects in index order within a particle).  One thread per wall or object replays the
+// records in that order, so the FP64 sums are the reference's own.
+__global__ void k_reactions(DemArgs a, double* react) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.nw + a.O) return;
+    V F{0, 0, 0};
+    if (t < a.nw) {
+        for (int i = 0; i < a.E; ++i) {
+            if (a.wall_of[i] != t) continue;
+            const double* r = a.wrec + 7 * (long long)i;
+            if (r[0] == 0.0) continue;
+            F = sub(F, V{r[1], r[2], r[3]});
+            if (r[0] == 2.0) F = add(F, V{r[4], r[5], r[6]});
+        }
+        react[3 * t] = F.x; react[3 * t + 1] = F.y; react[3 * t + 2] = F.z;
+    } else {
+        const int o = t - a.nw;
+        for (int i = 0; i < a.E; ++i) {
+            const int oc = a.obj_cnt[i];
+            for (int k = 0; k < oc; ++k) {
+                if (a.obj[(long long)i * OBJ_CAP + k] != o) continue;
+                const double* r = a.orec + 7 * ((long long)i * OBJ_CAP + k);
+                if (r[0] == 0.0) continue;
+                F = sub(F, V{r[1], r[2], r[3]});
+                if (r[0] == 2.0) F = add(F, V{r[4], r[5], r[6]});
+            }
+        }
+        double* dst = react + 3 * (MAX_WALLS + o);
+        dst[0] = F.x; dst[1] = F.y; dst[2] = F.z;
+    }
+}
+
+void launch_reactions(hb_ctx* c) {
+    if (c->d.E == 0 || !c->d.react) return;
+    k_reactions<<<ceil_div(c->d.nw + c->d.O, 64), 64, 0, c->stream>>>(dem_args(c), c->d.react);
 }
 
 void launch_couple_reduce(hb_ctx* c) {

@@ -40,6 +40,10 @@ def lib():
     L.hb_download_pairs.argtypes = [vp, vp, C.c_int64, P(C.c_int64)]
     L.hb_download_interface.argtypes = [vp, vp, C.c_int64, P(C.c_int64)]
     L.hb_download_walls.argtypes = [vp, vp, vp, P(C.c_int32)]
+    L.hb_download_objects.argtypes = [vp, vp, P(C.c_int32)]
+    L.hb_export_values.argtypes = [vp, P(abi.HbExport)]
+    L.hb_vtk_fluid_fields.argtypes = [vp] + [vp] * 6
+    L.hb_write_vtk_fluid.argtypes = [vp, C.c_char_p]
     L.hb_get_status.argtypes = [vp, P(abi.HbStatus)]
     L.hb_time_cycles.argtypes = [vp, C.c_int32, P(C.c_float), P(C.c_float), P(C.c_int32)]
     L.hb_profile_phases.argtypes = [vp, C.c_int32, vp, P(C.c_int32)]
@@ -130,6 +134,36 @@ class GpuSim:
         fp = np.zeros(18)
         check(self.L.hb_download_walls(self.h, _p(fh), _p(fp), C.byref(nw)))
         return fh[:3 * nw.value], fp[:3 * nw.value]
+
+    def objects(self):
+        """objects[].FParticle of the last substep, [3*O] (x, y, z per object)."""
+        no = C.c_int32(0)
+        check(self.L.hb_download_objects(self.h, None, C.byref(no)))
+        fp = np.zeros(3 * max(no.value, 1))
+        check(self.L.hb_download_objects(self.h, _p(fp), C.byref(no)))
+        return fp[:3 * no.value]
+
+    def export_values(self):
+        """The export.dat quantities of the current state (hb_export) as a dict."""
+        e = abi.HbExport()
+        check(self.L.hb_export_values(self.h, C.byref(e)))
+        out = {k: getattr(e, k) for k, _ in abi.HbExport._fields_}
+        out["object_force"] = np.array(e.object_force[:])
+        return out
+
+    def vtk_fields(self):
+        """Per-node arrays of the fluid image-data file (type, v [N,3], pressure, dynVisc,
+        mass, solidIndex)."""
+        N = self.N
+        out = {"type": np.zeros(N, np.int8), "v": np.zeros(3 * N), "pressure": np.zeros(N),
+               "dyn_visc": np.zeros(N), "mass": np.zeros(N), "solid_index": np.zeros(N, np.uint32)}
+        check(self.L.hb_vtk_fluid_fields(self.h, *[_p(out[k]) for k in
+                                                   ("type", "v", "pressure", "dyn_visc", "mass", "solid_index")]))
+        out["v"] = out["v"].reshape(N, 3)
+        return out
+
+    def write_vtk(self, path):
+        check(self.L.hb_write_vtk_fluid(self.h, str(path).encode()))
 
     def status(self):
         s = abi.HbStatus()

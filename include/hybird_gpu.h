@@ -125,6 +125,23 @@ typedef struct hb_status {
     double  total_mass;        /* FP64 sum of mass over active non-particle nodes            */
 } hb_status;
 
+/* Output-step quantities of the reference's export.dat line (IO::outputStep,
+ * IO.cpp:132-198) and of DEM::updateEnergy (DEM.cpp:2226-2276), in lattice units. */
+typedef struct hb_export {
+    double  max_fluid_speed;      /* sqrt(max |u|^2) over active nodes (IO.cpp:835-851)         */
+    double  total_fluid_mass;     /* sum of mass over active nodes outside particles (IO.cpp:987-999) */
+    double  plastic_percent;      /* 100 * plastic / active (IO.cpp:969-985)                     */
+    int64_t active_nodes;         /* fluid + interface nodes                                     */
+    int64_t plastic_nodes;        /* active nodes with visc > 0.95 (1.8 - 0.5) / 3               */
+    double  max_particle_speed;   /* sqrt(max |x1|^2) over elements (IO.cpp:853-862)             */
+    double  max_particle_spin;    /* sqrt(max |wGlobal|^2) (IO.cpp:864-871)                      */
+    double  collision_force;      /* sum |FParticle| + |FWall| in element order (IO.cpp:1074-1084) */
+    double  hydraulic_force;      /* sum |FHydro| in element order (IO.cpp:1064-1072)            */
+    double  particle_mass;        /* sum of element masses (IO.cpp:1001-1010)                    */
+    double  object_force[3];      /* sum of objects' FParticle (IO.cpp:1097-1106)                */
+    double  energy_kin, energy_rot_kin, energy_tr_kin, energy_grav, energy_total;
+} hb_export;
+
 typedef struct hb_ctx hb_ctx;
 
 /* ---- lifecycle ------------------------------------------------------------------- */
@@ -179,8 +196,29 @@ int hb_download_elements(hb_ctx* ctx, double* x0, double* x1, double* w, double*
 int hb_download_pairs(hb_ctx* ctx, uint32_t* pairs, int64_t capacity, int64_t* count);
 /* Interface cells, ascending node index.  *count receives the count. */
 int hb_download_interface(hb_ctx* ctx, uint32_t* cells, int64_t capacity, int64_t* count);
-/* Per-wall hydrodynamic force (walls[].FHydro, LB.cpp:1334) [3*nwalls]; *nwalls = count. */
+/* Per-wall hydrodynamic force (walls[].FHydro, LB.cpp:1334) and particle force
+ * (walls[].FParticle of the last substep, DEM.cpp:1123-1125, 1946, 1977) [3*nwalls];
+ * *nwalls = count.  Either array may be NULL. */
 int hb_download_walls(hb_ctx* ctx, double* fhydro, double* fparticle, int32_t* nwalls);
+/* ---- output mirror (IO.cpp:132-198, 698-1104) ------------------------------------- */
+/* The export.dat quantities of the current state, computed on the device: node sums in
+ * a fixed order (deterministic, not the reference's sequential rounding), element sums
+ * in element order (the reference's own).  Call after hb_cycle/hb_synchronize. */
+int hb_export_values(hb_ctx* ctx, hb_export* out);
+/* The per-node arrays of IO::exportParaviewFluidOld (IO.cpp:698-831) packed on the
+ * device: type (1 for nodes inside a particle, else the type code), v [3*N] (x, y, z per
+ * node), pressure 0.3333333 (n - 1), dynVisc, mass, solidIndex; zero for nodes that own
+ * no node object (gas, periodic, walls no non-wall node links to).  Any pointer may be
+ * NULL.  Node fields are those of the last full mirror (hb_cycle's last step). */
+int hb_vtk_fluid_fields(hb_ctx* ctx, int8_t* type, double* v, double* pressure, double* dyn_visc,
+                        double* mass, uint32_t* solid_index);
+/* Writes the fluid image-data file of IO::exportParaviewFluidOld (same layout and default
+ * stream formatting; dynVisc with nonNewtonianSolve, AAAmass with freeSurfaceSolve,
+ * solidIndex with demSolve). */
+int hb_write_vtk_fluid(hb_ctx* ctx, const char* path);
+/* Per-object particle force (objects[].FParticle of the last substep, DEM.cpp:1127-1129,
+ * 2103, 2132) [3*nobjects], summed in the reference's contact order; *nobjects = count. */
+int hb_download_objects(hb_ctx* ctx, double* fparticle, int32_t* nobjects);
 int hb_get_status(hb_ctx* ctx, hb_status* status);
 
 /* ---- measurement ------------------------------------------------------------------- */

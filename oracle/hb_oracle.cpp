@@ -1204,6 +1204,17 @@ int hbo_get_walls(const hbo_sim* s, double* fhydro, double* fparticle, int32_t* 
     return 0;
 }
 
+int hbo_get_objects(const hbo_sim* s, double* fparticle, int32_t* nobjects) {
+    const size_t O = s->obj.size();
+    if (nobjects) *nobjects = (int32_t)O;
+    for (size_t k = 0; k < O && fparticle; ++k) {
+        fparticle[3 * k] = s->obj[k].fparticle.x;
+        fparticle[3 * k + 1] = s->obj[k].fparticle.y;
+        fparticle[3 * k + 2] = s->obj[k].fparticle.z;
+    }
+    return 0;
+}
+
 double hbo_total_mass(const hbo_sim* s) {
     double m = 0.0;
     for (size_t i = 0; i < s->N; ++i)

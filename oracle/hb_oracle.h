@@ -45,6 +45,8 @@ int hbo_get_elements(const hbo_sim* s, double* x0, double* x1, double* w, double
 int64_t hbo_get_pairs(const hbo_sim* s, uint32_t* pairs, int64_t capacity);
 int64_t hbo_get_interface(const hbo_sim* s, uint32_t* cells, int64_t capacity);
 int hbo_get_walls(const hbo_sim* s, double* fhydro, double* fparticle, int32_t* nwalls);
+/* objects[].FParticle of the last substep (DEM.cpp:2103, 2132) [3*nobjects] */
+int hbo_get_objects(const hbo_sim* s, double* fparticle, int32_t* nobjects);
 double hbo_total_mass(const hbo_sim* s);
 int hbo_dem_scalars(const hbo_sim* s, double* out /* demTime,maxDisp,nebrRange,deltat */);
 /* drag on the objects along axis from the last step's post-collision populations */

@@ -3,7 +3,7 @@
 // tests/golden/ can be generated from the reference itself.  Nothing in the product
 // links or calls this file.
 //
-// Usage:  ref_dump <config.cfg> <workdir> <out.bin> <step> [<step> ...] [--gasbox fx fz]
+// Usage:  ref_dump <config.cfg> <workdir> <out.bin> <step> [<step> ...] [--gasbox fx fz] [--vtk]
 //
 // The driver mirrors hybird.cpp:245-344 (main): parseCommandLine -> parseConfigFile ->
 // io.initialize -> lb.latticeDefinition -> dem.discreteElementInit ->
@@ -14,6 +14,10 @@
 // 324-340) and marks gas where x >= fx*lbSizeX or z >= fz*lbSizeZ before the generic
 // interface loops (LB.cpp:787-814) run; this is the dam-break column used for the
 // free-surface fixtures, for which the reference has no problemName case.
+//
+// Besides the state, each record set holds the reference's own output-step quantities:
+// objects[].FParticle, the IO data-elaboration functions (IO.cpp:969-1106) and, with
+// --vtk, the text IO::exportParaviewFluidOld writes (IO.cpp:698-831).
 
 #include <cstdio>
 #include <cstdlib>
@@ -46,6 +50,8 @@ void goCycle(IO& io, DEM& dem, LB& lb);
 namespace {
 
 FILE* g_out = nullptr;
+bool g_vtk = false;
+std::string g_work;
 
 // record: char name[32]; uint32 dtype (0=f64,1=u32,2=u8,3=i64); uint64 count; payload
 void put(const char* name, uint32_t dtype, uint64_t count, const void* data, size_t esz) {
@@ -138,6 +144,40 @@ void dump(IO& io, DEM& dem, LB& lb, long step) {
                               dem.particleEnergy.trKin, dem.particleEnergy.rotKin,
                               dem.particleEnergy.grav};
     put_f64("dem_scalars", dm);
+    std::vector<double> of;
+    for (auto& o : dem.objects) { vec3(of, o.FParticle); }
+    put_f64("o_FParticle", of);
+
+    // IO::outputStep quantities (IO.cpp:132-198).  The two maximum-speed lines
+    // (IO.cpp:835-876) only print, so their maxima are taken here the same way.
+    double maxFluid = 0.0;
+    int64_t active = 0;
+    for (size_t i = 0; i < N; ++i)
+        if (lb.types[i].isActive()) {
+            maxFluid = std::max(maxFluid, lb.nodes[i]->u.norm2());
+            ++active;
+        }
+    double maxPart = 0.0, maxSpin = 0.0;
+    for (auto& e : dem.elmts) {
+        maxPart = std::max(maxPart, e.x1.norm2());
+        maxSpin = std::max(maxSpin, e.wGlobal.norm2());
+    }
+    const tVect objF = io.totForceObject(dem.objects);
+    std::vector<double> iv = {
+        sqrt(maxFluid), N ? io.totFluidMass(lb) : 0.0, (N && active) ? io.totPlastic(lb) : 0.0, (double)active,
+        sqrt(maxPart), sqrt(maxSpin), io.collisionForceTot(dem.elmts), io.hydraulicForceTot(dem.elmts),
+        io.totParticleMass(dem.elmts), objF.x, objF.y, objF.z,
+        dem.particleEnergy.kin, dem.particleEnergy.rotKin, dem.particleEnergy.trKin,
+        dem.particleEnergy.grav, dem.particleEnergy.total};
+    put_f64("io_values", iv);
+    if (g_vtk && N) {
+        const std::string path = g_work + "/fluid_dump.vti";
+        io.exportParaviewFluidOld(lb, path);
+        std::ifstream in(path, std::ios::binary);
+        std::string txt((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+        std::vector<uint8_t> bytes(txt.begin(), txt.end());
+        put_u8("vtk", bytes);
+    }
 }
 
 }  // namespace
@@ -148,11 +188,14 @@ int main(int argc, char** argv) {
         return 2;
     }
     std::string cfg = argv[1], work = argv[2], outp = argv[3];
+    g_work = work;
     std::vector<long> steps;
     bool gasbox = false;
     double gfx = 1.0, gfz = 1.0;
     for (int a = 4; a < argc; ++a) {
-        if (!strcmp(argv[a], "--gasbox") && a + 2 < argc) {
+        if (!strcmp(argv[a], "--vtk")) {
+            g_vtk = true;
+        } else if (!strcmp(argv[a], "--gasbox") && a + 2 < argc) {
             gasbox = true;
             gfx = atof(argv[a + 1]);
             gfz = atof(argv[a + 2]);

@@ -5,7 +5,11 @@ reference's own GetPot format) plus particle/object files, runs ``oracle/_ref/re
 (the unmodified reference sources, built by ``make -C oracle ref``) with
 OMP_NUM_THREADS=1 -- coupled force sums in the reference are thread-order dependent
 (LB.cpp:1897) -- and stores the reference's FP64 state at the listed step counts as a
-compressed ``<case>.npz``.
+compressed ``<case>.npz``, with the reference's output-step quantities (``io_values``:
+maximum fluid speed, IO::totFluidMass, IO::totPlastic, active count, maximum particle
+speed and spin, IO::collisionForceTot, IO::hydraulicForceTot, IO::totParticleMass,
+IO::totForceObject, particle energies kin/rotKin/trKin/grav/total) and, for the steps
+listed under ``vtk``, the text of IO::exportParaviewFluidOld.
 
 Run in a container that has the reference tree:
 
@@ -84,12 +88,12 @@ CASES = {
                  nonNewtonianSolve=1, plasticVisc=1.0 / 30.0, yieldStress=3e-6,
                  turbulenceSolve=1, turbConst=0.01,
                  boundary0=4, boundary1=4, boundary2=7, boundary3=7, boundary4=4, boundary5=4),
-        spheres=[], objects=[], steps=[0, 1, 10], full=[0, 1, 10]),
+        spheres=[], objects=[], steps=[0, 1, 10], full=[0, 1, 10], vtk=[10]),
     # closed box with a few spheres: DEM + direct-forcing coupling (LB.cpp:1851-2033)
     "box_spheres": dict(
         cfg=dict(lbSizeX=16, lbSizeY=14, lbSizeZ=16, lbFZ=-2e-4, initVisc=0.1, multiStep=3,
                  boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
-        spheres=("rsa", 11, 7, 2.2, 3.2), objects=[], steps=[0, 1, 2, 10, 30], full=[1, 30]),
+        spheres=("rsa", 11, 7, 2.2, 3.2), objects=[], steps=[0, 1, 2, 10, 30], full=[1, 30], vtk=[30]),
     # DEM only (no LB): spheres against walls and fixed objects (DEM.cpp:1668-2136)
     "dem_objects": dict(
         # particles stay > nebrRange from the side walls: the reference keeps only the
@@ -104,7 +108,8 @@ CASES = {
     "dambreak_fs": dict(
         cfg=dict(lbSizeX=20, lbSizeY=8, lbSizeZ=12, lbFZ=-5e-4, initVisc=0.05, freeSurfaceSolve=1,
                  boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
-        spheres=[], objects=[], gasbox=(0.4, 0.6), steps=[0, 1, 2, 5, 20, 60, 150], full=[0, 1, 20, 150]),
+        spheres=[], objects=[], gasbox=(0.4, 0.6), steps=[0, 1, 2, 5, 20, 60, 150], full=[0, 1, 20, 150],
+        vtk=[60]),
 }
 
 
@@ -175,6 +180,8 @@ def run_case(name, spec):
         cmd = [REF_DUMP, cpath, os.path.join(tmp, "work"), out] + [str(s) for s in spec["steps"]]
         if spec.get("gasbox"):
             cmd += ["--gasbox", str(spec["gasbox"][0]), str(spec["gasbox"][1])]
+        if spec.get("vtk"):
+            cmd += ["--vtk"]
         env = dict(os.environ, OMP_NUM_THREADS="1")
         subprocess.run(cmd, check=True, cwd=tmp, env=env, stdout=subprocess.DEVNULL, timeout=120)
         snaps = parse_dump(out)
@@ -206,10 +213,12 @@ def run_case(name, spec):
             if step in spec["full"]:
                 store[p + "f"] = s["f"]
                 store[p + "hydroForce"] = s["hydroForce"]
+            if step in spec.get("vtk", []):
+                store[p + "vtk"] = s["vtk"]
         for k in ("e_x0", "e_x1", "e_x2", "e_w", "e_q0", "e_FHydro", "e_MHydro", "e_FParticle",
                   "e_FWall", "e_MParticle", "e_MWall", "e_fluidVolume", "e_m", "e_I",
                   "neighborTable", "nearWallTable", "nearObjectTable", "w_FParticle",
-                  "dem_scalars"):
+                  "dem_scalars", "o_FParticle", "io_values"):
             store[p + k] = s[k]
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **store)
     return len(snaps)

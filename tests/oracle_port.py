@@ -47,6 +47,7 @@ def oracle_lib():
     lib.hbo_get_interface.restype = C.c_int64
     lib.hbo_get_interface.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
     lib.hbo_get_walls.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.hbo_get_objects.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     lib.hbo_total_mass.restype = C.c_double
     lib.hbo_total_mass.argtypes = [C.c_void_p]
     lib.hbo_dem_scalars.argtypes = [C.c_void_p, C.c_void_p]
@@ -147,6 +148,13 @@ class OracleSim:
         fp = np.zeros(3 * max(nw.value, 1))
         self.lib.hbo_get_walls(self.h, _p(fh), _p(fp), C.byref(nw))
         return fh[:3 * nw.value], fp[:3 * nw.value]
+
+    def objects(self):
+        no = C.c_int32(0)
+        self.lib.hbo_get_objects(self.h, None, C.byref(no))
+        fp = np.zeros(3 * max(no.value, 1))
+        self.lib.hbo_get_objects(self.h, _p(fp), C.byref(no))
+        return fp[:3 * no.value]
 
     def total_mass(self):
         return self.lib.hbo_total_mass(self.h)
