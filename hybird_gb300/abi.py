@@ -13,6 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libhybird_gpu.so")
 
 HB_OK = 0
+HB_ERR_ARG, HB_ERR_UNSUPPORTED, HB_ERR_CUDA, HB_ERR_NOMEM = 1, 2, 3, 4
+HB_ERR_CAPACITY, HB_ERR_STATE, HB_ERR_NUMERIC = 5, 6, 7
 HB_FP64, HB_FP32, HB_FP16S = 0, 1, 2
 HB_BGK, HB_TRT = 0, 1
 HB_LINEAR, HB_HERTZIAN = 0, 1

@@ -43,6 +43,14 @@ int seterr(int code, const char* fmt, ...) {
                           __FILE__, __LINE__);                                        \
     } while (0)
 
+}  // namespace
+
+namespace hb {
+int set_error(int code, const char* msg) { return seterr(code, "%s", msg); }
+}  // namespace hb
+
+namespace {
+
 template <class T>
 int dalloc(T** p, size_t count) {
     if (count == 0) count = 1;
@@ -112,7 +120,7 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         if (P.boundary[k] == HB_T_PERIODIC)
             return seterr(HB_ERR_UNSUPPORTED, "moving particles with periodic boundaries (ghost particles) are not implemented");
     // element fields, one allocation (elmt.h:53-135)
-    const int nfields = 6 * 3 * 4 + 6 * 4 * 2 + 4 * 3 + 6 * 3 + 1 + 1 + 3 + 1;
+    const int nfields = DEM_FIELDS;
     int rc;
     if ((rc = dalloc(&d.base, (size_t)nfields * E))) return rc;
     CK(cudaMemset(d.base, 0, sizeof(double) * nfields * E));
@@ -480,6 +488,14 @@ int hb_cycle(hb_ctx* c, int32_t nsteps) {
     int rc = run_cycles(c, nsteps, true);
     if (rc) return rc;
     CK(cudaGetLastError());
+    return HB_OK;
+}
+
+int hb_get_params(hb_ctx* c, hb_params* out, int32_t* elements, int32_t* objects) {
+    if (!c) return seterr(HB_ERR_ARG, "null ctx");
+    if (out) *out = c->P;
+    if (elements) *elements = c->d.E;
+    if (objects) *objects = c->d.O;
     return HB_OK;
 }
 

@@ -8,6 +8,10 @@
 
 #include "hb_common.cuh"
 
+// doubles per element in hb_dem_dev::base: x, xp, w, wp (6 x 3 each), q, qp (6 x 4 each),
+// wG, wL, wpG, wpL, FH, MH, FP, FW, MP, MW (3 each), fvol, m, I (3), rad
+constexpr int DEM_FIELDS = 6 * 3 * 4 + 6 * 4 * 2 + 4 * 3 + 6 * 3 + 1 + 1 + 3 + 1;
+
 struct hb_dem_dev {             // element state, FP64, component-major [3E] / [4E]
     int E = 0;
     double* base = nullptr;     // one allocation holding every field below
@@ -134,6 +138,8 @@ void launch_couple(hb_ctx* c, bool build_boxes, cudaEvent_t* ev = nullptr);
 void launch_dem_first_predict(hb_ctx* c);
 void launch_couple_reduce(hb_ctx* c);
 void launch_reactions(hb_ctx* c);
+int set_error(int code, const char* msg);  // hb_last_error text, returns code
+void fs_buffer_bytes(const hb_ctx* c, size_t* part, size_t* cnt);
 // output mirror (hb_io.cu)
 int io_prepare(hb_ctx* c);
 void launch_io_pack(hb_ctx* c, int8_t* type, double* v, double* pressure, double* visc, double* mass,

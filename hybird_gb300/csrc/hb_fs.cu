@@ -414,6 +414,12 @@ static FsArgs fs_args(hb_ctx* c, int cur) {
     return a;
 }
 
+void fs_buffer_bytes(const hb_ctx* c, size_t* part, size_t* cnt) {
+    const size_t blocks = (size_t)ceil_div(c->X, FS_BLOCK) * c->Y * c->Z;
+    *part = sizeof(double) * (FS_PARTS * blocks + 2 * FS_LEDGER_CHUNKS);
+    *cnt = sizeof(int) * blocks;
+}
+
 int fs_init(hb_ctx* c) {
     const long long N = c->N;
     const int blocks = ceil_div(c->X, FS_BLOCK) * c->Y * c->Z;

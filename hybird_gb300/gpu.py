@@ -44,6 +44,10 @@ def lib():
     L.hb_export_values.argtypes = [vp, P(abi.HbExport)]
     L.hb_vtk_fluid_fields.argtypes = [vp] + [vp] * 6
     L.hb_write_vtk_fluid.argtypes = [vp, C.c_char_p]
+    L.hb_get_params.argtypes = [vp, P(abi.HbParams), P(C.c_int32), P(C.c_int32)]
+    L.hb_checkpoint_save.argtypes = [vp, C.c_char_p]
+    L.hb_checkpoint_load.argtypes = [C.c_char_p, P(vp)]
+    L.hb_write_recycle_particles.argtypes = [vp, C.c_char_p]
     L.hb_get_status.argtypes = [vp, P(abi.HbStatus)]
     L.hb_time_cycles.argtypes = [vp, C.c_int32, P(C.c_float), P(C.c_float), P(C.c_int32)]
     L.hb_profile_phases.argtypes = [vp, C.c_int32, vp, P(C.c_int32)]
@@ -77,6 +81,17 @@ class GpuSim:
         X, Y, Z = params.lb_size
         self.N = X * Y * Z
         self.E = 0 if self.arrays.el is None else self.arrays.el.count
+
+    def _adopt(self, L, h):
+        """Wrap a context created by the library itself (hb_checkpoint_load)."""
+        self.L, self.h = L, h
+        self.params = abi.HbParams()
+        ne, no = C.c_int32(0), C.c_int32(0)
+        check(L.hb_get_params(h, C.byref(self.params), C.byref(ne), C.byref(no)))
+        self.arrays = None
+        X, Y, Z = self.params.lb_size
+        self.N = X * Y * Z
+        self.E = ne.value
 
     def close(self):
         if getattr(self, "h", None):
@@ -164,6 +179,23 @@ class GpuSim:
 
     def write_vtk(self, path):
         check(self.L.hb_write_vtk_fluid(self.h, str(path).encode()))
+
+    def save(self, path):
+        """Full-state checkpoint (hb_checkpoint_save)."""
+        check(self.L.hb_checkpoint_save(self.h, str(path).encode()))
+
+    def write_recycle(self, path):
+        check(self.L.hb_write_recycle_particles(self.h, str(path).encode()))
+
+    @classmethod
+    def load(cls, path):
+        """A simulation restored from a checkpoint file (hb_checkpoint_load)."""
+        L = lib()
+        h = C.c_void_p()
+        check(L.hb_checkpoint_load(str(path).encode(), C.byref(h)))
+        g = cls.__new__(cls)
+        g._adopt(L, h)
+        return g
 
     def status(self):
         s = abi.HbStatus()

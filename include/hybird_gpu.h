@@ -174,6 +174,9 @@ int hb_coupling_step(hb_ctx* ctx);   /* LB::latticeBoltzmannCouplingStep LB.cpp:
 int hb_lb_step(hb_ctx* ctx);         /* LB::latticeBolzmannStep         LB.cpp:221-233  */
 /* nsteps whole cycles (DEM, free surface, coupling, LB) replayed from one CUDA graph. */
 int hb_cycle(hb_ctx* ctx, int32_t nsteps);
+/* The context's parameters (as last set: lbF follows hb_set_body_force) and its element
+ * and object counts; any pointer may be NULL. */
+int hb_get_params(hb_ctx* ctx, hb_params* out, int32_t* elements, int32_t* objects);
 /* Changes the body force lbF used by the collision from the next step on (the reference
  * reads lb.lbF every collision, LB.cpp:1098-1111; problem code may change it). */
 int hb_set_body_force(hb_ctx* ctx, const double* force /* [3] */);
@@ -200,6 +203,21 @@ int hb_download_interface(hb_ctx* ctx, uint32_t* cells, int64_t capacity, int64_
  * (walls[].FParticle of the last substep, DEM.cpp:1123-1125, 1946, 1977) [3*nwalls];
  * *nwalls = count.  Either array may be NULL. */
 int hb_download_walls(hb_ctx* ctx, double* fhydro, double* fparticle, int32_t* nwalls);
+/* ---- checkpoint / restart ---------------------------------------------------------- */
+/* No counterpart in the reference (its .restart file, DEM.cpp:2337-2420, is DEM metadata
+ * and its recycle file six-digit particle rows).  Saves every device buffer that carries
+ * state between steps plus the host step state; a context loaded from the file continues
+ * bit-identically to the one that saved it.  The file is specific to this library
+ * version and to the host's byte order. */
+int hb_checkpoint_save(hb_ctx* ctx, const char* path);
+/* Builds a new context (hb_create + hb_init from the saved parameters, particles and
+ * objects) and restores the saved state into it. */
+int hb_checkpoint_load(const char* path, hb_ctx** out);
+/* IO::exportRecycleParticles (IO.cpp:486-535): the particle-file rows (index size radius
+ * x0 x1 w0 q0 q1) of the current elements, default stream formatting, readable as a
+ * particle file (DEM.cpp:81-127). */
+int hb_write_recycle_particles(hb_ctx* ctx, const char* path);
+
 /* ---- output mirror (IO.cpp:132-198, 698-1104) ------------------------------------- */
 /* The export.dat quantities of the current state, computed on the device: node sums in
  * a fixed order (deterministic, not the reference's sequential rounding), element sums

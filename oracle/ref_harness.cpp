@@ -17,7 +17,8 @@
 //
 // Besides the state, each record set holds the reference's own output-step quantities:
 // objects[].FParticle, the IO data-elaboration functions (IO.cpp:969-1106) and, with
-// --vtk, the text IO::exportParaviewFluidOld writes (IO.cpp:698-831).
+// --vtk, the text IO::exportParaviewFluidOld writes (IO.cpp:698-831) and the particle
+// recycle file of IO::exportRecycleParticles (IO.cpp:486-535).
 
 #include <cstdio>
 #include <cstdlib>
@@ -177,6 +178,15 @@ void dump(IO& io, DEM& dem, LB& lb, long step) {
         std::string txt((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
         std::vector<uint8_t> bytes(txt.begin(), txt.end());
         put_u8("vtk", bytes);
+    }
+    if (g_vtk && !dem.elmts.empty()) {  // IO::exportRecycleParticles (IO.cpp:486-535)
+        io.exportRecycleParticles(dem.elmts, dem.pbcs);
+        std::stringstream ss;
+        ss << io.partDirectory << "/recycle_" << io.currentTimeStep << ".dat";
+        std::ifstream in(ss.str(), std::ios::binary);
+        std::string txt((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+        std::vector<uint8_t> bytes(txt.begin(), txt.end());
+        put_u8("recycle", bytes);
     }
 }
 

@@ -9,7 +9,8 @@ compressed ``<case>.npz``, with the reference's output-step quantities (``io_val
 maximum fluid speed, IO::totFluidMass, IO::totPlastic, active count, maximum particle
 speed and spin, IO::collisionForceTot, IO::hydraulicForceTot, IO::totParticleMass,
 IO::totForceObject, particle energies kin/rotKin/trKin/grav/total) and, for the steps
-listed under ``vtk``, the text of IO::exportParaviewFluidOld.
+listed under ``vtk``, the text of IO::exportParaviewFluidOld and of
+IO::exportRecycleParticles.
 
 Run in a container that has the reference tree:
 
@@ -103,7 +104,7 @@ CASES = {
                  boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
         spheres=("rsa", 5, 14, 1.6, 2.6, (9.5, 9.5, 6.0), (22.5, 22.5, 28.0)),
         objects=[(13.0, 14.0, 4.0, 3.0), (19.0, 17.0, 3.5, 2.5)],
-        steps=[0, 1, 50, 100, 150], full=[]),
+        steps=[0, 1, 50, 100, 150], full=[], vtk=[50]),
     # free-surface dam break (LB.cpp:1492-1804), column x < 0.4 Lx, z < 0.6 Lz
     "dambreak_fs": dict(
         cfg=dict(lbSizeX=20, lbSizeY=8, lbSizeZ=12, lbFZ=-5e-4, initVisc=0.05, freeSurfaceSolve=1,
@@ -215,6 +216,8 @@ def run_case(name, spec):
                 store[p + "hydroForce"] = s["hydroForce"]
             if step in spec.get("vtk", []):
                 store[p + "vtk"] = s["vtk"]
+        if step in spec.get("vtk", []) and "recycle" in s:
+            store[p + "recycle"] = s["recycle"]
         for k in ("e_x0", "e_x1", "e_x2", "e_w", "e_q0", "e_FHydro", "e_MHydro", "e_FParticle",
                   "e_FWall", "e_MParticle", "e_MWall", "e_fluidVolume", "e_m", "e_I",
                   "neighborTable", "nearWallTable", "nearObjectTable", "w_FParticle",

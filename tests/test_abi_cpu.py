@@ -61,3 +61,19 @@ def test_create_rejects_bad_parameters_without_gpu(field, value, code):
     rc = lib.hb_create(C.byref(p), C.byref(h))
     assert rc == code, (rc, lib.hb_last_error())
     assert not h.value
+
+
+def test_checkpoint_load_rejects_a_foreign_file_without_gpu(tmp_path):
+    """hb_checkpoint_load validates the header before it builds a context."""
+    _ensure_built()
+    lib = C.CDLL(abi.LIB_PATH)
+    lib.hb_last_error.restype = C.c_char_p
+    lib.hb_checkpoint_load.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+    bad = tmp_path / "not_a_checkpoint.bin"
+    bad.write_bytes(b"HBCKPT99" + bytes(64))
+    h = C.c_void_p()
+    assert lib.hb_checkpoint_load(str(bad).encode(), C.byref(h)) == abi.HB_ERR_ARG
+    assert not h.value
+    assert b"checkpoint" in lib.hb_last_error()
+    missing = tmp_path / "missing.bin"
+    assert lib.hb_checkpoint_load(str(missing).encode(), C.byref(h)) == abi.HB_ERR_ARG

@@ -1,0 +1,110 @@
+"""Full-state checkpoint/restart (hb_checkpoint_save / hb_checkpoint_load) and the
+particle recycle file (IO::exportRecycleParticles, IO.cpp:486-535).
+
+Restart: a run that saves after k1 steps and continues k2 steps must end bit-identical
+to a context loaded from the file and stepped k2 times (every node field, population,
+element field, candidate pair and interface cell compared exactly).  Recycle file:
+against the text the reference itself writes (fixture), token by token, numbers allowed
+to differ only in the last of their six printed digits."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from hybird_gb300 import abi
+from hybird_gb300.workloads import rsa_spheres
+from oracle_port import golden_gasbox, golden_params, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu():
+    from hybird_gb300.gpu import GpuSim
+    return GpuSim
+
+
+def _state(g):
+    out = {"lat_" + k: v for k, v in g.lattice().items()}
+    if g.E:
+        out.update({"el_" + k: v for k, v in g.elements().items()})
+        out["pairs"] = g.pairs()
+    if g.params.free_surface:
+        out["interface"] = g.interface()
+    fh, fp = g.walls()
+    out["walls_fh"], out["walls_fp"] = fh, fp
+    ex = g.export_values()
+    out["export"] = np.array([ex[k] for k in ("max_fluid_speed", "total_fluid_mass", "active_nodes",
+                                              "hydraulic_force", "energy_total")], dtype=np.float64)
+    return out
+
+
+def _coupled_box(precision):
+    sph = rsa_spheres(7, 24, 3.0, 4.5, (2.0, 2.0, 2.0), (38.0, 38.0, 38.0))
+    p = abi.make_params((40, 40, 40), (7,) * 6, init_visc=0.1, lbF=(0, 0, -2e-5), precision=precision,
+                        collision=abi.HB_TRT, multi_step=3)
+    return p, sph, None
+
+
+def _dambreak():
+    d = load_golden("dambreak_fs")
+    return golden_params(d, gas_box=golden_gasbox("dambreak_fs")), None, None
+
+
+CASES = {
+    "coupled_fp32": lambda: _coupled_box(abi.HB_FP32),
+    "coupled_fp16s": lambda: _coupled_box(abi.HB_FP16S),
+    "coupled_fp64": lambda: _coupled_box(abi.HB_FP64),
+    "dambreak_fp64": _dambreak,
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("k1,k2", [(7, 9), (10, 0)])
+def test_restart_continues_bit_identically(name, k1, k2):
+    p, sph, obj = CASES[name]()
+    G = _gpu()
+    a = G(p, sph, obj)
+    a.cycle(k1)
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "state.hbck")
+        a.save(path)
+        if k2:
+            a.cycle(k2)
+        b = G.load(path)
+        if k2:
+            b.cycle(k2)
+        else:  # a checkpoint of the restored context is the same file
+            path2 = os.path.join(tmp, "state2.hbck")
+            b.save(path2)
+            assert open(path, "rb").read() == open(path2, "rb").read()
+        sa, sb = _state(a), _state(b)
+        assert sa.keys() == sb.keys()
+        for k in sa:
+            np.testing.assert_array_equal(sa[k], sb[k], err_msg=f"{name}: {k}")
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("name,step,late", [("box_spheres", 30, False), ("dem_objects", 50, False)])
+def test_recycle_file_matches_reference(name, step, late):
+    d = load_golden(name)
+    p = golden_params(d, gas_box=golden_gasbox(name))
+    g = _gpu()(p, d["spheres"], d["objects"])
+    g.cycle(step)
+    ref = bytes(d[f"s{step}_recycle"]).decode()
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "recycle.dat")
+        g.write_recycle(path)
+        ours = open(path).read()
+    assert ours.count("\n") == ref.count("\n")
+    a, b = ours.split(), ref.split()
+    assert len(a) == len(b)
+    bad = 0
+    for x, y in zip(a, b):
+        if x != y:
+            assert abs(float(x) - float(y)) <= 1e-5 * max(abs(float(y)), 1e-300), (x, y)
+            bad += 1
+    print(f"{name} step {step}: {len(a)} tokens, {bad} differ in the last printed digit")
+    assert bad <= 2
+    g.close()
