@@ -57,6 +57,7 @@ class HbParams(C.Structure):
         ("num_visc", C.c_double),
         ("cap_pairs", C.c_int64),
         ("cap_interface", C.c_int64),
+        ("slip_coefficient", C.c_double),
     ]
 
 
@@ -110,7 +111,8 @@ def make_params(lb_size, boundary, init_visc=0.1, lbF=(0.0, 0.0, 0.0), force_fie
                 collision=HB_BGK, trt_magic=3.0 / 16.0, precision=HB_FP64, gas_box=(0.0, 0.0),
                 lb_solve=1, dem_solve=1, multi_step=1, contact_model=HB_LINEAR, density=2.5,
                 linear_stiff=1e3, young_mod=1.0, poisson=0.3, restitution=0.8, visc_tang=0.5,
-                friction_part=0.5, friction_wall=0.5, num_visc=0.0, cap_pairs=0, cap_interface=0):
+                friction_part=0.5, friction_wall=0.5, num_visc=0.0, cap_pairs=0, cap_interface=0,
+                slip_coefficient=0.0):
     p = HbParams()
     p.lb_size[:] = list(lb_size)
     p.boundary[:] = list(boundary)
@@ -144,6 +146,7 @@ def make_params(lb_size, boundary, init_visc=0.1, lbF=(0.0, 0.0, 0.0), force_fie
     p.num_visc = num_visc
     p.cap_pairs = cap_pairs
     p.cap_interface = cap_interface
+    p.slip_coefficient = slip_coefficient
     return p
 
 

@@ -66,9 +66,14 @@ int check_params(const hb_params* p) {
         if (p->units[k] != 1.0) return seterr(HB_ERR_UNSUPPORTED, "units must be 1 (lattice units)");
     for (int k = 0; k < 6; ++k) {
         const int b = p->boundary[k];
-        if (b != HB_T_PERIODIC && b != HB_T_STATWALL && b != HB_T_DYNWALL)
-            return seterr(HB_ERR_UNSUPPORTED, "boundary%d = %d: only 4 (periodic), 7, 8 are implemented", k, b);
+        if (b != HB_T_PERIODIC && !(b >= HB_T_SLIPSTAT && b <= HB_T_DYNWALL))
+            return seterr(HB_ERR_UNSUPPORTED, "boundary%d = %d: only 4 (periodic), 5, 6 (slip), 7, 8 are implemented",
+                          k, b);
     }
+    if (!(p->slip_coefficient >= 0.0 && p->slip_coefficient <= 1.0)) return seterr(HB_ERR_ARG, "slip_coefficient");
+    for (int k = 0; k < 6; ++k)
+        if (p->free_surface && p->boundary[k] == HB_T_SLIPDYN)
+            return seterr(HB_ERR_UNSUPPORTED, "moving slip walls (6) with a free surface are not implemented");
     if (!(p->init_visc > 0.0)) return seterr(HB_ERR_ARG, "init_visc must be > 0");
     if (p->precision < HB_FP64 || p->precision > HB_FP16S) return seterr(HB_ERR_ARG, "precision");
     if (p->collision != HB_BGK && p->collision != HB_TRT) return seterr(HB_ERR_ARG, "collision");
@@ -91,9 +96,9 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     d.nw = 0;
     for (int k = 0; k < 6; ++k) {
         const int b = P.boundary[k];
-        if (b == HB_T_STATWALL || b == HB_T_DYNWALL) {
+        if (b == HB_T_SLIPSTAT || b == HB_T_SLIPDYN || b == HB_T_STATWALL || b == HB_T_DYNWALL) {
             for (int q = 0; q < 3; ++q) { d.wall_p[d.nw][q] = ps[k][q]; d.wall_n[d.nw][q] = ns[k][q]; }
-            d.wall_moving[d.nw] = b == HB_T_DYNWALL;
+            d.wall_code[d.nw] = b;
             ++d.nw;
         }
     }
@@ -272,7 +277,7 @@ int hb_destroy(hb_ctx* c) {
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
                     c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
-                    c->io_linked, c->io_part};
+                    c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -329,6 +334,7 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     if (launch_init_lattice(c, e && c->d.E ? c->d.x[0] : nullptr, c->d.E ? c->d.rad : nullptr, c->d.E,
                             c->d.obj_x0, c->d.obj_r, c->d.O))
         return seterr(HB_ERR_CUDA, "lattice init: %s", cudaGetErrorString(cudaGetLastError()));
+    if (slip_init(c)) return seterr(HB_ERR_CUDA, "slip-wall list: %s", cudaGetErrorString(cudaGetLastError()));
     // count dynamic-wall nodes
     {
         std::vector<uint8_t> t(N);

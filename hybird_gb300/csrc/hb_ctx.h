@@ -59,7 +59,7 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     // walls (boundary planes, DEM.cpp:435-633)
     int nw = 0;
     double wall_p[hb::MAX_WALLS][3], wall_n[hb::MAX_WALLS][3];
-    int wall_moving[hb::MAX_WALLS];
+    int wall_code[hb::MAX_WALLS];  // lattice type of the wall's nodes: 5/6 slip, 7/8 no-slip (LB.cpp:497-533)
 };
 
 namespace hb { struct hb_adj; }
@@ -109,6 +109,11 @@ struct hb_ctx {
     double* fs_part = nullptr;      // per-block FP64 partials for the surplus ledger
     int* fs_cnt = nullptr;          // per-block interface counts
     int* fs_first = nullptr;        // 1 until the first free-surface step has run
+    // slip walls (hb_slip.cu)
+    unsigned long long* slip_list = nullptr;  // (node, diagonal slip link) entries
+    double* slip_val = nullptr;
+    uint8_t* slip_mix = nullptr;
+    int slip_n = 0;
     // DEM
     hb_dem_dev d;
     // graph
@@ -140,6 +145,9 @@ void launch_couple_reduce(hb_ctx* c);
 void launch_reactions(hb_ctx* c);
 int set_error(int code, const char* msg);  // hb_last_error text, returns code
 void fs_buffer_bytes(const hb_ctx* c, size_t* part, size_t* cnt);
+// slip walls (hb_slip.cu)
+int slip_init(hb_ctx* c);
+void launch_slip(hb_ctx* c, void* f);
 // output mirror (hb_io.cu)
 int io_prepare(hb_ctx* c);
 void launch_io_pack(hb_ctx* c, int8_t* type, double* v, double* pressure, double* visc, double* mass,

@@ -227,8 +227,8 @@ __global__ void __launch_bounds__(256) k_collide_stream(LBArgs a) {
             const double uw = a.u[l] * cx(j) + a.u[N + l] * cy(j) + a.u[2 * N + l] * cz(j);
             const T BBi = T(6.0 * (double)n * wgt(j) * uw);
             P::store(fout + (long long)o * N + i, fs[j] - BBi);
-        } else if (lc == HB_T_STATWALL) {
-            P::store(fout + (long long)o * N + i, fs[j]);
+        } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN) {
+            P::store(fout + (long long)o * N + i, fs[j]);  // slip walls: mixed afterwards (hb_slip.cu)
         } else {
             flag_status(a.status, 1);  // TYPE ERROR (LB.cpp:1458-1461)
         }
@@ -303,7 +303,7 @@ struct InitArgs {
     int boundary[6];
     int nw;
     double wp[MAX_WALLS][3], wn[MAX_WALLS][3];
-    int wmov[MAX_WALLS];
+    int wcode[MAX_WALLS];
     double gas_x, gas_z;
 };
 
@@ -326,7 +326,7 @@ __global__ void k_init_types(InitArgs a, uint8_t* ntype, uint32_t* solid) {
                          a.wn[w][2] * ((double)z - a.wp[w][2]);
         if (d < 0.0) {
             s = (uint32_t)w;
-            t = a.wmov[w] ? HB_T_DYNWALL : HB_T_STATWALL;
+            t = a.wcode[w];
         }
     }
     ntype[i] = (uint8_t)t;
@@ -504,7 +504,8 @@ __global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, unsigned long lo
                 const long long l = (long long)xn + (long long)a.X * ((long long)yn + (long long)a.Y * zn);
                 const uint8_t tl = ntype[l];
                 const bool act = is_active(tl);
-                if ((tl & HB_TYPE_MASK) == HB_T_STATWALL) bb |= 1u << j;
+                const uint8_t tc = tl & HB_TYPE_MASK;
+                if (tc == HB_T_STATWALL || tc == HB_T_SLIPSTAT || tc == HB_T_SLIPDYN) bb |= 1u << j;
                 else if (!act || wj) mask |= 1u << j;
                 if (!act) bulk = false;
                 if (wj) wrap = true;
@@ -565,7 +566,7 @@ static InitArgs init_args(hb_ctx* c) {
             a.wp[w][k] = w < c->d.nw ? c->d.wall_p[w][k] : 0.0;
             a.wn[w][k] = w < c->d.nw ? c->d.wall_n[w][k] : 0.0;
         }
-        a.wmov[w] = w < c->d.nw ? c->d.wall_moving[w] : 0;
+        a.wcode[w] = w < c->d.nw ? c->d.wall_code[w] : HB_T_STATWALL;
     }
     a.gas_x = c->P.gas_box[0];
     a.gas_z = c->P.gas_box[1];
@@ -683,10 +684,11 @@ void launch_lb_step(hb_ctx* c, int cur) {
     dim3 g = lb_grid(c, block);
     if (c->P.precision == HB_FP64) {
         k_collide_stream<PolF64><<<g, block, 0, c->stream>>>(a);
-        return;
+    } else {
+        if (a.couple) cudaMemsetAsync(c->hacc, 0, sizeof(unsigned long long) * 7 * c->d.E, c->stream);
+        launch_lb_step_dev(c, a);
     }
-    if (a.couple) cudaMemsetAsync(c->hacc, 0, sizeof(unsigned long long) * 7 * c->d.E, c->stream);
-    launch_lb_step_dev(c, a);
+    launch_slip(c, a.fout);  // slip-wall mixing of the bounced-back diagonals (hb_slip.cu)
 }
 
 void launch_lb_wallforce(hb_ctx* c, int cur) {

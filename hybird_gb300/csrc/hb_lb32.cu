@@ -60,7 +60,7 @@ __device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fou
     const int N = (int)a.N;
     if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
         P::store(fout + j * N + l, g);
-    } else if (lc == HB_T_STATWALL) {
+    } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN) {  // slip: mixed afterwards
         P::store(fout + o * N + i, g);
     } else if (lc == HB_T_GAS) {
         const float vu = cdot(j, ux, uy, uz);
@@ -262,7 +262,7 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
 #pragma unroll
         for (int j = 1; j < Q; ++j) fo[a.so[j]] = P::enc_store(f[j]);
     } else if (__all_sync(warp, special == 0u)) {
-        // a static wall returns the population into the node's own opposite slot
+        // a static (or slip) wall returns the population into the node's own opposite slot
 #pragma unroll
         for (int j = 1; j < Q; ++j) fo[(bb & (1u << j)) ? opp(j) * N : a.so[j]] = P::enc_store(f[j]);
     } else {

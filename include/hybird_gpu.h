@@ -48,6 +48,8 @@ extern "C" {
 #define HB_T_GAS       2
 #define HB_T_INTERFACE 3
 #define HB_T_PERIODIC  4
+#define HB_T_SLIPSTAT  5
+#define HB_T_SLIPDYN   6
 #define HB_T_STATWALL  7
 #define HB_T_DYNWALL   8
 
@@ -56,7 +58,7 @@ extern "C" {
  * DEM::discreteElementGet (DEM.cpp:13-183) and parseConfigFile (hybird.cpp:132-223). */
 typedef struct hb_params {
     int32_t lb_size[3];        /* lbSizeX/Y/Z: nodes incl. the two boundary layers          */
-    int32_t boundary[6];       /* boundary0..5 (x-,x+,y-,y+,z-,z+): 4, 7 or 8               */
+    int32_t boundary[6];       /* boundary0..5 (x-,x+,y-,y+,z-,z+): 4, 5, 6, 7 or 8         */
     double  units[3];          /* unitLength, unitTime, unitDensity: must be 1.0            */
     double  init_visc;         /* initVisc (kinematic, lattice units): tau = 0.5 + 3 nu     */
     double  init_velocity[3];  /* initVelocityX/Y/Z                                          */
@@ -90,6 +92,7 @@ typedef struct hb_params {
     /* capacities of the fixed-size device lists (0 = library default) */
     int64_t cap_pairs;         /* DEM candidate pairs                                        */
     int64_t cap_interface;     /* interface cells                                            */
+    double  slip_coefficient;  /* slipCoefficient S of the slip walls 5/6 (LB.cpp:1154-1155) */
 } hb_params;
 
 /* Spheres: one element per particle (elmt size 1, DEM.cpp:81-127 particle file row). */

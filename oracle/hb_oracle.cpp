@@ -32,6 +32,33 @@ const int CX[Q] = {0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1}
 const int CY[Q] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 1, -1, -1, 1, 0, 0, 0, 0};
 const int CZ[Q] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, -1, 1};
 const int OPP[Q] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
+
+int dir_of(int x, int y, int z) {
+    for (int j = 0; j < Q; ++j)
+        if (CX[j] == x && CY[j] == y && CZ[j] == z) return j;
+    return -1;
+}
+// Slip-wall partners of a diagonal direction j (the lattice.h:87-94 tables): along each of
+// j's two non-zero axes, the neighbour one step along that axis and the direction j with
+// that component reversed -- the population that, reflected off a wall normal to the
+// other axis, arrives as opp(j).  Which axis is "1" does not matter: the rule uses the
+// one open side.
+struct SlipPair { int check[2], dir[2]; };
+SlipPair slip_pair(int j) {
+    SlipPair r{{0, 0}, {0, 0}};
+    const int c[3] = {CX[j], CY[j], CZ[j]};
+    int k = 0;
+    for (int a = 0; a < 3 && k < 2; ++a) {
+        if (!c[a]) continue;
+        int u[3] = {0, 0, 0}, f[3] = {c[0], c[1], c[2]};
+        u[a] = c[a];
+        f[a] = -c[a];
+        r.check[k] = dir_of(u[0], u[1], u[2]);
+        r.dir[k] = dir_of(f[0], f[1], f[2]);
+        ++k;
+    }
+    return r;
+}
 const double W[Q] = {12.0 / 36.0, 2.0 / 36.0, 2.0 / 36.0, 2.0 / 36.0, 2.0 / 36.0, 2.0 / 36.0,
                      2.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
                      1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
@@ -84,6 +111,7 @@ inline V3 newtonAcc(V3 m, V3 I, V3 w) {  // vector.cpp:371-376
 struct Wall {  // utils.h:18-82, built by DEM::initializeWalls (DEM.cpp:435-633)
     V3 p, n;
     bool moving;
+    bool slip = false;
     V3 vel, omega, rot;
     V3 fhydro, fparticle;
     double dist(V3 pt) const { return dot(n, sub(pt, p)); }  // utils.cpp:12-15
@@ -262,7 +290,7 @@ bool buildLattice(hbo_sim& s, const hb_elements* e, const hb_objects* o) {
         for (size_t i = 0; i < N; ++i) {
             if (dot(W0.n, sub(s.pos(i), W0.p)) < 0.0) {  // insidePlane, vector.cpp:172-175
                 s.solid[i] = (uint32_t)w;
-                s.type[i] = W0.moving ? 8 : 7;
+                s.type[i] = W0.slip ? (W0.moving ? 6 : 5) : (W0.moving ? 8 : 7);
             }
         }
     }
@@ -354,11 +382,12 @@ void buildWalls(hbo_sim& s) {  // DEM.cpp:435-633
     const V3 ns[6] = {v3(1, 0, 0), v3(-1, 0, 0), v3(0, 1, 0), v3(0, -1, 0), v3(0, 0, 1), v3(0, 0, -1)};
     for (int k = 0; k < 6; ++k) {
         const int b = P.boundary[k];
-        if (b == 7 || b == 8) {
+        if (b >= 5 && b <= 8) {
             Wall w;
             w.p = ps[k];
             w.n = ns[k];
-            w.moving = (b == 8);
+            w.moving = (b == 8 || b == 6);
+            w.slip = (b == 5 || b == 6);
             w.vel = v3(0, 0, 0);
             w.omega = v3(0, 0, 0);
             w.rot = (k == 2) ? v3(0.0, 0.5 + 0.4, 1.260) : v3(0, 0, 0);
@@ -838,6 +867,23 @@ bool streaming(hbo_sim& s) {  // LB.cpp:1144-1488
                 fi[OPP[j]] = fsi[j] - BBi;
             } else if (t == 7) {
                 fi[OPP[j]] = fsi[j];
+            } else if (t == 5 || t == 6) {  // slip walls, LB.cpp:1358-1456
+                // moving slip walls (6) bounce back with BBi of the wall node's velocity
+                const double BBi = t == 6 ? 6.0 * s.n[i] * W[j] * dot(s.u[l], cvec(j)) : 0.0;
+                const double S1 = s.P.slip_coefficient, S2 = 1.0 - s.P.slip_coefficient;
+                int c = -1, d = 0;
+                if (j > 6) {  // diagonal links: specular reflection when one side is open
+                    const SlipPair sp = slip_pair(j);
+                    const uint32_t c1 = s.nb[i * Q + sp.check[0]], c2 = s.nb[i * Q + sp.check[1]];
+                    const bool a1 = s.isActive(c1), a2 = s.isActive(c2);
+                    if (a1 && !a2) { c = (int)c1; d = sp.dir[0]; }
+                    else if (!a1 && a2) { c = (int)c2; d = sp.dir[1]; }
+                }
+                if (c >= 0)
+                    fi[OPP[j]] = t == 6 ? S1 * s.fs[(size_t)c * Q + d] + S2 * (fsi[j] - BBi)
+                                        : S1 * s.fs[(size_t)c * Q + d] + S2 * fsi[j];
+                else
+                    fi[OPP[j]] = t == 6 ? fsi[j] - BBi : fsi[j];
             } else {
                 bad += 1;
             }
@@ -889,6 +935,16 @@ void updateMass(hbo_sim& s) {  // LB.cpp:1492-1590
             else if (t == 0) a = 1.0;
             else if (t == 2) a = 0.0;
             else if (t == 8 || t == 9) a = 1.0 * s.mass[i];
+            else if (t == 6) {  // moving slip wall; a static slip wall (5) has no branch: 0
+                bool mixed = false;
+                if (j > 6) {
+                    const SlipPair sp = slip_pair(j);
+                    const bool a1 = s.isActive(s.nb[(size_t)i * Q + sp.check[0]]);
+                    const bool a2 = s.isActive(s.nb[(size_t)i * Q + sp.check[1]]);
+                    mixed = a1 != a2;
+                }
+                a += mixed ? 1.0 * (1.0 - s.P.slip_coefficient) * s.mass[i] : 1.0 * s.mass[i];
+            }
             dm += 1.0 * a * (s.f[(size_t)i * Q + OPP[j]] - s.fs[(size_t)i * Q + j]);
         }
         s.newMass[i] += dm;

@@ -105,6 +105,32 @@ CASES = {
         spheres=("rsa", 5, 14, 1.6, 2.6, (9.5, 9.5, 6.0), (22.5, 22.5, 28.0)),
         objects=[(13.0, 14.0, 4.0, 3.0), (19.0, 17.0, 3.5, 2.5)],
         steps=[0, 1, 50, 100, 150], full=[], vtk=[50]),
+    # slip walls (LB.cpp:1358-1456): static slip at y-, moving slip at y+, periodic x/z
+    "channel_slip": dict(
+        cfg=dict(lbSizeX=12, lbSizeY=8, lbSizeZ=6, lbFX=2e-5, lbFZ=-4e-6, initVisc=0.08,
+                 slipCoefficient=0.35, initVelocityX=0.01, initVelocityY=0.002,
+                 boundary0=4, boundary1=4, boundary2=5, boundary3=6, boundary4=4, boundary5=4),
+        spheres=[], objects=[], steps=[0, 1, 5, 30], full=[1, 30]),
+    # closed box of slip walls with particles (contacts with slip walls, DEM.cpp:442-471)
+    "box_slip": dict(
+        cfg=dict(lbSizeX=14, lbSizeY=12, lbSizeZ=14, lbFX=3e-5, lbFZ=-2e-4, initVisc=0.1,
+                 slipCoefficient=0.6, multiStep=3,
+                 boundary0=5, boundary1=7, boundary2=5, boundary3=5, boundary4=6, boundary5=5),
+        spheres=("rsa", 13, 4, 2.0, 2.6), objects=[], steps=[0, 1, 10, 40], full=[1, 40]),
+    # free surface against static slip walls (updateMass has no slip-static branch)
+    "dambreak_slip": dict(
+        cfg=dict(lbSizeX=20, lbSizeY=8, lbSizeZ=12, lbFZ=-5e-4, initVisc=0.05, freeSurfaceSolve=1,
+                 slipCoefficient=0.5,
+                 boundary0=5, boundary1=7, boundary2=7, boundary3=5, boundary4=5, boundary5=7),
+        spheres=[], objects=[], gasbox=(0.4, 0.6), steps=[0, 1, 5, 20, 60], full=[1, 20, 60]),
+    # Hertzian contacts (DEM.cpp:2138-2222): spheres falling onto the floor and onto each
+    # other, DEM only; kept > nebrRange from the side walls (first wall in range only)
+    "dem_hertz": dict(
+        cfg=dict(lbSizeX=28, lbSizeY=28, lbSizeZ=40, lbSolve=0, lbFZ=-2e-3, multiStep=20,
+                 contactModel="HERTZIAN", youngMod=5e3, poisson=0.3,
+                 boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
+        spheres=("rsa", 9, 10, 1.5, 2.2, (8.5, 8.5, 1.6), (19.5, 19.5, 30.0)),
+        objects=[], steps=[0, 1, 30, 60, 100], full=[], vtk=[60]),
     # free-surface dam break (LB.cpp:1492-1804), column x < 0.4 Lx, z < 0.6 Lz
     "dambreak_fs": dict(
         cfg=dict(lbSizeX=20, lbSizeY=8, lbSizeZ=12, lbFZ=-5e-4, initVisc=0.05, freeSurfaceSolve=1,

@@ -185,7 +185,7 @@ def golden_params(d, **over):
         density=c["density"], linear_stiff=c["linearStiff"], young_mod=c["youngMod"],
         poisson=c["poisson"], restitution=c["restitution"], visc_tang=c["viscTang"],
         friction_part=c["frictionCoefPart"], friction_wall=c["frictionCoefWall"],
-        num_visc=c["numVisc"],
+        num_visc=c["numVisc"], slip_coefficient=c["slipCoefficient"],
     )
     if "gasbox" in c:
         kw["gas_box"] = tuple(c["gasbox"])
@@ -194,7 +194,7 @@ def golden_params(d, **over):
 
 
 def golden_gasbox(name):
-    return {"dambreak_fs": (0.4, 0.6)}.get(name, (0.0, 0.0))
+    return {"dambreak_fs": (0.4, 0.6), "dambreak_slip": (0.4, 0.6)}.get(name, (0.0, 0.0))
 
 
 def rel_linf(a, b, mask=None):

@@ -44,7 +44,7 @@ def test_params_struct_matches_header_field_order():
 
 
 @pytest.mark.parametrize("field,value,code", [
-    ("boundary", (5, 7, 7, 7, 7, 7), abi.STATUS_NAMES and 2),   # slip walls: unsupported
+    ("boundary", (9, 7, 7, 7, 7, 7), abi.STATUS_NAMES and 2),   # curved walls: unsupported
     ("init_visc", 0.0, 1),
     ("precision", 7, 1),
 ])

@@ -17,7 +17,8 @@ def _gpu():
     return GpuSim
 
 
-@pytest.mark.parametrize("name", ["channel_bgk", "channel_movwall", "channel_bingham_smag", "box_spheres"])
+@pytest.mark.parametrize("name", ["channel_bgk", "channel_movwall", "channel_bingham_smag", "box_spheres",
+                                  "channel_slip", "box_slip"])
 def test_fp64_matches_reference_fixture(name):
     d = load_golden(name)
     p = golden_params(d, gas_box=golden_gasbox(name))
@@ -50,13 +51,15 @@ def test_fp64_matches_reference_fixture(name):
     g.close()
 
 
+@pytest.mark.parametrize("name", ["dambreak_fs", "dambreak_slip"])
 @pytest.mark.parametrize("prec", [abi.HB_FP64, abi.HB_FP32])
-def test_free_surface_matches_reference_fixture(prec):
-    """Dam break (LB.cpp:1492-1804): node types and the interface set must be identical
-    to the reference's at every snapshot; FP64 masses/fields to rounding (the surplus
-    ledger is summed in a different order, so 1e-11), FP32 to its storage precision."""
-    d = load_golden("dambreak_fs")
-    p = golden_params(d, gas_box=golden_gasbox("dambreak_fs"), precision=prec)
+def test_free_surface_matches_reference_fixture(prec, name):
+    """Dam break (LB.cpp:1492-1804), with no-slip and with static slip walls: node types
+    and the interface set must be identical to the reference's at every snapshot; FP64
+    masses/fields to rounding (the surplus ledger is summed in a different order, so
+    1e-11), FP32 to its storage precision."""
+    d = load_golden(name)
+    p = golden_params(d, gas_box=golden_gasbox(name), precision=prec)
     g = _gpu()(p)
     done = 0
     for step in d["steps"]:
@@ -92,8 +95,11 @@ def test_init_matches_reference_fixture():
     g.close()
 
 
-def test_dem_matches_reference_fixture():
-    d = load_golden("dem_objects")
+@pytest.mark.parametrize("name,early_steps", [("dem_objects", 50), ("dem_hertz", 30)])
+def test_dem_matches_reference_fixture(name, early_steps):
+    """LINEAR contacts against objects and walls; HERTZIAN contacts between spheres and
+    with the floor (DEM.cpp:2138-2222)."""
+    d = load_golden(name)
     p = golden_params(d)
     g = _gpu()(p, d["spheres"], d["objects"])
     done = 0
@@ -107,7 +113,7 @@ def test_dem_matches_reference_fixture():
         # contacts (kn = 1e3, friction switching between viscous and Coulomb branches)
         # start, ulp-level differences in the summation order grow, so the later
         # snapshots are held to a looser bound (positions 1e-5 of the box scale)
-        early = step <= 50
+        early = step <= early_steps
         for k, gk, tol in (("x0", "e_x0", 1e-10 if early else 1e-5), ("x1", "e_x1", 1e-8 if early else 1e-2)):
             ref = d[pre + gk].reshape(-1, 3).T.reshape(-1)
             assert rel_linf(ge[k], ref) <= tol, (step, k, rel_linf(ge[k], ref))
@@ -125,6 +131,22 @@ def _channel(shape=(64, 32, 32), precision=abi.HB_FP64, collision=abi.HB_BGK, ta
                            precision=precision, collision=collision, trt_magic=magic)
 
 
+def test_slip_channel_fp64_vs_oracle():
+    """Slip walls at a larger size than the fixture: FP64 GPU against the FP64 oracle
+    (itself pinned to the reference's channel_slip/box_slip/dambreak_slip fixtures)."""
+    p = _slip_channel()
+    g = _gpu()(p)
+    o = OracleSim(p, threads=4)
+    g.cycle(60)
+    o.cycle(60)
+    gl, ol = g.lattice(), o.lattice()
+    act = ol["type"] == 0
+    assert rel_linf(gl["u"].reshape(3, -1), ol["u"].reshape(3, -1), act) <= 1e-12
+    assert rel_linf(gl["f"].reshape(19, -1), ol["f"].reshape(19, -1), act) <= 1e-12
+    g.close()
+    o.close()
+
+
 def test_config1_fp64_vs_oracle_100_steps():
     p = _channel()
     g = _gpu()(p)
@@ -138,18 +160,42 @@ def test_config1_fp64_vs_oracle_100_steps():
         assert e <= FP64_TOL, (k, e)
 
 
-@pytest.mark.parametrize("prec,tol", [(abi.HB_FP32, 1e-5), (abi.HB_FP16S, 5e-2)])
-def test_reduced_precision_error_vs_fp64_oracle(prec, tol):
-    p64 = _channel()
-    p = _channel(precision=prec)
-    g = _gpu()(p)
+def _slip_channel(precision=abi.HB_FP64, walls=(5, 6)):
+    """32x24x16 channel, periodic x/z, static slip wall at y-, moving slip wall at y+
+    (walls=(7, 8): the same flow between no-slip walls)."""
+    return abi.make_params((32, 24, 16), (4, 4, walls[0], walls[1], 4, 4), init_visc=0.08, lbF=(2e-6, 0, -4e-7),
+                           precision=precision, slip_coefficient=0.35, init_velocity=(0.01, 0.002, 0.0))
+
+
+def _u_error_vs_oracle(make, prec):
+    p64 = make()
+    g = _gpu()(make(precision=prec))
     o = OracleSim(p64, threads=4)
     g.cycle(200)
     o.cycle(200)
     gl, ol = g.lattice(), o.lattice()
     act = ol["type"] == 0
+    np.testing.assert_array_equal(gl["type"], ol["type"])
     du = gl["u"].reshape(3, -1)[:, act] - ol["u"].reshape(3, -1)[:, act]
     l2 = np.sqrt((du ** 2).sum() / (ol["u"].reshape(3, -1)[:, act] ** 2).sum())
+    g.close()
+    o.close()
+    return l2, gl, ol, act
+
+
+@pytest.mark.parametrize("prec,tol", [(abi.HB_FP32, 1e-5), (abi.HB_FP16S, 5e-2)])
+@pytest.mark.parametrize("case", ["channel", "slip_channel"])
+def test_reduced_precision_error_vs_fp64_oracle(prec, tol, case):
+    """Relative L2 velocity error of the FP32 / FP16S storage forms against the FP64
+    oracle after 200 steps.  The slip channel is held to the larger of the bound and
+    twice the error of the same flow between no-slip walls: the slip mixing must add no
+    error beyond the storage rounding."""
+    make = _channel if case == "channel" else _slip_channel
+    l2, gl, ol, act = _u_error_vs_oracle(make, prec)
+    if case == "slip_channel":
+        ref, _, _, _ = _u_error_vs_oracle(lambda precision=abi.HB_FP64: _slip_channel(precision, (7, 8)), prec)
+        tol = max(tol, 2.0 * ref)
+        print(f"slip channel prec {prec}: {l2:.3e} (no-slip walls {ref:.3e})")
     assert l2 <= tol, l2
     dn = np.abs(gl["n"][act] - ol["n"][act]).max()
     assert dn <= 1e-6 if prec == abi.HB_FP32 else dn <= 1e-3
