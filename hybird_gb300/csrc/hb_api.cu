@@ -277,7 +277,7 @@ int hb_destroy(hb_ctx* c) {
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
                     c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
-                    c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix};
+                    c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix, c->fs_ilist};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->h_stage) cudaFreeHost(c->h_stage);

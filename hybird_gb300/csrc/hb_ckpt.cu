@@ -71,7 +71,7 @@ std::vector<Buf> state_buffers(hb_ctx* c) {
         add("fs_mass2", c->fs_mass2, 8 * N);
         add("fs_part", c->fs_part, part);
         add("fs_cnt", c->fs_cnt, cnt);
-        add("fs_first", c->fs_first, 4 * sizeof(int));
+        add("fs_first", c->fs_first, 6 * sizeof(int));
     }
     hb_dem_dev& d = c->d;
     const size_t E = (size_t)d.E;

@@ -108,7 +108,8 @@ struct hb_ctx {
     double* fs_mass2 = nullptr;     // new interface masses (updateMass reads the old ones)
     double* fs_part = nullptr;      // per-block FP64 partials for the surplus ledger
     int* fs_cnt = nullptr;          // per-block interface counts
-    int* fs_first = nullptr;        // 1 until the first free-surface step has run
+    int* fs_first = nullptr;        // [6] 1 until the first free-surface step has run; counters
+    uint32_t* fs_ilist = nullptr;   // [N] interface cells at the start of a step
     // slip walls (hb_slip.cu)
     unsigned long long* slip_list = nullptr;  // (node, diagonal slip link) entries
     double* slip_val = nullptr;

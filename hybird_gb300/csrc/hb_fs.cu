@@ -1,5 +1,7 @@
 // hb_fs.cu -- free-surface step (LB::latticeBoltzmannFreeSurfaceStep, LB.cpp:235-245,
-// 1492-1804) as full-grid passes over the node byte.
+// 1492-1804): the mass exchange runs on a compacted list of the interface cells (warp
+// ballots over the node byte, one warp per cell), the conversions as full-grid passes
+// over the node byte.
 //
 // The reference walks ordered lists (interface nodes sorted ascending, walked backwards;
 // filled/emptied lists; appended new interface cells).  Every conversion rule it applies
@@ -33,6 +35,7 @@ namespace hb {
 enum : uint8_t { FS_FILLED = 1, FS_EMPTIED = 2, FS_NEW_A = 4, FS_NEW_B = 8 };
 constexpr int FS_PARTS = 4;  // ledger partials: K3, K4, K5, K6
 constexpr int FS_BLOCK = 128;  // threads per block along x
+constexpr int FS_ZC = 8;       // z planes per block: a thread visits FS_ZC nodes
 
 struct FsArgs {
     int X, Y, Z;
@@ -57,21 +60,29 @@ struct FsArgs {
     int* nconv;             // [3] cells filled / emptied by this step's classify; cells whose
                             // activity changed (gas <-> interface) in this step
     int blocks;
+    uint32_t* ilist;        // [N] interface cells at the start of the step (unordered)
+    int* icount;            // its length
 };
 
-// Every pass runs on a 3D grid (x from the thread, y and z from the block), so a node's
-// coordinates come without divisions; neighbours follow the reference's periodic remap.
+// Every pass runs on a 3D grid (x from the thread, y and a group of ZC z planes from the
+// block; a thread visits its ZC nodes in turn), so a node's coordinates come without
+// divisions.  Light passes take ZC = FS_ZC planes, so block scheduling does not dominate
+// them; the mass exchange (18 links of every interface cell) and the redistribution take
+// one plane per block, so that a surface lying across the x rows spreads over many
+// blocks instead of queueing in one lane.  Neighbours follow the reference's periodic
+// remap.
 struct Node {
     int x, y, z;
     long long i;
     bool ok;
 };
-__device__ __forceinline__ Node node_of(const FsArgs& a) {
+template <int ZC = FS_ZC>
+__device__ __forceinline__ Node node_of(const FsArgs& a, int zz) {
     Node n;
     n.x = blockIdx.x * blockDim.x + threadIdx.x;
     n.y = blockIdx.y;
-    n.z = blockIdx.z;
-    n.ok = n.x < a.X;
+    n.z = blockIdx.z * ZC + zz;
+    n.ok = n.x < a.X && n.z < a.Z;
     n.i = (long long)n.x + (long long)a.X * ((long long)n.y + (long long)a.Y * n.z);
     return n;
 }
@@ -135,48 +146,89 @@ __device__ void block_ledger(const FsArgs& a, int k, double v) {
 }
 
 // K1 updateMass (LB.cpp:1492-1590): newMass = mass + sum_j a_j (f[opp j] - fs[j])
-template <class P>
-__global__ void __launch_bounds__(FS_BLOCK) k_fs_mass(FsArgs a) {
-    const Node nd = node_of(a);
-    if (!nd.ok) return;
-    const long long i = nd.i;
-    if (code_of(a, i) != HB_T_INTERFACE) return;
-    const bool first = *a.first != 0;
-    const double mi = a.mass[i];
-    double dm = 0.0;
-    for (int j = 1; j < Q; ++j) {
-        const long long l = fs_link(a, nd, j);
-        const uint8_t t = code_of(a, l);
-        double av = 0.0;
-        if (t == HB_T_INTERFACE) av = 0.5 * (a.mass[l] + mi);
-        else if (t == HB_T_FLUID) av = 1.0;
-        else if (t == HB_T_DYNWALL) av = 1.0 * mi;
-        else continue;  // gas, static wall: averageMass 0
-        if (t == HB_T_DYNWALL) {  // f[opp j] = fs[j] - BBi: the difference is -BBi
-            const double fin = fval<P>(a, opp(j), i);
-            const double uw = a.u[l] * cx(j) + a.u[a.N + l] * cy(j) + a.u[2 * a.N + l] * cz(j);
-            const double fs = first ? fval<P>(a, j, i) : fin + 6.0 * a.rho[i] * wgt(j) * uw;
-            dm += 1.0 * av * (fin - fs);
-            continue;
-        }
-        const long long src = first ? i : l;  // fs[j]: f = fs = f_eq at initialisation, else
-                                               // pushed to the active neighbour
-        if (P::DEV) {  // deviations: their FP32 difference is the difference of the populations
-            using S = typename P::S;
-            const S* fp = reinterpret_cast<const S*>(a.f);
-            const float d = P::load(fp + (long long)opp(j) * a.N + i) - P::load(fp + (long long)j * a.N + src);
-            dm += 1.0 * av * (double)d;
-        } else {
-            dm += 1.0 * av * (fval<P>(a, opp(j), i) - fval<P>(a, j, src));
-        }
+// Interface cells at the start of the step, compacted with warp ballots (order within
+// the list is irrelevant: each cell's mass exchange is independent of the others).
+__global__ void __launch_bounds__(FS_BLOCK) k_fs_ilist(FsArgs a) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    for (int zz = 0; zz < FS_ZC; ++zz) {
+        const Node nd = node_of(a, zz);
+        const bool is_if = nd.ok && code_of(a, nd.i) == HB_T_INTERFACE;
+        const unsigned b = __ballot_sync(full, is_if);
+        if (!b) continue;
+        int base = 0;
+        if (lane == 0) base = atomicAdd(a.icount, __popc(b));
+        base = __shfl_sync(full, base, 0);
+        if (is_if) a.ilist[base + __popc(b & ((1u << lane) - 1u))] = (uint32_t)nd.i;
     }
-    a.mass2[i] = mi + dm;
+}
+
+// K1 on the list: one warp per interface cell, lane j handles link j (all loads of the
+// cell in flight together), lane 0 adds the terms in link order as the reference does.
+template <class P>
+__global__ void __launch_bounds__(256) k_fs_mass_list(FsArgs a) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int n = *a.icount;
+    const bool first = *a.first != 0;
+    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += warps) {
+        const uint32_t iu = a.ilist[w];  // node indices fit 32 bits (the list is uint32)
+        const uint32_t X = (uint32_t)a.X, XY = (uint32_t)a.X * (uint32_t)a.Y;
+        Node nd;
+        nd.x = (int)(iu % X);
+        nd.y = (int)((iu % XY) / X);
+        nd.z = (int)(iu / XY);
+        nd.i = (long long)iu;
+        const long long i = nd.i;
+        nd.ok = true;
+        const double mi = a.mass[i];
+        double term = 0.0;
+        bool add = false;
+        const int j = lane;
+        if (j >= 1 && j < Q) {
+            const long long l = fs_link(a, nd, j);
+            const uint8_t t = code_of(a, l);
+            double av = 0.0;
+            if (t == HB_T_INTERFACE) av = 0.5 * (a.mass[l] + mi);
+            else if (t == HB_T_FLUID) av = 1.0;
+            else if (t == HB_T_DYNWALL) av = 1.0 * mi;  // gas, static walls: averageMass 0
+            if (av != 0.0) {
+                double diff;
+                if (t == HB_T_DYNWALL) {  // f[opp j] = fs[j] - BBi: the difference is -BBi
+                    const double fin = fval<P>(a, opp(j), i);
+                    const double uw = a.u[l] * cx(j) + a.u[a.N + l] * cy(j) + a.u[2 * a.N + l] * cz(j);
+                    const double fs = first ? fval<P>(a, j, i) : fin + 6.0 * a.rho[i] * wgt(j) * uw;
+                    diff = fin - fs;
+                } else {
+                    const long long src = first ? i : l;  // fs[j]: f = fs = f_eq at initialisation,
+                                                           // else pushed to the active neighbour
+                    if (P::DEV) {  // deviations: their FP32 difference is that of the populations
+                        using S = typename P::S;
+                        const S* fp = reinterpret_cast<const S*>(a.f);
+                        const float d = P::load(fp + (long long)opp(j) * a.N + i) - P::load(fp + (long long)j * a.N + src);
+                        diff = (double)d;
+                    } else {
+                        diff = fval<P>(a, opp(j), i) - fval<P>(a, j, src);
+                    }
+                }
+                term = 1.0 * av * diff;
+                add = true;
+            }
+        }
+        const unsigned adds = __ballot_sync(full, add);
+        double dm = 0.0;
+#pragma unroll
+        for (int k = 1; k < Q; ++k) {  // sequential in link order, as updateMass sums
+            const double tk = __shfl_sync(full, term, k);
+            if (adds & (1u << k)) dm += tk;
+        }
+        if (lane == 0) a.mass2[i] = mi + dm;
+    }
 }
 
 // K2 findInterfaceMutants (LB.cpp:1620-1650)
-__global__ void __launch_bounds__(FS_BLOCK) k_fs_classify(FsArgs a) {
-    const Node nd = node_of(a);
-    if (!nd.ok) return;
+__device__ __forceinline__ void fs_classify_node(const FsArgs& a, const Node& nd) {
     const long long i = nd.i;
     const uint8_t t = a.ntype[i];
     uint8_t fl = 0;
@@ -197,15 +249,23 @@ __global__ void __launch_bounds__(FS_BLOCK) k_fs_classify(FsArgs a) {
     }
     a.flag[i] = fl;
 }
+__global__ void __launch_bounds__(FS_BLOCK) k_fs_classify(FsArgs a) {
+    for (int zz = 0; zz < FS_ZC; ++zz) {
+        const Node nd = node_of(a, zz);
+        if (nd.ok) fs_classify_node(a, nd);
+    }
+}
 
 // K3 smoothenInterface, gas neighbours of filled cells (LB.cpp:1657-1677)
 template <class P>
 __global__ void __launch_bounds__(FS_BLOCK) k_fs_new_from_filled(FsArgs a) {
-    const Node nd = node_of(a);
-    const long long i = nd.i;
     double contrib = 0.0;
     // nothing filled in this step (the usual case): no cell changes, the partial is 0
-    if (a.nconv[0] != 0 && nd.ok && code_of(a, i) == HB_T_GAS && interior3(a, nd.x, nd.y, nd.z)) {
+    if (a.nconv[0] != 0)
+    for (int zz = 0; zz < FS_ZC; ++zz) {
+    const Node nd = node_of(a, zz);
+    const long long i = nd.i;
+    if (nd.ok && code_of(a, i) == HB_T_GAS && interior3(a, nd.x, nd.y, nd.z)) {
         long long parent = -1;
         for (int k = 1; k < Q; ++k) {  // filled cell m with link d[m][opp k] == i
             long long m;
@@ -238,18 +298,21 @@ __global__ void __launch_bounds__(FS_BLOCK) k_fs_new_from_filled(FsArgs a) {
             a.ntype[i] = (a.ntype[i] & ~HB_TYPE_MASK) | HB_T_INTERFACE;
             a.flag[i] |= FS_NEW_A;
             atomicAdd(a.nconv + 2, 1);
-            contrib = -0.01 * 1.0;
+            contrib += -0.01 * 1.0;
         }
+    }
     }
     block_ledger(a, 0, contrib);
 }
 
 // K4 smoothenInterface, fluid neighbours of emptied cells (LB.cpp:1679-1700)
 __global__ void __launch_bounds__(FS_BLOCK) k_fs_new_from_emptied(FsArgs a) {
-    const Node nd = node_of(a);
-    const long long i = nd.i;
     double contrib = 0.0;
-    if (a.nconv[1] != 0 && nd.ok && code_of(a, i) == HB_T_FLUID && interior3(a, nd.x, nd.y, nd.z)) {
+    if (a.nconv[1] != 0)
+    for (int zz = 0; zz < FS_ZC; ++zz) {
+    const Node nd = node_of(a, zz);
+    const long long i = nd.i;
+    if (nd.ok && code_of(a, i) == HB_T_FLUID && interior3(a, nd.x, nd.y, nd.z)) {
         bool hit = false;
         for (int k = 1; k < Q && !hit; ++k) {
             long long m;
@@ -258,19 +321,21 @@ __global__ void __launch_bounds__(FS_BLOCK) k_fs_new_from_emptied(FsArgs a) {
         if (hit) {
             const double n = a.rho[i];
             a.mass[i] = 0.99 * n;
-            contrib = 0.01 * n;
+            contrib += 0.01 * n;
             a.ntype[i] = (a.ntype[i] & ~HB_TYPE_MASK) | HB_T_INTERFACE;
             a.flag[i] |= FS_NEW_B;
         }
+    }
     }
     block_ledger(a, 1, contrib);
 }
 
 // K5 updateMutants (LB.cpp:1703-1742) and removeIsolated, first pass (LB.cpp:1749-1769)
 __global__ void __launch_bounds__(FS_BLOCK) k_fs_mutants_to_fluid(FsArgs a) {
-    const Node nd = node_of(a);
-    const long long i = nd.i;
     double contrib = 0.0;
+    for (int zz = 0; zz < FS_ZC; ++zz) {
+    const Node nd = node_of(a, zz);
+    const long long i = nd.i;
     if (nd.ok) {
         const uint8_t fl = a.flag[i];
         const uint8_t t = code_of(a, i);
@@ -291,26 +356,29 @@ __global__ void __launch_bounds__(FS_BLOCK) k_fs_mutants_to_fluid(FsArgs a) {
             }
         }
     }
+    }
     block_ledger(a, 2, contrib);
 }
 
 // K6 removeIsolated, second pass (LB.cpp:1771-1793)
 __global__ void __launch_bounds__(FS_BLOCK) k_fs_isolated_gas(FsArgs a) {
-    const Node nd = node_of(a);
-    const long long i = nd.i;
     double contrib = 0.0;
     int count = 0;
+    for (int zz = 0; zz < FS_ZC; ++zz) {
+    const Node nd = node_of(a, zz);
+    const long long i = nd.i;
     if (nd.ok && code_of(a, i) == HB_T_INTERFACE) {
         bool fluid = false;
         for (int j = 1; j < Q && !fluid; ++j)
             if (code_of(a, fs_link(a, nd, j)) == HB_T_FLUID) fluid = true;
         if (!fluid) {
-            contrib = a.mass[i];
+            contrib += a.mass[i];
             a.ntype[i] = (a.ntype[i] & ~HB_TYPE_MASK) | HB_T_GAS;
             atomicAdd(a.nconv + 2, 1);
         } else {
-            count = 1;
+            count += 1;
         }
+    }
     }
     block_ledger(a, 3, contrib);
     __shared__ int shc[FS_BLOCK];
@@ -382,10 +450,8 @@ __global__ void k_fs_ledger(FsArgs a, const double* csum, const long long* ccnt)
 
 // K7 redistributeMass (LB.cpp:1796-1804)
 __global__ void __launch_bounds__(FS_BLOCK) k_fs_redistribute(FsArgs a) {
-    const Node nd = node_of(a);
-    const long long i = nd.i;
-    if (!nd.ok || code_of(a, i) != HB_T_INTERFACE) return;
-    a.mass[i] += a.scal[0] / a.scal[1];
+    const Node nd = node_of<1>(a, 0);
+    if (nd.ok && code_of(a, nd.i) == HB_T_INTERFACE) a.mass[nd.i] += a.scal[0] / a.scal[1];
 }
 
 // ---- host side ---------------------------------------------------------------------------
@@ -410,40 +476,48 @@ static FsArgs fs_args(hb_ctx* c, int cur) {
     a.force = c->fs_force;
     a.first = c->fs_first;
     a.nconv = c->fs_first + 1;
-    a.blocks = ceil_div(c->X, FS_BLOCK) * c->Y * c->Z;
+    a.blocks = ceil_div(c->X, FS_BLOCK) * c->Y * ceil_div(c->Z, FS_ZC);
+    a.ilist = c->fs_ilist;
+    a.icount = c->fs_first + 4;
     return a;
 }
 
 void fs_buffer_bytes(const hb_ctx* c, size_t* part, size_t* cnt) {
-    const size_t blocks = (size_t)ceil_div(c->X, FS_BLOCK) * c->Y * c->Z;
+    const size_t blocks = (size_t)ceil_div(c->X, FS_BLOCK) * c->Y * ceil_div(c->Z, FS_ZC);
     *part = sizeof(double) * (FS_PARTS * blocks + 2 * FS_LEDGER_CHUNKS);
     *cnt = sizeof(int) * blocks;
 }
 
 int fs_init(hb_ctx* c) {
     const long long N = c->N;
-    const int blocks = ceil_div(c->X, FS_BLOCK) * c->Y * c->Z;
+    const int blocks = ceil_div(c->X, FS_BLOCK) * c->Y * ceil_div(c->Z, FS_ZC);
     if (cudaMalloc(&c->fs_flag, N) != cudaSuccess || cudaMalloc(&c->fs_mass2, sizeof(double) * N) != cudaSuccess ||
         cudaMalloc(&c->fs_part, sizeof(double) * (FS_PARTS * blocks + 2 * FS_LEDGER_CHUNKS)) != cudaSuccess ||
         cudaMalloc(&c->fs_cnt, sizeof(int) * blocks) != cudaSuccess ||
         cudaMalloc(&c->fs_scal, sizeof(double) * 2) != cudaSuccess ||
-        cudaMalloc(&c->fs_first, 4 * sizeof(int)) != cudaSuccess)
+        cudaMalloc(&c->fs_first, 6 * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&c->fs_ilist, sizeof(uint32_t) * N) != cudaSuccess)
         return HB_ERR_NOMEM;
     cudaMemset(c->fs_flag, 0, N);
     cudaMemset(c->fs_scal, 0, sizeof(double) * 2);
-    const int init[4] = {1, 0, 0, 0};  // first step; filled / emptied / activity-change counts
+    const int init[6] = {1, 0, 0, 0, 0, 0};  // first step; filled / emptied / activity-change
+                                              // counts; interface-list length
     cudaMemcpy(c->fs_first, init, sizeof(init), cudaMemcpyHostToDevice);
     return cudaGetLastError() == cudaSuccess ? HB_OK : HB_ERR_CUDA;
 }
 
 void launch_fs_step(hb_ctx* c, int cur) {
     FsArgs a = fs_args(c, cur);
-    const dim3 G((unsigned)ceil_div(c->X, FS_BLOCK), (unsigned)c->Y, (unsigned)c->Z);
+    const dim3 G((unsigned)ceil_div(c->X, FS_BLOCK), (unsigned)c->Y, (unsigned)ceil_div(c->Z, FS_ZC));
+    const dim3 G1((unsigned)ceil_div(c->X, FS_BLOCK), (unsigned)c->Y, (unsigned)c->Z);  // one plane per block
     const int B = FS_BLOCK;
     cudaStream_t s = c->stream;
-    if (c->P.precision == HB_FP64) k_fs_mass<PolF64><<<G, B, 0, s>>>(a);
-    else if (c->P.precision == HB_FP32) k_fs_mass<PolF32><<<G, B, 0, s>>>(a);
-    else k_fs_mass<PolF16><<<G, B, 0, s>>>(a);
+    cudaMemsetAsync(a.icount, 0, sizeof(int), s);
+    k_fs_ilist<<<G, B, 0, s>>>(a);
+    const int GL = 152 * 8;  // persistent: 8 blocks of 8 warps per SM over the list
+    if (c->P.precision == HB_FP64) k_fs_mass_list<PolF64><<<GL, 256, 0, s>>>(a);
+    else if (c->P.precision == HB_FP32) k_fs_mass_list<PolF32><<<GL, 256, 0, s>>>(a);
+    else k_fs_mass_list<PolF16><<<GL, 256, 0, s>>>(a);
     k_fs_classify<<<G, B, 0, s>>>(a);
     if (c->P.precision == HB_FP64) k_fs_new_from_filled<PolF64><<<G, B, 0, s>>>(a);
     else if (c->P.precision == HB_FP32) k_fs_new_from_filled<PolF32><<<G, B, 0, s>>>(a);
@@ -455,7 +529,7 @@ void launch_fs_step(hb_ctx* c, int cur) {
     long long* ccnt = reinterpret_cast<long long*>(csum + FS_LEDGER_CHUNKS);
     k_fs_ledger_part<<<FS_LEDGER_CHUNKS, 256, 0, s>>>(a, csum, ccnt);
     k_fs_ledger<<<1, FS_LEDGER_CHUNKS, 0, s>>>(a, csum, ccnt);
-    k_fs_redistribute<<<G, B, 0, s>>>(a);
+    k_fs_redistribute<<<G1, B, 0, s>>>(a);
     launch_refresh_bulk(c, c->fs_first + 3);  // only when a cell's activity changed
 }
 

@@ -480,10 +480,10 @@ __global__ void k_init_vars(InitArgs a, LBArgs b, const int* mx, double Fx, doub
 // 3D grid (x from the thread, y and z from the block).  With `changed` set, the pass
 // runs only when that counter is non-zero (the free surface changed some cell between
 // gas and interface) and resets it.
-__global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, unsigned long long* lmask, int* changed) {
-    if (changed && *changed == 0) return;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-    if (x >= a.X) return;
+constexpr int BULK_ZC = 8;  // z planes per block of the refresh pass
+
+__device__ __forceinline__ void bulk_node(const InitArgs& a, const PerFaces& pf, uint8_t* ntype,
+                                          unsigned long long* lmask, int x, int y, int z) {
     const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
     uint8_t t = ntype[i];
     bool bulk = is_active(t);
@@ -516,6 +516,16 @@ __global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, unsigned long lo
     nt = wrap ? (nt | HB_PWRAP) : (nt & ~HB_PWRAP);
     if (nt != t) ntype[i] = nt;
     if (lmask) lmask[i] = (unsigned long long)mask | ((unsigned long long)bb << 32);
+}
+
+__global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, unsigned long long* lmask, int* changed) {
+    if (changed && *changed == 0) return;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= a.X) return;
+    for (int zz = 0; zz < BULK_ZC; ++zz) {
+        const int z = blockIdx.z * BULK_ZC + zz;
+        if (z < a.Z) bulk_node(a, pf, ntype, lmask, x, y, z);
+    }
 }
 
 // resets the activity-change counter after the (conditional) refresh has run
@@ -663,8 +673,8 @@ int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int 
         k_init_vars<PolF32><<<G, B, 0, c->stream>>>(a, b, mx, F[0], F[1], F[2], iv[0], iv[1], iv[2], c->P.init_visc);
     else
         k_init_vars<PolF16><<<G, B, 0, c->stream>>>(a, b, mx, F[0], F[1], F[2], iv[0], iv[1], iv[2], c->P.init_visc);
-    k_bulk<<<dim3((unsigned)ceil_div(c->X, 128), (unsigned)c->Y, (unsigned)c->Z), 128, 0, c->stream>>>(
-        a, pf, c->ntype, c->lmask, nullptr);
+    k_bulk<<<dim3((unsigned)ceil_div(c->X, 128), (unsigned)c->Y, (unsigned)ceil_div(c->Z, BULK_ZC)), 128, 0,
+             c->stream>>>(a, pf, c->ntype, c->lmask, nullptr);
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (owner) cudaFree(owner);
     cudaFree(mx);
@@ -673,8 +683,8 @@ int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int 
 
 void launch_refresh_bulk(hb_ctx* c, int* changed) {
     InitArgs a = init_args(c);
-    k_bulk<<<dim3((unsigned)ceil_div(c->X, 128), (unsigned)c->Y, (unsigned)c->Z), 128, 0, c->stream>>>(
-        a, per_faces(c), c->ntype, c->lmask, changed);
+    k_bulk<<<dim3((unsigned)ceil_div(c->X, 128), (unsigned)c->Y, (unsigned)ceil_div(c->Z, BULK_ZC)), 128, 0,
+             c->stream>>>(a, per_faces(c), c->ntype, c->lmask, changed);
     if (changed) k_bulk_done<<<1, 1, 0, c->stream>>>(changed);
 }
 
