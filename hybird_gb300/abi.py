@@ -150,6 +150,31 @@ def make_params(lb_size, boundary, init_visc=0.1, lbF=(0.0, 0.0, 0.0), force_fie
     return p
 
 
+class HbCylinders(C.Structure):
+    _fields_ = [("count", C.c_int32), ("p1", C.POINTER(C.c_double)), ("p2", C.POINTER(C.c_double)),
+                ("radius", C.POINTER(C.c_double)), ("omega", C.POINTER(C.c_double)),
+                ("moving", C.POINTER(C.c_int32))]
+
+
+class CylinderArrays:
+    """Keeps the buffers behind an HbCylinders struct alive.  Rows: p1 (3), p2 (3), R,
+    optionally omega (3) and moving."""
+
+    def __init__(self, rows):
+        r = [list(map(float, row)) for row in rows]
+        n = len(r)
+        self.p1 = np.array([x[0:3] for x in r]).reshape(-1)
+        self.p2 = np.array([x[3:6] for x in r]).reshape(-1)
+        self.R = np.array([x[6] for x in r])
+        self.om = np.array([x[7:10] if len(x) >= 10 else [0.0, 0.0, 0.0] for x in r]).reshape(-1)
+        self.mv = np.array([int(x[10]) if len(x) >= 11 else 0 for x in r], dtype=np.int32)
+        self.cy = HbCylinders(n, dptr(self.p1), dptr(self.p2), dptr(self.R), dptr(self.om),
+                              self.mv.ctypes.data_as(C.POINTER(C.c_int32)))
+
+    def ptr(self):
+        return C.byref(self.cy)
+
+
 class ElementArrays:
     """Keeps the numpy buffers alive behind an HbElements / HbObjects struct."""
 

@@ -277,7 +277,8 @@ int hb_destroy(hb_ctx* c) {
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
                     c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
-                    c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix, c->fs_ilist};
+                    c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix, c->fs_ilist,
+                    c->curved_list, c->curved_cnt};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -288,8 +289,33 @@ int hb_destroy(hb_ctx* c) {
     return HB_OK;
 }
 
+int hb_set_cylinders(hb_ctx* c, const hb_cylinders* cy) {
+    if (!c || !cy) return seterr(HB_ERR_ARG, "null argument");
+    if (c->initialized) return seterr(HB_ERR_STATE, "cylinders must be set before hb_init");
+    if (cy->count < 0 || cy->count > 8 || (cy->count && (!cy->p1 || !cy->p2 || !cy->radius)))
+        return seterr(HB_ERR_ARG, "cylinders: 0..8 with p1, p2, radius");
+    c->cyl.clear();
+    for (int k = 0; k < cy->count; ++k) {
+        hb_cyl_host h = {};
+        for (int q = 0; q < 3; ++q) {
+            h.p1[q] = cy->p1[3 * k + q];
+            h.p2[q] = cy->p2[3 * k + q];
+            h.omega[q] = cy->omega ? cy->omega[3 * k + q] : 0.0;
+        }
+        h.R = cy->radius[k];
+        h.moving = cy->moving ? cy->moving[k] : 0;
+        if (h.p1[0] == h.p2[0] && h.p1[1] == h.p2[1] && h.p1[2] == h.p2[2]) return seterr(HB_ERR_ARG, "cylinder axis of zero length");
+        c->cyl.push_back(h);
+    }
+    return HB_OK;
+}
+
 int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     if (!c) return seterr(HB_ERR_ARG, "null ctx");
+    if (!c->cyl.empty() && c->P.free_surface)
+        return seterr(HB_ERR_UNSUPPORTED, "cylinders (curved walls) with a free surface are not implemented");
+    if (!c->cyl.empty() && c->P.dem_solve && e && e->count > 0)
+        return seterr(HB_ERR_UNSUPPORTED, "cylinders with moving particles (cylinder contacts) are not implemented");
     int rc = dem_init(c, e, o);
     if (rc) return rc;
     const long long N = c->N;
@@ -335,6 +361,7 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
                             c->d.obj_x0, c->d.obj_r, c->d.O))
         return seterr(HB_ERR_CUDA, "lattice init: %s", cudaGetErrorString(cudaGetLastError()));
     if (slip_init(c)) return seterr(HB_ERR_CUDA, "slip-wall list: %s", cudaGetErrorString(cudaGetLastError()));
+    if (curved_init(c)) return seterr(HB_ERR_CUDA, "curved-wall list: %s", cudaGetErrorString(cudaGetLastError()));
     // count dynamic-wall nodes
     {
         std::vector<uint8_t> t(N);

@@ -20,6 +20,7 @@
 #define HB_TYPE_MASK 0x0F
 #define HB_INSIDE 0x10
 #define HB_BULK 0x20
+#define HB_MIRROR 0x80  // the lattice kernels write this node's FP64 velocity (curved walls read it)
 #define HB_PWRAP 0x40   // some link of this node crosses a periodic face
 
 namespace hb {

@@ -12,6 +12,11 @@
 // wG, wL, wpG, wpL, FH, MH, FP, FW, MP, MW (3 each), fvol, m, I (3), rad
 constexpr int DEM_FIELDS = 6 * 3 * 4 + 6 * 4 * 2 + 4 * 3 + 6 * 3 + 1 + 1 + 3 + 1;
 
+struct hb_cyl_host {            // one cylinder as given to hb_set_cylinders
+    double p1[3], p2[3], R, omega[3];
+    int moving;
+};
+
 struct hb_dem_dev {             // element state, FP64, component-major [3E] / [4E]
     int E = 0;
     double* base = nullptr;     // one allocation holding every field below
@@ -110,6 +115,11 @@ struct hb_ctx {
     int* fs_cnt = nullptr;          // per-block interface counts
     int* fs_first = nullptr;        // [6] 1 until the first free-surface step has run; counters
     uint32_t* fs_ilist = nullptr;   // [N] interface cells at the start of a step
+    // cylinders and curved walls (hb_curved.cu)
+    std::vector<hb_cyl_host> cyl;
+    void* curved_list = nullptr;
+    int* curved_cnt = nullptr;
+    int curved_n = 0;
     // slip walls (hb_slip.cu)
     unsigned long long* slip_list = nullptr;  // (node, diagonal slip link) entries
     double* slip_val = nullptr;
@@ -146,6 +156,11 @@ void launch_couple_reduce(hb_ctx* c);
 void launch_reactions(hb_ctx* c);
 int set_error(int code, const char* msg);  // hb_last_error text, returns code
 void fs_buffer_bytes(const hb_ctx* c, size_t* part, size_t* cnt);
+// curved walls (hb_curved.cu)
+void launch_init_cylinders(hb_ctx* c);
+int curved_init(hb_ctx* c);
+void curved_remark(hb_ctx* c);
+void launch_curved(hb_ctx* c, void* f);
 // slip walls (hb_slip.cu)
 int slip_init(hb_ctx* c);
 void launch_slip(hb_ctx* c, void* f);

@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(256) k_collide_stream(LBArgs a) {
     // ---- node macros needed by later phases (free surface, downloads, wall force)
     const bool all = (mode & 1) != 0;
     if (all || a.free_surface || !(t & HB_BULK)) a.rho[i] = (double)n;
-    if (all || code == HB_T_INTERFACE) {
+    if (all || code == HB_T_INTERFACE || (t & HB_MIRROR)) {
         a.u[i] = (double)ux; a.u[N + i] = (double)uy; a.u[2 * N + i] = (double)uz;
         a.hf[i] = (double)hx; a.hf[N + i] = (double)hy; a.hf[2 * N + i] = (double)hz;
     }
@@ -227,8 +227,8 @@ __global__ void __launch_bounds__(256) k_collide_stream(LBArgs a) {
             const double uw = a.u[l] * cx(j) + a.u[N + l] * cy(j) + a.u[2 * N + l] * cz(j);
             const T BBi = T(6.0 * (double)n * wgt(j) * uw);
             P::store(fout + (long long)o * N + i, fs[j] - BBi);
-        } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN) {
-            P::store(fout + (long long)o * N + i, fs[j]);  // slip walls: mixed afterwards (hb_slip.cu)
+        } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN || lc == HB_T_CURVED) {
+            P::store(fout + (long long)o * N + i, fs[j]);  // slip / curved walls: completed afterwards
         } else {
             flag_status(a.status, 1);  // TYPE ERROR (LB.cpp:1458-1461)
         }
@@ -505,7 +505,7 @@ __device__ __forceinline__ void bulk_node(const InitArgs& a, const PerFaces& pf,
                 const uint8_t tl = ntype[l];
                 const bool act = is_active(tl);
                 const uint8_t tc = tl & HB_TYPE_MASK;
-                if (tc == HB_T_STATWALL || tc == HB_T_SLIPSTAT || tc == HB_T_SLIPDYN) bb |= 1u << j;
+                if (tc == HB_T_STATWALL || tc == HB_T_SLIPSTAT || tc == HB_T_SLIPDYN || tc == HB_T_CURVED) bb |= 1u << j;
                 else if (!act || wj) mask |= 1u << j;
                 if (!act) bulk = false;
                 if (wj) wrap = true;
@@ -656,6 +656,7 @@ int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int 
         cudaMemsetAsync(owner, 0xFF, sizeof(int) * c->N, c->stream);
         k_init_particles<<<E, 256, 0, c->stream>>>(a, el_x0, el_r, E, c->ntype, owner);
     }
+    launch_init_cylinders(c);  // after particles and walls, before objects (LB.cpp:324-337)
     k_init_objects<<<G, B, 0, c->stream>>>(a, ob_x0, ob_r, O, owner, c->ntype, c->solid);
     PerFaces pf = per_faces(c);
     k_init_interface<<<G, B, 0, c->stream>>>(a, pf, c->ntype);
@@ -698,7 +699,8 @@ void launch_lb_step(hb_ctx* c, int cur) {
         if (a.couple) cudaMemsetAsync(c->hacc, 0, sizeof(unsigned long long) * 7 * c->d.E, c->stream);
         launch_lb_step_dev(c, a);
     }
-    launch_slip(c, a.fout);  // slip-wall mixing of the bounced-back diagonals (hb_slip.cu)
+    launch_slip(c, a.fout);    // slip-wall mixing of the bounced-back diagonals (hb_slip.cu)
+    launch_curved(c, a.fout);  // curved-wall interpolation of the bounced-back links (hb_curved.cu)
 }
 
 void launch_lb_wallforce(hb_ctx* c, int cur) {

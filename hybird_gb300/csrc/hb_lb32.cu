@@ -60,7 +60,8 @@ __device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fou
     const int N = (int)a.N;
     if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
         P::store(fout + j * N + l, g);
-    } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN) {  // slip: mixed afterwards
+    } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN || lc == HB_T_CURVED) {
+        // slip and curved walls: completed after the kernel (hb_slip.cu, hb_curved.cu)
         P::store(fout + o * N + i, g);
     } else if (lc == HB_T_GAS) {
         const float vu = cdot(j, ux, uy, uz);
@@ -222,7 +223,7 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
 
     const bool all = (mode & 1) != 0;
     if (all || a.free_surface || !(t & HB_BULK)) write_rho(a.rho, i, n);
-    if (all || code == HB_T_INTERFACE) write_u_hf(a.u, a.hf, a.N, i, ux, uy, uz, hx, hy, hz);
+    if (all || code == HB_T_INTERFACE || (t & HB_MIRROR)) write_u_hf(a.u, a.hf, a.N, i, ux, uy, uz, hx, hy, hz);
 
     // Pairwise collision with per-node coefficients for the two link weights (w = 1/18 on
     // the axes, 1/36 on the diagonals), S = g_j + g_o, D = g_j - g_o, base = dn - 1.5 n u^2:

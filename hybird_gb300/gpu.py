@@ -45,6 +45,7 @@ def lib():
     L.hb_vtk_fluid_fields.argtypes = [vp] + [vp] * 6
     L.hb_write_vtk_fluid.argtypes = [vp, C.c_char_p]
     L.hb_get_params.argtypes = [vp, P(abi.HbParams), P(C.c_int32), P(C.c_int32)]
+    L.hb_set_cylinders.argtypes = [vp, P(abi.HbCylinders)]
     L.hb_checkpoint_save.argtypes = [vp, C.c_char_p]
     L.hb_checkpoint_load.argtypes = [C.c_char_p, P(vp)]
     L.hb_write_recycle_particles.argtypes = [vp, C.c_char_p]
@@ -70,13 +71,16 @@ def check(rc):
 class GpuSim:
     """One simulation context on the current CUDA device."""
 
-    def __init__(self, params, spheres=None, objects=None):
+    def __init__(self, params, spheres=None, objects=None, cylinders=None):
         self.L = lib()
         self.params = params
         self.arrays = abi.ElementArrays(spheres, objects)
         h = C.c_void_p()
         check(self.L.hb_create(C.byref(params), C.byref(h)))
         self.h = h
+        if cylinders is not None and len(cylinders):
+            self.cyl = abi.CylinderArrays(cylinders)
+            check(self.L.hb_set_cylinders(self.h, self.cyl.ptr()))
         check(self.L.hb_init(self.h, self.arrays.el_ptr(), self.arrays.ob_ptr()))
         X, Y, Z = params.lb_size
         self.N = X * Y * Z

@@ -52,6 +52,7 @@ extern "C" {
 #define HB_T_SLIPDYN   6
 #define HB_T_STATWALL  7
 #define HB_T_DYNWALL   8
+#define HB_T_CURVED    9
 
 /* ---- parameters -------------------------------------------------------------------- */
 /* Mirrors the cfg keys parsed by LB::latticeBoltzmannGet (LB.cpp:85-188),
@@ -145,9 +146,25 @@ typedef struct hb_export {
     double  energy_kin, energy_rot_kin, energy_tr_kin, energy_grav, energy_total;
 } hb_export;
 
+/* Cylinders (the reference's cylinder class, utils.h:85-110; problem code creates them,
+ * DEM.cpp:871-935): every lattice node outside a cylinder becomes a curved wall (9) with
+ * Mei-Luo-Shyy interpolated bounce-back (LB.cpp:552-603, 1278-1319). */
+typedef struct hb_cylinders {
+    int32_t count;
+    const double* p1;          /* [3*count] axis point 1                                     */
+    const double* p2;          /* [3*count] axis point 2                                     */
+    const double* radius;      /* [count]                                                    */
+    const double* omega;       /* [3*count] angular velocity (used when moving)              */
+    const int32_t* moving;     /* [count] 1: rotating (curved-node velocity omega x r)       */
+} hb_cylinders;
+
 typedef struct hb_ctx hb_ctx;
 
 /* ---- lifecycle ------------------------------------------------------------------- */
+/* Cylinders for the next hb_init (call between hb_create and hb_init).  Not combined
+ * with moving particles (cylinder-particle contacts, DEM.cpp:1719-2058, are not
+ * implemented) or with a free surface: hb_init returns HB_ERR_UNSUPPORTED. */
+int hb_set_cylinders(hb_ctx* ctx, const hb_cylinders* cylinders);
 /* Replaces the LB/DEM constructors + LB::latticeDefinition (LB.cpp:42-83) and
  * DEM::discreteElementInit parameter setup (DEM.cpp:185-297).  Allocates all device
  * memory once; nothing is allocated per step. */

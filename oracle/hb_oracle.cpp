@@ -136,6 +136,42 @@ struct Elmt {  // elmt.h:53-135 (single-sphere elements)
     V3 px0, px1;
 };
 
+struct Cyl {  // utils.h:85-110 (cylinder), initAxes utils.cpp:154-161
+    V3 p1, p2, naxes, omega;
+    double R;
+    bool moving;
+};
+
+// tinyVector::insideCylinder (vector.cpp:160-170)
+bool insideCylinder(const V3& pt, const V3& p1, const V3& naxes, double R) {
+    const V3 d = sub(pt, p1);
+    const V3 ax = mul(dot(d, naxes), naxes);
+    return norm2(sub(d, ax)) < R * R;
+}
+// cylinder::getSpeed (utils.cpp:106-120)
+V3 cylinderSpeed(const Cyl& c, const V3& pt) {
+    if (!c.moving) return v3(0.0, 0.0, 0.0);
+    const V3 pt1 = sub(pt, c.p1);
+    const V3 proj = add(c.p1, mul(dot(c.naxes, pt1), c.naxes));
+    return cross(c.omega, sub(pt, proj));
+}
+// cylinder::segmentIntercept (utils.cpp:177-224), both roots with -sqrt as the reference
+double segmentIntercept(const Cyl& c, const V3& start, const V3& dir) {
+    const V3 AB = sub(c.p2, c.p1);
+    const V3 AO = sub(start, c.p1);
+    const V3 AOxAB = cross(AO, AB);
+    const V3 VxAB = cross(dir, AB);
+    const double ab2 = dot(AB, AB);
+    const double a = dot(VxAB, VxAB);
+    const double b = 2 * dot(VxAB, AOxAB);
+    const double cc = dot(AOxAB, AOxAB) - (c.R * c.R * ab2);
+    const double disc = b * b - 4 * a * cc;
+    if (disc < 0) return 0.0;
+    const double t1 = (-b - std::sqrt(disc)) / (2 * a);
+    if (t1 < 0) return 0.0;
+    return t1;
+}
+
 struct Object {  // elmt.h:199-221
     double r;
     V3 x0, x1, fparticle;
@@ -162,6 +198,8 @@ struct hbo_sim {
     std::vector<Elmt> el;
     std::vector<Object> obj;
     std::vector<Wall> walls;
+    std::vector<Cyl> cyl;
+    std::vector<double> delta;  // [i*19+j] curve::delta of curved nodes (LB.cpp:589-603)
     V3 demF;
     double deltat, demTime, maxDisp, nebrRange, trigger;
     bool triggerSet;
@@ -294,6 +332,10 @@ bool buildLattice(hbo_sim& s, const hb_elements* e, const hb_objects* o) {
             }
         }
     }
+    // cylinders: nodes outside become curved walls (LB.cpp:552-586)
+    for (size_t ic = 0; ic < s.cyl.size(); ++ic)
+        for (size_t i = 0; i < N; ++i)
+            if (!insideCylinder(s.pos(i), s.cyl[ic].p1, s.cyl[ic].naxes, s.cyl[ic].R)) s.type[i] = 9;
     // objects become static wall nodes (LB.cpp:535-550)
     for (size_t io = 0; io < s.obj.size(); ++io) {
         const Object& ob = s.obj[io];
@@ -301,6 +343,19 @@ bool buildLattice(hbo_sim& s, const hb_elements* e, const hb_objects* o) {
             if (norm2(sub(s.pos(i), ob.x0)) < ob.r * ob.r) {
                 s.solid[i] = (uint32_t)io;
                 s.type[i] = 7;
+            }
+        }
+    }
+    // curve::delta of every curved node toward its non-wall neighbours, from the first
+    // cylinder (LB.cpp:589-603, cylinder::segmentIntercept utils.cpp:177-224)
+    if (!s.cyl.empty()) {
+        s.delta.assign(N * Q, 0.0);
+        for (size_t i = 0; i < N; ++i) {
+            if (s.type[i] != 9) continue;
+            for (int j = 1; j < Q; ++j) {
+                const uint32_t l = s.nb[i * Q + j];
+                if (s.isWall(l)) continue;
+                s.delta[i * Q + j] = 1.0 - segmentIntercept(s.cyl[0], s.pos(i), cvec(j));
             }
         }
     }
@@ -353,13 +408,19 @@ bool buildLattice(hbo_sim& s, const hb_elements* e, const hb_objects* o) {
         for (int j = 0; j < Q; ++j) {
             const uint32_t l = s.nb[i * Q + j];
             if (s.has[l]) continue;
-            if (s.type[l] == 7) {
+            if (s.type[l] == 7 || s.type[l] == 5) {
                 nodeInit(s, l, 1.0, v3(0, 0, 0), 0.0, 0.0, v3(0, 0, 0));
-            } else if (s.type[l] == 8) {
+            } else if (s.type[l] == 8 || s.type[l] == 6 || s.type[l] == 9) {
+                // the wall whose plane holds the node, else the cylinder it is outside of,
+                // else the object it is inside of (LB.cpp:969-990)
                 V3 vel = v3(0, 0, 0);
                 const uint32_t si = s.solid[l];
                 if (si < s.walls.size() && dot(s.walls[si].n, sub(s.pos(l), s.walls[si].p)) < 0.0)
                     vel = s.walls[si].speed(s.pos(l));
+                else if (si < s.cyl.size() && !insideCylinder(s.pos(l), s.cyl[si].p1, s.cyl[si].naxes, s.cyl[si].R))
+                    vel = cylinderSpeed(s.cyl[si], s.pos(l));
+                else if (si < s.obj.size() && norm2(sub(s.pos(l), s.obj[si].x0)) < s.obj[si].r * s.obj[si].r)
+                    vel = s.obj[si].x1;
                 nodeInit(s, l, 1.0, vel, 0.0, 0.0, v3(0, 0, 0));
             }
         }
@@ -867,6 +928,23 @@ bool streaming(hbo_sim& s) {  // LB.cpp:1144-1488
                 fi[OPP[j]] = fsi[j] - BBi;
             } else if (t == 7) {
                 fi[OPP[j]] = fsi[j];
+            } else if (t == 9) {  // curved walls, LB.cpp:1278-1319 (curve: node.cpp:458-472)
+                const V3 vel = s.u[l];
+                const double BBi = 2.0 * 3.0 * 1.0 * 1.0 * s.n[i] * W[j] * dot(vel, cvec(j));
+                const double dl = s.delta[(size_t)l * Q + OPP[j]];
+                const double tau = 0.5 + 3.0 * s.visc[i];
+                const double chi = dl >= 0.5 ? (2.0 * dl - 1.0) / tau : (2.0 * dl - 1.0) / (tau - 2.0);
+                V3 ubf = v3(0.0, 0.0, 0.0);
+                if (dl >= 0.5) {
+                    ubf = add(mul((dl - 1) / dl, s.u[i]), mul(1 / dl, vel));
+                } else {
+                    const uint32_t back = s.nb[i * Q + OPP[j]];
+                    ubf = (s.type[back] == 0 && s.has[back]) ? s.u[back] : vel;
+                }
+                const double usq = norm2(s.u[i]);
+                const double vu = dot(s.u[i], cvec(j));
+                const double fStar = s.n[i] * W[j] * (1 + 3.0 * dot(cvec(j), ubf) + 4.5 * vu * vu + 1.5 * usq);
+                fi[OPP[j]] = (1.0 - chi) * fsi[j] + chi * fStar - BBi;
             } else if (t == 5 || t == 6) {  // slip walls, LB.cpp:1358-1456
                 // moving slip walls (6) bounce back with BBi of the wall node's velocity
                 const double BBi = t == 6 ? 6.0 * s.n[i] * W[j] * dot(s.u[l], cvec(j)) : 0.0;
@@ -1087,8 +1165,26 @@ int hbo_set_threads(int n) {
 }
 
 hbo_sim* hbo_create(const hb_params* p, const hb_elements* e, const hb_objects* o) {
+    return hbo_create_cyl(p, e, o, nullptr);
+}
+
+hbo_sim* hbo_create_cyl(const hb_params* p, const hb_elements* e, const hb_objects* o, const hb_cylinders* cy) {
     if (!p) { g_err = "null params"; return nullptr; }
     hbo_sim* s = new hbo_sim();
+    if (cy) {
+        for (int k = 0; k < cy->count; ++k) {
+            Cyl c;
+            c.p1 = v3(cy->p1[3 * k], cy->p1[3 * k + 1], cy->p1[3 * k + 2]);
+            c.p2 = v3(cy->p2[3 * k], cy->p2[3 * k + 1], cy->p2[3 * k + 2]);
+            const V3 ax = sub(c.p2, c.p1);
+            const double nrm = std::sqrt(norm2(ax));
+            c.naxes = v3(ax.x / nrm, ax.y / nrm, ax.z / nrm);
+            c.R = cy->radius[k];
+            c.omega = cy->omega ? v3(cy->omega[3 * k], cy->omega[3 * k + 1], cy->omega[3 * k + 2]) : v3(0, 0, 0);
+            c.moving = cy->moving ? cy->moving[k] != 0 : false;
+            s->cyl.push_back(c);
+        }
+    }
     s->P = *p;
     s->X = p->lb_size[0]; s->Y = p->lb_size[1]; s->Z = p->lb_size[2];
     s->N = (size_t)s->X * s->Y * s->Z;

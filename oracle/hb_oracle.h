@@ -20,6 +20,8 @@ typedef struct hbo_sim hbo_sim;
 
 /* init as LB::latticeBolzmannInit + DEM::discreteElementInit; NULL on error */
 hbo_sim* hbo_create(const hb_params* p, const hb_elements* e, const hb_objects* o);
+/* the same with cylinders (curved walls, LB.cpp:552-603) */
+hbo_sim* hbo_create_cyl(const hb_params* p, const hb_elements* e, const hb_objects* o, const hb_cylinders* cy);
 void hbo_destroy(hbo_sim* s);
 const char* hbo_last_error(void);
 /* nsteps goCycle()s (hybird.cpp:35-66) */

@@ -4,11 +4,16 @@
 // links or calls this file.
 //
 // Usage:  ref_dump <config.cfg> <workdir> <out.bin> <step> [<step> ...] [--gasbox fx fz] [--vtk]
+//                  [--cylinder p1x p1y p1z p2x p2y p2z R]
 //
 // The driver mirrors hybird.cpp:245-344 (main): parseCommandLine -> parseConfigFile ->
 // io.initialize -> lb.latticeDefinition -> dem.discreteElementInit ->
 // lb.latticeBolzmannInit -> goCycle x N (hybird.cpp:35-66).  After each requested
 // step count the state is appended to <out.bin> as named records.
+//
+// --cylinder adds one static cylinder to dem.cylinders after dem.discreteElementInit (as
+// the DRUM/AVALANCHE/NET problem cases do, DEM.cpp:871-935, without their other
+// settings), so the lattice initialisation marks curved walls around it.
 //
 // --gasbox fx fz replaces lb.latticeBolzmannInit by its pieces (LB.cpp:190-219,
 // 324-340) and marks gas where x >= fx*lbSizeX or z >= fz*lbSizeZ before the generic
@@ -52,6 +57,8 @@ namespace {
 
 FILE* g_out = nullptr;
 bool g_vtk = false;
+bool g_cyl = false;
+double g_cylv[7] = {0, 0, 0, 0, 0, 0, 0};
 std::string g_work;
 
 // record: char name[32]; uint32 dtype (0=f64,1=u32,2=u8,3=i64); uint64 count; payload
@@ -205,6 +212,10 @@ int main(int argc, char** argv) {
     for (int a = 4; a < argc; ++a) {
         if (!strcmp(argv[a], "--vtk")) {
             g_vtk = true;
+        } else if (!strcmp(argv[a], "--cylinder") && a + 7 < argc) {
+            g_cyl = true;
+            for (int k = 0; k < 7; ++k) g_cylv[k] = atof(argv[a + 1 + k]);
+            a += 7;
         } else if (!strcmp(argv[a], "--gasbox") && a + 2 < argc) {
             gasbox = true;
             gfx = atof(argv[a + 1]);
@@ -230,6 +241,18 @@ int main(int argc, char** argv) {
     io.initialize();
     lb.latticeDefinition();
     dem.discreteElementInit(lb.boundary, lb.lbSize, lb.unit, lb.lbF);
+    if (g_cyl) {
+        cylinder cy;
+        cy.index = (unsigned int)dem.cylinders.size();
+        cy.p1 = tVect(g_cylv[0], g_cylv[1], g_cylv[2]);
+        cy.p2 = tVect(g_cylv[3], g_cylv[4], g_cylv[5]);
+        cy.R = g_cylv[6];
+        cy.omega.reset();
+        cy.initAxes();
+        cy.moving = false;
+        cy.slip = false;
+        dem.cylinders.push_back(cy);
+    }
     if (io.lbmSolve) {
         if (!gasbox) {
             lb.latticeBolzmannInit(dem.cylinders, dem.walls, dem.particles, dem.objects);

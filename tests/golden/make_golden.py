@@ -123,6 +123,12 @@ CASES = {
                  slipCoefficient=0.5,
                  boundary0=5, boundary1=7, boundary2=7, boundary3=5, boundary4=5, boundary5=7),
         spheres=[], objects=[], gasbox=(0.4, 0.6), steps=[0, 1, 5, 20, 60], full=[1, 20, 60]),
+    # curved walls (LB.cpp:552-603, 1278-1319): a pipe along x, periodic ends
+    "pipe_curved": dict(
+        cfg=dict(lbSizeX=10, lbSizeY=12, lbSizeZ=12, lbFX=2e-5, initVisc=0.1, initVelocityX=0.005,
+                 boundary0=4, boundary1=4, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
+        spheres=[], objects=[], cylinder=(0.0, 5.5, 5.3, 1.0, 5.5, 5.3, 4.6),
+        steps=[0, 1, 5, 30], full=[1, 30], vtk=[30]),
     # Hertzian contacts (DEM.cpp:2138-2222): spheres falling onto the floor and onto each
     # other, DEM only; kept > nebrRange from the side walls (first wall in range only)
     "dem_hertz": dict(
@@ -209,12 +215,16 @@ def run_case(name, spec):
             cmd += ["--gasbox", str(spec["gasbox"][0]), str(spec["gasbox"][1])]
         if spec.get("vtk"):
             cmd += ["--vtk"]
+        if spec.get("cylinder"):
+            cmd += ["--cylinder"] + [repr(v) for v in spec["cylinder"]]
         env = dict(os.environ, OMP_NUM_THREADS="1")
         subprocess.run(cmd, check=True, cwd=tmp, env=env, stdout=subprocess.DEVNULL, timeout=120)
         snaps = parse_dump(out)
 
     store = {}
     params = {k: v for k, v in cfg.items() if k not in ("particleFile", "objectFile")}
+    if spec.get("cylinder"):
+        params["cylinder"] = list(spec["cylinder"])
     store["params_json"] = np.frombuffer(json.dumps(params).encode(), dtype=np.uint8)
     store["spheres"] = np.array([[c[0], c[1], c[2], r] for (c, r) in spheres], dtype=np.float64).reshape(-1, 4)
     store["objects"] = np.array(spec["objects"], dtype=np.float64).reshape(-1, 4)

@@ -29,6 +29,8 @@ def oracle_lib():
     P = C.POINTER
     lib.hbo_create.restype = C.c_void_p
     lib.hbo_create.argtypes = [P(abi.HbParams), P(abi.HbElements), P(abi.HbObjects)]
+    lib.hbo_create_cyl.argtypes = [P(abi.HbParams), P(abi.HbElements), P(abi.HbObjects), P(abi.HbCylinders)]
+    lib.hbo_create_cyl.restype = C.c_void_p
     lib.hbo_destroy.argtypes = [C.c_void_p]
     lib.hbo_last_error.restype = C.c_char_p
     for name in ("hbo_cycle",):
@@ -65,12 +67,14 @@ def _p(a):
 class OracleSim:
     """One CPU-oracle simulation (FP64, reference semantics)."""
 
-    def __init__(self, params, spheres=None, objects=None, threads=1):
+    def __init__(self, params, spheres=None, objects=None, threads=1, cylinders=None):
         self.lib = oracle_lib()
         self.lib.hbo_set_threads(threads)
         self.params = params
         self.arrays = abi.ElementArrays(spheres, objects)
-        self.h = self.lib.hbo_create(C.byref(params), self.arrays.el_ptr(), self.arrays.ob_ptr())
+        self.cyl = abi.CylinderArrays(cylinders) if cylinders is not None and len(cylinders) else None
+        self.h = self.lib.hbo_create_cyl(C.byref(params), self.arrays.el_ptr(), self.arrays.ob_ptr(),
+                                         self.cyl.ptr() if self.cyl else None)
         if not self.h:
             raise RuntimeError("oracle init failed: " + self.lib.hbo_last_error().decode())
         self.N = int(self.lib.hbo_nodes(self.h))
@@ -191,6 +195,12 @@ def golden_params(d, **over):
         kw["gas_box"] = tuple(c["gasbox"])
     kw.update(over)
     return abi.make_params(**kw)
+
+
+def golden_cylinders(d):
+    """The cylinder rows a fixture was made with (p1, p2, R), or None."""
+    c = json.loads(bytes(d["params_json"]).decode())
+    return [c["cylinder"]] if "cylinder" in c else None
 
 
 def golden_gasbox(name):

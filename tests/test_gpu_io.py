@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 from hybird_gb300 import abi
-from oracle_port import OracleSim, golden_gasbox, golden_params, load_golden
+from oracle_port import OracleSim, golden_cylinders, golden_gasbox, golden_params, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -85,11 +85,12 @@ def _vtk_tokens_match(ours, ref):
     return bad, len(a)
 
 
-@pytest.mark.parametrize("name,step", [("channel_bingham_smag", 10), ("box_spheres", 30), ("dambreak_fs", 60)])
+@pytest.mark.parametrize("name,step", [("channel_bingham_smag", 10), ("box_spheres", 30), ("dambreak_fs", 60),
+                                       ("pipe_curved", 30)])
 def test_vtk_fluid_file_matches_reference(name, step):
     d = load_golden(name)
     p = golden_params(d, gas_box=golden_gasbox(name))
-    g = _gpu()(p, d["spheres"], d["objects"])
+    g = _gpu()(p, d["spheres"], d["objects"], cylinders=golden_cylinders(d))
     g.cycle(step)
     ref = bytes(d[f"s{step}_vtk"]).decode()
     with tempfile.TemporaryDirectory() as tmp:

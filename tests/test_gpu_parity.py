@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from hybird_gb300 import abi
-from oracle_port import OracleSim, golden_gasbox, golden_params, load_golden, rel_linf
+from oracle_port import OracleSim, golden_cylinders, golden_gasbox, golden_params, load_golden, rel_linf
 
 pytestmark = pytest.mark.gpu
 
@@ -18,11 +18,11 @@ def _gpu():
 
 
 @pytest.mark.parametrize("name", ["channel_bgk", "channel_movwall", "channel_bingham_smag", "box_spheres",
-                                  "channel_slip", "box_slip"])
+                                  "channel_slip", "box_slip", "pipe_curved"])
 def test_fp64_matches_reference_fixture(name):
     d = load_golden(name)
     p = golden_params(d, gas_box=golden_gasbox(name))
-    g = _gpu()(p, d["spheres"], d["objects"])
+    g = _gpu()(p, d["spheres"], d["objects"], cylinders=golden_cylinders(d))
     done = 0
     for step in d["steps"]:
         if step > done:
@@ -129,6 +129,38 @@ def test_dem_matches_reference_fixture(name, early_steps):
 def _channel(shape=(64, 32, 32), precision=abi.HB_FP64, collision=abi.HB_BGK, tau=0.8, magic=3 / 16):
     return abi.make_params(shape, (4, 4, 7, 7, 4, 4), init_visc=(tau - 0.5) / 3.0, lbF=(1e-6, 0, 0),
                            precision=precision, collision=collision, trt_magic=magic)
+
+
+def _pipe(precision=abi.HB_FP64):
+    """40x30x30 pipe along x (curved walls around a cylinder of radius 13.2), periodic ends."""
+    return abi.make_params((40, 30, 30), (4, 4, 7, 7, 7, 7), init_visc=0.1, lbF=(3e-6, 0, 0),
+                           precision=precision, init_velocity=(0.004, 0.0, 0.0))
+
+
+PIPE_CYL = [(0.0, 14.6, 14.3, 1.0, 14.6, 14.3, 13.2)]
+
+
+@pytest.mark.parametrize("prec,tol", [(abi.HB_FP64, 1e-12), (abi.HB_FP32, 1e-5), (abi.HB_FP16S, 5e-2)])
+def test_curved_pipe_vs_fp64_oracle(prec, tol):
+    """Curved walls at a larger size than the fixture: the GPU forms against the FP64
+    oracle (itself pinned to the reference's pipe_curved fixture) after 120 steps."""
+    g = _gpu()(_pipe(prec), cylinders=PIPE_CYL)
+    o = OracleSim(_pipe(), threads=4, cylinders=PIPE_CYL)
+    g.cycle(120)
+    o.cycle(120)
+    gl, ol = g.lattice(), o.lattice()
+    np.testing.assert_array_equal(gl["type"], ol["type"])
+    act = ol["type"] == 0
+    du = gl["u"].reshape(3, -1)[:, act] - ol["u"].reshape(3, -1)[:, act]
+    l2 = np.sqrt((du ** 2).sum() / (ol["u"].reshape(3, -1)[:, act] ** 2).sum())
+    print(f"curved pipe prec {prec}: u rel L2 {l2:.3e}")
+    if prec == abi.HB_FP64:
+        assert rel_linf(gl["u"].reshape(3, -1), ol["u"].reshape(3, -1), act) <= tol
+        assert rel_linf(gl["f"].reshape(19, -1), ol["f"].reshape(19, -1), act) <= tol
+    else:
+        assert l2 <= tol, l2
+    g.close()
+    o.close()
 
 
 def test_slip_channel_fp64_vs_oracle():

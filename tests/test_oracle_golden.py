@@ -8,17 +8,17 @@ particle flags, solid indices, interface sets, DEM pair sets) must be identical.
 import numpy as np
 import pytest
 
-from oracle_port import OracleSim, golden_gasbox, golden_params, load_golden, rel_linf
+from oracle_port import golden_cylinders, OracleSim, golden_gasbox, golden_params, load_golden, rel_linf
 
 LATTICE_CASES = ["channel_bgk", "channel_movwall", "channel_bingham_smag", "box_spheres",
-                 "dambreak_fs", "channel_slip", "box_slip", "dambreak_slip"]
+                 "dambreak_fs", "channel_slip", "box_slip", "dambreak_slip", "pipe_curved"]
 TOL = 1e-13
 
 
 def _run(name):
     d = load_golden(name)
     p = golden_params(d, gas_box=golden_gasbox(name))
-    sim = OracleSim(p, d["spheres"], d["objects"])
+    sim = OracleSim(p, d["spheres"], d["objects"], cylinders=golden_cylinders(d))
     return d, sim
 
 
