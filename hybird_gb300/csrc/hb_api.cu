@@ -201,10 +201,12 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         (rc = dalloc(&d.obj, (size_t)E * OBJ_CAP)) || (rc = dalloc(&d.obj_cnt, E)) || (rc = dalloc(&d.scal, 8)) ||
         (rc = dalloc(&d.contacts, 1)) || (rc = dalloc(&d.partial, hb::PARTIAL_CAP)) || (rc = dalloc(&d.done, 1)) ||
         (rc = dalloc(&d.wrec, (size_t)7 * E)) || (rc = dalloc(&d.orec, (size_t)7 * E * OBJ_CAP)) ||
+        (rc = dalloc(&d.cyl_of, E)) ||
         (rc = dalloc(&d.react, (size_t)3 * (MAX_WALLS + d.O))))
         return rc;
     CK(cudaMemset(d.react, 0, sizeof(double) * 3 * (MAX_WALLS + d.O)));
     CK(cudaMemset(d.wrec, 0, sizeof(double) * 7 * E));
+    CK(cudaMemset(d.cyl_of, 0xFF, sizeof(int) * E));
     CK(cudaMemset(d.orec, 0, sizeof(double) * 7 * E * OBJ_CAP));
     const double scal0[8] = {0.5 * d.nebrRange, 1.0, 0, 0, 0, 0, 0, 0};  // maxDisp, rebuild
     CK(cudaMemcpy(d.scal, scal0, sizeof(scal0), cudaMemcpyHostToDevice));
@@ -278,7 +280,7 @@ int hb_destroy(hb_ctx* c) {
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
                     c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
                     c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix, c->fs_ilist,
-                    c->curved_list, c->curved_cnt};
+                    c->curved_list, c->curved_cnt, c->d.cyl_of};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -314,8 +316,8 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     if (!c) return seterr(HB_ERR_ARG, "null ctx");
     if (!c->cyl.empty() && c->P.free_surface)
         return seterr(HB_ERR_UNSUPPORTED, "cylinders (curved walls) with a free surface are not implemented");
-    if (!c->cyl.empty() && c->P.dem_solve && e && e->count > 0)
-        return seterr(HB_ERR_UNSUPPORTED, "cylinders with moving particles (cylinder contacts) are not implemented");
+    if (c->cyl.size() > 4 && c->P.dem_solve && e && e->count > 0)
+        return seterr(HB_ERR_UNSUPPORTED, "more than 4 cylinders with moving particles");
     int rc = dem_init(c, e, o);
     if (rc) return rc;
     const long long N = c->N;

@@ -92,6 +92,7 @@ std::vector<Buf> state_buffers(hb_ctx* c) {
         add("obj_cnt", d.obj_cnt, 4 * E);
         add("dem_scal", d.scal, 8 * 8);
         add("contacts", d.contacts, 4);
+        add("cyl_of", d.cyl_of, 4 * E);
         add("wrec", d.wrec, 8 * 7 * E);
         add("orec", d.orec, 8 * 7 * E * hb::OBJ_CAP);
         add("react", d.react, 8 * 3 * ((size_t)hb::MAX_WALLS + d.O));

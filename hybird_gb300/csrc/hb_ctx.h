@@ -38,6 +38,7 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     int* wall_of = nullptr;     // [E] first wall in range or -1
     int* obj = nullptr;         // [E*OBJ_CAP]
     int* obj_cnt = nullptr;     // [E]
+    int* cyl_of = nullptr;      // [E] first cylinder in range or -1
     double* wrec = nullptr;     // [7E] last substep's wall contact per element: flag, normal, tangential force
     double* orec = nullptr;     // [7E*OBJ_CAP] the same per (element, object slot)
     double* react = nullptr;    // [3*(MAX_WALLS + O)] wall and object FParticle (ordered sums of the records)

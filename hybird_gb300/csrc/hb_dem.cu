@@ -25,6 +25,8 @@ namespace cg = cooperative_groups;
 
 namespace hb {
 
+constexpr int DEM_MAX_CYL = 4;  // cylinders the DEM contacts handle
+
 struct DemArgs {
     int E;
     double *x0, *x1, *x2, *x3, *x4, *x5;
@@ -41,6 +43,10 @@ struct DemArgs {
     int *cell_of, *cell_cnt, *cell_start, *cell_fill, *cell_items;
     int *nbr, *nbr_cnt, *wall_of, *obj, *obj_cnt;
     double *wrec, *orec;  // wall / object contact records of the current substep (7 doubles each)
+    int* cyl_of;          // [E] first cylinder in range or -1 (DEM.cpp:1535-1550)
+    int ncyl;
+    double cp1[DEM_MAX_CYL][3], cnax[DEM_MAX_CYL][3], cR[DEM_MAX_CYL], comg[DEM_MAX_CYL][3];
+    int cmov[DEM_MAX_CYL];
     double* scal;
     int* contacts;
     double* partial;
@@ -188,6 +194,14 @@ __device__ __noinline__ void nl_build_one(const DemArgs& a, int i) {
         if (d < a.nebrRange) { wo = w; break; }
     }
     a.wall_of[i] = wo;
+    int co = -1;  // evalNearCylinderTable: the first cylinder in range (cylinder::dist, utils.cpp:56-67)
+    for (int c = 0; c < a.ncyl; ++c) {
+        const V d = sub(xi, V{a.cp1[c][0], a.cp1[c][1], a.cp1[c][2]});
+        const V nx{a.cnax[c][0], a.cnax[c][1], a.cnax[c][2]};
+        const V dc = sub(mul(dot(d, nx), nx), d);
+        if (a.cR[c] - sqrt(nrm2(dc)) < a.nebrRange) { co = c; break; }
+    }
+    a.cyl_of[i] = co;
     int oc = 0;
     for (int o = 0; o < a.O; ++o) {
         const V d = sub(xi, V{a.ox0[o], a.ox0[a.O + o], a.ox0[2 * a.O + o]});
@@ -301,6 +315,42 @@ __device__ __noinline__ FM object_contact(const DemArgs& a, int o, V vd, double 
     return FM{FW, MW};
 }
 
+// cylinderParticleCollision (DEM.cpp:1984-2058): effective overlap 2x, wall friction; the
+// contact point moves with the cylinder (cylinder::getSpeed, utils.cpp:106-120)
+__device__ __noinline__ FM cylinder_contact(const DemArgs& a, int c, V xpi, double overlap, V xpv, V wpg, double ri,
+                                            double mi, V FW, V MW) {
+    const V p1{a.cp1[c][0], a.cp1[c][1], a.cp1[c][2]};
+    const V nx{a.cnax[c][0], a.cnax[c][1], a.cnax[c][2]};
+    // cylinder::vecDist (utils.cpp:69-82)
+    const V proj = add(p1, mul(dot(nx, sub(xpi, p1)), nx));
+    const V dfa = sub(xpi, proj);
+    const V vd = sub(xpi, add(proj, mul(a.cR[c], divs(dfa, sqrt(nrm2(dfa))))));
+    const V cp = sub(xpi, vd);
+    const V en = divs(vd, ri - overlap);
+    V cpv{0, 0, 0};
+    if (a.cmov[c]) {
+        const V q = add(p1, mul(dot(nx, sub(cp, p1)), nx));
+        cpv = cross(V{a.comg[c][0], a.comg[c][1], a.comg[c][2]}, sub(cp, q));
+    }
+    const V relVel = sub(xpv, cpv);
+    const double vn = dot(relVel, en);
+    const V nrv = mul(vn, en);
+    const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
+    const V nf = mul(fn, en);
+    const V vrJ = mul(-ri, en);
+    const V cJ = add(vrJ, V{0, 0, 0});  // + (particle centre - element centre), zero for spheres
+    FW = add(FW, nf);
+    const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
+    const double nt = sqrt(nrm2(tang));
+    if (nt != 0.0) {
+        const double ft = tangential_contact(a, nt, fn, ri, mi, a.muWall);
+        const V tfc = mul(ft, divs(tang, nt));
+        MW = sub(MW, cross(cJ, tfc));
+        FW = sub(FW, tfc);
+    }
+    return FM{FW, MW};
+}
+
 // contacts of particle i by one warp: lanes take candidates (and objects) in list
 // order, the sums use a fixed xor-shuffle tree, so the result is reproducible
 // a: the kernel's parameter block; ga: its device-memory copy for the out-of-line calls
@@ -341,6 +391,19 @@ __device__ void forces_warp(const DemArgs& a, const DemArgs& ga, int i, int lane
             }
         }
         if (!hit) a.wrec[7 * (long long)i] = 0.0;
+        const int cy = a.cyl_of[i];
+        if (cy >= 0) {  // cylinderParticelContacts (DEM.cpp:1719-1746)
+            const V d = sub(xpi, V{a.cp1[cy][0], a.cp1[cy][1], a.cp1[cy][2]});
+            const V nx{a.cnax[cy][0], a.cnax[cy][1], a.cnax[cy][2]};
+            const double dist = a.cR[cy] - sqrt(nrm2(sub(mul(dot(d, nx), nx), d)));
+            const double overlap = ri - dist;
+            if (overlap > 0.0) {
+                contrib = true;
+                const FM r = cylinder_contact(ga, cy, xpi, overlap, xpv, wpg, ri, mi, FW, MW);
+                FW = r.f;
+                MW = r.m;
+            }
+        }
     }
     const int oc = a.obj_cnt[i];
     for (int k = lane; k < oc; k += 32) {  // objectParticleCollision (DEM.cpp:2060-2136)
@@ -1167,6 +1230,25 @@ static DemArgs dem_args(hb_ctx* c) {
     a.cell_fill = d.cell_fill; a.cell_items = d.cell_items;
     a.nbr = d.nbr; a.nbr_cnt = d.nbr_cnt; a.wall_of = d.wall_of; a.obj = d.obj; a.obj_cnt = d.obj_cnt;
     a.wrec = d.wrec; a.orec = d.orec;
+    a.cyl_of = d.cyl_of;
+    a.ncyl = (int)std::min<size_t>(c->cyl.size(), DEM_MAX_CYL);
+    for (int k = 0; k < DEM_MAX_CYL; ++k) {
+        const bool on = k < a.ncyl;
+        double nx[3] = {0, 0, 0};
+        if (on) {  // cylinder::initAxes (utils.cpp:154-161)
+            const double ax[3] = {c->cyl[k].p2[0] - c->cyl[k].p1[0], c->cyl[k].p2[1] - c->cyl[k].p1[1],
+                                  c->cyl[k].p2[2] - c->cyl[k].p1[2]};
+            const double nrm = sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+            for (int q = 0; q < 3; ++q) nx[q] = ax[q] / nrm;
+        }
+        for (int q = 0; q < 3; ++q) {
+            a.cp1[k][q] = on ? c->cyl[k].p1[q] : 0.0;
+            a.cnax[k][q] = nx[q];
+            a.comg[k][q] = on ? c->cyl[k].omega[q] : 0.0;
+        }
+        a.cR[k] = on ? c->cyl[k].R : 0.0;
+        a.cmov[k] = on ? c->cyl[k].moving : 0;
+    }
     a.scal = d.scal; a.contacts = d.contacts; a.partial = d.partial; a.done = d.done;
     a.ncells = d.ncells; a.nC0 = d.nCells[0]; a.nC1 = d.nCells[1]; a.nC2 = d.nCells[2];
     a.cw0 = d.cellWidth[0]; a.cw1 = d.cellWidth[1]; a.cw2 = d.cellWidth[2];

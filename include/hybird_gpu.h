@@ -161,9 +161,10 @@ typedef struct hb_cylinders {
 typedef struct hb_ctx hb_ctx;
 
 /* ---- lifecycle ------------------------------------------------------------------- */
-/* Cylinders for the next hb_init (call between hb_create and hb_init).  Not combined
- * with moving particles (cylinder-particle contacts, DEM.cpp:1719-2058, are not
- * implemented) or with a free surface: hb_init returns HB_ERR_UNSUPPORTED. */
+/* Cylinders for the next hb_init (call between hb_create and hb_init): curved walls for
+ * the lattice and contact partners of the particles (DEM.cpp:1535-1550, 1719-2058; at most
+ * 4 with moving particles).  Not combined with a free surface: hb_init returns
+ * HB_ERR_UNSUPPORTED. */
 int hb_set_cylinders(hb_ctx* ctx, const hb_cylinders* cylinders);
 /* Replaces the LB/DEM constructors + LB::latticeDefinition (LB.cpp:42-83) and
  * DEM::discreteElementInit parameter setup (DEM.cpp:185-297).  Allocates all device

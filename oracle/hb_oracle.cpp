@@ -171,6 +171,18 @@ double segmentIntercept(const Cyl& c, const V3& start, const V3& dir) {
     if (t1 < 0) return 0.0;
     return t1;
 }
+// cylinder::dist (utils.cpp:56-67): distance of a point from the cylinder surface
+double cylinderDist(const Cyl& c, const V3& pt) {
+    const V3 d = sub(pt, c.p1);
+    const V3 ax = mul(dot(d, c.naxes), c.naxes);
+    return c.R - std::sqrt(norm2(sub(ax, d)));
+}
+// cylinder::vecDist (utils.cpp:69-82)
+V3 cylinderVecDist(const Cyl& c, const V3& pt) {
+    const V3 proj = add(c.p1, mul(dot(c.naxes, sub(pt, c.p1)), c.naxes));
+    const V3 dfa = sub(pt, proj);
+    return sub(pt, add(proj, mul(c.R, divs(dfa, std::sqrt(norm2(dfa))))));
+}
 
 struct Object {  // elmt.h:199-221
     double r;
@@ -207,7 +219,7 @@ struct hbo_sim {
     unsigned nCells[3];
     double dampCoeff, knConst, ksConst;
     std::vector<int> cellTable;
-    std::vector<uint32_t> neighborTable, nearWallTable, nearObjectTable;
+    std::vector<uint32_t> neighborTable, nearWallTable, nearObjectTable, nearCylinderTable;
     std::vector<int> tableCell;
 
     size_t idx(int x, int y, int z) const { return (size_t)x + (size_t)X * ((size_t)y + (size_t)Y * z); }
@@ -543,6 +555,14 @@ void evalNeighborTable(hbo_sim& s) {  // DEM.cpp:1326-1513 (cell table, half-she
                 s.nearObjectTable.push_back(n);
                 s.nearObjectTable.push_back((uint32_t)o);
             }
+    s.nearCylinderTable.clear();  // DEM.cpp:1535-1550: first cylinder in range only
+    for (unsigned n = 0; n < P; ++n)
+        for (size_t c = 0; c < s.cyl.size(); ++c)
+            if (cylinderDist(s.cyl[c], s.el[n].px0) < s.nebrRange) {
+                s.nearCylinderTable.push_back(n);
+                s.nearCylinderTable.push_back((uint32_t)c);
+                break;
+            }
 }
 
 // ---- DEM ----------------------------------------------------------------------------
@@ -625,6 +645,32 @@ void wallParticleCollision(hbo_sim& s, Wall& w, unsigned j, double overlap) {  /
         B.MWall = sub(B.MWall, cross(cJ, tf));
         B.FWall = sub(B.FWall, tf);
         w.fparticle = add(w.fparticle, tf);
+    }
+}
+
+void cylinderParticleCollision(hbo_sim& s, const Cyl& c, unsigned j, double overlap) {  // DEM.cpp:1984-2058
+    Elmt& B = s.el[j];
+    const double radJ = B.radius;
+    const V3 vd = cylinderVecDist(c, B.px0);
+    const V3 cp = sub(B.px0, vd);
+    const V3 en = divs(vd, radJ - overlap);
+    const V3 relVel = sub(B.px1, cylinderSpeed(c, cp));
+    const double vn = dot(relVel, en);
+    const V3 nrv = mul(vn, en);
+    const double fn = normalContact(s, 2.0 * overlap, vn, radJ, B.m);
+    const V3 nf = mul(fn, en);
+    const V3 vecRadJ = mul(-radJ, en);
+    const V3 cJ = add(vecRadJ, sub(B.px0, B.px0));  // + (particle - element centre): spheres
+    B.FWall = add(B.FWall, nf);
+    const V3 rvc = add(relVel, cross(B.wpGlobal, vecRadJ));
+    const V3 tang = sub(rvc, nrv);
+    const double nt = norm(tang);
+    if (nt != 0.0) {
+        const double ft = tangentialContact(s, nt, fn, radJ, B.m, s.P.friction_wall);
+        const V3 et = divs(tang, norm(tang));
+        const V3 tf = mul(ft, et);
+        B.MWall = sub(B.MWall, cross(cJ, tf));
+        B.FWall = sub(B.FWall, tf);
     }
 }
 
@@ -725,6 +771,12 @@ void demSubstep(hbo_sim& s) {  // DEM.cpp:336-374
         const V3 vd = sub(s.el[j].px0, o.x0);
         const double overlap = s.el[j].radius + o.r - norm(vd);
         if (overlap > 0.0) objectParticleCollision(s, o, j, vd);
+    }
+    for (size_t k = 0; k < s.nearCylinderTable.size(); k += 2) {  // DEM.cpp:1719-1746
+        const unsigned j = s.nearCylinderTable[k];
+        const Cyl& c = s.cyl[s.nearCylinderTable[k + 1]];
+        const double overlap = s.el[j].radius - cylinderDist(c, s.el[j].px0);
+        if (overlap > 0.0) cylinderParticleCollision(s, c, j, overlap);
     }
     const double nv = s.P.num_visc;
     for (auto& e : s.el) {

@@ -129,6 +129,19 @@ CASES = {
                  boundary0=4, boundary1=4, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
         spheres=[], objects=[], cylinder=(0.0, 5.5, 5.3, 1.0, 5.5, 5.3, 4.6),
         steps=[0, 1, 5, 30], full=[1, 30], vtk=[30]),
+    # coupled: spheres settling in a fluid-filled horizontal pipe closed at both ends
+    # (curved walls + cylinder contacts + coupling)
+    "pipe_spheres": dict(
+        cfg=dict(lbSizeX=14, lbSizeY=16, lbSizeZ=16, lbFZ=-2e-4, initVisc=0.1, multiStep=3,
+                 boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
+        spheres=("rsa", 23, 5, 1.6, 2.2, (1.5, 4.5, 3.5), (12.5, 10.5, 10.5)), objects=[],
+        cylinder=(0.0, 7.5, 7.5, 1.0, 7.5, 7.5, 6.8), steps=[0, 1, 10, 40], full=[1, 40]),
+    # DEM only: spheres falling inside a horizontal cylinder (DEM.cpp:1535-1550, 1719-2058)
+    "dem_cylinder": dict(
+        cfg=dict(lbSizeX=24, lbSizeY=20, lbSizeZ=20, lbSolve=0, lbFZ=-2e-3, multiStep=20,
+                 boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
+        spheres=("rsa", 21, 8, 1.2, 1.8, (4.0, 7.0, 5.0), (20.0, 13.0, 9.0)),
+        objects=[], cylinder=(0.0, 10.0, 10.0, 1.0, 10.0, 10.0, 8.6), steps=[0, 1, 30, 60, 100], full=[]),
     # Hertzian contacts (DEM.cpp:2138-2222): spheres falling onto the floor and onto each
     # other, DEM only; kept > nebrRange from the side walls (first wall in range only)
     "dem_hertz": dict(

@@ -18,7 +18,7 @@ def _gpu():
 
 
 @pytest.mark.parametrize("name", ["channel_bgk", "channel_movwall", "channel_bingham_smag", "box_spheres",
-                                  "channel_slip", "box_slip", "pipe_curved"])
+                                  "channel_slip", "box_slip", "pipe_curved", "pipe_spheres"])
 def test_fp64_matches_reference_fixture(name):
     d = load_golden(name)
     p = golden_params(d, gas_box=golden_gasbox(name))
@@ -95,13 +95,13 @@ def test_init_matches_reference_fixture():
     g.close()
 
 
-@pytest.mark.parametrize("name,early_steps", [("dem_objects", 50), ("dem_hertz", 30)])
+@pytest.mark.parametrize("name,early_steps", [("dem_objects", 50), ("dem_hertz", 30), ("dem_cylinder", 30)])
 def test_dem_matches_reference_fixture(name, early_steps):
     """LINEAR contacts against objects and walls; HERTZIAN contacts between spheres and
-    with the floor (DEM.cpp:2138-2222)."""
+    with the floor (DEM.cpp:2138-2222); contacts with a cylinder (DEM.cpp:1719-2058)."""
     d = load_golden(name)
     p = golden_params(d)
-    g = _gpu()(p, d["spheres"], d["objects"])
+    g = _gpu()(p, d["spheres"], d["objects"], cylinders=golden_cylinders(d))
     done = 0
     for step in d["steps"]:
         if step > done:

@@ -11,7 +11,7 @@ import pytest
 from oracle_port import golden_cylinders, OracleSim, golden_gasbox, golden_params, load_golden, rel_linf
 
 LATTICE_CASES = ["channel_bgk", "channel_movwall", "channel_bingham_smag", "box_spheres",
-                 "dambreak_fs", "channel_slip", "box_slip", "dambreak_slip", "pipe_curved"]
+                 "dambreak_fs", "channel_slip", "box_slip", "dambreak_slip", "pipe_curved", "pipe_spheres"]
 TOL = 1e-13
 
 
@@ -49,7 +49,7 @@ def test_lattice_matches_reference(name):
             assert np.allclose(fh, g["w_FHydro"], rtol=1e-12, atol=1e-15), (name, step, fh, g["w_FHydro"])
 
 
-@pytest.mark.parametrize("name", ["box_spheres", "dem_objects", "dem_hertz"])
+@pytest.mark.parametrize("name", ["box_spheres", "dem_objects", "dem_hertz", "dem_cylinder", "pipe_spheres"])
 def test_dem_matches_reference(name):
     d, sim = _run(name)
     done = 0
