@@ -8,7 +8,8 @@
 // bit-identically.  File layout (little-endian, native struct layout):
 //   header  "HBCKPT01", uint32 version, uint32 sizeof(hb_params), hb_params,
 //           int64 N, E, O, int64 steps, int32 cur, uint8 reduce_pending, dem_stepped
-//   records char name[24], uint64 bytes, payload   (the buffers of state_buffers())
+//   records char name[24], uint64 bytes, payload   (the cylinders as given, then the
+//           buffers of state_buffers())
 // The loader rebuilds the context with hb_create + hb_init from the saved parameters,
 // particles and objects (so every allocation and both cycle graphs exist), then
 // overwrites each buffer and the host step state.
@@ -131,6 +132,13 @@ int hb_checkpoint_save(hb_ctx* c, const char* path) {
     h.N = c->N; h.E = c->d.E; h.O = c->d.O; h.steps = c->steps; h.cur = c->cur;
     h.reduce_pending = c->reduce_pending; h.dem_stepped = c->dem_stepped;
     f.write(reinterpret_cast<const char*>(&h), sizeof(h));
+    {  // the cylinders (host data: they define the curved walls the loader rebuilds)
+        char nm[24] = "cylinders";
+        const uint64_t n = sizeof(hb_cyl_host) * c->cyl.size();
+        f.write(nm, 24);
+        f.write(reinterpret_cast<const char*>(&n), 8);
+        if (n) f.write(reinterpret_cast<const char*>(c->cyl.data()), (std::streamsize)n);
+    }
     std::vector<char> host;
     for (const Buf& b : state_buffers(c)) {
         char nm[24] = {};
@@ -207,6 +215,11 @@ int hb_checkpoint_load(const char* path, hb_ctx** out) {
     hb_ctx* c = nullptr;
     int rc = hb_create(&P, &c);
     if (rc) return rc;
+    if (const std::vector<char>* cy = find("cylinders")) {
+        const size_t nc = cy->size() / sizeof(hb_cyl_host);
+        c->cyl.assign(reinterpret_cast<const hb_cyl_host*>(cy->data()),
+                      reinterpret_cast<const hb_cyl_host*>(cy->data()) + nc);
+    }
     rc = hb_init(c, E > 0 ? &el : nullptr, O > 0 ? &ob : nullptr);
     if (rc) { hb_destroy(c); return rc; }
     if (c->N != h.N || c->d.E != E || c->d.O != O) {

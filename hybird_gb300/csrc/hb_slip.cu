@@ -105,8 +105,9 @@ __global__ void k_slip_mix(SlipArgs a) {
             const long long c = a0 ? c0 : c1;
             const int d = a0 ? d0 : d1;
             // the partner's own link d must end on a wall that bounced fs_c[d] back as is
+            // (static, slip or curved: the curved pass runs after this one)
             const uint8_t pl = a.ntype[slip_link(a, c, d)] & HB_TYPE_MASK;
-            if (!(slip_code(pl) || pl == HB_T_STATWALL)) flag_status(a.status, 1);
+            if (!(slip_code(pl) || pl == HB_T_STATWALL || pl == HB_T_CURVED)) flag_status(a.status, 1);
             const S* f = reinterpret_cast<const S*>(a.f);
             const double fp = (double)P::load(f + (long long)opp(d) * a.N + c);
             const double fo = (double)P::load(f + (long long)opp(j) * a.N + i);

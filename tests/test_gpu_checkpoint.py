@@ -51,12 +51,21 @@ def _dambreak():
     return golden_params(d, gas_box=golden_gasbox("dambreak_fs")), None, None
 
 
+def _pipe_slip():
+    """Curved walls around a cylinder along x plus slip walls at the x ends, FP32."""
+    p = abi.make_params((24, 20, 20), (5, 6, 7, 7, 7, 7), init_visc=0.1, lbF=(2e-5, 0, -1e-5),
+                        precision=abi.HB_FP32, slip_coefficient=0.4, init_velocity=(0.003, 0.0, 0.0))
+    return p, None, None
+
+
 CASES = {
     "coupled_fp32": lambda: _coupled_box(abi.HB_FP32),
     "coupled_fp16s": lambda: _coupled_box(abi.HB_FP16S),
     "coupled_fp64": lambda: _coupled_box(abi.HB_FP64),
     "dambreak_fp64": _dambreak,
+    "pipe_slip_fp32": _pipe_slip,
 }
+CYL = {"pipe_slip_fp32": [(0.0, 9.5, 9.7, 1.0, 9.5, 9.7, 8.3)]}
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -64,7 +73,7 @@ CASES = {
 def test_restart_continues_bit_identically(name, k1, k2):
     p, sph, obj = CASES[name]()
     G = _gpu()
-    a = G(p, sph, obj)
+    a = G(p, sph, obj, cylinders=CYL.get(name))
     a.cycle(k1)
     with tempfile.TemporaryDirectory() as tmp:
         path = os.path.join(tmp, "state.hbck")
