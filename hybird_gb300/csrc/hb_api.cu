@@ -77,7 +77,8 @@ int check_params(const hb_params* p) {
     if (!(p->init_visc > 0.0)) return seterr(HB_ERR_ARG, "init_visc must be > 0");
     if (p->precision < HB_FP64 || p->precision > HB_FP16S) return seterr(HB_ERR_ARG, "precision");
     if (p->collision != HB_BGK && p->collision != HB_TRT) return seterr(HB_ERR_ARG, "collision");
-    if (p->dem_solve && p->multi_step < 1) return seterr(HB_ERR_ARG, "multi_step must be >= 1");
+    if (p->dem_solve && (p->multi_step < 1 || p->multi_step > hb::MAX_MULTI))
+        return seterr(HB_ERR_ARG, "multi_step must be in 1..%d", hb::MAX_MULTI);
     const long long N = (long long)p->lb_size[0] * p->lb_size[1] * p->lb_size[2];
     if (p->precision != HB_FP64 && 19LL * N >= (1LL << 31))  // 32-bit population offsets
         return seterr(HB_ERR_UNSUPPORTED, "FP32/FP16 lattices are limited to 19 * nodes < 2^31 (%lld nodes)", N);

@@ -31,6 +31,7 @@ constexpr int NBR_CAP = 48;      // candidate neighbours kept per particle
 constexpr int OBJ_CAP = 16;      // objects in range kept per particle
 constexpr int STATUS_WORDS = 8;  // device status words (numeric, capacity, wait, ...)
 constexpr int PARTIAL_CAP = 4096;  // per-block partials of grid-wide reductions (>= any grid used)
+constexpr int MAX_MULTI = 64;      // DEM substeps per cycle (their maxima use the last partial slots)
 // fixed-point scale of the element force/torque/volume sums of the reduced-precision
 // lattice kernels: 64-bit integer sums are exact and order-free, so the atomics that
 // build them give the same bits on every run

@@ -1097,8 +1097,6 @@ __device__ __forceinline__ void warp_tasks(int& first, int& stride) {
 __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
     cg::grid_group grid = cg::this_grid();
     __shared__ double sh[7][256];
-    __shared__ double s_maxdisp;
-    __shared__ int s_rebuild;
     const int E = A.d.E;
     // element loops spread consecutive elements over different blocks, so the FP64 work
     // (narrow pipe on this part) lands on every SM instead of the first few
@@ -1119,7 +1117,10 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
     if (A.do_dem) {
         double maxDisp = A.d.scal[0];
         bool rebuild = A.d.scal[1] != 0.0;
+        // per-substep maxima of |x1|^2 (the last MAX_MULTI slots of the partials array)
+        unsigned long long* vmax = reinterpret_cast<unsigned long long*>(A.d.partial + PARTIAL_CAP - MAX_MULTI);
         if (blockIdx.x == 0 && threadIdx.x == 0) *A.d.contacts = 0;
+        if (blockIdx.x == 0 && (int)threadIdx.x < A.multi) vmax[threadIdx.x] = 0ull;
         grid.sync();
         stamp(A, k++);
         for (int s = 0; s < A.multi; ++s) {
@@ -1157,33 +1158,22 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
                     if (plain && c == 0) v2 = fmax(v2, x1c * x1c + y1 * y1 + z1 * z1);
                 }
             }
-            sh[0][threadIdx.x] = v2;
-            __syncthreads();
-            for (int q = blockDim.x / 2; q > 0; q >>= 1) {
-                if ((int)threadIdx.x < q) sh[0][threadIdx.x] = fmax(sh[0][threadIdx.x], sh[0][threadIdx.x + q]);
-                __syncthreads();
-            }
-            if (threadIdx.x == 0) A.d.partial[blockIdx.x] = sh[0][0];
+            // DEM.cpp:1314-1324, 334-347: the largest |x1|^2 of the substep, per warp by
+            // shuffles, then one 64-bit atomicMax per warp into this substep's slot
+            // (non-negative doubles order like their bit patterns; a maximum does not
+            // depend on the order), read back by every thread after the barrier
+            for (int off = 16; off > 0; off >>= 1) v2 = fmax(v2, __shfl_xor_sync(0xffffffffu, v2, off));
+            if (lane == 0 && v2 > 0.0) atomicMax(vmax + s, (unsigned long long)__double_as_longlong(v2));
             grid.sync();
             stamp(A, k++);
-            // DEM.cpp:1314-1324, 334-347: warp 0 of every block folds the block maxima with
-            // its lanes (max is order-independent, so every block gets the same flag) and
-            // hands the result to the rest of the block through shared memory
-            if (threadIdx.x < 32) {
-                double mx = 0.0;
-                for (int b = lane; b < (int)gridDim.x; b += 32) mx = fmax(mx, ((volatile double*)A.d.partial)[b]);
-                for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-                if (lane == 0) {
-                    double md = maxDisp + sqrt(mx) * A.d.dt;
-                    const bool rb = md > A.d.trigger;
-                    if (rb) md = 0.0;
-                    s_maxdisp = md;
-                    s_rebuild = rb ? 1 : 0;
-                }
+            {
+                const double mx = __longlong_as_double((long long)((volatile unsigned long long*)vmax)[s]);
+                double md = maxDisp + sqrt(mx) * A.d.dt;
+                const bool rb = md > A.d.trigger;
+                if (rb) md = 0.0;
+                maxDisp = md;
+                rebuild = rb;
             }
-            __syncthreads();
-            maxDisp = s_maxdisp;
-            rebuild = s_rebuild != 0;
         }
         if (A.do_boxes)  // positions are final: boxes for the coupling passes
             for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) build_box(A.c, p);
