@@ -394,6 +394,8 @@ int hb_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside, con
     if (!c->initialized) return seterr(HB_ERR_STATE, "hb_init must run first");
     if (launch_upload_lattice(c, type, inside, solid, f, n, u, mass, visc))
         return seterr(HB_ERR_CUDA, "upload: %s", cudaGetErrorString(cudaGetLastError()));
+    curved_remark(c);  // the uploaded node bytes carry no velocity-mirror bits
+    CK(cudaStreamSynchronize(c->stream));
     return HB_OK;
 }
 
