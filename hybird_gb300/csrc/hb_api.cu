@@ -281,7 +281,7 @@ int hb_destroy(hb_ctx* c) {
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
                     c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
                     c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix, c->fs_ilist,
-                    c->curved_list, c->curved_cnt, c->d.cyl_of};
+                    c->curved_list, c->curved_cnt, c->d.cyl_of, c->io_terms};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -451,7 +451,10 @@ constexpr int STAGE_DOUBLES_PER_ELEMENT = 35;
 struct GatherArgs {
     const double* src[11];
     long long off[12];
-    int n;
+    int hsum[11];  // >= 0: the field is the element sums' component hsum.. (FHydro 0, MHydro 3,
+                   // fluidVolume 6) converted from the fixed-point accumulators on the fly
+    int n, E;
+    const unsigned long long* hacc;
 };
 
 __global__ void k_gather(GatherArgs g, double* dst) {
@@ -459,7 +462,20 @@ __global__ void k_gather(GatherArgs g, double* dst) {
     if (t >= g.off[g.n]) return;
     int k = 0;
     while (k + 1 < g.n && t >= g.off[k + 1]) ++k;
-    dst[t] = g.src[k][t - g.off[k]];
+    const long long r = t - g.off[k];
+    if (g.hsum[k] >= 0) {  // (r / E) selects the component, as in convert_sums
+        const long long comp = r / g.E, p = r - comp * g.E;
+        dst[t] = (double)(long long)g.hacc[(g.hsum[k] + comp) * g.E + p] * HACC_INV;
+    } else {
+        dst[t] = g.src[k][r];
+    }
+}
+
+// lbF and its FP32 copy from kernel arguments (stream-ordered, no host staging)
+__global__ void k_set_force(double* f, double fx, double fy, double fz) {
+    f[0] = fx; f[1] = fy; f[2] = fz;
+    float* ff = reinterpret_cast<float*>(f + 3);
+    ff[0] = (float)fx; ff[1] = (float)fy; ff[2] = (float)fz; ff[3] = 0.0f;
 }
 }  // namespace hb
 
@@ -540,15 +556,7 @@ int hb_get_params(hb_ctx* c, hb_params* out, int32_t* elements, int32_t* objects
 int hb_set_body_force(hb_ctx* c, const double* force) {
     if (!c || !force || !c->initialized) return seterr(HB_ERR_ARG, "null argument or not initialised");
     for (int k = 0; k < 3; ++k) c->P.lbF[k] = force[k];
-    if (c->P.force_field) {
-        // one copy of the FP64 force and its FP32 copy; a copy from pageable memory is
-        // staged before cudaMemcpyAsync returns, so the local block may go out of scope
-        double blk[5];
-        float* ff = reinterpret_cast<float*>(blk + 3);
-        for (int k = 0; k < 3; ++k) { blk[k] = force[k]; ff[k] = (float)force[k]; }
-        ff[3] = 0.0f;
-        CK(cudaMemcpyAsync(c->lb_force, blk, sizeof(blk), cudaMemcpyHostToDevice, c->stream));
-    }
+    if (c->P.force_field) hb::k_set_force<<<1, 1, 0, c->stream>>>(c->lb_force, force[0], force[1], force[2]);
     return HB_OK;
 }
 
@@ -611,20 +619,28 @@ int hb_download_elements(hb_ctx* c, double* x0, double* x1, double* w, double* q
     // Everything is queued on the context stream behind the steps already issued: the
     // element-force conversion of the last lattice step (LB.cpp:1851-1919), one gather of
     // the requested fields into a device staging block, one copy into pinned host memory.
-    if (c->reduce_pending) launch_couple_reduce(c);
-    struct { double* dst; double* src; int comps; } items[] = {
-        {x0, c->d.x[0], 3}, {x1, c->d.x[1], 3}, {w, c->d.wG, 3}, {q0, c->d.q[0], 4}, {fhydro, c->d.FH, 3},
-        {mhydro, c->d.MH, 3}, {fparticle, c->d.FP, 3}, {fwall, c->d.FW, 3}, {mparticle, c->d.MP, 3},
-        {mwall, c->d.MW, 3}, {fluid_volume, c->d.fvol, 1}};
+    // With the FP32/FP16 lattice the element sums are read from their fixed-point
+    // accumulators inside the gather (the next cycle converts them itself); the FP64 form
+    // reduces them first.
+    const bool inline_sums = c->reduce_pending && c->hacc;
+    if (c->reduce_pending && !c->hacc) launch_couple_reduce(c);
+    struct { double* dst; double* src; int comps; int hsum; } items[] = {
+        {x0, c->d.x[0], 3, -1}, {x1, c->d.x[1], 3, -1}, {w, c->d.wG, 3, -1}, {q0, c->d.q[0], 4, -1},
+        {fhydro, c->d.FH, 3, inline_sums ? 0 : -1}, {mhydro, c->d.MH, 3, inline_sums ? 3 : -1},
+        {fparticle, c->d.FP, 3, -1}, {fwall, c->d.FW, 3, -1}, {mparticle, c->d.MP, 3, -1},
+        {mwall, c->d.MW, 3, -1}, {fluid_volume, c->d.fvol, 1, inline_sums ? 6 : -1}};
     if (!c->d_stage) {
         int rc = dalloc(&c->d_stage, (size_t)hb::STAGE_DOUBLES_PER_ELEMENT * E);
         if (rc) return rc;
         CK(cudaMallocHost((void**)&c->h_stage, sizeof(double) * hb::STAGE_DOUBLES_PER_ELEMENT * E));
     }
     hb::GatherArgs g = {};
+    g.E = E;
+    g.hacc = c->hacc;
     for (auto& it : items)
         if (it.dst) {
             g.src[g.n] = it.src;
+            g.hsum[g.n] = it.hsum;
             g.off[g.n + 1] = g.off[g.n] + (long long)it.comps * E;
             ++g.n;
         }

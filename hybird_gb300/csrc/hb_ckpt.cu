@@ -241,11 +241,13 @@ int hb_checkpoint_load(const char* path, hb_ctx** out) {
     c->steps = h.steps;
     c->reduce_pending = h.reduce_pending != 0;
     c->dem_stepped = h.dem_stepped != 0;
-    if (c->io_linked) {  // output-mirror marks are rebuilt from the restored types on demand
+    if (c->io_part) {  // output-mirror marks are rebuilt from the restored types on demand
         cudaFree(c->io_linked);
         cudaFree(c->io_part);
+        cudaFree(c->io_terms);
         c->io_linked = nullptr;
         c->io_part = nullptr;
+        c->io_terms = nullptr;
     }
     *out = c;
     return HB_OK;

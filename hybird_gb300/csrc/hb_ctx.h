@@ -106,6 +106,7 @@ struct hb_ctx {
     float* lb_force_f = nullptr;    // = (float*)(lb_force + 3), not a separate allocation
     uint8_t* io_linked = nullptr;   // [N] output mirror: wall nodes that own a node object
     void* io_part = nullptr;        // output mirror: per-block partials + result block
+    double* io_terms = nullptr;     // output mirror: per-element terms [7E]
     double* d_stage = nullptr;      // device staging of element downloads (35 E doubles)
     double* h_stage = nullptr;      // pinned host staging of element downloads (35 E doubles)
     // free surface

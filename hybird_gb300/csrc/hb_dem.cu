@@ -1381,38 +1381,55 @@ void launch_couple(hb_ctx* c, bool build, cudaEvent_t* ev) {
 // objects in index order within a particle).  One thread per wall or object replays the
 // records in that order, so the FP64 sums are the reference's own.
 __global__ void k_reactions(DemArgs a, double* react) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    // one warp per wall or object: the lanes scan 32 elements at a time for contacts
+    // (rare), then the contacts are added in element order (and slot order within an
+    // element) by the whole warp in lockstep
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (t >= a.nw + a.O) return;
+    const bool wall = t < a.nw;
+    const int o = t - a.nw;
     V F{0, 0, 0};
-    if (t < a.nw) {
-        for (int i = 0; i < a.E; ++i) {
-            if (a.wall_of[i] != t) continue;
-            const double* r = a.wrec + 7 * (long long)i;
-            if (r[0] == 0.0) continue;
-            F = sub(F, V{r[1], r[2], r[3]});
-            if (r[0] == 2.0) F = add(F, V{r[4], r[5], r[6]});
-        }
-        react[3 * t] = F.x; react[3 * t + 1] = F.y; react[3 * t + 2] = F.z;
-    } else {
-        const int o = t - a.nw;
-        for (int i = 0; i < a.E; ++i) {
-            const int oc = a.obj_cnt[i];
-            for (int k = 0; k < oc; ++k) {
-                if (a.obj[(long long)i * OBJ_CAP + k] != o) continue;
-                const double* r = a.orec + 7 * ((long long)i * OBJ_CAP + k);
-                if (r[0] == 0.0) continue;
-                F = sub(F, V{r[1], r[2], r[3]});
-                if (r[0] == 2.0) F = add(F, V{r[4], r[5], r[6]});
+    for (int base = 0; base < a.E; base += 32) {
+        const int i = base + lane;
+        bool hit = false;
+        if (i < a.E) {
+            if (wall) {
+                hit = a.wall_of[i] == t && a.wrec[7 * (long long)i] != 0.0;
+            } else {
+                const int oc = a.obj_cnt[i];
+                for (int k = 0; k < oc && !hit; ++k)
+                    hit = a.obj[(long long)i * OBJ_CAP + k] == o && a.orec[7 * ((long long)i * OBJ_CAP + k)] != 0.0;
             }
         }
-        double* dst = react + 3 * (MAX_WALLS + o);
-        dst[0] = F.x; dst[1] = F.y; dst[2] = F.z;
+        unsigned m = __ballot_sync(0xffffffffu, hit);
+        while (m) {
+            const int e = base + __ffs(m) - 1;
+            m &= m - 1;
+            if (wall) {
+                const double* r = a.wrec + 7 * (long long)e;
+                F = sub(F, V{r[1], r[2], r[3]});
+                if (r[0] == 2.0) F = add(F, V{r[4], r[5], r[6]});
+            } else {
+                const int oc = a.obj_cnt[e];
+                for (int k = 0; k < oc; ++k) {
+                    if (a.obj[(long long)e * OBJ_CAP + k] != o) continue;
+                    const double* r = a.orec + 7 * ((long long)e * OBJ_CAP + k);
+                    if (r[0] == 0.0) continue;
+                    F = sub(F, V{r[1], r[2], r[3]});
+                    if (r[0] == 2.0) F = add(F, V{r[4], r[5], r[6]});
+                }
+            }
+        }
     }
+    if (lane != 0) return;
+    double* dst = wall ? react + 3 * t : react + 3 * (MAX_WALLS + o);
+    dst[0] = F.x; dst[1] = F.y; dst[2] = F.z;
 }
 
 void launch_reactions(hb_ctx* c) {
     if (c->d.E == 0 || !c->d.react) return;
-    k_reactions<<<ceil_div(c->d.nw + c->d.O, 64), 64, 0, c->stream>>>(dem_args(c), c->d.react);
+    k_reactions<<<ceil_div(c->d.nw + c->d.O, 2), 64, 0, c->stream>>>(dem_args(c), c->d.react);
 }
 
 void launch_couple_reduce(hb_ctx* c) {

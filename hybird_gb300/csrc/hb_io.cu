@@ -172,9 +172,54 @@ enum IoSlot {
 
 __device__ __forceinline__ double n2(double x, double y, double z) { return x * x + y * y + z * z; }
 
-// One thread: the block partials in block order, then the element quantities in element
-// order exactly as IO.cpp:853-876, 1001-1010, 1064-1106 and DEM.cpp:2226-2276 write them.
-__global__ void k_io_final(const NodePart* part, int nparts, IoElem e, double* out) {
+// Element terms of IO.cpp:853-876, 1001-1010, 1064-1106 and DEM.cpp:2226-2276, one thread
+// per element (the sums over elements are formed afterwards in element order):
+// [0] |FParticle| [1] |FWall| [2] |FHydro| [3] m [4] 0.5 m |x1|^2 [5] I.(wL*wL) [6] m h |g|
+constexpr int IO_TERMS = 7;
+__global__ void k_io_terms(IoElem e, double* terms, double* maxima) {
+    const int E = e.E;
+    const double gn = sqrt(n2(e.demF[0], e.demF[1], e.demF[2]));
+    double zn[3] = {0.0, 0.0, 0.0}, zp[3] = {0.0, 0.0, 0.0};
+    if (gn != 0.0) {  // reference plane of the gravitational energy (DEM.cpp:2248-2264)
+        for (int k = 0; k < 3; ++k) zn[k] = -1.0 * e.demF[k] / gn;
+        for (int k = 0; k < 3; ++k)
+            if (zn[k] < 0) zp[k] += e.size[k];
+    }
+    double pmax = 0.0, wmax = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < E; i += gridDim.x * blockDim.x) {
+        const double vx = e.x1[i], vy = e.x1[E + i], vz = e.x1[2 * E + i];
+        pmax = fmax(pmax, n2(vx, vy, vz));
+        wmax = fmax(wmax, n2(e.wG[i], e.wG[E + i], e.wG[2 * E + i]));
+        double* t = terms + (long long)IO_TERMS * i;
+        t[0] = sqrt(n2(e.FP[i], e.FP[E + i], e.FP[2 * E + i]));
+        t[1] = sqrt(n2(e.FW[i], e.FW[E + i], e.FW[2 * E + i]));
+        t[2] = sqrt(n2(e.FH[i], e.FH[E + i], e.FH[2 * E + i]));
+        t[3] = e.m[i];
+        t[4] = 0.5 * e.m[i] * n2(vx, vy, vz);
+        const double wx = e.wL[i], wy = e.wL[E + i], wz = e.wL[2 * E + i];
+        t[5] = e.I[i] * (wx * wx) + e.I[E + i] * (wy * wy) + e.I[2 * E + i] * (wz * wz);
+        t[6] = 0.0;
+        if (gn != 0.0) {
+            const double h = zn[0] * (e.x0[i] - zp[0]) + zn[1] * (e.x0[E + i] - zp[1]) + zn[2] * (e.x0[2 * E + i] - zp[2]);
+            t[6] = e.m[i] * h * gn;
+        }
+    }
+    // maxima are order-independent: warp shuffles, then 64-bit atomicMax on the bit patterns
+    // of the non-negative values
+    for (int off = 16; off > 0; off >>= 1) {
+        pmax = fmax(pmax, __shfl_xor_sync(0xffffffffu, pmax, off));
+        wmax = fmax(wmax, __shfl_xor_sync(0xffffffffu, wmax, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(reinterpret_cast<unsigned long long*>(maxima), (unsigned long long)__double_as_longlong(pmax));
+        atomicMax(reinterpret_cast<unsigned long long*>(maxima + 1), (unsigned long long)__double_as_longlong(wmax));
+    }
+}
+
+// One thread: the block partials in block order, then the element sums in element order
+// (the reference's own accumulation order; the terms come from k_io_terms).
+__global__ void k_io_final(const NodePart* part, int nparts, IoElem e, const double* terms, const double* maxima,
+                           double* out) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double mx = 0.0, ms = 0.0;
     long long act = 0, pl = 0;
@@ -185,30 +230,16 @@ __global__ void k_io_final(const NodePart* part, int nparts, IoElem e, double* o
         pl += part[b].plastic;
     }
     out[S_MAXU2] = mx; out[S_FMASS] = ms; out[S_ACTIVE] = (double)act; out[S_PLASTIC] = (double)pl;
-    const int E = e.E;
-    double pmax = 0.0, wmax = 0.0, coll = 0.0, hydr = 0.0, pmass = 0.0, tKin = 0.0, rKin = 0.0, g = 0.0;
-    const double gn = sqrt(n2(e.demF[0], e.demF[1], e.demF[2]));
-    double zn[3] = {0.0, 0.0, 0.0}, zp[3] = {0.0, 0.0, 0.0};
-    if (gn != 0.0) {  // reference plane of the gravitational energy (DEM.cpp:2248-2264)
-        for (int k = 0; k < 3; ++k) zn[k] = -1.0 * e.demF[k] / gn;
-        for (int k = 0; k < 3; ++k)
-            if (zn[k] < 0) zp[k] += e.size[k];
-    }
-    for (int i = 0; i < E; ++i) {
-        const double vx = e.x1[i], vy = e.x1[E + i], vz = e.x1[2 * E + i];
-        pmax = fmax(pmax, n2(vx, vy, vz));
-        wmax = fmax(wmax, n2(e.wG[i], e.wG[E + i], e.wG[2 * E + i]));
-        coll += sqrt(n2(e.FP[i], e.FP[E + i], e.FP[2 * E + i]));
-        coll += sqrt(n2(e.FW[i], e.FW[E + i], e.FW[2 * E + i]));
-        hydr += sqrt(n2(e.FH[i], e.FH[E + i], e.FH[2 * E + i]));
-        pmass += e.m[i];
-        tKin += 0.5 * e.m[i] * n2(vx, vy, vz);
-        const double wx = e.wL[i], wy = e.wL[E + i], wz = e.wL[2 * E + i];
-        rKin += e.I[i] * (wx * wx) + e.I[E + i] * (wy * wy) + e.I[2 * E + i] * (wz * wz);
-        if (gn != 0.0) {
-            const double h = zn[0] * (e.x0[i] - zp[0]) + zn[1] * (e.x0[E + i] - zp[1]) + zn[2] * (e.x0[2 * E + i] - zp[2]);
-            g += e.m[i] * h * gn;
-        }
+    double coll = 0.0, hydr = 0.0, pmass = 0.0, tKin = 0.0, rKin = 0.0, g = 0.0;
+    for (int i = 0; i < e.E; ++i) {
+        const double* t = terms + (long long)IO_TERMS * i;
+        coll += t[0];
+        coll += t[1];
+        hydr += t[2];
+        pmass += t[3];
+        tKin += t[4];
+        rKin += t[5];
+        g += t[6];
     }
     double ox = 0.0, oy = 0.0, oz = 0.0;  // IO::totForceObject (IO.cpp:1097-1106)
     if (e.react)
@@ -216,7 +247,9 @@ __global__ void k_io_final(const NodePart* part, int nparts, IoElem e, double* o
             const double* f = e.react + 3 * (MAX_WALLS + o);
             ox += f[0]; oy += f[1]; oz += f[2];
         }
-    out[S_PMAX2] = pmax; out[S_WMAX2] = wmax; out[S_COLL] = coll; out[S_HYDR] = hydr; out[S_PMASS] = pmass;
+    out[S_PMAX2] = e.E ? maxima[0] : 0.0;
+    out[S_WMAX2] = e.E ? maxima[1] : 0.0;
+    out[S_COLL] = coll; out[S_HYDR] = hydr; out[S_PMASS] = pmass;
     out[S_OBJX] = ox; out[S_OBJY] = oy; out[S_OBJZ] = oz;
     out[S_TRKIN] = tKin; out[S_ROTKIN] = rKin; out[S_GRAV] = g;
 }
@@ -235,7 +268,9 @@ static IoArgs io_args(hb_ctx* c) {
 
 int io_prepare(hb_ctx* c) {
     if (c->io_part) return 0;
-    if (cudaMalloc(&c->io_part, sizeof(NodePart) * IO_BLOCKS + sizeof(double) * S_COUNT) != cudaSuccess) return -1;
+    if (cudaMalloc(&c->io_part, sizeof(NodePart) * IO_BLOCKS + sizeof(double) * (S_COUNT + 2)) != cudaSuccess)
+        return -1;
+    if (c->d.E > 0 && cudaMalloc(&c->io_terms, sizeof(double) * IO_TERMS * c->d.E) != cudaSuccess) return -1;
     if (!c->P.lb_solve || !c->ntype) return 0;  // DEM only: no lattice nodes
     if (cudaMalloc(&c->io_linked, (size_t)c->N) != cudaSuccess) return -1;
     cudaMemsetAsync(c->io_linked, 0, (size_t)c->N, c->stream);
@@ -270,7 +305,10 @@ double* launch_io_export(hb_ctx* c) {
         e.demF[k] = c->P.lbF[k];  // DEM.cpp:194
         e.size[k] = double(c->P.lb_size[k]) * 1.0;
     }
-    k_io_final<<<1, 32, 0, c->stream>>>(part, IO_BLOCKS, e, out);
+    double* maxima = out + S_COUNT;
+    cudaMemsetAsync(maxima, 0, 2 * sizeof(double), c->stream);
+    if (d.E > 0) k_io_terms<<<(unsigned)ceil_div(d.E, 256), 256, 0, c->stream>>>(e, c->io_terms, maxima);
+    k_io_final<<<1, 32, 0, c->stream>>>(part, IO_BLOCKS, e, c->io_terms, maxima, out);
     return out;
 }
 
