@@ -107,24 +107,53 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     d.dampCoeff = -1.0 * std::sqrt(2.0) * std::log(re) / std::sqrt((std::log(re) * std::log(re) + M_PI));
     d.knConst = 2.0 / 3.0 * P.young_mod / (1 - P.poisson * P.poisson);
     d.ksConst = 2.0 * P.young_mod / (2.0 - P.poisson) / (1.0 + P.poisson);
-    // objects
-    d.O = o ? o->count : 0;
-    if (d.O > 0) {
+    // objects (host copies: periodic images are appended once nebrRange is known)
+    const int O0 = o ? o->count : 0;
+    std::vector<double> ox(3 * (size_t)O0), ov(3 * (size_t)O0, 0.0), orr(O0);
+    for (int k = 0; k < O0; ++k) {
+        for (int q = 0; q < 3; ++q) {
+            ox[3 * k + q] = o->x0[(size_t)q * O0 + k];
+            if (o->x1) ov[3 * k + q] = o->x1[(size_t)q * O0 + k];
+        }
+        orr[k] = o->radius[k];
+    }
+    d.O_std = O0;
+    auto upload_objects = [&]() -> int {
+        d.O = (int)orr.size();
+        if (d.O == 0) return HB_OK;
         int rc;
         if ((rc = dalloc(&d.obj_x0, 3 * d.O)) || (rc = dalloc(&d.obj_x1, 3 * d.O)) || (rc = dalloc(&d.obj_r, d.O))) return rc;
-        CK(cudaMemcpy(d.obj_x0, o->x0, sizeof(double) * 3 * d.O, cudaMemcpyHostToDevice));
-        std::vector<double> z(3 * d.O, 0.0);
-        CK(cudaMemcpy(d.obj_x1, o->x1 ? o->x1 : z.data(), sizeof(double) * 3 * d.O, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.obj_r, o->radius, sizeof(double) * d.O, cudaMemcpyHostToDevice));
-    }
+        std::vector<double> a(3 * (size_t)d.O), v(3 * (size_t)d.O);
+        for (int k = 0; k < d.O; ++k)
+            for (int q = 0; q < 3; ++q) {
+                a[(size_t)q * d.O + k] = ox[3 * k + q];
+                v[(size_t)q * d.O + k] = ov[3 * k + q];
+            }
+        CK(cudaMemcpy(d.obj_x0, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.obj_x1, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.obj_r, orr.data(), sizeof(double) * d.O, cudaMemcpyHostToDevice));
+        return HB_OK;
+    };
     const int E = (P.dem_solve && e) ? e->count : 0;
     d.E = E;
     d.multi = E ? P.multi_step : 1;
     d.dt = E ? 1.0 / double(P.multi_step) : 1.0;
-    if (E == 0) return HB_OK;
-    for (int k = 0; k < 6; ++k)
-        if (P.boundary[k] == HB_T_PERIODIC)
-            return seterr(HB_ERR_UNSUPPORTED, "moving particles with periodic boundaries (ghost particles) are not implemented");
+    if (E == 0) return upload_objects();
+    // periodic face pairs (DEM::initializePbcs, DEM.cpp:937-989), lattice units
+    d.npbc = 0;
+    {
+        const int L[3] = {c->X, c->Y, c->Z};
+        for (int k = 0; k < 3; ++k) {
+            const bool lo = P.boundary[2 * k] == HB_T_PERIODIC, hi = P.boundary[2 * k + 1] == HB_T_PERIODIC;
+            if (lo != hi) return seterr(HB_ERR_UNSUPPORTED, "periodic boundary on one face of axis %d only", k);
+            if (!lo) continue;
+            for (int q = 0; q < 3; ++q) {
+                d.pbc_p[d.npbc][q] = q == k ? 0.5 : 0.0;
+                d.pbc_v[d.npbc][q] = q == k ? double(L[k]) - 2.0 : 0.0;
+            }
+            ++d.npbc;
+        }
+    }
     // element fields, one allocation (elmt.h:53-135)
     const int nfields = DEM_FIELDS;
     int rc;
@@ -196,8 +225,67 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     d.nebrRange = std::max(maxRad * 3.0, 0.5 * std::min(d.cellWidth[0], std::min(d.cellWidth[1], d.cellWidth[2])));
     d.trigger = 0.25 * d.nebrRange;
     d.ncells = d.nCells[0] * d.nCells[1] * d.nCells[2];
-    if ((rc = dalloc(&d.cell_of, E)) || (rc = dalloc(&d.cell_cnt, d.ncells)) || (rc = dalloc(&d.cell_start, d.ncells + 1)) ||
-        (rc = dalloc(&d.cell_fill, d.ncells)) || (rc = dalloc(&d.cell_items, E)) ||
+    if (d.npbc) {
+        // periodicObjects (DEM.cpp:990-1063): an object within 2 nebrRange of a face (pl1
+        // tested first) gets one image per face pair, then one per two images of the same
+        // object, appended after the uploaded objects
+        std::vector<int> gi;
+        std::vector<double> gv;
+        for (int b = 0; b < d.npbc; ++b) {
+            const double* v = d.pbc_v[b];
+            const double nv = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            const double n1[3] = {v[0] / nv, v[1] / nv, v[2] / nv};
+            for (int k = 0; k < O0; ++k) {
+                const double* x = &ox[3 * k];
+                const double ld = n1[0] * (x[0] - d.pbc_p[b][0]) + n1[1] * (x[1] - d.pbc_p[b][1]) + n1[2] * (x[2] - d.pbc_p[b][2]);
+                const double rd = (-1.0 * n1[0]) * (x[0] - (d.pbc_p[b][0] + v[0])) + (-1.0 * n1[1]) * (x[1] - (d.pbc_p[b][1] + v[1])) +
+                                  (-1.0 * n1[2]) * (x[2] - (d.pbc_p[b][2] + v[2]));
+                if (ld < 2.0 * d.nebrRange && ld > 0.0) {
+                    gi.push_back(k);
+                    for (int q = 0; q < 3; ++q) gv.push_back(v[q]);
+                } else if (rd < 2.0 * d.nebrRange && rd > 0.0) {
+                    gi.push_back(k);
+                    for (int q = 0; q < 3; ++q) gv.push_back(-1.0 * v[q]);
+                }
+            }
+        }
+        const size_t ns = gi.size();
+        for (size_t g1 = 0; g1 < ns; ++g1)
+            for (size_t g2 = g1 + 1; g2 < ns; ++g2)
+                if (gi[g1] == gi[g2]) {
+                    gi.push_back(gi[g1]);
+                    for (int q = 0; q < 3; ++q) gv.push_back(gv[3 * g1 + q] + gv[3 * g2 + q]);
+                }
+        for (size_t g = 0; g < gi.size(); ++g) {
+            for (int q = 0; q < 3; ++q) {
+                ox.push_back(ox[3 * gi[g] + q] + gv[3 * g + q]);
+                ov.push_back(ov[3 * gi[g] + q]);
+            }
+            orr.push_back(orr[gi[g]]);
+        }
+        // ghost particles: at most one per face pair and one per two of those per element
+        d.gcap = 6 * E;
+        if ((rc = dalloc(&d.gmeta, 2)) || (rc = dalloc(&d.gorig, d.gcap)) || (rc = dalloc(&d.gvec, 3 * (size_t)d.gcap)) ||
+            (rc = dalloc(&d.comp, 6 * (size_t)E)) || (rc = dalloc(&d.ccnt, E)) ||
+            (rc = dalloc(&d.px, 3 * ((size_t)E + d.gcap))))
+            return rc;
+        CK(cudaMemset(d.gmeta, 0, sizeof(int) * 2));
+        CK(cudaMemset(d.gorig, 0, sizeof(int) * d.gcap));
+        CK(cudaMemset(d.gvec, 0, sizeof(double) * 3 * d.gcap));
+        CK(cudaMemset(d.comp, 0, sizeof(int) * 6 * E));
+        CK(cudaMemset(d.ccnt, 0, sizeof(int) * E));
+        // ghost entries of the FP32 particle copy follow the elements'
+        float* pf2 = nullptr;
+        if ((rc = dalloc(&pf2, 12 * ((size_t)E + d.gcap)))) return rc;
+        CK(cudaMemset(pf2, 0, sizeof(float) * 12 * ((size_t)E + d.gcap)));
+        CK(cudaMemcpy(pf2, d.pf, sizeof(float) * 12 * (size_t)E, cudaMemcpyDeviceToDevice));
+        cudaFree(d.pf);
+        d.pf = pf2;
+    }
+    if ((rc = upload_objects())) return rc;
+    const size_t S = (size_t)E + d.gcap;
+    if ((rc = dalloc(&d.cell_of, S)) || (rc = dalloc(&d.cell_cnt, d.ncells)) || (rc = dalloc(&d.cell_start, d.ncells + 1)) ||
+        (rc = dalloc(&d.cell_fill, d.ncells)) || (rc = dalloc(&d.cell_items, S)) ||
         (rc = dalloc(&d.nbr, (size_t)E * NBR_CAP)) || (rc = dalloc(&d.nbr_cnt, E)) || (rc = dalloc(&d.wall_of, E)) ||
         (rc = dalloc(&d.obj, (size_t)E * OBJ_CAP)) || (rc = dalloc(&d.obj_cnt, E)) || (rc = dalloc(&d.scal, 8)) ||
         (rc = dalloc(&d.contacts, 1)) || (rc = dalloc(&d.partial, hb::PARTIAL_CAP)) || (rc = dalloc(&d.done, 1)) ||
@@ -281,7 +369,8 @@ int hb_destroy(hb_ctx* c) {
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
                     c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
                     c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix, c->fs_ilist,
-                    c->curved_list, c->curved_cnt, c->d.cyl_of, c->io_terms};
+                    c->curved_list, c->curved_cnt, c->d.cyl_of, c->io_terms, c->d.gmeta, c->d.gorig, c->d.gvec,
+                    c->d.comp, c->d.ccnt, c->d.px, c->d.remark};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -332,8 +421,12 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         }
         if (!c->d.claim_list && (rc = dalloc(&c->d.claim_list, 2 * N))) return rc;
         if (!c->d.claim_cnt && (rc = dalloc(&c->d.claim_cnt, 1))) return rc;
-        if (!c->d.boxes && (rc = dalloc((uint8_t**)&c->d.boxes, (size_t)c->d.E * 128))) return rc;
+        if (!c->d.boxes && (rc = dalloc((uint8_t**)&c->d.boxes, ((size_t)c->d.E + c->d.gcap) * 128))) return rc;
         CK(cudaMemset(c->d.claim_cnt, 0, sizeof(int)));
+        if (c->d.npbc && c->P.lb_solve && !c->d.remark) {
+            if ((rc = dalloc(&c->d.remark, N))) return rc;
+            CK(cudaMemset(c->d.remark, 0, sizeof(uint32_t) * N));
+        }
     }
     if (!c->wall_part) {
         const long long grid = (long long)ceil_div(c->X, c->X <= 64 ? 64 : (c->X <= 128 ? 128 : 256)) * (c->Y - 2) * (c->Z - 2);
@@ -360,6 +453,7 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     c->reduce_pending = false;
     c->steps = 0;
     c->dem_stepped = false;
+    if (launch_ghosts_init(c)) return seterr(HB_ERR_CUDA, "ghost particles: %s", cudaGetErrorString(cudaGetLastError()));
     if (launch_init_lattice(c, e && c->d.E ? c->d.x[0] : nullptr, c->d.E ? c->d.rad : nullptr, c->d.E,
                             c->d.obj_x0, c->d.obj_r, c->d.O))
         return seterr(HB_ERR_CUDA, "lattice init: %s", cudaGetErrorString(cudaGetLastError()));
@@ -677,6 +771,26 @@ int hb_download_pairs(hb_ctx* c, uint32_t* pairs, int64_t capacity, int64_t* cou
     const int64_t np = (int64_t)out.size() / 2;
     if (count) *count = np;
     if (pairs) memcpy(pairs, out.data(), sizeof(uint32_t) * 2 * std::min(np, capacity));
+    return HB_OK;
+}
+
+int hb_download_ghosts(hb_ctx* c, uint32_t* origin, double* shift, int64_t capacity, int64_t* count) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    CK(cudaStreamSynchronize(c->stream));
+    int G = 0;
+    if (c->d.npbc && c->d.E) CK(cudaMemcpy(&G, c->d.gmeta, sizeof(int), cudaMemcpyDeviceToHost));
+    if (count) *count = G;
+    const int64_t n = std::min<int64_t>(G, capacity);
+    if (n <= 0) return HB_OK;
+    std::vector<int> o(n);
+    std::vector<double> v(3 * (size_t)c->d.gcap);
+    CK(cudaMemcpy(o.data(), c->d.gorig, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(v.data(), c->d.gvec, sizeof(double) * v.size(), cudaMemcpyDeviceToHost));
+    for (int64_t g = 0; g < n; ++g) {
+        if (origin) origin[g] = (uint32_t)o[g];
+        if (shift)
+            for (int q = 0; q < 3; ++q) shift[3 * g + q] = v[(size_t)q * c->d.gcap + g];
+    }
     return HB_OK;
 }
 

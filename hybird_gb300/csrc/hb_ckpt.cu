@@ -79,13 +79,22 @@ std::vector<Buf> state_buffers(hb_ctx* c) {
     if (E) {
         add("hacc", c->hacc, 8 * 7 * E);
         add("dem_base", d.base, 8 * (size_t)DEM_FIELDS * E);
-        add("dem_pf", d.pf, 4 * 12 * E);
+        const size_t S = E + (size_t)d.gcap;
+        add("dem_pf", d.pf, 4 * 12 * S);
         add("dem_plain", d.plain, 4 * E);
-        add("cell_of", d.cell_of, 4 * E);
+        add("cell_of", d.cell_of, 4 * S);
         add("cell_cnt", d.cell_cnt, 4 * (size_t)d.ncells);
         add("cell_start", d.cell_start, 4 * ((size_t)d.ncells + 1));
         add("cell_fill", d.cell_fill, 4 * (size_t)d.ncells);
-        add("cell_items", d.cell_items, 4 * E);
+        add("cell_items", d.cell_items, 4 * S);
+        if (d.npbc) {  // ghost particles of the last rebuild
+            add("ghost_meta", d.gmeta, 2 * sizeof(int));
+            add("ghost_orig", d.gorig, 4 * (size_t)d.gcap);
+            add("ghost_vec", d.gvec, 8 * 3 * (size_t)d.gcap);
+            add("ghost_comp", d.comp, 4 * 6 * E);
+            add("ghost_ccnt", d.ccnt, 4 * E);
+            add("ghost_px", d.px, 8 * 3 * S);
+        }
         add("nbr", d.nbr, 4 * E * hb::NBR_CAP);
         add("nbr_cnt", d.nbr_cnt, 4 * E);
         add("wall_of", d.wall_of, 4 * E);
@@ -129,7 +138,7 @@ int hb_checkpoint_save(hb_ctx* c, const char* path) {
     f.write(reinterpret_cast<const char*>(&ps), 4);
     f.write(reinterpret_cast<const char*>(&c->P), ps);
     Header h = {};
-    h.N = c->N; h.E = c->d.E; h.O = c->d.O; h.steps = c->steps; h.cur = c->cur;
+    h.N = c->N; h.E = c->d.E; h.O = c->d.O_std; h.steps = c->steps; h.cur = c->cur;
     h.reduce_pending = c->reduce_pending; h.dem_stepped = c->dem_stepped;
     f.write(reinterpret_cast<const char*>(&h), sizeof(h));
     {  // the cylinders (host data: they define the curved walls the loader rebuilds)
@@ -204,11 +213,22 @@ int hb_checkpoint_load(const char* path, hb_ctx** out) {
         el.count = E;
         el.radius = rad.data(); el.x0 = x0.data(); el.x1 = x1.data(); el.w0 = w0.data(); el.q0 = q0.data();
     }
+    int Ot = 0;  // objects including the periodic images the loader's init appends again
     if (O > 0) {
         const std::vector<char>* a = find("obj_x0"), *v = find("obj_x1"), *r = find("obj_r");
         if (!a || !v || !r) return err(HB_ERR_ARG, "checkpoint lacks the objects");
-        ox0.assign(reinterpret_cast<const double*>(a->data()), reinterpret_cast<const double*>(a->data()) + 3 * O);
-        ox1.assign(reinterpret_cast<const double*>(v->data()), reinterpret_cast<const double*>(v->data()) + 3 * O);
+        Ot = (int)(r->size() / sizeof(double));
+        if (Ot < O || a->size() != 24 * (size_t)Ot || v->size() != 24 * (size_t)Ot)
+            return err(HB_ERR_ARG, "checkpoint object records of another size");
+        const double* pa = reinterpret_cast<const double*>(a->data());
+        const double* pv = reinterpret_cast<const double*>(v->data());
+        ox0.resize(3 * (size_t)O);
+        ox1.resize(3 * (size_t)O);
+        for (int q = 0; q < 3; ++q)
+            for (int k = 0; k < O; ++k) {
+                ox0[(size_t)q * O + k] = pa[(size_t)q * Ot + k];
+                ox1[(size_t)q * O + k] = pv[(size_t)q * Ot + k];
+            }
         orad.assign(reinterpret_cast<const double*>(r->data()), reinterpret_cast<const double*>(r->data()) + O);
         ob.count = O; ob.radius = orad.data(); ob.x0 = ox0.data(); ob.x1 = ox1.data();
     }
@@ -222,7 +242,7 @@ int hb_checkpoint_load(const char* path, hb_ctx** out) {
     }
     rc = hb_init(c, E > 0 ? &el : nullptr, O > 0 ? &ob : nullptr);
     if (rc) { hb_destroy(c); return rc; }
-    if (c->N != h.N || c->d.E != E || c->d.O != O) {
+    if (c->N != h.N || c->d.E != E || c->d.O != Ot) {
         hb_destroy(c);
         return err(HB_ERR_ARG, "checkpoint sizes do not match the rebuilt context");
     }

@@ -119,7 +119,10 @@ struct Particles {          // DEM elements as the coupling sees them (FP64)
     const double* x1;       // [3*E] velocity
     const double* w;        // [3*E] wGlobal
     const double* radius;   // [E]
-    const float* pf;        // [12*E] FP32 copy per particle: centre, velocity, wGlobal, pad
+    const float* pf;        // [12*(E+gcap)] FP32 copy per particle: centre, velocity, wGlobal, pad
+    const int* gorig;       // [gcap] element of ghost particle E + g (periodic faces), else null
+    const double* gvec;     // [3*gcap] its shift
+    int gcap;
 };
 
 struct LBArgs {

@@ -25,14 +25,14 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     double *wG, *wL, *wpG, *wpL;
     double *FH, *MH, *FP, *FW, *MP, *MW;
     double *fvol, *m, *I, *rad;
-    float* pf = nullptr;        // [12E] FP32 centre/velocity/wGlobal(+pad) per particle for the FP32 lattice kernel
+    float* pf = nullptr;        // [12(E+gcap)] FP32 centre/velocity/wGlobal(+pad) per particle (ghosts after the elements)
     int* plain = nullptr;       // [E] 1: orientation stays the identity (component-parallel Gear)
     // neighbour structures
-    int* cell_of = nullptr;     // [E]
+    int* cell_of = nullptr;     // [E + gcap]
     int* cell_cnt = nullptr;    // [nc]
     int* cell_start = nullptr;  // [nc+1]
     int* cell_fill = nullptr;   // [nc]
-    int* cell_items = nullptr;  // [E]
+    int* cell_items = nullptr;  // [E + gcap]
     int* nbr = nullptr;         // [E*NBR_CAP]
     int* nbr_cnt = nullptr;     // [E]
     int* wall_of = nullptr;     // [E] first wall in range or -1
@@ -44,7 +44,7 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     double* react = nullptr;    // [3*(MAX_WALLS + O)] wall and object FParticle (ordered sums of the records)
     uint32_t* claim_list = nullptr;  // [2N] (node, particle) pairs joined by the coupling in this step
     int* claim_cnt = nullptr;
-    void* boxes = nullptr;      // [E] per-particle spheres of the current step (coupling masks)
+    void* boxes = nullptr;      // [E+gcap] per-particle spheres of the current step (coupling masks)
     void* gargs = nullptr;      // device copy of the DEM/coupling parameter blocks
     double* scal = nullptr;     // device scalars: [0]=maxDisp [1]=rebuild flag [2]=contacts
     int* contacts = nullptr;    // overlapping pairs counter of the last substep
@@ -57,8 +57,20 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     double dt = 1.0;
     int multi = 1;
     double dampCoeff = 0, knConst = 0, ksConst = 0;
+    // periodic faces (DEM.cpp:937-989) and ghost particles (DEM.cpp:1554-1664)
+    int npbc = 0;
+    double pbc_p[3][3], pbc_v[3][3];
+    int gcap = 0;               // ghost slots: 6 per element (3 faces + 3 corners)
+    int* gmeta = nullptr;       // [0] ghosts of the last rebuild, [1] 1: particle nodes need a re-mark
+    int* gorig = nullptr;       // [gcap] element of each ghost
+    double* gvec = nullptr;     // [3*gcap] its shift (component-major, stride gcap)
+    int* comp = nullptr;        // [6E] ghost particle indices (E + g) of each element, in creation order
+    int* ccnt = nullptr;        // [E]
+    double* px = nullptr;       // [3*(E+gcap)] particle centres at the last rebuild (stride E+gcap)
+    uint32_t* remark = nullptr; // [N] last covering particle + 1 during a re-mark (LB.cpp:1826-1849)
     // objects
     int O = 0;
+    int O_std = 0;              // objects as uploaded; the rest are periodic images (DEM.cpp:990-1063)
     double* obj_x0 = nullptr;   // [3*O]
     double* obj_x1 = nullptr;   // [3*O]
     double* obj_r = nullptr;    // [O]
@@ -151,6 +163,7 @@ int launch_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside,
                           const uint32_t* solid, const double* f, const double* n, const double* u,
                           const double* mass, const double* visc);
 int launch_download_lattice(hb_ctx* c, double* f_dev, int which_parity);
+int launch_ghosts_init(hb_ctx* c);
 int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsigned long long* ts = nullptr);
 void launch_couple(hb_ctx* c, bool build_boxes, cudaEvent_t* ev = nullptr);
 void launch_dem_first_predict(hb_ctx* c);

@@ -65,6 +65,12 @@ struct DemArgs {
     double kn, damp, knConst, ksConst, viscTang, muPart, muWall, numVisc, demF[3];
     int* status;
     unsigned long long* total_contacts;
+    // periodic faces: plane pl1 (point pp1, normal pn) and pl2 (point pp1 + v, normal -pn)
+    // of each pair, and the shift v (pbc::setPlanes, utils.cpp:240-245)
+    int npbc, gcap;
+    double pp1[3][3], pp2[3][3], pn1[3][3], pn2[3][3], pv[3][3];
+    int *gmeta, *gorig, *comp, *ccnt;
+    double *gvec, *px;
 };
 
 struct V {
@@ -122,19 +128,35 @@ __device__ double tangential_contact(const DemArgs& a, double vt, double fn, dou
 
 // single CTA: cell of every particle (linearizePosition, vector.cpp:147-149), counting
 // sort into cells, then ascending order inside each cell
+// With periodic faces the table holds the ghosts too (after the elements, positions from
+// the rebuild's px) and a particle's cell is the reference's linear index itself: a ghost
+// above the last y cell row lands in row 0 of the next z slab, as in the reference's cell
+// table, so the half-shell sweep below finds exactly the reference's pairs.  An index
+// outside the table (the reference writes out of bounds there) flags an error.
 __device__ __noinline__ void nl_cells_block(const DemArgs& a) {
     const int E = a.E, nc = a.ncells;
+    const bool per = a.npbc > 0;
+    const int S = per ? E + a.gmeta[0] : E;
+    const long long st = per ? (long long)E + a.gcap : E;
+    const double* pos = per ? a.px : a.x0;
     for (int c = threadIdx.x; c < nc; c += blockDim.x) { a.cell_cnt[c] = 0; a.cell_fill[c] = 0; }
     __syncthreads();
-    for (int i = threadIdx.x; i < E; i += blockDim.x) {
-        const V x = ld3(a.x0, E, i);
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+        const V x{pos[i], pos[st + i], pos[2 * st + i]};
         const int c0 = (int)floor(x.x / a.cw0) + 1, c1 = (int)floor(x.y / a.cw1) + 2, c2 = (int)floor(x.z / a.cw2);
         int c = -1;
-        if (c0 >= 0 && c0 < a.nC0 && c1 >= 0 && c1 < a.nC1 && c2 >= 0 && c2 < a.nC2) c = c0 + a.nC0 * (c1 + a.nC1 * c2);
-        else atomicOr(a.status + 2, 2);  // particle outside the box
+        if (per) {
+            const long long L = c0 + (long long)a.nC0 * (c1 + (long long)a.nC1 * c2);  // vector.cpp:147-149
+            if (L >= 0 && L < nc) c = (int)L;
+        } else if (c0 >= 0 && c0 < a.nC0 && c1 >= 0 && c1 < a.nC1 && c2 >= 0 && c2 < a.nC2) {
+            c = c0 + a.nC0 * (c1 + a.nC1 * c2);
+        }
+        if (c < 0) atomicOr(a.status + 2, 2);  // particle outside the box
         a.cell_of[i] = c;
         if (c >= 0) atomicAdd(a.cell_cnt + c, 1);
     }
+    if (per)
+        for (int i = threadIdx.x; i < E; i += blockDim.x) a.nbr_cnt[i] = 0;
     __syncthreads();
     if (threadIdx.x == 0) {  // exclusive scan (ncells is small: a few thousand)
         int s = 0;
@@ -142,7 +164,7 @@ __device__ __noinline__ void nl_cells_block(const DemArgs& a) {
         a.cell_start[nc] = s;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < E; i += blockDim.x) {
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
         const int c = a.cell_of[i];
         if (c >= 0) a.cell_items[a.cell_start[c] + atomicAdd(a.cell_fill + c, 1)] = i;
     }
@@ -158,8 +180,10 @@ __device__ __noinline__ void nl_cells_block(const DemArgs& a) {
     }
 }
 
+__device__ __noinline__ void nl_near_one(const DemArgs& a, int i);
+
 // candidate list of every particle: all others within nebrRange in the 27 adjacent
-// cells; first wall within range (DEM.cpp:1502-1511); objects within range
+// cells, then the walls, cylinder and objects in range
 __device__ __noinline__ void nl_build_one(const DemArgs& a, int i) {
     const int E = a.E;
     const V xi = ld3(a.x0, E, i);
@@ -187,6 +211,15 @@ __device__ __noinline__ void nl_build_one(const DemArgs& a, int i) {
     }
     if (cnt > NBR_CAP) { atomicOr(a.status + 2, 1); cnt = NBR_CAP; }
     a.nbr_cnt[i] = cnt;
+    nl_near_one(a, i);
+}
+
+// first wall within range (DEM.cpp:1502-1511), first cylinder in range, objects in range
+// (standard particles only, DEM.cpp:1496-1550)
+__device__ __noinline__ void nl_near_one(const DemArgs& a, int i) {
+    const int E = a.E;
+    const V xi = ld3(a.x0, E, i);
+    const double r2 = a.nebrRange * a.nebrRange;
     int wo = -1;
     for (int w = 0; w < a.nw; ++w) {
         const double d = a.wn[w][0] * (xi.x - a.wp[w][0]) + a.wn[w][1] * (xi.y - a.wp[w][1]) +
@@ -214,6 +247,182 @@ __device__ __noinline__ void nl_build_one(const DemArgs& a, int i) {
     a.obj_cnt[i] = oc;
 }
 
+// ---- periodic faces: shift, ghosts, half-shell sweep (DEM.cpp:1395-1494, 1554-1664) ------
+
+__device__ __forceinline__ double plane_dist(const double* p, const double* n, V x) {  // wall::dist, utils.cpp:14-17
+    return n[0] * (x.x - p[0]) + n[1] * (x.y - p[1]) + n[2] * (x.z - p[2]);
+}
+
+// exclusive prefix sum of v over the block (blockDim.x a multiple of 32, at most 1024);
+// every thread of the block must call it
+__device__ int block_scan(int v, int& total) {
+    __shared__ int wsum[32];
+    __shared__ int tot;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int k = 0; k < nw; ++k) { const int t = wsum[k]; wsum[k] = run; run += t; }
+        tot = run;
+    }
+    __syncthreads();
+    const int r = wsum[w] + x - v;
+    total = tot;
+    __syncthreads();
+    return r;
+}
+
+// side of face pair b that element n's centre copies to: +1 near pl1 (copied by +v), -1
+// near pl2 (by -v), 0 neither; pl1 is tested first (DEM.cpp:1596-1616)
+__device__ __forceinline__ int ghost_side(const DemArgs& a, int b, V x) {
+    if (plane_dist(a.pp1[b], a.pn1[b], x) < a.nebrRange) return 1;
+    if (plane_dist(a.pp2[b], a.pn2[b], x) < a.nebrRange) return -1;
+    return 0;
+}
+
+// One block: pbcShift (elements whose centre left through a face move by the shift;
+// elmt::translate moves x0 and xp0, elmt.cpp:256-259), then createGhosts: one ghost per
+// (face pair, element) whose centre is within nebrRange of a face, face pairs outer and
+// elements inner, then one corner ghost per two ghosts of the same element, ordered by
+// the first ghost's index and then the second's.  Ghost g is particle E + g, like the
+// reference's particles list; px holds every particle's centre.
+__device__ __noinline__ void ghosts_block(const DemArgs& a) {
+    const int E = a.E;
+    const long long st = (long long)E + a.gcap;
+    for (int n = threadIdx.x; n < E; n += blockDim.x) {
+        V x = ld3(a.x0, E, n), xp = ld3(a.xp0, E, n);
+        for (int b = 0; b < a.npbc; ++b) {
+            const double ld = plane_dist(a.pp1[b], a.pn1[b], x), rd = plane_dist(a.pp2[b], a.pn2[b], x);
+            const V v{a.pv[b][0], a.pv[b][1], a.pv[b][2]};
+            if (ld < 0.0) { x = add(x, v); xp = add(xp, v); }
+            if (rd < 0.0) { const V mv = mul(-1.0, v); x = add(x, mv); xp = add(xp, mv); }
+        }
+        st3(a.x0, E, n, x);
+        st3(a.xp0, E, n, xp);
+        a.px[n] = x.x; a.px[st + n] = x.y; a.px[2 * st + n] = x.z;
+        a.ccnt[n] = 0;
+    }
+    __syncthreads();
+    int total = 0;
+    for (int b = 0; b < a.npbc; ++b) {  // face ghosts
+        for (int n0 = 0; n0 < E; n0 += blockDim.x) {
+            const int n = n0 + threadIdx.x;
+            const int sd = n < E ? ghost_side(a, b, V{a.px[n], a.px[st + n], a.px[2 * st + n]}) : 0;
+            int sum;
+            const int k = block_scan(sd != 0, sum);
+            if (sd) {
+                const int g = total + k;
+                a.gorig[g] = n;
+                for (int q = 0; q < 3; ++q) a.gvec[(long long)q * a.gcap + g] = sd > 0 ? a.pv[b][q] : -1.0 * a.pv[b][q];
+                a.comp[6 * n + a.ccnt[n]++] = E + g;
+            }
+            total += sum;
+        }
+    }
+    for (int b1 = 0; b1 < a.npbc; ++b1) {  // corner ghosts
+        for (int n0 = 0; n0 < E; n0 += blockDim.x) {
+            const int n = n0 + threadIdx.x;
+            int sd[3] = {0, 0, 0}, cnt = 0;
+            if (n < E) {
+                const V x{a.px[n], a.px[st + n], a.px[2 * st + n]};
+                for (int b = 0; b < a.npbc; ++b) sd[b] = ghost_side(a, b, x);
+                if (sd[b1])
+                    for (int b2 = b1 + 1; b2 < a.npbc; ++b2) cnt += sd[b2] != 0;
+            }
+            int sum;
+            const int k = block_scan(cnt, sum);
+            if (cnt) {
+                int g = total + k;
+                for (int b2 = b1 + 1; b2 < a.npbc; ++b2) {
+                    if (!sd[b2]) continue;
+                    a.gorig[g] = n;
+                    for (int q = 0; q < 3; ++q) {
+                        const double v1 = sd[b1] > 0 ? a.pv[b1][q] : -1.0 * a.pv[b1][q];
+                        const double v2 = sd[b2] > 0 ? a.pv[b2][q] : -1.0 * a.pv[b2][q];
+                        a.gvec[(long long)q * a.gcap + g] = v1 + v2;
+                    }
+                    a.comp[6 * n + a.ccnt[n]++] = E + g;
+                    ++g;
+                }
+            }
+            total += sum;
+        }
+    }
+    __syncthreads();
+    for (int g = threadIdx.x; g < total; g += blockDim.x) {  // ghostUpdate (elmt.cpp:292-299)
+        const int o = a.gorig[g];
+        for (int q = 0; q < 3; ++q) a.px[q * st + E + g] = a.px[q * st + o] + a.gvec[(long long)q * a.gcap + g];
+    }
+    if (threadIdx.x == 0) {
+        a.gmeta[0] = total;
+        a.gmeta[1] = 1;  // newNeighborList: the lattice re-marks its particle nodes
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void nbr_push(const DemArgs& a, int i, int j) {
+    const int k = atomicAdd(a.nbr_cnt + i, 1);
+    if (k < NBR_CAP) a.nbr[(long long)i * NBR_CAP + k] = j;
+}
+
+// The reference's sweep (DEM.cpp:1425-1479) from particle p's cell: the 14 half-shell
+// offsets, an index that reaches nCells wrapping to 0 and one below 0 taken as the
+// unsigned value it becomes there, p paired with every particle of the target cell (with
+// a lower index in its own cell) of another element within nebrRange.  Each pair is
+// pushed into the candidate list of each of its standard particles.
+__device__ __noinline__ void nl_pairs_pbc(const DemArgs& a, int p) {
+    constexpr int SH[14][3] = {{0, 0, 0}, {1, 0, 0},  {1, 1, 0},  {0, 1, 0},   {-1, 1, 0}, {0, 0, 1},  {1, 0, 1},
+                               {1, 1, 1}, {0, 1, 1}, {-1, 1, 1}, {-1, 0, 1}, {-1, -1, 1}, {0, -1, 1}, {1, -1, 1}};
+    const int E = a.E;
+    const long long st = (long long)E + a.gcap;
+    const int c = a.cell_of[p];
+    if (c < 0) return;
+    const int ep = p < E ? p : a.gorig[p - E];
+    const V xp{a.px[p], a.px[st + p], a.px[2 * st + p]};
+    const double r2 = a.nebrRange * a.nebrRange;
+    const unsigned n0 = (unsigned)a.nC0, n1 = (unsigned)a.nC1, n2 = (unsigned)a.nC2;
+    const int i0[3] = {c % a.nC0, (c / a.nC0) % a.nC1, c / (a.nC0 * a.nC1)};
+    const unsigned nc[3] = {n0, n1, n2};
+    for (int s = 0; s < 14; ++s) {
+        unsigned i1[3];
+        for (int k = 0; k < 3; ++k) {
+            i1[k] = (unsigned)(i0[k] + SH[s][k]);
+            if (i1[k] == nc[k]) i1[k] = 0u;
+        }
+        const unsigned cell1 = (i1[2] * n1 + i1[1]) * n0 + i1[0];
+        if (cell1 >= (unsigned)a.ncells) continue;  // not reached for three or more cells per axis
+        for (int k = a.cell_start[cell1]; k < a.cell_start[cell1 + 1]; ++k) {
+            const int q = a.cell_items[k];
+            if (s == 0 && !(q < p)) continue;
+            const int eq = q < E ? q : a.gorig[q - E];
+            if (eq == ep) continue;
+            const V d = sub(V{a.px[q], a.px[st + q], a.px[2 * st + q]}, xp);
+            if (!(nrm2(d) < r2)) continue;
+            if (p < E) nbr_push(a, p, q);
+            if (q < E) nbr_push(a, q, p);
+        }
+    }
+}
+
+// a standard particle's list in ascending order (the pushes come in any order)
+__device__ __noinline__ void nl_sort_one(const DemArgs& a, int i) {
+    int cnt = a.nbr_cnt[i];
+    if (cnt > NBR_CAP) { atomicOr(a.status + 2, 1); cnt = NBR_CAP; a.nbr_cnt[i] = cnt; }
+    int* l = a.nbr + (long long)i * NBR_CAP;
+    for (int k = 1; k < cnt; ++k) {
+        const int v = l[k];
+        int m = k - 1;
+        while (m >= 0 && l[m] > v) { l[m + 1] = l[m]; --m; }
+        l[m + 1] = v;
+    }
+}
+
 // ---- forces (DEM.cpp:1114-1182, 1801-2136) --------------------------------------------
 // Contact forces are rare (a handful of overlapping pairs among ~10^4 candidates), so
 // their arithmetic is kept out of line: inlined, it sets the register budget of the whole
@@ -223,23 +432,24 @@ struct FM {
     V f, m;
 };
 
-// particleParticleCollision with I = lower index (DEM.cpp:1801-1900), seen by particle i
-__device__ __noinline__ FM pp_contact(const DemArgs& a, int i, int I, int J, V vd, double rI, double rJ, V FP,
-                                      V MP) {
+// particleParticleCollision with I = lower particle index (DEM.cpp:1801-1900), seen by
+// particle i; eI, eJ are the elements of I and J (a ghost moves with its element)
+__device__ __noinline__ FM pp_contact(const DemArgs& a, int i, int I, int eI, int eJ, V vd, double rI, double rJ,
+                                      V FP, V MP) {
     const int E = a.E;
     const double dist = sqrt(nrm2(vd));
     const double overlap = rI + rJ - dist;
-    const V relVel = sub(ld3(a.xp1, E, J), ld3(a.xp1, E, I));
+    const V relVel = sub(ld3(a.xp1, E, eJ), ld3(a.xp1, E, eI));
     const V en = divs(vd, dist);
     const double vn = dot(relVel, en);
     const V nrv = mul(vn, en);
-    const double mI = a.m[I], mJ = a.m[J];
+    const double mI = a.m[eI], mJ = a.m[eJ];
     const double effMass = mI * mJ / (mI + mJ);
     const double effRad = rI * rJ / (rI + rJ);
     const double fn = normal_contact(a, overlap, vn, effRad, effMass);
     const V nf = mul(fn, en);
     const V vrI = mul(rI, en), vrJ = mul(-rJ, en);
-    const V rvc = add(sub(relVel, cross(ld3(a.wpG, E, I), vrI)), cross(ld3(a.wpG, E, J), vrJ));
+    const V rvc = add(sub(relVel, cross(ld3(a.wpG, E, eI), vrI)), cross(ld3(a.wpG, E, eJ), vrJ));
     const V tang = sub(rvc, nrv);
     const double nt = sqrt(nrm2(tang));
     V tf{0, 0, 0};
@@ -363,13 +573,25 @@ __device__ void forces_warp(const DemArgs& a, const DemArgs& ga, int i, int lane
     for (int k = lane; k < cnt; k += 32) {
         const int j = a.nbr[(long long)i * NBR_CAP + k];
         const int I = min(i, j), J = max(i, j);
-        const double rI = a.rad[I], rJ = a.rad[J];
+        // a ghost partner (J = E + g) sits at its element's predicted centre plus its shift
+        // (particle::ghostUpdate, elmt.cpp:292-299); only i's side takes the force
+        // (DEM.cpp:1845-1858, 1879-1888)
+        int eJ = J;
+        V xJ;
+        if (J >= E) {
+            const int g = J - E;
+            eJ = a.gorig[g];
+            xJ = add(ld3(a.xp0, E, eJ), V{a.gvec[g], a.gvec[a.gcap + g], a.gvec[2 * a.gcap + g]});
+        } else {
+            xJ = ld3(a.xp0, E, J);
+        }
+        const double rI = a.rad[I], rJ = a.rad[eJ];
         const double sig = rI + rJ;
-        const V vd = sub(ld3(a.xp0, E, J), ld3(a.xp0, E, I));
+        const V vd = sub(xJ, ld3(a.xp0, E, I));
         if (!(nrm2(vd) < sig * sig)) continue;
         if (i < j) ++ncont;
         contrib = true;
-        const FM r = pp_contact(ga, i, I, J, vd, rI, rJ, FP, MP);
+        const FM r = pp_contact(ga, i, I, I, eJ, vd, rI, rJ, FP, MP);
         FP = r.f;
         MP = r.m;
     }
@@ -761,14 +983,36 @@ struct CoupleArgs {
     const double* mass;
     int free_surface;
     double *FH, *MH, *fvol;
+    // ghost particles (periodic faces): particle E + g is element gorig[g] shifted by gvec
+    int ghosts, gcap;
+    int* gmeta;  // [0] ghosts, [1] re-mark pending
+    const int *gorig, *comp, *ccnt;
+    const double* gvec;
+    uint32_t* remark;
 };
+
+// centre and radius of particle p (an element, or a ghost: its element's centre + shift)
+__device__ __forceinline__ void part_centre(const CoupleArgs& a, int p, double& cx_, double& cy_, double& cz_,
+                                            double& r) {
+    const int E = a.E;
+    if (p < E) {
+        cx_ = a.x0[p]; cy_ = a.x0[E + p]; cz_ = a.x0[2 * E + p];
+        r = a.rad[p];
+        return;
+    }
+    const int g = p - E, o = a.gorig[g];
+    cx_ = a.x0[o] + a.gvec[g];
+    cy_ = a.x0[E + o] + a.gvec[a.gcap + g];
+    cz_ = a.x0[2 * E + o] + a.gvec[2 * a.gcap + g];
+    r = a.rad[o];
+}
 
 struct Box {
     int x0, y0, z0, nx, ny, nz;
 };
 __device__ __forceinline__ Box pbox(const CoupleArgs& a, int p, int margin) {
-    const int E = a.E;
-    const double cx_ = a.x0[p], cy_ = a.x0[E + p], cz_ = a.x0[2 * E + p], r = a.rad[p];
+    double cx_, cy_, cz_, r;
+    part_centre(a, p, cx_, cy_, cz_, r);
     Box b;
     b.x0 = max(0, (int)floor(cx_ - r) - margin);
     b.y0 = max(0, (int)floor(cy_ - r) - margin);
@@ -796,10 +1040,9 @@ struct Sph {
     float fx, fy, fz, lo, hi;
 };
 __device__ __forceinline__ Sph load_sph(const CoupleArgs& a, int p) {
-    const int E = a.E;
     Sph s;
-    s.cx = a.x0[p]; s.cy = a.x0[E + p]; s.cz = a.x0[2 * E + p];
-    const double r = a.rad[p];
+    double r;
+    part_centre(a, p, s.cx, s.cy, s.cz, r);
     s.r2 = r * r;
     s.ix = (int)floor(s.cx); s.iy = (int)floor(s.cy); s.iz = (int)floor(s.cz);
     s.fx = (float)(s.cx - s.ix); s.fy = (float)(s.cy - s.iy); s.fz = (float)(s.cz - s.iz);
@@ -835,6 +1078,33 @@ static_assert(sizeof(PartBox) <= 128, "the context allocates 128 bytes per parti
 
 __device__ __forceinline__ void build_box(const CoupleArgs& a, int p) { a.tab[p].s = load_sph(a, p); }
 
+// FP32 record of ghost particle p for the reduced-precision lattice kernels: its
+// element's velocity and spin, the shifted centre
+__device__ __forceinline__ void ghost_pf(const DemArgs& a, int p) {
+    const int E = a.E, g = p - E, o = a.gorig[g];
+    float* q = a.pf + 12 * (size_t)p;
+    for (int k = 0; k < 3; ++k) {
+        q[k] = (float)(a.x0[(long long)k * E + o] + a.gvec[(long long)k * a.gcap + g]);
+        q[3 + k] = (float)a.x1[(long long)k * E + o];
+        q[6 + k] = (float)a.wG[(long long)k * E + o];
+    }
+}
+
+// findNewActive / findNewSolid test a node against every particle of the element
+// (DEM components: the element's own sphere, then its ghosts in creation order,
+// LB.cpp:1937-1953, 1984-2001): the first that covers it, or -1
+__device__ __forceinline__ int cover_first(const CoupleArgs& a, uint32_t q, int x, int y, int z) {
+    if (!a.ghosts) return in_sph(a.tab[q].s, x, y, z) ? (int)q : -1;
+    const int e = (int)q < a.E ? (int)q : a.gorig[(int)q - a.E];
+    if (in_sph(a.tab[e].s, x, y, z)) return e;
+    const int n = a.ccnt[e];
+    for (int k = 0; k < n; ++k) {
+        const int g = a.comp[6 * e + k];
+        if (in_sph(a.tab[g].s, x, y, z)) return g;
+    }
+    return -1;
+}
+
 // Coupling masks, node-parallel (one thread per lattice node, coalesced):
 //  findNewActive (LB.cpp:1921-1967): a particle node no longer covered by its particle
 //    leaves it;
@@ -859,9 +1129,8 @@ __device__ __noinline__ void mask_node_general(const CoupleArgs& a, int x, int y
     const long long l = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
     const uint8_t t = a.ntype[l];
     if (t & HB_INSIDE) {
-        const uint32_t q = a.solid[l];
-        if (in_sph(a.tab[q].s, x, y, z)) return;  // stays
-        a.ntype[l] = t & ~HB_INSIDE;              // pop
+        if (cover_first(a, a.solid[l], x, y, z) >= 0) return;  // stays
+        a.ntype[l] = t & ~HB_INSIDE;                           // pop
     }
     unsigned long long best = ~0ull;
     for (int kk = 1; kk <= 6; ++kk) {  // source m with link d[m][kk] == l
@@ -880,9 +1149,10 @@ __device__ __noinline__ void mask_node_general(const CoupleArgs& a, int x, int y
         if (lz == 0 && a.per[4]) lz = a.Z - 2; else if (lz == a.Z - 1 && a.per[5]) lz = 1;
         if (lx != x || ly != y || lz != z) continue;
         const uint32_t q = a.solid[m];
-        const Sph& sq = a.tab[q].s;
-        if (!in_sph(sq, mx, my, mz) || !in_sph(sq, x, y, z)) continue;
-        const unsigned long long key = ((unsigned long long)m << 32) | q;
+        if (cover_first(a, q, mx, my, mz) < 0) continue;  // the source itself popped
+        const int cq = cover_first(a, q, x, y, z);
+        if (cq < 0) continue;
+        const unsigned long long key = ((unsigned long long)m << 32) | (uint32_t)cq;
         if (key < best) best = key;
     }
     if (best != ~0ull) claim_push(a, l, best);
@@ -901,7 +1171,7 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
     const bool pnear = ((a.per[0] | a.per[1]) && (x0 < 2 || x0 + 3 > a.X - 3)) ||
                        ((a.per[2] | a.per[3]) && (y < 2 || y > a.Y - 3)) ||
                        ((a.per[4] | a.per[5]) && (z < 2 || z > a.Z - 3));
-    if ((a.X & 3) || pnear) {
+    if ((a.X & 3) || pnear || a.ghosts) {
         for (int k = 0; k < 4 && x0 + k < a.X; ++k) mask_node_general(a, x0 + k, y, z);
         return;
     }
@@ -976,11 +1246,16 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
 
 // element hydrodynamic force, torque and entrained fluid (LB.cpp:1853-1918): fixed
 // thread-to-row assignment and a fixed-order tree, so the sum is reproducible
-__device__ __noinline__ void reduce_block(const CoupleArgs& a, int p, double (*sh)[256]) {
+__device__ __noinline__ void reduce_block(const CoupleArgs& a, int p0, double (*sh)[256]) {
     const int E = a.E;
-    const Box b = pbox(a, p, 1);
-    const double px = a.x0[p], py = a.x0[E + p], pz = a.x0[2 * E + p];
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    // the element's own sphere, then its ghosts (nodes carry the particle that covers them)
+    const int ncomp = a.ghosts ? 1 + a.ccnt[p0] : 1;
+    for (int kc = 0; kc < ncomp; ++kc) {
+    const int p = kc == 0 ? p0 : a.comp[6 * p0 + kc - 1];
+    const Box b = pbox(a, p, 1);
+    double px, py, pz, pr;
+    part_centre(a, p, px, py, pz, pr);
     for (int r = threadIdx.x; r < b.ny * b.nz; r += blockDim.x) {
         const int y = b.y0 + r % b.ny, z = b.z0 + r / b.ny;
         const long long base = (long long)a.X * ((long long)y + (long long)a.Y * z);
@@ -1014,6 +1289,7 @@ __device__ __noinline__ void reduce_block(const CoupleArgs& a, int p, double (*s
             }
         }
     }
+    }
     __syncthreads();
     for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] = acc[c];
     __syncthreads();
@@ -1023,9 +1299,9 @@ __device__ __noinline__ void reduce_block(const CoupleArgs& a, int p, double (*s
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        a.FH[p] = sh[0][0]; a.FH[E + p] = sh[1][0]; a.FH[2 * E + p] = sh[2][0];
-        a.MH[p] = sh[3][0]; a.MH[E + p] = sh[4][0]; a.MH[2 * E + p] = sh[5][0];
-        a.fvol[p] = sh[6][0];
+        a.FH[p0] = sh[0][0]; a.FH[E + p0] = sh[1][0]; a.FH[2 * E + p0] = sh[2][0];
+        a.MH[p0] = sh[3][0]; a.MH[E + p0] = sh[4][0]; a.MH[2 * E + p0] = sh[5][0];
+        a.fvol[p0] = sh[6][0];
     }
 }
 
@@ -1094,6 +1370,36 @@ __device__ __forceinline__ void warp_tasks(int& first, int& stride) {
     stride = B * W;
 }
 
+// neighbour rebuild with periodic faces (DEM.cpp:1395-1494) by the whole cooperative
+// grid, out of line so that its registers do not count against the substep loop
+__device__ __noinline__ void rebuild_pbc(const DemArgs* gd, int E, int gt, int gs) {
+    cg::grid_group grid = cg::this_grid();
+    if (blockIdx.x == 0) {
+        ghosts_block(*gd);
+        nl_cells_block(*gd);
+    }
+    grid.sync();
+    const int S = E + *(volatile int*)gd->gmeta;
+    for (int p = gt; p < S; p += gs) nl_pairs_pbc(*gd, p);
+    grid.sync();
+    for (int i = gt; i < E; i += gs) {
+        nl_sort_one(*gd, i);
+        nl_near_one(*gd, i);
+    }
+    grid.sync();  // the contact warps read other threads' candidate lists
+}
+
+__device__ __noinline__ void ghost_boxes(const CoupleArgs* gc, const DemArgs* gd, int E) {
+    const int S = E + *(volatile int*)gd->gmeta;
+    for (int p = E + blockIdx.x * blockDim.x + threadIdx.x; p < S; p += gridDim.x * blockDim.x) {
+        build_box(*gc, p);
+        ghost_pf(*gd, p);
+    }
+}
+
+// PBC: periodic faces with particles (ghost rebuilds); a separate instantiation, so the
+// calls of that path cost the other configurations no registers
+template <bool PBC>
 __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
     cg::grid_group grid = cg::this_grid();
     __shared__ double sh[7][256];
@@ -1125,10 +1431,14 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
         stamp(A, k++);
         for (int s = 0; s < A.multi; ++s) {
             if (rebuild) {
-                if (blockIdx.x == 0) nl_cells_block(*A.gd);
-                grid.sync();
-                for (int i = gt; i < E; i += gs) nl_build_one(*A.gd, i);
-                grid.sync();  // the contact warps read other threads' candidate lists
+                if (PBC) {
+                    rebuild_pbc(A.gd, E, gt, gs);
+                } else {
+                    if (blockIdx.x == 0) nl_cells_block(*A.gd);
+                    grid.sync();
+                    for (int i = gt; i < E; i += gs) nl_build_one(*A.gd, i);
+                    grid.sync();  // the contact warps read other threads' candidate lists
+                }
             }
             int ncont = 0;
             for (int i = gw; i < E; i += nw) forces_warp(A.d, *A.gd, i, lane, ncont);
@@ -1175,8 +1485,10 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
                 rebuild = rb;
             }
         }
-        if (A.do_boxes)  // positions are final: boxes for the coupling passes
+        if (A.do_boxes) {  // positions are final: boxes for the coupling passes
             for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) build_box(A.c, p);
+            if (PBC) ghost_boxes(A.gc, A.gd, E);
+        }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             A.d.scal[0] = maxDisp;
             A.d.scal[1] = rebuild ? 1.0 : 0.0;
@@ -1187,10 +1499,51 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
 // ---- coupling masks: separate full-occupancy kernels, one thread per (particle, row) --
 __global__ void __launch_bounds__(256) k_build_boxes(CoupleArgs a) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < a.E) build_box(a, p);
+    if (p < a.E + (a.ghosts ? a.gmeta[0] : 0)) build_box(a, p);
 }
 
+// updateIndices (LB.cpp:1826-1849) after a neighbour rebuild with periodic faces:
+// initializeParticleBoundaries (LB.cpp:475-495) over every particle, ghosts included --
+// every node loses its particle flag, and each active node inside a particle takes the
+// last such particle in list order (the largest index) -- then resetLists.  Mark pass:
+// one block per particle sweeps its box and keeps the largest index + 1 per node.
+__global__ void __launch_bounds__(256) k_remark_mark(CoupleArgs a) {
+    if (!a.gmeta[1]) return;
+    const int S = a.E + a.gmeta[0];
+    for (int p = blockIdx.x; p < S; p += gridDim.x) {
+        const Box b = pbox(a, p, 1);
+        const Sph sp = a.tab[p].s;
+        const int n = b.nx * b.ny * b.nz;
+        for (int r = threadIdx.x; r < n; r += blockDim.x) {
+            const int x = b.x0 + r % b.nx, y = b.y0 + (r / b.nx) % b.ny, z = b.z0 + r / (b.nx * b.ny);
+            const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
+            if (!is_active(a.ntype[i])) continue;
+            if (in_sph(sp, x, y, z)) atomicMax(a.remark + i, (uint32_t)p + 1u);
+        }
+    }
+}
+
+// apply pass: every node's flag and particle from the mark pass (particle index of a node
+// that ends outside stays as it was, like the reference's solidIndex)
+__global__ void __launch_bounds__(256) k_remark_apply(CoupleArgs a) {
+    if (!a.gmeta[1]) return;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.N; i += (long long)gridDim.x * blockDim.x) {
+        const uint32_t r = a.remark[i];
+        uint8_t t = a.ntype[i] & (uint8_t)~HB_INSIDE;
+        if (r) {
+            t |= HB_INSIDE;
+            a.solid[i] = r - 1u;
+            a.remark[i] = 0u;
+        }
+        a.ntype[i] = t;
+    }
+}
+
+// the ghosts of the initial positions (DEM.cpp:253-257: the neighbour table built at init)
+__global__ void __launch_bounds__(256) k_ghosts_init(DemArgs a) { ghosts_block(a); }
+
 __global__ void __launch_bounds__(256) k_commit(CoupleArgs a) {
+    if (a.ghosts && blockIdx.x == 0 && threadIdx.x == 0) a.gmeta[1] = 0;  // re-mark done
     const int n = *a.claim_cnt;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         const uint32_t l = a.claim_list[2 * q], p = a.claim_list[2 * q + 1];
@@ -1275,6 +1628,22 @@ static DemArgs dem_args(hb_ctx* c) {
     for (int k = 0; k < 3; ++k) a.demF[k] = c->P.lbF[k];  // DEM.cpp:194
     a.status = c->status;
     a.total_contacts = reinterpret_cast<unsigned long long*>(d.scal + 4);
+    a.npbc = d.npbc;
+    a.gcap = d.gcap;
+    for (int b = 0; b < 3; ++b) {
+        const bool on = b < d.npbc;
+        const double* v = d.pbc_v[b];
+        const double nv = on ? sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) : 1.0;
+        for (int q = 0; q < 3; ++q) {  // pbc::setPlanes (utils.cpp:240-245)
+            a.pv[b][q] = on ? v[q] : 0.0;
+            a.pp1[b][q] = on ? d.pbc_p[b][q] : 0.0;
+            a.pp2[b][q] = on ? d.pbc_p[b][q] + v[q] : 0.0;
+            a.pn1[b][q] = on ? v[q] / nv : 0.0;
+            a.pn2[b][q] = -1.0 * a.pn1[b][q];
+        }
+    }
+    a.gmeta = d.gmeta; a.gorig = d.gorig; a.comp = d.comp; a.ccnt = d.ccnt;
+    a.gvec = d.gvec; a.px = d.px;
     return a;
 }
 
@@ -1302,7 +1671,18 @@ static CoupleArgs couple_args(hb_ctx* c) {
     a.mass = c->mass;
     a.free_surface = c->P.free_surface;
     a.FH = c->d.FH; a.MH = c->d.MH; a.fvol = c->d.fvol;
+    a.ghosts = c->d.npbc > 0;
+    a.gcap = c->d.gcap;
+    a.gmeta = c->d.gmeta; a.gorig = c->d.gorig; a.comp = c->d.comp; a.ccnt = c->d.ccnt;
+    a.gvec = c->d.gvec;
+    a.remark = c->d.remark;
     return a;
+}
+
+int launch_ghosts_init(hb_ctx* c) {
+    if (c->d.E == 0 || c->d.npbc == 0) return 0;
+    k_ghosts_init<<<1, 256, 0, c->stream>>>(dem_args(c));
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 // the device copy of the DEM and coupling parameter blocks (constant after init)
@@ -1326,7 +1706,7 @@ int coop_grid(hb_ctx* c) {
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cycle, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cycle<false>, 256, 0);
     occ = occ < 1 ? 1 : (occ > 4 ? 4 : occ);
     cached = sms * occ;
     if (cached > PARTIAL_CAP) cached = PARTIAL_CAP;  // one trigger partial per block
@@ -1355,7 +1735,16 @@ int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsign
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_cycle, A) == cudaSuccess ? 0 : -1;
+    if (c->d.npbc) {
+        int occ = 0;  // the periodic instantiation must fit the same grid
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cycle<true>, 256, 0);
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if ((int)cfg.gridDim.x > occ * sms) return -1;
+        return cudaLaunchKernelEx(&cfg, k_cycle<true>, A) == cudaSuccess ? 0 : -1;
+    }
+    return cudaLaunchKernelEx(&cfg, k_cycle<false>, A) == cudaSuccess ? 0 : -1;
 }
 
 // findNewActive + findNewSolid (LB.cpp:247-280); boxes come from the cooperative kernel
@@ -1364,7 +1753,11 @@ int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsign
 void launch_couple(hb_ctx* c, bool build, cudaEvent_t* ev) {
     if (c->d.E == 0) return;
     CoupleArgs a = couple_args(c);
-    if (build) k_build_boxes<<<ceil_div(c->d.E, 256), 256, 0, c->stream>>>(a);
+    if (build) k_build_boxes<<<ceil_div(c->d.E + c->d.gcap, 256), 256, 0, c->stream>>>(a);
+    if (a.ghosts && a.remark) {  // after a neighbour rebuild (the kernels return at once otherwise)
+        k_remark_mark<<<std::min(c->d.E + c->d.gcap, 152 * 8), 256, 0, c->stream>>>(a);
+        k_remark_apply<<<152 * 8, 256, 0, c->stream>>>(a);
+    }
     if (ev) cudaEventRecord(ev[0], c->stream);
     cudaMemsetAsync(a.claim_cnt, 0, sizeof(int), c->stream);
     if (ev) cudaEventRecord(ev[1], c->stream);

@@ -38,6 +38,7 @@ def lib():
     L.hb_download_lattice.argtypes = [vp] + [vp] * 9
     L.hb_download_elements.argtypes = [vp] + [vp] * 11
     L.hb_download_pairs.argtypes = [vp, vp, C.c_int64, P(C.c_int64)]
+    L.hb_download_ghosts.argtypes = [vp, vp, vp, C.c_int64, P(C.c_int64)]
     L.hb_download_interface.argtypes = [vp, vp, C.c_int64, P(C.c_int64)]
     L.hb_download_walls.argtypes = [vp, vp, vp, P(C.c_int32)]
     L.hb_download_objects.argtypes = [vp, vp, P(C.c_int32)]
@@ -139,6 +140,15 @@ class GpuSim:
         buf = np.zeros(2 * max(n.value, 1), np.uint32)
         check(self.L.hb_download_pairs(self.h, _p(buf), n.value, C.byref(n)))
         return buf[:2 * n.value]
+
+    def ghosts(self):
+        """Ghost particles of the last rebuild: (element index [G], shift [G, 3])."""
+        n = C.c_int64(0)
+        check(self.L.hb_download_ghosts(self.h, None, None, 0, C.byref(n)))
+        o = np.zeros(max(n.value, 1), np.uint32)
+        v = np.zeros(3 * max(n.value, 1))
+        check(self.L.hb_download_ghosts(self.h, _p(o), _p(v), n.value, C.byref(n)))
+        return o[:n.value], v[:3 * n.value].reshape(-1, 3)
 
     def interface(self):
         n = C.c_int64(0)

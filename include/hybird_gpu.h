@@ -216,8 +216,15 @@ int hb_download_elements(hb_ctx* ctx, double* x0, double* x1, double* w, double*
                          double* fhydro, double* mhydro, double* fparticle, double* fwall,
                          double* mparticle, double* mwall, double* fluid_volume);
 /* Candidate pair list as sorted (min,max) pairs, like DEM::neighborTable
- * (DEM.cpp:1369-1494) after normalisation.  *count receives the pair count. */
+ * (DEM.cpp:1369-1494) after normalisation.  *count receives the pair count.  With
+ * periodic faces a ghost particle is numbered E + g (g its index in hb_download_ghosts),
+ * as in the reference's particles list; pairs of two ghosts (which carry no force) are
+ * not kept. */
 int hb_download_pairs(hb_ctx* ctx, uint32_t* pairs, int64_t capacity, int64_t* count);
+/* Ghost particles of the last neighbour rebuild with periodic faces, like DEM::ghosts
+ * (DEM.cpp:1586-1664): element index and shift (x, y, z per ghost).  *count receives
+ * the ghost count; either array may be null. */
+int hb_download_ghosts(hb_ctx* ctx, uint32_t* origin, double* shift, int64_t capacity, int64_t* count);
 /* Interface cells, ascending node index.  *count receives the count. */
 int hb_download_interface(hb_ctx* ctx, uint32_t* cells, int64_t capacity, int64_t* count);
 /* Per-wall hydrodynamic force (walls[].FHydro, LB.cpp:1334) and particle force

@@ -136,6 +136,12 @@ void dump(IO& io, DEM& dem, LB& lb, long step) {
     put_f64("e_MWall", emw); put_f64("e_fluidVolume", evol); put_f64("e_m", em); put_f64("e_I", eI);
     std::vector<uint32_t> nt(dem.neighborTable.begin(), dem.neighborTable.end());
     put_u32("neighborTable", nt);
+    // ghost particles of the periodic faces (DEM.cpp:1586-1664): origin and shift
+    std::vector<uint32_t> gi;
+    std::vector<double> gv;
+    for (auto& gh : dem.ghosts) { gi.push_back(gh.ghostIndex); vec3(gv, gh.pbcVector); }
+    put_u32("ghost_index", gi);
+    put_f64("ghost_vec", gv);
     std::vector<uint32_t> nw(dem.nearWallTable.begin(), dem.nearWallTable.end());
     put_u32("nearWallTable", nw);
     std::vector<uint32_t> no(dem.nearObjectTable.begin(), dem.nearObjectTable.end());

@@ -70,6 +70,32 @@ def rsa_spheres(seed, n, rmin, rmax, lo, hi, gap=0.0):
     return out
 
 
+def rsa_periodic(seed, n, rmin, rmax, lo, hi, period, gap=0.3):
+    """Seeded random sequential addition with centres uniform in [lo, hi] (not shrunk by
+    r) and overlaps checked through the minimum image along the axes with a period."""
+    rng = random.Random(seed)
+    out = []
+    tries = 0
+    while len(out) < n and tries < 200000:
+        tries += 1
+        r = rng.uniform(rmin, rmax)
+        c = [rng.uniform(lo[k], hi[k]) for k in range(3)]
+        ok = True
+        for (q, rq) in out:
+            d2 = 0.0
+            for k in range(3):
+                d = c[k] - q[k]
+                if period[k]:
+                    d -= period[k] * round(d / period[k])
+                d2 += d * d
+            if d2 < (r + rq + gap) ** 2:
+                ok = False
+                break
+        if ok:
+            out.append((c, r))
+    return out
+
+
 CASES = {
     # periodic-x/z channel with walls at y=0/Ly-1 (BASELINE config 1 shape, shrunk)
     "channel_bgk": dict(
@@ -150,6 +176,22 @@ CASES = {
                  boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
         spheres=("rsa", 9, 10, 1.5, 2.2, (8.5, 8.5, 1.6), (19.5, 19.5, 30.0)),
         objects=[], steps=[0, 1, 30, 60, 100], full=[], vtk=[60]),
+    # periodic DEM (DEM.cpp:937-1063, 1395-1411, 1554-1664): spheres under a tilted gravity
+    # cross the periodic x and y faces; DEM only
+    "dem_periodic": dict(
+        cfg=dict(lbSizeX=24, lbSizeY=20, lbSizeZ=28, lbSolve=0, lbFX=1e-3, lbFY=-6e-4, lbFZ=-2e-3,
+                 multiStep=20,
+                 boundary0=4, boundary1=4, boundary2=4, boundary3=4, boundary4=7, boundary5=7),
+        spheres=("rsa_periodic", 31, 14, 1.4, 2.0, (0.6, 0.6, 3.0), (22.4, 18.4, 22.0), (22.0, 18.0, 0.0)),
+        objects=[], steps=[0, 1, 30, 60, 100, 150], full=[]),
+    # the same with the lattice: ghost particles cover the nodes across the periodic faces
+    # and every neighbour rebuild re-marks the particle nodes (LB.cpp:1826-1849)
+    "box_periodic": dict(
+        cfg=dict(lbSizeX=18, lbSizeY=16, lbSizeZ=18, lbFX=1.5e-3, lbFY=-1e-3, lbFZ=-1e-3, initVisc=0.1,
+                 multiStep=3,
+                 boundary0=4, boundary1=4, boundary2=4, boundary3=4, boundary4=7, boundary5=7),
+        spheres=("rsa_periodic", 37, 9, 1.6, 2.2, (0.6, 0.6, 4.0), (16.4, 14.4, 13.0), (16.0, 14.0, 0.0)),
+        objects=[], steps=[0, 1, 2, 10, 40, 80, 120], full=[1, 120], vtk=[80]),
     # free-surface dam break (LB.cpp:1492-1804), column x < 0.4 Lx, z < 0.6 Lz
     "dambreak_fs": dict(
         cfg=dict(lbSizeX=20, lbSizeY=8, lbSizeZ=12, lbFZ=-5e-4, initVisc=0.05, freeSurfaceSolve=1,
@@ -207,7 +249,9 @@ def run_case(name, spec):
     cfg = dict(BASE)
     cfg.update(spec["cfg"])
     sizes = (cfg["lbSizeX"], cfg["lbSizeY"], cfg["lbSizeZ"])
-    if spec["spheres"]:
+    if spec["spheres"] and spec["spheres"][0] == "rsa_periodic":
+        spheres = rsa_periodic(*spec["spheres"][1:])
+    elif spec["spheres"]:
         seed, n, rmin, rmax = spec["spheres"][1:5]
         lo, hi = (1.5, 1.5, 1.5), (sizes[0] - 2.5, sizes[1] - 2.5, sizes[2] - 2.5)
         if len(spec["spheres"]) > 5:
@@ -270,7 +314,7 @@ def run_case(name, spec):
         for k in ("e_x0", "e_x1", "e_x2", "e_w", "e_q0", "e_FHydro", "e_MHydro", "e_FParticle",
                   "e_FWall", "e_MParticle", "e_MWall", "e_fluidVolume", "e_m", "e_I",
                   "neighborTable", "nearWallTable", "nearObjectTable", "w_FParticle",
-                  "dem_scalars", "o_FParticle", "io_values"):
+                  "dem_scalars", "o_FParticle", "io_values", "ghost_index", "ghost_vec"):
             store[p + k] = s[k]
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **store)
     return len(snaps)

@@ -31,6 +31,8 @@ def _state(g):
         out["pairs"] = g.pairs()
     if g.params.free_surface:
         out["interface"] = g.interface()
+    go, gv = g.ghosts()
+    out["ghost_orig"], out["ghost_vec"] = go, gv
     fh, fp = g.walls()
     out["walls_fh"], out["walls_fp"] = fh, fp
     ex = g.export_values()
@@ -58,12 +60,19 @@ def _pipe_slip():
     return p, None, None
 
 
+def _periodic_box():
+    """Periodic x and y with particles (ghost particles, re-marked particle nodes), FP32."""
+    d = load_golden("box_periodic")
+    return golden_params(d, precision=abi.HB_FP32), d["spheres"], None
+
+
 CASES = {
     "coupled_fp32": lambda: _coupled_box(abi.HB_FP32),
     "coupled_fp16s": lambda: _coupled_box(abi.HB_FP16S),
     "coupled_fp64": lambda: _coupled_box(abi.HB_FP64),
     "dambreak_fp64": _dambreak,
     "pipe_slip_fp32": _pipe_slip,
+    "periodic_fp32": _periodic_box,
 }
 CYL = {"pipe_slip_fp32": [(0.0, 9.5, 9.7, 1.0, 9.5, 9.7, 8.3)]}
 

@@ -86,7 +86,7 @@ def _vtk_tokens_match(ours, ref):
 
 
 @pytest.mark.parametrize("name,step", [("channel_bingham_smag", 10), ("box_spheres", 30), ("dambreak_fs", 60),
-                                       ("pipe_curved", 30)])
+                                       ("pipe_curved", 30), ("box_periodic", 80)])
 def test_vtk_fluid_file_matches_reference(name, step):
     d = load_golden(name)
     p = golden_params(d, gas_box=golden_gasbox(name))
