@@ -64,7 +64,8 @@ class HbParams(C.Structure):
 class HbElements(C.Structure):
     _fields_ = [("count", C.c_int32), ("radius", C.POINTER(C.c_double)),
                 ("x0", C.POINTER(C.c_double)), ("x1", C.POINTER(C.c_double)),
-                ("w0", C.POINTER(C.c_double)), ("q0", C.POINTER(C.c_double))]
+                ("w0", C.POINTER(C.c_double)), ("q0", C.POINTER(C.c_double)),
+                ("size", C.POINTER(C.c_int32))]
 
 
 class HbObjects(C.Structure):
@@ -178,7 +179,9 @@ class CylinderArrays:
 class ElementArrays:
     """Keeps the numpy buffers alive behind an HbElements / HbObjects struct."""
 
-    def __init__(self, spheres=None, objects=None):
+    def __init__(self, spheres=None, objects=None, sizes=None, quats=None):
+        """spheres: [n, 4] (x, y, z, radius) per element; sizes: spheres per element
+        (1..4, multi-sphere prototypes), quats: [n, 4] orientations (default identity)."""
         self.el = None
         self.ob = None
         if spheres is not None and len(spheres):
@@ -188,8 +191,11 @@ class ElementArrays:
             self.x0 = np.ascontiguousarray(s[:, :3].T.reshape(-1))
             self.x1 = np.zeros(3 * n)
             self.w0 = np.zeros(3 * n)
-            self.el = HbElements(n, dptr(self.radius), dptr(self.x0), dptr(self.x1),
-                                 dptr(self.w0), None)
+            self.q0 = None if quats is None else np.ascontiguousarray(np.asarray(quats, np.float64).reshape(-1, 4).T.reshape(-1))
+            self.size = None if sizes is None else np.ascontiguousarray(np.asarray(sizes, np.int32).reshape(-1))
+            self.el = HbElements(n, dptr(self.radius), dptr(self.x0), dptr(self.x1), dptr(self.w0),
+                                 None if self.q0 is None else dptr(self.q0),
+                                 None if self.size is None else self.size.ctypes.data_as(C.POINTER(C.c_int32)))
         if objects is not None and len(objects):
             o = np.asarray(objects, dtype=np.float64).reshape(-1, 4)
             m = len(o)

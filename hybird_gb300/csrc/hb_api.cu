@@ -154,6 +154,27 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
             ++d.npbc;
         }
     }
+    // particles of the elements (DEM::compositeProperties, elmt::generateParticles;
+    // DEM.cpp:404-433, elmt.cpp:122-137): element k owns particles efirst[k] ..
+    // efirst[k+1]-1 at its prototype's positions (radius units)
+    std::vector<int> esz(E, 1), efirst(E + 1, 0);
+    for (int k = 0; k < E; ++k) {
+        if (e->size) esz[k] = e->size[k];
+        if (esz[k] < 1 || esz[k] > 4) return seterr(HB_ERR_ARG, "element %d: size %d (1..4 spheres)", k, esz[k]);
+        efirst[k + 1] = efirst[k] + esz[k];
+    }
+    const int Pn = efirst[E];
+    d.P = Pn;
+    d.gen = (d.npbc > 0 || Pn != E) ? 1 : 0;
+    double proto[5][4][3] = {};
+    proto[2][0][0] = 0.5; proto[2][1][0] = -0.5;
+    proto[3][0][1] = 1.0;
+    proto[3][1][0] = -std::sqrt(3.0) / 2; proto[3][1][1] = -1 / 2;  // integer division: 0
+    proto[3][2][0] = std::sqrt(3.0) / 2; proto[3][2][1] = -1 / 2;
+    proto[4][0][2] = 1.0;
+    proto[4][1][1] = 2.0 * std::sqrt(2.0) / 3.0; proto[4][1][2] = -1.0 / 3.0;
+    proto[4][2][0] = 2.0 * std::sqrt(6.0) / 6.0; proto[4][2][1] = -2.0 * std::sqrt(2.0) / 6.0; proto[4][2][2] = -1.0 / 3.0;
+    proto[4][3][0] = -2.0 * std::sqrt(6.0) / 6.0; proto[4][3][1] = -2.0 * std::sqrt(2.0) / 6.0; proto[4][3][2] = -1.0 / 3.0;
     // element fields, one allocation (elmt.h:53-135)
     const int nfields = DEM_FIELDS;
     int rc;
@@ -177,9 +198,16 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         const double r = e->radius[k];
         maxRad = std::max(maxRad, r);
         const double sm = 4.0 / 3.0 * P.density * M_PI * r * r * r;
-        m[k] = 1 * sm;
-        const double iv = 1 * 2.0 / 5.0 * sm * r * r;
-        for (int q = 0; q < 3; ++q) I[q * E + k] = iv * 1.0 + sm * r * r * 0.0;
+        const int sz = esz[k];
+        m[k] = sz * sm;
+        // inertia of the spheres plus their transport terms (elmt.cpp:64-71)
+        const double iv = sz * 2.0 / 5.0 * sm * r * r;
+        for (int q = 0; q < 3; ++q) I[q * E + k] = 1.0 * iv;
+        for (int n = 0; n < sz; ++n) {
+            const double* v = proto[sz][n];
+            const double t[3] = {v[1] * v[1] + v[2] * v[2], v[2] * v[2] + v[0] * v[0], v[0] * v[0] + v[1] * v[1]};
+            for (int q = 0; q < 3; ++q) I[q * E + k] += t[q] * (sm * r * r);
+        }
         if (e->q0) for (int q = 0; q < 4; ++q) q0[q * E + k] = e->q0[q * E + k];
         else { q0[k] = 1.0; q0[E + k] = q0[2 * E + k] = q0[3 * E + k] = 0.0; }
         if (e->w0) for (int q = 0; q < 3; ++q) w0[q * E + k] = e->w0[q * E + k];
@@ -208,7 +236,7 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         std::vector<int> plain(E);
         for (int k = 0; k < E; ++k) {
             const bool ident = q0[k] == 1.0 && q0[E + k] == 0.0 && q0[2 * E + k] == 0.0 && q0[3 * E + k] == 0.0;
-            plain[k] = ident ? 1 : 0;  // q1 (quaternion rate) is zero for every uploaded element
+            plain[k] = ident && esz[k] == 1 ? 1 : 0;  // q1 (quaternion rate) is zero for every uploaded element
         }
         if ((rc = dalloc(&d.plain, E))) return rc;
         CK(cudaMemcpy(d.plain, plain.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
@@ -263,46 +291,70 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
             }
             orr.push_back(orr[gi[g]]);
         }
-        // ghost particles: at most one per face pair and one per two of those per element
-        d.gcap = 6 * E;
-        if ((rc = dalloc(&d.gmeta, 2)) || (rc = dalloc(&d.gorig, d.gcap)) || (rc = dalloc(&d.gvec, 3 * (size_t)d.gcap)) ||
-            (rc = dalloc(&d.comp, 6 * (size_t)E)) || (rc = dalloc(&d.ccnt, E)) ||
-            (rc = dalloc(&d.px, 3 * ((size_t)E + d.gcap))))
+    }
+    if (d.gen) {
+        // per-particle path: ghost particles (at most one per face pair and one per two of
+        // those per particle) and the particle tables
+        const size_t Ps = (size_t)Pn;
+        d.gcap = d.npbc ? 6 * Pn : 0;
+        const size_t S = Ps + d.gcap;
+        auto zi = [&](int** p_, size_t n) -> int {
+            int r_ = dalloc(p_, n);
+            if (!r_) cudaMemset(*p_, 0, sizeof(int) * std::max<size_t>(n, 1));
+            return r_;
+        };
+        auto zd = [&](double** p_, size_t n) -> int {
+            int r_ = dalloc(p_, n);
+            if (!r_) cudaMemset(*p_, 0, sizeof(double) * std::max<size_t>(n, 1));
+            return r_;
+        };
+        if ((rc = zi(&d.gmeta, 2)) || (rc = zi(&d.gorig, d.gcap)) || (rc = zd(&d.gvec, 3 * (size_t)d.gcap)) ||
+            (rc = zi(&d.comp, 6 * Ps)) || (rc = zi(&d.ccnt, Ps)) || (rc = zi(&d.ecomp, 6 * Ps)) ||
+            (rc = zi(&d.eccnt, E)) || (rc = zd(&d.px, 3 * S)) || (rc = zi(&d.pkey, S)) ||
+            (rc = zi(&d.efirst, (size_t)E + 1)) || (rc = zi(&d.esize, E)) || (rc = zd(&d.proto, 3 * Ps)) ||
+            (rc = zd(&d.ppos, 3 * S)) || (rc = zd(&d.pvel, 3 * S)) || (rc = zd(&d.prv, 3 * S)) ||
+            (rc = zd(&d.pF, 12 * Ps)) || (rc = zd(&d.pcen, 3 * S)))
             return rc;
-        CK(cudaMemset(d.gmeta, 0, sizeof(int) * 2));
-        CK(cudaMemset(d.gorig, 0, sizeof(int) * d.gcap));
-        CK(cudaMemset(d.gvec, 0, sizeof(double) * 3 * d.gcap));
-        CK(cudaMemset(d.comp, 0, sizeof(int) * 6 * E));
-        CK(cudaMemset(d.ccnt, 0, sizeof(int) * E));
-        // ghost entries of the FP32 particle copy follow the elements'
-        float* pf2 = nullptr;
-        if ((rc = dalloc(&pf2, 12 * ((size_t)E + d.gcap)))) return rc;
-        CK(cudaMemset(pf2, 0, sizeof(float) * 12 * ((size_t)E + d.gcap)));
-        CK(cudaMemcpy(pf2, d.pf, sizeof(float) * 12 * (size_t)E, cudaMemcpyDeviceToDevice));
+        std::vector<int> key(S, 0);
+        std::vector<double> pr(3 * Ps, 0.0);
+        for (int k = 0; k < E; ++k)
+            for (int n = 0; n < esz[k]; ++n) {
+                const int q = efirst[k] + n;
+                key[q] = k;
+                for (int c3 = 0; c3 < 3; ++c3) pr[c3 * Ps + q] = proto[esz[k]][n][c3];
+            }
+        CK(cudaMemcpy(d.pkey, key.data(), sizeof(int) * S, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.efirst, efirst.data(), sizeof(int) * (E + 1), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.esize, esz.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.proto, pr.data(), sizeof(double) * pr.size(), cudaMemcpyHostToDevice));
+        // the FP32 records are per particle (ghosts after the standard ones)
         cudaFree(d.pf);
-        d.pf = pf2;
+        d.pf = nullptr;
+        if ((rc = dalloc(&d.pf, 12 * S))) return rc;
+        CK(cudaMemset(d.pf, 0, sizeof(float) * 12 * S));
     }
     if ((rc = upload_objects())) return rc;
-    const size_t S = (size_t)E + d.gcap;
+    const size_t Pl = (size_t)(d.gen ? Pn : E);  // particles that own candidate lists
+    const size_t S = Pl + d.gcap;
     if ((rc = dalloc(&d.cell_of, S)) || (rc = dalloc(&d.cell_cnt, d.ncells)) || (rc = dalloc(&d.cell_start, d.ncells + 1)) ||
         (rc = dalloc(&d.cell_fill, d.ncells)) || (rc = dalloc(&d.cell_items, S)) ||
-        (rc = dalloc(&d.nbr, (size_t)E * NBR_CAP)) || (rc = dalloc(&d.nbr_cnt, E)) || (rc = dalloc(&d.wall_of, E)) ||
-        (rc = dalloc(&d.obj, (size_t)E * OBJ_CAP)) || (rc = dalloc(&d.obj_cnt, E)) || (rc = dalloc(&d.scal, 8)) ||
+        (rc = dalloc(&d.nbr, Pl * NBR_CAP)) || (rc = dalloc(&d.nbr_cnt, Pl)) || (rc = dalloc(&d.wall_of, Pl)) ||
+        (rc = dalloc(&d.obj, Pl * OBJ_CAP)) || (rc = dalloc(&d.obj_cnt, Pl)) || (rc = dalloc(&d.scal, 8)) ||
         (rc = dalloc(&d.contacts, 1)) || (rc = dalloc(&d.partial, hb::PARTIAL_CAP)) || (rc = dalloc(&d.done, 1)) ||
-        (rc = dalloc(&d.wrec, (size_t)7 * E)) || (rc = dalloc(&d.orec, (size_t)7 * E * OBJ_CAP)) ||
-        (rc = dalloc(&d.cyl_of, E)) ||
+        (rc = dalloc(&d.wrec, 7 * Pl)) || (rc = dalloc(&d.orec, 7 * Pl * OBJ_CAP)) ||
+        (rc = dalloc(&d.cyl_of, Pl)) ||
         (rc = dalloc(&d.react, (size_t)3 * (MAX_WALLS + d.O))))
         return rc;
     CK(cudaMemset(d.react, 0, sizeof(double) * 3 * (MAX_WALLS + d.O)));
-    CK(cudaMemset(d.wrec, 0, sizeof(double) * 7 * E));
-    CK(cudaMemset(d.cyl_of, 0xFF, sizeof(int) * E));
-    CK(cudaMemset(d.orec, 0, sizeof(double) * 7 * E * OBJ_CAP));
+    CK(cudaMemset(d.wrec, 0, sizeof(double) * 7 * Pl));
+    CK(cudaMemset(d.cyl_of, 0xFF, sizeof(int) * Pl));
+    CK(cudaMemset(d.orec, 0, sizeof(double) * 7 * Pl * OBJ_CAP));
     const double scal0[8] = {0.5 * d.nebrRange, 1.0, 0, 0, 0, 0, 0, 0};  // maxDisp, rebuild
     CK(cudaMemcpy(d.scal, scal0, sizeof(scal0), cudaMemcpyHostToDevice));
     CK(cudaMemset(d.contacts, 0, sizeof(int)));
     CK(cudaMemset(d.done, 0, sizeof(unsigned int)));
-    CK(cudaMemset(d.nbr_cnt, 0, sizeof(int) * E));
-    CK(cudaMemset(d.obj_cnt, 0, sizeof(int) * E));
+    CK(cudaMemset(d.nbr_cnt, 0, sizeof(int) * Pl));
+    CK(cudaMemset(d.obj_cnt, 0, sizeof(int) * Pl));
     return HB_OK;
 }
 
@@ -370,7 +422,8 @@ int hb_destroy(hb_ctx* c) {
                     c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
                     c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix, c->fs_ilist,
                     c->curved_list, c->curved_cnt, c->d.cyl_of, c->io_terms, c->d.gmeta, c->d.gorig, c->d.gvec,
-                    c->d.comp, c->d.ccnt, c->d.px, c->d.remark};
+                    c->d.comp, c->d.ccnt, c->d.px, c->d.remark, c->d.ecomp, c->d.eccnt, c->d.pkey, c->d.efirst,
+                    c->d.esize, c->d.proto, c->d.ppos, c->d.pvel, c->d.prv, c->d.pF, c->d.pcen};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -421,7 +474,7 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         }
         if (!c->d.claim_list && (rc = dalloc(&c->d.claim_list, 2 * N))) return rc;
         if (!c->d.claim_cnt && (rc = dalloc(&c->d.claim_cnt, 1))) return rc;
-        if (!c->d.boxes && (rc = dalloc((uint8_t**)&c->d.boxes, ((size_t)c->d.E + c->d.gcap) * 128))) return rc;
+        if (!c->d.boxes && (rc = dalloc((uint8_t**)&c->d.boxes, ((size_t)c->d.P + c->d.gcap) * 128))) return rc;
         CK(cudaMemset(c->d.claim_cnt, 0, sizeof(int)));
         if (c->d.npbc && c->P.lb_solve && !c->d.remark) {
             if ((rc = dalloc(&c->d.remark, N))) return rc;
@@ -453,7 +506,7 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     c->reduce_pending = false;
     c->steps = 0;
     c->dem_stepped = false;
-    if (launch_ghosts_init(c)) return seterr(HB_ERR_CUDA, "ghost particles: %s", cudaGetErrorString(cudaGetLastError()));
+    if (launch_ghosts_init(c)) return seterr(HB_ERR_CUDA, "particles: %s", cudaGetErrorString(cudaGetLastError()));
     if (launch_init_lattice(c, e && c->d.E ? c->d.x[0] : nullptr, c->d.E ? c->d.rad : nullptr, c->d.E,
                             c->d.obj_x0, c->d.obj_r, c->d.O))
         return seterr(HB_ERR_CUDA, "lattice init: %s", cudaGetErrorString(cudaGetLastError()));
@@ -755,7 +808,7 @@ int hb_download_elements(hb_ctx* c, double* x0, double* x1, double* w, double* q
 int hb_download_pairs(hb_ctx* c, uint32_t* pairs, int64_t capacity, int64_t* count) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
     CK(cudaStreamSynchronize(c->stream));
-    const int E = c->d.E;
+    const int E = c->d.P;  // particles (standard ones own the lists)
     std::vector<uint32_t> out;
     if (E > 0) {
         std::vector<int> nb((size_t)E * NBR_CAP), cnt(E);
@@ -857,8 +910,8 @@ int hb_get_status(hb_ctx* c, hb_status* s) {
         int k = 0;
         CK(cudaMemcpy(&k, c->d.contacts, sizeof(int), cudaMemcpyDeviceToHost));
         s->contacts = k;
-        std::vector<int> cnt(c->d.E);
-        CK(cudaMemcpy(cnt.data(), c->d.nbr_cnt, sizeof(int) * c->d.E, cudaMemcpyDeviceToHost));
+        std::vector<int> cnt(c->d.P);
+        CK(cudaMemcpy(cnt.data(), c->d.nbr_cnt, sizeof(int) * c->d.P, cudaMemcpyDeviceToHost));
         int64_t tot = 0;
         for (int v : cnt) tot += v;
         s->pairs = tot / 2;

@@ -13,6 +13,7 @@
 // The loader rebuilds the context with hb_create + hb_init from the saved parameters,
 // particles and objects (so every allocation and both cycle graphs exist), then
 // overwrites each buffer and the host step state.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -79,32 +80,38 @@ std::vector<Buf> state_buffers(hb_ctx* c) {
     if (E) {
         add("hacc", c->hacc, 8 * 7 * E);
         add("dem_base", d.base, 8 * (size_t)DEM_FIELDS * E);
-        const size_t S = E + (size_t)d.gcap;
-        add("dem_pf", d.pf, 4 * 12 * S);
+        const size_t Pl = (size_t)d.P;  // particles (= elements for single spheres)
+        const size_t S = Pl + (size_t)d.gcap;
+        add("dem_pf", d.pf, 4 * 12 * (d.gen ? S : E));
         add("dem_plain", d.plain, 4 * E);
         add("cell_of", d.cell_of, 4 * S);
         add("cell_cnt", d.cell_cnt, 4 * (size_t)d.ncells);
         add("cell_start", d.cell_start, 4 * ((size_t)d.ncells + 1));
         add("cell_fill", d.cell_fill, 4 * (size_t)d.ncells);
         add("cell_items", d.cell_items, 4 * S);
-        if (d.npbc) {  // ghost particles of the last rebuild
+        if (d.gen) {  // particles and the ghost particles of the last rebuild
             add("ghost_meta", d.gmeta, 2 * sizeof(int));
             add("ghost_orig", d.gorig, 4 * (size_t)d.gcap);
             add("ghost_vec", d.gvec, 8 * 3 * (size_t)d.gcap);
-            add("ghost_comp", d.comp, 4 * 6 * E);
-            add("ghost_ccnt", d.ccnt, 4 * E);
+            add("ghost_comp", d.comp, 4 * 6 * Pl);
+            add("ghost_ccnt", d.ccnt, 4 * Pl);
+            add("ghost_ecomp", d.ecomp, 4 * 6 * Pl);
+            add("ghost_eccnt", d.eccnt, 4 * E);
             add("ghost_px", d.px, 8 * 3 * S);
+            add("part_key", d.pkey, 4 * S);
+            add("part_cen", d.pcen, 8 * 3 * S);
+            add("dem_size", d.esize, 4 * E);
         }
-        add("nbr", d.nbr, 4 * E * hb::NBR_CAP);
-        add("nbr_cnt", d.nbr_cnt, 4 * E);
-        add("wall_of", d.wall_of, 4 * E);
-        add("obj", d.obj, 4 * E * hb::OBJ_CAP);
-        add("obj_cnt", d.obj_cnt, 4 * E);
+        add("nbr", d.nbr, 4 * Pl * hb::NBR_CAP);
+        add("nbr_cnt", d.nbr_cnt, 4 * Pl);
+        add("wall_of", d.wall_of, 4 * Pl);
+        add("obj", d.obj, 4 * Pl * hb::OBJ_CAP);
+        add("obj_cnt", d.obj_cnt, 4 * Pl);
         add("dem_scal", d.scal, 8 * 8);
         add("contacts", d.contacts, 4);
-        add("cyl_of", d.cyl_of, 4 * E);
-        add("wrec", d.wrec, 8 * 7 * E);
-        add("orec", d.orec, 8 * 7 * E * hb::OBJ_CAP);
+        add("cyl_of", d.cyl_of, 4 * Pl);
+        add("wrec", d.wrec, 8 * 7 * Pl);
+        add("orec", d.orec, 8 * 7 * Pl * hb::OBJ_CAP);
         add("react", d.react, 8 * 3 * ((size_t)hb::MAX_WALLS + d.O));
     }
     if (d.O) {
@@ -197,6 +204,7 @@ int hb_checkpoint_load(const char* path, hb_ctx** out) {
     };
     const int E = (int)h.E, O = (int)h.O;
     std::vector<double> rad, x0, x1, w0, q0, ox0, ox1, orad;
+    std::vector<int32_t> esz;
     hb_elements el = {};
     hb_objects ob = {};
     if (E > 0) {
@@ -212,6 +220,11 @@ int hb_checkpoint_load(const char* path, hb_ctx** out) {
         rad = field((size_t)DEM_FIELDS - 1, 1);
         el.count = E;
         el.radius = rad.data(); el.x0 = x0.data(); el.x1 = x1.data(); el.w0 = w0.data(); el.q0 = q0.data();
+        if (const std::vector<char>* sz = find("dem_size")) {  // multi-sphere elements
+            if (sz->size() != 4 * (size_t)E) return err(HB_ERR_ARG, "checkpoint element sizes of another count");
+            esz.assign(reinterpret_cast<const int32_t*>(sz->data()), reinterpret_cast<const int32_t*>(sz->data()) + E);
+            el.size = esz.data();
+        }
     }
     int Ot = 0;  // objects including the periodic images the loader's init appends again
     if (O > 0) {
@@ -274,8 +287,8 @@ int hb_checkpoint_load(const char* path, hb_ctx** out) {
 }
 
 // IO::exportRecycleParticles (IO.cpp:486-535): element count, then per element index,
-// size, radius, x0, x1, w0, q0, q1 with default stream formatting (no periodic boxes:
-// moving particles with periodic faces are not supported by this library).
+// size, radius, x0 (moved back into the box through the periodic faces), x1, w0, q0, q1
+// with default stream formatting.
 int hb_write_recycle_particles(hb_ctx* c, const char* path) {
     if (!c || !path || !c->initialized) return err(HB_ERR_ARG, "null argument or not initialised");
     const int E = c->d.E;
@@ -286,11 +299,26 @@ int hb_write_recycle_particles(hb_ctx* c, const char* path) {
     std::ofstream f(path);
     if (!f) return err(HB_ERR_ARG, std::string("cannot open ") + path);
     f.imbue(std::locale::classic());
+    std::vector<int> esz(E > 0 ? E : 1, 1);
+    if (E > 0 && c->d.esize && cudaMemcpy(esz.data(), c->d.esize, sizeof(int) * E, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return err(HB_ERR_CUDA, "element size download failed");
     f << (size_t)E << "\n";
     auto at = [&](size_t off, int k, int i) { return b[(off + k) * E + i]; };
     for (int i = 0; i < E; ++i) {
-        f << i << " " << 1 << " " << at((size_t)DEM_FIELDS - 1, 0, i) << " ";
-        for (int k = 0; k < 3; ++k) f << at(0, k, i) << " ";   // x0
+        f << i << " " << esz[i] << " " << at((size_t)DEM_FIELDS - 1, 0, i) << " ";
+        double x[3] = {at(0, 0, i), at(0, 1, i), at(0, 2, i)}, pp[3] = {x[0], x[1], x[2]};
+        for (int bb = 0; bb < c->d.npbc; ++bb) {  // pbc planes (utils.cpp:240-245)
+            const double* v = c->d.pbc_v[bb];
+            const double* p1 = c->d.pbc_p[bb];
+            const double nv = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            const double n1[3] = {v[0] / nv, v[1] / nv, v[2] / nv};
+            const double ld = n1[0] * (x[0] - p1[0]) + n1[1] * (x[1] - p1[1]) + n1[2] * (x[2] - p1[2]);
+            const double rd = (-1.0 * n1[0]) * (x[0] - (p1[0] + v[0])) + (-1.0 * n1[1]) * (x[1] - (p1[1] + v[1])) +
+                              (-1.0 * n1[2]) * (x[2] - (p1[2] + v[2]));
+            if (ld < 0.0) for (int k = 0; k < 3; ++k) pp[k] = pp[k] + v[k];
+            if (rd < 0.0) for (int k = 0; k < 3; ++k) pp[k] = pp[k] - v[k];
+        }
+        for (int k = 0; k < 3; ++k) f << pp[k] << " ";   // x0
         for (int k = 0; k < 3; ++k) f << at(3, k, i) << " ";   // x1
         for (int k = 0; k < 3; ++k) f << at(36, k, i) << " ";  // w0
         for (int k = 0; k < 4; ++k) f << at(72, k, i) << " ";  // q0

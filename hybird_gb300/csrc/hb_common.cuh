@@ -120,9 +120,11 @@ struct Particles {          // DEM elements as the coupling sees them (FP64)
     const double* w;        // [3*E] wGlobal
     const double* radius;   // [E]
     const float* pf;        // [12*(E+gcap)] FP32 copy per particle: centre, velocity, wGlobal, pad
-    const int* gorig;       // [gcap] element of ghost particle E + g (periodic faces), else null
-    const double* gvec;     // [3*gcap] its shift
-    int gcap;
+    // per-particle path (periodic faces, multi-sphere elements), else null: element of
+    // every particle and the centre its lever arm is taken from (stride pstride)
+    const int* pkey;
+    const double* pcen;
+    long long pstride;
 };
 
 struct LBArgs {

@@ -60,13 +60,28 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     // periodic faces (DEM.cpp:937-989) and ghost particles (DEM.cpp:1554-1664)
     int npbc = 0;
     double pbc_p[3][3], pbc_v[3][3];
-    int gcap = 0;               // ghost slots: 6 per element (3 faces + 3 corners)
+    int gcap = 0;               // ghost slots: 6 per particle (3 faces + 3 corners)
     int* gmeta = nullptr;       // [0] ghosts of the last rebuild, [1] 1: particle nodes need a re-mark
-    int* gorig = nullptr;       // [gcap] element of each ghost
+    int* gorig = nullptr;       // [gcap] particle each ghost copies
     double* gvec = nullptr;     // [3*gcap] its shift (component-major, stride gcap)
-    int* comp = nullptr;        // [6E] ghost particle indices (E + g) of each element, in creation order
-    int* ccnt = nullptr;        // [E]
-    double* px = nullptr;       // [3*(E+gcap)] particle centres at the last rebuild (stride E+gcap)
+    int* comp = nullptr;        // [6P] ghost particle indices (P + g) of each particle, in creation order
+    int* ccnt = nullptr;        // [P]
+    int* ecomp = nullptr;       // [6P] ghosts of each element (from 6*efirst[e]), in creation order
+    int* eccnt = nullptr;       // [E]
+    double* px = nullptr;       // [3*(P+gcap)] particle centres, corrected (stride P+gcap)
+    // particles (DEM.cpp:222-239): element e owns the P-index range efirst[e] .. efirst[e+1]-1,
+    // one sphere per prototype position (DEM.cpp:404-433); ghosts follow as P + g
+    int P = 0;                  // standard particles
+    int gen = 0;                // 1: periodic faces or multi-sphere elements (per-particle path)
+    int* pkey = nullptr;        // [P+gcap] element of every particle
+    int* efirst = nullptr;      // [E+1]
+    int* esize = nullptr;       // [E] spheres of the element (1..4)
+    double* proto = nullptr;    // [3P] prototype position of each particle, radius units (component-major)
+    double* ppos = nullptr;     // [3(P+gcap)] predicted centre of every particle in the substep
+    double* pvel = nullptr;     // [3(P+gcap)] its velocity (element velocity + spin x radiusVec)
+    double* prv = nullptr;      // [3(P+gcap)] radiusVec: centre - element centre
+    double* pF = nullptr;       // [12P] per-particle FParticle, MParticle, FWall, MWall of the substep
+    double* pcen = nullptr;     // [3(P+gcap)] corrected element centre (+ ghost shift) seen by the coupling
     uint32_t* remark = nullptr; // [N] last covering particle + 1 during a re-mark (LB.cpp:1826-1849)
     // objects
     int O = 0;

@@ -71,6 +71,13 @@ struct DemArgs {
     double pp1[3][3], pp2[3][3], pn1[3][3], pn2[3][3], pv[3][3];
     int *gmeta, *gorig, *comp, *ccnt;
     double *gvec, *px;
+    // per-particle path (periodic faces or multi-sphere elements): P standard particles,
+    // element e owns efirst[e] .. efirst[e+1]-1
+    int P, gen;
+    int *pkey, *ecomp, *eccnt;
+    const int *efirst, *esize;
+    const double* proto;
+    double *ppos, *pvel, *prv, *pF, *pcen;
 };
 
 struct V {
@@ -135,9 +142,9 @@ __device__ double tangential_contact(const DemArgs& a, double vt, double fn, dou
 // outside the table (the reference writes out of bounds there) flags an error.
 __device__ __noinline__ void nl_cells_block(const DemArgs& a) {
     const int E = a.E, nc = a.ncells;
-    const bool per = a.npbc > 0;
-    const int S = per ? E + a.gmeta[0] : E;
-    const long long st = per ? (long long)E + a.gcap : E;
+    const bool per = a.gen != 0;
+    const int S = per ? a.P + a.gmeta[0] : E;
+    const long long st = per ? (long long)a.P + a.gcap : E;
     const double* pos = per ? a.px : a.x0;
     for (int c = threadIdx.x; c < nc; c += blockDim.x) { a.cell_cnt[c] = 0; a.cell_fill[c] = 0; }
     __syncthreads();
@@ -156,7 +163,7 @@ __device__ __noinline__ void nl_cells_block(const DemArgs& a) {
         if (c >= 0) atomicAdd(a.cell_cnt + c, 1);
     }
     if (per)
-        for (int i = threadIdx.x; i < E; i += blockDim.x) a.nbr_cnt[i] = 0;
+        for (int i = threadIdx.x; i < a.P; i += blockDim.x) a.nbr_cnt[i] = 0;
     __syncthreads();
     if (threadIdx.x == 0) {  // exclusive scan (ncells is small: a few thousand)
         int s = 0;
@@ -218,7 +225,8 @@ __device__ __noinline__ void nl_build_one(const DemArgs& a, int i) {
 // (standard particles only, DEM.cpp:1496-1550)
 __device__ __noinline__ void nl_near_one(const DemArgs& a, int i) {
     const int E = a.E;
-    const V xi = ld3(a.x0, E, i);
+    const long long st = (long long)a.P + a.gcap;
+    const V xi = a.gen ? V{a.px[i], a.px[st + i], a.px[2 * st + i]} : ld3(a.x0, E, i);
     const double r2 = a.nebrRange * a.nebrRange;
     int wo = -1;
     for (int w = 0; w < a.nw; ++w) {
@@ -286,15 +294,26 @@ __device__ __forceinline__ int ghost_side(const DemArgs& a, int b, V x) {
     return 0;
 }
 
+// corrected centre of standard particle p (particle::updateCorrected, elmt.cpp:276-290)
+__device__ __forceinline__ V part_pos_corr(const DemArgs& a, int p) {
+    const int E = a.E, e = a.pkey[p];
+    const V x = ld3(a.x0, E, e);
+    if (a.esize[e] <= 1) return x;
+    const V pr{a.proto[p], a.proto[a.P + p], a.proto[2 * a.P + p]};
+    return add(x, mul(a.rad[e], project(pr, ldq(a.q0, E, e))));
+}
+
 // One block: pbcShift (elements whose centre left through a face move by the shift;
-// elmt::translate moves x0 and xp0, elmt.cpp:256-259), then createGhosts: one ghost per
-// (face pair, element) whose centre is within nebrRange of a face, face pairs outer and
-// elements inner, then one corner ghost per two ghosts of the same element, ordered by
-// the first ghost's index and then the second's.  Ghost g is particle E + g, like the
-// reference's particles list; px holds every particle's centre.
+// elmt::translate moves x0 and xp0, elmt.cpp:256-259), the particles from their elements,
+// then createGhosts: one ghost per (face pair, particle) whose centre is within
+// nebrRange of a face, face pairs outer and particles inner, then one corner ghost per
+// two ghosts of the same particle, ordered by the first ghost's index and then the
+// second's.  Ghost g is particle P + g, like the reference's particles list; px holds
+// every particle's centre, and each element lists its ghosts in creation order (the
+// reference appends them to the element's components).
 __device__ __noinline__ void ghosts_block(const DemArgs& a) {
-    const int E = a.E;
-    const long long st = (long long)E + a.gcap;
+    const int E = a.E, P = a.P;
+    const long long st = (long long)P + a.gcap;
     for (int n = threadIdx.x; n < E; n += blockDim.x) {
         V x = ld3(a.x0, E, n), xp = ld3(a.xp0, E, n);
         for (int b = 0; b < a.npbc; ++b) {
@@ -305,31 +324,37 @@ __device__ __noinline__ void ghosts_block(const DemArgs& a) {
         }
         st3(a.x0, E, n, x);
         st3(a.xp0, E, n, xp);
-        a.px[n] = x.x; a.px[st + n] = x.y; a.px[2 * st + n] = x.z;
-        a.ccnt[n] = 0;
+        a.eccnt[n] = 0;
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        const V x = part_pos_corr(a, p);
+        a.px[p] = x.x; a.px[st + p] = x.y; a.px[2 * st + p] = x.z;
+        a.ccnt[p] = 0;
     }
     __syncthreads();
     int total = 0;
     for (int b = 0; b < a.npbc; ++b) {  // face ghosts
-        for (int n0 = 0; n0 < E; n0 += blockDim.x) {
+        for (int n0 = 0; n0 < P; n0 += blockDim.x) {
             const int n = n0 + threadIdx.x;
-            const int sd = n < E ? ghost_side(a, b, V{a.px[n], a.px[st + n], a.px[2 * st + n]}) : 0;
+            const int sd = n < P ? ghost_side(a, b, V{a.px[n], a.px[st + n], a.px[2 * st + n]}) : 0;
             int sum;
             const int k = block_scan(sd != 0, sum);
             if (sd) {
                 const int g = total + k;
                 a.gorig[g] = n;
+                a.pkey[P + g] = a.pkey[n];
                 for (int q = 0; q < 3; ++q) a.gvec[(long long)q * a.gcap + g] = sd > 0 ? a.pv[b][q] : -1.0 * a.pv[b][q];
-                a.comp[6 * n + a.ccnt[n]++] = E + g;
+                a.comp[6 * n + a.ccnt[n]++] = P + g;
             }
             total += sum;
         }
     }
     for (int b1 = 0; b1 < a.npbc; ++b1) {  // corner ghosts
-        for (int n0 = 0; n0 < E; n0 += blockDim.x) {
+        for (int n0 = 0; n0 < P; n0 += blockDim.x) {
             const int n = n0 + threadIdx.x;
             int sd[3] = {0, 0, 0}, cnt = 0;
-            if (n < E) {
+            if (n < P) {
                 const V x{a.px[n], a.px[st + n], a.px[2 * st + n]};
                 for (int b = 0; b < a.npbc; ++b) sd[b] = ghost_side(a, b, x);
                 if (sd[b1])
@@ -342,12 +367,13 @@ __device__ __noinline__ void ghosts_block(const DemArgs& a) {
                 for (int b2 = b1 + 1; b2 < a.npbc; ++b2) {
                     if (!sd[b2]) continue;
                     a.gorig[g] = n;
+                    a.pkey[P + g] = a.pkey[n];
                     for (int q = 0; q < 3; ++q) {
                         const double v1 = sd[b1] > 0 ? a.pv[b1][q] : -1.0 * a.pv[b1][q];
                         const double v2 = sd[b2] > 0 ? a.pv[b2][q] : -1.0 * a.pv[b2][q];
                         a.gvec[(long long)q * a.gcap + g] = v1 + v2;
                     }
-                    a.comp[6 * n + a.ccnt[n]++] = E + g;
+                    a.comp[6 * n + a.ccnt[n]++] = P + g;
                     ++g;
                 }
             }
@@ -357,11 +383,24 @@ __device__ __noinline__ void ghosts_block(const DemArgs& a) {
     __syncthreads();
     for (int g = threadIdx.x; g < total; g += blockDim.x) {  // ghostUpdate (elmt.cpp:292-299)
         const int o = a.gorig[g];
-        for (int q = 0; q < 3; ++q) a.px[q * st + E + g] = a.px[q * st + o] + a.gvec[(long long)q * a.gcap + g];
+        for (int q = 0; q < 3; ++q) a.px[q * st + P + g] = a.px[q * st + o] + a.gvec[(long long)q * a.gcap + g];
+    }
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {  // the element's ghosts, ascending index
+        int* l = a.ecomp + 6 * (long long)a.efirst[e];
+        int n = 0;
+        for (int p = a.efirst[e]; p < a.efirst[e + 1]; ++p)
+            for (int k = 0; k < a.ccnt[p]; ++k) {
+                const int v = a.comp[6 * p + k];
+                int m = n - 1;
+                while (m >= 0 && l[m] > v) { l[m + 1] = l[m]; --m; }
+                l[m + 1] = v;
+                ++n;
+            }
+        a.eccnt[e] = n;
     }
     if (threadIdx.x == 0) {
         a.gmeta[0] = total;
-        a.gmeta[1] = 1;  // newNeighborList: the lattice re-marks its particle nodes
+        a.gmeta[1] = a.npbc > 0;  // newNeighborList (DEM.cpp:1396-1411): the lattice re-marks its particle nodes
     }
     __syncthreads();
 }
@@ -379,11 +418,11 @@ __device__ __forceinline__ void nbr_push(const DemArgs& a, int i, int j) {
 __device__ __noinline__ void nl_pairs_pbc(const DemArgs& a, int p) {
     constexpr int SH[14][3] = {{0, 0, 0}, {1, 0, 0},  {1, 1, 0},  {0, 1, 0},   {-1, 1, 0}, {0, 0, 1},  {1, 0, 1},
                                {1, 1, 1}, {0, 1, 1}, {-1, 1, 1}, {-1, 0, 1}, {-1, -1, 1}, {0, -1, 1}, {1, -1, 1}};
-    const int E = a.E;
-    const long long st = (long long)E + a.gcap;
+    const int P = a.P;
+    const long long st = (long long)P + a.gcap;
     const int c = a.cell_of[p];
     if (c < 0) return;
-    const int ep = p < E ? p : a.gorig[p - E];
+    const int ep = a.pkey[p];
     const V xp{a.px[p], a.px[st + p], a.px[2 * st + p]};
     const double r2 = a.nebrRange * a.nebrRange;
     const unsigned n0 = (unsigned)a.nC0, n1 = (unsigned)a.nC1, n2 = (unsigned)a.nC2;
@@ -400,12 +439,11 @@ __device__ __noinline__ void nl_pairs_pbc(const DemArgs& a, int p) {
         for (int k = a.cell_start[cell1]; k < a.cell_start[cell1 + 1]; ++k) {
             const int q = a.cell_items[k];
             if (s == 0 && !(q < p)) continue;
-            const int eq = q < E ? q : a.gorig[q - E];
-            if (eq == ep) continue;
+            if (a.pkey[q] == ep) continue;  // the same element (cluster)
             const V d = sub(V{a.px[q], a.px[st + q], a.px[2 * st + q]}, xp);
             if (!(nrm2(d) < r2)) continue;
-            if (p < E) nbr_push(a, p, q);
-            if (q < E) nbr_push(a, q, p);
+            if (p < P) nbr_push(a, p, q);
+            if (q < P) nbr_push(a, q, p);
         }
     }
 }
@@ -432,11 +470,10 @@ struct FM {
     V f, m;
 };
 
-// particleParticleCollision with I = lower particle index (DEM.cpp:1801-1900), seen by
-// particle i; eI, eJ are the elements of I and J (a ghost moves with its element)
-__device__ __noinline__ FM pp_contact(const DemArgs& a, int i, int I, int eI, int eJ, V vd, double rI, double rJ,
-                                      V FP, V MP) {
-    const int E = a.E;
+// particleParticleCollision with I = lower index (DEM.cpp:1801-1900), seen by particle i
+__device__ __noinline__ FM pp_contact(const DemArgs& a, int i, int I, int J, V vd, double rI, double rJ, V FP,
+                                      V MP) {
+    const int E = a.E, eI = I, eJ = J;
     const double dist = sqrt(nrm2(vd));
     const double overlap = rI + rJ - dist;
     const V relVel = sub(ld3(a.xp1, E, eJ), ld3(a.xp1, E, eI));
@@ -478,22 +515,26 @@ __device__ __forceinline__ void put_rec(double* rec, double flag, V nf, V tf) {
 }
 
 // wallParticleCollision (DEM.cpp:1902-1982), static walls, effective overlap 2x
+// rvJ: particle centre - element centre (predicted); clu: the element has several
+// spheres (its normal force then has a moment, DEM.cpp:1927-1940)
 __device__ __noinline__ FM wall_contact(const DemArgs& a, V wn, double overlap, V xpv, V wpg, double ri, double mi,
-                                        V FW, V MW, double* rec) {
+                                        V FW, V MW, double* rec, V rvJ = V{0, 0, 0}, bool clu = false) {
     const V relVel = sub(xpv, V{0, 0, 0});
     const double vn = dot(relVel, wn);
     const V nrv = mul(vn, wn);
     const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
     const V nf = mul(fn, wn);
     const V vrJ = mul(-ri, wn);
+    const V cJ = clu ? add(vrJ, rvJ) : vrJ;
     FW = add(FW, nf);
+    if (clu) MW = add(MW, cross(cJ, nf));
     const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
     const double nt = sqrt(nrm2(tang));
     V tfw{0, 0, 0};
     if (nt != 0.0) {
         const double ft = tangential_contact(a, nt, fn, ri, mi, a.muWall);
         tfw = mul(ft, divs(tang, nt));
-        MW = sub(MW, cross(vrJ, tfw));
+        MW = sub(MW, cross(cJ, tfw));
         FW = sub(FW, tfw);
     }
     put_rec(rec, nt != 0.0 ? 2.0 : 1.0, nf, tfw);  // wallI->FParticle (DEM.cpp:1946, 1977)
@@ -502,7 +543,8 @@ __device__ __noinline__ FM wall_contact(const DemArgs& a, V wn, double overlap, 
 
 // objectParticleCollision (DEM.cpp:2060-2136), effective overlap 2x, particle friction
 __device__ __noinline__ FM object_contact(const DemArgs& a, int o, V vd, double dist, double overlap, V xpv, V wpg,
-                                          double ri, double mi, V FW, V MW, double* rec) {
+                                          double ri, double mi, V FW, V MW, double* rec, V rvJ = V{0, 0, 0},
+                                          bool clu = false) {
     const V en = mul(1.0 / dist, vd);
     const V relVel = sub(xpv, V{a.ox1[o], a.ox1[a.O + o], a.ox1[2 * a.O + o]});
     const double vn = dot(relVel, en);
@@ -510,8 +552,9 @@ __device__ __noinline__ FM object_contact(const DemArgs& a, int o, V vd, double 
     const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
     const V nf = mul(fn, en);
     const V vrJ = mul(-ri, en);
-    const V cJ = add(vrJ, V{0, 0, 0});
+    const V cJ = add(vrJ, rvJ);
     FW = add(FW, nf);
+    if (clu) MW = add(MW, cross(cJ, nf));
     const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
     const double nt = sqrt(nrm2(tang));
     V tfo{0, 0, 0};
@@ -528,7 +571,7 @@ __device__ __noinline__ FM object_contact(const DemArgs& a, int o, V vd, double 
 // cylinderParticleCollision (DEM.cpp:1984-2058): effective overlap 2x, wall friction; the
 // contact point moves with the cylinder (cylinder::getSpeed, utils.cpp:106-120)
 __device__ __noinline__ FM cylinder_contact(const DemArgs& a, int c, V xpi, double overlap, V xpv, V wpg, double ri,
-                                            double mi, V FW, V MW) {
+                                            double mi, V FW, V MW, V rvJ = V{0, 0, 0}, bool clu = false) {
     const V p1{a.cp1[c][0], a.cp1[c][1], a.cp1[c][2]};
     const V nx{a.cnax[c][0], a.cnax[c][1], a.cnax[c][2]};
     // cylinder::vecDist (utils.cpp:69-82)
@@ -548,8 +591,9 @@ __device__ __noinline__ FM cylinder_contact(const DemArgs& a, int c, V xpi, doub
     const double fn = normal_contact(a, 2.0 * overlap, vn, ri, mi);
     const V nf = mul(fn, en);
     const V vrJ = mul(-ri, en);
-    const V cJ = add(vrJ, V{0, 0, 0});  // + (particle centre - element centre), zero for spheres
+    const V cJ = add(vrJ, rvJ);  // + (particle centre - element centre), zero for spheres
     FW = add(FW, nf);
+    if (clu) MW = add(MW, cross(cJ, nf));
     const V tang = sub(add(relVel, cross(wpg, vrJ)), nrv);
     const double nt = sqrt(nrm2(tang));
     if (nt != 0.0) {
@@ -573,25 +617,13 @@ __device__ void forces_warp(const DemArgs& a, const DemArgs& ga, int i, int lane
     for (int k = lane; k < cnt; k += 32) {
         const int j = a.nbr[(long long)i * NBR_CAP + k];
         const int I = min(i, j), J = max(i, j);
-        // a ghost partner (J = E + g) sits at its element's predicted centre plus its shift
-        // (particle::ghostUpdate, elmt.cpp:292-299); only i's side takes the force
-        // (DEM.cpp:1845-1858, 1879-1888)
-        int eJ = J;
-        V xJ;
-        if (J >= E) {
-            const int g = J - E;
-            eJ = a.gorig[g];
-            xJ = add(ld3(a.xp0, E, eJ), V{a.gvec[g], a.gvec[a.gcap + g], a.gvec[2 * a.gcap + g]});
-        } else {
-            xJ = ld3(a.xp0, E, J);
-        }
-        const double rI = a.rad[I], rJ = a.rad[eJ];
+        const double rI = a.rad[I], rJ = a.rad[J];
         const double sig = rI + rJ;
-        const V vd = sub(xJ, ld3(a.xp0, E, I));
+        const V vd = sub(ld3(a.xp0, E, J), ld3(a.xp0, E, I));
         if (!(nrm2(vd) < sig * sig)) continue;
         if (i < j) ++ncont;
         contrib = true;
-        const FM r = pp_contact(ga, i, I, I, eJ, vd, rI, rJ, FP, MP);
+        const FM r = pp_contact(ga, i, I, J, vd, rI, rJ, FP, MP);
         FP = r.f;
         MP = r.m;
     }
@@ -660,6 +692,171 @@ __device__ void forces_warp(const DemArgs& a, const DemArgs& ga, int i, int lane
     st3(a.MW, E, i, V{v[9], v[10], v[11]});
 }
 
+// ---- per-particle path (periodic faces, multi-sphere elements) ---------------------------
+
+__device__ __forceinline__ V pv3(const double* arr, long long st, int q) { return V{arr[q], arr[st + q], arr[2 * st + q]}; }
+
+// predicted state of particle p for this substep (particle::updatePredicted and
+// ghostUpdate, elmt.cpp:261-274, 292-299): centre, velocity, radiusVec
+__device__ __noinline__ void part_predict(const DemArgs& a, int p) {
+    const int E = a.E, P = a.P;
+    const long long st = (long long)P + a.gcap;
+    const int o = p < P ? p : a.gorig[p - P];
+    const int e = a.pkey[o];
+    V x = ld3(a.xp0, E, e), v = ld3(a.xp1, E, e), rv{0, 0, 0};
+    if (a.esize[e] > 1) {
+        const V pr{a.proto[o], a.proto[P + o], a.proto[2 * P + o]};
+        x = add(x, mul(a.rad[e], project(pr, ldq(a.qp0, E, e))));
+        rv = sub(x, ld3(a.xp0, E, e));
+        v = add(v, cross(ld3(a.wpG, E, e), rv));
+    }
+    if (p >= P) {
+        const int g = p - P;
+        x = add(x, V{a.gvec[g], a.gvec[a.gcap + g], a.gvec[2 * a.gcap + g]});
+    }
+    a.ppos[p] = x.x; a.ppos[st + p] = x.y; a.ppos[2 * st + p] = x.z;
+    a.pvel[p] = v.x; a.pvel[st + p] = v.y; a.pvel[2 * st + p] = v.z;
+    a.prv[p] = rv.x; a.prv[st + p] = rv.y; a.prv[2 * st + p] = rv.z;
+}
+
+// particleParticleCollision (DEM.cpp:1801-1900) between particles I < J of elements eI, eJ,
+// seen by particle `self` (I or J): particle velocities include the element spin, the
+// lever arms include radiusVec, and the normal force has a moment on multi-sphere
+// elements.  Only standard particles take forces (a ghost's copy acts on its own side).
+__device__ __noinline__ FM pp_contact_gen(const DemArgs& a, bool selfI, int I, int J, int eI, int eJ, V vd, double rI,
+                                          double rJ, V FP, V MP) {
+    const int E = a.E;
+    const long long st = (long long)a.P + a.gcap;
+    const double dist = sqrt(nrm2(vd));
+    const double overlap = rI + rJ - dist;
+    const V relVel = sub(pv3(a.pvel, st, J), pv3(a.pvel, st, I));
+    const V en = divs(vd, dist);
+    const double vn = dot(relVel, en);
+    const V nrv = mul(vn, en);
+    const double mI = a.m[eI], mJ = a.m[eJ];
+    const double effMass = mI * mJ / (mI + mJ);
+    const double effRad = rI * rJ / (rI + rJ);
+    const double fn = normal_contact(a, overlap, vn, effRad, effMass);
+    const V nf = mul(fn, en);
+    const V vrI = mul(rI, en), vrJ = mul(-rJ, en);
+    const V cI = add(vrI, pv3(a.prv, st, I)), cJ = add(vrJ, pv3(a.prv, st, J));
+    if (selfI) {
+        FP = sub(FP, nf);
+        if (a.esize[eI] > 1) MP = sub(MP, cross(cI, nf));
+    } else {
+        FP = add(FP, nf);
+        if (a.esize[eJ] > 1) MP = add(MP, cross(cJ, nf));
+    }
+    const V rvc = add(sub(relVel, cross(ld3(a.wpG, E, eI), vrI)), cross(ld3(a.wpG, E, eJ), vrJ));
+    const V tang = sub(rvc, nrv);
+    const double nt = sqrt(nrm2(tang));
+    if (nt != 0.0) {
+        const double ft = tangential_contact(a, nt, fn, effRad, effMass, a.muPart);
+        const V tf = mul(ft, divs(tang, nt));
+        if (selfI) { MP = add(MP, cross(cI, tf)); FP = add(FP, tf); }
+        else { MP = sub(MP, cross(cJ, tf)); FP = sub(FP, tf); }
+    }
+    return FM{FP, MP};
+}
+
+// contacts of standard particle p by one warp (as forces_warp), into the particle's
+// partial sums; the element sums them over its particles before Newton
+__device__ void forces_gen(const DemArgs& a, const DemArgs& ga, int p, int lane, int& ncont) {
+    const int E = a.E, P = a.P;
+    const long long st = (long long)P + a.gcap;
+    const int e = a.pkey[p];
+    const V xpi = pv3(a.ppos, st, p);
+    V FP{0, 0, 0}, MP{0, 0, 0}, FW{0, 0, 0}, MW{0, 0, 0};
+    bool contrib = false;
+    const int cnt = a.nbr_cnt[p];
+    for (int k = lane; k < cnt; k += 32) {
+        const int j = a.nbr[(long long)p * NBR_CAP + k];
+        const int I = min(p, j), J = max(p, j);
+        const int eI = a.pkey[I], eJ = a.pkey[J];
+        const double rI = a.rad[eI], rJ = a.rad[eJ];
+        const double sig = rI + rJ;
+        const V vd = sub(pv3(a.ppos, st, J), pv3(a.ppos, st, I));
+        if (!(nrm2(vd) < sig * sig)) continue;
+        if (p < j) ++ncont;
+        contrib = true;
+        const FM r = pp_contact_gen(ga, p == I, I, J, eI, eJ, vd, rI, rJ, FP, MP);
+        FP = r.f;
+        MP = r.m;
+    }
+    const double ri = a.rad[e], mi = a.m[e];
+    const V xpv = pv3(a.pvel, st, p);
+    const V wpg = ld3(a.wpG, E, e);
+    const V rv = pv3(a.prv, st, p);
+    const bool clu = a.esize[e] > 1;
+    const int w = a.wall_of[p];
+    if (lane == 0) {
+        bool hit = false;
+        if (w >= 0) {
+            const V wn{a.wn[w][0], a.wn[w][1], a.wn[w][2]};
+            const double dist = dot(wn, sub(xpi, V{a.wp[w][0], a.wp[w][1], a.wp[w][2]}));
+            const double overlap = ri - dist;
+            if (overlap > 0.0) {
+                contrib = hit = true;
+                const FM r = wall_contact(ga, wn, overlap, xpv, wpg, ri, mi, FW, MW, a.wrec + 7 * (long long)p, rv, clu);
+                FW = r.f;
+                MW = r.m;
+            }
+        }
+        if (!hit) a.wrec[7 * (long long)p] = 0.0;
+        const int cy = a.cyl_of[p];
+        if (cy >= 0) {
+            const V d = sub(xpi, V{a.cp1[cy][0], a.cp1[cy][1], a.cp1[cy][2]});
+            const V nx{a.cnax[cy][0], a.cnax[cy][1], a.cnax[cy][2]};
+            const double dist = a.cR[cy] - sqrt(nrm2(sub(mul(dot(d, nx), nx), d)));
+            const double overlap = ri - dist;
+            if (overlap > 0.0) {
+                contrib = true;
+                const FM r = cylinder_contact(ga, cy, xpi, overlap, xpv, wpg, ri, mi, FW, MW, rv, clu);
+                FW = r.f;
+                MW = r.m;
+            }
+        }
+    }
+    const int oc = a.obj_cnt[p];
+    for (int k = lane; k < oc; k += 32) {
+        const int o = a.obj[(long long)p * OBJ_CAP + k];
+        const V vd = sub(xpi, V{a.ox0[o], a.ox0[a.O + o], a.ox0[2 * a.O + o]});
+        const double dist = sqrt(nrm2(vd));
+        const double overlap = ri + a.orad[o] - dist;
+        double* rec = a.orec + 7 * ((long long)p * OBJ_CAP + k);
+        if (!(overlap > 0.0)) {
+            rec[0] = 0.0;
+            continue;
+        }
+        contrib = true;
+        const FM r = object_contact(ga, o, vd, dist, overlap, xpv, wpg, ri, mi, FW, MW, rec, rv, clu);
+        FW = r.f;
+        MW = r.m;
+    }
+    const unsigned who = __ballot_sync(0xffffffffu, contrib);
+    double v[12] = {FP.x, FP.y, FP.z, MP.x, MP.y, MP.z, FW.x, FW.y, FW.z, MW.x, MW.y, MW.z};
+    if (who & ~1u) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+            for (int c = 0; c < 12; ++c) v[c] += __shfl_xor_sync(0xffffffffu, v[c], off);
+    }
+    if (lane != 0) return;
+#pragma unroll
+    for (int c = 0; c < 12; ++c) a.pF[(long long)c * P + p] = v[c];
+}
+
+// element sums of the particle partials, particles in order: component c of FParticle,
+// MParticle, FWall, MWall (c = 0..11)
+__device__ __forceinline__ void gather_one(const DemArgs& a, int e, int c) {
+    const int E = a.E, P = a.P;
+    const int f = a.efirst[e], l = a.efirst[e + 1];
+    double s = a.pF[(long long)c * P + f];
+    for (int p = f + 1; p < l; ++p) s += a.pF[(long long)c * P + p];
+    double* dst = c < 3 ? a.FP : (c < 6 ? a.MP : (c < 9 ? a.FW : a.MW));
+    dst[(long long)(c % 3) * E + e] = s;
+}
+
 // Newton (DEM.cpp:1149-1181): accelerations from the forces of this substep
 __device__ void newton_one(const DemArgs& a, int i) {
     const int E = a.E;
@@ -680,6 +877,12 @@ __device__ void newton_one(const DemArgs& a, int i) {
     const V waBf{(mBf.x + (Iv.y - Iv.z) * wl.y * wl.z) / Iv.x, (mBf.y + (Iv.z - Iv.x) * wl.z * wl.x) / Iv.y,
                  (mBf.z + (Iv.x - Iv.y) * wl.x * wl.y) / Iv.z};
     st3(a.w1, E, i, project(waBf, qp0));
+    if (a.esize && a.esize[i] > 1) {  // q2 = 0.5 qp0 quatAcc(waBf, qp1) (DEM.cpp:1176-1179, vector.cpp:500-504)
+        const Qt q1 = ldq(a.qp1, E, i);
+        const double n2 = q1.a * q1.a + q1.b * q1.b + q1.c * q1.c + q1.d * q1.d;
+        const Qt r = qmul(qp0, Qt{-2.0 * n2, waBf.x, waBf.y, waBf.z});
+        stq(a.q2, E, i, Qt{0.5 * r.a, 0.5 * r.b, 0.5 * r.c, 0.5 * r.d});
+    }
 }
 
 // The same for one Cartesian component of an identity-orientation element (lane c of
@@ -983,28 +1186,28 @@ struct CoupleArgs {
     const double* mass;
     int free_surface;
     double *FH, *MH, *fvol;
-    // ghost particles (periodic faces): particle E + g is element gorig[g] shifted by gvec
-    int ghosts, gcap;
+    // per-particle path (periodic faces, multi-sphere elements): P standard particles,
+    // ghost g is particle P + g; pkey gives every particle's element
+    int ghosts, gcap, P;
     int* gmeta;  // [0] ghosts, [1] re-mark pending
-    const int *gorig, *comp, *ccnt;
-    const double* gvec;
+    const int *gorig, *pkey, *efirst, *ecomp, *eccnt;
+    const double *gvec, *px, *pcen;
     uint32_t* remark;
 };
 
-// centre and radius of particle p (an element, or a ghost: its element's centre + shift)
+// centre and radius of particle p (the element itself, or on the per-particle path the
+// corrected particle centre of this cycle)
 __device__ __forceinline__ void part_centre(const CoupleArgs& a, int p, double& cx_, double& cy_, double& cz_,
                                             double& r) {
     const int E = a.E;
-    if (p < E) {
+    if (!a.ghosts) {
         cx_ = a.x0[p]; cy_ = a.x0[E + p]; cz_ = a.x0[2 * E + p];
         r = a.rad[p];
         return;
     }
-    const int g = p - E, o = a.gorig[g];
-    cx_ = a.x0[o] + a.gvec[g];
-    cy_ = a.x0[E + o] + a.gvec[a.gcap + g];
-    cz_ = a.x0[2 * E + o] + a.gvec[2 * a.gcap + g];
-    r = a.rad[o];
+    const long long st = (long long)a.P + a.gcap;
+    cx_ = a.px[p]; cy_ = a.px[st + p]; cz_ = a.px[2 * st + p];
+    r = a.rad[a.pkey[p]];
 }
 
 struct Box {
@@ -1078,15 +1281,30 @@ static_assert(sizeof(PartBox) <= 128, "the context allocates 128 bytes per parti
 
 __device__ __forceinline__ void build_box(const CoupleArgs& a, int p) { a.tab[p].s = load_sph(a, p); }
 
-// FP32 record of ghost particle p for the reduced-precision lattice kernels: its
-// element's velocity and spin, the shifted centre
-__device__ __forceinline__ void ghost_pf(const DemArgs& a, int p) {
-    const int E = a.E, g = p - E, o = a.gorig[g];
+// Per-particle path, positions final: particle p's corrected centre (px, for its
+// sphere), the centre of its element as the coupling sees it (pcen: the element's
+// corrected centre, plus the shift for a ghost -- the lever arm of LB.cpp:1871 is
+// node - particle centre + radiusVec) and its FP32 record (that centre, the element's
+// velocity and spin) for the reduced-precision lattice kernels.
+__device__ __noinline__ void part_state(const DemArgs& a, int p) {
+    const int E = a.E, P = a.P;
+    const long long st = (long long)P + a.gcap;
+    const int o = p < P ? p : a.gorig[p - P];
+    const int e = a.pkey[o];
+    V x = part_pos_corr(a, o), c = ld3(a.x0, E, e);
+    if (p >= P) {
+        const int g = p - P;
+        const V sh{a.gvec[g], a.gvec[a.gcap + g], a.gvec[2 * a.gcap + g]};
+        x = add(x, sh);
+        c = add(c, sh);
+    }
+    a.px[p] = x.x; a.px[st + p] = x.y; a.px[2 * st + p] = x.z;
+    a.pcen[p] = c.x; a.pcen[st + p] = c.y; a.pcen[2 * st + p] = c.z;
     float* q = a.pf + 12 * (size_t)p;
+    q[0] = (float)c.x; q[1] = (float)c.y; q[2] = (float)c.z;
     for (int k = 0; k < 3; ++k) {
-        q[k] = (float)(a.x0[(long long)k * E + o] + a.gvec[(long long)k * a.gcap + g]);
-        q[3 + k] = (float)a.x1[(long long)k * E + o];
-        q[6 + k] = (float)a.wG[(long long)k * E + o];
+        q[3 + k] = (float)a.x1[(long long)k * E + e];
+        q[6 + k] = (float)a.wG[(long long)k * E + e];
     }
 }
 
@@ -1095,13 +1313,13 @@ __device__ __forceinline__ void ghost_pf(const DemArgs& a, int p) {
 // LB.cpp:1937-1953, 1984-2001): the first that covers it, or -1
 __device__ __forceinline__ int cover_first(const CoupleArgs& a, uint32_t q, int x, int y, int z) {
     if (!a.ghosts) return in_sph(a.tab[q].s, x, y, z) ? (int)q : -1;
-    const int e = (int)q < a.E ? (int)q : a.gorig[(int)q - a.E];
-    if (in_sph(a.tab[e].s, x, y, z)) return e;
-    const int n = a.ccnt[e];
-    for (int k = 0; k < n; ++k) {
-        const int g = a.comp[6 * e + k];
-        if (in_sph(a.tab[g].s, x, y, z)) return g;
-    }
+    const int e = a.pkey[q];
+    for (int p = a.efirst[e]; p < a.efirst[e + 1]; ++p)
+        if (in_sph(a.tab[p].s, x, y, z)) return p;
+    const int n = a.eccnt[e];
+    const int* l = a.ecomp + 6 * (long long)a.efirst[e];
+    for (int k = 0; k < n; ++k)
+        if (in_sph(a.tab[l[k]].s, x, y, z)) return l[k];
     return -1;
 }
 
@@ -1249,13 +1467,20 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
 __device__ __noinline__ void reduce_block(const CoupleArgs& a, int p0, double (*sh)[256]) {
     const int E = a.E;
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-    // the element's own sphere, then its ghosts (nodes carry the particle that covers them)
-    const int ncomp = a.ghosts ? 1 + a.ccnt[p0] : 1;
+    // the element's particles, then its ghosts (nodes carry the particle that covers
+    // them); the lever arm is taken from the element's centre (+ the ghost's shift)
+    const int nstd = a.ghosts ? a.efirst[p0 + 1] - a.efirst[p0] : 1;
+    const int ncomp = a.ghosts ? nstd + a.eccnt[p0] : 1;
     for (int kc = 0; kc < ncomp; ++kc) {
-    const int p = kc == 0 ? p0 : a.comp[6 * p0 + kc - 1];
+    const int p = !a.ghosts ? p0 : (kc < nstd ? a.efirst[p0] + kc : a.ecomp[6 * (long long)a.efirst[p0] + kc - nstd]);
     const Box b = pbox(a, p, 1);
-    double px, py, pz, pr;
-    part_centre(a, p, px, py, pz, pr);
+    double px, py, pz;
+    if (a.ghosts) {
+        const long long st = (long long)a.P + a.gcap;
+        px = a.pcen[p]; py = a.pcen[st + p]; pz = a.pcen[2 * st + p];
+    } else {
+        px = a.x0[p]; py = a.x0[E + p]; pz = a.x0[2 * E + p];
+    }
     for (int r = threadIdx.x; r < b.ny * b.nz; r += blockDim.x) {
         const int y = b.y0 + r % b.ny, z = b.z0 + r / b.ny;
         const long long base = (long long)a.X * ((long long)y + (long long)a.Y * z);
@@ -1333,8 +1558,8 @@ __global__ void k_convert_sums(CoupleArgs a) {
 //   R  hydrodynamic force of every element from the previous lattice step
 //   D  multiStep DEM substeps: [neighbour rebuild] forces | correct + next predict +
 //      displacement trigger
-constexpr size_t GARGS_COUPLE = 2048;  // byte offset of the CoupleArgs copy in the parameter buffer
-constexpr size_t GARGS_BYTES = 4096;
+constexpr size_t GARGS_COUPLE = 2560;  // byte offset of the CoupleArgs copy in the parameter buffer
+constexpr size_t GARGS_BYTES = 4608;
 
 struct CycleArgs {
     DemArgs d;
@@ -1372,29 +1597,36 @@ __device__ __forceinline__ void warp_tasks(int& first, int& stride) {
 
 // neighbour rebuild with periodic faces (DEM.cpp:1395-1494) by the whole cooperative
 // grid, out of line so that its registers do not count against the substep loop
-__device__ __noinline__ void rebuild_pbc(const DemArgs* gd, int E, int gt, int gs) {
+__device__ __noinline__ void rebuild_pbc(const DemArgs* gd, int gt, int gs) {
     cg::grid_group grid = cg::this_grid();
     if (blockIdx.x == 0) {
         ghosts_block(*gd);
         nl_cells_block(*gd);
     }
     grid.sync();
-    const int S = E + *(volatile int*)gd->gmeta;
+    const int P = gd->P;
+    const int S = P + *(volatile int*)gd->gmeta;
     for (int p = gt; p < S; p += gs) nl_pairs_pbc(*gd, p);
     grid.sync();
-    for (int i = gt; i < E; i += gs) {
+    for (int i = gt; i < P; i += gs) {
         nl_sort_one(*gd, i);
         nl_near_one(*gd, i);
     }
     grid.sync();  // the contact warps read other threads' candidate lists
 }
 
-__device__ __noinline__ void ghost_boxes(const CoupleArgs* gc, const DemArgs* gd, int E) {
-    const int S = E + *(volatile int*)gd->gmeta;
-    for (int p = E + blockIdx.x * blockDim.x + threadIdx.x; p < S; p += gridDim.x * blockDim.x) {
+__device__ __noinline__ void part_boxes(const CoupleArgs* gc, const DemArgs* gd) {
+    const int S = gd->P + *(volatile int*)gd->gmeta;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S; p += gridDim.x * blockDim.x) {
+        part_state(*gd, p);
         build_box(*gc, p);
-        ghost_pf(*gd, p);
     }
+}
+
+// every particle's predicted state for the substep (the contacts read other particles')
+__device__ __noinline__ void part_predict_all(const DemArgs* gd, int gt, int gs) {
+    const int S = gd->P + *(volatile int*)gd->gmeta;
+    for (int p = gt; p < S; p += gs) part_predict(*gd, p);
 }
 
 // PBC: periodic faces with particles (ghost rebuilds); a separate instantiation, so the
@@ -1432,7 +1664,7 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
         for (int s = 0; s < A.multi; ++s) {
             if (rebuild) {
                 if (PBC) {
-                    rebuild_pbc(A.gd, E, gt, gs);
+                    rebuild_pbc(A.gd, gt, gs);
                 } else {
                     if (blockIdx.x == 0) nl_cells_block(*A.gd);
                     grid.sync();
@@ -1441,7 +1673,13 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
                 }
             }
             int ncont = 0;
-            for (int i = gw; i < E; i += nw) forces_warp(A.d, *A.gd, i, lane, ncont);
+            if (PBC) {
+                part_predict_all(A.gd, gt, gs);
+                grid.sync();
+                for (int p = gw; p < A.d.P; p += nw) forces_gen(A.d, *A.gd, p, lane, ncont);
+            } else {
+                for (int i = gw; i < E; i += nw) forces_warp(A.d, *A.gd, i, lane, ncont);
+            }
             if (s == A.multi - 1) {  // overlapping pairs of the last substep (integer atomics)
                 for (int off = 16; off > 0; off >>= 1) ncont += __shfl_down_sync(0xffffffffu, ncont, off);
                 if ((threadIdx.x & 31) == 0 && ncont) {
@@ -1459,6 +1697,14 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
                     const int i = base + grp;
                     const bool on = grp < 5 && i < E;
                     const bool plain = on && A.d.plain[i];
+                    if (PBC && on) {  // element sums of its particles' contact forces
+                        if (plain) {  // the components lane c's Newton reads
+                            gather_one(A.d, i, c);
+                            gather_one(A.d, i, 6 + c);
+                        } else if (c == 0) {
+                            for (int k = 0; k < 12; ++k) gather_one(A.d, i, k);
+                        }
+                    }
                     double x1c = 0.0;
                     if (plain) x1c = correct_predict_plain(A.d, i, c, newton_plain(A.d, i, c));
                     else if (on && c == 0) v2 = fmax(v2, correct_predict_one(*A.gd, i));
@@ -1486,8 +1732,9 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
             }
         }
         if (A.do_boxes) {  // positions are final: boxes for the coupling passes
-            for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) build_box(A.c, p);
-            if (PBC) ghost_boxes(A.gc, A.gd, E);
+            if (PBC) part_boxes(A.gc, A.gd);
+            else
+                for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) build_box(A.c, p);
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             A.d.scal[0] = maxDisp;
@@ -1499,7 +1746,14 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
 // ---- coupling masks: separate full-occupancy kernels, one thread per (particle, row) --
 __global__ void __launch_bounds__(256) k_build_boxes(CoupleArgs a) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < a.E + (a.ghosts ? a.gmeta[0] : 0)) build_box(a, p);
+    if (p < (a.ghosts ? a.P + a.gmeta[0] : a.E)) build_box(a, p);
+}
+
+// per-particle path: particle centres, coupling centres and FP32 records from the
+// element state (before k_build_boxes when the cooperative kernel did not build them)
+__global__ void __launch_bounds__(256) k_part_state(DemArgs a) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < a.P + a.gmeta[0]) part_state(a, p);
 }
 
 // updateIndices (LB.cpp:1826-1849) after a neighbour rebuild with periodic faces:
@@ -1509,7 +1763,7 @@ __global__ void __launch_bounds__(256) k_build_boxes(CoupleArgs a) {
 // one block per particle sweeps its box and keeps the largest index + 1 per node.
 __global__ void __launch_bounds__(256) k_remark_mark(CoupleArgs a) {
     if (!a.gmeta[1]) return;
-    const int S = a.E + a.gmeta[0];
+    const int S = a.P + a.gmeta[0];
     for (int p = blockIdx.x; p < S; p += gridDim.x) {
         const Box b = pbox(a, p, 1);
         const Sph sp = a.tab[p].s;
@@ -1644,6 +1898,11 @@ static DemArgs dem_args(hb_ctx* c) {
     }
     a.gmeta = d.gmeta; a.gorig = d.gorig; a.comp = d.comp; a.ccnt = d.ccnt;
     a.gvec = d.gvec; a.px = d.px;
+    a.P = d.gen ? d.P : d.E;
+    a.gen = d.gen;
+    a.pkey = d.pkey; a.ecomp = d.ecomp; a.eccnt = d.eccnt;
+    a.efirst = d.efirst; a.esize = d.esize; a.proto = d.proto;
+    a.ppos = d.ppos; a.pvel = d.pvel; a.prv = d.prv; a.pF = d.pF; a.pcen = d.pcen;
     return a;
 }
 
@@ -1671,17 +1930,23 @@ static CoupleArgs couple_args(hb_ctx* c) {
     a.mass = c->mass;
     a.free_surface = c->P.free_surface;
     a.FH = c->d.FH; a.MH = c->d.MH; a.fvol = c->d.fvol;
-    a.ghosts = c->d.npbc > 0;
+    a.ghosts = c->d.gen;
     a.gcap = c->d.gcap;
-    a.gmeta = c->d.gmeta; a.gorig = c->d.gorig; a.comp = c->d.comp; a.ccnt = c->d.ccnt;
-    a.gvec = c->d.gvec;
+    a.P = c->d.gen ? c->d.P : c->d.E;
+    a.gmeta = c->d.gmeta; a.gorig = c->d.gorig; a.pkey = c->d.pkey; a.efirst = c->d.efirst;
+    a.ecomp = c->d.ecomp; a.eccnt = c->d.eccnt;
+    a.gvec = c->d.gvec; a.px = c->d.px; a.pcen = c->d.pcen;
     a.remark = c->d.remark;
     return a;
 }
 
+// per-particle path at init: the particles, the ghosts of the initial positions
+// (DEM.cpp:253-257: the neighbour table built at init) and the coupling state
 int launch_ghosts_init(hb_ctx* c) {
-    if (c->d.E == 0 || c->d.npbc == 0) return 0;
-    k_ghosts_init<<<1, 256, 0, c->stream>>>(dem_args(c));
+    if (c->d.E == 0 || !c->d.gen) return 0;
+    const DemArgs a = dem_args(c);
+    k_ghosts_init<<<1, 256, 0, c->stream>>>(a);
+    k_part_state<<<ceil_div(c->d.P + c->d.gcap, 256), 256, 0, c->stream>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -1735,8 +2000,8 @@ int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsign
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (c->d.npbc) {
-        int occ = 0;  // the periodic instantiation must fit the same grid
+    if (c->d.gen) {
+        int occ = 0;  // the per-particle instantiation must fit the same grid
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cycle<true>, 256, 0);
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
@@ -1753,9 +2018,10 @@ int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsign
 void launch_couple(hb_ctx* c, bool build, cudaEvent_t* ev) {
     if (c->d.E == 0) return;
     CoupleArgs a = couple_args(c);
-    if (build) k_build_boxes<<<ceil_div(c->d.E + c->d.gcap, 256), 256, 0, c->stream>>>(a);
+    if (build && c->d.gen) k_part_state<<<ceil_div(c->d.P + c->d.gcap, 256), 256, 0, c->stream>>>(dem_args(c));
+    if (build) k_build_boxes<<<ceil_div(c->d.P + c->d.gcap, 256), 256, 0, c->stream>>>(a);
     if (a.ghosts && a.remark) {  // after a neighbour rebuild (the kernels return at once otherwise)
-        k_remark_mark<<<std::min(c->d.E + c->d.gcap, 152 * 8), 256, 0, c->stream>>>(a);
+        k_remark_mark<<<std::min(c->d.P + c->d.gcap, 152 * 8), 256, 0, c->stream>>>(a);
         k_remark_apply<<<152 * 8, 256, 0, c->stream>>>(a);
     }
     if (ev) cudaEventRecord(ev[0], c->stream);
@@ -1783,10 +2049,10 @@ __global__ void k_reactions(DemArgs a, double* react) {
     const bool wall = t < a.nw;
     const int o = t - a.nw;
     V F{0, 0, 0};
-    for (int base = 0; base < a.E; base += 32) {
+    for (int base = 0; base < a.P; base += 32) {  // particles (= elements for single spheres)
         const int i = base + lane;
         bool hit = false;
-        if (i < a.E) {
+        if (i < a.P) {
             if (wall) {
                 hit = a.wall_of[i] == t && a.wrec[7 * (long long)i] != 0.0;
             } else {

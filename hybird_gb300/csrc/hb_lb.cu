@@ -86,12 +86,10 @@ __global__ void __launch_bounds__(256) k_collide_stream(LBArgs a) {
         int p = (int)a.solid[i];
         const int E = a.parts.count;
         double cxp, cyp, czp;
-        if (p >= E) {  // ghost particle across a periodic face: its element, shifted
-            const int g = p - E;
-            p = a.parts.gorig[g];
-            cxp = a.parts.x0[p] + a.parts.gvec[g];
-            cyp = a.parts.x0[E + p] + a.parts.gvec[a.parts.gcap + g];
-            czp = a.parts.x0[2 * E + p] + a.parts.gvec[2 * a.parts.gcap + g];
+        if (a.parts.pkey) {  // a particle of an element or a ghost: its element's centre (+ shift)
+            const long long st = a.parts.pstride;
+            cxp = a.parts.pcen[p]; cyp = a.parts.pcen[st + p]; czp = a.parts.pcen[2 * st + p];
+            p = a.parts.pkey[p];
         } else {
             cxp = a.parts.x0[p]; cyp = a.parts.x0[E + p]; czp = a.parts.x0[2 * E + p];
         }
@@ -343,14 +341,15 @@ __global__ void k_init_types(InitArgs a, uint8_t* ntype, uint32_t* solid) {
     solid[i] = s;
 }
 
-// particle flags, last particle in list order wins (LB.cpp:475-495).  With periodic
-// faces the list holds the ghosts after the elements: centres from px (stride st),
-// radius of the ghost's element, count E + gmeta[0].
-__global__ void k_init_particles(InitArgs a, const double* x0, long long st, const double* r, int E,
-                                 const int* gorig, const int* gmeta, const uint8_t* ntype, int* owner) {
+// particle flags, last particle in list order wins (LB.cpp:475-495).  On the
+// per-particle path (periodic faces, multi-sphere elements) the list holds the P
+// particles and then the ghosts: centres from px (stride st), radius of the particle's
+// element, count P + gmeta[0].
+__global__ void k_init_particles(InitArgs a, const double* x0, long long st, const double* r, int P,
+                                 const int* pkey, const int* gmeta, const uint8_t* ntype, int* owner) {
     const int p = blockIdx.x;
-    if (gmeta && p >= E + gmeta[0]) return;
-    const double cxp = x0[p], cyp = x0[st + p], czp = x0[2 * st + p], rr = r[p < E ? p : gorig[p - E]];
+    if (gmeta && p >= P + gmeta[0]) return;
+    const double cxp = x0[p], cyp = x0[st + p], czp = x0[2 * st + p], rr = r[pkey ? pkey[p] : p];
     const int x0i = max(0, (int)floor(cxp - rr) - 1), x1i = min(a.X - 1, (int)ceil(cxp + rr) + 1);
     const int y0i = max(0, (int)floor(cyp - rr) - 1), y1i = min(a.Y - 1, (int)ceil(cyp + rr) + 1);
     const int z0i = max(0, (int)floor(czp - rr) - 1), z1i = min(a.Z - 1, (int)ceil(czp + rr) + 1);
@@ -646,9 +645,9 @@ LBArgs lb_args(hb_ctx* c, int cur) {
     a.parts.w = c->d.E ? c->d.wG : nullptr;
     a.parts.radius = c->d.E ? c->d.rad : nullptr;
     a.parts.pf = c->d.E ? c->d.pf : nullptr;
-    a.parts.gorig = c->d.npbc ? c->d.gorig : nullptr;
-    a.parts.gvec = c->d.npbc ? c->d.gvec : nullptr;
-    a.parts.gcap = c->d.gcap;
+    a.parts.pkey = c->d.gen ? c->d.pkey : nullptr;
+    a.parts.pcen = c->d.gen ? c->d.pcen : nullptr;
+    a.parts.pstride = (long long)c->d.P + c->d.gcap;
     a.status = c->status;
     a.wall_part = c->wall_part;
     a.nwalls = c->d.nw;
@@ -670,9 +669,10 @@ int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int 
     if (E > 0) {
         cudaMalloc(&owner, sizeof(int) * c->N);
         cudaMemsetAsync(owner, 0xFF, sizeof(int) * c->N, c->stream);
-        if (c->d.npbc)
-            k_init_particles<<<E + c->d.gcap, 256, 0, c->stream>>>(a, c->d.px, (long long)E + c->d.gcap, el_r, E,
-                                                                    c->d.gorig, c->d.gmeta, c->ntype, owner);
+        if (c->d.gen)
+            k_init_particles<<<c->d.P + c->d.gcap, 256, 0, c->stream>>>(a, c->d.px, (long long)c->d.P + c->d.gcap,
+                                                                         el_r, c->d.P, c->d.pkey, c->d.gmeta,
+                                                                         c->ntype, owner);
         else
             k_init_particles<<<E, 256, 0, c->stream>>>(a, el_x0, E, el_r, E, nullptr, nullptr, c->ntype, owner);
     }

@@ -166,7 +166,7 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
             const float lf = m * inv;
             const float dvx = lf * (ux - lvx), dvy = lf * (uy - lvy), dvz = lf * (uz - lvz);
             hx = -dvx; hy = -dvy; hz = -dvz;
-            key = p < a.parts.count ? p : a.parts.gorig[p - a.parts.count];  // a ghost sums into its element
+            key = a.parts.pkey ? a.parts.pkey[p] : p;  // a particle sums into its element
             v[0] = dvx; v[1] = dvy; v[2] = dvz;  // element F, M, fluidVolume (LB.cpp:1893-1899)
             v[3] = ry * dvz - rz * dvy;
             v[4] = rz * dvx - rx * dvz;

@@ -72,10 +72,10 @@ def check(rc):
 class GpuSim:
     """One simulation context on the current CUDA device."""
 
-    def __init__(self, params, spheres=None, objects=None, cylinders=None):
+    def __init__(self, params, spheres=None, objects=None, cylinders=None, sizes=None, quats=None):
         self.L = lib()
         self.params = params
-        self.arrays = abi.ElementArrays(spheres, objects)
+        self.arrays = abi.ElementArrays(spheres, objects, sizes, quats)
         h = C.c_void_p()
         check(self.L.hb_create(C.byref(params), C.byref(h)))
         self.h = h
@@ -142,7 +142,7 @@ class GpuSim:
         return buf[:2 * n.value]
 
     def ghosts(self):
-        """Ghost particles of the last rebuild: (element index [G], shift [G, 3])."""
+        """Ghost particles of the last rebuild: (particle each copies [G], shift [G, 3])."""
         n = C.c_int64(0)
         check(self.L.hb_download_ghosts(self.h, None, None, 0, C.byref(n)))
         o = np.zeros(max(n.value, 1), np.uint32)

@@ -104,6 +104,9 @@ typedef struct hb_elements {
     const double* x1;          /* [3*count] velocity                                         */
     const double* w0;          /* [3*count] angular velocity                                 */
     const double* q0;          /* [4*count] orientation quaternion (p,q,r,s); NULL = (1,0,0,0) */
+    const int32_t* size;       /* [count] spheres of the element, 1..4, at the prototype
+                                  positions of DEM::compositeProperties (DEM.cpp:404-433);
+                                  NULL = single spheres                                       */
 } hb_elements;
 
 /* Fixed spherical objects (DEM.cpp:129-173 object file row); they become static-wall

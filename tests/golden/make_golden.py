@@ -192,6 +192,19 @@ CASES = {
                  boundary0=4, boundary1=4, boundary2=4, boundary3=4, boundary4=7, boundary5=7),
         spheres=("rsa_periodic", 37, 9, 1.6, 2.2, (0.6, 0.6, 4.0), (16.4, 14.4, 13.0), (16.0, 14.0, 0.0)),
         objects=[], steps=[0, 1, 2, 10, 40, 80, 120], full=[1, 120], vtk=[80]),
+    # multi-sphere elements (DEM.cpp:404-433, elmt.cpp:17-137): clusters of 1-4 spheres
+    # falling onto the floor and onto each other, DEM only
+    "dem_clusters": dict(
+        cfg=dict(lbSizeX=30, lbSizeY=30, lbSizeZ=40, lbSolve=0, lbFX=3e-4, lbFZ=-2e-3, multiStep=20,
+                 boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
+        spheres=("clusters", 41, 12, 1.2, 1.7, (1.0, 1.0, 1.0), (29.0, 29.0, 36.0)),
+        objects=[(15.0, 15.0, 5.0, 3.0)], steps=[0, 1, 30, 60, 100, 150], full=[]),
+    # the same shapes in a fluid with periodic x (ghost copies of cluster spheres)
+    "box_clusters": dict(
+        cfg=dict(lbSizeX=20, lbSizeY=18, lbSizeZ=20, lbFX=8e-4, lbFZ=-8e-4, initVisc=0.1, multiStep=3,
+                 boundary0=4, boundary1=4, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
+        spheres=("clusters", 43, 8, 1.6, 2.0, (0.6, 1.0, 1.0), (19.4, 17.0, 17.0)),
+        objects=[], steps=[0, 1, 2, 10, 40, 80], full=[1, 80], vtk=[40]),
     # free-surface dam break (LB.cpp:1492-1804), column x < 0.4 Lx, z < 0.6 Lz
     "dambreak_fs": dict(
         cfg=dict(lbSizeX=20, lbSizeY=8, lbSizeZ=12, lbFZ=-5e-4, initVisc=0.05, freeSurfaceSolve=1,
@@ -207,13 +220,38 @@ def write_cfg(path, cfg):
             fh.write(f"{k} = {v}\n")
 
 
-def write_particles(path, spheres):
+def write_particles(path, spheres, sizes=None, quats=None):
     with open(path, "w") as fh:
         fh.write(f"{len(spheres)}\n")
         for i, (c, r) in enumerate(spheres):
-            vals = [i, 1, repr(r), repr(c[0]), repr(c[1]), repr(c[2]), 0.0, 0.0, 0.0,
-                    0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0]
+            size = 1 if sizes is None else int(sizes[i])
+            q = (1.0, 0.0, 0.0, 0.0) if quats is None else tuple(quats[i])
+            vals = [i, size, repr(r), repr(c[0]), repr(c[1]), repr(c[2]), 0.0, 0.0, 0.0,
+                    0.0, 0.0, 0.0, repr(q[0]), repr(q[1]), repr(q[2]), repr(q[3]), 0.0, 0.0, 0.0, 0.0]
             fh.write(" ".join(str(v) for v in vals) + "\n")
+
+
+def cluster_elements(seed, n, rmin, rmax, lo, hi):
+    """Seeded multi-sphere elements (1 to 4 spheres, DEM.cpp:404-433 prototypes) with
+    random unit orientations, placed so that their bounding spheres (radius 2r) do not
+    overlap."""
+    rng = random.Random(seed)
+    out = []
+    tries = 0
+    while len(out) < n and tries < 200000:
+        tries += 1
+        r = rng.uniform(rmin, rmax)
+        size = 1 + len(out) % 4
+        c = [rng.uniform(lo[k] + 2 * r, hi[k] - 2 * r) for k in range(3)]
+        if any(sum((c[k] - q[k]) ** 2 for k in range(3)) < (2 * r + 2 * rq + 0.3) ** 2 for (q, rq, _, _) in out):
+            continue
+        q = [rng.gauss(0.0, 1.0) for _ in range(4)]
+        nq = sum(v * v for v in q) ** 0.5
+        q = [v / nq for v in q]
+        if q[0] < 0:
+            q = [-v for v in q]
+        out.append((c, r, size, q))
+    return out
 
 
 def write_objects(path, objects):
@@ -249,7 +287,13 @@ def run_case(name, spec):
     cfg = dict(BASE)
     cfg.update(spec["cfg"])
     sizes = (cfg["lbSizeX"], cfg["lbSizeY"], cfg["lbSizeZ"])
-    if spec["spheres"] and spec["spheres"][0] == "rsa_periodic":
+    sizes = quats = None
+    if spec["spheres"] and spec["spheres"][0] == "clusters":
+        els = cluster_elements(*spec["spheres"][1:])
+        spheres = [(c, r) for (c, r, _, _) in els]
+        sizes = [sz for (_, _, sz, _) in els]
+        quats = [q for (_, _, _, q) in els]
+    elif spec["spheres"] and spec["spheres"][0] == "rsa_periodic":
         spheres = rsa_periodic(*spec["spheres"][1:])
     elif spec["spheres"]:
         seed, n, rmin, rmax = spec["spheres"][1:5]
@@ -262,7 +306,7 @@ def run_case(name, spec):
     with tempfile.TemporaryDirectory() as tmp:
         cfg["particleFile"] = os.path.join(tmp, "particles.dat")
         cfg["objectFile"] = os.path.join(tmp, "objects.dat")
-        write_particles(cfg["particleFile"], spheres)
+        write_particles(cfg["particleFile"], spheres, sizes, quats)
         write_objects(cfg["objectFile"], spec["objects"])
         cpath = os.path.join(tmp, "case.cfg")
         write_cfg(cpath, cfg)
@@ -285,6 +329,9 @@ def run_case(name, spec):
     store["params_json"] = np.frombuffer(json.dumps(params).encode(), dtype=np.uint8)
     store["spheres"] = np.array([[c[0], c[1], c[2], r] for (c, r) in spheres], dtype=np.float64).reshape(-1, 4)
     store["objects"] = np.array(spec["objects"], dtype=np.float64).reshape(-1, 4)
+    if sizes is not None:
+        store["sizes"] = np.array(sizes, dtype=np.int32)
+        store["quats"] = np.array(quats, dtype=np.float64).reshape(-1, 4)
     store["steps"] = np.array(spec["steps"], dtype=np.int64)
     lattice = cfg.get("lbSolve", 1) == 1
     for s in snaps:

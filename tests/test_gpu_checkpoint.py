@@ -73,7 +73,10 @@ CASES = {
     "dambreak_fp64": _dambreak,
     "pipe_slip_fp32": _pipe_slip,
     "periodic_fp32": _periodic_box,
+    "clusters_fp64": lambda: (golden_params(load_golden("box_clusters")), load_golden("box_clusters")["spheres"], None),
 }
+# multi-sphere elements: sizes and orientations of the box_clusters fixture
+SHAPES = {"clusters_fp64": "box_clusters"}
 CYL = {"pipe_slip_fp32": [(0.0, 9.5, 9.7, 1.0, 9.5, 9.7, 8.3)]}
 
 
@@ -82,7 +85,11 @@ CYL = {"pipe_slip_fp32": [(0.0, 9.5, 9.7, 1.0, 9.5, 9.7, 8.3)]}
 def test_restart_continues_bit_identically(name, k1, k2):
     p, sph, obj = CASES[name]()
     G = _gpu()
-    a = G(p, sph, obj, cylinders=CYL.get(name))
+    extra = {}
+    if name in SHAPES:
+        dd = load_golden(SHAPES[name])
+        extra = dict(sizes=dd["sizes"], quats=dd["quats"])
+    a = G(p, sph, obj, cylinders=CYL.get(name), **extra)
     a.cycle(k1)
     with tempfile.TemporaryDirectory() as tmp:
         path = os.path.join(tmp, "state.hbck")
@@ -104,11 +111,13 @@ def test_restart_continues_bit_identically(name, k1, k2):
     b.close()
 
 
-@pytest.mark.parametrize("name,step,late", [("box_spheres", 30, False), ("dem_objects", 50, False)])
+@pytest.mark.parametrize("name,step,late", [("box_spheres", 30, False), ("dem_objects", 50, False),
+                                            ("box_periodic", 80, False), ("box_clusters", 40, False)])
 def test_recycle_file_matches_reference(name, step, late):
     d = load_golden(name)
     p = golden_params(d, gas_box=golden_gasbox(name))
-    g = _gpu()(p, d["spheres"], d["objects"])
+    extra = dict(sizes=d["sizes"], quats=d["quats"]) if "sizes" in d.files else {}
+    g = _gpu()(p, d["spheres"], d["objects"], **extra)
     g.cycle(step)
     ref = bytes(d[f"s{step}_recycle"]).decode()
     with tempfile.TemporaryDirectory() as tmp:

@@ -86,11 +86,12 @@ def _vtk_tokens_match(ours, ref):
 
 
 @pytest.mark.parametrize("name,step", [("channel_bingham_smag", 10), ("box_spheres", 30), ("dambreak_fs", 60),
-                                       ("pipe_curved", 30), ("box_periodic", 80)])
+                                       ("pipe_curved", 30), ("box_periodic", 80), ("box_clusters", 40)])
 def test_vtk_fluid_file_matches_reference(name, step):
     d = load_golden(name)
     p = golden_params(d, gas_box=golden_gasbox(name))
-    g = _gpu()(p, d["spheres"], d["objects"], cylinders=golden_cylinders(d))
+    extra = dict(sizes=d["sizes"], quats=d["quats"]) if "sizes" in d.files else {}
+    g = _gpu()(p, d["spheres"], d["objects"], cylinders=golden_cylinders(d), **extra)
     g.cycle(step)
     ref = bytes(d[f"s{step}_vtk"]).decode()
     with tempfile.TemporaryDirectory() as tmp:
