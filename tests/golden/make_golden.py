@@ -193,12 +193,13 @@ CASES = {
         spheres=("rsa_periodic", 37, 9, 1.6, 2.2, (0.6, 0.6, 4.0), (16.4, 14.4, 13.0), (16.0, 14.0, 0.0)),
         objects=[], steps=[0, 1, 2, 10, 40, 80, 120], full=[1, 120], vtk=[80]),
     # multi-sphere elements (DEM.cpp:404-433, elmt.cpp:17-137): clusters of 1-4 spheres
-    # falling onto the floor and onto each other, DEM only
+    # falling onto the floor, a fixed object and each other, DEM only; kept > nebrRange
+    # from the side walls (first wall in range only, DEM.cpp:1502-1511)
     "dem_clusters": dict(
-        cfg=dict(lbSizeX=30, lbSizeY=30, lbSizeZ=40, lbSolve=0, lbFX=3e-4, lbFZ=-2e-3, multiStep=20,
+        cfg=dict(lbSizeX=40, lbSizeY=40, lbSizeZ=40, lbSolve=0, lbFX=3e-4, lbFZ=-2e-3, multiStep=20,
                  boundary0=7, boundary1=7, boundary2=7, boundary3=7, boundary4=7, boundary5=7),
-        spheres=("clusters", 41, 12, 1.2, 1.7, (1.0, 1.0, 1.0), (29.0, 29.0, 36.0)),
-        objects=[(15.0, 15.0, 5.0, 3.0)], steps=[0, 1, 30, 60, 100, 150], full=[]),
+        spheres=("clusters", 41, 12, 1.2, 1.7, (6.5, 6.5, 1.0), (33.0, 33.0, 38.0)),
+        objects=[(20.0, 20.0, 5.0, 3.0)], steps=[0, 1, 30, 60, 100, 150], full=[]),
     # the same shapes in a fluid with periodic x (ghost copies of cluster spheres)
     "box_clusters": dict(
         cfg=dict(lbSizeX=20, lbSizeY=18, lbSizeZ=20, lbFX=8e-4, lbFZ=-8e-4, initVisc=0.1, multiStep=3,
