@@ -123,8 +123,9 @@ struct Wall {  // utils.h:18-82, built by DEM::initializeWalls (DEM.cpp:435-633)
     }
 };
 
-struct Elmt {  // elmt.h:53-135 (single-sphere elements)
+struct Elmt {  // elmt.h:53-135
     double radius, m;
+    int size;
     V3 I;
     V3 x0, x1, x2, x3, x4, x5, xp0, xp1, xp2, xp3, xp4, xp5;
     Quat q0, q1, q2, q3, q4, q5, qp0, qp1, qp2, qp3, qp4, qp5;
@@ -132,9 +133,43 @@ struct Elmt {  // elmt.h:53-135 (single-sphere elements)
     V3 wGlobal, wLocal, wpGlobal, wpLocal;
     V3 FHydro, FParticle, FWall, MHydro, MParticle, MWall;
     double fluidVolume;
-    // particle view (particle::updatePredicted/Corrected, elmt.cpp:261-290)
-    V3 px0, px1;
 };
+
+struct Part {  // particle (elmt.h:137-187): one sphere of an element, or a ghost copy of one
+    unsigned cluster;
+    int proto;
+    double r;
+    V3 x0, x1, radiusVec;
+};
+
+struct Ghost {  // elmt.h:189-197
+    unsigned index;
+    V3 vec;
+};
+
+struct Pbc {  // utils.h:144-163: base point, shift and the two planes (pbc::setPlanes)
+    V3 p, v;
+    V3 p1, n1, p2, n2;
+    double dist1(V3 x) const { return dot(n1, sub(x, p1)); }
+    double dist2(V3 x) const { return dot(n2, sub(x, p2)); }
+};
+
+// prototypes of the multi-sphere elements, radius units (DEM::compositeProperties,
+// DEM.cpp:404-433; "-1/2" there is an integer division)
+V3 prototype(int size, int k) {
+    if (size == 2) return k == 0 ? v3(0.5, 0.0, 0.0) : v3(-0.5, 0.0, 0.0);
+    if (size == 3) {
+        if (k == 0) return v3(0.0, 1.0, 0.0);
+        return k == 1 ? v3(-std::sqrt(3.0) / 2, -1 / 2, 0.0) : v3(std::sqrt(3.0) / 2, -1 / 2, 0.0);
+    }
+    if (size == 4) {
+        if (k == 0) return v3(0.0, 0.0, 1.0);
+        if (k == 1) return v3(0.0, 2.0 * std::sqrt(2.0) / 3.0, -1.0 / 3.0);
+        if (k == 2) return v3(2.0 * std::sqrt(6.0) / 6.0, -2.0 * std::sqrt(2.0) / 6.0, -1.0 / 3.0);
+        return v3(-2.0 * std::sqrt(6.0) / 6.0, -2.0 * std::sqrt(2.0) / 6.0, -1.0 / 3.0);
+    }
+    return v3(0.0, 0.0, 0.0);
+}
 
 struct Cyl {  // utils.h:85-110 (cylinder), initAxes utils.cpp:154-161
     V3 p1, p2, naxes, omega;
@@ -208,6 +243,13 @@ struct hbo_sim {
     double totalMass;
     // DEM
     std::vector<Elmt> el;
+    std::vector<Part> parts;                   // standard particles, then ghosts
+    unsigned stdParticles = 0;
+    std::vector<std::vector<unsigned>> comps;  // per element: its particles, ghosts appended
+    std::vector<Pbc> pbcs;
+    std::vector<Ghost> ghosts;
+    unsigned stdObjects = 0;
+    bool newNeighborList = false;
     std::vector<Object> obj;
     std::vector<Wall> walls;
     std::vector<Cyl> cyl;
@@ -315,10 +357,10 @@ bool buildLattice(hbo_sim& s, const hb_elements* e, const hb_objects* o) {
         for (int j = 1; j < Q; ++j) s.nb[i * Q + j] = (uint32_t)((int64_t)s.nb[i * Q + j] + pbc[j]);
     }
     // particle flags: last particle in list order containing the node wins (LB.cpp:475-495)
-    if (e) {
-        for (int p = 0; p < e->count; ++p) {
-            const V3 c = v3(e->x0[p], e->x0[e->count + p], e->x0[2 * e->count + p]);
-            const double r = e->radius[p];
+    if (e) {  // every particle, ghosts included (LB.cpp:475-495)
+        for (size_t p = 0; p < s.parts.size(); ++p) {
+            const V3 c = s.parts[p].x0;
+            const double r = s.parts[p].r;
             const int x0 = std::max(0, (int)std::floor(c.x - r) - 1), x1 = std::min(X - 1, (int)std::ceil(c.x + r) + 1);
             const int y0 = std::max(0, (int)std::floor(c.y - r) - 1), y1 = std::min(Y - 1, (int)std::ceil(c.y + r) + 1);
             const int z0 = std::max(0, (int)std::floor(c.z - r) - 1), z1 = std::min(Z - 1, (int)std::ceil(c.z + r) + 1);
@@ -485,16 +527,82 @@ void initNeighborParameters(hbo_sim& s) {  // DEM.cpp:1270-1312
     s.maxDisp = 0.5 * s.nebrRange;
 }
 
+// particle::updatePredicted / updateCorrected (elmt.cpp:261-290) for the standard
+// particles, particle::ghostUpdate (elmt.cpp:292-299) for the ghosts (DEM.cpp:1184-1230)
+void updateParticles(hbo_sim& s, bool predicted) {
+    for (unsigned p = 0; p < s.stdParticles; ++p) {
+        Part& q = s.parts[p];
+        const Elmt& e = s.el[q.cluster];
+        q.x0 = predicted ? e.xp0 : e.x0;
+        q.radiusVec = v3(0, 0, 0);
+        q.x1 = predicted ? e.xp1 : e.x1;
+        if (e.size > 1) {
+            q.x0 = add(q.x0, mul(q.r, project(prototype(e.size, q.proto), predicted ? e.qp0 : e.q0)));
+            q.radiusVec = sub(q.x0, predicted ? e.xp0 : e.x0);
+            q.x1 = add(q.x1, cross(predicted ? e.wpGlobal : e.wGlobal, q.radiusVec));
+        }
+    }
+    for (size_t g = 0; g < s.ghosts.size(); ++g) {
+        Part& q = s.parts[s.stdParticles + g];
+        const Part& o = s.parts[s.ghosts[g].index];
+        q.x0 = add(o.x0, s.ghosts[g].vec);
+        q.radiusVec = o.radiusVec;
+        q.x1 = o.x1;
+    }
+}
+
+void pbcShift(hbo_sim& s) {  // DEM.cpp:1554-1584 (elmt::translate moves x0 and xp0)
+    for (const Pbc& b : s.pbcs)
+        for (auto& e : s.el) {
+            const double ld = b.dist1(e.x0), rd = b.dist2(e.x0);
+            if (ld < 0.0) { e.x0 = add(e.x0, b.v); e.xp0 = add(e.xp0, b.v); }
+            if (rd < 0.0) { const V3 mv = mul(-1.0, b.v); e.x0 = add(e.x0, mv); e.xp0 = add(e.xp0, mv); }
+        }
+}
+
+void createGhosts(hbo_sim& s) {  // DEM.cpp:1586-1664
+    s.ghosts.clear();
+    for (const Pbc& b : s.pbcs)
+        for (size_t n = 0; n < s.el.size(); ++n)
+            for (unsigned j = 0; j < (unsigned)s.el[n].size; ++j) {
+                const unsigned p = s.comps[n][j];
+                if (b.dist1(s.parts[p].x0) < s.nebrRange) s.ghosts.push_back(Ghost{p, b.v});
+                else if (b.dist2(s.parts[p].x0) < s.nebrRange) s.ghosts.push_back(Ghost{p, mul(-1.0, b.v)});
+            }
+    const size_t ns = s.ghosts.size();
+    for (size_t g1 = 0; g1 < ns; ++g1)
+        for (size_t g2 = g1 + 1; g2 < ns; ++g2)
+            if (s.ghosts[g1].index == s.ghosts[g2].index)
+                s.ghosts.push_back(Ghost{s.ghosts[g1].index, add(s.ghosts[g1].vec, s.ghosts[g2].vec)});
+    s.parts.resize(s.stdParticles);
+    for (size_t n = 0; n < s.el.size(); ++n) s.comps[n].resize(s.el[n].size);
+    for (size_t g = 0; g < s.ghosts.size(); ++g) {
+        Part q = s.parts[s.ghosts[g].index];
+        s.comps[q.cluster].push_back(s.stdParticles + (unsigned)g);
+        s.parts.push_back(q);
+    }
+}
+
 void evalNeighborTable(hbo_sim& s) {  // DEM.cpp:1326-1513 (cell table, half-shell sweep)
     static const int shift[14][3] = {{0, 0, 0},  {1, 0, 0},  {1, 1, 0},  {0, 1, 0},  {-1, 1, 0},
                                      {0, 0, 1},  {1, 0, 1},  {1, 1, 1},  {0, 1, 1},  {-1, 1, 1},
                                      {-1, 0, 1}, {-1, -1, 1}, {0, -1, 1}, {1, -1, 1}};
-    const unsigned P = (unsigned)s.el.size();
+    if (!s.pbcs.empty()) {  // DEM.cpp:1395-1411
+        s.ghosts.clear();
+        s.parts.resize(s.stdParticles);
+        for (size_t n = 0; n < s.el.size(); ++n) s.comps[n].resize(s.el[n].size);
+        pbcShift(s);
+        updateParticles(s, false);
+        createGhosts(s);
+        updateParticles(s, false);
+        s.newNeighborList = true;
+    }
+    const unsigned P = (unsigned)s.parts.size();
     const unsigned nc = s.nCells[0] * s.nCells[1] * s.nCells[2];
     s.cellTable.assign(P + nc, -1);
     s.tableCell.assign(P, 0);
     for (unsigned n = 0; n < P; ++n) {
-        const V3 x = s.el[n].px0;  // linearizePosition, vector.cpp:147-149
+        const V3 x = s.parts[n].x0;  // linearizePosition, vector.cpp:147-149
         const int c = (int)(std::floor(x.x / s.cellWidth[0]) + 1 +
                             s.nCells[0] * (std::floor(x.y / s.cellWidth[1]) + 1 +
                                            (s.nCells[1] * (std::floor(x.z / s.cellWidth[2])) + 1))) +
@@ -527,8 +635,8 @@ void evalNeighborTable(hbo_sim& s) {  // DEM.cpp:1326-1513 (cell table, half-she
                         int n1 = s.cellTable[cell1];
                         while (n1 > -1) {
                             if (cell0 != cell1 || n1 < n0) {
-                                if (n0 != n1) {  // single-sphere clusters: clusterIndex == index
-                                    const V3 r10 = sub(s.el[n1].px0, s.el[n0].px0);
+                                if (s.parts[n0].cluster != s.parts[n1].cluster) {
+                                    const V3 r10 = sub(s.parts[n1].x0, s.parts[n0].x0);
                                     if (norm2(r10) < r2) {
                                         s.neighborTable.push_back((uint32_t)n0);
                                         s.neighborTable.push_back((uint32_t)n1);
@@ -540,25 +648,26 @@ void evalNeighborTable(hbo_sim& s) {  // DEM.cpp:1326-1513 (cell table, half-she
                         n0 = s.cellTable[n0];
                     }
                 }
+    const unsigned Ps = s.stdParticles;
     s.nearWallTable.clear();  // DEM.cpp:1496-1513: first wall in range only
-    for (unsigned n = 0; n < P; ++n)
+    for (unsigned n = 0; n < Ps; ++n)
         for (size_t w = 0; w < s.walls.size(); ++w)
-            if (s.walls[w].dist(s.el[n].px0) < s.nebrRange) {
+            if (s.walls[w].dist(s.parts[n].x0) < s.nebrRange) {
                 s.nearWallTable.push_back(n);
                 s.nearWallTable.push_back((uint32_t)w);
                 break;
             }
     s.nearObjectTable.clear();  // DEM.cpp:1515-1533
-    for (unsigned n = 0; n < P; ++n)
+    for (unsigned n = 0; n < Ps; ++n)
         for (size_t o = 0; o < s.obj.size(); ++o)
-            if (norm2(sub(s.el[n].px0, s.obj[o].x0)) < r2) {
+            if (norm2(sub(s.parts[n].x0, s.obj[o].x0)) < r2) {
                 s.nearObjectTable.push_back(n);
                 s.nearObjectTable.push_back((uint32_t)o);
             }
     s.nearCylinderTable.clear();  // DEM.cpp:1535-1550: first cylinder in range only
-    for (unsigned n = 0; n < P; ++n)
+    for (unsigned n = 0; n < Ps; ++n)
         for (size_t c = 0; c < s.cyl.size(); ++c)
-            if (cylinderDist(s.cyl[c], s.el[n].px0) < s.nebrRange) {
+            if (cylinderDist(s.cyl[c], s.parts[n].x0) < s.nebrRange) {
                 s.nearCylinderTable.push_back(n);
                 s.nearCylinderTable.push_back((uint32_t)c);
                 break;
@@ -589,13 +698,17 @@ double tangentialContact(const hbo_sim& s, double vt, double fn, double effRad, 
     return std::min(gs * vt, fsMax);
 }
 
+// the element sides take forces only from standard particles (DEM.cpp:1845-1858,
+// 1879-1888); the normal force has a moment on multi-sphere elements
 void particleParticleCollision(hbo_sim& s, unsigned i, unsigned j, V3 vd) {  // DEM.cpp:1801-1900
-    Elmt& A = s.el[i];
-    Elmt& B = s.el[j];
-    const double radI = A.radius, radJ = B.radius;
+    const Part& pI = s.parts[i];
+    const Part& pJ = s.parts[j];
+    Elmt& A = s.el[pI.cluster];
+    Elmt& B = s.el[pJ.cluster];
+    const double radI = pI.r, radJ = pJ.r;
     const double distance = norm(vd);
     const double overlap = radI + radJ - distance;
-    const V3 relVel = sub(B.px1, A.px1);
+    const V3 relVel = sub(pJ.x1, pI.x1);
     const V3 en = divs(vd, distance);
     const double normRelVel = dot(relVel, en);
     const V3 normalRelVel = mul(normRelVel, en);
@@ -605,9 +718,16 @@ void particleParticleCollision(hbo_sim& s, unsigned i, unsigned j, V3 vd) {  // 
     const V3 normalForce = mul(fn, en);
     const V3 vecRadI = mul(radI, en);
     const V3 vecRadJ = mul(-radJ, en);
-    const V3 cI = add(vecRadI, v3(0, 0, 0)), cJ = add(vecRadJ, v3(0, 0, 0));
-    A.FParticle = sub(A.FParticle, normalForce);
-    B.FParticle = add(B.FParticle, normalForce);
+    const V3 cI = add(vecRadI, pI.radiusVec), cJ = add(vecRadJ, pJ.radiusVec);
+    const bool stdI = i < s.stdParticles, stdJ = j < s.stdParticles;
+    if (stdI) {
+        A.FParticle = sub(A.FParticle, normalForce);
+        if (A.size > 1) A.MParticle = sub(A.MParticle, cross(cI, normalForce));
+    }
+    if (stdJ) {
+        B.FParticle = add(B.FParticle, normalForce);
+        if (B.size > 1) B.MParticle = add(B.MParticle, cross(cJ, normalForce));
+    }
     const V3 relVelContact = add(sub(relVel, cross(A.wpGlobal, vecRadI)), cross(B.wpGlobal, vecRadJ));
     const V3 tang = sub(relVelContact, normalRelVel);
     const double nt = norm(tang);
@@ -615,26 +735,33 @@ void particleParticleCollision(hbo_sim& s, unsigned i, unsigned j, V3 vd) {  // 
         const double ft = tangentialContact(s, nt, fn, effRad, effMass, s.P.friction_part);
         const V3 et = divs(tang, nt);
         const V3 tf = mul(ft, et);
-        A.MParticle = add(A.MParticle, cross(cI, tf));
-        A.FParticle = add(A.FParticle, tf);
-        B.MParticle = sub(B.MParticle, cross(cJ, tf));
-        B.FParticle = sub(B.FParticle, tf);
+        if (stdI) {
+            A.MParticle = add(A.MParticle, cross(cI, tf));
+            A.FParticle = add(A.FParticle, tf);
+        }
+        if (stdJ) {
+            B.MParticle = sub(B.MParticle, cross(cJ, tf));
+            B.FParticle = sub(B.FParticle, tf);
+        }
     }
 }
 
 void wallParticleCollision(hbo_sim& s, Wall& w, unsigned j, double overlap) {  // DEM.cpp:1902-1982
-    Elmt& B = s.el[j];
-    const double radJ = B.radius;
+    const Part& pJ = s.parts[j];
+    Elmt& B = s.el[pJ.cluster];
+    const double radJ = pJ.r;
     const V3 en = w.n;
-    const V3 relVel = sub(B.px1, w.speed(B.px0));
+    const V3 relVel = sub(pJ.x1, w.speed(pJ.x0));
     const double vn = dot(relVel, en);
     const V3 nrv = mul(vn, en);
     const double fn = normalContact(s, 2.0 * overlap, vn, radJ, B.m);
     const V3 nf = mul(fn, en);
     const V3 vecRadJ = mul(-radJ, en);
-    const V3 cJ = vecRadJ;
+    V3 cJ = vecRadJ;
+    if (B.size > 1) cJ = add(cJ, sub(pJ.x0, B.xp0));
     B.FWall = add(B.FWall, nf);
     w.fparticle = sub(w.fparticle, nf);
+    if (B.size > 1) B.MWall = add(B.MWall, cross(cJ, nf));
     const V3 rvc = add(relVel, cross(B.wpGlobal, vecRadJ));
     const V3 tang = sub(rvc, nrv);
     const double nt = norm(tang);
@@ -649,19 +776,21 @@ void wallParticleCollision(hbo_sim& s, Wall& w, unsigned j, double overlap) {  /
 }
 
 void cylinderParticleCollision(hbo_sim& s, const Cyl& c, unsigned j, double overlap) {  // DEM.cpp:1984-2058
-    Elmt& B = s.el[j];
-    const double radJ = B.radius;
-    const V3 vd = cylinderVecDist(c, B.px0);
-    const V3 cp = sub(B.px0, vd);
+    const Part& pJ = s.parts[j];
+    Elmt& B = s.el[pJ.cluster];
+    const double radJ = pJ.r;
+    const V3 vd = cylinderVecDist(c, pJ.x0);
+    const V3 cp = sub(pJ.x0, vd);
     const V3 en = divs(vd, radJ - overlap);
-    const V3 relVel = sub(B.px1, cylinderSpeed(c, cp));
+    const V3 relVel = sub(pJ.x1, cylinderSpeed(c, cp));
     const double vn = dot(relVel, en);
     const V3 nrv = mul(vn, en);
     const double fn = normalContact(s, 2.0 * overlap, vn, radJ, B.m);
     const V3 nf = mul(fn, en);
     const V3 vecRadJ = mul(-radJ, en);
-    const V3 cJ = add(vecRadJ, sub(B.px0, B.px0));  // + (particle - element centre): spheres
+    const V3 cJ = add(vecRadJ, sub(pJ.x0, B.xp0));
     B.FWall = add(B.FWall, nf);
+    if (B.size > 1) B.MWall = add(B.MWall, cross(cJ, nf));
     const V3 rvc = add(relVel, cross(B.wpGlobal, vecRadJ));
     const V3 tang = sub(rvc, nrv);
     const double nt = norm(tang);
@@ -675,20 +804,22 @@ void cylinderParticleCollision(hbo_sim& s, const Cyl& c, unsigned j, double over
 }
 
 void objectParticleCollision(hbo_sim& s, Object& o, unsigned j, V3 vd) {  // DEM.cpp:2060-2136
-    Elmt& B = s.el[j];
-    const double radJ = B.radius;
+    const Part& pJ = s.parts[j];
+    Elmt& B = s.el[pJ.cluster];
+    const double radJ = pJ.r;
     const double distance = norm(vd);
     const double overlap = radJ + o.r - distance;
     const V3 en = mul(1.0 / distance, vd);
-    const V3 relVel = sub(B.px1, o.x1);
+    const V3 relVel = sub(pJ.x1, o.x1);
     const double vn = dot(relVel, en);
     const V3 nrv = mul(vn, en);
     const double fn = normalContact(s, 2.0 * overlap, vn, radJ, B.m);
     const V3 nf = mul(fn, en);
     const V3 vecRadJ = mul(-radJ, en);
-    const V3 cJ = add(vecRadJ, sub(B.px0, B.xp0));
+    const V3 cJ = add(vecRadJ, sub(pJ.x0, B.xp0));
     B.FWall = add(B.FWall, nf);
     o.fparticle = sub(o.fparticle, nf);
+    if (B.size > 1) B.MWall = add(B.MWall, cross(cJ, nf));
     const V3 rvc = add(relVel, cross(B.wpGlobal, vecRadJ));
     const V3 tang = sub(rvc, nrv);
     const double nt = norm(tang);
@@ -744,9 +875,8 @@ void demSubstep(hbo_sim& s) {  // DEM.cpp:336-374
         e.wp5 = e.w5;
         e.wpGlobal = e.wp0;
         e.wpLocal = project(e.wpGlobal, qadj(e.qp0));
-        e.px0 = e.xp0;  // particle::updatePredicted
-        e.px1 = e.xp1;
     }
+    updateParticles(s, true);
     // forces (DEM.cpp:1114-1182)
     for (auto& e : s.el) {
         e.FParticle = e.FWall = e.MParticle = e.MWall = v3(0, 0, 0);
@@ -755,27 +885,27 @@ void demSubstep(hbo_sim& s) {  // DEM.cpp:336-374
     for (auto& o : s.obj) o.fparticle = v3(0, 0, 0);
     for (size_t k = 0; k < s.neighborTable.size(); k += 2) {  // DEM.cpp:1668-1690
         const unsigned i = s.neighborTable[k], j = s.neighborTable[k + 1];
-        const double sig = s.el[i].radius + s.el[j].radius;
-        const V3 vd = sub(s.el[j].px0, s.el[i].px0);
+        const double sig = s.parts[i].r + s.parts[j].r;
+        const V3 vd = sub(s.parts[j].x0, s.parts[i].x0);
         if (norm2(vd) < sig * sig) particleParticleCollision(s, i, j, vd);
     }
     for (size_t k = 0; k < s.nearWallTable.size(); k += 2) {  // DEM.cpp:1692-1717
         const unsigned j = s.nearWallTable[k];
         Wall& w = s.walls[s.nearWallTable[k + 1]];
-        const double overlap = s.el[j].radius - w.dist(s.el[j].px0);
+        const double overlap = s.parts[j].r - w.dist(s.parts[j].x0);
         if (overlap > 0.0) wallParticleCollision(s, w, j, overlap);
     }
     for (size_t k = 0; k < s.nearObjectTable.size(); k += 2) {  // DEM.cpp:1747-1770
         const unsigned j = s.nearObjectTable[k];
         Object& o = s.obj[s.nearObjectTable[k + 1]];
-        const V3 vd = sub(s.el[j].px0, o.x0);
-        const double overlap = s.el[j].radius + o.r - norm(vd);
+        const V3 vd = sub(s.parts[j].x0, o.x0);
+        const double overlap = s.parts[j].r + o.r - norm(vd);
         if (overlap > 0.0) objectParticleCollision(s, o, j, vd);
     }
     for (size_t k = 0; k < s.nearCylinderTable.size(); k += 2) {  // DEM.cpp:1719-1746
         const unsigned j = s.nearCylinderTable[k];
         const Cyl& c = s.cyl[s.nearCylinderTable[k + 1]];
-        const double overlap = s.el[j].radius - cylinderDist(c, s.el[j].px0);
+        const double overlap = s.parts[j].r - cylinderDist(c, s.parts[j].x0);
         if (overlap > 0.0) cylinderParticleCollision(s, c, j, overlap);
     }
     const double nv = s.P.num_visc;
@@ -787,6 +917,10 @@ void demSubstep(hbo_sim& s) {  // DEM.cpp:336-374
         const V3 mBf = project(moment, qadj(e.qp0));
         const V3 waBf = newtonAcc(mBf, e.I, e.wpLocal);
         e.w1 = project(waBf, e.qp0);
+        if (e.size > 1) {  // quatAcc (vector.cpp:500-504), DEM.cpp:1176-1179
+            const double n2 = e.qp1.q0 * e.qp1.q0 + e.qp1.q1 * e.qp1.q1 + e.qp1.q2 * e.qp1.q2 + e.qp1.q3 * e.qp1.q3;
+            e.q2 = qscale(qmul(e.qp0, Quat{-2.0 * n2, waBf.x, waBf.y, waBf.z}), 0.5);
+        }
     }
     // corrector (DEM.cpp:1082-1112, elmt.cpp:179-254)
     const double g1[6] = {95.0 / 288.0, 1.0, 25.0 / 24.0, 35.0 / 72.0, 5.0 / 48.0, 1.0 / 120.0};
@@ -820,9 +954,8 @@ void demSubstep(hbo_sim& s) {  // DEM.cpp:336-374
         e.qp0 = e.q0; e.qp1 = e.q1; e.qp2 = e.q2; e.qp3 = e.q3; e.qp4 = e.q4; e.qp5 = e.q5;
         e.wGlobal = e.w0;
         e.wLocal = project(e.wGlobal, qadj(e.q0));
-        e.px0 = e.x0;  // particle::updateCorrected
-        e.px1 = e.x1;
     }
+    updateParticles(s, false);
 }
 
 // ---- LB -----------------------------------------------------------------------------
@@ -870,8 +1003,9 @@ void computeHydroForces(hbo_sim& s) {  // LB.cpp:1851-1919
         const size_t i = s.activeNodes[k];
         s.hf[i] = v3(0, 0, 0);
         if (!s.inside[i]) continue;
-        Elmt& e = s.el[s.solid[i]];
-        const V3 radius = add(sub(s.pos(i), e.px0), v3(0, 0, 0));
+        const Part& q = s.parts[s.solid[i]];
+        Elmt& e = s.el[q.cluster];
+        const V3 radius = add(sub(s.pos(i), q.x0), q.radiusVec);
         const V3 localVel = add(e.x1, cross(e.wGlobal, radius));
         const V3 diffVel = mul(s.mass[i] / s.n[i], sub(s.u[i], localVel));
         s.hf[i] = add(s.hf[i], mul(-1.0, diffVel));
@@ -1175,28 +1309,52 @@ void updateInterface(hbo_sim& s) {  // LB.cpp:1592-1804
 
 // ---- coupling (LB.cpp:1921-2033) ----------------------------------------------------
 
+// the first particle of the element (its spheres, then its ghosts) that covers pt, or -1
+int coveringComponent(const hbo_sim& s, unsigned cluster, V3 pt) {
+    for (unsigned c : s.comps[cluster]) {
+        const Part& q = s.parts[c];
+        if (norm2(sub(pt, q.x0)) < q.r * q.r) return (int)c;  // insideSphere, vector.cpp:153-158
+    }
+    return -1;
+}
+
+// LB::latticeBoltzmannCouplingStep (LB.cpp:247-280): updateIndices after a neighbour
+// rebuild with periodic faces (LB.cpp:1826-1849: initializeParticleBoundaries over every
+// particle, then resetLists), findNewActive, findNewSolid
 void couplingStep(hbo_sim& s) {
+    if (s.newNeighborList) {
+        for (size_t i = 0; i < s.N; ++i) {
+            s.inside[i] = 0;
+            if (!s.isActive(i)) continue;
+            for (size_t n = 0; n < s.parts.size(); ++n)
+                if (norm2(sub(s.pos(i), s.parts[n].x0)) < s.parts[n].r * s.parts[n].r) {
+                    s.inside[i] = 1;
+                    s.solid[i] = (uint32_t)n;
+                }
+        }
+        s.particleNodes.clear();
+        for (size_t i = 0; i < s.N; ++i)
+            if (s.inside[i]) s.particleNodes.push_back((uint32_t)i);
+        s.newNeighborList = false;
+    }
     std::vector<uint32_t> pop;
     for (uint32_t i : s.particleNodes) {  // findNewActive
-        const Elmt& e = s.el[s.solid[i]];
-        if (!(norm2(sub(s.pos(i), e.px0)) < e.radius * e.radius)) {
+        if (coveringComponent(s, s.parts[s.solid[i]].cluster, s.pos(i)) < 0) {
             pop.push_back(i);
             s.inside[i] = 0;
         }
     }
     for (uint32_t i : pop) eraseValue(s.particleNodes, i);
-    std::vector<uint32_t> newSolid;
     for (size_t k = 0; k < s.particleNodes.size(); ++k) {  // findNewSolid (list grows)
         const uint32_t i = s.particleNodes[k];
-        const uint32_t p = s.solid[i];
+        const unsigned cl = s.parts[s.solid[i]].cluster;
         for (int kk = 1; kk < 7; ++kk) {
             const uint32_t l = s.nb[(size_t)i * Q + kk];
             if (s.inside[l]) continue;
-            const Elmt& e = s.el[p];
-            if (norm2(sub(s.pos(l), e.px0)) < e.radius * e.radius) {
-                s.solid[l] = p;
+            const int c = coveringComponent(s, cl, s.pos(l));
+            if (c >= 0) {
+                s.solid[l] = (uint32_t)c;
                 s.inside[l] = 1;
-                newSolid.push_back(l);
                 s.particleNodes.push_back(l);
             }
         }
@@ -1271,14 +1429,47 @@ hbo_sim* hbo_create_cyl(const hb_params* p, const hb_elements* e, const hb_objec
         el.xp1 = el.x1;
         el.qp0 = el.q0;
         el.wpGlobal = el.wGlobal = el.wpLocal = el.wLocal = el.w0;
+        el.size = e->size ? e->size[k] : 1;
+        if (el.size < 1 || el.size > 4) { g_err = "element size outside 1..4"; delete s; return nullptr; }
         const double sm = 4.0 / 3.0 * p->density * M_PI * el.radius * el.radius * el.radius;
-        el.m = 1 * sm;
-        el.I = mul(1 * 2.0 / 5.0 * sm * el.radius * el.radius, v3(1.0, 1.0, 1.0));
-        el.I = add(el.I, mul(sm * el.radius * el.radius, v3(0, 0, 0)));
-        el.px0 = el.x0;
-        el.px1 = el.x1;
+        el.m = el.size * sm;  // elmt.cpp:62-71, Huygens-Steiner over the prototype positions
+        el.I = mul(el.size * 2.0 / 5.0 * sm * el.radius * el.radius, v3(1.0, 1.0, 1.0));
+        for (int n = 0; n < el.size; ++n) {
+            const V3 t = prototype(el.size, n);
+            el.I = add(el.I, mul(sm * el.radius * el.radius, v3(t.y * t.y + t.z * t.z, t.z * t.z + t.x * t.x,
+                                                               t.x * t.x + t.y * t.y)));
+        }
         s->el.push_back(el);
     }
+    // particles (elmt::generateParticles, elmt.cpp:122-137), in element order
+    s->comps.assign(ne, {});
+    for (int k = 0; k < ne; ++k)
+        for (int n = 0; n < s->el[k].size; ++n) {
+            Part q;
+            q.cluster = (unsigned)k;
+            q.proto = n;
+            q.r = s->el[k].radius;
+            q.x0 = q.x1 = q.radiusVec = v3(0, 0, 0);
+            s->comps[k].push_back((unsigned)s->parts.size());
+            s->parts.push_back(q);
+        }
+    s->stdParticles = (unsigned)s->parts.size();
+    updateParticles(*s, false);
+    // periodic face pairs (DEM::initializePbcs, DEM.cpp:937-989)
+    const int L[3] = {s->X, s->Y, s->Z};
+    for (int k = 0; k < 3; ++k) {
+        if (p->boundary[2 * k] != 4) continue;
+        if (p->boundary[2 * k + 1] != 4) { g_err = "periodic boundary on one face only"; delete s; return nullptr; }
+        Pbc b;
+        b.p = v3(k == 0 ? 0.5 : 0.0, k == 1 ? 0.5 : 0.0, k == 2 ? 0.5 : 0.0);
+        b.v = v3(k == 0 ? L[0] - 2.0 : 0.0, k == 1 ? L[1] - 2.0 : 0.0, k == 2 ? L[2] - 2.0 : 0.0);
+        b.p1 = b.p;
+        b.p2 = add(b.p, b.v);
+        b.n1 = divs(b.v, norm(b.v));
+        b.n2 = mul(-1.0, b.n1);
+        s->pbcs.push_back(b);
+    }
+    s->stdObjects = (unsigned)s->obj.size();
     s->deltat = ne ? 1.0 / double(p->multi_step) : 1.0;
     s->demTime = 0.0;
     s->maxDisp = 0.0;
@@ -1286,6 +1477,23 @@ hbo_sim* hbo_create_cyl(const hb_params* p, const hb_elements* e, const hb_objec
     s->triggerSet = false;
     if (ne) {
         initNeighborParameters(*s);
+        // periodicObjects (DEM.cpp:990-1063): images of the objects near the faces
+        std::vector<Ghost> og;
+        for (const Pbc& b : s->pbcs)
+            for (unsigned k = 0; k < s->stdObjects; ++k) {
+                const double ld = b.dist1(s->obj[k].x0), rd = b.dist2(s->obj[k].x0);
+                if (ld < 2.0 * s->nebrRange && ld > 0.0) og.push_back(Ghost{k, b.v});
+                else if (rd < 2.0 * s->nebrRange && rd > 0.0) og.push_back(Ghost{k, mul(-1.0, b.v)});
+            }
+        const size_t ns = og.size();
+        for (size_t g1 = 0; g1 < ns; ++g1)
+            for (size_t g2 = g1 + 1; g2 < ns; ++g2)
+                if (og[g1].index == og[g2].index) og.push_back(Ghost{og[g1].index, add(og[g1].vec, og[g2].vec)});
+        for (const Ghost& g : og) {
+            Object ob = s->obj[g.index];
+            ob.x0 = add(ob.x0, g.vec);
+            s->obj.push_back(ob);
+        }
         evalNeighborTable(*s);
     }
     if (!buildLattice(*s, e, o)) { delete s; return nullptr; }

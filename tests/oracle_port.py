@@ -67,11 +67,11 @@ def _p(a):
 class OracleSim:
     """One CPU-oracle simulation (FP64, reference semantics)."""
 
-    def __init__(self, params, spheres=None, objects=None, threads=1, cylinders=None):
+    def __init__(self, params, spheres=None, objects=None, threads=1, cylinders=None, sizes=None, quats=None):
         self.lib = oracle_lib()
         self.lib.hbo_set_threads(threads)
         self.params = params
-        self.arrays = abi.ElementArrays(spheres, objects)
+        self.arrays = abi.ElementArrays(spheres, objects, sizes, quats)
         self.cyl = abi.CylinderArrays(cylinders) if cylinders is not None and len(cylinders) else None
         self.h = self.lib.hbo_create_cyl(C.byref(params), self.arrays.el_ptr(), self.arrays.ob_ptr(),
                                          self.cyl.ptr() if self.cyl else None)
