@@ -158,15 +158,18 @@ def cpu_sample(params, spheres, steps, threads):
 
 
 def fp64_compare(p32, spheres, steps):
-    """The FP64 form of the same workload: its step time, and the FP32 form's velocity and
-    density error against it after `steps` cycles from the same initial state."""
+    """The FP64 form of the same workload: its step time, and the FP32 and FP16-storage
+    forms' velocity and density errors against it after `steps` cycles from the same
+    initial state."""
     from hybird_gb300 import abi
     from hybird_gb300.gpu import GpuSim
     p64 = abi.HbParams.from_buffer_copy(p32)
     p64.precision = abi.HB_FP64
+    p16 = abi.HbParams.from_buffer_copy(p32)
+    p16.precision = abi.HB_FP16S
     out = {"steps": steps}
     lat = {}
-    for name, p in (("f64", p64), ("f32", p32)):
+    for name, p in (("f64", p64), ("f32", p32), ("f16s", p16)):
         g = GpuSim(p, spheres)
         if name == "f64":
             g.cycle(3)
@@ -184,6 +187,10 @@ def fp64_compare(p32, spheres, steps):
     out["u_rel_l2"] = float(np.sqrt((du ** 2).sum() / (u64 ** 2).sum()))
     out["u_rel_linf"] = float(np.abs(du).max() / np.abs(u64).max())
     out["rho_abs_linf"] = float(np.abs(lat["f32"]["n"][act] - lat["f64"]["n"][act]).max())
+    d16 = lat["f16s"]["u"].reshape(3, -1)[:, act] - u64
+    out["fp16s"] = {"u_rel_l2": float(np.sqrt((d16 ** 2).sum() / (u64 ** 2).sum())),
+                    "u_rel_linf": float(np.abs(d16).max() / np.abs(u64).max()),
+                    "rho_abs_linf": float(np.abs(lat["f16s"]["n"][act] - lat["f64"]["n"][act]).max())}
     return out
 
 
@@ -375,7 +382,10 @@ def main():
                      "traffic": lattice_traffic(prec), "kernel": "k_collide_stream_dev" if prec != abi.HB_FP64 else "k_collide_stream", "kernel_ms": round(ms_lb, 5),
                      "peak_kind": peak_kind, "bytes_per_launch": bytes_launch},
         "clocks": clk.summary(),
-        "dem": {"contacts_last_substep": st.contacts, "candidate_pairs": st.pairs},
+        # candidate pairs are evaluated every substep; contacts/s at the last substep's count
+        "dem": {"contacts_last_substep": st.contacts, "candidate_pairs": st.pairs,
+                "pairs_evaluated_per_s": round(st.pairs * p.multi_step / (ms_step * 1e-3), 1),
+                "contacts_per_s": round(st.contacts * p.multi_step / (ms_step * 1e-3), 1)},
     }
     if fp64:
         fp64["fp32_speedup"] = round(fp64.pop("ms_per_step_f64") / ms_step, 2)
