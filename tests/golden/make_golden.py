@@ -97,7 +97,7 @@ def rsa_periodic(seed, n, rmin, rmax, lo, hi, period, gap=0.3):
 
 
 CASES = {
-    # periodic-x/z channel with walls at y=0/Ly-1 (BASELINE config 1 shape, shrunk)
+    # periodic-x/z channel with walls at y=0/Ly-1 (the 64x32x32 channel workload, shrunk)
     "channel_bgk": dict(
         cfg=dict(lbSizeX=12, lbSizeY=8, lbSizeZ=6, lbFX=2e-5, initVisc=0.1,
                  boundary0=4, boundary1=4, boundary2=7, boundary3=7, boundary4=4, boundary5=4),
