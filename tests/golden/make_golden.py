@@ -184,6 +184,14 @@ CASES = {
                  boundary0=4, boundary1=4, boundary2=4, boundary3=4, boundary4=7, boundary5=7),
         spheres=("rsa_periodic", 31, 14, 1.4, 2.0, (0.6, 0.6, 3.0), (22.4, 18.4, 22.0), (22.0, 18.0, 0.0)),
         objects=[], steps=[0, 1, 30, 60, 100, 150], full=[]),
+    # fixed objects near the periodic faces get images across them (DEM.cpp:990-1063);
+    # spheres driven along x meet them through the faces, DEM only
+    "dem_periodic_objects": dict(
+        cfg=dict(lbSizeX=24, lbSizeY=20, lbSizeZ=20, lbSolve=0, lbFX=3e-3, lbFZ=-5e-4, multiStep=20,
+                 boundary0=4, boundary1=4, boundary2=4, boundary3=4, boundary4=7, boundary5=7),
+        spheres=("rsa_periodic", 33, 6, 1.4, 1.8, (15.0, 7.5, 3.5), (20.5, 12.5, 8.0), (22.0, 18.0, 0.0)),
+        objects=[(1.5, 10.0, 5.5, 2.2), (12.0, 10.0, 2.5, 1.5)],
+        steps=[0, 1, 30, 60, 90, 120], full=[]),
     # the same with the lattice: ghost particles cover the nodes across the periodic faces
     # and every neighbour rebuild re-marks the particle nodes (LB.cpp:1826-1849)
     "box_periodic": dict(

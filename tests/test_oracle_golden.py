@@ -70,7 +70,7 @@ def test_dem_matches_reference(name):
         np.testing.assert_array_equal(pairs, gp)  # same sweep order as the reference
 
 
-@pytest.mark.parametrize("name", ["dem_periodic", "box_periodic", "dem_clusters", "box_clusters"])
+@pytest.mark.parametrize("name", ["dem_periodic", "box_periodic", "dem_clusters", "box_clusters", "dem_periodic_objects"])
 def test_periodic_and_cluster_dem_match_reference(name):
     """Ghost particles across periodic faces and multi-sphere elements (DEM.cpp:404-433,
     1395-1494, 1554-1664; LB.cpp:1826-1849): the oracle's candidate table equals the
