@@ -96,7 +96,7 @@ typedef struct hb_params {
     double  slip_coefficient;  /* slipCoefficient S of the slip walls 5/6 (LB.cpp:1154-1155) */
 } hb_params;
 
-/* Spheres: one element per particle (elmt size 1, DEM.cpp:81-127 particle file row). */
+/* Elements (DEM.cpp:81-127 particle file row): single spheres, or 2-4 spheres when size is given. */
 typedef struct hb_elements {
     int32_t count;
     const double* radius;      /* [count]                                                    */

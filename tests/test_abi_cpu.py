@@ -77,3 +77,35 @@ def test_checkpoint_load_rejects_a_foreign_file_without_gpu(tmp_path):
     assert b"checkpoint" in lib.hb_last_error()
     missing = tmp_path / "missing.bin"
     assert lib.hb_checkpoint_load(str(missing).encode(), C.byref(h)) == abi.HB_ERR_ARG
+
+
+STRUCTS = [("hb_params", "HbParams"), ("hb_elements", "HbElements"), ("hb_objects", "HbObjects"),
+           ("hb_status", "HbStatus"), ("hb_export", "HbExport"), ("hb_cylinders", "HbCylinders"),
+           ("hb_adjoint_cfg", "HbAdjointCfg")]
+
+
+def test_ctypes_mirrors_match_the_c_layout(tmp_path):
+    """Every struct of the header and its ctypes mirror: same size, same field offsets
+    (a C program built from the header prints them)."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "hybird_gpu.h"', "int main(void) {"]
+    for cname, pyname in STRUCTS:
+        cls = getattr(abi, pyname)
+        lines.append(f'printf("{cname} sizeof() %zu\\n", sizeof({cname}));')
+        for f in cls._fields_:
+            lines.append(f'printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, pyname in STRUCTS:
+        cls = getattr(abi, pyname)
+        assert got[(cname, "sizeof()")] == C.sizeof(cls), cname
+        for f in cls._fields_:
+            assert got[(cname, f[0])] == getattr(cls, f[0]).offset, (cname, f[0])
