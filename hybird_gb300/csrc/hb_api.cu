@@ -713,7 +713,11 @@ int hb_synchronize(hb_ctx* c) {
     int st[STATUS_WORDS];
     CK(cudaMemcpy(st, c->status, sizeof(st), cudaMemcpyDeviceToHost));
     if (st[1]) return seterr(HB_ERR_UNSUPPORTED, "TYPE ERROR: an active node links to an unsupported node type");
-    if (st[2]) return seterr(HB_ERR_CAPACITY, "device list capacity exceeded (code %d)", st[2]);
+    if (st[2])  // status word 2: 1 candidate list full, 2 particle outside the cell grid, 4 object list full
+        return seterr(HB_ERR_CAPACITY, "DEM list capacity exceeded (code %d:%s%s%s; limits %d candidates, %d objects)",
+                      st[2], (st[2] & 1) ? " candidate list full" : "",
+                      (st[2] & 2) ? " a particle outside the DEM cell grid" : "",
+                      (st[2] & 4) ? " object list full" : "", NBR_CAP, OBJ_CAP);
     return HB_OK;
 }
 
