@@ -105,3 +105,28 @@ def test_periodic_and_cluster_dem_match_reference(name):
             act = (d[pre + "type"] == 0) | (d[pre + "type"] == 3)
             assert rel_linf(o["u"].reshape(3, -1), d[pre + "u"].reshape(3, -1), act) <= 1e-12, (name, step, "u")
 
+
+
+@pytest.mark.parametrize("name", ["channel_bgk", "channel_movwall"])
+def test_trt_with_equal_rates_matches_the_reference_bgk(name):
+    """The TRT restatement (no reference counterpart) with the magic parameter
+    (tau - 1/2)^2, so that both rates equal 1/tau, must reproduce the reference's BGK
+    fixture to FP64 rounding."""
+    from hybird_gb300 import abi
+    d = load_golden(name)
+    p = golden_params(d)
+    tau = 0.5 + 3.0 * p.init_visc
+    p.collision = abi.HB_TRT
+    p.trt_magic = (tau - 0.5) ** 2
+    sim = OracleSim(p)
+    done = 0
+    for step in d["steps"]:
+        sim.cycle(int(step) - done)
+        done = int(step)
+        g = {k[len(f"s{step}_"):]: d[k] for k in d.files if k.startswith(f"s{step}_")}
+        o = sim.lattice()
+        act = (g["type"] == 0) | (g["type"] == 3)
+        if "f" in g:
+            assert rel_linf(o["f"].reshape(19, -1), g["f"].reshape(19, -1), act) <= 1e-13, (name, step)
+        if step:
+            assert rel_linf(o["u"].reshape(3, -1), g["u"].reshape(3, -1), act) <= 1e-12, (name, step)
