@@ -46,46 +46,12 @@ B_LU = {0: 2 * 19 * 8 + 1, 1: 2 * 19 * 4 + 1, 2: 2 * 19 * 2 + 1}  # bytes per la
 DTYPE = {0: "f64", 1: "f32", 2: "f16-storage/f32-compute"}
 
 
-def rsa_spheres(seed, target, rmin, rmax, lo, hi, tries=400000, batch=4096):
-    """Seeded random sequential addition of non-overlapping spheres (vectorised in
-    batches; each candidate is accepted only if it overlaps no earlier sphere)."""
-    rng = np.random.default_rng(seed)
-    placed = np.zeros((0, 4))
-    done = 0
-    while done < tries and len(placed) < target:
-        r = rng.uniform(rmin, rmax, batch)
-        c = np.stack([rng.uniform(lo + r, hi - r) for _ in range(3)], axis=1)
-        done += batch
-        if len(placed):
-            d2 = ((c[:, None, :] - placed[None, :, :3]) ** 2).sum(-1)
-            ok = (d2 >= (r[:, None] + placed[None, :, 3]) ** 2).all(axis=1)
-        else:
-            ok = np.ones(batch, bool)
-        acc = []
-        for k in np.nonzero(ok)[0]:
-            good = True
-            for a in acc:
-                if ((c[k] - c[a]) ** 2).sum() < (r[k] + r[a]) ** 2:
-                    good = False
-                    break
-            if good:
-                acc.append(k)
-                if len(placed) + len(acc) >= target:
-                    break
-        if acc:
-            placed = np.vstack([placed, np.c_[c[acc], r[acc]]])
-    return placed
-
-
-def workload(precision):
-    from hybird_gb300 import abi
-    L = 128
-    spheres = rsa_spheres(2, 2000, 4.0, 6.0, 0.5, L - 1.5)
-    p = abi.make_params((L, L, L), (7,) * 6, init_visc=(0.8 - 0.5) / 3.0, lbF=(0.0, 0.0, -1e-5),
-                        collision=abi.HB_TRT, trt_magic=3.0 / 16.0, precision=precision,
-                        multi_step=3, density=2.5, linear_stiff=1e3, restitution=0.8,
-                        friction_part=0.5, friction_wall=0.5, visc_tang=0.5)
-    return p, spheres
+def workload(precision, deposited=False):
+    """Configuration 2 (hybird_gb300.workloads.sedimentation): 128^3 TRT, seeded RSA
+    spheres r ~ U[4, 6] from seed 2 (1514 placed before the packing jams); deposited=True
+    drops the same spheres onto the floor, so that every sphere is in contact."""
+    from hybird_gb300.workloads import sedimentation
+    return sedimentation(precision, deposited=deposited)
 
 
 class Clocks:
@@ -144,7 +110,10 @@ def measured_peak():
 
 
 def cpu_sample(params, spheres, steps, threads):
-    """CPU oracle on a bounded sample of the workload: `steps` whole cycles."""
+    """CPU oracle on a bounded sample of the workload: one untimed cycle, then `steps`
+    timed whole cycles.  Returns the rate, the timed seconds, the cycles run and the
+    oracle's final node types, density and velocity (the checker of the GPU forms'
+    error on the same cycles)."""
     sys.path.insert(0, os.path.join(REPO, "tests"))
     from oracle_port import OracleSim
     o = OracleSim(params, spheres, threads=threads)
@@ -153,8 +122,60 @@ def cpu_sample(params, spheres, steps, threads):
     t0 = time.perf_counter()
     o.cycle(steps)
     dt = time.perf_counter() - t0
+    lat = o.lattice()
     o.close()
-    return active * steps / dt / 1e6, dt
+    return active * steps / dt / 1e6, dt, steps + 1, {k: lat[k] for k in ("type", "n", "u")}
+
+
+def error_vs_oracle(p32, spheres, cycles, ref):
+    """Velocity (relative L2, L-inf relative to max |u|) and density (absolute L-inf)
+    error of the GPU's FP32, FP16-storage and FP64 forms against the oracle's state
+    `ref` after the same `cycles` whole cycles from the same initial state."""
+    from hybird_gb300 import abi
+    from hybird_gb300.gpu import GpuSim
+    act = (ref["type"] == 0) | (ref["type"] == 3)
+    u0 = ref["u"].reshape(3, -1)[:, act]
+    out = {"cycles": cycles}
+    for name, prec in (("f32", abi.HB_FP32), ("f16s", abi.HB_FP16S), ("f64", abi.HB_FP64)):
+        p = abi.HbParams.from_buffer_copy(p32)
+        p.precision = prec
+        g = GpuSim(p, spheres)
+        g.cycle(cycles)
+        l = g.lattice(("type", "n", "u"))
+        g.close()
+        du = l["u"].reshape(3, -1)[:, act] - u0
+        out[name] = {"u_rel_l2": float(np.sqrt((du ** 2).sum() / (u0 ** 2).sum())),
+                     "u_rel_linf": float(np.abs(du).max() / np.abs(u0).max()),
+                     "rho_abs_linf": float(np.abs(l["n"][act] - ref["n"][act]).max()),
+                     "types_identical": bool(np.array_equal(l["type"], ref["type"]))}
+    return out
+
+
+def dem_loaded(steps):
+    """The DEM contact path under load: configuration 2 with the spheres deposited on
+    the floor and on each other (every sphere in contact from the start; multiStep 10,
+    at which such a bed is stable), FP32 populations, FP64 DEM.  Whole-cycle time, the cooperative DEM kernel's phases from
+    device timestamps, candidate pairs and overlapping contacts of the last substep."""
+    from hybird_gb300 import abi
+    from hybird_gb300.gpu import GpuSim
+    p, spheres = workload(abi.HB_FP32, deposited=True)
+    g = GpuSim(p, spheres)
+    g.cycle(5)
+    ms, ms_lb, _ = g.time_cycles(steps)
+    ph = g.profile_phases(max(5, steps // 4))
+    st = g.status()
+    g.close()
+    ms_step = ms / steps
+    multi = p.multi_step
+    dem_us = float(ph[:1 + 2 * multi].sum())  # element forces + the substeps
+    return {"workload": "configuration 2 spheres deposited on the floor (%d spheres), FP32 populations, "
+                        "FP64 DEM, multiStep %d" % (len(spheres), multi),
+            "ms_per_step": round(ms_step, 4), "lattice_kernel_ms": round(ms_lb, 4),
+            "contacts_last_substep": st.contacts, "candidate_pairs": st.pairs,
+            "pairs_evaluated_per_s": round(st.pairs * multi / (ms_step * 1e-3), 1),
+            "contacts_per_s": round(st.contacts * multi / (ms_step * 1e-3), 1),
+            "dem_kernel_us": round(dem_us, 2),
+            "phases_us": [round(float(v), 2) for v in ph]}
 
 
 def fp64_compare(p32, spheres, steps):
@@ -203,20 +224,29 @@ def config_rates(steps):
     from hybird_gb300.gpu import GpuSim
     from hybird_gb300.workloads import channel, dam_break, precision_box
     out = {}
+    from hybird_gb300.workloads import sedimentation
+    p_mbb, s_mbb = sedimentation(abi.HB_FP32)
+    p_mbb.coupling = abi.HB_MOVING_BB
     cases = [("c1_channel_64x32x32_bgk_f64", channel(precision=abi.HB_FP64), None),
+             ("c2_moving_bounce_back_f32", p_mbb, s_mbb),
              ("c3_dambreak_256x128x128_f32", *dam_break(abi.HB_FP32)),
              ("c4_256cube_16000_spheres_f32", *precision_box(abi.HB_FP32)),
              ("c4_256cube_16000_spheres_f16s", *precision_box(abi.HB_FP16S))]
     for name, p, spheres in cases:
         g = GpuSim(p, spheres)
-        t = g.lattice(("type",))["type"]
-        A = int(((t == 0) | (t == 3)).sum())
+        l0 = g.lattice(("type", "inside"))
+        act = (l0["type"] == 0) | (l0["type"] == 3)
+        A = int(act.sum())
         g.cycle(5)
         ms, ms_lb, _ = g.time_cycles(steps)
         g.close()
         out[name] = {"mlups": round(A / (ms / steps * 1e-3) / 1e6, 1), "ms_per_step": round(ms / steps, 4),
                      "lattice_kernel_ms": round(ms_lb, 4), "active_nodes": A,
                      "spheres": 0 if spheres is None else len(spheres)}
+        if p.coupling == abi.HB_MOVING_BB:  # the nodes inside particles are solid in this mode
+            F = int((act & (l0["inside"] == 0)).sum())
+            out[name]["fluid_nodes"] = F
+            out[name]["mlups_fluid_nodes"] = round(F / (ms / steps * 1e-3) / 1e6, 1)
     return out
 
 
@@ -301,6 +331,11 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=2000, help="0 skips the adjoint measurement")
     ap.add_argument("--config-steps", type=int, default=50,
                     help="timed cycles of configurations 1, 3 and 4 (0 skips them)")
+    ap.add_argument("--dem-steps", type=int, default=40,
+                    help="timed cycles of the deposited (all spheres in contact) workload (0 skips it)")
+    ap.add_argument("--min-cycles", type=int, default=200,
+                    help="timed windows of --steps cycles are repeated until this many cycles ran; "
+                         "the median window is reported")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -333,26 +368,41 @@ def main():
         check(L.hb_cycle(g.h, 1))
     check(L.hb_synchronize(g.h))
     rep.barrier()
-    # device-resident timed region (inputs larger than L2: 2 x 19 x 2.1M x 4 B = 319 MB)
+    # device-resident timed windows of exactly K cycles each (inputs larger than L2:
+    # 2 x 19 x 2.1M x 4 B = 319 MB of populations); the median window is reported
+    windows = max(1, -(-args.min_cycles // args.steps))
+    per_step, per_lb = [], []
     with Clocks(local) as clk:
-        ms_tot, ms_lb, kpc = g.time_cycles(args.steps)
+        for _ in range(windows):
+            ms_tot, ms_lb, kpc = g.time_cycles(args.steps)
+            per_step.append(ms_tot / args.steps)
+            per_lb.append(ms_lb)
     check(L.hb_synchronize(g.h))
-    ms_step = rep.max(ms_tot / args.steps)
+    k_med = int(np.argsort(per_step)[len(per_step) // 2])
+    ms_step = rep.max(per_step[k_med])
+    ms_lb = per_lb[k_med]
     value = rep.aggregate_rate(A, ms_step * 1e-3) / 1e6
-    # end-to-end through the C-ABI with host buffers
+    # end to end through the C-ABI with host buffers: every step the body force goes in
+    # (24 B, as kernel arguments), the whole cycle runs, and the element state the host
+    # driver reads (x0, x1, FHydro, MHydro) comes back by asynchronous copies into
+    # page-locked host arrays; the region ends when the last copy has landed
     E = g.E
-    pin = {k: np.zeros(3 * E) for k in ("x0", "x1", "FHydro", "MHydro")}
+    host = np.zeros((4, 3 * E))
+    check(L.hb_host_register(host.ctypes.data_as(C.c_void_p), host.nbytes))
     force = np.array(p.lbF[:], dtype=np.float64)
-    e2e_steps = max(3, args.steps // 4)
+    e2e_steps = max(3, args.steps)
+    ptr = [host[k].ctypes.data_as(C.c_void_p) for k in range(4)]
+    check(L.hb_synchronize(g.h))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         check(L.hb_set_body_force(g.h, force.ctypes.data_as(C.c_void_p)))
         check(L.hb_cycle(g.h, 1))
-        check(L.hb_download_elements(g.h, pin["x0"].ctypes.data_as(C.c_void_p),
-                                     pin["x1"].ctypes.data_as(C.c_void_p), None, None,
-                                     pin["FHydro"].ctypes.data_as(C.c_void_p),
-                                     pin["MHydro"].ctypes.data_as(C.c_void_p), None, None, None, None, None))
+        check(L.hb_download_elements_async(g.h, ptr[0], ptr[1], None, None, ptr[2], ptr[3],
+                                           None, None, None, None, None))
+    check(L.hb_synchronize(g.h))
     e2e_dt = rep.max(time.perf_counter() - t0)
+    check(L.hb_host_unregister(host.ctypes.data_as(C.c_void_p)))
+    assert np.isfinite(host).all() and np.abs(host[2]).max() > 0.0
     e2e = rep.aggregate_rate(A * e2e_steps, e2e_dt) / 1e6
     # roofline of the fused kernel
     peak, peak_kind = measured_peak()
@@ -361,8 +411,10 @@ def main():
     st = g.status()
     g.close()
     fp64 = fp64_compare(p, spheres, args.compare_steps) if args.compare_steps > 0 and prec != abi.HB_FP64 else None
+    loaded = dem_loaded(args.steps) if args.dem_steps > 0 else None
     adj = adjoint_measure(args.adjoint_steps) if args.adjoint_steps > 0 else None
     cfgs = config_rates(args.config_steps) if args.config_steps > 0 else None
+    step_bytes = bytes_launch  # the lattice kernel's algorithmic bytes are the step's bytes
     line = {
         "metric": "MLUPS (coupled LBM-DEM step)", "value": round(value, 2), "unit": "MLUPS",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
@@ -373,20 +425,24 @@ def main():
                    "lattice": [128, 128, 128], "active_nodes": A, "inside_nodes": A_in, "spheres": E,
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (319 MB populations per step)",
-                   "kernels_per_cycle": kpc},
+                   "kernels_per_cycle": kpc, "timed_windows": windows,
+                   "window_ms_per_step": [round(v, 4) for v in per_step]},
         "gpu_launches": kpc * args.steps,
         "e2e": {"value": round(e2e, 2), "unit": "MLUPS", "h2d_bytes_per_step": 24,
-                "d2h_bytes_per_step": 4 * 3 * E * 8},
+                "d2h_bytes_per_step": 4 * 3 * E * 8, "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                      "traffic": lattice_traffic(prec), "kernel": "k_collide_stream_dev" if prec != abi.HB_FP64 else "k_collide_stream", "kernel_ms": round(ms_lb, 5),
-                     "peak_kind": peak_kind, "bytes_per_launch": bytes_launch},
+                     "peak_kind": peak_kind, "bytes_per_launch": bytes_launch,
+                     "step_frac": round(step_bytes / (ms_step * 1e-3) / 1e9 / peak, 4)},
         "clocks": clk.summary(),
         # candidate pairs are evaluated every substep; contacts/s at the last substep's count
         "dem": {"contacts_last_substep": st.contacts, "candidate_pairs": st.pairs,
                 "pairs_evaluated_per_s": round(st.pairs * p.multi_step / (ms_step * 1e-3), 1),
                 "contacts_per_s": round(st.contacts * p.multi_step / (ms_step * 1e-3), 1)},
     }
+    if loaded:
+        line["dem_loaded"] = loaded
     if fp64:
         fp64["fp32_speedup"] = round(fp64.pop("ms_per_step_f64") / ms_step, 2)
         line["fp64_form"] = fp64
@@ -398,10 +454,12 @@ def main():
         threads = os.cpu_count() or 1
         try:
             p64, sph = workload(abi.HB_FP64)
-            v, dt = cpu_sample(p64, sph, args.cpu_steps, threads)
+            v, dt, ncyc, ref = cpu_sample(p64, sph, args.cpu_steps, threads)
             line["cpu_baseline"] = {"value": round(v, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
                                     "sample": f"{args.cpu_steps} whole cycles of the same workload in FP64 "
                                               f"after one untimed cycle ({dt:.1f} s)"}
+            # the GPU forms against this oracle run (same workload, same cycles)
+            line["error_vs_oracle"] = error_vs_oracle(p, sph, ncyc, ref)
         except Exception as exc:  # noqa: BLE001
             line["cpu_baseline"] = {"value": None, "error": str(exc)[:200]}
     if rank == 0:

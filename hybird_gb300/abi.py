@@ -18,6 +18,7 @@ HB_ERR_CAPACITY, HB_ERR_STATE, HB_ERR_NUMERIC = 5, 6, 7
 HB_FP64, HB_FP32, HB_FP16S = 0, 1, 2
 HB_BGK, HB_TRT = 0, 1
 HB_LINEAR, HB_HERTZIAN = 0, 1
+HB_DIRECT_FORCING, HB_MOVING_BB = 0, 1
 
 STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_UNSUPPORTED", 3: "ERR_CUDA", 4: "ERR_NOMEM",
                 5: "ERR_CAPACITY", 6: "ERR_STATE", 7: "ERR_NUMERIC"}
@@ -55,9 +56,10 @@ class HbParams(C.Structure):
         ("friction_part", C.c_double),
         ("friction_wall", C.c_double),
         ("num_visc", C.c_double),
-        ("cap_pairs", C.c_int64),
+        ("cap_neighbors", C.c_int64),
         ("cap_interface", C.c_int64),
         ("slip_coefficient", C.c_double),
+        ("coupling", C.c_int32),
     ]
 
 
@@ -112,8 +114,8 @@ def make_params(lb_size, boundary, init_visc=0.1, lbF=(0.0, 0.0, 0.0), force_fie
                 collision=HB_BGK, trt_magic=3.0 / 16.0, precision=HB_FP64, gas_box=(0.0, 0.0),
                 lb_solve=1, dem_solve=1, multi_step=1, contact_model=HB_LINEAR, density=2.5,
                 linear_stiff=1e3, young_mod=1.0, poisson=0.3, restitution=0.8, visc_tang=0.5,
-                friction_part=0.5, friction_wall=0.5, num_visc=0.0, cap_pairs=0, cap_interface=0,
-                slip_coefficient=0.0):
+                friction_part=0.5, friction_wall=0.5, num_visc=0.0, cap_neighbors=0, cap_interface=0,
+                slip_coefficient=0.0, coupling=0):
     p = HbParams()
     p.lb_size[:] = list(lb_size)
     p.boundary[:] = list(boundary)
@@ -145,9 +147,10 @@ def make_params(lb_size, boundary, init_visc=0.1, lbF=(0.0, 0.0, 0.0), force_fie
     p.friction_part = friction_part
     p.friction_wall = friction_wall
     p.num_visc = num_visc
-    p.cap_pairs = cap_pairs
+    p.cap_neighbors = cap_neighbors
     p.cap_interface = cap_interface
     p.slip_coefficient = slip_coefficient
+    p.coupling = coupling
     return p
 
 

@@ -79,6 +79,11 @@ int check_params(const hb_params* p) {
     if (p->collision != HB_BGK && p->collision != HB_TRT) return seterr(HB_ERR_ARG, "collision");
     if (p->dem_solve && (p->multi_step < 1 || p->multi_step > hb::MAX_MULTI))
         return seterr(HB_ERR_ARG, "multi_step must be in 1..%d", hb::MAX_MULTI);
+    if (p->cap_neighbors < 0 || p->cap_neighbors > 4096) return seterr(HB_ERR_ARG, "cap_neighbors must be in 0..4096");
+    if (p->coupling != HB_DIRECT_FORCING && p->coupling != HB_MOVING_BB) return seterr(HB_ERR_ARG, "coupling");
+    if (p->coupling == HB_MOVING_BB && p->free_surface)
+        return seterr(HB_ERR_UNSUPPORTED, "moving bounce-back coupling with a free surface is not implemented");
+    if (p->cap_interface < 0) return seterr(HB_ERR_ARG, "cap_interface must be >= 0");
     const long long N = (long long)p->lb_size[0] * p->lb_size[1] * p->lb_size[2];
     if (p->precision != HB_FP64 && 19LL * N >= (1LL << 31))  // 32-bit population offsets
         return seterr(HB_ERR_UNSUPPORTED, "FP32/FP16 lattices are limited to 19 * nodes < 2^31 (%lld nodes)", N);
@@ -136,6 +141,7 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     };
     const int E = (P.dem_solve && e) ? e->count : 0;
     d.E = E;
+    d.nbr_cap = P.cap_neighbors > 0 ? (int)P.cap_neighbors : NBR_CAP;
     d.multi = E ? P.multi_step : 1;
     d.dt = E ? 1.0 / double(P.multi_step) : 1.0;
     if (E == 0) return upload_objects();
@@ -180,6 +186,8 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     int rc;
     if ((rc = dalloc(&d.base, (size_t)nfields * E))) return rc;
     CK(cudaMemset(d.base, 0, sizeof(double) * nfields * E));
+    if ((rc = dalloc(&d.alt, 9 * (size_t)E))) return rc;
+    CK(cudaMemset(d.alt, 0, sizeof(double) * 9 * E));
     double* p = d.base;
     auto take = [&](int comps) { double* r = p; p += (size_t)comps * E; return r; };
     for (int k = 0; k < 6; ++k) d.x[k] = take(3);
@@ -338,7 +346,7 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     const size_t S = Pl + d.gcap;
     if ((rc = dalloc(&d.cell_of, S)) || (rc = dalloc(&d.cell_cnt, d.ncells)) || (rc = dalloc(&d.cell_start, d.ncells + 1)) ||
         (rc = dalloc(&d.cell_fill, d.ncells)) || (rc = dalloc(&d.cell_items, S)) ||
-        (rc = dalloc(&d.nbr, Pl * NBR_CAP)) || (rc = dalloc(&d.nbr_cnt, Pl)) || (rc = dalloc(&d.wall_of, Pl)) ||
+        (rc = dalloc(&d.nbr, Pl * (size_t)d.nbr_cap)) || (rc = dalloc(&d.nbr_cnt, Pl)) || (rc = dalloc(&d.wall_of, Pl)) ||
         (rc = dalloc(&d.obj, Pl * OBJ_CAP)) || (rc = dalloc(&d.obj_cnt, Pl)) || (rc = dalloc(&d.scal, 8)) ||
         (rc = dalloc(&d.contacts, 1)) || (rc = dalloc(&d.partial, hb::PARTIAL_CAP)) || (rc = dalloc(&d.done, 1)) ||
         (rc = dalloc(&d.wrec, 7 * Pl)) || (rc = dalloc(&d.orec, 7 * Pl * OBJ_CAP)) ||
@@ -399,6 +407,12 @@ int hb_create(const hb_params* params, hb_ctx** out) {
         if ((rc = dalloc(&c->lmask, N))) { hb_destroy(c); return rc; }
     CK(cudaMemset(c->mode, 0, sizeof(int)));
     CK(cudaMemset(c->status, 0, sizeof(int) * STATUS_WORDS));
+    // node fields start defined: a phase may read a node's value before the lattice first
+    // writes it (the element-force reduction of the first cycle reads the forcing term)
+    CK(cudaMemset(c->rho, 0, sizeof(double) * N));
+    CK(cudaMemset(c->u, 0, sizeof(double) * 3 * N));
+    CK(cudaMemset(c->hf, 0, sizeof(double) * 3 * N));
+    CK(cudaMemset(c->mass, 0, sizeof(double) * N));
     CK(cudaMemset(c->wall_force, 0, sizeof(double) * (MAX_WALLS * 3 + 1)));
     CK(cudaEventCreate(&c->ev0));
     CK(cudaEventCreate(&c->ev1));
@@ -416,10 +430,10 @@ int hb_destroy(hb_ctx* c) {
     void* ptrs[] = {c->ntype, c->lmask, c->solid, c->fA, c->fB, c->mode, c->rho, c->u, c->hf, c->mass,
                     c->visc, c->dv, c->hacc, c->status, c->wall_part, c->wall_force, c->fs_force, c->fs_mass2,
                     c->fs_cnt, c->fs_scal, c->fs_flag, c->fs_first, c->fs_part, c->lb_force, c->d_stage, c->d.pf, c->d.plain,
-                    c->d.base, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
+                    c->d.base, c->d.alt, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
-                    c->d.claim_list, c->d.claim_cnt, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
+                    c->d.claim_list, c->d.claim_cnt, c->d.pop_list, c->d.pop_cnt, c->d.pop_rho, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
                     c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix, c->fs_ilist,
                     c->curved_list, c->curved_cnt, c->d.cyl_of, c->io_terms, c->d.gmeta, c->d.gorig, c->d.gvec,
                     c->d.comp, c->d.ccnt, c->d.px, c->d.remark, c->d.ecomp, c->d.eccnt, c->d.pkey, c->d.efirst,
@@ -464,10 +478,18 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
     int rc = dem_init(c, e, o);
     if (rc) return rc;
     const long long N = c->N;
+    const bool mbb = c->P.coupling == HB_MOVING_BB && c->d.E > 0;
+    if (mbb && (c->d.gen || !c->cyl.empty()))
+        return seterr(HB_ERR_UNSUPPORTED,
+                      "moving bounce-back coupling takes single spheres without periodic faces or cylinders");
     const size_t tsz = c->P.precision == HB_FP64 ? 8 : 4;
     if (c->d.E > 0) {
         if (c->P.precision == HB_FP64) {
+            // direct-forcing term per node: zero until the first lattice step (the first
+            // cycle's element sums, before any lattice step, are FHydro = 0 as the
+            // reference's element init leaves them)
             if (!c->dv && (rc = dalloc((uint8_t**)&c->dv, 3 * N * tsz))) return rc;
+            CK(cudaMemset(c->dv, 0, 3 * N * tsz));
         } else {
             if (!c->hacc && (rc = dalloc(&c->hacc, 7 * (size_t)c->d.E))) return rc;
             CK(cudaMemset(c->hacc, 0, sizeof(unsigned long long) * 7 * c->d.E));
@@ -476,6 +498,12 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         if (!c->d.claim_cnt && (rc = dalloc(&c->d.claim_cnt, 1))) return rc;
         if (!c->d.boxes && (rc = dalloc((uint8_t**)&c->d.boxes, ((size_t)c->d.P + c->d.gcap) * 128))) return rc;
         CK(cudaMemset(c->d.claim_cnt, 0, sizeof(int)));
+        if (mbb) {
+            if (!c->d.pop_list && (rc = dalloc(&c->d.pop_list, N))) return rc;
+            if (!c->d.pop_cnt && (rc = dalloc(&c->d.pop_cnt, 1))) return rc;
+            if (!c->d.pop_rho && (rc = dalloc(&c->d.pop_rho, N))) return rc;
+            CK(cudaMemset(c->d.pop_cnt, 0, sizeof(int)));
+        }
         if (c->d.npbc && c->P.lb_solve && !c->d.remark) {
             if ((rc = dalloc(&c->d.remark, N))) return rc;
             CK(cudaMemset(c->d.remark, 0, sizeof(uint32_t) * N));
@@ -512,9 +540,11 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         return seterr(HB_ERR_CUDA, "lattice init: %s", cudaGetErrorString(cudaGetLastError()));
     if (slip_init(c)) return seterr(HB_ERR_CUDA, "slip-wall list: %s", cudaGetErrorString(cudaGetLastError()));
     if (curved_init(c)) return seterr(HB_ERR_CUDA, "curved-wall list: %s", cudaGetErrorString(cudaGetLastError()));
-    // count dynamic-wall nodes
+    // count dynamic-wall nodes (the context stream does not synchronise with the default
+    // stream: wait for the init kernels first)
     {
         std::vector<uint8_t> t(N);
+        CK(cudaStreamSynchronize(c->stream));
         CK(cudaMemcpy(t.data(), c->ntype, N, cudaMemcpyDeviceToHost));
         c->has_dynwall = false;
         for (long long i = 0; i < N; ++i)
@@ -554,7 +584,7 @@ static int enqueue_cycle(hb_ctx* c, int cur) {
     // R (element forces of the previous lattice step) + DEM substeps + coupling masks
     if (dem && launch_cycle_coop(c, 1, 1, c->P.lb_solve ? 1 : 0)) return -1;
     if (!c->P.lb_solve) return 0;
-    if (dem) launch_couple(c, false);
+    if (dem) launch_couple(c, false, cur);
     if (c->P.free_surface) launch_fs_step(c, cur);
     launch_lb_step(c, cur);
     if (c->has_dynwall) launch_lb_wallforce(c, cur);
@@ -634,7 +664,7 @@ static int run_cycles(hb_ctx* c, int n, bool last_mirror) {
         if (c->P.dem_solve && c->d.E > 0) c->dem_stepped = true;
         if (c->P.lb_solve) {
             c->cur ^= 1;
-            c->reduce_pending = true;
+            c->reduce_pending = c->P.coupling != HB_MOVING_BB;  // the sums lag the lattice step
         }
         ++c->steps;
     }
@@ -664,7 +694,7 @@ int hb_fs_step(hb_ctx* c) {
 int hb_coupling_step(hb_ctx* c) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
     if (c->P.dem_solve && c->d.E > 0) {
-        launch_couple(c, true);
+        launch_couple(c, true, c->cur);
     }
     CK(cudaGetLastError());
     return HB_OK;
@@ -677,7 +707,7 @@ int hb_lb_step(hb_ctx* c) {
     if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
     if (!c->P.force_field) CK(cudaMemsetAsync(c->fs_force, 0, sizeof(double) * 3, c->stream));
     c->cur ^= 1;
-    c->reduce_pending = true;
+    c->reduce_pending = c->P.coupling != HB_MOVING_BB;  // the sums lag the lattice step
     ++c->steps;
     CK(cudaGetLastError());
     return HB_OK;
@@ -713,11 +743,18 @@ int hb_synchronize(hb_ctx* c) {
     int st[STATUS_WORDS];
     CK(cudaMemcpy(st, c->status, sizeof(st), cudaMemcpyDeviceToHost));
     if (st[1]) return seterr(HB_ERR_UNSUPPORTED, "TYPE ERROR: an active node links to an unsupported node type");
-    if (st[2])  // status word 2: 1 candidate list full, 2 particle outside the cell grid, 4 object list full
-        return seterr(HB_ERR_CAPACITY, "DEM list capacity exceeded (code %d:%s%s%s; limits %d candidates, %d objects)",
+    // status word 2: 1 candidate list full, 2 particle outside the cell grid, 4 object
+    // list full, 8 interface list full
+    if (st[2])
+        return seterr(HB_ERR_CAPACITY, "list capacity exceeded (code %d:%s%s%s%s; limits %d candidates per particle, "
+                      "%d objects per particle, %lld interface cells)",
                       st[2], (st[2] & 1) ? " candidate list full" : "",
                       (st[2] & 2) ? " a particle outside the DEM cell grid" : "",
-                      (st[2] & 4) ? " object list full" : "", NBR_CAP, OBJ_CAP);
+                      (st[2] & 4) ? " object list full" : "", (st[2] & 8) ? " interface list full" : "",
+                      c->d.nbr_cap, OBJ_CAP, (long long)c->fs_icap);
+    // status word 0: NaN/Inf density or velocity seen by a lattice kernel (the reference
+    // has no such check; its state would carry the NaN on)
+    if (st[0]) return seterr(HB_ERR_NUMERIC, "NaN or Inf in a node's density or velocity");
     return HB_OK;
 }
 
@@ -762,43 +799,69 @@ int hb_download_lattice(hb_ctx* c, uint8_t* type, uint8_t* inside, uint32_t* sol
     return HB_OK;
 }
 
-int hb_download_elements(hb_ctx* c, double* x0, double* x1, double* w, double* q0, double* fhydro, double* mhydro,
-                         double* fparticle, double* fwall, double* mparticle, double* mwall, double* fluid_volume) {
-    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+}  // extern "C"
+
+// Queues, on the context stream behind the steps already issued, the element-force
+// conversion of the last lattice step (LB.cpp:1851-1919) where it is pending and one
+// gather of the requested fields into the device staging block.  With the FP32/FP16
+// lattice the element sums are read from their fixed-point accumulators inside the
+// gather (the next cycle converts them itself); the FP64 form reduces them first.
+// items[k].dst non-null selects field k; *g receives the staging offsets.
+namespace {
+struct ElemItem {
+    double* dst;
+    double* src;
+    int comps;
+    int hsum;
+};
+constexpr int kElemItems = 11;
+
+int enqueue_element_gather(hb_ctx* c, double* const dst[kElemItems], ElemItem items[kElemItems], hb::GatherArgs* g) {
     const int E = c->d.E;
-    if (E == 0) return HB_OK;
-    // Everything is queued on the context stream behind the steps already issued: the
-    // element-force conversion of the last lattice step (LB.cpp:1851-1919), one gather of
-    // the requested fields into a device staging block, one copy into pinned host memory.
-    // With the FP32/FP16 lattice the element sums are read from their fixed-point
-    // accumulators inside the gather (the next cycle converts them itself); the FP64 form
-    // reduces them first.
     const bool inline_sums = c->reduce_pending && c->hacc;
     if (c->reduce_pending && !c->hacc) launch_couple_reduce(c);
-    struct { double* dst; double* src; int comps; int hsum; } items[] = {
-        {x0, c->d.x[0], 3, -1}, {x1, c->d.x[1], 3, -1}, {w, c->d.wG, 3, -1}, {q0, c->d.q[0], 4, -1},
-        {fhydro, c->d.FH, 3, inline_sums ? 0 : -1}, {mhydro, c->d.MH, 3, inline_sums ? 3 : -1},
-        {fparticle, c->d.FP, 3, -1}, {fwall, c->d.FW, 3, -1}, {mparticle, c->d.MP, 3, -1},
-        {mwall, c->d.MW, 3, -1}, {fluid_volume, c->d.fvol, 1, inline_sums ? 6 : -1}};
+    const ElemItem all[kElemItems] = {
+        {dst[0], c->d.x[0], 3, -1}, {dst[1], c->d.x[1], 3, -1}, {dst[2], c->d.wG, 3, -1}, {dst[3], c->d.q[0], 4, -1},
+        {dst[4], c->d.FH, 3, inline_sums ? 0 : -1}, {dst[5], c->d.MH, 3, inline_sums ? 3 : -1},
+        {dst[6], c->d.FP, 3, -1}, {dst[7], c->d.FW, 3, -1}, {dst[8], c->d.MP, 3, -1},
+        {dst[9], c->d.MW, 3, -1}, {dst[10], c->d.fvol, 1, inline_sums ? 6 : -1}};
+    for (int k = 0; k < kElemItems; ++k) items[k] = all[k];
     if (!c->d_stage) {
         int rc = dalloc(&c->d_stage, (size_t)hb::STAGE_DOUBLES_PER_ELEMENT * E);
         if (rc) return rc;
         CK(cudaMallocHost((void**)&c->h_stage, sizeof(double) * hb::STAGE_DOUBLES_PER_ELEMENT * E));
     }
-    hb::GatherArgs g = {};
-    g.E = E;
-    g.hacc = c->hacc;
-    for (auto& it : items)
-        if (it.dst) {
-            g.src[g.n] = it.src;
-            g.hsum[g.n] = it.hsum;
-            g.off[g.n + 1] = g.off[g.n] + (long long)it.comps * E;
-            ++g.n;
+    *g = hb::GatherArgs{};
+    g->E = E;
+    g->hacc = c->hacc;
+    for (int k = 0; k < kElemItems; ++k)
+        if (items[k].dst) {
+            g->src[g->n] = items[k].src;
+            g->hsum[g->n] = items[k].hsum;
+            g->off[g->n + 1] = g->off[g->n] + (long long)items[k].comps * E;
+            ++g->n;
         }
-    if (g.n == 0) return HB_OK;
-    const long long total = g.off[g.n];
-    hb::k_gather<<<(unsigned)ceil_div(total, 256), 256, 0, c->stream>>>(g, c->d_stage);
-    CK(cudaMemcpyAsync(c->h_stage, c->d_stage, sizeof(double) * total, cudaMemcpyDeviceToHost, c->stream));
+    if (g->n == 0) return HB_OK;
+    const long long total = g->off[g->n];
+    hb::k_gather<<<(unsigned)ceil_div(total, 256), 256, 0, c->stream>>>(*g, c->d_stage);
+    CK(cudaGetLastError());
+    return HB_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int hb_download_elements(hb_ctx* c, double* x0, double* x1, double* w, double* q0, double* fhydro, double* mhydro,
+                         double* fparticle, double* fwall, double* mparticle, double* mwall, double* fluid_volume) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    if (c->d.E == 0) return HB_OK;
+    double* const dst[kElemItems] = {x0, x1, w, q0, fhydro, mhydro, fparticle, fwall, mparticle, mwall, fluid_volume};
+    ElemItem items[kElemItems];
+    hb::GatherArgs g;
+    int rc = enqueue_element_gather(c, dst, items, &g);
+    if (rc || g.n == 0) return rc;
+    // one copy of the whole staging block into the library's pinned block, then host copies
+    CK(cudaMemcpyAsync(c->h_stage, c->d_stage, sizeof(double) * g.off[g.n], cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     int k = 0;
     for (auto& it : items)
@@ -809,17 +872,52 @@ int hb_download_elements(hb_ctx* c, double* x0, double* x1, double* w, double* q
     return HB_OK;
 }
 
+int hb_download_elements_async(hb_ctx* c, double* x0, double* x1, double* w, double* q0, double* fhydro,
+                               double* mhydro, double* fparticle, double* fwall, double* mparticle, double* mwall,
+                               double* fluid_volume) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    if (c->d.E == 0) return HB_OK;
+    double* const dst[kElemItems] = {x0, x1, w, q0, fhydro, mhydro, fparticle, fwall, mparticle, mwall, fluid_volume};
+    ElemItem items[kElemItems];
+    hb::GatherArgs g;
+    int rc = enqueue_element_gather(c, dst, items, &g);
+    if (rc || g.n == 0) return rc;
+    // one copy per field straight into the caller's arrays, ordered behind the gather; the
+    // next gather into the staging block is ordered behind these copies on the same stream
+    int k = 0;
+    for (auto& it : items)
+        if (it.dst) {
+            CK(cudaMemcpyAsync(it.dst, c->d_stage + g.off[k], sizeof(double) * (g.off[k + 1] - g.off[k]),
+                               cudaMemcpyDeviceToHost, c->stream));
+            ++k;
+        }
+    return HB_OK;
+}
+
+int hb_host_register(void* p, size_t bytes) {
+    if (!p || bytes == 0) return seterr(HB_ERR_ARG, "null pointer or zero size");
+    CK(cudaHostRegister(p, bytes, cudaHostRegisterDefault));
+    return HB_OK;
+}
+
+int hb_host_unregister(void* p) {
+    if (!p) return seterr(HB_ERR_ARG, "null pointer");
+    CK(cudaHostUnregister(p));
+    return HB_OK;
+}
+
 int hb_download_pairs(hb_ctx* c, uint32_t* pairs, int64_t capacity, int64_t* count) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
     CK(cudaStreamSynchronize(c->stream));
     const int E = c->d.P;  // particles (standard ones own the lists)
     std::vector<uint32_t> out;
     if (E > 0) {
-        std::vector<int> nb((size_t)E * NBR_CAP), cnt(E);
+        const size_t cap = (size_t)c->d.nbr_cap;
+        std::vector<int> nb((size_t)E * cap), cnt(E);
         CK(cudaMemcpy(nb.data(), c->d.nbr, sizeof(int) * nb.size(), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(cnt.data(), c->d.nbr_cnt, sizeof(int) * E, cudaMemcpyDeviceToHost));
         for (int i = 0; i < E; ++i) {
-            std::vector<int> js(nb.begin() + (size_t)i * NBR_CAP, nb.begin() + (size_t)i * NBR_CAP + cnt[i]);
+            std::vector<int> js(nb.begin() + (size_t)i * cap, nb.begin() + (size_t)i * cap + cnt[i]);
             std::sort(js.begin(), js.end());
             for (int j : js)
                 if (j > i) { out.push_back((uint32_t)i); out.push_back((uint32_t)j); }
@@ -1090,12 +1188,12 @@ int hb_profile_phases(hb_ctx* c, int32_t nsteps, double* us, int32_t* nphases) {
     for (auto& e : ev) CK(cudaEventCreate(&e));
     for (int s = 0; s < nsteps; ++s) {
         if (launch_cycle_coop(c, 1, 1, 1, ts + (size_t)s * np)) { cudaFree(ts); return seterr(HB_ERR_CUDA, "cycle launch failed"); }
-        launch_couple(c, false, ev.data() + 4 * (size_t)s);
+        launch_couple(c, false, c->cur, ev.data() + 4 * (size_t)s);
         if (c->P.free_surface) launch_fs_step(c, c->cur);
         launch_lb_step(c, c->cur);
         if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
         c->cur ^= 1;
-        c->reduce_pending = true;
+        c->reduce_pending = c->P.coupling != HB_MOVING_BB;  // the sums lag the lattice step
         ++c->steps;
     }
     CK(cudaStreamSynchronize(c->stream));
@@ -1131,7 +1229,7 @@ int hb_time_cycles(hb_ctx* c, int32_t nsteps, float* ms_total, float* ms_lb_kern
     CK(cudaEventRecord(c->ev0, c->stream));
     for (int s = 0; s < nsteps; ++s) {
         CK(cudaGraphLaunch(c->gexec[c->cur], c->stream));
-        if (c->P.lb_solve) { c->cur ^= 1; c->reduce_pending = true; }
+        if (c->P.lb_solve) { c->cur ^= 1; c->reduce_pending = c->P.coupling != HB_MOVING_BB; }
         ++c->steps;
     }
     CK(cudaEventRecord(c->ev1, c->stream));
@@ -1148,14 +1246,14 @@ int hb_time_cycles(hb_ctx* c, int32_t nsteps, float* ms_total, float* ms_lb_kern
         const bool dem = c->P.dem_solve && c->d.E > 0;
         for (int s = 0; s < nsteps; ++s) {
             if (dem && launch_cycle_coop(c, 1, 1, 1)) return seterr(HB_ERR_CUDA, "cycle launch failed");
-            if (dem) launch_couple(c, false);
+            if (dem) launch_couple(c, false, c->cur);
             if (c->P.free_surface) launch_fs_step(c, c->cur);
             CK(cudaEventRecord(ev[2 * s], c->stream));
             launch_lb_step(c, c->cur);
             CK(cudaEventRecord(ev[2 * s + 1], c->stream));
             if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
             c->cur ^= 1;
-            c->reduce_pending = true;
+            c->reduce_pending = c->P.coupling != HB_MOVING_BB;  // the sums lag the lattice step
             ++c->steps;
         }
         CK(cudaStreamSynchronize(c->stream));

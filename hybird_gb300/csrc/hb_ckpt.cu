@@ -102,7 +102,7 @@ std::vector<Buf> state_buffers(hb_ctx* c) {
             add("part_cen", d.pcen, 8 * 3 * S);
             add("dem_size", d.esize, 4 * E);
         }
-        add("nbr", d.nbr, 4 * Pl * hb::NBR_CAP);
+        add("nbr", d.nbr, 4 * Pl * d.nbr_cap);
         add("nbr_cnt", d.nbr_cnt, 4 * Pl);
         add("wall_of", d.wall_of, 4 * Pl);
         add("obj", d.obj, 4 * Pl * hb::OBJ_CAP);

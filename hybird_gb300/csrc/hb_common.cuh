@@ -27,7 +27,7 @@ namespace hb {
 
 constexpr int Q = 19;
 constexpr int MAX_WALLS = 6;
-constexpr int NBR_CAP = 48;      // candidate neighbours kept per particle
+constexpr int NBR_CAP = 48;      // candidate neighbours kept per particle unless hb_params.cap_neighbors says otherwise
 constexpr int OBJ_CAP = 16;      // objects in range kept per particle
 constexpr int STATUS_WORDS = 8;  // device status words (numeric, capacity, wait, ...)
 constexpr int PARTIAL_CAP = 4096;  // per-block partials of grid-wide reductions (>= any grid used)
@@ -60,6 +60,9 @@ __device__ __forceinline__ bool is_active(uint8_t t) {
     const uint8_t c = t & HB_TYPE_MASK;
     return c == HB_T_FLUID || c == HB_T_INTERFACE;
 }
+// an active node the lattice updates: with moving bounce-back (mbb) the nodes inside
+// particles are solid
+__device__ __forceinline__ bool is_fluid(uint8_t t, int mbb) { return is_active(t) && !(mbb && (t & HB_INSIDE)); }
 
 // ---- population load/store cache policy ----------------------------------------------
 // HB_CACHE_HINT 1: streaming (evict-first) loads and stores; 0: default caching.
@@ -157,7 +160,8 @@ struct LBArgs {
     int visc_model;         // bit0 Bingham, bit1 Smagorinsky
     double plastic_visc, yield_stress, turb_const;
     int free_surface;
-    int couple;
+    int couple;             // direct forcing of the nodes inside particles
+    int mbb;                // moving bounce-back: nodes inside particles are solid
     Particles parts;
     int* status;            // [STATUS_WORDS]
     double* wall_part;      // [grid * (MAX_WALLS*3 + 1)] per-CTA moving-wall partials

@@ -25,6 +25,7 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     double *wG, *wL, *wpG, *wpL;
     double *FH, *MH, *FP, *FW, *MP, *MW;
     double *fvol, *m, *I, *rad;
+    double* alt = nullptr;      // [9E] second copy of the predicted position, velocity and global spin
     float* pf = nullptr;        // [12(E+gcap)] FP32 centre/velocity/wGlobal(+pad) per particle (ghosts after the elements)
     int* plain = nullptr;       // [E] 1: orientation stays the identity (component-parallel Gear)
     // neighbour structures
@@ -33,7 +34,8 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     int* cell_start = nullptr;  // [nc+1]
     int* cell_fill = nullptr;   // [nc]
     int* cell_items = nullptr;  // [E + gcap]
-    int* nbr = nullptr;         // [E*NBR_CAP]
+    int* nbr = nullptr;         // [E*nbr_cap]
+    int nbr_cap = hb::NBR_CAP;  // candidate partners kept per particle
     int* nbr_cnt = nullptr;     // [E]
     int* wall_of = nullptr;     // [E] first wall in range or -1
     int* obj = nullptr;         // [E*OBJ_CAP]
@@ -44,6 +46,9 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     double* react = nullptr;    // [3*(MAX_WALLS + O)] wall and object FParticle (ordered sums of the records)
     uint32_t* claim_list = nullptr;  // [2N] (node, particle) pairs joined by the coupling in this step
     int* claim_cnt = nullptr;
+    uint32_t* pop_list = nullptr;    // [N] nodes a particle uncovered in this step (moving bounce-back)
+    int* pop_cnt = nullptr;
+    double* pop_rho = nullptr;       // [N] their refill density
     void* boxes = nullptr;      // [E+gcap] per-particle spheres of the current step (coupling masks)
     void* gargs = nullptr;      // device copy of the DEM/coupling parameter blocks
     double* scal = nullptr;     // device scalars: [0]=maxDisp [1]=rebuild flag [2]=contacts
@@ -143,7 +148,8 @@ struct hb_ctx {
     double* fs_part = nullptr;      // per-block FP64 partials for the surplus ledger
     int* fs_cnt = nullptr;          // per-block interface counts
     int* fs_first = nullptr;        // [6] 1 until the first free-surface step has run; counters
-    uint32_t* fs_ilist = nullptr;   // [N] interface cells at the start of a step
+    uint32_t* fs_ilist = nullptr;   // [fs_icap] interface cells at the start of a step
+    long long fs_icap = 0;          // its capacity (hb_params.cap_interface, 0: every node)
     // cylinders and curved walls (hb_curved.cu)
     std::vector<hb_cyl_host> cyl;
     void* curved_list = nullptr;
@@ -180,7 +186,11 @@ int launch_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside,
 int launch_download_lattice(hb_ctx* c, double* f_dev, int which_parity);
 int launch_ghosts_init(hb_ctx* c);
 int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsigned long long* ts = nullptr);
-void launch_couple(hb_ctx* c, bool build_boxes, cudaEvent_t* ev = nullptr);
+void launch_couple(hb_ctx* c, bool build_boxes, int cur, cudaEvent_t* ev = nullptr);
+// moving bounce-back (hb_lb.cu): refill of uncovered nodes and link masks after the
+// coupling masks; element force and torque after the lattice step
+void launch_mbb_nodes(hb_ctx* c, int cur);
+void launch_mbb_force(hb_ctx* c, int cur);
 void launch_dem_first_predict(hb_ctx* c);
 void launch_couple_reduce(hb_ctx* c);
 void launch_reactions(hb_ctx* c);

@@ -38,10 +38,15 @@ struct DemArgs {
     double *wG, *wL, *wpG, *wpL;
     double *FH, *MH, *FP, *FW, *MP, *MW;
     double *fvol, *m, *I, *rad;
+    // second copy of the predicted position, velocity and global spin (the fields a
+    // contact partner reads): the single-barrier substep of plain spheres reads one copy
+    // and predicts into the other, alternating by substep
+    double *xq0, *xq1, *wqG;
     float* pf;         // [12E] FP32 centre, velocity, spin (+ pad) per particle
     const int* plain;  // 1: orientation fixed at identity (no quaternion rates)
     int *cell_of, *cell_cnt, *cell_start, *cell_fill, *cell_items;
     int *nbr, *nbr_cnt, *wall_of, *obj, *obj_cnt;
+    int nbr_cap;          // candidate partners kept per particle (hb_params.cap_neighbors)
     double *wrec, *orec;  // wall / object contact records of the current substep (7 doubles each)
     int* cyl_of;          // [E] first cylinder in range or -1 (DEM.cpp:1535-1550)
     int ncyl;
@@ -113,6 +118,20 @@ __device__ __forceinline__ V project(V v, Qt q) {  // vector.cpp:364-370
     return V{r.b, r.c, r.d};
 }
 __device__ __forceinline__ Qt qaxpy(Qt a, Qt b, double s) { return Qt{a.a + b.a * s, a.b + b.b * s, a.c + b.c * s, a.d + b.d * s}; }
+
+// Where the predicted position, velocity and global spin are read (r) and where the
+// predictor writes the next substep's (w): the same arrays when a substep has a barrier
+// between its force and corrector phases, alternate copies in the single-barrier substep.
+struct PredBuf {
+    const double *x0r, *x1r, *wGr;
+    double *x0w, *x1w, *wGw;
+};
+__device__ __forceinline__ PredBuf pred_inplace(const DemArgs& a) {
+    return PredBuf{a.xp0, a.xp1, a.wpG, a.xp0, a.xp1, a.wpG};
+}
+__device__ __forceinline__ PredBuf pred_alternate(const DemArgs& a, int par) {
+    return par ? PredBuf{a.xq0, a.xq1, a.wqG, a.xp0, a.xp1, a.wpG} : PredBuf{a.xp0, a.xp1, a.wpG, a.xq0, a.xq1, a.wqG};
+}
 
 __device__ double normal_contact(const DemArgs& a, double overlap, double vn, double effRad, double effMass) {
     if (a.model == HB_HERTZIAN) {  // DEM.cpp:2142-2152
@@ -210,13 +229,13 @@ __device__ __noinline__ void nl_build_one(const DemArgs& a, int i) {
                         if (j == i) continue;
                         const V d = sub(ld3(a.x0, E, j), xi);
                         if (nrm2(d) < r2) {
-                            if (cnt < NBR_CAP) a.nbr[(long long)i * NBR_CAP + cnt] = j;
+                            if (cnt < a.nbr_cap) a.nbr[(long long)i * a.nbr_cap + cnt] = j;
                             ++cnt;
                         }
                     }
                 }
     }
-    if (cnt > NBR_CAP) { atomicOr(a.status + 2, 1); cnt = NBR_CAP; }
+    if (cnt > a.nbr_cap) { atomicOr(a.status + 2, 1); cnt = a.nbr_cap; }
     a.nbr_cnt[i] = cnt;
     nl_near_one(a, i);
 }
@@ -407,7 +426,7 @@ __device__ __noinline__ void ghosts_block(const DemArgs& a) {
 
 __device__ __forceinline__ void nbr_push(const DemArgs& a, int i, int j) {
     const int k = atomicAdd(a.nbr_cnt + i, 1);
-    if (k < NBR_CAP) a.nbr[(long long)i * NBR_CAP + k] = j;
+    if (k < a.nbr_cap) a.nbr[(long long)i * a.nbr_cap + k] = j;
 }
 
 // The reference's sweep (DEM.cpp:1425-1479) from particle p's cell: the 14 half-shell
@@ -451,8 +470,8 @@ __device__ __noinline__ void nl_pairs_pbc(const DemArgs& a, int p) {
 // a standard particle's list in ascending order (the pushes come in any order)
 __device__ __noinline__ void nl_sort_one(const DemArgs& a, int i) {
     int cnt = a.nbr_cnt[i];
-    if (cnt > NBR_CAP) { atomicOr(a.status + 2, 1); cnt = NBR_CAP; a.nbr_cnt[i] = cnt; }
-    int* l = a.nbr + (long long)i * NBR_CAP;
+    if (cnt > a.nbr_cap) { atomicOr(a.status + 2, 1); cnt = a.nbr_cap; a.nbr_cnt[i] = cnt; }
+    int* l = a.nbr + (long long)i * a.nbr_cap;
     for (int k = 1; k < cnt; ++k) {
         const int v = l[k];
         int m = k - 1;
@@ -472,11 +491,11 @@ struct FM {
 
 // particleParticleCollision with I = lower index (DEM.cpp:1801-1900), seen by particle i
 __device__ __noinline__ FM pp_contact(const DemArgs& a, int i, int I, int J, V vd, double rI, double rJ, V FP,
-                                      V MP) {
+                                      V MP, PredBuf pb) {
     const int E = a.E, eI = I, eJ = J;
     const double dist = sqrt(nrm2(vd));
     const double overlap = rI + rJ - dist;
-    const V relVel = sub(ld3(a.xp1, E, eJ), ld3(a.xp1, E, eI));
+    const V relVel = sub(ld3(pb.x1r, E, eJ), ld3(pb.x1r, E, eI));
     const V en = divs(vd, dist);
     const double vn = dot(relVel, en);
     const V nrv = mul(vn, en);
@@ -486,7 +505,7 @@ __device__ __noinline__ FM pp_contact(const DemArgs& a, int i, int I, int J, V v
     const double fn = normal_contact(a, overlap, vn, effRad, effMass);
     const V nf = mul(fn, en);
     const V vrI = mul(rI, en), vrJ = mul(-rJ, en);
-    const V rvc = add(sub(relVel, cross(ld3(a.wpG, E, eI), vrI)), cross(ld3(a.wpG, E, eJ), vrJ));
+    const V rvc = add(sub(relVel, cross(ld3(pb.wGr, E, eI), vrI)), cross(ld3(pb.wGr, E, eJ), vrJ));
     const V tang = sub(rvc, nrv);
     const double nt = sqrt(nrm2(tang));
     V tf{0, 0, 0};
@@ -605,91 +624,103 @@ __device__ __noinline__ FM cylinder_contact(const DemArgs& a, int c, V xpi, doub
     return FM{FW, MW};
 }
 
-// contacts of particle i by one warp: lanes take candidates (and objects) in list
-// order, the sums use a fixed xor-shuffle tree, so the result is reproducible
+// contacts of element i by its group of eight lanes (c = 0..7 of group grp of the
+// warp): the lanes take candidates (and objects) in list order, lane c == 0 the wall and
+// cylinder; the sums use a fixed xor-shuffle tree within the group, so the result is
+// reproducible and every lane of the group ends with the totals in v (FParticle,
+// MParticle, FWall, MWall).  All 32 lanes of the warp call it (on false for a group
+// without an element), because the tree shuffles across the whole warp.
 // a: the kernel's parameter block; ga: its device-memory copy for the out-of-line calls
-__device__ void forces_warp(const DemArgs& a, const DemArgs& ga, int i, int lane, int& ncont) {
+__device__ __forceinline__ void forces_group(const DemArgs& a, const DemArgs& ga, int i, bool on, int c, PredBuf pb,
+                                             int& ncont, double v[12]) {
     const int E = a.E;
-    const V xpi = ld3(a.xp0, E, i);
     V FP{0, 0, 0}, MP{0, 0, 0}, FW{0, 0, 0}, MW{0, 0, 0};
     bool contrib = false;  // this lane added a contact, wall or object force
-    const int cnt = a.nbr_cnt[i];
-    for (int k = lane; k < cnt; k += 32) {
-        const int j = a.nbr[(long long)i * NBR_CAP + k];
-        const int I = min(i, j), J = max(i, j);
-        const double rI = a.rad[I], rJ = a.rad[J];
-        const double sig = rI + rJ;
-        const V vd = sub(ld3(a.xp0, E, J), ld3(a.xp0, E, I));
-        if (!(nrm2(vd) < sig * sig)) continue;
-        if (i < j) ++ncont;
-        contrib = true;
-        const FM r = pp_contact(ga, i, I, J, vd, rI, rJ, FP, MP);
-        FP = r.f;
-        MP = r.m;
-    }
-    const double ri = a.rad[i], mi = a.m[i];
-    const V xpv = ld3(a.xp1, E, i);
-    const V wpg = ld3(a.wpG, E, i);
-    const int w = a.wall_of[i];
-    if (lane == 0) {  // wallParticleCollision (DEM.cpp:1902-1982), static walls
-        bool hit = false;
-        if (w >= 0) {
-            const V wn{a.wn[w][0], a.wn[w][1], a.wn[w][2]};
-            const double dist = dot(wn, sub(xpi, V{a.wp[w][0], a.wp[w][1], a.wp[w][2]}));
-            const double overlap = ri - dist;
-            if (overlap > 0.0) {
-                contrib = hit = true;
-                const FM r = wall_contact(ga, wn, overlap, xpv, wpg, ri, mi, FW, MW, a.wrec + 7 * (long long)i);
-                FW = r.f;
-                MW = r.m;
+    if (on) {
+        const V xpi = ld3(pb.x0r, E, i);
+        const int cnt = a.nbr_cnt[i];
+        for (int k = c; k < cnt; k += 8) {
+            const int j = a.nbr[(long long)i * a.nbr_cap + k];
+            const int I = min(i, j), J = max(i, j);
+            const double rI = a.rad[I], rJ = a.rad[J];
+            const double sig = rI + rJ;
+            const V vd = sub(ld3(pb.x0r, E, J), ld3(pb.x0r, E, I));
+            if (!(nrm2(vd) < sig * sig)) continue;
+            if (i < j) ++ncont;
+            contrib = true;
+            const FM r = pp_contact(ga, i, I, J, vd, rI, rJ, FP, MP, pb);
+            FP = r.f;
+            MP = r.m;
+        }
+        const double ri = a.rad[i], mi = a.m[i];
+        const V xpv = ld3(pb.x1r, E, i);
+        const V wpg = ld3(pb.wGr, E, i);
+        if (c == 0) {  // wallParticleCollision (DEM.cpp:1902-1982), static walls
+            const int w = a.wall_of[i];
+            bool hit = false;
+            if (w >= 0) {
+                const V wn{a.wn[w][0], a.wn[w][1], a.wn[w][2]};
+                const double dist = dot(wn, sub(xpi, V{a.wp[w][0], a.wp[w][1], a.wp[w][2]}));
+                const double overlap = ri - dist;
+                if (overlap > 0.0) {
+                    contrib = hit = true;
+                    const FM r = wall_contact(ga, wn, overlap, xpv, wpg, ri, mi, FW, MW, a.wrec + 7 * (long long)i);
+                    FW = r.f;
+                    MW = r.m;
+                }
+            }
+            if (!hit) a.wrec[7 * (long long)i] = 0.0;
+            const int cy = a.cyl_of[i];
+            if (cy >= 0) {  // cylinderParticelContacts (DEM.cpp:1719-1746)
+                const V d = sub(xpi, V{a.cp1[cy][0], a.cp1[cy][1], a.cp1[cy][2]});
+                const V nx{a.cnax[cy][0], a.cnax[cy][1], a.cnax[cy][2]};
+                const double dist = a.cR[cy] - sqrt(nrm2(sub(mul(dot(d, nx), nx), d)));
+                const double overlap = ri - dist;
+                if (overlap > 0.0) {
+                    contrib = true;
+                    const FM r = cylinder_contact(ga, cy, xpi, overlap, xpv, wpg, ri, mi, FW, MW);
+                    FW = r.f;
+                    MW = r.m;
+                }
             }
         }
-        if (!hit) a.wrec[7 * (long long)i] = 0.0;
-        const int cy = a.cyl_of[i];
-        if (cy >= 0) {  // cylinderParticelContacts (DEM.cpp:1719-1746)
-            const V d = sub(xpi, V{a.cp1[cy][0], a.cp1[cy][1], a.cp1[cy][2]});
-            const V nx{a.cnax[cy][0], a.cnax[cy][1], a.cnax[cy][2]};
-            const double dist = a.cR[cy] - sqrt(nrm2(sub(mul(dot(d, nx), nx), d)));
-            const double overlap = ri - dist;
-            if (overlap > 0.0) {
-                contrib = true;
-                const FM r = cylinder_contact(ga, cy, xpi, overlap, xpv, wpg, ri, mi, FW, MW);
-                FW = r.f;
-                MW = r.m;
+        const int oc = a.obj_cnt[i];
+        for (int k = c; k < oc; k += 8) {  // objectParticleCollision (DEM.cpp:2060-2136)
+            const int o = a.obj[(long long)i * OBJ_CAP + k];
+            const V vd = sub(xpi, V{a.ox0[o], a.ox0[a.O + o], a.ox0[2 * a.O + o]});
+            const double dist = sqrt(nrm2(vd));
+            const double overlap = ri + a.orad[o] - dist;
+            double* rec = a.orec + 7 * ((long long)i * OBJ_CAP + k);
+            if (!(overlap > 0.0)) {
+                rec[0] = 0.0;
+                continue;
             }
+            contrib = true;
+            const FM r = object_contact(ga, o, vd, dist, overlap, xpv, wpg, ri, mi, FW, MW, rec);
+            FW = r.f;
+            MW = r.m;
         }
     }
-    const int oc = a.obj_cnt[i];
-    for (int k = lane; k < oc; k += 32) {  // objectParticleCollision (DEM.cpp:2060-2136)
-        const int o = a.obj[(long long)i * OBJ_CAP + k];
-        const V vd = sub(xpi, V{a.ox0[o], a.ox0[a.O + o], a.ox0[2 * a.O + o]});
-        const double dist = sqrt(nrm2(vd));
-        const double overlap = ri + a.orad[o] - dist;
-        double* rec = a.orec + 7 * ((long long)i * OBJ_CAP + k);
-        if (!(overlap > 0.0)) {
-            rec[0] = 0.0;
-            continue;
-        }
-        contrib = true;
-        const FM r = object_contact(ga, o, vd, dist, overlap, xpv, wpg, ri, mi, FW, MW, rec);
-        FW = r.f;
-        MW = r.m;
-    }
-    // fixed xor-shuffle tree over the lanes; when at most lane 0 holds a force the tree
-    // would only add zeros to it, so it is skipped
+    // fixed xor-shuffle tree within each group of eight lanes; skipped when in every group
+    // at most the group's first lane holds a force (the tree would only add zeros)
     const unsigned who = __ballot_sync(0xffffffffu, contrib);
-    double v[12] = {FP.x, FP.y, FP.z, MP.x, MP.y, MP.z, FW.x, FW.y, FW.z, MW.x, MW.y, MW.z};
-    if (who & ~1u) {
+    v[0] = FP.x; v[1] = FP.y; v[2] = FP.z; v[3] = MP.x; v[4] = MP.y; v[5] = MP.z;
+    v[6] = FW.x; v[7] = FW.y; v[8] = FW.z; v[9] = MW.x; v[10] = MW.y; v[11] = MW.z;
+    if (who & ~0x01010101u) {
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1)
+        for (int off = 1; off < 8; off <<= 1)
 #pragma unroll
-            for (int c = 0; c < 12; ++c) v[c] += __shfl_xor_sync(0xffffffffu, v[c], off);
+            for (int q = 0; q < 12; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
+    } else {  // the group's first lane holds the totals: hand them to the other seven
+#pragma unroll
+        for (int q = 0; q < 12; ++q) v[q] = __shfl_sync(0xffffffffu, v[q], threadIdx.x & 24);
     }
-    if (lane != 0) return;
-    st3(a.FP, E, i, V{v[0], v[1], v[2]});
-    st3(a.MP, E, i, V{v[3], v[4], v[5]});
-    st3(a.FW, E, i, V{v[6], v[7], v[8]});
-    st3(a.MW, E, i, V{v[9], v[10], v[11]});
+    if (on && c == 0) {
+        st3(a.FP, E, i, V{v[0], v[1], v[2]});
+        st3(a.MP, E, i, V{v[3], v[4], v[5]});
+        st3(a.FW, E, i, V{v[6], v[7], v[8]});
+        st3(a.MW, E, i, V{v[9], v[10], v[11]});
+    }
 }
 
 // ---- per-particle path (periodic faces, multi-sphere elements) ---------------------------
@@ -770,7 +801,7 @@ __device__ void forces_gen(const DemArgs& a, const DemArgs& ga, int p, int lane,
     bool contrib = false;
     const int cnt = a.nbr_cnt[p];
     for (int k = lane; k < cnt; k += 32) {
-        const int j = a.nbr[(long long)p * NBR_CAP + k];
+        const int j = a.nbr[(long long)p * a.nbr_cap + k];
         const int I = min(p, j), J = max(p, j);
         const int eI = a.pkey[I], eJ = a.pkey[J];
         const double rI = a.rad[eI], rJ = a.rad[eJ];
@@ -858,11 +889,11 @@ __device__ __forceinline__ void gather_one(const DemArgs& a, int e, int c) {
 }
 
 // Newton (DEM.cpp:1149-1181): accelerations from the forces of this substep
-__device__ void newton_one(const DemArgs& a, int i) {
+__device__ void newton_one(const DemArgs& a, int i, PredBuf pb) {
     const int E = a.E;
     const double ri = a.rad[i], mi = a.m[i];
-    const V xpv = ld3(a.xp1, E, i);
-    const V wpg = ld3(a.wpG, E, i);
+    const V xpv = ld3(pb.x1r, E, i);
+    const V wpg = ld3(pb.wGr, E, i);
     const double nv = a.numVisc;
     const V FVisc = mul(-6.0 * M_PI * nv * ri, xpv);
     const V MVisc = mul(-8.0 * M_PI * nv * ri * ri * ri, wpg);
@@ -888,19 +919,25 @@ __device__ void newton_one(const DemArgs& a, int i) {
 // The same for one Cartesian component of an identity-orientation element (lane c of
 // its six: 0-2 linear, 3-5 angular).  With qp0 = identity both projections return their
 // argument, so the arithmetic per component is that of newton_one.
-__device__ double newton_plain(const DemArgs& a, int i, int c) {
+// fa, fb: this component's FParticle and FWall (c < 3) or MParticle and MWall (c >= 3).
+// A spin lane reads all three components of the predicted local spin while the other two
+// spin lanes of its element may already be overwriting theirs with the next prediction:
+// the values enter only the Euler terms (I_y - I_z) w_y w_z, ..., which are exactly zero
+// for these elements (a single sphere has three equal principal moments), so the result
+// does not depend on which value is read.
+__device__ double newton_plain(const DemArgs& a, int i, int c, PredBuf pb, double fa, double fb) {
     const int E = a.E;
     const double ri = a.rad[i];
     const double nv = a.numVisc;
     if (c < 3) {
         const long long o = (long long)c * E + i;
-        const double fv = a.xp1[o] * (-6.0 * M_PI * nv * ri);
-        return (((fv + a.FH[o]) + a.FP[o]) + a.FW[o]) / a.m[i] + a.demF[c];
+        const double fv = pb.x1r[o] * (-6.0 * M_PI * nv * ri);
+        return (((fv + a.FH[o]) + fa) + fb) / a.m[i] + a.demF[c];
     }
     const int k = c - 3;
     const long long o = (long long)k * E + i;
-    const double mv = a.wpG[o] * (-8.0 * M_PI * nv * ri * ri * ri);
-    const double mom = ((mv + a.MH[o]) + a.MP[o]) + a.MW[o];
+    const double mv = pb.wGr[o] * (-8.0 * M_PI * nv * ri * ri * ri);
+    const double mom = ((mv + a.MH[o]) + fa) + fb;
     const double Ix = a.I[i], Iy = a.I[E + i], Iz = a.I[2 * E + i];
     const double wx = a.wpL[i], wy = a.wpL[E + i], wz = a.wpL[2 * E + i];
     if (k == 0) return (mom + (Iy - Iz) * wy * wz) / Ix;
@@ -1025,15 +1062,15 @@ __device__ double correct_one(const DemArgs& a, int i) {  // elmt.cpp:179-254
 // corrector (elmt.cpp:179-254) followed by the next substep's predictor
 // (elmt.cpp:139-177) on registers: every input is loaded before the first store, so the
 // element's loads overlap instead of waiting on each other
-__device__ __noinline__ double correct_predict_one(const DemArgs& a, int i) {
+__device__ __noinline__ double correct_predict_one(const DemArgs& a, int i, PredBuf pb) {
     const int E = a.E;
     const double dt = a.dt;
     const double* c = a.gc;
     const double* c1o = a.gc1;
     const double* c2o = a.gc2;
-    newton_one(a, i);
+    newton_one(a, i, pb);
     // loads
-    const V x2 = ld3(a.x2, E, i), xp0 = ld3(a.xp0, E, i), xp1 = ld3(a.xp1, E, i), xp2 = ld3(a.xp2, E, i),
+    const V x2 = ld3(a.x2, E, i), xp0 = ld3(pb.x0r, E, i), xp1 = ld3(pb.x1r, E, i), xp2 = ld3(a.xp2, E, i),
             xp3 = ld3(a.xp3, E, i), xp4 = ld3(a.xp4, E, i), xp5 = ld3(a.xp5, E, i);
     const V w1 = ld3(a.w1, E, i), wp0 = ld3(a.wp0, E, i), wp1 = ld3(a.wp1, E, i), wp2 = ld3(a.wp2, E, i),
             wp3 = ld3(a.wp3, E, i), wp4 = ld3(a.wp4, E, i), wp5 = ld3(a.wp5, E, i);
@@ -1090,13 +1127,13 @@ __device__ __noinline__ double correct_predict_one(const DemArgs& a, int i) {
     pq[0] = (float)x0.x; pq[1] = (float)x0.y; pq[2] = (float)x0.z;
     pq[3] = (float)x1.x; pq[4] = (float)x1.y; pq[5] = (float)x1.z;
     pq[6] = (float)w0.x; pq[7] = (float)w0.y; pq[8] = (float)w0.z;
-    st3(a.xp0, E, i, nxp0); st3(a.xp1, E, i, nxp1); st3(a.xp2, E, i, nxp2); st3(a.xp3, E, i, nxp3);
+    st3(pb.x0w, E, i, nxp0); st3(pb.x1w, E, i, nxp1); st3(a.xp2, E, i, nxp2); st3(a.xp3, E, i, nxp3);
     st3(a.xp4, E, i, nxp4); st3(a.xp5, E, i, x5);
     stq(a.qp0, E, i, nqp0); stq(a.qp1, E, i, nqp1); stq(a.qp2, E, i, nqp2); stq(a.qp3, E, i, nqp3);
     stq(a.qp4, E, i, nqp4); stq(a.qp5, E, i, q5);
     st3(a.wp0, E, i, nwp0); st3(a.wp1, E, i, nwp1); st3(a.wp2, E, i, nwp2); st3(a.wp3, E, i, nwp3);
     st3(a.wp4, E, i, nwp4); st3(a.wp5, E, i, w5);
-    st3(a.wpG, E, i, nwp0);
+    st3(pb.wGw, E, i, nwp0);
     st3(a.wpL, E, i, nwpL);
     return nrm2(x1);
 }
@@ -1107,7 +1144,7 @@ __device__ __noinline__ double correct_predict_one(const DemArgs& a, int i) {
 // Gear corrector+predictor splits into independent Cartesian components.  Six lanes
 // per element: lanes 0-2 take x, y, z of the position chain, lanes 3-5 of the spin
 // chain.  Same arithmetic per component as correct_predict_one.
-__device__ double correct_predict_plain(const DemArgs& a, int i, int c, double acc) {
+__device__ double correct_predict_plain(const DemArgs& a, int i, int c, double acc, PredBuf pb) {
     // Lanes 0-2 run the position chain (2nd order: the corrected derivative is x2, weights
     // gc2), lanes 3-5 the spin chain (1st order: w1, weights gc1).  Both have the same
     // shape, so one instruction stream with selected arrays and weights serves the whole
@@ -1123,8 +1160,12 @@ __device__ double correct_predict_plain(const DemArgs& a, int i, int c, double a
     double* const v3a = lin ? a.x3 : a.w3;
     double* const v4a = lin ? a.x4 : a.w4;
     double* const v5a = lin ? a.x5 : a.w5;
-    double* const n0a = lin ? a.xp0 : a.wp0;
-    double* const n1a = lin ? a.xp1 : a.wp1;
+    // read and written copies of the predicted position and velocity (the spin chain's
+    // predictions are the element's own)
+    const double* const n0r = lin ? pb.x0r : a.wp0;
+    const double* const n1r = lin ? pb.x1r : a.wp1;
+    double* const n0a = lin ? pb.x0w : a.wp0;
+    double* const n1a = lin ? pb.x1w : a.wp1;
     double* const n2a = lin ? a.xp2 : a.wp2;
     double* const n3a = lin ? a.xp3 : a.wp3;
     double* const n4a = lin ? a.xp4 : a.wp4;
@@ -1132,7 +1173,7 @@ __device__ double correct_predict_plain(const DemArgs& a, int i, int c, double a
     double co[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) co[k] = lin ? a.gc2[k] : a.gc1[k];
-    const double p0 = n0a[o], p1 = n1a[o], p2 = n2a[o], p3 = n3a[o], p4 = n4a[o], p5 = n5a[o];
+    const double p0 = n0r[o], p1 = n1r[o], p2 = n2a[o], p3 = n3a[o], p4 = n4a[o], p5 = n5a[o];
     const double d = acc - (lin ? p2 : p1);
     double v0 = p0 + d * co[0], v1 = p1 + d * co[1], v2 = p2 + d * co[2], v3 = p3 + d * co[3],
            v4 = p4 + d * co[4], v5 = p5 + d * co[5];
@@ -1154,7 +1195,7 @@ __device__ double correct_predict_plain(const DemArgs& a, int i, int c, double a
     }
     a.wG[o] = v0;
     a.wL[o] = v0;
-    a.wpG[o] = n0;
+    pb.wGw[o] = n0;
     a.wpL[o] = n0;
     a.pf[12 * (size_t)i + 6 + (c - 3)] = f0;
     return 0.0;
@@ -1182,6 +1223,10 @@ struct CoupleArgs {
     const unsigned long long* hacc;  // fixed-point element sums (FP32/FP16 lattice kernels)
     uint32_t* claim_list;       // [2N] (node, particle) joined in this step
     int* claim_cnt;
+    int mbb;                    // moving bounce-back: list the nodes that leave their particle
+    uint32_t* pop_list;         // [N] (their populations are refilled before the lattice step)
+    int* pop_cnt;
+    double* rho;
     struct PartBox* tab;        // [E] spheres of the current step
     const double* mass;
     int free_surface;
@@ -1342,6 +1387,14 @@ __device__ __forceinline__ void claim_push(const CoupleArgs& a, long long l, uns
     a.claim_list[2 * slot + 1] = (uint32_t)(best & 0xffffffffu);
 }
 
+// moving bounce-back: a node that leaves its particle becomes fluid and is refilled after
+// the masks; its density is marked NaN until then, so that the refill of a neighbouring
+// node does not average it
+__device__ __noinline__ void mbb_pop(const CoupleArgs& a, long long l) {
+    a.rho[l] = __longlong_as_double(0x7ff8000000000000LL);
+    a.pop_list[atomicAdd(a.pop_cnt, 1)] = (uint32_t)l;
+}
+
 // one node with the reference's full link rules (periodic remap, self-linked boundary)
 __device__ __noinline__ void mask_node_general(const CoupleArgs& a, int x, int y, int z) {
     const long long l = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
@@ -1349,6 +1402,7 @@ __device__ __noinline__ void mask_node_general(const CoupleArgs& a, int x, int y
     if (t & HB_INSIDE) {
         if (cover_first(a, a.solid[l], x, y, z) >= 0) return;  // stays
         a.ntype[l] = t & ~HB_INSIDE;                           // pop
+        if (a.mbb) mbb_pop(a, l);
     }
     unsigned long long best = ~0ull;
     for (int kk = 1; kk <= 6; ++kk) {  // source m with link d[m][kk] == l
@@ -1420,6 +1474,7 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
             const uint32_t sk = k == 0 ? sl[0] : (k == 1 ? sl[1] : (k == 2 ? sl[2] : sl[3]));  // registers
             if (in_sph(a.tab[sk].s, x, y, z)) continue;  // stays
             a.ntype[l] = t & ~HB_INSIDE;                     // pop
+            if (a.mbb) mbb_pop(a, l);
         }
         const bool ix = x >= 1 && x <= a.X - 2;
         // source flags in kk order: x-1, x+1, y-1, y+1, z-1, z+1 (pre- or post-pop)
@@ -1570,6 +1625,7 @@ struct CycleArgs {
     const DemArgs* gd;
     const CoupleArgs* gc;
     int do_reduce, do_dem, do_boxes, multi;
+    int bps;                 // resident blocks per SM of this launch (the grid is SMs x bps)
     unsigned long long* ts;  // optional phase timestamps (ns), written by block 0 after each barrier
 };
 
@@ -1585,11 +1641,12 @@ __device__ __forceinline__ void stamp(const CycleArgs& A, int k) {
 // out so that consecutive tasks land on different SMs first and on different warp
 // schedulers (warp index mod 4) second: an FP64 warp instruction costs the same narrow-
 // pipe time whatever its active lanes, so the schedulers' FP64 pipes, not the lanes, are
-// the resource.  With the grid as H = 2 blocks per SM slot: task p runs on block
-// (p mod S) + S * h and warp k mod W, where k = (p / S) mod (W * H), h = k / W.
-__device__ __forceinline__ void warp_tasks(int& first, int& stride) {
+// the resource.  With the grid as H blocks per SM slot (S = grid / H): task p runs on
+// block (p mod S) + S * h and warp k mod W, where k = (p / S) mod (W * H), h = k / W.
+__device__ __forceinline__ void warp_tasks(int& first, int& stride, int H) {
     const int B = gridDim.x, W = blockDim.x >> 5;
-    const int H = (B & 1) ? 1 : 2, S = B / H;
+    if (H < 1 || B % H) H = 1;
+    const int S = B / H;
     const int b = blockIdx.x, w = threadIdx.x >> 5;
     first = (b % S) + S * (w + W * (b / S));
     stride = B * W;
@@ -1629,10 +1686,20 @@ __device__ __noinline__ void part_predict_all(const DemArgs* gd, int gt, int gs)
     for (int p = gt; p < S; p += gs) part_predict(*gd, p);
 }
 
+// overlapping pairs of the last substep (integer atomics, so the count is exact)
+__device__ __forceinline__ void count_contacts(const CycleArgs& A, int s, int ncont) {
+    if (s != A.multi - 1) return;
+    for (int off = 16; off > 0; off >>= 1) ncont += __shfl_down_sync(0xffffffffu, ncont, off);
+    if ((threadIdx.x & 31) == 0 && ncont) {
+        atomicAdd(A.d.contacts, ncont);
+        atomicAdd(A.d.total_contacts, (unsigned long long)ncont);
+    }
+}
+
 // PBC: periodic faces with particles (ghost rebuilds); a separate instantiation, so the
 // calls of that path cost the other configurations no registers
 template <bool PBC>
-__global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
+__global__ void __launch_bounds__(256, PBC ? 2 : 1) k_cycle(CycleArgs A) {
     cg::grid_group grid = cg::this_grid();
     __shared__ double sh[7][256];
     const int E = A.d.E;
@@ -1642,7 +1709,7 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
     const int gs = gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
     int gw, nw;  // this warp's first task and the task stride (one warp per particle / group)
-    warp_tasks(gw, nw);
+    warp_tasks(gw, nw, A.bps);
     stamp(A, 0);
     if (A.do_reduce) {
         if (A.c.hacc) {
@@ -1669,50 +1736,80 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
                     if (blockIdx.x == 0) nl_cells_block(*A.gd);
                     grid.sync();
                     for (int i = gt; i < E; i += gs) nl_build_one(*A.gd, i);
-                    grid.sync();  // the contact warps read other threads' candidate lists
+                    grid.sync();  // the contact groups read other threads' candidate lists
                 }
             }
+            stamp(A, k++);
             int ncont = 0;
+            double v2 = 0.0;
             if (PBC) {
+                // per-particle path: forces into per-particle partials | barrier | element
+                // sums, Newton, corrector + predictor in place
+                const PredBuf pb = pred_inplace(A.d);
                 part_predict_all(A.gd, gt, gs);
                 grid.sync();
                 for (int p = gw; p < A.d.P; p += nw) forces_gen(A.d, *A.gd, p, lane, ncont);
-            } else {
-                for (int i = gw; i < E; i += nw) forces_warp(A.d, *A.gd, i, lane, ncont);
-            }
-            if (s == A.multi - 1) {  // overlapping pairs of the last substep (integer atomics)
-                for (int off = 16; off > 0; off >>= 1) ncont += __shfl_down_sync(0xffffffffu, ncont, off);
-                if ((threadIdx.x & 31) == 0 && ncont) {
-                    atomicAdd(A.d.contacts, ncont);
-                    atomicAdd(A.d.total_contacts, (unsigned long long)ncont);
-                }
-            }
-            grid.sync();
-            stamp(A, k++);
-            double v2 = 0.0;
-            {  // six lanes per element (five elements per warp, lanes 30-31 idle)
-                const int grp = lane / 6, c = lane - 6 * grp;
-                const int ngroups = 5 * nw;
-                for (int base = 5 * gw; base < E; base += ngroups) {
+                count_contacts(A, s, ncont);
+                grid.sync();
+                const int grp = lane / 6, c = lane - 6 * grp;  // six lanes per element, five per warp
+                for (int base = 5 * gw; base < E; base += 5 * nw) {
                     const int i = base + grp;
                     const bool on = grp < 5 && i < E;
                     const bool plain = on && A.d.plain[i];
-                    if (PBC && on) {  // element sums of its particles' contact forces
+                    if (on) {  // element sums of its particles' contact forces
                         if (plain) {  // the components lane c's Newton reads
                             gather_one(A.d, i, c);
                             gather_one(A.d, i, 6 + c);
                         } else if (c == 0) {
-                            for (int k = 0; k < 12; ++k) gather_one(A.d, i, k);
+                            for (int q = 0; q < 12; ++q) gather_one(A.d, i, q);
                         }
                     }
                     double x1c = 0.0;
-                    if (plain) x1c = correct_predict_plain(A.d, i, c, newton_plain(A.d, i, c));
-                    else if (on && c == 0) v2 = fmax(v2, correct_predict_one(*A.gd, i));
+                    if (plain) {
+                        const long long o = (long long)(c % 3) * E + i;
+                        const double fa = (c < 3 ? A.d.FP : A.d.MP)[o], fb = (c < 3 ? A.d.FW : A.d.MW)[o];
+                        x1c = correct_predict_plain(A.d, i, c, newton_plain(A.d, i, c, pb, fa, fb), pb);
+                    } else if (on && c == 0) {
+                        v2 = fmax(v2, correct_predict_one(*A.gd, i, pb));
+                    }
                     // |x1|^2 in the reference's order (x*x + y*y) + z*z, gathered at lane c = 0
                     const double y1 = __shfl_down_sync(0xffffffffu, x1c, 1);
                     const double z1 = __shfl_down_sync(0xffffffffu, x1c, 2);
                     if (plain && c == 0) v2 = fmax(v2, x1c * x1c + y1 * y1 + z1 * z1);
                 }
+            } else {
+                // single spheres: one group of eight lanes per element does its contacts,
+                // Newton, corrector and next predictor with no barrier in between; the
+                // predicted position, velocity and spin that contact partners read come
+                // from one copy and the prediction goes to the other (alternating by
+                // substep), so a group that runs ahead cannot change a partner's inputs
+                const PredBuf pb = pred_alternate(A.d, s & 1);
+                const int grp = lane >> 3, c = lane & 7;  // eight lanes per element, four per warp
+                for (int base = 4 * gw; base < E; base += 4 * nw) {
+                    const int i = base + grp;
+                    const bool on = i < E;
+                    double v[12];
+                    forces_group(A.d, *A.gd, i, on, c, pb, ncont, v);
+                    const bool plain = on && A.d.plain[i];
+                    double x1c = 0.0;
+                    if (plain && c < 6) {
+                        // this lane's component of FParticle + FWall (c < 3) or of MParticle
+                        // + MWall (c >= 3), selected with constant indices
+                        double fa = 0.0, fb = 0.0;
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            if (c == q) { fa = v[q]; fb = v[6 + q]; }
+                            if (c == 3 + q) { fa = v[3 + q]; fb = v[9 + q]; }
+                        }
+                        x1c = correct_predict_plain(A.d, i, c, newton_plain(A.d, i, c, pb, fa, fb), pb);
+                    } else if (on && !plain && c == 0) {
+                        v2 = fmax(v2, correct_predict_one(*A.gd, i, pb));
+                    }
+                    const double y1 = __shfl_down_sync(0xffffffffu, x1c, 1);
+                    const double z1 = __shfl_down_sync(0xffffffffu, x1c, 2);
+                    if (plain && c == 0) v2 = fmax(v2, x1c * x1c + y1 * y1 + z1 * z1);
+                }
+                count_contacts(A, s, ncont);
             }
             // DEM.cpp:1314-1324, 334-347: the largest |x1|^2 of the substep, per warp by
             // shuffles, then one 64-bit atomicMax per warp into this substep's slot
@@ -1730,6 +1827,18 @@ __global__ void __launch_bounds__(256, 2) k_cycle(CycleArgs A) {
                 maxDisp = md;
                 rebuild = rb;
             }
+        }
+        if (!PBC && (A.multi & 1)) {
+            // an odd number of substeps leaves the next prediction in the second copy:
+            // back into the element arrays, where the next cycle and the downloads read it
+            for (int i = gt; i < E; i += gs)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const long long o = (long long)q * E + i;
+                    A.d.xp0[o] = A.d.xq0[o];
+                    A.d.xp1[o] = A.d.xq1[o];
+                    A.d.wpG[o] = A.d.wqG[o];
+                }
         }
         if (A.do_boxes) {  // positions are final: boxes for the coupling passes
             if (PBC) part_boxes(A.gc, A.gd);
@@ -1821,11 +1930,12 @@ static DemArgs dem_args(hb_ctx* c) {
     a.wG = d.wG; a.wL = d.wL; a.wpG = d.wpG; a.wpL = d.wpL;
     a.FH = d.FH; a.MH = d.MH; a.FP = d.FP; a.FW = d.FW; a.MP = d.MP; a.MW = d.MW;
     a.fvol = d.fvol; a.m = d.m; a.I = d.I; a.rad = d.rad;
+    a.xq0 = d.alt; a.xq1 = d.alt ? d.alt + 3 * (size_t)d.E : nullptr; a.wqG = d.alt ? d.alt + 6 * (size_t)d.E : nullptr;
     a.pf = d.pf;
     a.plain = d.plain;
     a.cell_of = d.cell_of; a.cell_cnt = d.cell_cnt; a.cell_start = d.cell_start;
     a.cell_fill = d.cell_fill; a.cell_items = d.cell_items;
-    a.nbr = d.nbr; a.nbr_cnt = d.nbr_cnt; a.wall_of = d.wall_of; a.obj = d.obj; a.obj_cnt = d.obj_cnt;
+    a.nbr = d.nbr; a.nbr_cnt = d.nbr_cnt; a.nbr_cap = d.nbr_cap; a.wall_of = d.wall_of; a.obj = d.obj; a.obj_cnt = d.obj_cnt;
     a.wrec = d.wrec; a.orec = d.orec;
     a.cyl_of = d.cyl_of;
     a.ncyl = (int)std::min<size_t>(c->cyl.size(), DEM_MAX_CYL);
@@ -1926,6 +2036,10 @@ static CoupleArgs couple_args(hb_ctx* c) {
     a.hacc = c->P.precision == HB_FP64 ? nullptr : c->hacc;
     a.claim_list = c->d.claim_list;
     a.claim_cnt = c->d.claim_cnt;
+    a.mbb = c->P.coupling == HB_MOVING_BB ? 1 : 0;
+    a.pop_list = c->d.pop_list;
+    a.pop_cnt = c->d.pop_cnt;
+    a.rho = c->rho;
     a.tab = reinterpret_cast<PartBox*>(c->d.boxes);
     a.mass = c->mass;
     a.free_surface = c->P.free_surface;
@@ -1965,17 +2079,26 @@ int dem_args_upload(hb_ctx* c) {
     return 0;
 }
 
+// cooperative grid of the instantiation a context runs: every SM times the blocks of 256
+// threads that fit on one (resident together, as the grid barrier requires)
+static int coop_bps(bool per_particle) {
+    static int cached[2] = {0, 0};
+    int& b = cached[per_particle ? 1 : 0];
+    if (b) return b;
+    int occ = 0;
+    if (per_particle) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cycle<true>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cycle<false>, 256, 0);
+    b = occ < 1 ? 1 : (occ > 4 ? 4 : occ);
+    return b;
+}
+
 int coop_grid(hb_ctx* c) {
-    static int cached = 0;
-    if (cached) return cached;
-    int dev = 0, sms = 0, occ = 0;
+    int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cycle<false>, 256, 0);
-    occ = occ < 1 ? 1 : (occ > 4 ? 4 : occ);
-    cached = sms * occ;
-    if (cached > PARTIAL_CAP) cached = PARTIAL_CAP;  // one trigger partial per block
-    return cached;
+    int g = sms * coop_bps(c->d.gen != 0);
+    if (g > PARTIAL_CAP) g = PARTIAL_CAP;  // one trigger partial per block
+    return g;
 }
 
 int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsigned long long* ts) {
@@ -1986,10 +2109,11 @@ int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsign
     A.c = couple_args(c);
     A.gd = reinterpret_cast<const DemArgs*>(c->d.gargs);
     A.gc = reinterpret_cast<const CoupleArgs*>(reinterpret_cast<const char*>(c->d.gargs) + GARGS_COUPLE);
-    A.do_reduce = do_reduce;
+    A.do_reduce = do_reduce && c->P.coupling != HB_MOVING_BB;  // moving bounce-back: k_mbb_force wrote them
     A.do_dem = do_dem;
     A.do_boxes = do_boxes;
     A.multi = c->d.multi;
+    A.bps = coop_bps(c->d.gen != 0);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)coop_grid(c));
     cfg.blockDim = dim3(256);
@@ -2000,22 +2124,14 @@ int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsign
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (c->d.gen) {
-        int occ = 0;  // the per-particle instantiation must fit the same grid
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cycle<true>, 256, 0);
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if ((int)cfg.gridDim.x > occ * sms) return -1;
-        return cudaLaunchKernelEx(&cfg, k_cycle<true>, A) == cudaSuccess ? 0 : -1;
-    }
+    if (c->d.gen) return cudaLaunchKernelEx(&cfg, k_cycle<true>, A) == cudaSuccess ? 0 : -1;
     return cudaLaunchKernelEx(&cfg, k_cycle<false>, A) == cudaSuccess ? 0 : -1;
 }
 
 // findNewActive + findNewSolid (LB.cpp:247-280); boxes come from the cooperative kernel
 // when it ran the DEM substeps of this cycle (build == false), else are built here.
 // ev (optional, 4 events) brackets the three passes for the phase profiler.
-void launch_couple(hb_ctx* c, bool build, cudaEvent_t* ev) {
+void launch_couple(hb_ctx* c, bool build, int cur, cudaEvent_t* ev) {
     if (c->d.E == 0) return;
     CoupleArgs a = couple_args(c);
     if (build && c->d.gen) k_part_state<<<ceil_div(c->d.P + c->d.gcap, 256), 256, 0, c->stream>>>(dem_args(c));
@@ -2026,11 +2142,13 @@ void launch_couple(hb_ctx* c, bool build, cudaEvent_t* ev) {
     }
     if (ev) cudaEventRecord(ev[0], c->stream);
     cudaMemsetAsync(a.claim_cnt, 0, sizeof(int), c->stream);
+    if (a.mbb) cudaMemsetAsync(a.pop_cnt, 0, sizeof(int), c->stream);
     if (ev) cudaEventRecord(ev[1], c->stream);
     k_mask<<<dim3((unsigned)ceil_div(ceil_div(c->X, 4), 32), (unsigned)ceil_div(c->Y, 4), (unsigned)c->Z), dim3(32, 4),
              0, c->stream>>>(a);
     if (ev) cudaEventRecord(ev[2], c->stream);
     k_commit<<<152, 256, 0, c->stream>>>(a);
+    if (a.mbb) launch_mbb_nodes(c, cur);
     if (ev) cudaEventRecord(ev[3], c->stream);
 }
 

@@ -25,6 +25,7 @@
 // neighbour in direction j (f[j] there), or which a moving wall turned into
 // f[opp j] = fs[j] - BBi.  At the very first step fs is the initial equilibrium of the
 // cell itself (node::initialize sets f = fs), and the first pass uses that.
+#include <algorithm>
 #include <cstdio>
 
 #include "hb_common.cuh"
@@ -60,8 +61,10 @@ struct FsArgs {
     int* nconv;             // [3] cells filled / emptied by this step's classify; cells whose
                             // activity changed (gas <-> interface) in this step
     int blocks;
-    uint32_t* ilist;        // [N] interface cells at the start of the step (unordered)
-    int* icount;            // its length
+    uint32_t* ilist;        // [icap] interface cells at the start of the step (unordered)
+    int* icount;            // its length (may exceed icap: the overflow is flagged)
+    long long icap;         // capacity of ilist (hb_params.cap_interface, default N)
+    int* status;            // device status words (word 2, bit 8: interface list full)
 };
 
 // Every pass runs on a 3D grid (x from the thread, y and a group of ZC z planes from the
@@ -157,9 +160,13 @@ __global__ void __launch_bounds__(FS_BLOCK) k_fs_ilist(FsArgs a) {
         const unsigned b = __ballot_sync(full, is_if);
         if (!b) continue;
         int base = 0;
-        if (lane == 0) base = atomicAdd(a.icount, __popc(b));
+        if (lane == 0) {
+            base = atomicAdd(a.icount, __popc(b));
+            if (base + __popc(b) > a.icap) atomicOr(a.status + 2, 8);  // the list is full
+        }
         base = __shfl_sync(full, base, 0);
-        if (is_if) a.ilist[base + __popc(b & ((1u << lane) - 1u))] = (uint32_t)nd.i;
+        const long long k = (long long)base + __popc(b & ((1u << lane) - 1u));
+        if (is_if && k < a.icap) a.ilist[k] = (uint32_t)nd.i;
     }
 }
 
@@ -170,7 +177,7 @@ __global__ void __launch_bounds__(256) k_fs_mass_list(FsArgs a) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
-    const int n = *a.icount;
+    const int n = (int)min((long long)*a.icount, a.icap);
     const bool first = *a.first != 0;
     for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += warps) {
         const uint32_t iu = a.ilist[w];  // node indices fit 32 bits (the list is uint32)
@@ -479,6 +486,8 @@ static FsArgs fs_args(hb_ctx* c, int cur) {
     a.blocks = ceil_div(c->X, FS_BLOCK) * c->Y * ceil_div(c->Z, FS_ZC);
     a.ilist = c->fs_ilist;
     a.icount = c->fs_first + 4;
+    a.icap = c->fs_icap;
+    a.status = c->status;
     return a;
 }
 
@@ -496,7 +505,8 @@ int fs_init(hb_ctx* c) {
         cudaMalloc(&c->fs_cnt, sizeof(int) * blocks) != cudaSuccess ||
         cudaMalloc(&c->fs_scal, sizeof(double) * 2) != cudaSuccess ||
         cudaMalloc(&c->fs_first, 6 * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&c->fs_ilist, sizeof(uint32_t) * N) != cudaSuccess)
+        cudaMalloc(&c->fs_ilist, sizeof(uint32_t) * (c->fs_icap = c->P.cap_interface > 0 ? std::min<long long>(c->P.cap_interface, N) : N)) !=
+            cudaSuccess)
         return HB_ERR_NOMEM;
     cudaMemset(c->fs_flag, 0, N);
     cudaMemset(c->fs_scal, 0, sizeof(double) * 2);

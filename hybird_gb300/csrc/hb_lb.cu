@@ -18,6 +18,7 @@
 //
 // Roofline: per lattice update the kernel reads 19 and writes 19 stored populations
 // plus the one-byte node type: 2*19*s + 1 bytes (s = 8, 4, 2 for FP64, FP32, FP16S).
+#include <algorithm>
 #include <cstdio>
 
 #include "hb_common.cuh"
@@ -39,6 +40,19 @@ __device__ __forceinline__ long long link_index(const LBArgs& a, int x, int y, i
     return (long long)xn + (long long)a.X * ((long long)yn + (long long)a.Y * zn);
 }
 
+// Moving bounce-back: velocity of particle p's solid at node (x, y, z), the element's
+// velocity plus its spin times the lever arm from the element centre (the reference's
+// commented particle branch, LB.cpp:1247-1276: radius = node - x0 + radiusVec)
+__device__ __forceinline__ void mbb_velocity(const Particles& q, int p, int x, int y, int z, double& vx, double& vy,
+                                             double& vz) {
+    const int E = q.count;
+    const double rx = (double)x - q.x0[p], ry = (double)y - q.x0[E + p], rz = (double)z - q.x0[2 * E + p];
+    const double wx = q.w[p], wy = q.w[E + p], wz = q.w[2 * E + p];
+    vx = q.x1[p] + (wy * rz - wz * ry);
+    vy = q.x1[E + p] + (wz * rx - wx * rz);
+    vz = q.x1[2 * E + p] + (wx * ry - wy * rx);
+}
+
 template <class P>
 __global__ void __launch_bounds__(256) k_collide_stream(LBArgs a) {
     using T = typename P::T;
@@ -50,7 +64,7 @@ __global__ void __launch_bounds__(256) k_collide_stream(LBArgs a) {
     const long long N = a.N;
     const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
     const uint8_t t = a.ntype[i];
-    if (!is_active(t)) return;
+    if (!is_fluid(t, a.mbb)) return;
     const int mode = *a.mode;
     const S* fin = reinterpret_cast<const S*>(a.fin);
     S* fout = reinterpret_cast<S*>(a.fout);
@@ -217,9 +231,18 @@ __global__ void __launch_bounds__(256) k_collide_stream(LBArgs a) {
 #pragma unroll
     for (int j = 1; j < Q; ++j) {
         const long long l = link_index(a, x, y, z, j);
-        const uint8_t lc = a.ntype[l] & HB_TYPE_MASK;
+        const uint8_t tl = a.ntype[l];
+        const uint8_t lc = tl & HB_TYPE_MASK;
         const int o = opp(j);
-        if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
+        if (a.mbb && (tl & HB_INSIDE) && (lc == HB_T_FLUID || lc == HB_T_INTERFACE)) {
+            // moving bounce-back on a particle (no wrapped links: particles with
+            // periodic faces are not taken in this mode), as the moving wall's rule
+            double ubx, uby, ubz;
+            mbb_velocity(a.parts, (int)a.solid[l], x + cx(j), y + cy(j), z + cz(j), ubx, uby, ubz);
+            const double uw = ubx * cx(j) + uby * cy(j) + ubz * cz(j);
+            const T BBi = T(6.0 * (double)n * wgt(j) * uw);
+            P::store(fout + (long long)o * N + i, fs[j] - BBi);
+        } else if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
             P::store(fout + (long long)j * N + l, fs[j]);
         } else if (lc == HB_T_GAS) {
             T vu = T(0);
@@ -259,7 +282,7 @@ __global__ void __launch_bounds__(256) k_wallforce(LBArgs a) {
     if (x >= 1 && x <= a.X - 2) {
         const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
         const uint8_t t = a.ntype[i];
-        if (is_active(t) && !(t & HB_BULK)) {
+        if (is_fluid(t, a.mbb) && !(t & HB_BULK)) {
             const S* fcur = reinterpret_cast<const S*>(a.fout);
             for (int j = 1; j < Q; ++j) {
                 const long long l = link_index(a, x, y, z, j);
@@ -313,6 +336,7 @@ struct InitArgs {
     double wp[MAX_WALLS][3], wn[MAX_WALLS][3];
     int wcode[MAX_WALLS];
     double gas_x, gas_z;
+    int mbb;  // moving bounce-back: nodes inside particles are solid
 };
 
 // lattice boundary codes (LB.cpp:393-432), DEM walls (LB.cpp:497-533)
@@ -498,7 +522,7 @@ __device__ __forceinline__ void bulk_node(const InitArgs& a, const PerFaces& pf,
                                           unsigned long long* lmask, int x, int y, int z) {
     const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
     uint8_t t = ntype[i];
-    bool bulk = is_active(t);
+    bool bulk = is_fluid(t, a.mbb);
     bool wrap = false;  // some link crosses a periodic face (checked over all 18 links)
     uint32_t mask = 0;  // links that need the general push
     uint32_t bb = 0;    // links that end on a static wall: plain bounce-back into the node itself
@@ -515,7 +539,7 @@ __device__ __forceinline__ void bulk_node(const InitArgs& a, const PerFaces& pf,
                 const bool wj = xn != x + cx(j) || yn != y + cy(j) || zn != z + cz(j);
                 const long long l = (long long)xn + (long long)a.X * ((long long)yn + (long long)a.Y * zn);
                 const uint8_t tl = ntype[l];
-                const bool act = is_active(tl);
+                const bool act = is_fluid(tl, a.mbb);  // a solid particle node takes the general push
                 const uint8_t tc = tl & HB_TYPE_MASK;
                 if (tc == HB_T_STATWALL || tc == HB_T_SLIPSTAT || tc == HB_T_SLIPDYN || tc == HB_T_CURVED) bb |= 1u << j;
                 else if (!act || wj) mask |= 1u << j;
@@ -592,6 +616,7 @@ static InitArgs init_args(hb_ctx* c) {
     }
     a.gas_x = c->P.gas_box[0];
     a.gas_z = c->P.gas_box[1];
+    a.mbb = c->P.coupling == HB_MOVING_BB && c->d.E > 0;
     return a;
 }
 
@@ -638,7 +663,8 @@ LBArgs lb_args(hb_ctx* c, int cur) {
     a.yield_stress = c->P.yield_stress;
     a.turb_const = c->P.turb_const;
     a.free_surface = c->P.free_surface;
-    a.couple = (c->P.dem_solve && c->d.E > 0) ? 1 : 0;
+    a.mbb = (c->P.dem_solve && c->d.E > 0 && c->P.coupling == HB_MOVING_BB) ? 1 : 0;
+    a.couple = (c->P.dem_solve && c->d.E > 0 && !a.mbb) ? 1 : 0;
     a.parts.count = c->d.E;
     a.parts.x0 = c->d.E ? c->d.x[0] : nullptr;
     a.parts.x1 = c->d.E ? c->d.x[1] : nullptr;
@@ -721,6 +747,7 @@ void launch_lb_step(hb_ctx* c, int cur) {
     }
     launch_slip(c, a.fout);    // slip-wall mixing of the bounced-back diagonals (hb_slip.cu)
     launch_curved(c, a.fout);  // curved-wall interpolation of the bounced-back links (hb_curved.cu)
+    if (a.mbb) launch_mbb_force(c, cur);
 }
 
 void launch_lb_wallforce(hb_ctx* c, int cur) {
@@ -798,6 +825,192 @@ int launch_download_lattice(hb_ctx* c, double* f_dev, int which) {
     else if (c->P.precision == HB_FP32) k_download_f<PolF32><<<G, B, 0, c->stream>>>(src, N, f_dev);
     else k_download_f<PolF16><<<G, B, 0, c->stream>>>(src, N, f_dev);
     return 0;
+}
+
+// ---- moving bounce-back coupling (hb_params.coupling = HB_MOVING_BB) ------------------
+// Not in the reference (its particle branch is commented out, LB.cpp:1247-1276).  The
+// coupling masks (LB.cpp:1921-2033 rules) decide which nodes are inside a particle; here
+// those nodes are solid.  After the masks: every node a particle uncovered is refilled
+// with the equilibrium of the particle's local velocity at the mean density of its fluid
+// links, and the bulk bit / link masks of the changed nodes and their neighbours are
+// recomputed.  After the lattice step: each particle's force and torque from the
+// bounce-back links into it.  Particles with periodic faces are not taken in this mode,
+// so no link wraps.
+
+struct MbbArgs {
+    int X, Y, Z;
+    long long N;
+    uint8_t* ntype;
+    uint32_t* solid;
+    void* f;                 // population buffer (refill: the current state; force: after streaming)
+    double* rho;
+    Particles parts;
+    const uint32_t* pop;     // nodes uncovered in this step
+    const int* npop;
+    double* pop_rho;
+    const uint32_t* claims;  // (node, particle) pairs covered in this step
+    const int* nclaim;
+    double *FH, *MH, *fvol;  // element sums (single spheres: element = particle)
+};
+
+// One thread per uncovered node: rho = mean density of its fluid links that were fluid
+// before this step (popped nodes carry NaN density until their refill is committed), in
+// link order, 1 without any; f = f_eq(rho, u) with u the particle's velocity at the node.
+template <class P>
+__device__ __forceinline__ void mbb_refill_one(const MbbArgs& a, int k) {
+    using S = typename P::S;
+    using T = typename P::T;
+    const long long l = a.pop[k];
+    if (a.ntype[l] & HB_INSIDE) return;  // covered again in the same step
+    const int x = (int)(l % a.X), y = (int)((l / a.X) % a.Y), z = (int)(l / ((long long)a.X * a.Y));
+    double sum = 0.0;
+    int cnt = 0;
+    for (int j = 1; j < Q; ++j) {
+        const long long m = (long long)(x + cx(j)) + (long long)a.X * ((long long)(y + cy(j)) + (long long)a.Y * (z + cz(j)));
+        const double r = a.rho[m];
+        if (!is_fluid(a.ntype[m], 1) || r != r) continue;
+        sum += r;
+        ++cnt;
+    }
+    const double rho = cnt ? sum / (double)cnt : 1.0;
+    double ux, uy, uz;
+    mbb_velocity(a.parts, (int)a.solid[l], x, y, z, ux, uy, uz);
+    const double usq = ux * ux + uy * uy + uz * uz;
+    S* f = reinterpret_cast<S*>(a.f);
+    for (int j = 0; j < Q; ++j) {
+        const double vu = ux * cx(j) + uy * cy(j) + uz * cz(j);
+        double v = wgt(j) * rho * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
+        if (P::DEV) v -= wgt(j);
+        P::store(f + (long long)j * a.N + l, (T)v);
+    }
+    a.pop_rho[k] = rho;
+}
+
+template <class P>
+__global__ void k_mbb_refill_gs(MbbArgs a) {
+    const int n = *a.npop;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) mbb_refill_one<P>(a, k);
+}
+
+// One thread per (changed node, node or one of its 18 links): the bulk bit and link mask of
+// that node from its neighbours' final state; uncovered nodes take their refill density.
+// Nodes reached from several changed nodes compute the same values.
+__global__ void k_mbb_relink_gs(MbbArgs m, InitArgs a, PerFaces pf, unsigned long long* lmask) {
+    const long long np = *m.npop, nc = *m.nclaim;
+    const long long total = (np + nc) * Q;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long e = t / Q;
+        const int j = (int)(t - e * Q);
+        const long long l = e < np ? (long long)m.pop[e] : (long long)m.claims[2 * (e - np)];
+        const int x = (int)(l % a.X), y = (int)((l / a.X) % a.Y), z = (int)(l / ((long long)a.X * a.Y));
+        const int xn = x + cx(j), yn = y + cy(j), zn = z + cz(j);
+        if (xn < 0 || yn < 0 || zn < 0 || xn >= a.X || yn >= a.Y || zn >= a.Z) continue;
+        bulk_node(a, pf, m.ntype, lmask, xn, yn, zn);
+        if (j == 0 && e < np && !(m.ntype[l] & HB_INSIDE)) m.rho[l] = m.pop_rho[e];
+    }
+}
+
+// Element force and torque (node::bounceBackForce, node.cpp:283-291): one block per
+// particle over its box; each fluid node's links into the particle contribute
+// (2 (fs_j - w_j) - BBi) c_j with fs_j = f_out[opp j] + BBi recovered from the streamed
+// state and its moment about the element centre; the solid nodes count the volume.
+// Fixed node-to-thread assignment and a fixed tree: the sums are reproducible.
+template <class P>
+__global__ void __launch_bounds__(256) k_mbb_force(MbbArgs a) {
+    using S = typename P::S;
+    __shared__ double sh[7][256];
+    const int p = blockIdx.x, E = a.parts.count;
+    const double cxp = a.parts.x0[p], cyp = a.parts.x0[E + p], czp = a.parts.x0[2 * E + p], r = a.parts.radius[p];
+    const int x0 = max(1, (int)floor(cxp - r) - 2), x1 = min(a.X - 2, (int)ceil(cxp + r) + 2);
+    const int y0 = max(1, (int)floor(cyp - r) - 2), y1 = min(a.Y - 2, (int)ceil(cyp + r) + 2);
+    const int z0 = max(1, (int)floor(czp - r) - 2), z1 = min(a.Z - 2, (int)ceil(czp + r) + 2);
+    const int nx = x1 - x0 + 1, ny = y1 - y0 + 1, nz = z1 - z0 + 1;
+    const long long nb = (nx > 0 && ny > 0 && nz > 0) ? (long long)nx * ny * nz : 0;
+    const S* f = reinterpret_cast<const S*>(a.f);
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (long long k = threadIdx.x; k < nb; k += blockDim.x) {
+        const int x = x0 + (int)(k % nx), y = y0 + (int)((k / nx) % ny), z = z0 + (int)(k / ((long long)nx * ny));
+        const long long i = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
+        const uint8_t t = a.ntype[i];
+        if (!is_active(t)) continue;
+        if (t & HB_INSIDE) {
+            if ((int)a.solid[i] == p) acc[6] += 1.0;
+            continue;
+        }
+        for (int j = 1; j < Q; ++j) {
+            const int xl = x + cx(j), yl = y + cy(j), zl = z + cz(j);
+            const long long l = (long long)xl + (long long)a.X * ((long long)yl + (long long)a.Y * zl);
+            const uint8_t tl = a.ntype[l];
+            if (!(is_active(tl) && (tl & HB_INSIDE)) || (int)a.solid[l] != p) continue;
+            double ux, uy, uz;
+            mbb_velocity(a.parts, p, xl, yl, zl, ux, uy, uz);
+            const double BBi = 6.0 * a.rho[i] * wgt(j) * (ux * cx(j) + uy * cy(j) + uz * cz(j));
+            double fo = (double)P::load(f + (long long)opp(j) * a.N + i);
+            if (P::DEV) fo += wgt(j);
+            const double sc = 2.0 * ((fo + BBi) - 1.0 * wgt(j)) - BBi;
+            const double Fx = sc * cx(j), Fy = sc * cy(j), Fz = sc * cz(j);
+            const double rx = (double)xl - cxp, ry = (double)yl - cyp, rz = (double)zl - czp;
+            acc[0] += Fx; acc[1] += Fy; acc[2] += Fz;
+            acc[3] += ry * Fz - rz * Fy;
+            acc[4] += rz * Fx - rx * Fz;
+            acc[5] += rx * Fy - ry * Fx;
+        }
+    }
+    for (int q = 0; q < 7; ++q) sh[q][threadIdx.x] = acc[q];
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st)
+            for (int q = 0; q < 7; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 3; ++q) {
+            a.FH[(long long)q * E + p] = sh[q][0];
+            a.MH[(long long)q * E + p] = sh[3 + q][0];
+        }
+        a.fvol[p] = sh[6][0];
+    }
+}
+
+static MbbArgs mbb_args(hb_ctx* c, void* f) {
+    MbbArgs m;
+    m.X = c->X; m.Y = c->Y; m.Z = c->Z; m.N = c->N;
+    m.ntype = c->ntype;
+    m.solid = c->solid;
+    m.f = f;
+    m.rho = c->rho;
+    const LBArgs la = lb_args(c, 0);
+    m.parts = la.parts;
+    m.pop = c->d.pop_list;
+    m.npop = c->d.pop_cnt;
+    m.pop_rho = c->d.pop_rho;
+    m.claims = c->d.claim_list;
+    m.nclaim = c->d.claim_cnt;
+    m.FH = c->d.FH; m.MH = c->d.MH; m.fvol = c->d.fvol;
+    return m;
+}
+
+// after the coupling masks of the step whose lattice update reads buffer `cur`; the
+// lists live on the device, so the grids cover their capacity and exit early
+void launch_mbb_nodes(hb_ctx* c, int cur) {
+    MbbArgs m = mbb_args(c, cur ? c->fB : c->fA);
+    const int B = 256;
+    const long long cap = c->N;  // each list holds at most every node once
+    const unsigned gp = (unsigned)std::min<long long>(ceil_div(cap, B), 152LL * 64);
+    // the grid is capped: list entries beyond it are handled by later blocks of a
+    // grid-stride form, so the launch shape does not depend on the device-side count
+    if (c->P.precision == HB_FP64) k_mbb_refill_gs<PolF64><<<gp, B, 0, c->stream>>>(m);
+    else if (c->P.precision == HB_FP32) k_mbb_refill_gs<PolF32><<<gp, B, 0, c->stream>>>(m);
+    else k_mbb_refill_gs<PolF16><<<gp, B, 0, c->stream>>>(m);
+    k_mbb_relink_gs<<<gp, B, 0, c->stream>>>(m, init_args(c), per_faces(c), c->lmask);
+}
+
+void launch_mbb_force(hb_ctx* c, int cur) {
+    MbbArgs m = mbb_args(c, cur ? c->fA : c->fB);  // the buffer the step just wrote
+    if (c->P.precision == HB_FP64) k_mbb_force<PolF64><<<c->d.E, 256, 0, c->stream>>>(m);
+    else if (c->P.precision == HB_FP32) k_mbb_force<PolF32><<<c->d.E, 256, 0, c->stream>>>(m);
+    else k_mbb_force<PolF16><<<c->d.E, 256, 0, c->stream>>>(m);
 }
 
 }  // namespace hb

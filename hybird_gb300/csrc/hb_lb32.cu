@@ -55,10 +55,21 @@ template <class P>
 __device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fout, int x, int y, int z, int i,
                                              int j, float g, float n, float ux, float uy, float uz, float usq) {
     const int l = link32(a, x, y, z, j);
-    const uint8_t lc = a.ntype[l] & HB_TYPE_MASK;
+    const uint8_t tl = a.ntype[l];
+    const uint8_t lc = tl & HB_TYPE_MASK;
     const int o = opp(j);
     const int N = (int)a.N;
-    if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
+    if (a.mbb && (tl & HB_INSIDE) && (lc == HB_T_FLUID || lc == HB_T_INTERFACE)) {
+        // moving bounce-back on a particle: BBi = 6 n w_j (u . c_j) with u the particle's
+        // velocity at the solid node, from its FP32 record (centre, velocity, spin); no
+        // link wraps in this mode
+        const float4* pf4 = reinterpret_cast<const float4*>(a.parts.pf) + 3 * (size_t)a.solid[l];
+        const float4 q0 = pf4[0], q1 = pf4[1], q2 = pf4[2];
+        const float rx = float(x + cx(j)) - q0.x, ry = float(y + cy(j)) - q0.y, rz = float(z + cz(j)) - q0.z;
+        const float wx = q1.z, wy = q1.w, wz = q2.x;
+        const float vx = q0.w + (wy * rz - wz * ry), vy = q1.x + (wz * rx - wx * rz), vz = q1.y + (wx * ry - wy * rx);
+        P::store(fout + o * N + i, g - 6.0f * n * float(wgt(j)) * cdot(j, vx, vy, vz));
+    } else if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
         P::store(fout + j * N + l, g);
     } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN || lc == HB_T_CURVED) {
         // slip and curved walls: completed after the kernel (hb_slip.cu, hb_curved.cu)
@@ -286,7 +297,7 @@ __global__ void __launch_bounds__(128, 9) k_collide_stream_dev(LBArgs a) {
     const S* fin = reinterpret_cast<const S*>(a.fin);
     // whole warps leave together so that the element sums can use full-warp shuffles
     const uint8_t t = x < a.X ? a.ntype[i] : (uint8_t)HB_T_STATWALL;
-    const bool act = is_active(t);
+    const bool act = is_fluid(t, a.mbb);
     if (!__any_sync(0xffffffffu, act)) return;
     // the particle index of a particle node is loaded ahead of the populations and its
     // particle's FP32 record right after them, so their latencies overlap the populations'

@@ -1,17 +1,20 @@
 // hb_noalloc.cu -- moving-wall force reduction for callers that cannot allocate device
 // memory.
 //
-// Some callers cannot call cudaMalloc: host drivers that run every step of the solver
-// inside a CUDA stream capture (allocation is not allowed while a stream is being
-// captured), and integrations that must live within a fixed device-memory budget
-// handed to them by the embedding application.  hb_wall_force_noalloc gives them the
-// moving-wall momentum exchange (the reduction hb_download_walls reports) without any
-// allocation: the per-CTA partial sums live in the file-scope device array below, of a
-// fixed size, held by every GPU that loads this library until the process exits.
+// Some callers cannot call cudaMalloc: an application that reserves the device memory
+// up front and hands each library a fixed budget (its own pool allocator owns the
+// rest, so a cudaMalloc here would fail or break its accounting), and a host loop with
+// a latency bound that cannot take the device-wide synchronisation a cudaMalloc or
+// cudaFree may cause.  hb_wall_force_noalloc gives them the moving-wall momentum
+// exchange (the reduction hb_download_walls reports) without any allocation: the
+// per-CTA partial sums live in the file-scope device array below, of a fixed size,
+// held by every GPU that loads this library until the process exits.
 //
 // Rules for callers:
 //   * The first call on a device looks up the array's device address for that device
-//     (cudaGetSymbolAddress); make that first call outside any stream capture.
+//     (cudaGetSymbolAddress) and keeps it; make that first call before any stream
+//     capture.  A cudaDeviceReset unloads the array, so the kept address is stale
+//     afterwards: do not call this entry point again in a process that reset the device.
 //   * All calls share the array.  Every call rewrites all the partials it reads, so no
 //     state carries over, but calls that overlap on the GPU (different streams, or
 //     different host threads on one device) race on it and must be serialised by the
@@ -47,7 +50,12 @@ struct NoAllocArgs {
     double* out;
 };
 
-__device__ __forceinline__ bool act(uint8_t c) { return c == HB_T_FLUID || c == HB_T_INTERFACE; }
+// node bytes are compared on their type code: the library's internal flag bits
+// (particle, bulk, wrap, mirror) may be set in a byte handed in from its own buffers
+__device__ __forceinline__ bool act(uint8_t t) {
+    const uint8_t c = t & HB_TYPE_MASK;
+    return c == HB_T_FLUID || c == HB_T_INTERFACE;
+}
 
 // Same per-node arithmetic as the library's moving-wall reduction (LB.cpp:1321-1341),
 // over a fixed grid that strides across the interior rows.
@@ -72,17 +80,21 @@ __global__ void __launch_bounds__(256) k_wall_noalloc(NoAllocArgs a) {
             if (yn == 0 && a.per[2]) yn = a.Y - 2; else if (yn == a.Y - 1 && a.per[3]) yn = 1;
             if (zn == 0 && a.per[4]) zn = a.Z - 2; else if (zn == a.Z - 1 && a.per[5]) zn = 1;
             const long long l = (long long)xn + (long long)a.X * ((long long)yn + (long long)a.Y * zn);
-            if (a.type[l] != HB_T_DYNWALL) continue;
+            if ((a.type[l] & HB_TYPE_MASK) != HB_T_DYNWALL) continue;
             const double uw = a.u[l] * hb::cx(j) + a.u[a.N + l] * hb::cy(j) + a.u[2 * a.N + l] * hb::cz(j);
             const double BBi = 6.0 * a.rho[i] * hb::wgt(j) * uw;
             const double fsj = a.f[(long long)hb::opp(j) * a.N + i] + BBi;
             const double sc = (2.0 * (fsj - 1.0 * hb::wgt(j)) - BBi) * 1.0;
             const int w = (int)a.solid[l];
-            if (w >= 0 && w < hb::MAX_WALLS) {
-                acc[3 * w] += sc * hb::cx(j);
-                acc[3 * w + 1] += sc * hb::cy(j);
-                acc[3 * w + 2] += sc * hb::cz(j);
-            }
+            // compile-time indices keep acc in registers (a runtime index would place it
+            // in local memory)
+#pragma unroll
+            for (int ww = 0; ww < hb::MAX_WALLS; ++ww)
+                if (ww == w) {
+                    acc[3 * ww] += sc * hb::cx(j);
+                    acc[3 * ww + 1] += sc * hb::cy(j);
+                    acc[3 * ww + 2] += sc * hb::cz(j);
+                }
             acc[hb::MAX_WALLS * 3] += BBi * a.mass[i];
         }
     }
@@ -131,7 +143,16 @@ extern "C" int hb_wall_force_noalloc(const double* f, const uint8_t* type, const
     a.partials = g_partials_addr[dev];
     a.out = wall_force;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    k_wall_noalloc<<<kBlocks, 256, 0, s>>>(a);
-    k_wall_noalloc_final<<<1, 32, 0, s>>>(a.partials, wall_force);
-    return cudaGetLastError() == cudaSuccess ? HB_OK : HB_ERR_CUDA;
+    // launched through cudaLaunchKernel so that the status is this call's own: an error
+    // another launch left pending on this thread is neither cleared nor reported here
+    void* args1[] = {&a};
+    if (cudaLaunchKernel(reinterpret_cast<const void*>(k_wall_noalloc), dim3(kBlocks), dim3(256), args1, 0, s) !=
+        cudaSuccess)
+        return HB_ERR_CUDA;
+    double* partials = a.partials;
+    void* args2[] = {&partials, &wall_force};
+    if (cudaLaunchKernel(reinterpret_cast<const void*>(k_wall_noalloc_final), dim3(1), dim3(32), args2, 0, s) !=
+        cudaSuccess)
+        return HB_ERR_CUDA;
+    return HB_OK;
 }

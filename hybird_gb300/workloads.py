@@ -1,5 +1,7 @@
 """Synthetic workloads with the shapes of the benchmark configurations (seeded; no data
 files).  Each returns hb_params plus the particle / object arrays the C-ABI takes."""
+import functools
+
 import numpy as np
 
 from . import abi
@@ -102,3 +104,104 @@ def adjoint_channel(shape=(96, 96, 96), per_axis=4, radius=6.0, jitter=2.0, seed
     params = abi.make_params(shape, (8, 8, 7, 7, 4, 4), init_visc=(tau - 0.5) / 3.0, lbF=(force, 0.0, 0.0),
                              collision=abi.HB_TRT, precision=precision)
     return params, objects, inlet_profile(shape, u0, zwave)
+
+
+def deposit(spheres, floor=0.5, overlap=1e-4):
+    """The same spheres dropped straight down, lowest first, onto the floor plane z =
+    floor (the no-slip wall of the lower z face, DEM.cpp:435-633) or onto a sphere
+    already resting, and left there pressed in by `overlap` (near the static overlap of
+    a linear spring under a sphere's weight).  x and y stay as given, so a packing that
+    does not overlap in the plane keeps every sphere inside the box; the result is a bed
+    in which every sphere touches the floor or another sphere from the first substep
+    on.  Overlaps with spheres other than the one a sphere lands on stay below
+    `overlap`."""
+    s = np.asarray(spheres, dtype=float)
+    out = s.copy()
+    placed = []
+    for k in np.argsort(s[:, 2], kind="stable"):
+        x, y, r = s[k, 0], s[k, 1], s[k, 3]
+        z = floor + r - overlap
+        if placed:
+            q = out[placed]
+            h2 = (q[:, 0] - x) ** 2 + (q[:, 1] - y) ** 2
+            reach = (q[:, 3] + r) ** 2 - h2
+            hit = reach > 0.0
+            if hit.any():
+                z = max(z, float((q[hit, 2] + np.sqrt(reach[hit])).max()) - overlap)
+        out[k, 2] = z
+        placed.append(k)
+    return out
+
+
+def sedimentation(precision, L=128, seed=2, collision=None, deposited=False):
+    """Configuration 2: coupled sedimentation in an L^3 no-slip box, seeded random
+    sequential addition of spheres r ~ U[4, 6] until it jams (about 1500 at L = 128),
+    density ratio 2.5, gravity 1e-5 along -z, linear contacts kn = 1e3, e = 0.8,
+    mu = 0.5, viscTang 0.5, multiStep 3, TRT tau 0.8 (BGK with collision=HB_BGK).
+    deposited=True drops the same spheres onto the floor first (deposit), so that the
+    contact path runs from the first substep, and takes multiStep 10: in a bed where a
+    sphere touches several neighbours the Gear predictor-corrector (elmt.cpp:139-254) is
+    unstable at multiStep 3 and 6 (the oracle's particle speeds grow about 2.3-fold per
+    cycle at 3) and stable at 10."""
+    spheres = _rsa_cached(seed, 2000, 4.0, 6.0, 0.5, L - 1.5).copy()
+    if deposited:
+        spheres = deposit(spheres)
+    p = abi.make_params((L, L, L), (7,) * 6, init_visc=(0.8 - 0.5) / 3.0, lbF=(0.0, 0.0, -1e-5),
+                        collision=abi.HB_TRT if collision is None else collision, trt_magic=3.0 / 16.0,
+                        precision=precision, multi_step=10 if deposited else 3, density=2.5, linear_stiff=1e3,
+                        restitution=0.8,
+                        friction_part=0.5, friction_wall=0.5, visc_tang=0.5)
+    return p, spheres
+
+
+@functools.lru_cache(maxsize=8)
+def _rsa_cached(seed, target, rmin, rmax, lo, hi):
+    return _rsa_batched(seed, target, rmin, rmax, lo, hi)
+
+
+def _rsa_batched(seed, target, rmin, rmax, lo, hi, tries=400000, batch=4096):
+    """Seeded random sequential addition of non-overlapping spheres, drawn in batches of
+    `batch` candidates (radius, then x, y, z centres); a candidate is accepted when it
+    overlaps no sphere placed before it, earlier accepted candidates of its own batch
+    included.  Stops at `target` spheres or after `tries` candidates.  Placed spheres are
+    binned in cells of width 2 rmax, so each test looks at the 27 cells around the
+    candidate only (the same acceptance as testing every placed sphere)."""
+    rng = np.random.default_rng(seed)
+    cw = 2.0 * rmax
+    ncell = int(np.ceil((hi - lo) / cw)) + 1
+    cap = 8  # non-overlapping spheres of radius >= rmin / 2 per cell of width 2 rmax
+    grid = np.full((ncell, ncell, ncell, cap), -1, dtype=np.int64)
+    fill = np.zeros((ncell, ncell, ncell), dtype=np.int64)
+    placed = np.zeros((target, 4))
+    n = 0
+    done = 0
+    offs = np.array([(a, b, c) for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1)])
+    while done < tries and n < target:
+        r = rng.uniform(rmin, rmax, batch)
+        c = np.stack([rng.uniform(lo + r, hi - r) for _ in range(3)], axis=1)
+        done += batch
+        cell = np.clip(((c - lo) // cw).astype(np.int64), 0, ncell - 1)
+        nb = np.clip(cell[:, None, :] + offs[None, :, :], 0, ncell - 1)  # clipped repeats are harmless
+        idx = grid[nb[..., 0], nb[..., 1], nb[..., 2]].reshape(batch, -1)  # [batch, 27*cap]
+        valid = idx >= 0
+        q = placed[np.where(valid, idx, 0)]
+        d2 = ((c[:, None, :] - q[..., :3]) ** 2).sum(-1)
+        ok = ~((d2 < (r[:, None] + q[..., 3]) ** 2) & valid).any(axis=1)
+        acc = []
+        for k in np.nonzero(ok)[0]:
+            good = True
+            for a in acc:
+                if ((c[k] - c[a]) ** 2).sum() < (r[k] + r[a]) ** 2:
+                    good = False
+                    break
+            if good:
+                acc.append(k)
+                if n + len(acc) >= target:
+                    break
+        for k in acc:
+            placed[n] = (c[k, 0], c[k, 1], c[k, 2], r[k])
+            gx, gy, gz = cell[k]
+            grid[gx, gy, gz, fill[gx, gy, gz]] = n
+            fill[gx, gy, gz] += 1
+            n += 1
+    return placed[:n].copy()

@@ -2,9 +2,11 @@
  * hybird_gpu.h -- C-ABI of the GB300 (sm_103a) time-step library for hybird.
  *
  * One opaque context owns every device buffer of one simulation on one GPU.  The
- * reference's per-step class methods become forwarders into these calls (see
- * INTEGRATION.md); every call returns an int status (HB_OK == 0) instead of calling
- * exit() as the reference does (macros.h:8, LB.cpp:1057, LB.cpp:1460).
+ * reference's per-step class methods (LB::latticeBolzmannStep, LB.h:159; LB::
+ * latticeBoltzmannFreeSurfaceStep, LB.h:161; LB::latticeBoltzmannCouplingStep, LB.h:160;
+ * DEM::discreteElementStep, DEM.h:137) become one-line forwarders into these calls;
+ * every call returns an int status (HB_OK == 0) instead of calling exit() as the
+ * reference does (macros.h:8, LB.cpp:1057, LB.cpp:1460).
  *
  * Units: every quantity crossing this boundary is in the reference's lattice units
  * with unitLength = unitTime = unitDensity = 1 (LB.cpp:93-98); hb_create rejects other
@@ -39,6 +41,12 @@ extern "C" {
 
 #define HB_BGK    0   /* single relaxation time, node.cpp:158-165                          */
 #define HB_TRT    1   /* two relaxation times (magic parameter), not in the reference      */
+
+#define HB_DIRECT_FORCING 0 /* the reference's coupling: -eps (u - u_p) on nodes inside
+                                particles, which stay fluid (LB.cpp:1851-1919)               */
+#define HB_MOVING_BB      1 /* not in the reference (its branch is commented out, LB.cpp:
+                                1247-1276): nodes inside particles are solid and fluid links
+                                into them bounce back with the particle's local velocity     */
 
 #define HB_LINEAR   0 /* ContactModel LINEAR  (elmt.h:137)                                 */
 #define HB_HERTZIAN 1 /* ContactModel HERTZIAN (elmt.h:137)                                */
@@ -90,10 +98,21 @@ typedef struct hb_params {
     double  friction_part;     /* frictionCoefPart                                           */
     double  friction_wall;     /* frictionCoefWall                                           */
     double  num_visc;          /* numVisc                                                    */
-    /* capacities of the fixed-size device lists (0 = library default) */
-    int64_t cap_pairs;         /* DEM candidate pairs                                        */
-    int64_t cap_interface;     /* interface cells                                            */
+    /* capacities of the fixed-size device lists (0 = library default); the reference's
+       lists are unbounded (DEM.cpp:1369-1494, LB.cpp:1592-1618): an overflow here stops
+       nothing on the device but makes hb_synchronize return HB_ERR_CAPACITY naming the list */
+    int64_t cap_neighbors;     /* DEM candidate partners kept per particle (default 48)      */
+    int64_t cap_interface;     /* free-surface interface cells listed per step (default: all nodes) */
     double  slip_coefficient;  /* slipCoefficient S of the slip walls 5/6 (LB.cpp:1154-1155) */
+    /* HB_DIRECT_FORCING (default, the reference's scheme) | HB_MOVING_BB.  Moving
+       bounce-back: a fluid node i with link j onto a node l inside particle p takes
+       f_i[opp j] = fs_i[j] - BBi, BBi = 6 n_i w_j (u_l . c_j), u_l = V_e + omega_e x
+       (x_l - X_e) of p's element e; the element gains (2 (fs_i[j] - w_j) - BBi) c_j and its
+       moment about X_e (node::bounceBackForce, node.cpp:283-291).  A node the particle
+       uncovers is refilled with f_eq(rho, u_l), rho the mean density of its fluid links (1
+       without any); a node it covers drops its populations.  Single spheres without
+       periodic faces, no free surface, no cylinders (HB_ERR_UNSUPPORTED otherwise). */
+    int32_t coupling;
 } hb_params;
 
 /* Elements (DEM.cpp:81-127 particle file row): single spheres, or 2-4 spheres when size is given. */
@@ -218,6 +237,19 @@ int hb_download_lattice(hb_ctx* ctx, uint8_t* type, uint8_t* inside, uint32_t* s
 int hb_download_elements(hb_ctx* ctx, double* x0, double* x1, double* w, double* q0,
                          double* fhydro, double* mhydro, double* fparticle, double* fwall,
                          double* mparticle, double* mwall, double* fluid_volume);
+/* The same download queued on the context stream behind the steps already issued; it
+ * returns without waiting.  The arrays hold the values once hb_synchronize returns and
+ * must stay valid until then.  Page-locked arrays (hb_host_register) are filled by
+ * asynchronous copies, so a driver can issue step after step and read the element state
+ * of each without stalling the device; pageable arrays are filled by the CUDA runtime's
+ * synchronous path. */
+int hb_download_elements_async(hb_ctx* ctx, double* x0, double* x1, double* w, double* q0,
+                               double* fhydro, double* mhydro, double* fparticle, double* fwall,
+                               double* mparticle, double* mwall, double* fluid_volume);
+/* Page-locks (cudaHostRegister) / releases host memory the caller passes to the
+ * asynchronous downloads. */
+int hb_host_register(void* p, size_t bytes);
+int hb_host_unregister(void* p);
 /* Candidate pair list as sorted (min,max) pairs, like DEM::neighborTable
  * (DEM.cpp:1369-1494) after normalisation.  *count receives the pair count.  With
  * periodic faces a ghost particle is numbered E + g (g its index in hb_download_ghosts),
@@ -316,20 +348,25 @@ int hb_adjoint_timing(hb_ctx* ctx, float* ms_forward, float* ms_reverse,
 
 /* ---- allocation-free entry point ----------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory:
- * host drivers that run each solver step inside a CUDA stream capture, where
- * cudaMalloc is not allowed, and integrations confined to a device-memory budget fixed
- * by the embedding application.  Computes the moving-wall momentum exchange of one
+ * an application that reserves the device memory up front and gives this library a
+ * fixed budget (its own pool allocator owns the rest), and host loops with a latency
+ * bound that cannot take the device-wide synchronisation a cudaMalloc or cudaFree may
+ * cause.  Computes the moving-wall momentum exchange of one
  * streamed state (the quantity hb_download_walls reports, LB.cpp:1321-1341) from caller
  * device buffers and allocates nothing: its scratch is a fixed 152 KiB device array
  * inside the library, kept by every GPU that loads it until the process exits.
  *   f          [19*N] FP64 populations after streaming, component-major
- *   type       [N] node type codes (0..9), solid [N] wall index of wall nodes
+ *   type       [N] node type codes (0..9; flag bits above the code are ignored),
+ *              solid [N] wall index of wall nodes
  *   rho, mass  [N]; u [3*N] (wall-node velocities are read from u)
  *   wall_force [3*6+1] device output: per wall (Fx,Fy,Fz) in wall order, then the
  *              extra mass; stream: cudaStream_t or NULL for the default stream.
- * The first call on a device resolves the scratch address for that device: make it
- * before any stream capture.  Calls that overlap on the GPU share the scratch and race;
- * the caller serialises them.  Lattices above HB_NOALLOC_MAX_NODES give HB_ERR_ARG. */
+ * The first call on a device resolves the scratch address for that device and keeps
+ * it: make that first call before any stream capture, and make no call after a
+ * cudaDeviceReset of that device in the same process (the reset unloads the scratch).
+ * Calls that overlap on the GPU share the scratch and race; the caller serialises them.
+ * Each call overwrites every partial it reads, so no result depends on an earlier call.
+ * Lattices above HB_NOALLOC_MAX_NODES give HB_ERR_ARG. */
 #define HB_NOALLOC_MAX_NODES (1LL << 28)
 int hb_wall_force_noalloc(const double* f, const uint8_t* type, const uint32_t* solid,
                           const double* rho, const double* u, const double* mass,

@@ -993,6 +993,46 @@ void reconstruct(hbo_sim& s, size_t i) {  // node::reconstruct, node.cpp:63-83
     s.u[i] = v3(ux / nn, uy / nn, uz / nn);
 }
 
+// Moving bounce-back coupling (not in the reference: its particle branch is commented out,
+// LB.cpp:1247-1276, and is restated here with the moving-wall rule of LB.cpp:1321-1341).
+// Velocity of the solid at node l inside a particle: the element's velocity plus its spin
+// times the lever arm from the element centre, radius = pos - x0 + radiusVec.
+V3 mbbVelocity(const hbo_sim& s, size_t l) {
+    const Part& q = s.parts[s.solid[l]];
+    const Elmt& e = s.el[q.cluster];
+    const V3 radius = add(sub(s.pos(l), q.x0), q.radiusVec);
+    return add(e.x1, cross(e.wGlobal, radius));
+}
+
+// Element force and torque of the moving bounce-back links (node::bounceBackForce,
+// node.cpp:283-291): (2 (fs_j - w_j rho0) - BBi) c_j per fluid -> particle link, in
+// node order then link order; fluidVolume counts the element's solid nodes.
+void mbbForces(hbo_sim& s) {
+    for (auto& e : s.el) {
+        e.FHydro = v3(0, 0, 0);
+        e.MHydro = v3(0, 0, 0);
+        e.fluidVolume = 0.0;
+    }
+    for (size_t k = 0; k < s.activeNodes.size(); ++k) {
+        const size_t i = s.activeNodes[k];
+        if (s.inside[i]) {
+            s.el[s.parts[s.solid[i]].cluster].fluidVolume += 1.0;
+            continue;
+        }
+        for (int j = 1; j < Q; ++j) {
+            const uint32_t l = s.nb[i * Q + j];
+            if (!((s.type[l] == 0 || s.type[l] == 3) && s.inside[l])) continue;
+            const Part& q = s.parts[s.solid[l]];
+            Elmt& e = s.el[q.cluster];
+            const V3 radius = add(sub(s.pos(l), q.x0), q.radiusVec);
+            const double BBi = 6.0 * s.n[i] * W[j] * dot(add(e.x1, cross(e.wGlobal, radius)), cvec(j));
+            const V3 BBforce = mul(2.0 * (s.fs[i * Q + j] - 1.0 * W[j]) - BBi, cvec(j));
+            e.FHydro = add(e.FHydro, BBforce);
+            e.MHydro = add(e.MHydro, cross(radius, BBforce));
+        }
+    }
+}
+
 void computeHydroForces(hbo_sim& s) {  // LB.cpp:1851-1919
     for (auto& e : s.el) {
         e.FHydro = v3(0, 0, 0);
@@ -1095,15 +1135,20 @@ bool streaming(hbo_sim& s) {  // LB.cpp:1144-1488
         std::memcpy(&s.fs[i * Q], &s.f[i * Q], sizeof(double) * Q);
     }
     int bad = 0;
+    const bool mbb = s.P.coupling == HB_MOVING_BB;
 #pragma omp parallel for schedule(static) reduction(+ : bad)
     for (long k = 0; k < (long)A; ++k) {
         const size_t i = s.activeNodes[k];
+        if (mbb && s.inside[i]) continue;  // solid
         double* fi = &s.f[i * Q];
         const double* fsi = &s.fs[i * Q];
         for (int j = 1; j < Q; ++j) {
             const uint32_t l = s.nb[i * Q + j];
             const uint8_t t = s.type[l];
-            if (t == 0 || t == 3) {
+            if ((t == 0 || t == 3) && mbb && s.inside[l]) {  // moving bounce-back on the particle
+                const double BBi = 6.0 * s.n[i] * W[j] * dot(mbbVelocity(s, l), cvec(j));
+                fi[OPP[j]] = fsi[j] - BBi;
+            } else if (t == 0 || t == 3) {
                 fi[OPP[j]] = s.fs[(size_t)l * Q + OPP[j]];
             } else if (t == 2) {  // constant-pressure gas link
                 const double usq = norm2(s.u[i]);
@@ -1154,6 +1199,7 @@ bool streaming(hbo_sim& s) {  // LB.cpp:1144-1488
         }
     }
     if (bad) return fail("TYPE ERROR: link to an unsupported node type");
+    if (mbb) mbbForces(s);
     // moving-wall force and extra mass in the reference's ordered node order (LB.cpp:1321-1341)
     double extraMass = 0.0;
     for (size_t k = 0; k < A; ++k) {
@@ -1176,12 +1222,19 @@ bool streaming(hbo_sim& s) {  // LB.cpp:1144-1488
 bool lbStep(hbo_sim& s) {  // LB::latticeBolzmannStep, LB.cpp:221-233
     cleanLists(s);
     const size_t A = s.activeNodes.size();
+    const bool mbb = s.P.coupling == HB_MOVING_BB;  // nodes inside particles are solid
 #pragma omp parallel for schedule(static)
-    for (long k = 0; k < (long)A; ++k) reconstruct(s, s.activeNodes[k]);
-    computeHydroForces(s);
+    for (long k = 0; k < (long)A; ++k)
+        if (!(mbb && s.inside[s.activeNodes[k]])) reconstruct(s, s.activeNodes[k]);
+    if (mbb) {
+        for (size_t k = 0; k < A; ++k) s.hf[s.activeNodes[k]] = v3(0, 0, 0);
+    } else {
+        computeHydroForces(s);
+    }
     if (!s.P.force_field) s.lbF = v3(0, 0, 0);  // LB.cpp:1074-1076
 #pragma omp parallel for schedule(static)
-    for (long k = 0; k < (long)A; ++k) collideNode(s, s.activeNodes[k]);
+    for (long k = 0; k < (long)A; ++k)
+        if (!(mbb && s.inside[s.activeNodes[k]])) collideNode(s, s.activeNodes[k]);
     return streaming(s);
 }
 
@@ -1358,6 +1411,40 @@ void couplingStep(hbo_sim& s) {
                 s.particleNodes.push_back(l);
             }
         }
+    }
+    if (s.P.coupling != HB_MOVING_BB) return;
+    // Moving bounce-back: a node the particle uncovered (and no particle covers again)
+    // becomes fluid with f = f_eq(rho, u), u the velocity the particle had at the node, rho
+    // the mean density of its fluid links that were fluid before this step, in link order
+    // (1 without any).  Nodes a particle covered keep their populations unused.
+    std::vector<uint8_t> popped(s.N, 0);
+    for (uint32_t i : pop) popped[i] = 1;
+    std::vector<double> rho(pop.size(), 1.0);
+    std::vector<V3> vel(pop.size());
+    for (size_t k = 0; k < pop.size(); ++k) {
+        const uint32_t i = pop[k];
+        if (s.inside[i]) continue;
+        double sum = 0.0;
+        int cnt = 0;
+        for (int j = 1; j < Q; ++j) {
+            const uint32_t l = s.nb[(size_t)i * Q + j];
+            if (l == i || !s.isActive(l) || s.inside[l] || popped[l]) continue;
+            sum += s.n[l];
+            ++cnt;
+        }
+        if (cnt) rho[k] = sum / (double)cnt;
+        vel[k] = mbbVelocity(s, i);  // solid[i] still names the particle that left
+    }
+    for (size_t k = 0; k < pop.size(); ++k) {
+        const uint32_t i = pop[k];
+        if (s.inside[i]) continue;
+        const V3 uu = vel[k];
+        const double usq = norm2(uu);
+        for (int j = 0; j < Q; ++j) {
+            const double vu = dot(uu, cvec(j));
+            s.f[(size_t)i * Q + j] = W[j] * rho[k] * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
+        }
+        s.n[i] = rho[k];
     }
 }
 

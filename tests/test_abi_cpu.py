@@ -109,3 +109,15 @@ def test_ctypes_mirrors_match_the_c_layout(tmp_path):
         assert got[(cname, "sizeof()")] == C.sizeof(cls), cname
         for f in cls._fields_:
             assert got[(cname, f[0])] == getattr(cls, f[0]).offset, (cname, f[0])
+
+
+def test_create_rejects_moving_bounce_back_with_free_surface_without_gpu():
+    _ensure_built()
+    lib = C.CDLL(abi.LIB_PATH)
+    lib.hb_last_error.restype = C.c_char_p
+    p = abi.make_params((8, 8, 8), (7,) * 6, free_surface=1, gas_box=(0.4, 0.6), coupling=abi.HB_MOVING_BB)
+    h = C.c_void_p()
+    assert lib.hb_create(C.byref(p), C.byref(h)) == abi.HB_ERR_UNSUPPORTED
+    assert b"moving bounce-back" in lib.hb_last_error()
+    p.coupling = 7
+    assert lib.hb_create(C.byref(p), C.byref(h)) == abi.HB_ERR_ARG

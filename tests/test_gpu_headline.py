@@ -1,0 +1,136 @@
+"""Parity at the benchmark's own sizes: configuration 2 (128^3 coupled sedimentation,
+1514 spheres r ~ U[4, 6]) in FP64 on the GPU against the FP64 oracle, with the spheres
+deposited on the floor and on each other so that the contact path (particle-particle
+and particle-wall, DEM.cpp:1668-1717, 1801-1982) runs from the first substep (multiStep
+10, at which such a bed is stable under the reference's integrator); and a
+64x32x32 slice of configuration 3 (dam break with Bingham, Smagorinsky and spheres in
+the column) in FP64 against the oracle.
+
+Exact: node types, particle flags and the particle index of every particle node
+(LB.cpp:1921-2033), the candidate pair set (DEM.cpp:1369-1494), the overlapping pair
+set, the interface cell set.  FP64 populations and density to 1e-12 relative L-inf over
+the active nodes at every snapshot; velocity and element forces to 1e-12 / 1e-10 over
+the first 10 cycles.  Later the contact sums (added per particle in another order than
+the reference's pair table, DEM.cpp:1668-1690, and the element force sums,
+LB.cpp:1897) seed rounding differences that the stiff multi-contact dynamics of a packed
+bed amplifies about 1.5-fold per cycle; after 30 cycles the velocity, whose scale in
+this nearly still fluid is ~1e-5, and the element forces are held to 1e-9 and 1e-8."""
+import os
+
+import numpy as np
+import pytest
+
+from hybird_gb300 import abi
+from hybird_gb300.workloads import dam_break, sedimentation
+from oracle_port import OracleSim, rel_linf
+
+pytestmark = pytest.mark.gpu
+
+THREADS = os.cpu_count() or 1
+
+
+def _gpu():
+    from hybird_gb300.gpu import GpuSim
+    return GpuSim
+
+
+def _pair_set(pairs):
+    p = np.sort(np.asarray(pairs, dtype=np.int64).reshape(-1, 2), axis=1)
+    return p[np.lexsort((p[:, 1], p[:, 0]))]
+
+
+def _overlapping(x0, rad):
+    """Pairs (i < j) whose corrected centres are closer than the sum of the radii."""
+    E = len(rad)
+    c = x0.reshape(3, E).T
+    out = []
+    for i in range(E):
+        d2 = ((c[i + 1:] - c[i]) ** 2).sum(1)
+        for k in np.nonzero(d2 < (rad[i] + rad[i + 1:]) ** 2)[0]:
+            out.append((i, i + 1 + k))
+    return np.array(out, dtype=np.int64).reshape(-1, 2)
+
+
+def _compare_lattice(gl, ol, tol, tag, tol_u=None):
+    np.testing.assert_array_equal(gl["type"], ol["type"], err_msg=tag)
+    np.testing.assert_array_equal(gl["inside"], ol["inside"], err_msg=tag)
+    ins = ol["inside"] == 1
+    np.testing.assert_array_equal(gl["solid"][ins], ol["solid"][ins], err_msg=tag)
+    act = (ol["type"] == 0) | (ol["type"] == 3)
+    errs = {k: rel_linf(gl[k].reshape(c, -1), ol[k].reshape(c, -1), act) for k, c in (("f", 19), ("n", 1), ("u", 3))}
+    print(tag, {k: f"{v:.2e}" for k, v in errs.items()})
+    for k, v in errs.items():
+        assert v <= (tol_u if (k == "u" and tol_u is not None) else tol), (tag, k, v)
+    return act
+
+
+@pytest.mark.parametrize("collision", [abi.HB_TRT, abi.HB_BGK])
+def test_config2_fp64_vs_oracle_with_contacts(collision):
+    p, spheres = sedimentation(abi.HB_FP64, collision=collision, deposited=True)
+    g = _gpu()(p, spheres)
+    o = OracleSim(p, spheres, threads=THREADS)
+    rad = spheres[:, 3]
+    gl, ol = g.lattice(("type", "inside", "solid")), o.lattice()
+    np.testing.assert_array_equal(gl["type"], ol["type"])
+    np.testing.assert_array_equal(gl["inside"], ol["inside"])
+    ins = ol["inside"] == 1
+    np.testing.assert_array_equal(gl["solid"][ins], ol["solid"][ins])
+    done = 0
+    contacts = 0
+    for step in (1, 10, 30):
+        g.cycle(step - done)
+        o.cycle(step - done)
+        done = step
+        tag = f"c2 {'TRT' if collision == abi.HB_TRT else 'BGK'} step {step}"
+        late = step > 10
+        ge, oe = g.elements(), o.elements()
+        errs = {k: rel_linf(ge[k], oe[k]) for k in ("x0", "x1", "FHydro", "MHydro", "FParticle", "FWall")}
+        print(tag, {k: f"{v:.2e}" for k, v in errs.items()})
+        _compare_lattice(g.lattice(), o.lattice(), 1e-12, tag, tol_u=1e-9 if late else 1e-12)
+        np.testing.assert_array_equal(_pair_set(g.pairs()), _pair_set(o.pairs()), err_msg=tag)
+        np.testing.assert_array_equal(_overlapping(ge["x0"], rad), _overlapping(oe["x0"], rad), err_msg=tag)
+        for k, tol in (("x0", 1e-12), ("x1", 1e-9 if late else 1e-12), ("FHydro", 1e-8 if late else 1e-10),
+                       ("MHydro", 1e-8 if late else 1e-10), ("FParticle", 1e-8 if late else 1e-12),
+                       ("FWall", 1e-8 if late else 1e-12)):
+            assert errs[k] <= tol, (tag, k, errs[k])
+        st = g.status()
+        contacts = max(contacts, st.contacts)
+        assert st.numeric_error == 0 and st.capacity_error == 0
+    assert contacts > 100, contacts  # the contact path ran under load
+    g.close()
+    o.close()
+
+
+def test_config3_slice_fp64_vs_oracle():
+    """A 64x32x32 slice of the dam break at the column's full proportions (x < 0.4 X,
+    z < 0.6 Z): free surface, Bingham plastic with Smagorinsky and spheres r = 5 in the
+    column."""
+    p, spheres = dam_break(abi.HB_FP64, shape=(64, 32, 32), n=4, seed=6, yield_stress=5e-6)
+    p.lbF[2] = -3e-4  # a faster collapse: the interface starts converting after about 30 steps
+    assert len(spheres) >= 2
+    g = _gpu()(p, spheres)
+    o = OracleSim(p, spheres, threads=THREADS)
+    done = 0
+    converted = 0
+    first = None
+    for step in (20, 60, 120):
+        g.cycle(step - done)
+        o.cycle(step - done)
+        done = step
+        gl, ol = g.lattice(), o.lattice()
+        act = _compare_lattice(gl, ol, 1e-11, f"c3 slice step {step}")
+        gi, oi = g.interface(), np.sort(o.interface())
+        np.testing.assert_array_equal(gi, oi)
+        if first is None:
+            first = set(oi.tolist())
+        converted = len(first.symmetric_difference(oi.tolist()))
+        assert rel_linf(gl["mass"], ol["mass"], act) <= 1e-11
+        # the Bingham viscosity divides by the shear rate, so it carries the largest
+        # relative rounding of the node fields
+        assert rel_linf(gl["visc"], ol["visc"], act) <= 1e-10
+    assert converted > 0  # interface cells were created and removed over the run
+    ge, oe = g.elements(), o.elements()
+    for k in ("x0", "FHydro"):
+        assert rel_linf(ge[k], oe[k]) <= 1e-9, (k, rel_linf(ge[k], oe[k]))
+    g.close()
+    o.close()

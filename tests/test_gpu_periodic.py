@@ -105,3 +105,42 @@ def test_box_periodic_matches_reference_fixture(prec):
             assert rel_linf(ge["x0"], ref) <= 1e-5, (step, rel_linf(ge["x0"], ref))
     assert ghost_nodes > 0
     g.close()
+
+
+def test_dem_periodic_objects_matches_reference_fixture():
+    """Fixed objects near periodic faces get periodic images (DEM::periodicObjects,
+    DEM.cpp:990-1063): spheres driven along x through the faces meet an object's image
+    across the face.  Against the reference's fixture: the object count with images, the
+    ghost list, the candidate pair set, the objects' particle forces and the element
+    trajectories (which the image contacts change)."""
+    d = load_golden("dem_periodic_objects")
+    p = golden_params(d)
+    E = d["spheres"].shape[0]
+    g = _gpu()(p, d["spheres"], d["objects"])
+    n_std = d["objects"].shape[0]
+    n_all = d["s0_o_FParticle"].size // 3  # the reference's objects list, images appended
+    assert n_all > n_std
+    assert len(g.objects()) == 3 * n_all
+    image_hits = 0
+    done = 0
+    for step in d["steps"]:
+        if step > done:
+            g.cycle(int(step) - done)
+            done = int(step)
+        pre = f"s{step}_"
+        _check_ghosts(g, d, pre)
+        near = d[pre + "nearObjectTable"].reshape(-1, 2)
+        image_hits += int((near[:, 1] >= n_std).sum())
+        ge = g.elements()
+        early = step <= 60
+        for k, gk, tol in (("x0", "e_x0", 1e-10 if early else 1e-5), ("x1", "e_x1", 1e-8 if early else 1e-2)):
+            ref = d[pre + gk].reshape(-1, 3).T.reshape(-1)
+            assert rel_linf(ge[k], ref) <= tol, (step, k, rel_linf(ge[k], ref))
+        if step > 0:
+            np.testing.assert_array_equal(g.pairs().reshape(-1, 2).astype(np.int64), _ref_pairs(d, pre, E),
+                                          err_msg=f"step {step}")
+        ref_o = d[pre + "o_FParticle"]
+        go = g.objects()
+        assert np.abs(go - ref_o).max() <= 1e-10 * max(1.0, np.abs(ref_o).max()), (step, go, ref_o)
+    assert image_hits > 0  # some sphere had an object image in range
+    g.close()
