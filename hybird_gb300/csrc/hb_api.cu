@@ -62,6 +62,8 @@ int dalloc(T** p, size_t count) {
 int check_params(const hb_params* p) {
     for (int k = 0; k < 3; ++k)
         if (p->lb_size[k] < 3) return seterr(HB_ERR_ARG, "lb_size[%d] = %d < 3", k, p->lb_size[k]);
+    for (int k = 0; k < 3; ++k)  // node coordinates travel as 16-bit values in the mask queues
+        if (p->lb_size[k] > 65535) return seterr(HB_ERR_UNSUPPORTED, "lb_size[%d] = %d > 65535", k, p->lb_size[k]);
     for (int k = 0; k < 3; ++k)
         if (p->units[k] != 1.0) return seterr(HB_ERR_UNSUPPORTED, "units must be 1 (lattice units)");
     for (int k = 0; k < 6; ++k) {
@@ -372,6 +374,12 @@ using namespace hb;
 
 static int build_graph(hb_ctx* c);
 
+// the element force sums of a lattice step are completed by the next cycle (or a
+// download) -- except with moving bounce-back in FP64, whose force pass writes them
+static bool sums_lag(const hb_ctx* c) {
+    return !(c->P.coupling == HB_MOVING_BB && c->P.precision == HB_FP64);
+}
+
 extern "C" {
 
 const char* hb_last_error(void) { return g_err.c_str(); }
@@ -433,7 +441,7 @@ int hb_destroy(hb_ctx* c) {
                     c->d.base, c->d.alt, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
                     c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
-                    c->d.claim_list, c->d.claim_cnt, c->d.pop_list, c->d.pop_cnt, c->d.pop_rho, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
+                    c->d.claim_list, c->d.claim_cnt, c->d.mask_done, c->d.pop_list, c->d.pop_cnt, c->d.pop_rho, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
                     c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix, c->fs_ilist,
                     c->curved_list, c->curved_cnt, c->d.cyl_of, c->io_terms, c->d.gmeta, c->d.gorig, c->d.gvec,
                     c->d.comp, c->d.ccnt, c->d.px, c->d.remark, c->d.ecomp, c->d.eccnt, c->d.pkey, c->d.efirst,
@@ -496,6 +504,8 @@ int hb_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         }
         if (!c->d.claim_list && (rc = dalloc(&c->d.claim_list, 2 * N))) return rc;
         if (!c->d.claim_cnt && (rc = dalloc(&c->d.claim_cnt, 1))) return rc;
+        if (!c->d.mask_done && (rc = dalloc(&c->d.mask_done, 1))) return rc;
+        CK(cudaMemset(c->d.mask_done, 0, sizeof(unsigned int)));
         if (!c->d.boxes && (rc = dalloc((uint8_t**)&c->d.boxes, ((size_t)c->d.P + c->d.gcap) * 128))) return rc;
         CK(cudaMemset(c->d.claim_cnt, 0, sizeof(int)));
         if (mbb) {
@@ -627,6 +637,7 @@ namespace hb {
 constexpr int STAGE_DOUBLES_PER_ELEMENT = 35;
 struct GatherArgs {
     const double* src[11];
+    double* dst[11];  // per-field destinations (mapped host memory), or all null: the staging block
     long long off[12];
     int hsum[11];  // >= 0: the field is the element sums' component hsum.. (FHydro 0, MHydro 3,
                    // fluidVolume 6) converted from the fixed-point accumulators on the fly
@@ -640,12 +651,15 @@ __global__ void k_gather(GatherArgs g, double* dst) {
     int k = 0;
     while (k + 1 < g.n && t >= g.off[k + 1]) ++k;
     const long long r = t - g.off[k];
+    double v;
     if (g.hsum[k] >= 0) {  // (r / E) selects the component, as in convert_sums
         const long long comp = r / g.E, p = r - comp * g.E;
-        dst[t] = (double)(long long)g.hacc[(g.hsum[k] + comp) * g.E + p] * HACC_INV;
+        v = (double)(long long)g.hacc[(g.hsum[k] + comp) * g.E + p] * HACC_INV;
     } else {
-        dst[t] = g.src[k][r];
+        v = g.src[k][r];
     }
+    if (g.dst[k]) g.dst[k][r] = v;  // straight into the caller's mapped host array
+    else dst[t] = v;
 }
 
 // lbF and its FP32 copy from kernel arguments (stream-ordered, no host staging)
@@ -664,7 +678,7 @@ static int run_cycles(hb_ctx* c, int n, bool last_mirror) {
         if (c->P.dem_solve && c->d.E > 0) c->dem_stepped = true;
         if (c->P.lb_solve) {
             c->cur ^= 1;
-            c->reduce_pending = c->P.coupling != HB_MOVING_BB;  // the sums lag the lattice step
+            c->reduce_pending = sums_lag(c);  // the sums lag the lattice step
         }
         ++c->steps;
     }
@@ -707,7 +721,7 @@ int hb_lb_step(hb_ctx* c) {
     if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
     if (!c->P.force_field) CK(cudaMemsetAsync(c->fs_force, 0, sizeof(double) * 3, c->stream));
     c->cur ^= 1;
-    c->reduce_pending = c->P.coupling != HB_MOVING_BB;  // the sums lag the lattice step
+    c->reduce_pending = sums_lag(c);  // the sums lag the lattice step
     ++c->steps;
     CK(cudaGetLastError());
     return HB_OK;
@@ -816,7 +830,8 @@ struct ElemItem {
 };
 constexpr int kElemItems = 11;
 
-int enqueue_element_gather(hb_ctx* c, double* const dst[kElemItems], ElemItem items[kElemItems], hb::GatherArgs* g) {
+int enqueue_element_gather(hb_ctx* c, double* const dst[kElemItems], ElemItem items[kElemItems], hb::GatherArgs* g,
+                           double* const* alias = nullptr) {
     const int E = c->d.E;
     const bool inline_sums = c->reduce_pending && c->hacc;
     if (c->reduce_pending && !c->hacc) launch_couple_reduce(c);
@@ -837,6 +852,7 @@ int enqueue_element_gather(hb_ctx* c, double* const dst[kElemItems], ElemItem it
     for (int k = 0; k < kElemItems; ++k)
         if (items[k].dst) {
             g->src[g->n] = items[k].src;
+            g->dst[g->n] = alias ? alias[k] : nullptr;
             g->hsum[g->n] = items[k].hsum;
             g->off[g->n + 1] = g->off[g->n] + (long long)items[k].comps * E;
             ++g->n;
@@ -846,6 +862,17 @@ int enqueue_element_gather(hb_ctx* c, double* const dst[kElemItems], ElemItem it
     hb::k_gather<<<(unsigned)ceil_div(total, 256), 256, 0, c->stream>>>(*g, c->d_stage);
     CK(cudaGetLastError());
     return HB_OK;
+}
+
+// device address of a host array the GPU can write directly (page-locked and mapped, as
+// hb_host_register makes it), or null
+double* mapped_alias(double* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // an unregistered pointer is not an error here
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? static_cast<double*>(at.devicePointer) : nullptr;
 }
 }  // namespace
 
@@ -878,8 +905,14 @@ int hb_download_elements_async(hb_ctx* c, double* x0, double* x1, double* w, dou
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
     if (c->d.E == 0) return HB_OK;
     double* const dst[kElemItems] = {x0, x1, w, q0, fhydro, mhydro, fparticle, fwall, mparticle, mwall, fluid_volume};
+    // page-locked, mapped arrays: the gather kernel writes them directly (no copy)
+    double* alias[kElemItems] = {};
+    bool mapped = true;
+    for (int k = 0; k < kElemItems; ++k)
+        if (dst[k] && !(alias[k] = mapped_alias(dst[k]))) mapped = false;
     ElemItem items[kElemItems];
     hb::GatherArgs g;
+    if (mapped) return enqueue_element_gather(c, dst, items, &g, alias);
     int rc = enqueue_element_gather(c, dst, items, &g);
     if (rc || g.n == 0) return rc;
     // one copy per field straight into the caller's arrays, ordered behind the gather; the
@@ -896,7 +929,7 @@ int hb_download_elements_async(hb_ctx* c, double* x0, double* x1, double* w, dou
 
 int hb_host_register(void* p, size_t bytes) {
     if (!p || bytes == 0) return seterr(HB_ERR_ARG, "null pointer or zero size");
-    CK(cudaHostRegister(p, bytes, cudaHostRegisterDefault));
+    CK(cudaHostRegister(p, bytes, cudaHostRegisterMapped));
     return HB_OK;
 }
 
@@ -1193,7 +1226,7 @@ int hb_profile_phases(hb_ctx* c, int32_t nsteps, double* us, int32_t* nphases) {
         launch_lb_step(c, c->cur);
         if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
         c->cur ^= 1;
-        c->reduce_pending = c->P.coupling != HB_MOVING_BB;  // the sums lag the lattice step
+        c->reduce_pending = sums_lag(c);  // the sums lag the lattice step
         ++c->steps;
     }
     CK(cudaStreamSynchronize(c->stream));
@@ -1229,7 +1262,7 @@ int hb_time_cycles(hb_ctx* c, int32_t nsteps, float* ms_total, float* ms_lb_kern
     CK(cudaEventRecord(c->ev0, c->stream));
     for (int s = 0; s < nsteps; ++s) {
         CK(cudaGraphLaunch(c->gexec[c->cur], c->stream));
-        if (c->P.lb_solve) { c->cur ^= 1; c->reduce_pending = c->P.coupling != HB_MOVING_BB; }
+        if (c->P.lb_solve) { c->cur ^= 1; c->reduce_pending = sums_lag(c); }
         ++c->steps;
     }
     CK(cudaEventRecord(c->ev1, c->stream));
@@ -1253,7 +1286,7 @@ int hb_time_cycles(hb_ctx* c, int32_t nsteps, float* ms_total, float* ms_lb_kern
             CK(cudaEventRecord(ev[2 * s + 1], c->stream));
             if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
             c->cur ^= 1;
-            c->reduce_pending = c->P.coupling != HB_MOVING_BB;  // the sums lag the lattice step
+            c->reduce_pending = sums_lag(c);  // the sums lag the lattice step
             ++c->steps;
         }
         CK(cudaStreamSynchronize(c->stream));

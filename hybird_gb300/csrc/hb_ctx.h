@@ -46,6 +46,7 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     double* react = nullptr;    // [3*(MAX_WALLS + O)] wall and object FParticle (ordered sums of the records)
     uint32_t* claim_list = nullptr;  // [2N] (node, particle) pairs joined by the coupling in this step
     int* claim_cnt = nullptr;
+    unsigned int* mask_done = nullptr;  // finished blocks of the mask pass (its last block commits)
     uint32_t* pop_list = nullptr;    // [N] nodes a particle uncovered in this step (moving bounce-back)
     int* pop_cnt = nullptr;
     double* pop_rho = nullptr;       // [N] their refill density

@@ -153,7 +153,8 @@ __device__ double tangential_contact(const DemArgs& a, double vt, double fn, dou
 // ---- neighbour rebuild (DEM.cpp:1326-1533) -------------------------------------------
 
 // single CTA: cell of every particle (linearizePosition, vector.cpp:147-149), counting
-// sort into cells, then ascending order inside each cell
+// sort into cells (counts, a block-wide scan, scatter), then ascending order inside each
+// cell: the particles sorted by (cell, index)
 // With periodic faces the table holds the ghosts too (after the elements, positions from
 // the rebuild's px) and a particle's cell is the reference's linear index itself: a ghost
 // above the last y cell row lands in row 0 of the next z slab, as in the reference's cell
@@ -184,10 +185,29 @@ __device__ __noinline__ void nl_cells_block(const DemArgs& a) {
     if (per)
         for (int i = threadIdx.x; i < a.P; i += blockDim.x) a.nbr_cnt[i] = 0;
     __syncthreads();
-    if (threadIdx.x == 0) {  // exclusive scan (ncells is small: a few thousand)
-        int s = 0;
-        for (int c = 0; c < nc; ++c) { a.cell_start[c] = s; s += a.cell_cnt[c]; }
-        a.cell_start[nc] = s;
+    {  // exclusive scan of the cell counts by the whole block, a chunk of blockDim cells at
+       // a time (Hillis-Steele in shared memory), carrying the running total
+        __shared__ int sc[256];
+        __shared__ int carry;
+        if (threadIdx.x == 0) carry = 0;
+        __syncthreads();
+        for (int c0 = 0; c0 < nc; c0 += blockDim.x) {
+            const int c = c0 + threadIdx.x;
+            const int v = c < nc ? a.cell_cnt[c] : 0;
+            sc[threadIdx.x] = v;
+            __syncthreads();
+            for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+                const int add = threadIdx.x >= (unsigned)off ? sc[threadIdx.x - off] : 0;
+                __syncthreads();
+                sc[threadIdx.x] += add;
+                __syncthreads();
+            }
+            if (c < nc) a.cell_start[c] = carry + sc[threadIdx.x] - v;
+            __syncthreads();
+            if (threadIdx.x == blockDim.x - 1) carry += sc[threadIdx.x];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) a.cell_start[nc] = carry;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
@@ -1223,6 +1243,7 @@ struct CoupleArgs {
     const unsigned long long* hacc;  // fixed-point element sums (FP32/FP16 lattice kernels)
     uint32_t* claim_list;       // [2N] (node, particle) joined in this step
     int* claim_cnt;
+    unsigned int* mask_done;    // blocks of the mask kernel that have finished (the last one commits)
     int mbb;                    // moving bounce-back: list the nodes that leave their particle
     uint32_t* pop_list;         // [N] (their populations are refilled before the lattice step)
     int* pop_cnt;
@@ -1379,7 +1400,8 @@ __device__ __forceinline__ int cover_first(const CoupleArgs& a, uint32_t q, int 
 //    above half a lattice unit per step) join in the next step.
 // Each node decides only for itself.  A source's own flag may be read before or after
 // its own pop; both give the same decision because a source must also still be covered
-// (in_sph).  New members are listed and joined by k_commit, so no node added in this
+// (in_sph).  New members are listed and joined after every block has decided (by the
+// last block of the mask kernel), so no node added in this
 // pass acts as a source in it.
 __device__ __forceinline__ void claim_push(const CoupleArgs& a, long long l, unsigned long long best) {
     const int slot = atomicAdd(a.claim_cnt, 1);
@@ -1432,52 +1454,123 @@ __device__ __noinline__ void mask_node_general(const CoupleArgs& a, int x, int y
 
 __device__ __forceinline__ uint8_t byte_of(uint32_t w, int k) { return (uint8_t)(w >> (8 * k)); }
 
+// the claim decision of one node (x, y, z) = l whose 6-neighbour sources in kk order
+// (x-1, x+1, y-1, y+1, z-1, z+1) carry the particle flag where bit kk of tm is set: the
+// particle q of each flagged source m, the lowest (m, q) among those where q still covers
+// m and covers l (findNewSolid, LB.cpp:1969-2033)
+__device__ __forceinline__ void claim_node(const CoupleArgs& a, int x, int y, int z, long long l, unsigned tm) {
+    const long long sy = a.X, sz = (long long)a.X * a.Y;
+    const long long ms[6] = {l - 1, l + 1, l - sy, l + sy, l - sz, l + sz};
+    // the sources' particles in one round of independent loads (own index for
+    // non-sources, a valid address); usually every flagged source has the same one
+    uint32_t qs[6];
+#pragma unroll
+    for (int kk = 0; kk < 6; ++kk) qs[kk] = a.solid[((tm >> kk) & 1u) ? ms[kk] : l];
+    uint32_t q0 = 0xffffffffu;
+    bool several = false;
+#pragma unroll
+    for (int kk = 0; kk < 6; ++kk)
+        if ((tm >> kk) & 1u) {
+            if (q0 == 0xffffffffu) q0 = qs[kk];
+            else if (qs[kk] != q0) several = true;
+        }
+    const bool cov0 = in_sph(a.tab[q0].s, x, y, z);
+    if (!cov0 && !several) return;  // just outside its particle: the common case
+    unsigned long long best = ~0ull;
+#pragma unroll
+    for (int kk = 0; kk < 6; ++kk) {
+        if (!((tm >> kk) & 1u)) continue;
+        const uint32_t q = qs[kk];
+        const Sph& sq = a.tab[q].s;
+        const bool covered = q == q0 ? cov0 : in_sph(sq, x, y, z);
+        if (!covered || !in_sph(sq, x - cx(kk + 1), y - cy(kk + 1), z - cz(kk + 1))) continue;
+        const unsigned long long key = ((unsigned long long)ms[kk] << 32) | q;
+        if (key < best) best = key;
+    }
+    if (best != ~0ull) claim_push(a, l, best);
+}
+
+// The claimed nodes join their particles once every block of the mask pass has decided:
+// the last block to finish (a counter of finished blocks, each publishing its claims
+// first) applies the list, so no node claimed in the pass acted as a source in it.
+__device__ __forceinline__ void commit_when_last(const CoupleArgs& a) {
+    __shared__ bool s_last;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int nthreads = blockDim.x * blockDim.y;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+        s_last = atomicAdd(a.mask_done, 1u) == nb - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (a.ghosts && tid == 0) a.gmeta[1] = 0;  // re-mark done
+    const int n = *(volatile int*)a.claim_cnt;
+    for (int q = tid; q < n; q += nthreads) {
+        const uint32_t l = a.claim_list[2 * q], p = a.claim_list[2 * q + 1];
+        a.ntype[l] = a.ntype[l] | HB_INSIDE;
+        a.solid[l] = p;
+    }
+    if (tid == 0) *a.mask_done = 0u;  // ready for the next pass
+}
+
 // Four consecutive nodes of a row per thread, 4-byte loads of the node bytes of the row
-// and of the four neighbouring rows, so a thread's loads are in flight together.  Rows
-// near a periodic face, or of a length that is not a multiple of 4, take the general
-// per-node rules.
+// and of the four neighbouring rows, so a thread's loads are in flight together.  A warp
+// owns 128 nodes of one row; it first sorts them with ballots into two queues in shared
+// memory -- particle nodes (a pop test each) and other nodes with a flagged 6-neighbour (a
+// claim test each) -- and then works each queue with all its lanes on the same kind of
+// item, instead of each lane walking its own mix of node kinds.  A node that pops joins
+// the claim queue when a neighbour carries the flag.  Rows near a periodic face, or of a
+// length that is not a multiple of 4, take the general per-node rules.
 __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
+    __shared__ uint32_t s_pop[4][128];    // x | node byte << 16 | neighbour flags << 24
+    __shared__ uint32_t s_psk[4][128];    // the particle of a queued particle node
+    __shared__ uint32_t s_claim[4][128];  // x | neighbour flags << 16
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x, w = threadIdx.y;
+    const unsigned lt = (1u << lane) - 1u;
     const int x0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
-    if (x0 >= a.X || y >= a.Y) return;
+    const bool valid = x0 < a.X && y < a.Y;
     const bool pnear = ((a.per[0] | a.per[1]) && (x0 < 2 || x0 + 3 > a.X - 3)) ||
                        ((a.per[2] | a.per[3]) && (y < 2 || y > a.Y - 3)) ||
                        ((a.per[4] | a.per[5]) && (z < 2 || z > a.Z - 3));
-    if ((a.X & 3) || pnear || a.ghosts) {
+    const bool general = valid && ((a.X & 3) || pnear || a.ghosts);
+    if (general)
         for (int k = 0; k < 4 && x0 + k < a.X; ++k) mask_node_general(a, x0 + k, y, z);
-        return;
-    }
+    const bool fast = valid && !general;
     // without a periodic face nearby every link is plain arithmetic: a source is the
     // interior node one step back, and its forward link lands here
     const long long sy = a.X, sz = (long long)a.X * a.Y;
     const long long l0 = (long long)x0 + sy * y + sz * z;
     const bool iy = y >= 1 && y <= a.Y - 2, iz = z >= 1 && z <= a.Z - 2;
     const uint32_t* w32 = reinterpret_cast<const uint32_t*>(a.ntype);
-    const uint32_t tw = w32[l0 >> 2];
-    const uint32_t wym = (y - 1 >= 1 && iz) ? w32[(l0 - sy) >> 2] : 0u;
-    const uint32_t wyp = (y + 1 <= a.Y - 2 && iz) ? w32[(l0 + sy) >> 2] : 0u;
-    const uint32_t wzm = (z - 1 >= 1 && iy) ? w32[(l0 - sz) >> 2] : 0u;
-    const uint32_t wzp = (z + 1 <= a.Z - 2 && iy) ? w32[(l0 + sz) >> 2] : 0u;
-    const uint8_t tl = (x0 - 1 >= 1 && iy && iz) ? a.ntype[l0 - 1] : (uint8_t)0;
-    const uint8_t tr = (x0 + 4 <= a.X - 2 && iy && iz) ? a.ntype[l0 + 4] : (uint8_t)0;
+    uint32_t tw = 0u, wym = 0u, wyp = 0u, wzm = 0u, wzp = 0u;
+    uint8_t tl = 0, tr = 0;
     uint32_t sl[4] = {0u, 0u, 0u, 0u};
-    if (tw & 0x10101010u) {  // HB_INSIDE in any of the four bytes
-        const uint4 v = *reinterpret_cast<const uint4*>(a.solid + l0);
-        sl[0] = v.x; sl[1] = v.y; sl[2] = v.z; sl[3] = v.w;
+    if (fast) {
+        tw = w32[l0 >> 2];
+        wym = (y - 1 >= 1 && iz) ? w32[(l0 - sy) >> 2] : 0u;
+        wyp = (y + 1 <= a.Y - 2 && iz) ? w32[(l0 + sy) >> 2] : 0u;
+        wzm = (z - 1 >= 1 && iy) ? w32[(l0 - sz) >> 2] : 0u;
+        wzp = (z + 1 <= a.Z - 2 && iy) ? w32[(l0 + sz) >> 2] : 0u;
+        tl = (x0 - 1 >= 1 && iy && iz) ? a.ntype[l0 - 1] : (uint8_t)0;
+        tr = (x0 + 4 <= a.X - 2 && iy && iz) ? a.ntype[l0 + 4] : (uint8_t)0;
+        if (tw & 0x10101010u) {  // HB_INSIDE in any of the four bytes
+            const uint4 v = *reinterpret_cast<const uint4*>(a.solid + l0);
+            sl[0] = v.x; sl[1] = v.y; sl[2] = v.z; sl[3] = v.w;
+        }
     }
-#pragma unroll 1
+    // queue the four nodes of every lane (ballots give each item its slot)
+    int np = 0, nc = 0;
+#pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int x = x0 + k;
-        const long long l = l0 + k;
         const uint8_t t = byte_of(tw, k);
-        if (t & HB_INSIDE) {
-            const uint32_t sk = k == 0 ? sl[0] : (k == 1 ? sl[1] : (k == 2 ? sl[2] : sl[3]));  // registers
-            if (in_sph(a.tab[sk].s, x, y, z)) continue;  // stays
-            a.ntype[l] = t & ~HB_INSIDE;                     // pop
-            if (a.mbb) mbb_pop(a, l);
-        }
         const bool ix = x >= 1 && x <= a.X - 2;
-        // source flags in kk order: x-1, x+1, y-1, y+1, z-1, z+1 (pre- or post-pop)
+        // source flags in kk order: x-1, x+1, y-1, y+1, z-1, z+1
         uint8_t tm[6];
         tm[0] = (x - 1 >= 1 && iy && iz) ? (k > 0 ? byte_of(tw, k - 1) : tl) : (uint8_t)0;
         tm[1] = (x + 1 <= a.X - 2 && iy && iz) ? (k < 3 ? byte_of(tw, k + 1) : tr) : (uint8_t)0;
@@ -1485,36 +1578,51 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
         tm[3] = ix ? byte_of(wyp, k) : (uint8_t)0;
         tm[4] = ix ? byte_of(wzm, k) : (uint8_t)0;
         tm[5] = ix ? byte_of(wzp, k) : (uint8_t)0;
-        if (!((tm[0] | tm[1] | tm[2] | tm[3] | tm[4] | tm[5]) & HB_INSIDE)) continue;
-        const long long ms[6] = {l - 1, l + 1, l - sy, l + sy, l - sz, l + sz};
-        // the six sources' particles in one round of independent loads (own index for
-        // non-sources, a valid address); usually every flagged source has the same one
-        uint32_t qs[6];
+        unsigned bits = 0u;
 #pragma unroll
-        for (int kk = 0; kk < 6; ++kk) qs[kk] = a.solid[(tm[kk] & HB_INSIDE) ? ms[kk] : l];
-        uint32_t q0 = 0xffffffffu;
-        bool several = false;
-#pragma unroll
-        for (int kk = 0; kk < 6; ++kk)
-            if (tm[kk] & HB_INSIDE) {
-                if (q0 == 0xffffffffu) q0 = qs[kk];
-                else if (qs[kk] != q0) several = true;
-            }
-        const bool cov0 = in_sph(a.tab[q0].s, x, y, z);
-        if (!cov0 && !several) continue;  // just outside its particle: the common case
-        unsigned long long best = ~0ull;
-#pragma unroll
-        for (int kk = 0; kk < 6; ++kk) {
-            if (!(tm[kk] & HB_INSIDE)) continue;
-            const uint32_t q = qs[kk];
-            const Sph& sq = a.tab[q].s;
-            const bool covered = q == q0 ? cov0 : in_sph(sq, x, y, z);
-            if (!covered || !in_sph(sq, x - cx(kk + 1), y - cy(kk + 1), z - cz(kk + 1))) continue;
-            const unsigned long long key = ((unsigned long long)ms[kk] << 32) | q;
-            if (key < best) best = key;
+        for (int kk = 0; kk < 6; ++kk) bits |= ((tm[kk] & HB_INSIDE) ? 1u : 0u) << kk;
+        const bool pc = fast && (t & HB_INSIDE);
+        const unsigned bp = __ballot_sync(full, pc);
+        if (pc) {
+            const int q = np + __popc(bp & lt);
+            s_pop[w][q] = (uint32_t)x | ((uint32_t)t << 16) | (bits << 24);
+            s_psk[w][q] = k == 0 ? sl[0] : (k == 1 ? sl[1] : (k == 2 ? sl[2] : sl[3]));  // registers
         }
-        if (best != ~0ull) claim_push(a, l, best);
+        np += __popc(bp);
+        const bool cc = fast && !(t & HB_INSIDE) && bits != 0u;
+        const unsigned bc = __ballot_sync(full, cc);
+        if (cc) s_claim[w][nc + __popc(bc & lt)] = (uint32_t)x | (bits << 16);
+        nc += __popc(bc);
     }
+    __syncwarp();
+    // findNewActive (LB.cpp:1921-1967): a particle node no longer covered by its particle
+    // leaves it; then it may be claimed like any other node
+    for (int base = 0; base < np; base += 32) {
+        const int q = base + lane;
+        bool join = false;
+        uint32_t item = 0u;
+        if (q < np) {
+            item = s_pop[w][q];
+            const int x = (int)(item & 0xFFFFu);
+            const long long l = l0 - x0 + x;
+            if (!in_sph(a.tab[s_psk[w][q]].s, x, y, z)) {
+                a.ntype[l] = (uint8_t)((item >> 16) & 0xFFu) & ~HB_INSIDE;  // pop
+                if (a.mbb) mbb_pop(a, l);
+                join = (item >> 24) != 0u;
+            }
+        }
+        const unsigned bj = __ballot_sync(full, join);
+        if (join) s_claim[w][nc + __popc(bj & lt)] = (item & 0xFFFFu) | ((item >> 24) << 16);
+        nc += __popc(bj);
+    }
+    __syncwarp();
+    // findNewSolid (LB.cpp:1969-2033) on the queued nodes
+    for (int q = lane; q < nc; q += 32) {
+        const uint32_t item = s_claim[w][q];
+        const int x = (int)(item & 0xFFFFu);
+        claim_node(a, x, y, z, l0 - x0 + x, item >> 16);
+    }
+    commit_when_last(a);
 }
 
 // element hydrodynamic force, torque and entrained fluid (LB.cpp:1853-1918): fixed
@@ -1905,15 +2013,6 @@ __global__ void __launch_bounds__(256) k_remark_apply(CoupleArgs a) {
 // the ghosts of the initial positions (DEM.cpp:253-257: the neighbour table built at init)
 __global__ void __launch_bounds__(256) k_ghosts_init(DemArgs a) { ghosts_block(a); }
 
-__global__ void __launch_bounds__(256) k_commit(CoupleArgs a) {
-    if (a.ghosts && blockIdx.x == 0 && threadIdx.x == 0) a.gmeta[1] = 0;  // re-mark done
-    const int n = *a.claim_cnt;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        const uint32_t l = a.claim_list[2 * q], p = a.claim_list[2 * q + 1];
-        a.ntype[l] = a.ntype[l] | HB_INSIDE;
-        a.solid[l] = p;
-    }
-}
 
 // ---- host side ------------------------------------------------------------------------
 
@@ -2036,6 +2135,7 @@ static CoupleArgs couple_args(hb_ctx* c) {
     a.hacc = c->P.precision == HB_FP64 ? nullptr : c->hacc;
     a.claim_list = c->d.claim_list;
     a.claim_cnt = c->d.claim_cnt;
+    a.mask_done = c->d.mask_done;
     a.mbb = c->P.coupling == HB_MOVING_BB ? 1 : 0;
     a.pop_list = c->d.pop_list;
     a.pop_cnt = c->d.pop_cnt;
@@ -2109,7 +2209,8 @@ int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsign
     A.c = couple_args(c);
     A.gd = reinterpret_cast<const DemArgs*>(c->d.gargs);
     A.gc = reinterpret_cast<const CoupleArgs*>(reinterpret_cast<const char*>(c->d.gargs) + GARGS_COUPLE);
-    A.do_reduce = do_reduce && c->P.coupling != HB_MOVING_BB;  // moving bounce-back: k_mbb_force wrote them
+    // moving bounce-back in FP64: the force pass after the lattice step wrote the sums
+    A.do_reduce = do_reduce && !(c->P.coupling == HB_MOVING_BB && c->P.precision == HB_FP64);
     A.do_dem = do_dem;
     A.do_boxes = do_boxes;
     A.multi = c->d.multi;
@@ -2147,7 +2248,6 @@ void launch_couple(hb_ctx* c, bool build, int cur, cudaEvent_t* ev) {
     k_mask<<<dim3((unsigned)ceil_div(ceil_div(c->X, 4), 32), (unsigned)ceil_div(c->Y, 4), (unsigned)c->Z), dim3(32, 4),
              0, c->stream>>>(a);
     if (ev) cudaEventRecord(ev[2], c->stream);
-    k_commit<<<152, 256, 0, c->stream>>>(a);
     if (a.mbb) launch_mbb_nodes(c, cur);
     if (ev) cudaEventRecord(ev[3], c->stream);
 }

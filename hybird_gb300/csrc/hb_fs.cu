@@ -170,67 +170,56 @@ __global__ void __launch_bounds__(FS_BLOCK) k_fs_ilist(FsArgs a) {
     }
 }
 
-// K1 on the list: one warp per interface cell, lane j handles link j (all loads of the
-// cell in flight together), lane 0 adds the terms in link order as the reference does.
+// K1 on the list: one thread per interface cell, its 18 links in order; the sum runs in
+// link order, as updateMass adds its terms, so each cell's new mass is the reference's
+// expression.  (One cell per thread rather than one per warp: the FP64 work of a cell
+// then shares its warp instructions with 31 other cells on this part's narrow FP64 pipe.)
 template <class P>
 __global__ void __launch_bounds__(256) k_fs_mass_list(FsArgs a) {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
     const int n = (int)min((long long)*a.icount, a.icap);
     const bool first = *a.first != 0;
-    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += warps) {
+    const uint32_t X = (uint32_t)a.X, XY = (uint32_t)a.X * (uint32_t)a.Y;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x) {
         const uint32_t iu = a.ilist[w];  // node indices fit 32 bits (the list is uint32)
-        const uint32_t X = (uint32_t)a.X, XY = (uint32_t)a.X * (uint32_t)a.Y;
         Node nd;
         nd.x = (int)(iu % X);
         nd.y = (int)((iu % XY) / X);
         nd.z = (int)(iu / XY);
         nd.i = (long long)iu;
-        const long long i = nd.i;
         nd.ok = true;
+        const long long i = nd.i;
         const double mi = a.mass[i];
-        double term = 0.0;
-        bool add = false;
-        const int j = lane;
-        if (j >= 1 && j < Q) {
+        double dm = 0.0;
+#pragma unroll
+        for (int j = 1; j < Q; ++j) {
             const long long l = fs_link(a, nd, j);
             const uint8_t t = code_of(a, l);
             double av = 0.0;
             if (t == HB_T_INTERFACE) av = 0.5 * (a.mass[l] + mi);
             else if (t == HB_T_FLUID) av = 1.0;
             else if (t == HB_T_DYNWALL) av = 1.0 * mi;  // gas, static walls: averageMass 0
-            if (av != 0.0) {
-                double diff;
-                if (t == HB_T_DYNWALL) {  // f[opp j] = fs[j] - BBi: the difference is -BBi
-                    const double fin = fval<P>(a, opp(j), i);
-                    const double uw = a.u[l] * cx(j) + a.u[a.N + l] * cy(j) + a.u[2 * a.N + l] * cz(j);
-                    const double fs = first ? fval<P>(a, j, i) : fin + 6.0 * a.rho[i] * wgt(j) * uw;
-                    diff = fin - fs;
+            if (av == 0.0) continue;
+            double diff;
+            if (t == HB_T_DYNWALL) {  // f[opp j] = fs[j] - BBi: the difference is -BBi
+                const double fin = fval<P>(a, opp(j), i);
+                const double uw = a.u[l] * cx(j) + a.u[a.N + l] * cy(j) + a.u[2 * a.N + l] * cz(j);
+                const double fs = first ? fval<P>(a, j, i) : fin + 6.0 * a.rho[i] * wgt(j) * uw;
+                diff = fin - fs;
+            } else {
+                const long long src = first ? i : l;  // fs[j]: f = fs = f_eq at initialisation,
+                                                       // else pushed to the active neighbour
+                if (P::DEV) {  // deviations: their FP32 difference is that of the populations
+                    using S = typename P::S;
+                    const S* fp = reinterpret_cast<const S*>(a.f);
+                    const float d = P::load(fp + (long long)opp(j) * a.N + i) - P::load(fp + (long long)j * a.N + src);
+                    diff = (double)d;
                 } else {
-                    const long long src = first ? i : l;  // fs[j]: f = fs = f_eq at initialisation,
-                                                           // else pushed to the active neighbour
-                    if (P::DEV) {  // deviations: their FP32 difference is that of the populations
-                        using S = typename P::S;
-                        const S* fp = reinterpret_cast<const S*>(a.f);
-                        const float d = P::load(fp + (long long)opp(j) * a.N + i) - P::load(fp + (long long)j * a.N + src);
-                        diff = (double)d;
-                    } else {
-                        diff = fval<P>(a, opp(j), i) - fval<P>(a, j, src);
-                    }
+                    diff = fval<P>(a, opp(j), i) - fval<P>(a, j, src);
                 }
-                term = 1.0 * av * diff;
-                add = true;
             }
+            dm += 1.0 * av * diff;
         }
-        const unsigned adds = __ballot_sync(full, add);
-        double dm = 0.0;
-#pragma unroll
-        for (int k = 1; k < Q; ++k) {  // sequential in link order, as updateMass sums
-            const double tk = __shfl_sync(full, term, k);
-            if (adds & (1u << k)) dm += tk;
-        }
-        if (lane == 0) a.mass2[i] = mi + dm;
+        a.mass2[i] = mi + dm;
     }
 }
 

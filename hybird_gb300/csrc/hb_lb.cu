@@ -742,12 +742,12 @@ void launch_lb_step(hb_ctx* c, int cur) {
     if (c->P.precision == HB_FP64) {
         k_collide_stream<PolF64><<<g, block, 0, c->stream>>>(a);
     } else {
-        if (a.couple) cudaMemsetAsync(c->hacc, 0, sizeof(unsigned long long) * 7 * c->d.E, c->stream);
+        if (a.couple || a.mbb) cudaMemsetAsync(c->hacc, 0, sizeof(unsigned long long) * 7 * c->d.E, c->stream);
         launch_lb_step_dev(c, a);
     }
     launch_slip(c, a.fout);    // slip-wall mixing of the bounced-back diagonals (hb_slip.cu)
     launch_curved(c, a.fout);  // curved-wall interpolation of the bounced-back links (hb_curved.cu)
-    if (a.mbb) launch_mbb_force(c, cur);
+    if (a.mbb && c->P.precision == HB_FP64) launch_mbb_force(c, cur);  // FP32/FP16: in the lattice kernel
 }
 
 void launch_lb_wallforce(hb_ctx* c, int cur) {
@@ -911,8 +911,8 @@ __global__ void k_mbb_relink_gs(MbbArgs m, InitArgs a, PerFaces pf, unsigned lon
     }
 }
 
-// Element force and torque (node::bounceBackForce, node.cpp:283-291): one block per
-// particle over its box; each fluid node's links into the particle contribute
+// Element force and torque of the FP64 form (node::bounceBackForce, node.cpp:283-291; the
+// FP32/FP16 forms sum them inside the lattice kernel): one block per particle over its box; each fluid node's links into the particle contribute
 // (2 (fs_j - w_j) - BBi) c_j with fs_j = f_out[opp j] + BBi recovered from the streamed
 // state and its moment about the element centre; the solid nodes count the volume.
 // Fixed node-to-thread assignment and a fixed tree: the sums are reproducible.
@@ -938,6 +938,7 @@ __global__ void __launch_bounds__(256) k_mbb_force(MbbArgs a) {
             if ((int)a.solid[i] == p) acc[6] += 1.0;
             continue;
         }
+        if (t & HB_BULK) continue;  // every link of a bulk node ends on a fluid node
         for (int j = 1; j < Q; ++j) {
             const int xl = x + cx(j), yl = y + cy(j), zl = z + cz(j);
             const long long l = (long long)xl + (long long)a.X * ((long long)yl + (long long)a.Y * zl);

@@ -47,28 +47,57 @@ __device__ __forceinline__ float cdot(int j, float vx, float vy, float vz) {
     return r;
 }
 
+// v * 2^38 rounded to a 64-bit integer, from 32-bit conversions only (a 64-bit float to
+// integer conversion issues on the narrow FP64 pipe of this part): a = |v| * 2^6 splits
+// into floor(a) (the high word) and the exact fraction times 2^32 (the low word,
+// < 2^32); the sign is applied to the 64-bit result.
+__device__ __forceinline__ unsigned long long to_fixed(float v) {
+    const float a = fabsf(v) * 64.0f;
+    const float h = floorf(a);
+    const unsigned long long m =
+        ((unsigned long long)__float2uint_rn(h) << 32) + __float2uint_rn((a - h) * 4294967296.0f);
+    return v < 0.0f ? 0ull - m : m;
+}
+
 // One post-collision population of a node with non-trivial links, the pull rules of
 // LB.cpp:1231-1356 seen from the sending node.  (A form with selected target index and
 // value, keeping the lanes of a warp converged, measured slower on GB300 than this
 // branch chain.)
-template <class P>
+template <class P, bool MBB>
 __device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fout, int x, int y, int z, int i,
-                                             int j, float g, float n, float ux, float uy, float uz, float usq) {
+                                             int j, float g, float n, float ux, float uy, float uz, float usq,
+                                             float* mv, int& mkey) {
     const int l = link32(a, x, y, z, j);
     const uint8_t tl = a.ntype[l];
     const uint8_t lc = tl & HB_TYPE_MASK;
     const int o = opp(j);
     const int N = (int)a.N;
-    if (a.mbb && (tl & HB_INSIDE) && (lc == HB_T_FLUID || lc == HB_T_INTERFACE)) {
+    if (MBB && (tl & HB_INSIDE) && (lc == HB_T_FLUID || lc == HB_T_INTERFACE)) {
         // moving bounce-back on a particle: BBi = 6 n w_j (u . c_j) with u the particle's
         // velocity at the solid node, from its FP32 record (centre, velocity, spin); no
-        // link wraps in this mode
-        const float4* pf4 = reinterpret_cast<const float4*>(a.parts.pf) + 3 * (size_t)a.solid[l];
+        // link wraps in this mode.  The link's momentum exchange (2 (fs_j - w_j) - BBi) c_j
+        // (g = fs_j - w_j) and its moment about the element centre go to the node's sums
+        // for its first particle, or straight to another particle's fixed-point sums.
+        const int pl = (int)a.solid[l];
+        const float4* pf4 = reinterpret_cast<const float4*>(a.parts.pf) + 3 * (size_t)pl;
         const float4 q0 = pf4[0], q1 = pf4[1], q2 = pf4[2];
         const float rx = float(x + cx(j)) - q0.x, ry = float(y + cy(j)) - q0.y, rz = float(z + cz(j)) - q0.z;
         const float wx = q1.z, wy = q1.w, wz = q2.x;
         const float vx = q0.w + (wy * rz - wz * ry), vy = q1.x + (wz * rx - wx * rz), vz = q1.y + (wx * ry - wy * rx);
-        P::store(fout + o * N + i, g - 6.0f * n * float(wgt(j)) * cdot(j, vx, vy, vz));
+        const float BBi = 6.0f * n * float(wgt(j)) * cdot(j, vx, vy, vz);
+        P::store(fout + o * N + i, g - BBi);
+        const float sc = 2.0f * g - BBi;
+        const float fx = float(cx(j)) * sc, fy = float(cy(j)) * sc, fz = float(cz(j)) * sc;
+        const float v6[6] = {fx, fy, fz, ry * fz - rz * fy, rz * fx - rx * fz, rx * fy - ry * fx};
+        if (mkey < 0) mkey = pl;
+        if (pl == mkey) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) mv[k] += v6[k];
+        } else {  // a second particle next to this node (rare)
+            const int E = a.parts.count;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) atomicAdd(a.hacc + (long long)k * E + pl, to_fixed(v6[k]));
+        }
     } else if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
         P::store(fout + j * N + l, g);
     } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN || lc == HB_T_CURVED) {
@@ -84,18 +113,6 @@ __device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fou
     } else {
         flag_status(a.status, 1);
     }
-}
-
-// v * 2^38 rounded to a 64-bit integer, from 32-bit conversions only (a 64-bit float to
-// integer conversion issues on the narrow FP64 pipe of this part): a = |v| * 2^6 splits
-// into floor(a) (the high word) and the exact fraction times 2^32 (the low word,
-// < 2^32); the sign is applied to the 64-bit result.
-__device__ __forceinline__ unsigned long long to_fixed(float v) {
-    const float a = fabsf(v) * 64.0f;
-    const float h = floorf(a);
-    const unsigned long long m =
-        ((unsigned long long)__float2uint_rn(h) << 32) + __float2uint_rn((a - h) * 4294967296.0f);
-    return v < 0.0f ? 0ull - m : m;
 }
 
 // FP64 node fields (read by the free surface, the wall force and downloads) are written
@@ -138,9 +155,9 @@ __device__ __forceinline__ void element_sums_warp(unsigned long long* hacc, int 
 // The update of one node from its 19 post-streaming deviations f: moments, coupling,
 // collision, push.  Every lane of a warp calls it (act false for lanes without an active
 // node), because the element sums use full-warp shuffles.
-template <class P>
+template <class P, bool MBB>
 __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, int i, uint8_t t, bool act,
-                                        float* f, int p, float4 q0, float4 q1, float4 q2) {
+                                        float* f, int p, float4 q0, float4 q1, float4 q2, float* mv, int& mkey) {
     using S = typename P::S;
     const int N = (int)a.N;
     S* fout = reinterpret_cast<S*>(a.fout);
@@ -161,7 +178,7 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
     if (!(n > 0.0f) || ux != ux || uy != uy || uz != uz) flag_status(a.status, 0);
 
     float hx = 0.0f, hy = 0.0f, hz = 0.0f;
-    if (a.couple) {
+    if (!MBB && a.couple) {
         int key = -1;
         float v[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (p >= 0) {  // LB.cpp:1863-1904 with FP32 particle copies
@@ -278,7 +295,8 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
     } else {
 #pragma unroll
         for (int j = 1; j < Q; ++j) {
-            if (special & (1u << j)) push_general<P>(a, fout, x, y, z, i, j, f[j], n, ux, uy, uz, usq);
+            if (special & (1u << j))
+                push_general<P, MBB>(a, fout, x, y, z, i, j, f[j], n, ux, uy, uz, usq, mv, mkey);
             else fo[(bb & (1u << j)) ? opp(j) * N : a.so[j]] = P::enc_store(f[j]);
         }
     }
@@ -287,7 +305,10 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
 // One thread per node, populations loaded straight from HBM.  Nine blocks of 128 per SM
 // (56 registers, no spills) measured faster than eight (64 registers) and ten (48, with
 // spills).
-template <class P>
+// MBB: moving bounce-back (nodes inside particles are solid; their links bounce back
+// with the particle's velocity and the momentum exchange builds the element sums); a
+// separate instantiation, so the direct-forcing kernel keeps its instruction count.
+template <class P, bool MBB>
 __global__ void __launch_bounds__(128, 9) k_collide_stream_dev(LBArgs a) {
     using S = typename P::S;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -297,8 +318,9 @@ __global__ void __launch_bounds__(128, 9) k_collide_stream_dev(LBArgs a) {
     const S* fin = reinterpret_cast<const S*>(a.fin);
     // whole warps leave together so that the element sums can use full-warp shuffles
     const uint8_t t = x < a.X ? a.ntype[i] : (uint8_t)HB_T_STATWALL;
-    const bool act = is_fluid(t, a.mbb);
-    if (!__any_sync(0xffffffffu, act)) return;
+    const bool act = MBB ? is_fluid(t, 1) : is_active(t);
+    const bool solidp = MBB && is_active(t) && (t & HB_INSIDE);  // counts its particle's volume
+    if (!__any_sync(0xffffffffu, act || solidp)) return;
     // the particle index of a particle node is loaded ahead of the populations and its
     // particle's FP32 record right after them, so their latencies overlap the populations'
     // instead of following the moments (0.092 -> 0.082 ms per coupled 128^3 launch)
@@ -311,14 +333,26 @@ __global__ void __launch_bounds__(128, 9) k_collide_stream_dev(LBArgs a) {
         const float4* pf4 = reinterpret_cast<const float4*>(a.parts.pf) + 3 * (size_t)p;
         q0 = pf4[0]; q1 = pf4[1]; q2 = pf4[2];
     }
-    lb_node<P>(a, x, y, z, i, t, act, f, p, q0, q1, q2);
+    float mv[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int mkey = -1;
+    if (MBB && solidp) {
+        mkey = (int)a.solid[i];
+        mv[6] = 1.0f;
+    }
+    lb_node<P, MBB>(a, x, y, z, i, t, act, f, p, q0, q1, q2, mv, mkey);
+    if (MBB) element_sums_warp(a.hacc, a.parts.count, mkey, mv);  // every lane of the warp
 }
 
 void launch_lb_step_dev(hb_ctx* c, const LBArgs& a) {
     const int b2 = c->X <= 64 ? 64 : 128;
     dim3 g2((unsigned)ceil_div(c->X, b2), (unsigned)(c->Y - 2), (unsigned)(c->Z - 2));
-    if (c->P.precision == HB_FP32) k_collide_stream_dev<PolF32><<<g2, b2, 0, c->stream>>>(a);
-    else k_collide_stream_dev<PolF16><<<g2, b2, 0, c->stream>>>(a);
+    if (a.mbb) {
+        if (c->P.precision == HB_FP32) k_collide_stream_dev<PolF32, true><<<g2, b2, 0, c->stream>>>(a);
+        else k_collide_stream_dev<PolF16, true><<<g2, b2, 0, c->stream>>>(a);
+    } else {
+        if (c->P.precision == HB_FP32) k_collide_stream_dev<PolF32, false><<<g2, b2, 0, c->stream>>>(a);
+        else k_collide_stream_dev<PolF16, false><<<g2, b2, 0, c->stream>>>(a);
+    }
 }
 
 }  // namespace hb

@@ -239,15 +239,15 @@ int hb_download_elements(hb_ctx* ctx, double* x0, double* x1, double* w, double*
                          double* mparticle, double* mwall, double* fluid_volume);
 /* The same download queued on the context stream behind the steps already issued; it
  * returns without waiting.  The arrays hold the values once hb_synchronize returns and
- * must stay valid until then.  Page-locked arrays (hb_host_register) are filled by
- * asynchronous copies, so a driver can issue step after step and read the element state
- * of each without stalling the device; pageable arrays are filled by the CUDA runtime's
- * synchronous path. */
+ * must stay valid until then.  Arrays registered with hb_host_register (page-locked and
+ * mapped) are written by the gather kernel itself, so a driver can issue step after step
+ * and read the element state of each without a copy or a stall; other arrays are filled
+ * by copies on the stream (pageable memory takes the CUDA runtime's synchronous path). */
 int hb_download_elements_async(hb_ctx* ctx, double* x0, double* x1, double* w, double* q0,
                                double* fhydro, double* mhydro, double* fparticle, double* fwall,
                                double* mparticle, double* mwall, double* fluid_volume);
-/* Page-locks (cudaHostRegister) / releases host memory the caller passes to the
- * asynchronous downloads. */
+/* Page-locks and maps (cudaHostRegister, mapped) / releases host memory the caller passes
+ * to the asynchronous downloads. */
 int hb_host_register(void* p, size_t bytes);
 int hb_host_unregister(void* p);
 /* Candidate pair list as sorted (min,max) pairs, like DEM::neighborTable

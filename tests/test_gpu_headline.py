@@ -9,8 +9,10 @@ the column) in FP64 against the oracle.
 Exact: node types, particle flags and the particle index of every particle node
 (LB.cpp:1921-2033), the candidate pair set (DEM.cpp:1369-1494), the overlapping pair
 set, the interface cell set.  FP64 populations and density to 1e-12 relative L-inf over
-the active nodes at every snapshot; velocity and element forces to 1e-12 / 1e-10 over
-the first 10 cycles.  Later the contact sums (added per particle in another order than
+the active nodes at every snapshot; velocity to 1e-12 after one cycle and 1e-11 after
+10 (relative to the largest velocity, ~1e-5 in this nearly still fluid, so that rounding
+of the populations weighs more in it), element forces to 1e-10 over the first 10
+cycles.  Later the contact sums (added per particle in another order than
 the reference's pair table, DEM.cpp:1668-1690, and the element force sums,
 LB.cpp:1897) seed rounding differences that the stiff multi-contact dynamics of a packed
 bed amplifies about 1.5-fold per cycle; after 30 cycles the velocity, whose scale in
@@ -86,7 +88,7 @@ def test_config2_fp64_vs_oracle_with_contacts(collision):
         ge, oe = g.elements(), o.elements()
         errs = {k: rel_linf(ge[k], oe[k]) for k in ("x0", "x1", "FHydro", "MHydro", "FParticle", "FWall")}
         print(tag, {k: f"{v:.2e}" for k, v in errs.items()})
-        _compare_lattice(g.lattice(), o.lattice(), 1e-12, tag, tol_u=1e-9 if late else 1e-12)
+        _compare_lattice(g.lattice(), o.lattice(), 1e-12, tag, tol_u=1e-9 if late else (1e-11 if step > 1 else 1e-12))
         np.testing.assert_array_equal(_pair_set(g.pairs()), _pair_set(o.pairs()), err_msg=tag)
         np.testing.assert_array_equal(_overlapping(ge["x0"], rad), _overlapping(oe["x0"], rad), err_msg=tag)
         for k, tol in (("x0", 1e-12), ("x1", 1e-9 if late else 1e-12), ("FHydro", 1e-8 if late else 1e-10),
