@@ -9,9 +9,11 @@ masks, fused collide+stream, element force reduction.
 
 value      MLUPS over the active nodes (inside-particle nodes included, as the
            reference counts activeNodes), device-resident, graph-replayed cycles.
-e2e        same metric through the C-ABI per step with host buffers: hb_cycle(1) plus
-           the host<->device copies a host driver makes every step (body force in,
-           element state and hydrodynamic forces out).
+e2e        same metric through the C-ABI per step with host buffers: hb_set_body_force
+           and hb_cycle(1) every step, the body force going in as graph kernel parameters
+           and the element state and hydrodynamic forces coming out into page-locked
+           mapped host arrays (hb_set_element_sink), timed until the last step's state
+           is on the host.
 roofline   the fused collide+stream kernel: algorithmic bytes per launch / its
            CUDA-event duration, against the measured HBM copy bandwidth.
 cpu_baseline  the CPU oracle (this repository's C++ restatement of the reference, the
@@ -368,42 +370,46 @@ def main():
         check(L.hb_cycle(g.h, 1))
     check(L.hb_synchronize(g.h))
     rep.barrier()
-    # device-resident timed windows of exactly K cycles each (inputs larger than L2:
-    # 2 x 19 x 2.1M x 4 B = 319 MB of populations); the median window is reported
+    # Timed windows of exactly K cycles, repeated until --min-cycles ran; the median
+    # window is reported.  Each device-resident window (inputs larger than L2:
+    # 2 x 19 x 2.1M x 4 B = 319 MB of populations) is followed by an end-to-end window of
+    # K steps through the C-ABI with host buffers, so both are measured at the same state
+    # of the settling suspension: every step the host sets the body force (24 B, carried
+    # into the cycle graph as kernel parameters) and runs one cycle, whose last kernel
+    # writes the element state a host driver reads (x0, x1, FHydro, MHydro) into
+    # page-locked mapped host arrays (hb_set_element_sink); an end-to-end window ends when
+    # the last step's state has landed on the host.
+    E = g.E
+    host = np.zeros((4, 3 * E))
+    check(L.hb_host_register(host.ctypes.data_as(C.c_void_p), host.nbytes))
+    force = np.array(p.lbF[:], dtype=np.float64)
+    ptr = [host[k].ctypes.data_as(C.c_void_p) for k in range(4)]
     windows = max(1, -(-args.min_cycles // args.steps))
-    per_step, per_lb = [], []
+    per_step, per_lb, e2e_step = [], [], []
     with Clocks(local) as clk:
         for _ in range(windows):
             ms_tot, ms_lb, kpc = g.time_cycles(args.steps)
             per_step.append(ms_tot / args.steps)
             per_lb.append(ms_lb)
-    check(L.hb_synchronize(g.h))
+            check(L.hb_set_element_sink(g.h, ptr[0], ptr[1], None, None, ptr[2], ptr[3],
+                                        None, None, None, None, None))
+            check(L.hb_synchronize(g.h))
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                check(L.hb_set_body_force(g.h, force.ctypes.data_as(C.c_void_p)))
+                check(L.hb_cycle(g.h, 1))
+            check(L.hb_synchronize(g.h))
+            e2e_step.append((time.perf_counter() - t0) / args.steps)
+            check(L.hb_set_element_sink(g.h, *([None] * 11)))
+    check(L.hb_host_unregister(host.ctypes.data_as(C.c_void_p)))
+    assert np.isfinite(host).all() and np.abs(host[2]).max() > 0.0
     k_med = int(np.argsort(per_step)[len(per_step) // 2])
     ms_step = rep.max(per_step[k_med])
     ms_lb = per_lb[k_med]
     value = rep.aggregate_rate(A, ms_step * 1e-3) / 1e6
-    # end to end through the C-ABI with host buffers: every step the body force goes in
-    # (24 B, as kernel arguments), the whole cycle runs, and the element state the host
-    # driver reads (x0, x1, FHydro, MHydro) comes back by asynchronous copies into
-    # page-locked host arrays; the region ends when the last copy has landed
-    E = g.E
-    host = np.zeros((4, 3 * E))
-    check(L.hb_host_register(host.ctypes.data_as(C.c_void_p), host.nbytes))
-    force = np.array(p.lbF[:], dtype=np.float64)
-    e2e_steps = max(3, args.steps)
-    ptr = [host[k].ctypes.data_as(C.c_void_p) for k in range(4)]
-    check(L.hb_synchronize(g.h))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        check(L.hb_set_body_force(g.h, force.ctypes.data_as(C.c_void_p)))
-        check(L.hb_cycle(g.h, 1))
-        check(L.hb_download_elements_async(g.h, ptr[0], ptr[1], None, None, ptr[2], ptr[3],
-                                           None, None, None, None, None))
-    check(L.hb_synchronize(g.h))
-    e2e_dt = rep.max(time.perf_counter() - t0)
-    check(L.hb_host_unregister(host.ctypes.data_as(C.c_void_p)))
-    assert np.isfinite(host).all() and np.abs(host[2]).max() > 0.0
-    e2e = rep.aggregate_rate(A * e2e_steps, e2e_dt) / 1e6
+    e2e_dt = rep.max(float(np.median(e2e_step)))
+    e2e = rep.aggregate_rate(A, e2e_dt) / 1e6
+    e2e_steps = args.steps * windows
     # roofline of the fused kernel
     peak, peak_kind = measured_peak()
     bytes_launch = A * B_LU[prec] + A_in * (4 + 3 * (8 if prec == abi.HB_FP64 else 4))
@@ -429,7 +435,8 @@ def main():
                    "window_ms_per_step": [round(v, 4) for v in per_step]},
         "gpu_launches": kpc * args.steps,
         "e2e": {"value": round(e2e, 2), "unit": "MLUPS", "h2d_bytes_per_step": 24,
-                "d2h_bytes_per_step": 4 * 3 * E * 8, "steps": e2e_steps},
+                "d2h_bytes_per_step": 4 * 3 * E * 8, "steps": e2e_steps,
+                "window_ms_per_step": [round(v * 1e3, 4) for v in e2e_step]},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                      "traffic": lattice_traffic(prec), "kernel": "k_collide_stream_dev" if prec != abi.HB_FP64 else "k_collide_stream", "kernel_ms": round(ms_lb, 5),

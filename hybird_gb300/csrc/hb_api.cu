@@ -353,7 +353,8 @@ int dem_init(hb_ctx* c, const hb_elements* e, const hb_objects* o) {
         (rc = dalloc(&d.contacts, 1)) || (rc = dalloc(&d.partial, hb::PARTIAL_CAP)) || (rc = dalloc(&d.done, 1)) ||
         (rc = dalloc(&d.wrec, 7 * Pl)) || (rc = dalloc(&d.orec, 7 * Pl * OBJ_CAP)) ||
         (rc = dalloc(&d.cyl_of, Pl)) ||
-        (rc = dalloc(&d.react, (size_t)3 * (MAX_WALLS + d.O))))
+        (rc = dalloc(&d.react, (size_t)3 * (MAX_WALLS + d.O))) ||
+        (!d.gen && (rc = dalloc(&d.npc, 4 * Pl * (size_t)d.nbr_cap))))
         return rc;
     CK(cudaMemset(d.react, 0, sizeof(double) * 3 * (MAX_WALLS + d.O)));
     CK(cudaMemset(d.wrec, 0, sizeof(double) * 7 * Pl));
@@ -437,9 +438,9 @@ int hb_destroy(hb_ctx* c) {
     if (c->graph2) cudaGraphDestroy(c->graph2);
     void* ptrs[] = {c->ntype, c->lmask, c->solid, c->fA, c->fB, c->mode, c->rho, c->u, c->hf, c->mass,
                     c->visc, c->dv, c->hacc, c->status, c->wall_part, c->wall_force, c->fs_force, c->fs_mass2,
-                    c->fs_cnt, c->fs_scal, c->fs_flag, c->fs_first, c->fs_part, c->lb_force, c->d_stage, c->d.pf, c->d.plain,
+                    c->fs_scal, c->fs_flag, c->fs_first, c->fs_parent, c->lb_force, c->d_stage, c->d.pf, c->d.plain,
                     c->d.base, c->d.alt, c->d.cell_of, c->d.cell_cnt, c->d.cell_start, c->d.cell_fill, c->d.cell_items,
-                    c->d.nbr, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
+                    c->d.nbr, c->d.npc, c->d.nbr_cnt, c->d.wall_of, c->d.obj, c->d.obj_cnt, c->d.scal, c->d.contacts,
                     c->d.partial, c->d.done, c->d.obj_x0, c->d.obj_x1, c->d.obj_r,
                     c->d.claim_list, c->d.claim_cnt, c->d.mask_done, c->d.pop_list, c->d.pop_cnt, c->d.pop_rho, c->d.boxes, c->d.gargs, c->d.wrec, c->d.orec, c->d.react,
                     c->io_linked, c->io_part, c->slip_list, c->slip_val, c->slip_mix, c->fs_ilist,
@@ -582,11 +583,14 @@ int hb_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside, con
     if (launch_upload_lattice(c, type, inside, solid, f, n, u, mass, visc))
         return seterr(HB_ERR_CUDA, "upload: %s", cudaGetErrorString(cudaGetLastError()));
     curved_remark(c);  // the uploaded node bytes carry no velocity-mirror bits
+    hb::fs_invalidate(c);  // new node types: the interface list is rebuilt at the next step
     CK(cudaStreamSynchronize(c->stream));
     return HB_OK;
 }
 
 }  // extern "C"
+
+static int enqueue_sink_gather(hb_ctx* c);
 
 // one whole cycle on the context stream, starting from population buffer `cur`
 static int enqueue_cycle(hb_ctx* c, int cur) {
@@ -599,10 +603,12 @@ static int enqueue_cycle(hb_ctx* c, int cur) {
     launch_lb_step(c, cur);
     if (c->has_dynwall) launch_lb_wallforce(c, cur);
     if (!c->P.force_field) cudaMemsetAsync(c->fs_force, 0, sizeof(double) * 3, c->stream);
+    if (c->sink_on && enqueue_sink_gather(c)) return -1;
     return 0;
 }
 
 static int build_graph(hb_ctx* c) {
+    hb::flush_body_force(c);  // the capture takes lbF from the parameters
     for (int k = 0; k < 2; ++k) {
         if (c->gexec[k]) { cudaGraphExecDestroy(c->gexec[k]); c->gexec[k] = nullptr; }
     }
@@ -617,6 +623,7 @@ static int build_graph(hb_ctx* c) {
             return seterr(HB_ERR_CUDA, "cycle capture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : cudaGetLastError()));
         CK(cudaGraphInstantiate(&c->gexec[k], g, 0));
         if (k == 0) c->graph = g; else c->graph2 = g;
+        c->mask_node[k] = hb::find_mask_node(g);
     }
     size_t nn = 0;
     CK(cudaGraphGetNodes(c->graph, nullptr, &nn));
@@ -668,13 +675,25 @@ __global__ void k_set_force(double* f, double fx, double fy, double fz) {
     float* ff = reinterpret_cast<float*>(f + 3);
     ff[0] = (float)fx; ff[1] = (float)fy; ff[2] = (float)fz; ff[3] = 0.0f;
 }
+
+// paths outside the cycle graphs (single phases, checkpoints, a new capture) read
+// lb_force itself: write it now when the graphs hold a newer lbF
+void flush_body_force(hb_ctx* c) {
+    if (!c->force_dirty) return;
+    k_set_force<<<1, 1, 0, c->stream>>>(c->lb_force, c->P.lbF[0], c->P.lbF[1], c->P.lbF[2]);
+    c->force_dirty = false;
+}
 }  // namespace hb
 
 static int run_cycles(hb_ctx* c, int n, bool last_mirror) {
     for (int s = 0; s < n; ++s) {
         const int m = (last_mirror && s == n - 1) ? 1 : 0;
-        CK(cudaMemsetAsync(c->mode, m, sizeof(int), c->stream));
+        if (m != c->mode_val) {
+            CK(cudaMemsetAsync(c->mode, m, sizeof(int), c->stream));
+            c->mode_val = m;
+        }
         CK(cudaGraphLaunch(c->gexec[c->cur], c->stream));
+        c->force_dirty = false;  // the graph's mask kernel wrote lb_force
         if (c->P.dem_solve && c->d.E > 0) c->dem_stepped = true;
         if (c->P.lb_solve) {
             c->cur ^= 1;
@@ -700,6 +719,7 @@ int hb_dem_step(hb_ctx* c) {
 
 int hb_fs_step(hb_ctx* c) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    hb::flush_body_force(c);
     if (c->P.free_surface) launch_fs_step(c, c->cur);
     CK(cudaGetLastError());
     return HB_OK;
@@ -716,7 +736,9 @@ int hb_coupling_step(hb_ctx* c) {
 
 int hb_lb_step(hb_ctx* c) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    hb::flush_body_force(c);
     CK(cudaMemsetAsync(c->mode, 1, sizeof(int), c->stream));
+    c->mode_val = 1;
     launch_lb_step(c, c->cur);
     if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
     if (!c->P.force_field) CK(cudaMemsetAsync(c->fs_force, 0, sizeof(double) * 3, c->stream));
@@ -747,7 +769,16 @@ int hb_get_params(hb_ctx* c, hb_params* out, int32_t* elements, int32_t* objects
 int hb_set_body_force(hb_ctx* c, const double* force) {
     if (!c || !force || !c->initialized) return seterr(HB_ERR_ARG, "null argument or not initialised");
     for (int k = 0; k < 3; ++k) c->P.lbF[k] = force[k];
-    if (c->P.force_field) hb::k_set_force<<<1, 1, 0, c->stream>>>(c->lb_force, force[0], force[1], force[2]);
+    if (!c->P.force_field) return HB_OK;
+    if (c->mask_node[0] && c->mask_node[1]) {
+        // the cycle graphs' mask kernel writes it before the lattice step: no launch of its
+        // own between two cycles
+        if (hb::update_mask_force(c)) return seterr(HB_ERR_CUDA, "graph update: %s", cudaGetErrorString(cudaGetLastError()));
+        c->force_dirty = true;
+        return HB_OK;
+    }
+    hb::k_set_force<<<1, 1, 0, c->stream>>>(c->lb_force, force[0], force[1], force[2]);
+    CK(cudaGetLastError());
     return HB_OK;
 }
 
@@ -830,6 +861,8 @@ struct ElemItem {
 };
 constexpr int kElemItems = 11;
 
+int ensure_stage(hb_ctx* c);
+
 int enqueue_element_gather(hb_ctx* c, double* const dst[kElemItems], ElemItem items[kElemItems], hb::GatherArgs* g,
                            double* const* alias = nullptr) {
     const int E = c->d.E;
@@ -841,11 +874,8 @@ int enqueue_element_gather(hb_ctx* c, double* const dst[kElemItems], ElemItem it
         {dst[6], c->d.FP, 3, -1}, {dst[7], c->d.FW, 3, -1}, {dst[8], c->d.MP, 3, -1},
         {dst[9], c->d.MW, 3, -1}, {dst[10], c->d.fvol, 1, inline_sums ? 6 : -1}};
     for (int k = 0; k < kElemItems; ++k) items[k] = all[k];
-    if (!c->d_stage) {
-        int rc = dalloc(&c->d_stage, (size_t)hb::STAGE_DOUBLES_PER_ELEMENT * E);
-        if (rc) return rc;
-        CK(cudaMallocHost((void**)&c->h_stage, sizeof(double) * hb::STAGE_DOUBLES_PER_ELEMENT * E));
-    }
+    int rc = ensure_stage(c);
+    if (rc) return rc;
     *g = hb::GatherArgs{};
     g->E = E;
     g->hacc = c->hacc;
@@ -864,6 +894,15 @@ int enqueue_element_gather(hb_ctx* c, double* const dst[kElemItems], ElemItem it
     return HB_OK;
 }
 
+int ensure_stage(hb_ctx* c) {
+    if (c->d_stage) return HB_OK;
+    const int E = c->d.E;
+    int rc = dalloc(&c->d_stage, (size_t)hb::STAGE_DOUBLES_PER_ELEMENT * E);
+    if (rc) return rc;
+    CK(cudaMallocHost((void**)&c->h_stage, sizeof(double) * hb::STAGE_DOUBLES_PER_ELEMENT * E));
+    return HB_OK;
+}
+
 // device address of a host array the GPU can write directly (page-locked and mapped, as
 // hb_host_register makes it), or null
 double* mapped_alias(double* p) {
@@ -876,7 +915,43 @@ double* mapped_alias(double* p) {
 }
 }  // namespace
 
+// The element sink at the end of a captured cycle: the lattice step's element sums are
+// pending there (FP32/FP16 forms read them from the fixed-point accumulators, the FP64
+// form reduces them first, as a download would).
+static int enqueue_sink_gather(hb_ctx* c) {
+    const bool pending = c->reduce_pending;
+    c->reduce_pending = c->P.lb_solve && sums_lag(c);
+    ElemItem items[kElemItems];
+    hb::GatherArgs g;
+    const int rc = enqueue_element_gather(c, c->sink, items, &g, c->sink);
+    c->reduce_pending = pending;
+    return rc;
+}
+
 extern "C" {
+
+int hb_set_element_sink(hb_ctx* c, double* x0, double* x1, double* w, double* q0, double* fhydro, double* mhydro,
+                        double* fparticle, double* fwall, double* mparticle, double* mwall, double* fluid_volume) {
+    if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    double* const dst[kElemItems] = {x0, x1, w, q0, fhydro, mhydro, fparticle, fwall, mparticle, mwall, fluid_volume};
+    double* alias[kElemItems] = {};
+    bool any = false;
+    for (int k = 0; k < kElemItems; ++k) {
+        if (!dst[k]) continue;
+        if (!(alias[k] = mapped_alias(dst[k])))
+            return seterr(HB_ERR_ARG, "sink array %d is not page-locked and mapped (hb_host_register)", k);
+        any = true;
+    }
+    if (any && c->d.E == 0) return seterr(HB_ERR_STATE, "no elements");
+    if (any) {
+        int rc = ensure_stage(c);
+        if (rc) return rc;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < kElemItems; ++k) c->sink[k] = alias[k];
+    c->sink_on = any;
+    return build_graph(c);
+}
 
 int hb_download_elements(hb_ctx* c, double* x0, double* x1, double* w, double* q0, double* fhydro, double* mhydro,
                          double* fparticle, double* fwall, double* mparticle, double* mwall, double* fluid_volume) {
@@ -1259,9 +1334,11 @@ int hb_time_cycles(hb_ctx* c, int32_t nsteps, float* ms_total, float* ms_lb_kern
     CK(cudaStreamSynchronize(c->stream));
     // whole cycles replayed from the graphs
     CK(cudaMemsetAsync(c->mode, 0, sizeof(int), c->stream));
+    c->mode_val = 0;
     CK(cudaEventRecord(c->ev0, c->stream));
     for (int s = 0; s < nsteps; ++s) {
         CK(cudaGraphLaunch(c->gexec[c->cur], c->stream));
+        c->force_dirty = false;
         if (c->P.lb_solve) { c->cur ^= 1; c->reduce_pending = sums_lag(c); }
         ++c->steps;
     }

@@ -28,7 +28,7 @@
 namespace {
 
 constexpr char MAGIC[8] = {'H', 'B', 'C', 'K', 'P', 'T', '0', '1'};
-constexpr uint32_t VERSION = 1;
+constexpr uint32_t VERSION = 2;
 
 struct Buf {
     const char* name;
@@ -65,15 +65,11 @@ std::vector<Buf> state_buffers(hb_ctx* c) {
     add("wall_force", c->wall_force, sizeof(double) * (hb::MAX_WALLS * 3 + 1));
     add("fs_force", c->fs_force, sizeof(double) * 3);
     add("lb_force", c->lb_force, sizeof(double) * 5);
-    if (c->fs_flag) {
-        size_t part = 0, cnt = 0;
-        hb::fs_buffer_bytes(c, &part, &cnt);
-        add("fs_scal", c->fs_scal, sizeof(double) * 2);
+    if (c->fs_flag) {  // the interface list itself is rebuilt from the node bytes after a load
+        add("fs_scal", c->fs_scal, sizeof(double) * 3);
         add("fs_flag", c->fs_flag, N);
         add("fs_mass2", c->fs_mass2, 8 * N);
-        add("fs_part", c->fs_part, part);
-        add("fs_cnt", c->fs_cnt, cnt);
-        add("fs_first", c->fs_first, 6 * sizeof(int));
+        add("fs_first", c->fs_first, hb::fs_count_bytes());
     }
     hb_dem_dev& d = c->d;
     const size_t E = (size_t)d.E;
@@ -103,6 +99,7 @@ std::vector<Buf> state_buffers(hb_ctx* c) {
             add("dem_size", d.esize, 4 * E);
         }
         add("nbr", d.nbr, 4 * Pl * d.nbr_cap);
+        add("nbr_pair_constants", d.npc, 8 * 4 * Pl * d.nbr_cap);
         add("nbr_cnt", d.nbr_cnt, 4 * Pl);
         add("wall_of", d.wall_of, 4 * Pl);
         add("obj", d.obj, 4 * Pl * hb::OBJ_CAP);
@@ -136,6 +133,7 @@ extern "C" {
 
 int hb_checkpoint_save(hb_ctx* c, const char* path) {
     if (!c || !path || !c->initialized) return err(HB_ERR_ARG, "null argument or not initialised");
+    hb::flush_body_force(c);  // the saved lb_force is the current lbF
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return err(HB_ERR_CUDA, "stream synchronize failed");
     std::ofstream f(path, std::ios::binary);
     if (!f) return err(HB_ERR_ARG, std::string("cannot open ") + path);
@@ -163,6 +161,7 @@ int hb_checkpoint_save(hb_ctx* c, const char* path) {
         host.resize(b.bytes);
         if (cudaMemcpy(host.data(), b.ptr, b.bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
             return err(HB_ERR_CUDA, std::string("checkpoint read of ") + b.name);
+        if (b.ptr == c->fs_first) hb::fs_count_for_file(host.data());
         f.write(nm, 24);
         f.write(reinterpret_cast<const char*>(&n), 8);
         f.write(host.data(), (std::streamsize)b.bytes);
@@ -271,6 +270,7 @@ int hb_checkpoint_load(const char* path, hb_ctx** out) {
             return err(HB_ERR_CUDA, std::string("checkpoint restore of ") + b.name);
         }
     }
+    hb::fs_invalidate(c);
     c->steps = h.steps;
     c->reduce_pending = h.reduce_pending != 0;
     c->dem_stepped = h.dem_stepped != 0;

@@ -35,6 +35,8 @@ struct hb_dem_dev {             // element state, FP64, component-major [3E] / [
     int* cell_fill = nullptr;   // [nc]
     int* cell_items = nullptr;  // [E + gcap]
     int* nbr = nullptr;         // [E*nbr_cap]
+    double* npc = nullptr;      // [4*E*nbr_cap] per candidate pair (single spheres): effMass,
+                                // effRad and the linear model's two damping coefficients
     int nbr_cap = hb::NBR_CAP;  // candidate partners kept per particle
     int* nbr_cnt = nullptr;     // [E]
     int* wall_of = nullptr;     // [E] first wall in range or -1
@@ -146,11 +148,11 @@ struct hb_ctx {
     double* fs_scal = nullptr;      // [0]=surplus [1]=interface count as double
     uint8_t* fs_flag = nullptr;     // per-node conversion flags of the current step
     double* fs_mass2 = nullptr;     // new interface masses (updateMass reads the old ones)
-    double* fs_part = nullptr;      // per-block FP64 partials for the surplus ledger
-    int* fs_cnt = nullptr;          // per-block interface counts
-    int* fs_first = nullptr;        // [6] 1 until the first free-surface step has run; counters
-    uint32_t* fs_ilist = nullptr;   // [fs_icap] interface cells at the start of a step
-    long long fs_icap = 0;          // its capacity (hb_params.cap_interface, 0: every node)
+    int* fs_first = nullptr;        // 64-byte step state of the free surface (first-step flag,
+                                    // list selector and counts, 128-bit surplus ledger)
+    uint32_t* fs_ilist = nullptr;   // [4 fs_icap] two interface lists, conversion list, new cells
+    uint32_t* fs_parent = nullptr;  // [N] claim slots of the new interface cells (zero between steps)
+    long long fs_icap = 0;          // list capacity (hb_params.cap_interface, 0: every node)
     // cylinders and curved walls (hb_curved.cu)
     std::vector<hb_cyl_host> cyl;
     void* curved_list = nullptr;
@@ -167,6 +169,13 @@ struct hb_ctx {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // cycle graphs starting from fA / fB
     cudaGraph_t graph2 = nullptr;
+    cudaGraphNode_t mask_node[2] = {nullptr, nullptr};  // the mask kernel in graph / graph2 (carries lbF)
+    bool force_dirty = false;    // lbF changed through the graphs' nodes, lb_force not yet written
+    int mode_val = -1;           // value last written to *mode (-1: unknown)
+    // element sink (hb_set_element_sink): device aliases of mapped host arrays the cycle
+    // graphs fill at the end of every cycle, in the order of hb_download_elements
+    double* sink[11] = {};
+    bool sink_on = false;
     bool reduce_pending = false; // element forces lag the last lattice step
     int kernels_per_cycle = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -188,6 +197,9 @@ int launch_download_lattice(hb_ctx* c, double* f_dev, int which_parity);
 int launch_ghosts_init(hb_ctx* c);
 int launch_cycle_coop(hb_ctx* c, int do_reduce, int do_dem, int do_boxes, unsigned long long* ts = nullptr);
 void launch_couple(hb_ctx* c, bool build_boxes, int cur, cudaEvent_t* ev = nullptr);
+cudaGraphNode_t find_mask_node(cudaGraph_t g);
+int update_mask_force(hb_ctx* c);
+void flush_body_force(hb_ctx* c);  // write lb_force now if the graphs hold a newer lbF
 // moving bounce-back (hb_lb.cu): refill of uncovered nodes and link masks after the
 // coupling masks; element force and torque after the lattice step
 void launch_mbb_nodes(hb_ctx* c, int cur);
@@ -196,7 +208,9 @@ void launch_dem_first_predict(hb_ctx* c);
 void launch_couple_reduce(hb_ctx* c);
 void launch_reactions(hb_ctx* c);
 int set_error(int code, const char* msg);  // hb_last_error text, returns code
-void fs_buffer_bytes(const hb_ctx* c, size_t* part, size_t* cnt);
+size_t fs_count_bytes();
+void fs_invalidate(hb_ctx* c);  // rebuild the interface list from the node bytes at the next step
+void fs_count_for_file(void* rec);  // the step state as a checkpoint holds it (no list)
 // curved walls (hb_curved.cu)
 void launch_init_cylinders(hb_ctx* c);
 int curved_init(hb_ctx* c);

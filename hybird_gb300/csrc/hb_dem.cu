@@ -17,6 +17,7 @@
 // Coupling: one CTA per particle (grid-stride) sweeps the particle's bounding box.
 #include <cooperative_groups.h>
 #include <cstdio>
+#include <vector>
 
 #include "hb_common.cuh"
 #include "hb_ctx.h"
@@ -46,6 +47,7 @@ struct DemArgs {
     const int* plain;  // 1: orientation fixed at identity (no quaternion rates)
     int *cell_of, *cell_cnt, *cell_start, *cell_fill, *cell_items;
     int *nbr, *nbr_cnt, *wall_of, *obj, *obj_cnt;
+    double* npc;          // [4 E nbr_cap] constants of each candidate pair (single spheres)
     int nbr_cap;          // candidate partners kept per particle (hb_params.cap_neighbors)
     double *wrec, *orec;  // wall / object contact records of the current substep (7 doubles each)
     int* cyl_of;          // [E] first cylinder in range or -1 (DEM.cpp:1535-1550)
@@ -230,6 +232,24 @@ __device__ __noinline__ void nl_near_one(const DemArgs& a, int i);
 
 // candidate list of every particle: all others within nebrRange in the 27 adjacent
 // cells, then the walls, cylinder and objects in range
+// The constants of candidate pair (i, j) in slot k of i's list, computed once per
+// neighbour rebuild with the expressions particleParticleCollision evaluates at every
+// contact (DEM.cpp:1801-1900, 2153-2222): effMass = mI mJ / (mI + mJ), effRad =
+// rI rJ / (rI + rJ), and for the linear model the normal and tangential damping
+// coefficients 2 damp sqrt(kn effMass), 2 viscTang sqrt(effMass kn).  Products and sums
+// are commutative in IEEE arithmetic, so the values are those of the I = min(i, j)
+// evaluation bit for bit; the contacts then take no FP64 division or square root for them.
+__device__ __forceinline__ void pair_constants(const DemArgs& a, int i, int j, int k) {
+    const long long st = (long long)a.E * a.nbr_cap, o = (long long)i * a.nbr_cap + k;
+    const int I = min(i, j), J = max(i, j);
+    const double mI = a.m[I], mJ = a.m[J], rI = a.rad[I], rJ = a.rad[J];
+    const double effMass = mI * mJ / (mI + mJ);
+    a.npc[o] = effMass;
+    a.npc[st + o] = rI * rJ / (rI + rJ);
+    a.npc[2 * st + o] = a.model == HB_HERTZIAN ? 0.0 : 2.0 * a.damp * sqrt(a.kn * effMass);
+    a.npc[3 * st + o] = a.model == HB_HERTZIAN ? 0.0 : 2.0 * a.viscTang * sqrt(effMass * a.kn);
+}
+
 __device__ __noinline__ void nl_build_one(const DemArgs& a, int i) {
     const int E = a.E;
     const V xi = ld3(a.x0, E, i);
@@ -249,7 +269,10 @@ __device__ __noinline__ void nl_build_one(const DemArgs& a, int i) {
                         if (j == i) continue;
                         const V d = sub(ld3(a.x0, E, j), xi);
                         if (nrm2(d) < r2) {
-                            if (cnt < a.nbr_cap) a.nbr[(long long)i * a.nbr_cap + cnt] = j;
+                            if (cnt < a.nbr_cap) {
+                                a.nbr[(long long)i * a.nbr_cap + cnt] = j;
+                                if (a.npc) pair_constants(a, i, j, cnt);
+                            }
                             ++cnt;
                         }
                     }
@@ -510,19 +533,23 @@ struct FM {
 };
 
 // particleParticleCollision with I = lower index (DEM.cpp:1801-1900), seen by particle i
+// slot: the pair's constants (pair_constants), stride apart
 __device__ __noinline__ FM pp_contact(const DemArgs& a, int i, int I, int J, V vd, double rI, double rJ, V FP,
-                                      V MP, PredBuf pb) {
+                                      V MP, PredBuf pb, const double* slot) {
     const int E = a.E, eI = I, eJ = J;
+    const long long st = (long long)a.E * a.nbr_cap;
     const double dist = sqrt(nrm2(vd));
     const double overlap = rI + rJ - dist;
     const V relVel = sub(ld3(pb.x1r, E, eJ), ld3(pb.x1r, E, eI));
     const V en = divs(vd, dist);
     const double vn = dot(relVel, en);
     const V nrv = mul(vn, en);
-    const double mI = a.m[eI], mJ = a.m[eJ];
-    const double effMass = mI * mJ / (mI + mJ);
-    const double effRad = rI * rJ / (rI + rJ);
-    const double fn = normal_contact(a, overlap, vn, effRad, effMass);
+    const double effMass = slot[0];
+    const double effRad = slot[st];
+    const bool lin = a.model != HB_HERTZIAN;
+    // the linear model's damping coefficients come from the slot (the same expressions)
+    const double fn = lin ? fmax(a.kn * overlap + (-slot[2 * st] * vn), 0.0)
+                          : normal_contact(a, overlap, vn, effRad, effMass);
     const V nf = mul(fn, en);
     const V vrI = mul(rI, en), vrJ = mul(-rJ, en);
     const V rvc = add(sub(relVel, cross(ld3(pb.wGr, E, eI), vrI)), cross(ld3(pb.wGr, E, eJ), vrJ));
@@ -531,7 +558,8 @@ __device__ __noinline__ FM pp_contact(const DemArgs& a, int i, int I, int J, V v
     V tf{0, 0, 0};
     const bool hasT = nt != 0.0;
     if (hasT) {
-        const double ft = tangential_contact(a, nt, fn, effRad, effMass, a.muPart);
+        const double ft = lin ? fmin(slot[3 * st] * nt, a.muPart * fn)
+                              : tangential_contact(a, nt, fn, effRad, effMass, a.muPart);
         tf = mul(ft, divs(tang, nt));
     }
     if (i == I) {
@@ -668,7 +696,7 @@ __device__ __forceinline__ void forces_group(const DemArgs& a, const DemArgs& ga
             if (!(nrm2(vd) < sig * sig)) continue;
             if (i < j) ++ncont;
             contrib = true;
-            const FM r = pp_contact(ga, i, I, J, vd, rI, rJ, FP, MP, pb);
+            const FM r = pp_contact(ga, i, I, J, vd, rI, rJ, FP, MP, pb, a.npc + (long long)i * a.nbr_cap + k);
             FP = r.f;
             MP = r.m;
         }
@@ -1259,6 +1287,12 @@ struct CoupleArgs {
     const int *gorig, *pkey, *efirst, *ecomp, *eccnt;
     const double *gvec, *px, *pcen;
     uint32_t* remark;
+    // the body force of the coming lattice step: the mask kernel writes force[] (and its
+    // FP32 copy) into lb_force when set_force, so that a cycle graph takes a new force
+    // through an update of this kernel node's parameters
+    double* lb_force;
+    double force[3];
+    int set_force;
 };
 
 // centre and radius of particle p (the element itself, or on the per-particle path the
@@ -1418,13 +1452,15 @@ __device__ __noinline__ void mbb_pop(const CoupleArgs& a, long long l) {
 }
 
 // one node with the reference's full link rules (periodic remap, self-linked boundary)
-__device__ __noinline__ void mask_node_general(const CoupleArgs& a, int x, int y, int z) {
+__device__ __noinline__ bool mask_node_general(const CoupleArgs& a, int x, int y, int z) {
     const long long l = (long long)x + (long long)a.X * ((long long)y + (long long)a.Y * z);
     const uint8_t t = a.ntype[l];
+    bool wrote = false;
     if (t & HB_INSIDE) {
-        if (cover_first(a, a.solid[l], x, y, z) >= 0) return;  // stays
-        a.ntype[l] = t & ~HB_INSIDE;                           // pop
+        if (cover_first(a, a.solid[l], x, y, z) >= 0) return false;  // stays
+        a.ntype[l] = t & ~HB_INSIDE;                                 // pop
         if (a.mbb) mbb_pop(a, l);
+        wrote = true;
     }
     unsigned long long best = ~0ull;
     for (int kk = 1; kk <= 6; ++kk) {  // source m with link d[m][kk] == l
@@ -1450,6 +1486,7 @@ __device__ __noinline__ void mask_node_general(const CoupleArgs& a, int x, int y
         if (key < best) best = key;
     }
     if (best != ~0ull) claim_push(a, l, best);
+    return wrote || best != ~0ull;
 }
 
 __device__ __forceinline__ uint8_t byte_of(uint32_t w, int k) { return (uint8_t)(w >> (8 * k)); }
@@ -1458,7 +1495,7 @@ __device__ __forceinline__ uint8_t byte_of(uint32_t w, int k) { return (uint8_t)
 // (x-1, x+1, y-1, y+1, z-1, z+1) carry the particle flag where bit kk of tm is set: the
 // particle q of each flagged source m, the lowest (m, q) among those where q still covers
 // m and covers l (findNewSolid, LB.cpp:1969-2033)
-__device__ __forceinline__ void claim_node(const CoupleArgs& a, int x, int y, int z, long long l, unsigned tm) {
+__device__ __forceinline__ bool claim_node(const CoupleArgs& a, int x, int y, int z, long long l, unsigned tm) {
     const long long sy = a.X, sz = (long long)a.X * a.Y;
     const long long ms[6] = {l - 1, l + 1, l - sy, l + sy, l - sz, l + sz};
     // the sources' particles in one round of independent loads (own index for
@@ -1475,7 +1512,7 @@ __device__ __forceinline__ void claim_node(const CoupleArgs& a, int x, int y, in
             else if (qs[kk] != q0) several = true;
         }
     const bool cov0 = in_sph(a.tab[q0].s, x, y, z);
-    if (!cov0 && !several) return;  // just outside its particle: the common case
+    if (!cov0 && !several) return false;  // just outside its particle: the common case
     unsigned long long best = ~0ull;
 #pragma unroll
     for (int kk = 0; kk < 6; ++kk) {
@@ -1488,16 +1525,18 @@ __device__ __forceinline__ void claim_node(const CoupleArgs& a, int x, int y, in
         if (key < best) best = key;
     }
     if (best != ~0ull) claim_push(a, l, best);
+    return best != ~0ull;
 }
 
 // The claimed nodes join their particles once every block of the mask pass has decided:
-// the last block to finish (a counter of finished blocks, each publishing its claims
-// first) applies the list, so no node claimed in the pass acted as a source in it.
-__device__ __forceinline__ void commit_when_last(const CoupleArgs& a) {
+// the last block to finish (a counter of finished blocks, each publishing its pops and
+// claims first: a fence by every thread that wrote, then the block barrier) applies the
+// list, so no node claimed in the pass acted as a source in it.
+__device__ __forceinline__ void commit_when_last(const CoupleArgs& a, bool wrote) {
     __shared__ bool s_last;
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const int nthreads = blockDim.x * blockDim.y;
-    __threadfence();
+    if (wrote) __threadfence();
     __syncthreads();
     if (tid == 0) {
         const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
@@ -1533,13 +1572,19 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
     const unsigned lt = (1u << lane) - 1u;
     const int x0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
+    if (a.set_force && (blockIdx.x | blockIdx.y | blockIdx.z | threadIdx.x | threadIdx.y) == 0) {
+        a.lb_force[0] = a.force[0]; a.lb_force[1] = a.force[1]; a.lb_force[2] = a.force[2];
+        float* ff = reinterpret_cast<float*>(a.lb_force + 3);
+        ff[0] = (float)a.force[0]; ff[1] = (float)a.force[1]; ff[2] = (float)a.force[2]; ff[3] = 0.0f;
+    }
     const bool valid = x0 < a.X && y < a.Y;
     const bool pnear = ((a.per[0] | a.per[1]) && (x0 < 2 || x0 + 3 > a.X - 3)) ||
                        ((a.per[2] | a.per[3]) && (y < 2 || y > a.Y - 3)) ||
                        ((a.per[4] | a.per[5]) && (z < 2 || z > a.Z - 3));
     const bool general = valid && ((a.X & 3) || pnear || a.ghosts);
+    bool wrote = false;  // a pop or a claim of this thread, published before the commit
     if (general)
-        for (int k = 0; k < 4 && x0 + k < a.X; ++k) mask_node_general(a, x0 + k, y, z);
+        for (int k = 0; k < 4 && x0 + k < a.X; ++k) wrote |= mask_node_general(a, x0 + k, y, z);
     const bool fast = valid && !general;
     // without a periodic face nearby every link is plain arithmetic: a source is the
     // interior node one step back, and its forward link lands here
@@ -1563,24 +1608,32 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
             sl[0] = v.x; sl[1] = v.y; sl[2] = v.z; sl[3] = v.w;
         }
     }
+    // Source flags of the four nodes at once, in kk order (x-1, x+1, y-1, y+1, z-1, z+1):
+    // the particle bit (0x10) of every byte of the six neighbour words moved to bits 0-5
+    // of the node's byte.  A source along x must be an interior node of an interior row;
+    // the y and z sources count for interior nodes x (their words are 0 where the source
+    // row is not interior).
+    static_assert(HB_INSIDE == 0x10, "the shifts below move bit 4 of each byte");
+    const uint32_t IN4 = 0x01010101u * HB_INSIDE;
+    uint32_t m0 = 0u, m1 = 0u, mx = 0u;  // 0xFF in the bytes where each kind of source counts
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int x = x0 + k;
+        if (x - 1 >= 1) m0 |= 0xFFu << (8 * k);
+        if (x + 1 <= a.X - 2) m1 |= 0xFFu << (8 * k);
+        if (x >= 1 && x <= a.X - 2) mx |= 0xFFu << (8 * k);
+    }
+    const uint32_t wxm = (iy && iz) ? ((tw << 8) | tl) & m0 : 0u;
+    const uint32_t wxp = (iy && iz) ? ((tw >> 8) | ((uint32_t)tr << 24)) & m1 : 0u;
+    const uint32_t nb = ((wxm & IN4) >> 4) | ((wxp & IN4) >> 3) | ((wym & mx & IN4) >> 2) |
+                        ((wyp & mx & IN4) >> 1) | (wzm & mx & IN4) | ((wzp & mx & IN4) << 1);
     // queue the four nodes of every lane (ballots give each item its slot)
     int np = 0, nc = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int x = x0 + k;
         const uint8_t t = byte_of(tw, k);
-        const bool ix = x >= 1 && x <= a.X - 2;
-        // source flags in kk order: x-1, x+1, y-1, y+1, z-1, z+1
-        uint8_t tm[6];
-        tm[0] = (x - 1 >= 1 && iy && iz) ? (k > 0 ? byte_of(tw, k - 1) : tl) : (uint8_t)0;
-        tm[1] = (x + 1 <= a.X - 2 && iy && iz) ? (k < 3 ? byte_of(tw, k + 1) : tr) : (uint8_t)0;
-        tm[2] = ix ? byte_of(wym, k) : (uint8_t)0;
-        tm[3] = ix ? byte_of(wyp, k) : (uint8_t)0;
-        tm[4] = ix ? byte_of(wzm, k) : (uint8_t)0;
-        tm[5] = ix ? byte_of(wzp, k) : (uint8_t)0;
-        unsigned bits = 0u;
-#pragma unroll
-        for (int kk = 0; kk < 6; ++kk) bits |= ((tm[kk] & HB_INSIDE) ? 1u : 0u) << kk;
+        const unsigned bits = (nb >> (8 * k)) & 0x3Fu;
         const bool pc = fast && (t & HB_INSIDE);
         const unsigned bp = __ballot_sync(full, pc);
         if (pc) {
@@ -1609,6 +1662,7 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
                 a.ntype[l] = (uint8_t)((item >> 16) & 0xFFu) & ~HB_INSIDE;  // pop
                 if (a.mbb) mbb_pop(a, l);
                 join = (item >> 24) != 0u;
+                wrote = true;
             }
         }
         const unsigned bj = __ballot_sync(full, join);
@@ -1620,9 +1674,9 @@ __global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
     for (int q = lane; q < nc; q += 32) {
         const uint32_t item = s_claim[w][q];
         const int x = (int)(item & 0xFFFFu);
-        claim_node(a, x, y, z, l0 - x0 + x, item >> 16);
+        wrote |= claim_node(a, x, y, z, l0 - x0 + x, item >> 16);
     }
-    commit_when_last(a);
+    commit_when_last(a, wrote);
 }
 
 // element hydrodynamic force, torque and entrained fluid (LB.cpp:1853-1918): fixed
@@ -2034,7 +2088,7 @@ static DemArgs dem_args(hb_ctx* c) {
     a.plain = d.plain;
     a.cell_of = d.cell_of; a.cell_cnt = d.cell_cnt; a.cell_start = d.cell_start;
     a.cell_fill = d.cell_fill; a.cell_items = d.cell_items;
-    a.nbr = d.nbr; a.nbr_cnt = d.nbr_cnt; a.nbr_cap = d.nbr_cap; a.wall_of = d.wall_of; a.obj = d.obj; a.obj_cnt = d.obj_cnt;
+    a.nbr = d.nbr; a.npc = d.npc; a.nbr_cnt = d.nbr_cnt; a.nbr_cap = d.nbr_cap; a.wall_of = d.wall_of; a.obj = d.obj; a.obj_cnt = d.obj_cnt;
     a.wrec = d.wrec; a.orec = d.orec;
     a.cyl_of = d.cyl_of;
     a.ncyl = (int)std::min<size_t>(c->cyl.size(), DEM_MAX_CYL);
@@ -2151,7 +2205,42 @@ static CoupleArgs couple_args(hb_ctx* c) {
     a.ecomp = c->d.ecomp; a.eccnt = c->d.eccnt;
     a.gvec = c->d.gvec; a.px = c->d.px; a.pcen = c->d.pcen;
     a.remark = c->d.remark;
+    a.lb_force = c->lb_force;
+    for (int k = 0; k < 3; ++k) a.force[k] = c->P.lbF[k];
+    a.set_force = (c->P.force_field && c->lb_force) ? 1 : 0;
     return a;
+}
+
+// the mask kernel's node in a captured cycle graph, or null
+cudaGraphNode_t find_mask_node(cudaGraph_t g) {
+    size_t n = 0;
+    if (!g || cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return nullptr;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return nullptr;
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams kp;
+        if (cudaGraphKernelNodeGetParams(nd, &kp) == cudaSuccess && kp.func == reinterpret_cast<void*>(k_mask))
+            return nd;
+    }
+    return nullptr;
+}
+
+// the current body force into both cycle graphs: the mask kernel node's captured
+// arguments with force[] replaced (launches already enqueued keep theirs)
+int update_mask_force(hb_ctx* c) {
+    for (int k = 0; k < 2; ++k) {
+        cudaKernelNodeParams kp;
+        if (cudaGraphKernelNodeGetParams(c->mask_node[k], &kp) != cudaSuccess) return -1;
+        CoupleArgs a = *static_cast<const CoupleArgs*>(kp.kernelParams[0]);
+        for (int q = 0; q < 3; ++q) a.force[q] = c->P.lbF[q];
+        void* args[1] = {&a};
+        kp.kernelParams = args;
+        kp.extra = nullptr;
+        if (cudaGraphExecKernelNodeSetParams(c->gexec[k], c->mask_node[k], &kp) != cudaSuccess) return -1;
+    }
+    return 0;
 }
 
 // per-particle path at init: the particles, the ghosts of the initial positions

@@ -1,24 +1,28 @@
 // hb_fs.cu -- free-surface step (LB::latticeBoltzmannFreeSurfaceStep, LB.cpp:235-245,
-// 1492-1804): the mass exchange runs on a compacted list of the interface cells (warp
-// ballots over the node byte, one warp per cell), the conversions as full-grid passes
-// over the node byte.
+// 1492-1804) on compacted cell lists.
 //
 // The reference walks ordered lists (interface nodes sorted ascending, walked backwards;
 // filled/emptied lists; appended new interface cells).  Every conversion rule it applies
 // depends only on a node's own state and on neighbour types that the same pass does not
-// change, so each rule becomes one parallel pass:
-//   K1 mass exchange of interface cells (updateMass)          -> mass2
-//   K2 classify: mass > n filled -> fluid, mass < 0 emptied -> gas
+// change, so each rule becomes one parallel pass over a list:
+//   K1 mass exchange of the interface cells (updateMass)              -> mass2
+//   K2 classify the interface cells: mass > n filled -> fluid, mass < 0 emptied -> gas
+//      (the conversion list); fluid cells take mass = n (one lean pass over the grid)
 //   K3 gas cells next to a filled cell -> interface, initialised from the filled
 //      neighbour with the LARGEST index (the reference visits filled cells in descending
 //      order and the first visitor initialises the cell), surplus -= 0.01
 //   K4 fluid cells next to an emptied cell -> interface, mass = 0.99 n, surplus += 0.01 n
 //   K5 mutants (emptied not re-interfaced: surplus += mass; filled not re-interfaced:
 //      surplus += mass - n, mass = n) and isolated interface without gas links -> fluid
-//   K6 isolated interface without fluid links -> gas (surplus += mass)
+//   K6 isolated interface without fluid links -> gas (surplus += mass); the others form
+//      the next step's interface list
 //   K7 surplus / count added to every interface cell (redistributeMass)
-// The FP64 surplus ledger is summed from per-block partials in a fixed order.  Only the
-// summation order of that ledger differs from the reference (rounding level).
+// K3 and K4 start from the conversion list and visit the cells' 18 neighbours; K5-K7 run
+// over the interface cells (the list of the step's start minus the converted ones, plus
+// the new ones).  The lists are unordered, so the FP64 surplus ledger is a 128-bit
+// fixed-point sum (2^-100 resolution, integer atomics): its value does not depend on the
+// order of the additions, and it differs from the reference's sequential FP64 sum at the
+// rounding level only.
 //
 // Streamed populations: the reference's massStream(j) = f[opp j] - fs[j] needs the
 // post-collision value fs[j] of the cell, which the push kernel delivered to the active
@@ -26,6 +30,7 @@
 // f[opp j] = fs[j] - BBi.  At the very first step fs is the initial equilibrium of the
 // cell itself (node::initialize sets f = fs), and the first pass uses that.
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 
 #include "hb_common.cuh"
@@ -34,9 +39,22 @@
 namespace hb {
 
 enum : uint8_t { FS_FILLED = 1, FS_EMPTIED = 2, FS_NEW_A = 4, FS_NEW_B = 8 };
-constexpr int FS_PARTS = 4;  // ledger partials: K3, K4, K5, K6
-constexpr int FS_BLOCK = 128;  // threads per block along x
-constexpr int FS_ZC = 8;       // z planes per block: a thread visits FS_ZC nodes
+constexpr int FS_LIST_GRID = 152 * 4;  // blocks of 256 threads of the list passes
+
+// Step state of the free surface in device memory (the fields from ccount on are zeroed
+// at the start of every step).
+struct FsCount {
+    int first;       // 1 until the first free-surface step has run
+    int valid;       // the current interface list holds the interface cells
+    int sel;         // which of the two interface lists is current
+    int changed;     // cells whose activity changed (gas <-> interface) in this step
+    int icount[2];   // lengths of the two interface lists
+    int ccount;      // filled and emptied cells of this step (the conversion list)
+    int ncount;      // new interface cells of this step
+    unsigned long long ledger[2];  // surplus of this step, 128-bit fixed point (low, high)
+};
+static_assert(sizeof(FsCount) <= 64, "the count block has 64 bytes");
+constexpr double LEDGER_ONE = 1267650600228229401496703205376.0;  // 2^100
 
 struct FsArgs {
     int X, Y, Z;
@@ -51,46 +69,24 @@ struct FsArgs {
     double* mass2;
     void* visc;             // persistent viscosity or nullptr
     double init_visc;
-    uint8_t* flag;
-    double* part;           // [FS_PARTS * blocks]
-    int* cnt_part;          // [blocks] interface counts
-    double* scal;           // [0] surplus [1] interface count
+    uint8_t* flag;          // per-node conversion flags of this step (zero between steps)
+    double* scal;           // [0] surplus [1] interface count [2] surplus / count
     const double* force;    // lbF as the free surface sees it (zeroed after the first step
                             // when forceFieldSolve = 0)
-    int* first;             // device flag: 1 until the first free-surface step has run
-    int* nconv;             // [3] cells filled / emptied by this step's classify; cells whose
-                            // activity changed (gas <-> interface) in this step
-    int blocks;
-    uint32_t* ilist;        // [icap] interface cells at the start of the step (unordered)
-    int* icount;            // its length (may exceed icap: the overflow is flagged)
-    long long icap;         // capacity of ilist (hb_params.cap_interface, default N)
+    FsCount* cnt;
+    uint32_t* ilist;        // [2 * icap] the two interface lists (current, next)
+    uint32_t* clist;        // [icap] filled and emptied cells of this step
+    uint32_t* nlist;        // [icap] new interface cells of this step
+    uint32_t* parent;       // [N] zero between steps: the filled parent (+1) of a new cell
+    long long icap;         // capacity of each list (hb_params.cap_interface, default N)
     int* status;            // device status words (word 2, bit 8: interface list full)
 };
 
-// Every pass runs on a 3D grid (x from the thread, y and a group of ZC z planes from the
-// block; a thread visits its ZC nodes in turn), so a node's coordinates come without
-// divisions.  Light passes take ZC = FS_ZC planes, so block scheduling does not dominate
-// them; the mass exchange (18 links of every interface cell) and the redistribution take
-// one plane per block, so that a surface lying across the x rows spreads over many
-// blocks instead of queueing in one lane.  Neighbours follow the reference's periodic
-// remap.
 struct Node {
     int x, y, z;
     long long i;
     bool ok;
 };
-template <int ZC = FS_ZC>
-__device__ __forceinline__ Node node_of(const FsArgs& a, int zz) {
-    Node n;
-    n.x = blockIdx.x * blockDim.x + threadIdx.x;
-    n.y = blockIdx.y;
-    n.z = blockIdx.z * ZC + zz;
-    n.ok = n.x < a.X && n.z < a.Z;
-    n.i = (long long)n.x + (long long)a.X * ((long long)n.y + (long long)a.Y * n.z);
-    return n;
-}
-// linear block index of the 3D grid (ledger partial slot)
-__device__ __forceinline__ int block_id() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
 
 __device__ __forceinline__ void fs_link3(const FsArgs& a, int x, int y, int z, int j, int& xn, int& yn, int& zn) {
     xn = x + cx(j); yn = y + cy(j); zn = z + cz(j);
@@ -109,18 +105,6 @@ __device__ __forceinline__ long long fs_link(const FsArgs& a, const Node& n, int
 __device__ __forceinline__ bool interior3(const FsArgs& a, int x, int y, int z) {
     return x > 0 && y > 0 && z > 0 && x < a.X - 1 && y < a.Y - 1 && z < a.Z - 1;
 }
-// the interior cell m with link d[m][opp(k)] == n, if any (the reference's neighbour table:
-// interior nodes link arithmetically with the periodic remap, boundary nodes to themselves)
-__device__ __forceinline__ bool source_of(const FsArgs& a, const Node& n, int k, long long& m) {
-    int xm, ym, zm;
-    fs_link3(a, n.x, n.y, n.z, k, xm, ym, zm);
-    if (!interior3(a, xm, ym, zm)) return false;
-    int xb, yb, zb;
-    fs_link3(a, xm, ym, zm, opp(k), xb, yb, zb);
-    if (xb != n.x || yb != n.y || zb != n.z) return false;
-    m = lin(a, xm, ym, zm);
-    return true;
-}
 __device__ __forceinline__ uint8_t code_of(const FsArgs& a, long long i) { return a.ntype[i] & HB_TYPE_MASK; }
 
 template <class P>
@@ -130,43 +114,90 @@ __device__ __forceinline__ double fval(const FsArgs& a, int j, long long i) {
     return v;
 }
 
-// block-sum of one FP64 value into part[k*blocks + block] (fixed-order tree)
-__device__ void block_ledger(const FsArgs& a, int k, double v) {
-    __shared__ double sh[FS_BLOCK];
-    // most blocks convert nothing: their partial is 0 without FP64 work (narrow pipe)
-    if (!__syncthreads_or(__double_as_longlong(v) != 0)) {
-        if (threadIdx.x == 0) a.part[(long long)k * a.blocks + block_id()] = 0.0;
-        return;
+// ---- lists ------------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t* cur_list(const FsArgs& a) { return a.ilist + (a.cnt->sel ? a.icap : 0); }
+__device__ __forceinline__ uint32_t* next_list(const FsArgs& a) { return a.ilist + (a.cnt->sel ? 0 : a.icap); }
+__device__ __forceinline__ int cur_count(const FsArgs& a) { return (int)min((long long)a.cnt->icount[a.cnt->sel], a.icap); }
+
+// append `item` of the lanes with `take` to list[0 .. cap) at *count (warp ballot, one
+// atomic per warp); a full list sets status word 2, bit 8
+__device__ __forceinline__ void list_push(const FsArgs& a, uint32_t* list, int* count, bool take, uint32_t item) {
+    const unsigned warp = __activemask();
+    const unsigned b = __ballot_sync(warp, take);
+    if (!b) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(b) - 1;
+    int base = 0;
+    if (lane == leader) {
+        base = atomicAdd(count, __popc(b));
+        if (base + __popc(b) > a.icap) atomicOr(a.status + 2, 8);
     }
-    sh[threadIdx.x] = v;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-        __syncthreads();
+    base = __shfl_sync(warp, base, leader);
+    const long long k = (long long)base + __popc(b & ((1u << lane) - 1u));
+    if (take && k < a.icap) list[k] = item;
+}
+
+__device__ __forceinline__ Node node_at(const FsArgs& a, uint32_t iu) {
+    const uint32_t X = (uint32_t)a.X, XY = (uint32_t)a.X * (uint32_t)a.Y;
+    Node nd;
+    nd.x = (int)(iu % X);
+    nd.y = (int)((iu % XY) / X);
+    nd.z = (int)(iu / XY);
+    nd.i = (long long)iu;
+    nd.ok = true;
+    return nd;
+}
+
+// the surplus ledger: v * 2^100 rounded to the nearest 128-bit integer (ties to even),
+// from the bits of v with integer instructions, added with two 64-bit atomics (the low
+// word's carry goes into the high word with it).  Integer sums do not depend on the
+// order of the additions.  |v| below 2^-54 rounds to 0; the total stays below 2^26.
+__device__ void ledger_add(const FsArgs& a, double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FFu);
+    if (e == 0) return;  // zero or subnormal
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int s = e - 1075 + 100;  // v 2^100 = m 2^s
+    unsigned long long lo, hi;
+    if (s >= 64) {
+        lo = 0ull;
+        hi = m << min(s - 64, 10);
+    } else if (s > 0) {
+        lo = m << s;
+        hi = m >> (64 - s);
+    } else if (s == 0) {
+        lo = m;
+        hi = 0ull;
+    } else {
+        const int k = -s;
+        if (k > 54) return;
+        const unsigned long long q = m >> k, rem = m & ((1ull << k) - 1ull), half = 1ull << (k - 1);
+        lo = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+        hi = 0ull;
     }
-    if (threadIdx.x == 0) a.part[(long long)k * a.blocks + block_id()] = sh[0];
-    __syncthreads();
+    if (b >> 63) {  // two's complement of the 128-bit magnitude
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+    }
+    const unsigned long long old = atomicAdd(&a.cnt->ledger[0], lo);
+    atomicAdd(&a.cnt->ledger[1], hi + ((old + lo < old) ? 1ull : 0ull));
 }
 
 // K1 updateMass (LB.cpp:1492-1590): newMass = mass + sum_j a_j (f[opp j] - fs[j])
-// Interface cells at the start of the step, compacted with warp ballots (order within
-// the list is irrelevant: each cell's mass exchange is independent of the others).
-__global__ void __launch_bounds__(FS_BLOCK) k_fs_ilist(FsArgs a) {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    for (int zz = 0; zz < FS_ZC; ++zz) {
-        const Node nd = node_of(a, zz);
-        const bool is_if = nd.ok && code_of(a, nd.i) == HB_T_INTERFACE;
-        const unsigned b = __ballot_sync(full, is_if);
-        if (!b) continue;
-        int base = 0;
-        if (lane == 0) {
-            base = atomicAdd(a.icount, __popc(b));
-            if (base + __popc(b) > a.icap) atomicOr(a.status + 2, 8);  // the list is full
-        }
-        base = __shfl_sync(full, base, 0);
-        const long long k = (long long)base + __popc(b & ((1u << lane) - 1u));
-        if (is_if && k < a.icap) a.ilist[k] = (uint32_t)nd.i;
+// The interface list is carried from step to step (K6 writes the next one); after an
+// upload or a restore of the node types it is rebuilt here from the node bytes, by warp
+// ballots (order within the list is irrelevant: each cell's mass exchange is independent
+// of the others).
+__global__ void __launch_bounds__(256) k_fs_ilist(FsArgs a) {
+    if (a.cnt->valid) return;
+    uint32_t* list = cur_list(a);
+    int* count = &a.cnt->icount[a.cnt->sel];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long n_up = (a.N + 31) / 32 * 32;  // whole warps take part in the ballots
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_up; i += stride) {
+        const bool is_if = i < a.N && (a.ntype[i] & HB_TYPE_MASK) == HB_T_INTERFACE;
+        list_push(a, list, count, is_if, (uint32_t)i);
     }
 }
 
@@ -176,17 +207,11 @@ __global__ void __launch_bounds__(FS_BLOCK) k_fs_ilist(FsArgs a) {
 // then shares its warp instructions with 31 other cells on this part's narrow FP64 pipe.)
 template <class P>
 __global__ void __launch_bounds__(256) k_fs_mass_list(FsArgs a) {
-    const int n = (int)min((long long)*a.icount, a.icap);
-    const bool first = *a.first != 0;
-    const uint32_t X = (uint32_t)a.X, XY = (uint32_t)a.X * (uint32_t)a.Y;
+    const int n = cur_count(a);
+    const uint32_t* list = cur_list(a);
+    const bool first = a.cnt->first != 0;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x) {
-        const uint32_t iu = a.ilist[w];  // node indices fit 32 bits (the list is uint32)
-        Node nd;
-        nd.x = (int)(iu % X);
-        nd.y = (int)((iu % XY) / X);
-        nd.z = (int)(iu / XY);
-        nd.i = (long long)iu;
-        nd.ok = true;
+        const Node nd = node_at(a, list[w]);
         const long long i = nd.i;
         const double mi = a.mass[i];
         double dm = 0.0;
@@ -223,231 +248,272 @@ __global__ void __launch_bounds__(256) k_fs_mass_list(FsArgs a) {
     }
 }
 
-// K2 findInterfaceMutants (LB.cpp:1620-1650)
-__device__ __forceinline__ void fs_classify_node(const FsArgs& a, const Node& nd) {
-    const long long i = nd.i;
-    const uint8_t t = a.ntype[i];
-    uint8_t fl = 0;
-    if ((t & HB_TYPE_MASK) == HB_T_FLUID) a.mass[i] = a.rho[i];  // fluid mass = n (LB.cpp:1582-1585)
-    if ((t & HB_TYPE_MASK) == HB_T_INTERFACE) {
-        const double m = a.mass2[i];
-        a.mass[i] = m;
-        if (m > a.rho[i]) {
-            fl = FS_FILLED;
-            a.ntype[i] = (t & ~HB_TYPE_MASK) | HB_T_FLUID;
-            atomicAdd(a.nconv, 1);
-        } else if (m < 0.0) {
-            fl = FS_EMPTIED;
-            a.ntype[i] = (t & ~HB_TYPE_MASK) | HB_T_GAS;
-            atomicAdd(a.nconv + 1, 1);
-            atomicAdd(a.nconv + 2, 1);
-        }
-    }
-    a.flag[i] = fl;
-}
-__global__ void __launch_bounds__(FS_BLOCK) k_fs_classify(FsArgs a) {
-    for (int zz = 0; zz < FS_ZC; ++zz) {
-        const Node nd = node_of(a, zz);
-        if (nd.ok) fs_classify_node(a, nd);
-    }
-}
-
-// K3 smoothenInterface, gas neighbours of filled cells (LB.cpp:1657-1677)
-template <class P>
-__global__ void __launch_bounds__(FS_BLOCK) k_fs_new_from_filled(FsArgs a) {
-    double contrib = 0.0;
-    // nothing filled in this step (the usual case): no cell changes, the partial is 0
-    if (a.nconv[0] != 0)
-    for (int zz = 0; zz < FS_ZC; ++zz) {
-    const Node nd = node_of(a, zz);
-    const long long i = nd.i;
-    if (nd.ok && code_of(a, i) == HB_T_GAS && interior3(a, nd.x, nd.y, nd.z)) {
-        long long parent = -1;
-        for (int k = 1; k < Q; ++k) {  // filled cell m with link d[m][opp k] == i
-            long long m;
-            if (!source_of(a, nd, k, m) || !(a.flag[m] & FS_FILLED)) continue;
-            if (m > parent) parent = m;
-        }
-        if (parent >= 0) {
-            const long long p = parent;
-            const double F[3] = {a.hf[p] + a.force[0], a.hf[a.N + p] + a.force[1], a.hf[2 * a.N + p] + a.force[2]};
-            const double ux = 1.0 * F[0] / 2.0 / 1.0 + a.u[p];  // node::initialize, node.cpp:26-38
-            const double uy = 1.0 * F[1] / 2.0 / 1.0 + a.u[a.N + p];
-            const double uz = 1.0 * F[2] / 2.0 / 1.0 + a.u[2 * a.N + p];
-            const double usq = ux * ux + uy * uy + uz * uz;
-            using S = typename P::S;
-            S* f = reinterpret_cast<S*>(a.f);
-            for (int j = 0; j < Q; ++j) {
-                const double vu = ux * cx(j) + uy * cy(j) + uz * cz(j);
-                double fe = wgt(j) * 1.0 * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
-                if (P::DEV) fe -= wgt(j);
-                P::store(f + (long long)j * a.N + i, (typename P::T)fe);
-            }
-            a.rho[i] = 1.0;
-            a.u[i] = ux; a.u[a.N + i] = uy; a.u[2 * a.N + i] = uz;
-            a.hf[i] = 0.0; a.hf[a.N + i] = 0.0; a.hf[2 * a.N + i] = 0.0;
-            a.mass[i] = 0.01 * 1.0;
-            if (a.visc) {
-                if (P::DEV) reinterpret_cast<float*>(a.visc)[i] = reinterpret_cast<float*>(a.visc)[p];
-                else reinterpret_cast<double*>(a.visc)[i] = reinterpret_cast<double*>(a.visc)[p];
-            }
-            a.ntype[i] = (a.ntype[i] & ~HB_TYPE_MASK) | HB_T_INTERFACE;
-            a.flag[i] |= FS_NEW_A;
-            atomicAdd(a.nconv + 2, 1);
-            contrib += -0.01 * 1.0;
-        }
-    }
-    }
-    block_ledger(a, 0, contrib);
-}
-
-// K4 smoothenInterface, fluid neighbours of emptied cells (LB.cpp:1679-1700)
-__global__ void __launch_bounds__(FS_BLOCK) k_fs_new_from_emptied(FsArgs a) {
-    double contrib = 0.0;
-    if (a.nconv[1] != 0)
-    for (int zz = 0; zz < FS_ZC; ++zz) {
-    const Node nd = node_of(a, zz);
-    const long long i = nd.i;
-    if (nd.ok && code_of(a, i) == HB_T_FLUID && interior3(a, nd.x, nd.y, nd.z)) {
-        bool hit = false;
-        for (int k = 1; k < Q && !hit; ++k) {
-            long long m;
-            if (source_of(a, nd, k, m) && (a.flag[m] & FS_EMPTIED)) hit = true;
-        }
-        if (hit) {
-            const double n = a.rho[i];
-            a.mass[i] = 0.99 * n;
-            contrib += 0.01 * n;
-            a.ntype[i] = (a.ntype[i] & ~HB_TYPE_MASK) | HB_T_INTERFACE;
-            a.flag[i] |= FS_NEW_B;
-        }
-    }
-    }
-    block_ledger(a, 1, contrib);
-}
-
-// K5 updateMutants (LB.cpp:1703-1742) and removeIsolated, first pass (LB.cpp:1749-1769)
-__global__ void __launch_bounds__(FS_BLOCK) k_fs_mutants_to_fluid(FsArgs a) {
-    double contrib = 0.0;
-    for (int zz = 0; zz < FS_ZC; ++zz) {
-    const Node nd = node_of(a, zz);
-    const long long i = nd.i;
-    if (nd.ok) {
-        const uint8_t fl = a.flag[i];
-        const uint8_t t = code_of(a, i);
-        if ((fl & FS_EMPTIED) && !(fl & FS_NEW_A)) {
-            contrib += a.mass[i];
-        } else if ((fl & FS_FILLED) && !(fl & FS_NEW_B)) {
-            contrib += a.mass[i] - a.rho[i];
-            a.mass[i] = a.rho[i];
-        }
-        if (t == HB_T_INTERFACE) {
-            bool gas = false;
-            for (int j = 1; j < Q && !gas; ++j)
-                if (code_of(a, fs_link(a, nd, j)) == HB_T_GAS) gas = true;
-            if (!gas) {
-                contrib += a.mass[i] - a.rho[i];
-                a.mass[i] = a.rho[i];
-                a.ntype[i] = (a.ntype[i] & ~HB_TYPE_MASK) | HB_T_FLUID;
-            }
-        }
-    }
-    }
-    block_ledger(a, 2, contrib);
-}
-
-// K6 removeIsolated, second pass (LB.cpp:1771-1793)
-__global__ void __launch_bounds__(FS_BLOCK) k_fs_isolated_gas(FsArgs a) {
-    double contrib = 0.0;
-    int count = 0;
-    for (int zz = 0; zz < FS_ZC; ++zz) {
-    const Node nd = node_of(a, zz);
-    const long long i = nd.i;
-    if (nd.ok && code_of(a, i) == HB_T_INTERFACE) {
-        bool fluid = false;
-        for (int j = 1; j < Q && !fluid; ++j)
-            if (code_of(a, fs_link(a, nd, j)) == HB_T_FLUID) fluid = true;
-        if (!fluid) {
-            contrib += a.mass[i];
-            a.ntype[i] = (a.ntype[i] & ~HB_TYPE_MASK) | HB_T_GAS;
-            atomicAdd(a.nconv + 2, 1);
+// fluid mass = n (LB.cpp:1582-1585): a lean pass over the node bytes, eight per thread
+__global__ void __launch_bounds__(256) k_fs_fluid_mass(FsArgs a) {
+    const long long nw = (a.N + 7) / 8;
+    for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nw; w += (long long)gridDim.x * blockDim.x) {
+        const long long i0 = 8 * w;
+        uint8_t t[8];
+        if (i0 + 8 <= a.N && (a.N & 7) == 0) {
+            const uint2 v = reinterpret_cast<const uint2*>(a.ntype)[w];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) { t[k] = (uint8_t)(v.x >> (8 * k)); t[4 + k] = (uint8_t)(v.y >> (8 * k)); }
         } else {
-            count += 1;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) t[k] = i0 + k < a.N ? a.ntype[i0 + k] : (uint8_t)HB_T_GAS;
         }
-    }
-    }
-    block_ledger(a, 3, contrib);
-    __shared__ int shc[FS_BLOCK];
-    shc[threadIdx.x] = count;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s) shc[threadIdx.x] += shc[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) a.cnt_part[block_id()] = shc[0];
-}
-
-// ledger total and interface count: k_fs_ledger_part sums fixed chunks of the block
-// partials (one block per chunk, fixed-order tree), k_fs_ledger the chunk sums; zero
-// partials are skipped by an integer test of their bits
-constexpr int FS_LEDGER_CHUNKS = 256;
-
-__global__ void k_fs_ledger_part(FsArgs a, double* csum, long long* ccnt) {
-    __shared__ double shs[256];
-    __shared__ long long shc[256];
-    const int per = (a.blocks + FS_LEDGER_CHUNKS - 1) / FS_LEDGER_CHUNKS;
-    const int b0 = blockIdx.x * per, b1 = min(a.blocks, b0 + per);
-    double s = 0.0;
-    long long c = 0;
-    for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
-        for (int k = 0; k < FS_PARTS; ++k) {
-            const double v = a.part[(long long)k * a.blocks + b];
-            if (__double_as_longlong(v) != 0) s += v;
-        }
-        c += a.cnt_part[b];
-    }
-    shs[threadIdx.x] = s;
-    shc[threadIdx.x] = c;
-    __syncthreads();
-    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
-        if ((int)threadIdx.x < k) {
-            if (__double_as_longlong(shs[threadIdx.x + k]) != 0) shs[threadIdx.x] += shs[threadIdx.x + k];
-            shc[threadIdx.x] += shc[threadIdx.x + k];
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        csum[blockIdx.x] = shs[0];
-        ccnt[blockIdx.x] = shc[0];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if ((t[k] & HB_TYPE_MASK) == HB_T_FLUID) a.mass[i0 + k] = a.rho[i0 + k];
     }
 }
 
-__global__ void k_fs_ledger(FsArgs a, const double* csum, const long long* ccnt) {
-    __shared__ double shs[FS_LEDGER_CHUNKS];
-    __shared__ long long shc[FS_LEDGER_CHUNKS];
-    shs[threadIdx.x] = csum[threadIdx.x];
-    shc[threadIdx.x] = ccnt[threadIdx.x];
-    __syncthreads();
-    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
-        if ((int)threadIdx.x < k) {
-            if (__double_as_longlong(shs[threadIdx.x + k]) != 0) shs[threadIdx.x] += shs[threadIdx.x + k];
-            shc[threadIdx.x] += shc[threadIdx.x + k];
+// K2 findInterfaceMutants (LB.cpp:1620-1650) over the interface list
+__global__ void __launch_bounds__(256) k_fs_classify(FsArgs a) {
+    const int n = cur_count(a);
+    const uint32_t* list = cur_list(a);
+    const int n_up = (n + 31) / 32 * 32;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n_up; w += gridDim.x * blockDim.x) {
+        bool conv = false;
+        uint32_t iu = 0u;
+        if (w < n) {
+            iu = list[w];
+            const long long i = iu;
+            const uint8_t t = a.ntype[i];
+            const double m = a.mass2[i];
+            a.mass[i] = m;
+            if (m > a.rho[i]) {
+                a.flag[i] = FS_FILLED;
+                a.ntype[i] = (t & ~HB_TYPE_MASK) | HB_T_FLUID;
+                conv = true;
+            } else if (m < 0.0) {
+                a.flag[i] = FS_EMPTIED;
+                a.ntype[i] = (t & ~HB_TYPE_MASK) | HB_T_GAS;
+                atomicAdd(&a.cnt->changed, 1);
+                conv = true;
+            }
         }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        a.scal[0] = shs[0];
-        a.scal[1] = (double)shc[0];
-        *a.first = 0;
-        a.nconv[0] = 0;  // counts of the next step's classify
-        a.nconv[1] = 0;
+        list_push(a, a.clist, &a.cnt->ccount, conv, iu);
     }
 }
 
-// K7 redistributeMass (LB.cpp:1796-1804)
-__global__ void __launch_bounds__(FS_BLOCK) k_fs_redistribute(FsArgs a) {
-    const Node nd = node_of<1>(a, 0);
-    if (nd.ok && code_of(a, nd.i) == HB_T_INTERFACE) a.mass[nd.i] += a.scal[0] / a.scal[1];
+// K3 smoothenInterface, gas neighbours of filled cells (LB.cpp:1657-1677).  First every
+// filled cell m offers itself to its interior gas neighbours g (those whose link back
+// along the same direction reaches m: the reference's neighbour table), keeping the
+// largest m + 1 per g; then the winner initialises g.
+__global__ void __launch_bounds__(256) k_fs_filled_parent(FsArgs a) {
+    const int n = min(a.cnt->ccount, (int)a.icap);
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x) {
+        const uint32_t m = a.clist[w];
+        if (!(a.flag[m] & FS_FILLED)) continue;
+        const Node nd = node_at(a, m);
+        if (!interior3(a, nd.x, nd.y, nd.z)) continue;
+        for (int j = 1; j < Q; ++j) {
+            int xg, yg, zg;
+            fs_link3(a, nd.x, nd.y, nd.z, j, xg, yg, zg);
+            if (!interior3(a, xg, yg, zg)) continue;
+            const long long g = lin(a, xg, yg, zg);
+            if (code_of(a, g) == HB_T_GAS) atomicMax(a.parent + g, m + 1u);
+        }
+    }
+}
+
+template <class P>
+__global__ void __launch_bounds__(256) k_fs_new_from_filled(FsArgs a) {
+    const int n = min(a.cnt->ccount, (int)a.icap);
+    const int n_up = (n + 31) / 32 * 32;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n_up; w += gridDim.x * blockDim.x) {
+        const uint32_t m = w < n ? a.clist[w] : 0u;
+        const bool filled = w < n && (a.flag[m] & FS_FILLED);
+        const Node nd = node_at(a, m);
+        const bool src = filled && interior3(a, nd.x, nd.y, nd.z);
+        for (int j = 1; j < Q; ++j) {
+            bool mine = false;
+            long long g = 0;
+            if (src) {
+                int xg, yg, zg;
+                fs_link3(a, nd.x, nd.y, nd.z, j, xg, yg, zg);
+                g = lin(a, xg, yg, zg);
+                mine = interior3(a, xg, yg, zg) && a.parent[g] == m + 1u;
+            }
+            if (mine) {
+                const long long i = g, p = m;
+                const double F[3] = {a.hf[p] + a.force[0], a.hf[a.N + p] + a.force[1], a.hf[2 * a.N + p] + a.force[2]};
+                const double ux = 1.0 * F[0] / 2.0 / 1.0 + a.u[p];  // node::initialize, node.cpp:26-38
+                const double uy = 1.0 * F[1] / 2.0 / 1.0 + a.u[a.N + p];
+                const double uz = 1.0 * F[2] / 2.0 / 1.0 + a.u[2 * a.N + p];
+                const double usq = ux * ux + uy * uy + uz * uz;
+                using S = typename P::S;
+                S* f = reinterpret_cast<S*>(a.f);
+                for (int q = 0; q < Q; ++q) {
+                    const double vu = ux * cx(q) + uy * cy(q) + uz * cz(q);
+                    double fe = wgt(q) * 1.0 * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
+                    if (P::DEV) fe -= wgt(q);
+                    P::store(f + (long long)q * a.N + i, (typename P::T)fe);
+                }
+                a.rho[i] = 1.0;
+                a.u[i] = ux; a.u[a.N + i] = uy; a.u[2 * a.N + i] = uz;
+                a.hf[i] = 0.0; a.hf[a.N + i] = 0.0; a.hf[2 * a.N + i] = 0.0;
+                a.mass[i] = 0.01 * 1.0;
+                if (a.visc) {
+                    if (P::DEV) reinterpret_cast<float*>(a.visc)[i] = reinterpret_cast<float*>(a.visc)[p];
+                    else reinterpret_cast<double*>(a.visc)[i] = reinterpret_cast<double*>(a.visc)[p];
+                }
+                a.ntype[i] = (a.ntype[i] & ~HB_TYPE_MASK) | HB_T_INTERFACE;
+                a.flag[i] |= FS_NEW_A;
+                a.parent[i] = 0u;
+                atomicAdd(&a.cnt->changed, 1);
+                ledger_add(a, -0.01 * 1.0);
+            }
+            list_push(a, a.nlist, &a.cnt->ncount, mine, (uint32_t)g);
+        }
+    }
+}
+
+// K4 smoothenInterface, fluid neighbours of emptied cells (LB.cpp:1679-1700); the first
+// emptied neighbour to claim a cell (parent slot) converts it
+__global__ void __launch_bounds__(256) k_fs_new_from_emptied(FsArgs a) {
+    const int n = min(a.cnt->ccount, (int)a.icap);
+    const int n_up = (n + 31) / 32 * 32;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n_up; w += gridDim.x * blockDim.x) {
+        const uint32_t m = w < n ? a.clist[w] : 0u;
+        const bool emptied = w < n && (a.flag[m] & FS_EMPTIED);
+        const Node nd = node_at(a, m);
+        const bool src = emptied && interior3(a, nd.x, nd.y, nd.z);
+        for (int j = 1; j < Q; ++j) {
+            bool mine = false;
+            long long g = 0;
+            if (src) {
+                int xg, yg, zg;
+                fs_link3(a, nd.x, nd.y, nd.z, j, xg, yg, zg);
+                g = lin(a, xg, yg, zg);
+                mine = interior3(a, xg, yg, zg) && code_of(a, g) == HB_T_FLUID &&
+                       atomicCAS(a.parent + g, 0u, 0xFFFFFFFFu) == 0u;
+            }
+            if (mine) {
+                const double nn = a.rho[g];
+                a.mass[g] = 0.99 * nn;
+                ledger_add(a, 0.01 * nn);
+                a.ntype[g] = (a.ntype[g] & ~HB_TYPE_MASK) | HB_T_INTERFACE;
+                a.flag[g] |= FS_NEW_B;
+            }
+            list_push(a, a.nlist, &a.cnt->ncount, mine, (uint32_t)g);
+        }
+    }
+}
+
+// the interface cells after K3/K4: the step's list minus the converted cells (flag set),
+// then the new cells; k indexes that concatenation
+__device__ __forceinline__ bool interface_cell(const FsArgs& a, int k, int n0, uint32_t& iu) {
+    if (k < n0) {
+        iu = cur_list(a)[k];
+        return a.flag[iu] == 0;
+    }
+    iu = a.nlist[k - n0];
+    return true;
+}
+
+// K5 updateMutants (LB.cpp:1703-1742) over the conversion list, and removeIsolated, first
+// pass (LB.cpp:1749-1769) over the interface cells
+__global__ void __launch_bounds__(256) k_fs_mutants_to_fluid(FsArgs a) {
+    const int nc = min(a.cnt->ccount, (int)a.icap);
+    const int n0 = cur_count(a), nn = min(a.cnt->ncount, (int)a.icap);
+    const int total = nc + n0 + nn;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < total; w += gridDim.x * blockDim.x) {
+        if (w < nc) {
+            const uint32_t i = a.clist[w];
+            const uint8_t fl = a.flag[i];
+            if ((fl & FS_EMPTIED) && !(fl & FS_NEW_A)) {
+                ledger_add(a, a.mass[i]);
+            } else if ((fl & FS_FILLED) && !(fl & FS_NEW_B)) {
+                ledger_add(a, a.mass[i] - a.rho[i]);
+                a.mass[i] = a.rho[i];
+            }
+            continue;
+        }
+        uint32_t iu;
+        if (!interface_cell(a, w - nc, n0, iu)) continue;
+        const Node nd = node_at(a, iu);
+        bool gas = false;
+        for (int j = 1; j < Q && !gas; ++j)
+            if (code_of(a, fs_link(a, nd, j)) == HB_T_GAS) gas = true;
+        if (!gas) {
+            ledger_add(a, a.mass[iu] - a.rho[iu]);
+            a.mass[iu] = a.rho[iu];
+            a.ntype[iu] = (a.ntype[iu] & ~HB_TYPE_MASK) | HB_T_FLUID;
+        }
+    }
+}
+
+// K6 removeIsolated, second pass (LB.cpp:1771-1793); the cells that stay interface form
+// the next interface list
+__global__ void __launch_bounds__(256) k_fs_isolated_gas(FsArgs a) {
+    const int n0 = cur_count(a), nn = min(a.cnt->ncount, (int)a.icap);
+    const int total = n0 + nn;
+    const int t_up = (total + 31) / 32 * 32;
+    uint32_t* next = next_list(a);
+    int* ncount = &a.cnt->icount[a.cnt->sel ^ 1];
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < t_up; w += gridDim.x * blockDim.x) {
+        uint32_t iu = 0u;
+        bool keep = false;
+        if (w < total && interface_cell(a, w, n0, iu) && (a.ntype[iu] & HB_TYPE_MASK) == HB_T_INTERFACE) {
+            const Node nd = node_at(a, iu);
+            bool fluid = false;
+            for (int j = 1; j < Q && !fluid; ++j)
+                if (code_of(a, fs_link(a, nd, j)) == HB_T_FLUID) fluid = true;
+            if (!fluid) {
+                ledger_add(a, a.mass[iu]);
+                a.ntype[iu] = (a.ntype[iu] & ~HB_TYPE_MASK) | HB_T_GAS;
+                atomicAdd(&a.cnt->changed, 1);
+            } else {
+                keep = true;
+            }
+        }
+        list_push(a, next, ncount, keep, iu);
+    }
+}
+
+// the surplus and the interface count of the step; the next list becomes current
+__global__ void k_fs_ledger(FsArgs a) {
+    FsCount* c = a.cnt;
+    const int nxt = c->sel ^ 1;
+    const long long count = min((long long)c->icount[nxt], a.icap);
+    unsigned long long lo = c->ledger[0], hi = c->ledger[1];
+    const bool neg = (long long)hi < 0;
+    if (neg) {
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+    }
+    double surplus = ((double)hi * 18446744073709551616.0 + (double)lo) / LEDGER_ONE;
+    if (neg) surplus = -surplus;
+    a.scal[0] = surplus;
+    a.scal[1] = (double)count;
+    a.scal[2] = surplus / (double)count;  // redistributeMass adds surplus / count to each cell
+    c->first = 0;
+    c->valid = 1;
+    c->icount[c->sel] = 0;  // the retired list is the next step's "next"
+    c->sel = nxt;
+}
+
+// K7 redistributeMass (LB.cpp:1796-1804): the quotient surplus / count is formed once
+// (k_fs_ledger), as the reference forms addMass once; then the step's conversion flags
+// and claim slots go back to zero
+__global__ void __launch_bounds__(256) k_fs_redistribute(FsArgs a) {
+    const int n0 = cur_count(a);
+    const int nc = min(a.cnt->ccount, (int)a.icap), nn = min(a.cnt->ncount, (int)a.icap);
+    const uint32_t* list = cur_list(a);
+    const double add = a.scal[2];
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n0 + nc + nn; w += gridDim.x * blockDim.x) {
+        if (w < n0) {
+            a.mass[list[w]] += add;
+        } else if (w < n0 + nc) {
+            a.flag[a.clist[w - n0]] = 0;
+        } else {
+            const uint32_t g = a.nlist[w - n0 - nc];
+            a.flag[g] = 0;
+            a.parent[g] = 0u;
+        }
+    }
 }
 
 // ---- host side ---------------------------------------------------------------------------
@@ -466,70 +532,81 @@ static FsArgs fs_args(hb_ctx* c, int cur) {
     a.visc = c->visc;
     a.init_visc = c->P.init_visc;
     a.flag = c->fs_flag;
-    a.part = c->fs_part;
-    a.cnt_part = c->fs_cnt;
     a.scal = c->fs_scal;
     a.force = c->fs_force;
-    a.first = c->fs_first;
-    a.nconv = c->fs_first + 1;
-    a.blocks = ceil_div(c->X, FS_BLOCK) * c->Y * ceil_div(c->Z, FS_ZC);
+    a.cnt = reinterpret_cast<FsCount*>(c->fs_first);
     a.ilist = c->fs_ilist;
-    a.icount = c->fs_first + 4;
+    a.clist = c->fs_ilist + 2 * c->fs_icap;
+    a.nlist = c->fs_ilist + 3 * c->fs_icap;
+    a.parent = c->fs_parent;
     a.icap = c->fs_icap;
     a.status = c->status;
     return a;
 }
 
-void fs_buffer_bytes(const hb_ctx* c, size_t* part, size_t* cnt) {
-    const size_t blocks = (size_t)ceil_div(c->X, FS_BLOCK) * c->Y * ceil_div(c->Z, FS_ZC);
-    *part = sizeof(double) * (FS_PARTS * blocks + 2 * FS_LEDGER_CHUNKS);
-    *cnt = sizeof(int) * blocks;
+size_t fs_count_bytes() { return 64; }
+
+// the interface list is rebuilt from the node bytes at the next step (after an upload of
+// the node types or a restore)
+void fs_invalidate(hb_ctx* c) {
+    if (!c->fs_first) return;
+    FsCount h = {};
+    cudaMemcpy(&h, c->fs_first, sizeof(h), cudaMemcpyDeviceToHost);
+    h.valid = 0;
+    h.icount[0] = h.icount[1] = 0;
+    cudaMemcpy(c->fs_first, &h, sizeof(h), cudaMemcpyHostToDevice);
+}
+
+// a checkpoint carries no interface list (the loader rebuilds it from the node bytes),
+// so its copy of the step state says so, whichever list was current
+void fs_count_for_file(void* rec) {
+    FsCount* h = static_cast<FsCount*>(rec);
+    h->valid = 0;
+    h->sel = 0;
+    h->icount[0] = h->icount[1] = 0;
 }
 
 int fs_init(hb_ctx* c) {
     const long long N = c->N;
-    const int blocks = ceil_div(c->X, FS_BLOCK) * c->Y * ceil_div(c->Z, FS_ZC);
+    c->fs_icap = c->P.cap_interface > 0 ? std::min<long long>(c->P.cap_interface, N) : N;
     if (cudaMalloc(&c->fs_flag, N) != cudaSuccess || cudaMalloc(&c->fs_mass2, sizeof(double) * N) != cudaSuccess ||
-        cudaMalloc(&c->fs_part, sizeof(double) * (FS_PARTS * blocks + 2 * FS_LEDGER_CHUNKS)) != cudaSuccess ||
-        cudaMalloc(&c->fs_cnt, sizeof(int) * blocks) != cudaSuccess ||
-        cudaMalloc(&c->fs_scal, sizeof(double) * 2) != cudaSuccess ||
-        cudaMalloc(&c->fs_first, 6 * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&c->fs_ilist, sizeof(uint32_t) * (c->fs_icap = c->P.cap_interface > 0 ? std::min<long long>(c->P.cap_interface, N) : N)) !=
-            cudaSuccess)
+        cudaMalloc(&c->fs_scal, sizeof(double) * 3) != cudaSuccess ||
+        cudaMalloc(&c->fs_first, fs_count_bytes()) != cudaSuccess ||
+        cudaMalloc(&c->fs_parent, sizeof(uint32_t) * N) != cudaSuccess ||
+        cudaMalloc(&c->fs_ilist, sizeof(uint32_t) * 4 * c->fs_icap) != cudaSuccess)
         return HB_ERR_NOMEM;
     cudaMemset(c->fs_flag, 0, N);
-    cudaMemset(c->fs_scal, 0, sizeof(double) * 2);
-    const int init[6] = {1, 0, 0, 0, 0, 0};  // first step; filled / emptied / activity-change
-                                              // counts; interface-list length
-    cudaMemcpy(c->fs_first, init, sizeof(init), cudaMemcpyHostToDevice);
+    cudaMemset(c->fs_parent, 0, sizeof(uint32_t) * N);
+    cudaMemset(c->fs_scal, 0, sizeof(double) * 3);
+    FsCount h = {};
+    h.first = 1;  // first step; the interface list is built at the first step
+    cudaMemset(c->fs_first, 0, fs_count_bytes());
+    cudaMemcpy(c->fs_first, &h, sizeof(h), cudaMemcpyHostToDevice);
     return cudaGetLastError() == cudaSuccess ? HB_OK : HB_ERR_CUDA;
 }
 
 void launch_fs_step(hb_ctx* c, int cur) {
     FsArgs a = fs_args(c, cur);
-    const dim3 G((unsigned)ceil_div(c->X, FS_BLOCK), (unsigned)c->Y, (unsigned)ceil_div(c->Z, FS_ZC));
-    const dim3 G1((unsigned)ceil_div(c->X, FS_BLOCK), (unsigned)c->Y, (unsigned)c->Z);  // one plane per block
-    const int B = FS_BLOCK;
     cudaStream_t s = c->stream;
-    cudaMemsetAsync(a.icount, 0, sizeof(int), s);
-    k_fs_ilist<<<G, B, 0, s>>>(a);
-    const int GL = 152 * 8;  // persistent: 8 blocks of 8 warps per SM over the list
+    const int GL = FS_LIST_GRID;
+    // this step's conversion and new-cell counts and its ledger start at zero
+    cudaMemsetAsync(&a.cnt->ccount, 0, sizeof(FsCount) - offsetof(FsCount, ccount), s);
+    k_fs_ilist<<<GL, 256, 0, s>>>(a);
     if (c->P.precision == HB_FP64) k_fs_mass_list<PolF64><<<GL, 256, 0, s>>>(a);
     else if (c->P.precision == HB_FP32) k_fs_mass_list<PolF32><<<GL, 256, 0, s>>>(a);
     else k_fs_mass_list<PolF16><<<GL, 256, 0, s>>>(a);
-    k_fs_classify<<<G, B, 0, s>>>(a);
-    if (c->P.precision == HB_FP64) k_fs_new_from_filled<PolF64><<<G, B, 0, s>>>(a);
-    else if (c->P.precision == HB_FP32) k_fs_new_from_filled<PolF32><<<G, B, 0, s>>>(a);
-    else k_fs_new_from_filled<PolF16><<<G, B, 0, s>>>(a);
-    k_fs_new_from_emptied<<<G, B, 0, s>>>(a);
-    k_fs_mutants_to_fluid<<<G, B, 0, s>>>(a);
-    k_fs_isolated_gas<<<G, B, 0, s>>>(a);
-    double* csum = reinterpret_cast<double*>(c->fs_part + (size_t)FS_PARTS * a.blocks);
-    long long* ccnt = reinterpret_cast<long long*>(csum + FS_LEDGER_CHUNKS);
-    k_fs_ledger_part<<<FS_LEDGER_CHUNKS, 256, 0, s>>>(a, csum, ccnt);
-    k_fs_ledger<<<1, FS_LEDGER_CHUNKS, 0, s>>>(a, csum, ccnt);
-    k_fs_redistribute<<<G1, B, 0, s>>>(a);
-    launch_refresh_bulk(c, c->fs_first + 3);  // only when a cell's activity changed
+    k_fs_fluid_mass<<<152 * 8, 256, 0, s>>>(a);
+    k_fs_classify<<<GL, 256, 0, s>>>(a);
+    k_fs_filled_parent<<<GL, 256, 0, s>>>(a);
+    if (c->P.precision == HB_FP64) k_fs_new_from_filled<PolF64><<<GL, 256, 0, s>>>(a);
+    else if (c->P.precision == HB_FP32) k_fs_new_from_filled<PolF32><<<GL, 256, 0, s>>>(a);
+    else k_fs_new_from_filled<PolF16><<<GL, 256, 0, s>>>(a);
+    k_fs_new_from_emptied<<<GL, 256, 0, s>>>(a);
+    k_fs_mutants_to_fluid<<<GL, 256, 0, s>>>(a);
+    k_fs_isolated_gas<<<GL, 256, 0, s>>>(a);
+    k_fs_ledger<<<1, 1, 0, s>>>(a);
+    k_fs_redistribute<<<GL, 256, 0, s>>>(a);
+    launch_refresh_bulk(c, &a.cnt->changed);  // only when a cell's activity changed
 }
 
 }  // namespace hb

@@ -997,10 +997,9 @@ static MbbArgs mbb_args(hb_ctx* c, void* f) {
 void launch_mbb_nodes(hb_ctx* c, int cur) {
     MbbArgs m = mbb_args(c, cur ? c->fB : c->fA);
     const int B = 256;
-    const long long cap = c->N;  // each list holds at most every node once
-    const unsigned gp = (unsigned)std::min<long long>(ceil_div(cap, B), 152LL * 64);
-    // the grid is capped: list entries beyond it are handled by later blocks of a
-    // grid-stride form, so the launch shape does not depend on the device-side count
+    // the lists hold a few thousand entries per step: a fixed grid with grid-stride loops
+    // (the launch shape does not depend on the device-side counts)
+    const unsigned gp = 152 * 4;
     if (c->P.precision == HB_FP64) k_mbb_refill_gs<PolF64><<<gp, B, 0, c->stream>>>(m);
     else if (c->P.precision == HB_FP32) k_mbb_refill_gs<PolF32><<<gp, B, 0, c->stream>>>(m);
     else k_mbb_refill_gs<PolF16><<<gp, B, 0, c->stream>>>(m);

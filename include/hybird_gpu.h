@@ -221,7 +221,9 @@ int hb_cycle(hb_ctx* ctx, int32_t nsteps);
  * and object counts; any pointer may be NULL. */
 int hb_get_params(hb_ctx* ctx, hb_params* out, int32_t* elements, int32_t* objects);
 /* Changes the body force lbF used by the collision from the next step on (the reference
- * reads lb.lbF every collision, LB.cpp:1098-1111; problem code may change it). */
+ * reads lb.lbF every collision, LB.cpp:1098-1111; problem code may change it).  With
+ * particles the new value travels in the parameters of the cycle graphs' mask kernel,
+ * which writes it before the lattice step: no launch of its own between two cycles. */
 int hb_set_body_force(hb_ctx* ctx, const double* force /* [3] */);
 int hb_synchronize(hb_ctx* ctx);
 
@@ -247,9 +249,21 @@ int hb_download_elements_async(hb_ctx* ctx, double* x0, double* x1, double* w, d
                                double* fhydro, double* mhydro, double* fparticle, double* fwall,
                                double* mparticle, double* mwall, double* fluid_volume);
 /* Page-locks and maps (cudaHostRegister, mapped) / releases host memory the caller passes
- * to the asynchronous downloads. */
+ * to the asynchronous downloads and the element sink. */
 int hb_host_register(void* p, size_t bytes);
 int hb_host_unregister(void* p);
+/* Element sink: the arrays (same fields and layout as hb_download_elements, each
+ * registered with hb_host_register, any of them null) are written at the end of every
+ * cycle hb_cycle runs, by a gather kernel inside the cycle graph -- a host driver that
+ * reads the element state after every step (the reference's DEM::particles feeding its
+ * output and its own loop, hybird.cpp:35-66) gets it with no launch or copy of its own.
+ * After hb_synchronize the arrays hold the state after the last cycle.  All arrays null
+ * removes the sink.  The call re-captures the cycle graphs (it synchronises the stream);
+ * the arrays must stay registered and valid until the sink is removed or the context
+ * destroyed. */
+int hb_set_element_sink(hb_ctx* ctx, double* x0, double* x1, double* w, double* q0, double* fhydro,
+                        double* mhydro, double* fparticle, double* fwall, double* mparticle,
+                        double* mwall, double* fluid_volume);
 /* Candidate pair list as sorted (min,max) pairs, like DEM::neighborTable
  * (DEM.cpp:1369-1494) after normalisation.  *count receives the pair count.  With
  * periodic faces a ghost particle is numbered E + g (g its index in hb_download_ghosts),

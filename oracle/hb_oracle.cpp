@@ -1660,6 +1660,14 @@ int hbo_set_lattice(hbo_sim* s, const double* f, const double* n, const double* 
     return 0;
 }
 
+// problem code changing lb.lbF between steps: the collision reads it every step
+// (LB.cpp:1098-1111); zero without forceFieldSolve (LB.cpp:1074-1076); demF keeps the
+// value captured at init (DEM.cpp:194)
+int hbo_set_body_force(hbo_sim* s, const double* force) {
+    s->lbF = s->P.force_field ? v3(force[0], force[1], force[2]) : v3(0, 0, 0);
+    return 0;
+}
+
 int hbo_get_elements(const hbo_sim* s, double* x0, double* x1, double* w, double* q0,
                      double* fhydro, double* mhydro, double* fparticle, double* fwall,
                      double* mparticle, double* mwall, double* fluid_volume) {

@@ -40,6 +40,7 @@ int hbo_get_lattice(const hbo_sim* s, uint8_t* type, uint8_t* inside, uint32_t* 
                     double* visc, double* hydro_force);
 int hbo_set_lattice(hbo_sim* s, const double* f, const double* n, const double* u,
                     const double* mass, const double* visc);
+int hbo_set_body_force(hbo_sim* s, const double* force);
 int hbo_get_elements(const hbo_sim* s, double* x0, double* x1, double* w, double* q0,
                      double* fhydro, double* mhydro, double* fparticle, double* fwall,
                      double* mparticle, double* mwall, double* fluid_volume);

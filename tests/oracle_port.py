@@ -43,6 +43,7 @@ def oracle_lib():
     lib.hbo_active.argtypes = [C.c_void_p]
     lib.hbo_get_lattice.argtypes = [C.c_void_p] + [C.c_void_p] * 10
     lib.hbo_set_lattice.argtypes = [C.c_void_p] + [C.c_void_p] * 5
+    lib.hbo_set_body_force.argtypes = [C.c_void_p, C.c_void_p]
     lib.hbo_get_elements.argtypes = [C.c_void_p] + [C.c_void_p] * 11
     lib.hbo_get_pairs.restype = C.c_int64
     lib.hbo_get_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
@@ -106,6 +107,10 @@ class OracleSim:
 
     def set_lattice(self, f=None, n=None, u=None, mass=None, visc=None):
         self.lib.hbo_set_lattice(self.h, _p(f), _p(n), _p(u), _p(mass), _p(visc))
+
+    def set_body_force(self, force):
+        f = np.ascontiguousarray(force, dtype=np.float64)
+        self.lib.hbo_set_body_force(self.h, f.ctypes.data_as(C.c_void_p))
 
     def object_drag(self, axis=0):
         return self.lib.hbo_object_drag(self.h, axis)
