@@ -584,6 +584,7 @@ int hb_upload_lattice(hb_ctx* c, const uint8_t* type, const uint8_t* inside, con
         return seterr(HB_ERR_CUDA, "upload: %s", cudaGetErrorString(cudaGetLastError()));
     curved_remark(c);  // the uploaded node bytes carry no velocity-mirror bits
     hb::fs_invalidate(c);  // new node types: the interface list is rebuilt at the next step
+    c->mirror_valid = true;  // the node fields are the uploaded ones
     CK(cudaStreamSynchronize(c->stream));
     return HB_OK;
 }
@@ -701,10 +702,24 @@ static int run_cycles(hb_ctx* c, int n, bool last_mirror) {
         }
         ++c->steps;
     }
+    if (n > 0 && c->P.lb_solve) c->mirror_valid = last_mirror;
     return HB_OK;
 }
 
+static int need_mirror(const hb_ctx* c) {
+    if (c->mirror_valid || !c->P.lb_solve) return HB_OK;
+    return seterr(HB_ERR_STATE, "the node fields (rho, u, hydroForce) of the last step were not written: the last "
+                  "cycles ran with hb_set_lattice_mirror(ctx, 0) or through the timing entry points; run a cycle "
+                  "with the mirror on first");
+}
+
 extern "C" {
+
+int hb_set_lattice_mirror(hb_ctx* c, int32_t on) {
+    if (!c) return seterr(HB_ERR_ARG, "null ctx");
+    c->mirror = on != 0;
+    return HB_OK;
+}
 
 int hb_dem_step(hb_ctx* c) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
@@ -739,6 +754,7 @@ int hb_lb_step(hb_ctx* c) {
     hb::flush_body_force(c);
     CK(cudaMemsetAsync(c->mode, 1, sizeof(int), c->stream));
     c->mode_val = 1;
+    c->mirror_valid = true;
     launch_lb_step(c, c->cur);
     if (c->has_dynwall) launch_lb_wallforce(c, c->cur);
     if (!c->P.force_field) CK(cudaMemsetAsync(c->fs_force, 0, sizeof(double) * 3, c->stream));
@@ -752,7 +768,7 @@ int hb_lb_step(hb_ctx* c) {
 int hb_cycle(hb_ctx* c, int32_t nsteps) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
     if (nsteps < 0) return seterr(HB_ERR_ARG, "nsteps < 0");
-    int rc = run_cycles(c, nsteps, true);
+    int rc = run_cycles(c, nsteps, c->mirror);
     if (rc) return rc;
     CK(cudaGetLastError());
     return HB_OK;
@@ -806,6 +822,7 @@ int hb_synchronize(hb_ctx* c) {
 int hb_download_lattice(hb_ctx* c, uint8_t* type, uint8_t* inside, uint32_t* solid, double* f, double* n,
                         double* u, double* mass, double* visc, double* hydro_force) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
+    if ((n || u || hydro_force) && need_mirror(c)) return HB_ERR_STATE;
     CK(cudaStreamSynchronize(c->stream));
     const long long N = c->N;
     if (type || inside) {
@@ -1132,7 +1149,7 @@ int hb_get_status(hb_ctx* c, hb_status* s) {
         s->mass_surplus = sc[0];
         s->interface_cells = (int64_t)sc[1];
     }
-    if (c->P.lb_solve) {
+    if (c->P.lb_solve && c->mirror_valid) {  // else active_nodes and total_mass stay 0
         hb_export ex;
         const int rc = hb_export_values(c, &ex);
         if (rc) return rc;
@@ -1144,6 +1161,7 @@ int hb_get_status(hb_ctx* c, hb_status* s) {
 
 int hb_export_values(hb_ctx* c, hb_export* out) {
     if (!c || !out || !c->initialized) return seterr(HB_ERR_ARG, "null argument or not initialised");
+    if (need_mirror(c)) return HB_ERR_STATE;
     if (hb::io_prepare(c)) return seterr(HB_ERR_CUDA, "output mirror: %s", cudaGetErrorString(cudaGetLastError()));
     if (c->reduce_pending) launch_couple_reduce(c);      // FHydro of the last lattice step (LB.cpp:1851-1919)
     if (c->d.E > 0 && c->d.react) hb::launch_reactions(c);  // objects' FParticle of the last substep
@@ -1180,6 +1198,7 @@ int hb_vtk_fluid_fields(hb_ctx* c, int8_t* type, double* v, double* pressure, do
                         uint32_t* solid_index) {
     if (!c || !c->initialized) return seterr(HB_ERR_STATE, "not initialised");
     if (!c->P.lb_solve) return seterr(HB_ERR_STATE, "no lattice (lbSolve = 0)");
+    if (need_mirror(c)) return HB_ERR_STATE;
     if (hb::io_prepare(c)) return seterr(HB_ERR_CUDA, "output mirror: %s", cudaGetErrorString(cudaGetLastError()));
     const long long N = c->N;
     // one device block for the requested arrays, one copy per array
@@ -1305,6 +1324,7 @@ int hb_profile_phases(hb_ctx* c, int32_t nsteps, double* us, int32_t* nphases) {
         ++c->steps;
     }
     CK(cudaStreamSynchronize(c->stream));
+    if (c->mode_val != 1) c->mirror_valid = !c->P.lb_solve;
     std::vector<unsigned long long> h((size_t)np * nsteps);
     CK(cudaMemcpy(h.data(), ts, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost));
     cudaFree(ts);
@@ -1335,6 +1355,7 @@ int hb_time_cycles(hb_ctx* c, int32_t nsteps, float* ms_total, float* ms_lb_kern
     // whole cycles replayed from the graphs
     CK(cudaMemsetAsync(c->mode, 0, sizeof(int), c->stream));
     c->mode_val = 0;
+    c->mirror_valid = !c->P.lb_solve;
     CK(cudaEventRecord(c->ev0, c->stream));
     for (int s = 0; s < nsteps; ++s) {
         CK(cudaGraphLaunch(c->gexec[c->cur], c->stream));

@@ -39,7 +39,7 @@ struct Buf {
 struct Header {
     int64_t N, E, O, steps;
     int32_t cur;
-    uint8_t reduce_pending, dem_stepped, pad[2];
+    uint8_t reduce_pending, dem_stepped, mirror_valid, pad;
 };
 
 // Every buffer whose contents a later step reads.  Scratch that each step rewrites
@@ -144,7 +144,7 @@ int hb_checkpoint_save(hb_ctx* c, const char* path) {
     f.write(reinterpret_cast<const char*>(&c->P), ps);
     Header h = {};
     h.N = c->N; h.E = c->d.E; h.O = c->d.O_std; h.steps = c->steps; h.cur = c->cur;
-    h.reduce_pending = c->reduce_pending; h.dem_stepped = c->dem_stepped;
+    h.reduce_pending = c->reduce_pending; h.dem_stepped = c->dem_stepped; h.mirror_valid = c->mirror_valid;
     f.write(reinterpret_cast<const char*>(&h), sizeof(h));
     {  // the cylinders (host data: they define the curved walls the loader rebuilds)
         char nm[24] = "cylinders";
@@ -274,6 +274,7 @@ int hb_checkpoint_load(const char* path, hb_ctx** out) {
     c->steps = h.steps;
     c->reduce_pending = h.reduce_pending != 0;
     c->dem_stepped = h.dem_stepped != 0;
+    c->mirror_valid = h.mirror_valid != 0;
     if (c->io_part) {  // output-mirror marks are rebuilt from the restored types on demand
         cudaFree(c->io_linked);
         cudaFree(c->io_part);

@@ -172,6 +172,8 @@ struct hb_ctx {
     cudaGraphNode_t mask_node[2] = {nullptr, nullptr};  // the mask kernel in graph / graph2 (carries lbF)
     bool force_dirty = false;    // lbF changed through the graphs' nodes, lb_force not yet written
     int mode_val = -1;           // value last written to *mode (-1: unknown)
+    bool mirror = true;          // hb_cycle's last step writes every node's rho, u, hydroForce
+    bool mirror_valid = true;    // those node fields are the last step's (downloads need them)
     // element sink (hb_set_element_sink): device aliases of mapped host arrays the cycle
     // graphs fill at the end of every cycle, in the order of hb_download_elements
     double* sink[11] = {};

@@ -41,6 +41,7 @@ def lib():
     L.hb_host_register.argtypes = [vp, C.c_size_t]
     L.hb_host_unregister.argtypes = [vp]
     L.hb_set_element_sink.argtypes = [vp] + [vp] * 11
+    L.hb_set_lattice_mirror.argtypes = [vp, C.c_int32]
     L.hb_download_pairs.argtypes = [vp, vp, C.c_int64, P(C.c_int64)]
     L.hb_download_ghosts.argtypes = [vp, vp, vp, C.c_int64, P(C.c_int64)]
     L.hb_download_interface.argtypes = [vp, vp, C.c_int64, P(C.c_int64)]

@@ -215,8 +215,18 @@ int hb_dem_step(hb_ctx* ctx);        /* DEM::discreteElementStep        DEM.cpp:
 int hb_fs_step(hb_ctx* ctx);         /* LB::latticeBoltzmannFreeSurfaceStep LB.cpp:235-245 */
 int hb_coupling_step(hb_ctx* ctx);   /* LB::latticeBoltzmannCouplingStep LB.cpp:247-280  */
 int hb_lb_step(hb_ctx* ctx);         /* LB::latticeBolzmannStep         LB.cpp:221-233  */
-/* nsteps whole cycles (DEM, free surface, coupling, LB) replayed from one CUDA graph. */
+/* nsteps whole cycles (DEM, free surface, coupling, LB) replayed from one CUDA graph.  The
+ * last cycle of the call also writes every node's density, velocity and hydrodynamic force
+ * (the reference's node fields, which hb_download_lattice, hb_export_values and the VTK
+ * writer read) unless the lattice mirror is off. */
 int hb_cycle(hb_ctx* ctx, int32_t nsteps);
+/* on (default, 1): hb_cycle's last cycle writes the node fields as above; off (0): the
+ * cycles write them only where a later phase of the step reads them (the state itself is
+ * the same), for a driver that reads element state only.  While the last cycles ran with
+ * the mirror off (or through hb_time_cycles / hb_profile_phases), the entry points that
+ * read those node fields return HB_ERR_STATE and hb_get_status leaves active_nodes and
+ * total_mass at 0. */
+int hb_set_lattice_mirror(hb_ctx* ctx, int32_t on);
 /* The context's parameters (as last set: lbF follows hb_set_body_force) and its element
  * and object counts; any pointer may be NULL. */
 int hb_get_params(hb_ctx* ctx, hb_params* out, int32_t* elements, int32_t* objects);

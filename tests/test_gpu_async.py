@@ -111,3 +111,33 @@ def test_body_force_change_matches_oracle(spheres):
         assert rel_linf(eg["FHydro"], eo["FHydro"]) <= 1e-10
     g.close()
     o.close()
+
+
+def test_lattice_mirror_off_keeps_the_state_and_guards_the_node_fields():
+    """hb_set_lattice_mirror(ctx, 0): the cycles skip writing every node's rho, u and
+    hydroForce; the populations, node types and element state stay bit-identical to a
+    mirrored run, the node-field downloads report HB_ERR_STATE until a mirrored cycle has
+    run, and then equal the mirrored run's."""
+    from hybird_gb300.gpu import HbError, check
+    a, b = _sim(), _sim()
+    check(a.L.hb_set_lattice_mirror(a.h, 0))
+    a.cycle(5)
+    b.cycle(5)
+    la, lb = a.lattice(("type", "f")), b.lattice(("type", "f"))
+    np.testing.assert_array_equal(la["type"], lb["type"])
+    np.testing.assert_array_equal(la["f"], lb["f"])
+    ea, eb = a.elements(), b.elements()
+    for k in ("x0", "x1", "FHydro", "MHydro"):
+        np.testing.assert_array_equal(ea[k], eb[k], err_msg=k)
+    with pytest.raises(HbError):
+        a.lattice(("n", "u"))
+    with pytest.raises(HbError):
+        a.export_values()
+    check(a.L.hb_set_lattice_mirror(a.h, 1))
+    a.cycle(1)
+    b.cycle(1)
+    la, lb = a.lattice(("n", "u", "hydroForce")), b.lattice(("n", "u", "hydroForce"))
+    for k in ("n", "u", "hydroForce"):
+        np.testing.assert_array_equal(la[k], lb[k], err_msg=k)
+    a.close()
+    b.close()
