@@ -195,27 +195,27 @@ __device__ __forceinline__ void adj_local(const R* g, R* mu, R Awall, const Mac<
     for (int k = 0; k < Q; ++k) mu[k] += A + R(cx(k)) * bx + R(cy(k)) * by + R(cz(k)) * bz;
 }
 
-// Deterministic block sum of nv per-thread values into part[blk*NPART + off ...]:
-// warp shuffle in R, warps combined in FP64 in warp order, added to the block's slot.
+// Deterministic block sum of nv per-thread values into part[blk*NPART + off ...]: warp
+// shuffles in R, the warps combined in R in warp order by one thread per value, added to
+// the block's FP64 slot.  (Combining them in FP64 on one thread cost a serial chain of
+// FP64 additions per block on this part's narrow FP64 pipe.)
 template <class R>
 __device__ __forceinline__ void block_accumulate(R* v, int nv, int off, double* part) {
-    __shared__ double sh[NPART][AMAXW];
+    __shared__ R sh[NPART][AMAXW];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int k = 0; k < nv; ++k) {
         R x = v[k];
 #pragma unroll
         for (int s = 16; s > 0; s >>= 1) x += __shfl_down_sync(0xffffffffu, x, s);
-        if (lane == 0) sh[k][wid] = (double)x;
+        if (lane == 0) sh[k][wid] = x;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if ((int)threadIdx.x < nv) {
         const int nw = (blockDim.x + 31) >> 5;
         const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-        for (int k = 0; k < nv; ++k) {
-            double t = 0.0;
-            for (int w = 0; w < nw; ++w) t += sh[k][w];
-            part[blk * NPART + off + k] += t;
-        }
+        R t = R(0);
+        for (int w = 0; w < nw; ++w) t += sh[threadIdx.x][w];
+        part[blk * NPART + off + threadIdx.x] += (double)t;
     }
 }
 

@@ -974,23 +974,31 @@ __device__ void newton_one(const DemArgs& a, int i, PredBuf pb) {
 // for these elements (a single sphere has three equal principal moments), so the result
 // does not depend on which value is read.
 __device__ double newton_plain(const DemArgs& a, int i, int c, PredBuf pb, double fa, double fb) {
+    // One instruction stream for the position lanes (c < 3) and the spin lanes (c >= 3),
+    // with selected operands: an FP64 warp instruction costs the same narrow-pipe time
+    // whatever its active lanes, so the two chains are not run one after the other.  Per
+    // lane the operations and their order are those of the chain it takes:
+    //   position: x1 (-6 pi nv ri) + FH + fa + fb, / m, + demF
+    //   spin:     w (-8 pi nv ri ri ri) + MH + fa + fb + (I_a - I_b) w_a w_b, / I_k
     const int E = a.E;
-    const double ri = a.rad[i];
-    const double nv = a.numVisc;
-    if (c < 3) {
-        const long long o = (long long)c * E + i;
-        const double fv = pb.x1r[o] * (-6.0 * M_PI * nv * ri);
-        return (((fv + a.FH[o]) + fa) + fb) / a.m[i] + a.demF[c];
-    }
-    const int k = c - 3;
+    const bool lin = c < 3;
+    const int k = lin ? c : c - 3;
     const long long o = (long long)k * E + i;
-    const double mv = pb.wGr[o] * (-8.0 * M_PI * nv * ri * ri * ri);
-    const double mom = ((mv + a.MH[o]) + fa) + fb;
-    const double Ix = a.I[i], Iy = a.I[E + i], Iz = a.I[2 * E + i];
-    const double wx = a.wpL[i], wy = a.wpL[E + i], wz = a.wpL[2 * E + i];
-    if (k == 0) return (mom + (Iy - Iz) * wy * wz) / Ix;
-    if (k == 1) return (mom + (Iz - Ix) * wz * wx) / Iy;
-    return (mom + (Ix - Iy) * wx * wy) / Iz;
+    const double ri = a.rad[i];
+    const double t1 = (lin ? -6.0 * M_PI : -8.0 * M_PI) * a.numVisc;
+    const double t2 = t1 * ri;
+    const double t4 = (t2 * ri) * ri;
+    const double vel = lin ? pb.x1r[o] : pb.wGr[o];
+    const double H = lin ? a.FH[o] : a.MH[o];
+    const double num = ((vel * (lin ? t2 : t4) + H) + fa) + fb;
+    // Euler term of the spin chain (k: (y, z), (z, x), (x, y))
+    const int ka = k == 0 ? 1 : (k == 1 ? 2 : 0), kb = k == 0 ? 2 : (k == 1 ? 0 : 1);
+    const double Ia = a.I[(long long)ka * E + i], Ib = a.I[(long long)kb * E + i];
+    const double wa = a.wpL[(long long)ka * E + i], wb = a.wpL[(long long)kb * E + i];
+    const double eul = num + (Ia - Ib) * wa * wb;
+    const double q = (lin ? num : eul) / (lin ? a.m[i] : a.I[o]);
+    const double qd = q + a.demF[k];
+    return lin ? qd : q;
 }
 
 __device__ void predict_one(const DemArgs& a, int i) {  // elmt.cpp:139-177
@@ -1749,11 +1757,37 @@ __device__ __noinline__ void reduce_block(const CoupleArgs& a, int p0, double (*
 
 // the reduced-precision lattice kernels leave the same seven sums as 64-bit fixed-point
 // integers; converting them is the whole reduction
+// (double)v * 2^-38 for the 64-bit two's-complement fixed-point value v, from its bits
+// with integer instructions: the conversion rounds to nearest even as the hardware's
+// int64 -> double conversion does, and the scaling only moves the exponent (|v| 2^-38 is
+// normal for every v != 0), so the result is that expression's bit for bit without an
+// instruction on the narrow FP64 pipe.
+__device__ __forceinline__ double fixed_to_double(unsigned long long u) {
+    if (u == 0ull) return 0.0;
+    const unsigned long long sgn = u & 0x8000000000000000ull;
+    const unsigned long long m = sgn ? 0ull - u : u;
+    const int msb = 63 - __clzll((long long)m);
+    int e = msb - 38;
+    unsigned long long mant;
+    if (msb <= 52) {
+        mant = m << (52 - msb);
+    } else {
+        const int sh = msb - 52;
+        const unsigned long long q = m >> sh, rem = m & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        mant = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+        if (mant >> 53) {
+            mant >>= 1;
+            e += 1;
+        }
+    }
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
 __device__ __forceinline__ void convert_sums(const CoupleArgs& a, int p) {
     const int E = a.E;
     double v[7];
 #pragma unroll
-    for (int k = 0; k < 7; ++k) v[k] = (double)(long long)a.hacc[(long long)k * E + p] * HACC_INV;
+    for (int k = 0; k < 7; ++k) v[k] = fixed_to_double(a.hacc[(long long)k * E + p]);
     a.FH[p] = v[0]; a.FH[E + p] = v[1]; a.FH[2 * E + p] = v[2];
     a.MH[p] = v[3]; a.MH[E + p] = v[4]; a.MH[2 * E + p] = v[5];
     a.fvol[p] = v[6];
@@ -1875,7 +1909,7 @@ __global__ void __launch_bounds__(256, PBC ? 2 : 1) k_cycle(CycleArgs A) {
     stamp(A, 0);
     if (A.do_reduce) {
         if (A.c.hacc) {
-            for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) convert_sums(A.c, p);
+            for (int p = gt; p < E; p += gs) convert_sums(A.c, p);
         } else {
             for (int p = blockIdx.x; p < E; p += gridDim.x) reduce_block(*A.gc, p, sh);
         }
@@ -1977,17 +2011,28 @@ __global__ void __launch_bounds__(256, PBC ? 2 : 1) k_cycle(CycleArgs A) {
             // shuffles, then one 64-bit atomicMax per warp into this substep's slot
             // (non-negative doubles order like their bit patterns; a maximum does not
             // depend on the order), read back by every thread after the barrier
-            for (int off = 16; off > 0; off >>= 1) v2 = fmax(v2, __shfl_xor_sync(0xffffffffu, v2, off));
-            if (lane == 0 && v2 > 0.0) atomicMax(vmax + s, (unsigned long long)__double_as_longlong(v2));
+            unsigned long long vb = (unsigned long long)__double_as_longlong(v2);  // v2 >= 0, never NaN
+            for (int off = 16; off > 0; off >>= 1) vb = max(vb, __shfl_xor_sync(0xffffffffu, vb, off));
+            if (lane == 0 && vb != 0ull) atomicMax(vmax + s, vb);
             grid.sync();
             stamp(A, k++);
             {
-                const double mx = __longlong_as_double((long long)((volatile unsigned long long*)vmax)[s]);
-                double md = maxDisp + sqrt(mx) * A.d.dt;
-                const bool rb = md > A.d.trigger;
-                if (rb) md = 0.0;
-                maxDisp = md;
-                rebuild = rb;
+                // one thread per block evaluates the trigger (FP64 square root and compare:
+                // narrow-pipe instructions that every warp would otherwise repeat), the
+                // block takes it from shared memory; every block gets the same value
+                __shared__ double s_md;
+                __shared__ int s_rb;
+                if (threadIdx.x == 0) {
+                    const double mx = __longlong_as_double((long long)((volatile unsigned long long*)vmax)[s]);
+                    double md = maxDisp + sqrt(mx) * A.d.dt;
+                    const bool rb = md > A.d.trigger;
+                    if (rb) md = 0.0;
+                    s_md = md;
+                    s_rb = rb ? 1 : 0;
+                }
+                __syncthreads();
+                maxDisp = s_md;
+                rebuild = s_rb != 0;
             }
         }
         if (!PBC && (A.multi & 1)) {
@@ -2004,8 +2049,8 @@ __global__ void __launch_bounds__(256, PBC ? 2 : 1) k_cycle(CycleArgs A) {
         }
         if (A.do_boxes) {  // positions are final: boxes for the coupling passes
             if (PBC) part_boxes(A.gc, A.gd);
-            else
-                for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) build_box(A.c, p);
+            else  // spread over the blocks: the sphere table's FP64 work lands on every SM
+                for (int p = gt; p < E; p += gs) build_box(A.c, p);
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             A.d.scal[0] = maxDisp;
