@@ -758,7 +758,17 @@ __device__ __forceinline__ void forces_group(const DemArgs& a, const DemArgs& ga
 #pragma unroll
         for (int off = 1; off < 8; off <<= 1)
 #pragma unroll
-            for (int q = 0; q < 12; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
+            for (int q = 0; q < 6; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
+        if (a.O > 0) {  // object contacts can sit in any lane
+#pragma unroll
+            for (int off = 1; off < 8; off <<= 1)
+#pragma unroll
+                for (int q = 6; q < 12; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
+        } else {  // wall and cylinder forces sit in the group's first lane only (never -0.0,
+                  // so the tree's additions of +0.0 would leave them as they are)
+#pragma unroll
+            for (int q = 6; q < 12; ++q) v[q] = __shfl_sync(0xffffffffu, v[q], threadIdx.x & 24);
+        }
     } else {  // the group's first lane holds the totals: hand them to the other seven
 #pragma unroll
         for (int q = 0; q < 12; ++q) v[q] = __shfl_sync(0xffffffffu, v[q], threadIdx.x & 24);
@@ -1757,37 +1767,11 @@ __device__ __noinline__ void reduce_block(const CoupleArgs& a, int p0, double (*
 
 // the reduced-precision lattice kernels leave the same seven sums as 64-bit fixed-point
 // integers; converting them is the whole reduction
-// (double)v * 2^-38 for the 64-bit two's-complement fixed-point value v, from its bits
-// with integer instructions: the conversion rounds to nearest even as the hardware's
-// int64 -> double conversion does, and the scaling only moves the exponent (|v| 2^-38 is
-// normal for every v != 0), so the result is that expression's bit for bit without an
-// instruction on the narrow FP64 pipe.
-__device__ __forceinline__ double fixed_to_double(unsigned long long u) {
-    if (u == 0ull) return 0.0;
-    const unsigned long long sgn = u & 0x8000000000000000ull;
-    const unsigned long long m = sgn ? 0ull - u : u;
-    const int msb = 63 - __clzll((long long)m);
-    int e = msb - 38;
-    unsigned long long mant;
-    if (msb <= 52) {
-        mant = m << (52 - msb);
-    } else {
-        const int sh = msb - 52;
-        const unsigned long long q = m >> sh, rem = m & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
-        mant = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
-        if (mant >> 53) {
-            mant >>= 1;
-            e += 1;
-        }
-    }
-    return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
-}
-
 __device__ __forceinline__ void convert_sums(const CoupleArgs& a, int p) {
     const int E = a.E;
     double v[7];
 #pragma unroll
-    for (int k = 0; k < 7; ++k) v[k] = fixed_to_double(a.hacc[(long long)k * E + p]);
+    for (int k = 0; k < 7; ++k) v[k] = (double)(long long)a.hacc[(long long)k * E + p] * HACC_INV;
     a.FH[p] = v[0]; a.FH[E + p] = v[1]; a.FH[2 * E + p] = v[2];
     a.MH[p] = v[3]; a.MH[E + p] = v[4]; a.MH[2 * E + p] = v[5];
     a.fvol[p] = v[6];
@@ -1909,7 +1893,7 @@ __global__ void __launch_bounds__(256, PBC ? 2 : 1) k_cycle(CycleArgs A) {
     stamp(A, 0);
     if (A.do_reduce) {
         if (A.c.hacc) {
-            for (int p = gt; p < E; p += gs) convert_sums(A.c, p);
+            for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) convert_sums(A.c, p);
         } else {
             for (int p = blockIdx.x; p < E; p += gridDim.x) reduce_block(*A.gc, p, sh);
         }
@@ -2050,7 +2034,7 @@ __global__ void __launch_bounds__(256, PBC ? 2 : 1) k_cycle(CycleArgs A) {
         if (A.do_boxes) {  // positions are final: boxes for the coupling passes
             if (PBC) part_boxes(A.gc, A.gd);
             else  // spread over the blocks: the sphere table's FP64 work lands on every SM
-                for (int p = gt; p < E; p += gs) build_box(A.c, p);
+                for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < E; p += gridDim.x * blockDim.x) build_box(A.c, p);
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             A.d.scal[0] = maxDisp;

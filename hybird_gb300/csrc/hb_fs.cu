@@ -223,7 +223,8 @@ __global__ void __launch_bounds__(256) k_fs_mass_list(FsArgs a) {
             if (t == HB_T_INTERFACE) av = 0.5 * (a.mass[l] + mi);
             else if (t == HB_T_FLUID) av = 1.0;
             else if (t == HB_T_DYNWALL) av = 1.0 * mi;  // gas, static walls: averageMass 0
-            if (av == 0.0) continue;
+            // av == 0 (either sign) by the bits: an FP64 compare would take the narrow pipe
+            if (((unsigned long long)__double_as_longlong(av) << 1) == 0ull) continue;
             double diff;
             if (t == HB_T_DYNWALL) {  // f[opp j] = fs[j] - BBi: the difference is -BBi
                 const double fin = fval<P>(a, opp(j), i);
