@@ -315,7 +315,7 @@ def lattice_traffic(prec):
     try:
         with open(os.path.join(REPO, "profiles", "lattice_kernel_traffic.json")) as fh:
             d = json.load(fh)
-        return d["dram_bytes_per_launch"].get(DTYPE[prec])
+        return d["dram_bytes_per_launch"].get({0: "f64", 1: "f32", 2: "f16s"}[prec])
     except (OSError, KeyError, ValueError):
         return None
 

@@ -77,7 +77,7 @@ class HbObjects(C.Structure):
 
 class HbStatus(C.Structure):
     _fields_ = [("numeric_error", C.c_int32), ("capacity_error", C.c_int32),
-                ("wait_timeout", C.c_int32), ("reserved", C.c_int32),
+                ("unsupported_link", C.c_int32), ("reserved", C.c_int32),
                 ("interface_cells", C.c_int64), ("active_nodes", C.c_int64),
                 ("pairs", C.c_int64), ("contacts", C.c_int64),
                 ("mass_surplus", C.c_double), ("total_mass", C.c_double)]

@@ -1132,7 +1132,7 @@ int hb_get_status(hb_ctx* c, hb_status* s) {
     memset(s, 0, sizeof(*s));
     s->numeric_error = st[0];
     s->capacity_error = st[2];
-    s->wait_timeout = st[3];
+    s->unsupported_link = st[1];
     if (c->d.E > 0) {
         int k = 0;
         CK(cudaMemcpy(&k, c->d.contacts, sizeof(int), cudaMemcpyDeviceToHost));

@@ -98,6 +98,13 @@ struct PolF32 {
     __device__ static __forceinline__ void store(S* p, T v) { HB_ST(p, v); }
     __device__ static __forceinline__ S enc(T v) { return v; }
     __device__ static __forceinline__ S enc_store(T v) { return v; }
+    // the stored value itself (units of UNIT per deviation): the lattice kernel computes on
+    // these, so FP16 storage needs no scaling per load and store
+    static constexpr float UNIT = 1.0f;
+    static constexpr float INVU = 1.0f;
+    __device__ static __forceinline__ T load_raw(const S* p) { return HB_LD(p); }
+    __device__ static __forceinline__ S enc_raw(T v) { return v; }
+    __device__ static __forceinline__ void store_raw(S* p, T v) { HB_ST(p, v); }
 };
 struct PolF16 {
     using S = __half;
@@ -113,6 +120,15 @@ struct PolF16 {
         HB_ST(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(v * SCALE)));
     }
     __device__ static __forceinline__ S enc_store(T v) { return __float2half_rn(v * SCALE); }
+    static constexpr float UNIT = SCALE;
+    static constexpr float INVU = INV;
+    __device__ static __forceinline__ T load_raw(const S* p) {
+        return __half2float(__ushort_as_half(HB_LD(reinterpret_cast<const unsigned short*>(p))));
+    }
+    __device__ static __forceinline__ S enc_raw(T v) { return __float2half_rn(v); }
+    __device__ static __forceinline__ void store_raw(S* p, T v) {
+        HB_ST(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(v)));
+    }
 };
 
 // ---- device-side views of the context ----------------------------------------------

@@ -85,8 +85,8 @@ __device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fou
         const float wx = q1.z, wy = q1.w, wz = q2.x;
         const float vx = q0.w + (wy * rz - wz * ry), vy = q1.x + (wz * rx - wx * rz), vz = q1.y + (wx * ry - wy * rx);
         const float BBi = 6.0f * n * float(wgt(j)) * cdot(j, vx, vy, vz);
-        P::store(fout + o * N + i, g - BBi);
-        const float sc = 2.0f * g - BBi;
+        P::store_raw(fout + o * N + i, g - P::UNIT * BBi);
+        const float sc = (2.0f * g - P::UNIT * BBi) * P::INVU;
         const float fx = float(cx(j)) * sc, fy = float(cy(j)) * sc, fz = float(cz(j)) * sc;
         const float v6[6] = {fx, fy, fz, ry * fz - rz * fy, rz * fx - rx * fz, rx * fy - ry * fx};
         if (mkey < 0) mkey = pl;
@@ -99,17 +99,17 @@ __device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fou
             for (int k = 0; k < 6; ++k) atomicAdd(a.hacc + (long long)k * E + pl, to_fixed(v6[k]));
         }
     } else if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
-        P::store(fout + j * N + l, g);
+        P::store_raw(fout + j * N + l, g);
     } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN || lc == HB_T_CURVED) {
         // slip and curved walls: completed after the kernel (hb_slip.cu, hb_curved.cu)
-        P::store(fout + o * N + i, g);
+        P::store_raw(fout + o * N + i, g);
     } else if (lc == HB_T_GAS) {
         const float vu = cdot(j, ux, uy, uz);
         const float w = float(wgt(j));
-        P::store(fout + o * N + i, -g + w * (9.0f * vu * vu - 3.0f * usq));
+        P::store_raw(fout + o * N + i, -g + (w * P::UNIT) * (9.0f * vu * vu - 3.0f * usq));
     } else if (lc == HB_T_DYNWALL) {
         const float uw = float(a.u[l] * cx(j) + a.u[a.N + l] * cy(j) + a.u[2 * a.N + l] * cz(j));
-        P::store(fout + o * N + i, g - 6.0f * n * float(wgt(j)) * uw);
+        P::store_raw(fout + o * N + i, g - (6.0f * P::UNIT) * n * float(wgt(j)) * uw);
     } else {
         flag_status(a.status, 1);
     }
@@ -164,6 +164,8 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
     const int mode = *a.mode;
     const uint8_t code = t & HB_TYPE_MASK;
 
+    // f holds the stored values (units of P::UNIT); the sums scale exactly by INVU (a power
+    // of two), so they equal the sums of the deviations bit for bit
     float dn = 0.0f, mx = 0.0f, my = 0.0f, mz = 0.0f;
 #pragma unroll
     for (int j = 0; j < Q; ++j) {
@@ -172,6 +174,7 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
         if (cy(j)) my += cy(j) > 0 ? f[j] : -f[j];
         if (cz(j)) mz += cz(j) > 0 ? f[j] : -f[j];
     }
+    dn *= P::INVU; mx *= P::INVU; my *= P::INVU; mz *= P::INVU;
     const float n = 1.0f + dn;
     const float inv = 1.0f / n;
     float ux = mx * inv, uy = my * inv, uz = mz * inv;
@@ -225,7 +228,7 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
             const float vu = cdot(j, ux, uy, uz);
             const float w = float(wgt(j));
             const float ep = w * (dn + n * (4.5f * vu * vu - 1.5f * usq));
-            const float d = (f[j] + f[o]) - 2.0f * ep;
+            const float d = (f[j] + f[o]) * P::INVU - 2.0f * ep;
             if (cx(j)) pxx += d;
             if (cy(j)) pyy += d;
             if (cz(j)) pzz += d;
@@ -262,14 +265,15 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
         const float w = q == 0 ? float(1.0 / 18.0) : float(1.0 / 36.0);
-        K0[q] = w * kb;
-        Kq[q] = 4.5f * wp * w * n;
-        Kc[q] = 9.0f * ap * w;
-        Lu[q] = 3.0f * wm * w * n;
-        Lf[q] = 3.0f * am * w;
+        // in units of P::UNIT, as f: the products scale exactly
+        K0[q] = (w * kb) * P::UNIT;
+        Kq[q] = (4.5f * wp * w * n) * P::UNIT;
+        Kc[q] = (9.0f * ap * w) * P::UNIT;
+        Lu[q] = (3.0f * wm * w * n) * P::UNIT;
+        Lf[q] = (3.0f * am * w) * P::UNIT;
     }
     S* fo = fout + i;
-    fo[0] = P::enc_store(2.0f * c1 * f[0] + float(wgt(0)) * kb);  // rest population
+    fo[0] = P::enc_raw(2.0f * c1 * f[0] + float(wgt(0)) * (kb * P::UNIT));  // rest population
 #pragma unroll
     for (int j = 1; j < Q; j += 2) {  // post-collision values replace f in place
         const int o = j + 1;
@@ -287,17 +291,17 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
     const unsigned warp = __activemask();
     if (__all_sync(warp, lm == 0ull)) {
 #pragma unroll
-        for (int j = 1; j < Q; ++j) fo[a.so[j]] = P::enc_store(f[j]);
+        for (int j = 1; j < Q; ++j) fo[a.so[j]] = P::enc_raw(f[j]);
     } else if (__all_sync(warp, special == 0u)) {
         // a static (or slip) wall returns the population into the node's own opposite slot
 #pragma unroll
-        for (int j = 1; j < Q; ++j) fo[(bb & (1u << j)) ? opp(j) * N : a.so[j]] = P::enc_store(f[j]);
+        for (int j = 1; j < Q; ++j) fo[(bb & (1u << j)) ? opp(j) * N : a.so[j]] = P::enc_raw(f[j]);
     } else {
 #pragma unroll
         for (int j = 1; j < Q; ++j) {
             if (special & (1u << j))
                 push_general<P, MBB>(a, fout, x, y, z, i, j, f[j], n, ux, uy, uz, usq, mv, mkey);
-            else fo[(bb & (1u << j)) ? opp(j) * N : a.so[j]] = P::enc_store(f[j]);
+            else fo[(bb & (1u << j)) ? opp(j) * N : a.so[j]] = P::enc_raw(f[j]);
         }
     }
 }
@@ -327,7 +331,7 @@ __global__ void __launch_bounds__(128, 9) k_collide_stream_dev(LBArgs a) {
     const int p = (a.couple && act && (t & HB_INSIDE)) ? (int)a.solid[i] : -1;
     float f[Q];
 #pragma unroll
-    for (int j = 0; j < Q; ++j) f[j] = act ? P::load(fin + a.jn[j] + i) : 0.0f;
+    for (int j = 0; j < Q; ++j) f[j] = act ? P::load_raw(fin + a.jn[j] + i) : 0.0f;
     float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, q2 = q0;
     if (p >= 0) {  // centre, velocity, spin
         const float4* pf4 = reinterpret_cast<const float4*>(a.parts.pf) + 3 * (size_t)p;

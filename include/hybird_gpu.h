@@ -141,7 +141,8 @@ typedef struct hb_objects {
 typedef struct hb_status {
     int32_t numeric_error;     /* NaN/Inf seen in rho or u                                   */
     int32_t capacity_error;    /* a device list overflowed                                   */
-    int32_t wait_timeout;      /* a bounded device wait gave up                              */
+    int32_t unsupported_link;  /* an active node linked to an unsupported node type (the
+                                  reference's TYPE ERROR exit, LB.cpp:1458-1461)            */
     int32_t reserved;
     int64_t interface_cells;   /* current interface count                                    */
     int64_t active_nodes;      /* fluid + interface nodes (activeNodes.size())               */

@@ -75,7 +75,7 @@ def test_config3_dam_break_full_size():
         m1, _ = _liquid_mass(g)
         g.cycle(200)
         st = g.status()
-        assert st.numeric_error == 0 and st.capacity_error == 0 and st.wait_timeout == 0
+        assert st.numeric_error == 0 and st.capacity_error == 0 and st.unsupported_link == 0
         m2, i2 = _liquid_mass(g)
         out[prec] = (m0, m1, m2, i0, i2, g.lattice(("type", "n", "u")))
         g.close()

@@ -136,3 +136,31 @@ def test_config3_slice_fp64_vs_oracle():
         assert rel_linf(ge[k], oe[k]) <= 1e-9, (k, rel_linf(ge[k], oe[k]))
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("config", ["c2", "c4"])
+def test_particles_move_less_than_half_a_node_per_step(config):
+    """The coupling masks let a node claimed in a pass join one step later instead of
+    claiming further nodes in the same pass (the reference appends it to the list it
+    walks, LB.cpp:1969-2033); the two agree unless a particle moves about half a lattice
+    unit in one step.  On the benchmark workloads (configuration 2 settling from rest,
+    configuration 4 at 256^3) the fastest element stays far below that: its speed, in
+    lattice units per step, is checked every 25 of 300 cycles (100 at 256^3)."""
+    from hybird_gb300.workloads import precision_box
+    G = _gpu()
+    if config == "c2":
+        p, sph = sedimentation(abi.HB_FP32)
+        cycles = 300
+    else:
+        p, sph = precision_box(abi.HB_FP32)
+        cycles = 100
+    g = G(p, sph)
+    vmax = 0.0
+    for _ in range(cycles // 25):
+        g.cycle(25)
+        e = g.elements()
+        v = np.asarray(e["x1"]).reshape(3, -1)
+        vmax = max(vmax, float(np.sqrt((v ** 2).sum(0)).max()))
+    g.close()
+    print(config, "largest element speed", vmax)
+    assert 0.0 < vmax < 0.25, vmax
