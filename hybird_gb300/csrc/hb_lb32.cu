@@ -19,8 +19,8 @@ namespace hb {
 // fixed offsets ne[j].  (Measured on GB300: the scattered push stores cost no more than
 // aligned or gathered ones; this kernel is bound by its instruction count.)
 
-__device__ __forceinline__ int link32(const LBArgs& a, int x, int y, int z, int j) {
-    int xn = x + cx(j), yn = y + cy(j), zn = z + cz(j);
+__device__ __forceinline__ int link32c(const LBArgs& a, int x, int y, int z, int kx, int ky, int kz) {
+    int xn = x + kx, yn = y + ky, zn = z + kz;
     if (xn == 0 && a.per[0]) xn = a.X - 2;
     else if (xn == a.X - 1 && a.per[1]) xn = 1;
     if (yn == 0 && a.per[2]) yn = a.Y - 2;
@@ -28,6 +28,9 @@ __device__ __forceinline__ int link32(const LBArgs& a, int x, int y, int z, int 
     if (zn == 0 && a.per[4]) zn = a.Z - 2;
     else if (zn == a.Z - 1 && a.per[5]) zn = 1;
     return xn + a.X * (yn + a.Y * zn);
+}
+__device__ __forceinline__ int link32(const LBArgs& a, int x, int y, int z, int j) {
+    return link32c(a, x, y, z, cx(j), cy(j), cz(j));
 }
 
 // c_j . v with the zero components of c_j left out: without fast-math the compiler keeps
@@ -63,31 +66,82 @@ __device__ __forceinline__ unsigned long long to_fixed(float v) {
 // LB.cpp:1231-1356 seen from the sending node.  (A form with selected target index and
 // value, keeping the lanes of a warp converged, measured slower on GB300 than this
 // branch chain.)
-template <class P, bool MBB>
+template <class P>
 __device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fout, int x, int y, int z, int i,
-                                             int j, float g, float n, float ux, float uy, float uz, float usq,
-                                             float* mv, int& mkey) {
+                                             int j, float g, float n, float ux, float uy, float uz, float usq) {
     const int l = link32(a, x, y, z, j);
-    const uint8_t tl = a.ntype[l];
-    const uint8_t lc = tl & HB_TYPE_MASK;
+    const uint8_t lc = a.ntype[l] & HB_TYPE_MASK;
     const int o = opp(j);
     const int N = (int)a.N;
-    if (MBB && (tl & HB_INSIDE) && (lc == HB_T_FLUID || lc == HB_T_INTERFACE)) {
-        // moving bounce-back on a particle: BBi = 6 n w_j (u . c_j) with u the particle's
-        // velocity at the solid node, from its FP32 record (centre, velocity, spin); no
-        // link wraps in this mode.  The link's momentum exchange (2 (fs_j - w_j) - BBi) c_j
-        // (g = fs_j - w_j) and its moment about the element centre go to the node's sums
-        // for its first particle, or straight to another particle's fixed-point sums.
+    if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
+        P::store_raw(fout + j * N + l, g);
+    } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN || lc == HB_T_CURVED) {
+        // slip and curved walls: completed after the kernel (hb_slip.cu, hb_curved.cu)
+        P::store_raw(fout + o * N + i, g);
+    } else if (lc == HB_T_GAS) {
+        const float vu = cdot(j, ux, uy, uz);
+        const float w = float(wgt(j));
+        P::store_raw(fout + o * N + i, -g + (w * P::UNIT) * (9.0f * vu * vu - 3.0f * usq));
+    } else if (lc == HB_T_DYNWALL) {
+        const float uw = float(a.u[l] * cx(j) + a.u[a.N + l] * cy(j) + a.u[2 * a.N + l] * cz(j));
+        P::store_raw(fout + o * N + i, g - (6.0f * P::UNIT) * n * float(wgt(j)) * uw);
+    } else {
+        flag_status(a.status, 1);
+    }
+}
+
+// Direction components of a link index known only at run time: 2-bit fields c + 1.
+__host__ __device__ constexpr unsigned long long dir_bits(int k) {
+    unsigned long long r = 0;
+    for (int j = 0; j < Q; ++j)
+        r |= (unsigned long long)((k == 0 ? cx(j) : (k == 1 ? cy(j) : cz(j))) + 1) << (2 * j);
+    return r;
+}
+__device__ __forceinline__ int dir_rt(int k, int j) {
+    constexpr unsigned long long B[3] = {dir_bits(0), dir_bits(1), dir_bits(2)};
+    return (int)((B[k] >> (2 * j)) & 3ull) - 1;
+}
+// cdot for a run-time link: the same terms, signs and order of additions
+__device__ __forceinline__ float cdot_rt(int kx, int ky, int kz, float vx, float vy, float vz) {
+    float r = kx != 0 ? (kx > 0 ? vx : -vx) : (ky != 0 ? (ky > 0 ? vy : -vy) : (kz > 0 ? vz : -vz));
+    if (kx != 0 && ky != 0) r = ky > 0 ? r + vy : r - vy;
+    if ((kx != 0 || ky != 0) && kz != 0) r = kz > 0 ? r + vz : r - vz;
+    return r;
+}
+
+// push_general of the moving-bounce-back kernel, out of line with the link index j
+// (1..18) as a run-time value.  Next to particle surfaces most warps take the general
+// push for several links; 18 inlined copies of this body (one per unrolled link) made
+// the kernel instruction-fetch bound (no_instructions 51 % of the stall samples, local
+// spills at 56 registers).  The arithmetic is push_general's, plus the particle links:
+// BBi = 6 n w_j (u . c_j) with u the particle's velocity at the solid node, from its
+// FP32 record (centre, velocity, spin); no link wraps in this mode.  The link's momentum
+// exchange (2 (fs_j - w_j) - BBi) c_j (g = fs_j - w_j) and its moment about the element
+// centre go to the node's sums mv for its first particle *mkey, or straight to another
+// particle's fixed-point sums.
+template <class P>
+__device__ __forceinline__ void push_link_mbb(const LBArgs& a, int x, int y, int z, int i, int j, float g,
+                                              float n, float ux, float uy, float uz, float usq, float* mv,
+                                              int& mkey) {
+    typename P::S* fout = reinterpret_cast<typename P::S*>(a.fout);
+    const int kx = dir_rt(0, j), ky = dir_rt(1, j), kz = dir_rt(2, j);
+    const int l = link32c(a, x, y, z, kx, ky, kz);
+    const uint8_t tl = a.ntype[l];
+    const uint8_t lc = tl & HB_TYPE_MASK;
+    const int o = (j & 1) ? j + 1 : j - 1;
+    const int N = (int)a.N;
+    const float w = j <= 6 ? float(wgt(1)) : float(wgt(7));
+    if ((tl & HB_INSIDE) && (lc == HB_T_FLUID || lc == HB_T_INTERFACE)) {
         const int pl = (int)a.solid[l];
         const float4* pf4 = reinterpret_cast<const float4*>(a.parts.pf) + 3 * (size_t)pl;
         const float4 q0 = pf4[0], q1 = pf4[1], q2 = pf4[2];
-        const float rx = float(x + cx(j)) - q0.x, ry = float(y + cy(j)) - q0.y, rz = float(z + cz(j)) - q0.z;
+        const float rx = float(x + kx) - q0.x, ry = float(y + ky) - q0.y, rz = float(z + kz) - q0.z;
         const float wx = q1.z, wy = q1.w, wz = q2.x;
         const float vx = q0.w + (wy * rz - wz * ry), vy = q1.x + (wz * rx - wx * rz), vz = q1.y + (wx * ry - wy * rx);
-        const float BBi = 6.0f * n * float(wgt(j)) * cdot(j, vx, vy, vz);
+        const float BBi = 6.0f * n * w * cdot_rt(kx, ky, kz, vx, vy, vz);
         P::store_raw(fout + o * N + i, g - P::UNIT * BBi);
         const float sc = (2.0f * g - P::UNIT * BBi) * P::INVU;
-        const float fx = float(cx(j)) * sc, fy = float(cy(j)) * sc, fz = float(cz(j)) * sc;
+        const float fx = float(kx) * sc, fy = float(ky) * sc, fz = float(kz) * sc;
         const float v6[6] = {fx, fy, fz, ry * fz - rz * fy, rz * fx - rx * fz, rx * fy - ry * fx};
         if (mkey < 0) mkey = pl;
         if (pl == mkey) {
@@ -101,15 +155,13 @@ __device__ __forceinline__ void push_general(const LBArgs& a, typename P::S* fou
     } else if (lc == HB_T_FLUID || lc == HB_T_INTERFACE) {
         P::store_raw(fout + j * N + l, g);
     } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN || lc == HB_T_CURVED) {
-        // slip and curved walls: completed after the kernel (hb_slip.cu, hb_curved.cu)
         P::store_raw(fout + o * N + i, g);
     } else if (lc == HB_T_GAS) {
-        const float vu = cdot(j, ux, uy, uz);
-        const float w = float(wgt(j));
+        const float vu = cdot_rt(kx, ky, kz, ux, uy, uz);
         P::store_raw(fout + o * N + i, -g + (w * P::UNIT) * (9.0f * vu * vu - 3.0f * usq));
     } else if (lc == HB_T_DYNWALL) {
-        const float uw = float(a.u[l] * cx(j) + a.u[a.N + l] * cy(j) + a.u[2 * a.N + l] * cz(j));
-        P::store_raw(fout + o * N + i, g - (6.0f * P::UNIT) * n * float(wgt(j)) * uw);
+        const float uw = float(a.u[l] * kx + a.u[a.N + l] * ky + a.u[2 * a.N + l] * kz);
+        P::store_raw(fout + o * N + i, g - (6.0f * P::UNIT) * n * w * uw);
     } else {
         flag_status(a.status, 1);
     }
@@ -296,11 +348,26 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
         // a static (or slip) wall returns the population into the node's own opposite slot
 #pragma unroll
         for (int j = 1; j < Q; ++j) fo[(bb & (1u << j)) ? opp(j) * N : a.so[j]] = P::enc_raw(f[j]);
+    } else if constexpr (MBB) {
+        // Next to particle surfaces most warps have general links, in different directions
+        // per lane.  The plain and wall links are stored here; the general ones are staged
+        // in shared memory and pushed by one loop over each lane's set bits (ascending j,
+        // so the node's sums add in link order), so the lanes of a warp run that one body
+        // together whatever their links.
+        __shared__ float sf[Q - 1][128];
+#pragma unroll
+        for (int j = 1; j < Q; ++j) {
+            if (special & (1u << j)) sf[j - 1][threadIdx.x] = f[j];
+            else fo[(bb & (1u << j)) ? opp(j) * N : a.so[j]] = P::enc_raw(f[j]);
+        }
+        for (uint32_t s = special; s != 0u; s &= s - 1u) {
+            const int j = __ffs(s) - 1;
+            push_link_mbb<P>(a, x, y, z, i, j, sf[j - 1][threadIdx.x], n, ux, uy, uz, usq, mv, mkey);
+        }
     } else {
 #pragma unroll
         for (int j = 1; j < Q; ++j) {
-            if (special & (1u << j))
-                push_general<P, MBB>(a, fout, x, y, z, i, j, f[j], n, ux, uy, uz, usq, mv, mkey);
+            if (special & (1u << j)) push_general<P>(a, fout, x, y, z, i, j, f[j], n, ux, uy, uz, usq);
             else fo[(bb & (1u << j)) ? opp(j) * N : a.so[j]] = P::enc_raw(f[j]);
         }
     }
