@@ -387,8 +387,9 @@ __global__ void __launch_bounds__(128, 9) k_collide_stream_dev(LBArgs a) {
     const int z = blockIdx.z + 1;
     const int i = x + a.X * (y + a.Y * z);
     const S* fin = reinterpret_cast<const S*>(a.fin);
-    // whole warps leave together so that the element sums can use full-warp shuffles
-    const uint8_t t = x < a.X ? a.ntype[i] : (uint8_t)HB_T_STATWALL;
+    // whole warps leave together so that the element sums can use full-warp shuffles;
+    // lanes past the row end are inactive and marked bulk, so no link mask is read there
+    const uint8_t t = x < a.X ? a.ntype[i] : (uint8_t)(HB_T_STATWALL | HB_BULK);
     const bool act = MBB ? is_fluid(t, 1) : is_active(t);
     const bool solidp = MBB && is_active(t) && (t & HB_INSIDE);  // counts its particle's volume
     if (!__any_sync(0xffffffffu, act || solidp)) return;
