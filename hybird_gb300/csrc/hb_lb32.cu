@@ -101,14 +101,6 @@ __device__ __forceinline__ int dir_rt(int k, int j) {
     constexpr unsigned long long B[3] = {dir_bits(0), dir_bits(1), dir_bits(2)};
     return (int)((B[k] >> (2 * j)) & 3ull) - 1;
 }
-// cdot for a run-time link: the same terms, signs and order of additions
-__device__ __forceinline__ float cdot_rt(int kx, int ky, int kz, float vx, float vy, float vz) {
-    float r = kx != 0 ? (kx > 0 ? vx : -vx) : (ky != 0 ? (ky > 0 ? vy : -vy) : (kz > 0 ? vz : -vz));
-    if (kx != 0 && ky != 0) r = ky > 0 ? r + vy : r - vy;
-    if ((kx != 0 || ky != 0) && kz != 0) r = kz > 0 ? r + vz : r - vz;
-    return r;
-}
-
 // push_general of the moving-bounce-back kernel, out of line with the link index j
 // (1..18) as a run-time value.  Next to particle surfaces most warps take the general
 // push for several links; 18 inlined copies of this body (one per unrolled link) made
@@ -121,16 +113,16 @@ __device__ __forceinline__ float cdot_rt(int kx, int ky, int kz, float vx, float
 // particle's fixed-point sums.
 template <class P>
 __device__ __forceinline__ void push_link_mbb(const LBArgs& a, int x, int y, int z, int i, int j, float g,
-                                              float n, float ux, float uy, float uz, float usq, float* mv,
-                                              int& mkey) {
+                                              float n, float* mv, int& mkey) {
     typename P::S* fout = reinterpret_cast<typename P::S*>(a.fout);
     const int kx = dir_rt(0, j), ky = dir_rt(1, j), kz = dir_rt(2, j);
-    const int l = link32c(a, x, y, z, kx, ky, kz);
+    const int l = i + kx + a.X * (ky + a.Y * kz);  // no link wraps in this mode
     const uint8_t tl = a.ntype[l];
     const uint8_t lc = tl & HB_TYPE_MASK;
     const int o = (j & 1) ? j + 1 : j - 1;
     const int N = (int)a.N;
     const float w = j <= 6 ? float(wgt(1)) : float(wgt(7));
+    const float fkx = (float)kx, fky = (float)ky, fkz = (float)kz;
     if ((tl & HB_INSIDE) && (lc == HB_T_FLUID || lc == HB_T_INTERFACE)) {
         const int pl = (int)a.solid[l];
         const float4* pf4 = reinterpret_cast<const float4*>(a.parts.pf) + 3 * (size_t)pl;
@@ -138,10 +130,10 @@ __device__ __forceinline__ void push_link_mbb(const LBArgs& a, int x, int y, int
         const float rx = float(x + kx) - q0.x, ry = float(y + ky) - q0.y, rz = float(z + kz) - q0.z;
         const float wx = q1.z, wy = q1.w, wz = q2.x;
         const float vx = q0.w + (wy * rz - wz * ry), vy = q1.x + (wz * rx - wx * rz), vz = q1.y + (wx * ry - wy * rx);
-        const float BBi = 6.0f * n * w * cdot_rt(kx, ky, kz, vx, vy, vz);
+        const float BBi = 6.0f * n * w * fmaf(fkz, vz, fmaf(fky, vy, fkx * vx));
         P::store_raw(fout + o * N + i, g - P::UNIT * BBi);
         const float sc = (2.0f * g - P::UNIT * BBi) * P::INVU;
-        const float fx = float(kx) * sc, fy = float(ky) * sc, fz = float(kz) * sc;
+        const float fx = fkx * sc, fy = fky * sc, fz = fkz * sc;
         const float v6[6] = {fx, fy, fz, ry * fz - rz * fy, rz * fx - rx * fz, rx * fy - ry * fx};
         if (mkey < 0) mkey = pl;
         if (pl == mkey) {
@@ -156,13 +148,10 @@ __device__ __forceinline__ void push_link_mbb(const LBArgs& a, int x, int y, int
         P::store_raw(fout + j * N + l, g);
     } else if (lc == HB_T_STATWALL || lc == HB_T_SLIPSTAT || lc == HB_T_SLIPDYN || lc == HB_T_CURVED) {
         P::store_raw(fout + o * N + i, g);
-    } else if (lc == HB_T_GAS) {
-        const float vu = cdot_rt(kx, ky, kz, ux, uy, uz);
-        P::store_raw(fout + o * N + i, -g + (w * P::UNIT) * (9.0f * vu * vu - 3.0f * usq));
     } else if (lc == HB_T_DYNWALL) {
         const float uw = float(a.u[l] * kx + a.u[a.N + l] * ky + a.u[2 * a.N + l] * kz);
         P::store_raw(fout + o * N + i, g - (6.0f * P::UNIT) * n * w * uw);
-    } else {
+    } else {  // gas links do not occur: no free surface in this mode
         flag_status(a.status, 1);
     }
 }
@@ -362,7 +351,7 @@ __device__ __forceinline__ void lb_node(const LBArgs& a, int x, int y, int z, in
         }
         for (uint32_t s = special; s != 0u; s &= s - 1u) {
             const int j = __ffs(s) - 1;
-            push_link_mbb<P>(a, x, y, z, i, j, sf[j - 1][threadIdx.x], n, ux, uy, uz, usq, mv, mkey);
+            push_link_mbb<P>(a, x, y, z, i, j, sf[j - 1][threadIdx.x], n, mv, mkey);
         }
     } else {
 #pragma unroll
