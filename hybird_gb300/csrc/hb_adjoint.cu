@@ -79,6 +79,26 @@ __device__ __forceinline__ int alink(const Geom& G, int x, int y, int z, int j) 
     return xn + G.X * (yn + G.Y * zn);
 }
 
+// c_j . v and acc + c s with the zero components of c_j left out (compile-time j):
+// without fast-math the compiler keeps every 0 * v product
+template <class R>
+__device__ __forceinline__ R cdotR(int j, R vx, R vy, R vz) {
+    R r;
+    if (cx(j) != 0) {
+        r = cx(j) > 0 ? vx : -vx;
+        if (cy(j) != 0) r = cy(j) > 0 ? r + vy : r - vy;
+        if (cz(j) != 0) r = cz(j) > 0 ? r + vz : r - vz;
+    } else if (cy(j) != 0) {
+        r = cy(j) > 0 ? vy : -vy;
+        if (cz(j) != 0) r = cz(j) > 0 ? r + vz : r - vz;
+    } else {
+        r = cz(j) > 0 ? vz : -vz;
+    }
+    return r;
+}
+template <class R>
+__device__ __forceinline__ R addc(R acc, int c, R s) { return c == 0 ? acc : (c > 0 ? acc + s : acc - s); }
+
 template <class R>
 struct Mac {
     R dn, n, inv, ux, uy, uz, usq, uF;
@@ -114,8 +134,8 @@ __device__ __forceinline__ void collide(const R* g, const Mac<R>& M, const Coef<
     for (int j = 1; j < Q; j += 2) {
         const int o = j + 1;
         const R w = R(wgt(j));
-        const R vu = R(cx(j)) * M.ux + R(cy(j)) * M.uy + R(cz(j)) * M.uz;
-        const R cF = R(cx(j)) * C.F[0] + R(cy(j)) * C.F[1] + R(cz(j)) * C.F[2];
+        const R vu = cdotR<R>(j, M.ux, M.uy, M.uz);
+        const R cF = cdotR<R>(j, C.F[0], C.F[1], C.F[2]);
         const R ep = w * (M.dn + M.n * (R(4.5) * vu * vu - R(1.5) * M.usq));
         const R em = R(3) * w * M.n * vu;
         const R fp = R(0.5) * (g[j] + g[o]), fm = R(0.5) * (g[j] - g[o]);
@@ -156,9 +176,8 @@ __device__ __forceinline__ void adj_local(const R* g, R* mu, R Awall, const Mac<
     for (int j = 1; j < Q; j += 2) {
         const int o = j + 1;
         const R w = R(wgt(j));
-        const R cxj = R(cx(j)), cyj = R(cy(j)), czj = R(cz(j));
-        const R vu = cxj * ux + cyj * uy + czj * uz;
-        const R cF = cxj * Fx + cyj * Fy + czj * Fz;
+        const R vu = cdotR<R>(j, ux, uy, uz);
+        const R cF = cdotR<R>(j, Fx, Fy, Fz);
         const R ep = w * (M.dn + n * (R(4.5) * vu * vu - R(1.5) * usq));
         const R em = R(3) * w * n * vu;
         const R fp = R(0.5) * (g[j] + g[o]), fm = R(0.5) * (g[j] - g[o]);
@@ -169,15 +188,15 @@ __device__ __forceinline__ void adj_local(const R* g, R* mu, R Awall, const Mac<
         const R kc = s * (C.wp * w * n * R(9) * vu + C.ap * w * R(9) * cF) + d * C.wm * R(3) * w * n;
         const R ku = s * C.wp * w * n * R(-3);
         const R kF = s * C.ap * w * R(-3);
-        Bx += kc * cxj + ku * ux + kF * Fx;
-        By += kc * cyj + ku * uy + kF * Fy;
-        Bz += kc * czj + ku * uz + kF * Fz;
+        Bx += addc<R>(ku * ux + kF * Fx, cx(j), kc);
+        By += addc<R>(ku * uy + kF * Fy, cy(j), kc);
+        Bz += addc<R>(ku * uz + kF * Fz, cz(j), kc);
         // direct dependence of S+ and S- on F
         const R gc = s * C.ap * w * R(9) * vu + d * C.am * R(3) * w;
         const R gu = s * C.ap * w * R(-3);
-        gr[0] += gc * cxj + gu * ux;
-        gr[1] += gc * cyj + gu * uy;
-        gr[2] += gc * czj + gu * uz;
+        gr[0] += addc<R>(gu * ux, cx(j), gc);
+        gr[1] += addc<R>(gu * uy, cy(j), gc);
+        gr[2] += addc<R>(gu * uz, cz(j), gc);
         gr[3] += s * (-(fp - ep) - R(0.5) * Fs);
         gr[4] += d * (-(fm - em) - R(0.5) * Fa);
         const R ls = R(0.5) * (R(1) - C.wp) * s, ld = R(0.5) * (R(1) - C.wm) * d;
@@ -192,7 +211,7 @@ __device__ __forceinline__ void adj_local(const R* g, R* mu, R Awall, const Mac<
     gr[1] += R(0.5) * by;
     gr[2] += R(0.5) * bz;
 #pragma unroll
-    for (int k = 0; k < Q; ++k) mu[k] += A + R(cx(k)) * bx + R(cy(k)) * by + R(cz(k)) * bz;
+    for (int k = 0; k < Q; ++k) mu[k] += addc<R>(addc<R>(addc<R>(A, cx(k), bx), cy(k), by), cz(k), bz);
 }
 
 // Deterministic block sum of nv per-thread values into part[blk*NPART + off ...]: warp
