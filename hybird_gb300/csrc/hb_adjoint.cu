@@ -221,7 +221,8 @@ __device__ __forceinline__ void adj_local(const R* g, R* mu, R Awall, const Mac<
 template <class R>
 __device__ __forceinline__ void block_accumulate(R* v, int nv, int off, double* part) {
     __shared__ R sh[NPART][AMAXW];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = tid & 31, wid = tid >> 5;
     for (int k = 0; k < nv; ++k) {
         R x = v[k];
 #pragma unroll
@@ -229,12 +230,12 @@ __device__ __forceinline__ void block_accumulate(R* v, int nv, int off, double* 
         if (lane == 0) sh[k][wid] = x;
     }
     __syncthreads();
-    if ((int)threadIdx.x < nv) {
-        const int nw = (blockDim.x + 31) >> 5;
+    if (tid < nv) {
+        const int nw = (blockDim.x * blockDim.y + 31) >> 5;
         const long long blk = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
         R t = R(0);
-        for (int w = 0; w < nw; ++w) t += sh[threadIdx.x][w];
-        part[blk * NPART + off + threadIdx.x] += (double)t;
+        for (int w = 0; w < nw; ++w) t += sh[tid][w];
+        part[blk * NPART + off + tid] += (double)t;
     }
 }
 
@@ -307,8 +308,8 @@ template <class R>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1) k_adj_fwd(Geom G, Coef<R> C, const R* __restrict__ gin,
                                                  R* __restrict__ gout, const R* __restrict__ uin) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y + 1, z = blockIdx.z + 1;
-    if (x >= G.X) return;
+    const int y = blockIdx.y + 1, z = blockIdx.z * blockDim.y + threadIdx.y + 1;
+    if (x >= G.X || z > G.Z - 2) return;
     const int N = (int)G.N;
     const int i = x + G.X * (y + G.Y * z);
     const uint8_t k = G.kind[i];
@@ -388,11 +389,13 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_adj_step(Geom G
                                                   const R* __restrict__ lin, R* __restrict__ lout,
                                                   const R* __restrict__ uin, double* __restrict__ acc,
                                                   double* part) {
+    // blockDim.y z rows per block: the block's partial sums (a barrier and an FP64
+    // addition per value) are paid once for all of them
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y + 1, z = blockIdx.z + 1;
+    const int y = blockIdx.y + 1, z = blockIdx.z * blockDim.y + threadIdx.y + 1;
     const int N = (int)G.N;
     R gr[5] = {0, 0, 0, 0, 0};
-    if (x < G.X) {
+    if (x < G.X && z <= G.Z - 2) {
         const int i = x + G.X * (y + G.Y * z);
         const uint8_t k = G.kind[i];
         if ((k & K_CODE) == K_ACT) {
@@ -650,11 +653,14 @@ int adj_run(hb_ctx* c, hb_adj* a, const hb_adjoint_cfg* cfg, bool reverse, Geom 
         else
             k_adj_load<PolF16, R><<<Gd, B, 0, st>>>(G, (const __half*)(c->cur ? c->fB : c->fA), g0);
     }
+    // forward blocks: as many z rows as fit in 256 threads
+    const unsigned frows = L.block.x >= 256 ? 1u : 256u / L.block.x;
+    const dim3 FB(L.block.x, frows), FG(L.grid.x, L.grid.y, (unsigned)ceil_div(L.grid.z, (int)frows));
     // forward pass: g^0 .. g^{T-1}, checkpoints at multiples of K
     R* cur = state(0, 0);
     for (int t = 0; t + 1 <= T - 1; ++t) {
         R* out = ((t + 1) % K == 0) ? state((t + 1) / K, 0) : state(0, 1 + (t & 1));
-        k_adj_fwd<R><<<L.grid, L.block, 0, st>>>(G, C, cur, out, uin);
+        k_adj_fwd<R><<<FG, FB, 0, st>>>(G, C, cur, out, uin);
         cur = out;
     }
     a->fwd_steps = T - 1;
@@ -664,18 +670,21 @@ int adj_run(hb_ctx* c, hb_adj* a, const hb_adjoint_cfg* cfg, bool reverse, Geom 
     ACK(cudaEventRecord(a->e[1], st));
     if (reverse) {
         int p = 0;
+        // reverse-step blocks: as many z rows as fit in 256 threads
+        const unsigned rows = L.block.x >= 256 ? 1u : 256u / L.block.x;
+        const dim3 LSb(L.block.x, rows), LSg(L.grid.x, L.grid.y, (unsigned)ceil_div(L.grid.z, (int)rows));
         for (int ci = Cn - 1; ci >= 0; --ci) {
             const int t0 = ci * K;
             const int t1 = (t0 + K < T ? t0 + K : T) - 1;
             for (int s = 0; s < t1 - t0; ++s)
-                k_adj_fwd<R><<<L.grid, L.block, 0, st>>>(G, C, state(ci, s), state(ci, s + 1), uin);
+                k_adj_fwd<R><<<FG, FB, 0, st>>>(G, C, state(ci, s), state(ci, s + 1), uin);
             a->fwd_steps += t1 - t0;
             for (int t = t1; t >= t0; --t) {
                 R* g = state(ci, t - t0);
                 if (t == T - 1) {
                     k_adj_terminal<R><<<L.grid, L.block, 0, st>>>(G, C, g, lamb(p), a->part);
                 } else {
-                    k_adj_step<R><<<L.grid, L.block, 0, st>>>(G, C, g, lamb(p), lamb(1 - p), uin, a->acc, a->part);
+                    k_adj_step<R><<<LSg, LSb, 0, st>>>(G, C, g, lamb(p), lamb(1 - p), uin, a->acc, a->part);
                     p ^= 1;
                     a->rev_steps += 1;
                 }
