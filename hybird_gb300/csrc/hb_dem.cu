@@ -681,29 +681,66 @@ __device__ __noinline__ FM cylinder_contact(const DemArgs& a, int c, V xpi, doub
 // a: the kernel's parameter block; ga: its device-memory copy for the out-of-line calls
 __device__ __forceinline__ void forces_group(const DemArgs& a, const DemArgs& ga, int i, bool on, int c, PredBuf pb,
                                              int& ncont, double v[12]) {
+    __shared__ unsigned s_cm[256];  // each lane's overlapping candidates (bit t: k = c + 8 t)
     const int E = a.E;
     V FP{0, 0, 0}, MP{0, 0, 0}, FW{0, 0, 0}, MW{0, 0, 0};
-    bool contrib = false;  // this lane added a contact, wall or object force
-    if (on) {
-        const V xpi = ld3(pb.x0r, E, i);
-        const int cnt = a.nbr_cnt[i];
-        for (int k = c; k < cnt; k += 8) {
-            const int j = a.nbr[(long long)i * a.nbr_cap + k];
-            const int I = min(i, j), J = max(i, j);
-            const double rI = a.rad[I], rJ = a.rad[J];
-            const double sig = rI + rJ;
-            const V vd = sub(ld3(pb.x0r, E, J), ld3(pb.x0r, E, I));
-            if (!(nrm2(vd) < sig * sig)) continue;
+    bool contribP = false, contribW = false;  // this lane added a particle / a wall or object force
+    // pass 1: the contact test (DEM.cpp:1801-1900) of this lane's candidates k = c, c + 8, ...
+    unsigned m = 0u;
+    const V xpi = on ? ld3(pb.x0r, E, i) : V{0, 0, 0};
+    const int cnt = on ? a.nbr_cnt[i] : 0;
+    for (int k = c, t = 0; k < cnt; k += 8, ++t) {
+        const int j = a.nbr[(long long)i * a.nbr_cap + k];
+        const int I = min(i, j), J = max(i, j);
+        const double sig = a.rad[I] + a.rad[J];
+        const V vd = sub(ld3(pb.x0r, E, J), ld3(pb.x0r, E, I));
+        if (nrm2(vd) < sig * sig) {
+            m |= 1u << t;
             if (i < j) ++ncont;
-            contrib = true;
-            const FM r = pp_contact(ga, i, I, J, vd, rI, rJ, FP, MP, pb, a.npc + (long long)i * a.nbr_cap + k);
-            FP = r.f;
-            MP = r.m;
         }
+    }
+    // pass 2: the group's contacts, numbered by lane and then by candidate, go round-robin
+    // over its eight lanes (contact q on lane q mod 8), and the wall and cylinder tests to
+    // the lane after the last one: no lane runs a second contact chain while another has
+    // none.  Each lane adds its contacts in increasing q.
+    int T = 0;  // the group's contacts
+    if (__any_sync(0xffffffffu, m != 0u)) {
+        __syncwarp();  // the previous group's pass 2 has read s_cm
+        s_cm[threadIdx.x] = m;
+        int incl = __popc(m);
+#pragma unroll
+        for (int d = 1; d < 8; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, d, 8);
+            if (c >= d) incl += y;
+        }
+        T = __shfl_sync(0xffffffffu, incl, 7, 8);
+        __syncwarp();
+    }
+    const unsigned* gm = s_cm + (threadIdx.x & ~7);
+    for (int q = c; q < T; q += 8) {
+        int L = 0, base = 0;
+        for (; L < 7; ++L) {
+            const int nl = __popc(gm[L]);
+            if (q < base + nl) break;
+            base += nl;
+        }
+        unsigned mm = gm[L];
+        for (int r = q - base; r > 0; --r) mm &= mm - 1u;
+        const int k = L + 8 * (__ffs(mm) - 1);
+        const int j = a.nbr[(long long)i * a.nbr_cap + k];
+        const int I = min(i, j), J = max(i, j);
+        const double rI = a.rad[I], rJ = a.rad[J];
+        const V vd = sub(ld3(pb.x0r, E, J), ld3(pb.x0r, E, I));
+        contribP = true;
+        const FM r = pp_contact(ga, i, I, J, vd, rI, rJ, FP, MP, pb, a.npc + (long long)i * a.nbr_cap + k);
+        FP = r.f;
+        MP = r.m;
+    }
+    if (on) {
         const double ri = a.rad[i], mi = a.m[i];
         const V xpv = ld3(pb.x1r, E, i);
         const V wpg = ld3(pb.wGr, E, i);
-        if (c == 0) {  // wallParticleCollision (DEM.cpp:1902-1982), static walls
+        if (c == (T & 7)) {  // wallParticleCollision (DEM.cpp:1902-1982), static walls
             const int w = a.wall_of[i];
             bool hit = false;
             if (w >= 0) {
@@ -711,7 +748,7 @@ __device__ __forceinline__ void forces_group(const DemArgs& a, const DemArgs& ga
                 const double dist = dot(wn, sub(xpi, V{a.wp[w][0], a.wp[w][1], a.wp[w][2]}));
                 const double overlap = ri - dist;
                 if (overlap > 0.0) {
-                    contrib = hit = true;
+                    contribW = hit = true;
                     const FM r = wall_contact(ga, wn, overlap, xpv, wpg, ri, mi, FW, MW, a.wrec + 7 * (long long)i);
                     FW = r.f;
                     MW = r.m;
@@ -725,7 +762,7 @@ __device__ __forceinline__ void forces_group(const DemArgs& a, const DemArgs& ga
                 const double dist = a.cR[cy] - sqrt(nrm2(sub(mul(dot(d, nx), nx), d)));
                 const double overlap = ri - dist;
                 if (overlap > 0.0) {
-                    contrib = true;
+                    contribW = true;
                     const FM r = cylinder_contact(ga, cy, xpi, overlap, xpv, wpg, ri, mi, FW, MW);
                     FW = r.f;
                     MW = r.m;
@@ -743,35 +780,35 @@ __device__ __forceinline__ void forces_group(const DemArgs& a, const DemArgs& ga
                 rec[0] = 0.0;
                 continue;
             }
-            contrib = true;
+            contribW = true;
             const FM r = object_contact(ga, o, vd, dist, overlap, xpv, wpg, ri, mi, FW, MW, rec);
             FW = r.f;
             MW = r.m;
         }
     }
-    // fixed xor-shuffle tree within each group of eight lanes; skipped when in every group
-    // at most the group's first lane holds a force (the tree would only add zeros)
-    const unsigned who = __ballot_sync(0xffffffffu, contrib);
+    // fixed xor-shuffle tree within each group of eight lanes.  Particle forces: skipped
+    // when in every group at most the group's first lane holds one (the group's first
+    // lane then holds the totals).  Wall, cylinder and object forces: the tree whenever a
+    // lane of the warp holds one (sums that start at +0.0 are never -0.0, so the tree's
+    // additions of +0.0 leave a single lane's force as it is).
+    const unsigned whoP = __ballot_sync(0xffffffffu, contribP);
+    const unsigned whoW = __ballot_sync(0xffffffffu, contribW);
     v[0] = FP.x; v[1] = FP.y; v[2] = FP.z; v[3] = MP.x; v[4] = MP.y; v[5] = MP.z;
     v[6] = FW.x; v[7] = FW.y; v[8] = FW.z; v[9] = MW.x; v[10] = MW.y; v[11] = MW.z;
-    if (who & ~0x01010101u) {
+    if (whoP & ~0x01010101u) {
 #pragma unroll
         for (int off = 1; off < 8; off <<= 1)
 #pragma unroll
             for (int q = 0; q < 6; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
-        if (a.O > 0) {  // object contacts can sit in any lane
+    } else {
 #pragma unroll
-            for (int off = 1; off < 8; off <<= 1)
+        for (int q = 0; q < 6; ++q) v[q] = __shfl_sync(0xffffffffu, v[q], threadIdx.x & 24);
+    }
+    if (whoW) {
 #pragma unroll
-                for (int q = 6; q < 12; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
-        } else {  // wall and cylinder forces sit in the group's first lane only (never -0.0,
-                  // so the tree's additions of +0.0 would leave them as they are)
+        for (int off = 1; off < 8; off <<= 1)
 #pragma unroll
-            for (int q = 6; q < 12; ++q) v[q] = __shfl_sync(0xffffffffu, v[q], threadIdx.x & 24);
-        }
-    } else {  // the group's first lane holds the totals: hand them to the other seven
-#pragma unroll
-        for (int q = 0; q < 12; ++q) v[q] = __shfl_sync(0xffffffffu, v[q], threadIdx.x & 24);
+            for (int q = 6; q < 12; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
     }
     if (on && c == 0) {
         st3(a.FP, E, i, V{v[0], v[1], v[2]});
