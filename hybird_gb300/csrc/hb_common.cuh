@@ -188,4 +188,29 @@ inline int ceil_div(long long a, int b) { return (int)((a + b - 1) / b); }
 
 __device__ __forceinline__ void flag_status(int* status, int word) { atomicOr(status + word, 1); }
 
+// Programmatic dependent launch for chains of short kernels: a kernel launched with
+// launch_pdl may be scheduled while its predecessor in the stream still runs, so its
+// launch latency hides behind that kernel's tail.  Every such kernel starts with
+// pdl_enter(): it waits until the predecessor grid has completed and its memory is
+// visible (griddepcontrol.wait) before any access, then lets its own successor be
+// scheduled.  In a kernel launched normally both instructions do nothing.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 }  // namespace hb

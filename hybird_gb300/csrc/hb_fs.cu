@@ -190,6 +190,7 @@ __device__ void ledger_add(const FsArgs& a, double v) {
 // ballots (order within the list is irrelevant: each cell's mass exchange is independent
 // of the others).
 __global__ void __launch_bounds__(256) k_fs_ilist(FsArgs a) {
+    pdl_enter();
     if (a.cnt->valid) return;
     uint32_t* list = cur_list(a);
     int* count = &a.cnt->icount[a.cnt->sel];
@@ -207,6 +208,7 @@ __global__ void __launch_bounds__(256) k_fs_ilist(FsArgs a) {
 // then shares its warp instructions with 31 other cells on this part's narrow FP64 pipe.)
 template <class P>
 __global__ void __launch_bounds__(256) k_fs_mass_list(FsArgs a) {
+    pdl_enter();
     const int n = cur_count(a);
     const uint32_t* list = cur_list(a);
     const bool first = a.cnt->first != 0;
@@ -251,6 +253,7 @@ __global__ void __launch_bounds__(256) k_fs_mass_list(FsArgs a) {
 
 // fluid mass = n (LB.cpp:1582-1585): a lean pass over the node bytes, eight per thread
 __global__ void __launch_bounds__(256) k_fs_fluid_mass(FsArgs a) {
+    pdl_enter();
     const long long nw = (a.N + 7) / 8;
     for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nw; w += (long long)gridDim.x * blockDim.x) {
         const long long i0 = 8 * w;
@@ -271,6 +274,7 @@ __global__ void __launch_bounds__(256) k_fs_fluid_mass(FsArgs a) {
 
 // K2 findInterfaceMutants (LB.cpp:1620-1650) over the interface list
 __global__ void __launch_bounds__(256) k_fs_classify(FsArgs a) {
+    pdl_enter();
     const int n = cur_count(a);
     const uint32_t* list = cur_list(a);
     const int n_up = (n + 31) / 32 * 32;
@@ -303,6 +307,7 @@ __global__ void __launch_bounds__(256) k_fs_classify(FsArgs a) {
 // along the same direction reaches m: the reference's neighbour table), keeping the
 // largest m + 1 per g; then the winner initialises g.
 __global__ void __launch_bounds__(256) k_fs_filled_parent(FsArgs a) {
+    pdl_enter();
     const int n = min(a.cnt->ccount, (int)a.icap);
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x) {
         const uint32_t m = a.clist[w];
@@ -321,6 +326,7 @@ __global__ void __launch_bounds__(256) k_fs_filled_parent(FsArgs a) {
 
 template <class P>
 __global__ void __launch_bounds__(256) k_fs_new_from_filled(FsArgs a) {
+    pdl_enter();
     const int n = min(a.cnt->ccount, (int)a.icap);
     const int n_up = (n + 31) / 32 * 32;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n_up; w += gridDim.x * blockDim.x) {
@@ -374,6 +380,7 @@ __global__ void __launch_bounds__(256) k_fs_new_from_filled(FsArgs a) {
 // K4 smoothenInterface, fluid neighbours of emptied cells (LB.cpp:1679-1700); the first
 // emptied neighbour to claim a cell (parent slot) converts it
 __global__ void __launch_bounds__(256) k_fs_new_from_emptied(FsArgs a) {
+    pdl_enter();
     const int n = min(a.cnt->ccount, (int)a.icap);
     const int n_up = (n + 31) / 32 * 32;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n_up; w += gridDim.x * blockDim.x) {
@@ -417,6 +424,7 @@ __device__ __forceinline__ bool interface_cell(const FsArgs& a, int k, int n0, u
 // K5 updateMutants (LB.cpp:1703-1742) over the conversion list, and removeIsolated, first
 // pass (LB.cpp:1749-1769) over the interface cells
 __global__ void __launch_bounds__(256) k_fs_mutants_to_fluid(FsArgs a) {
+    pdl_enter();
     const int nc = min(a.cnt->ccount, (int)a.icap);
     const int n0 = cur_count(a), nn = min(a.cnt->ncount, (int)a.icap);
     const int total = nc + n0 + nn;
@@ -449,6 +457,7 @@ __global__ void __launch_bounds__(256) k_fs_mutants_to_fluid(FsArgs a) {
 // K6 removeIsolated, second pass (LB.cpp:1771-1793); the cells that stay interface form
 // the next interface list
 __global__ void __launch_bounds__(256) k_fs_isolated_gas(FsArgs a) {
+    pdl_enter();
     const int n0 = cur_count(a), nn = min(a.cnt->ncount, (int)a.icap);
     const int total = n0 + nn;
     const int t_up = (total + 31) / 32 * 32;
@@ -476,6 +485,7 @@ __global__ void __launch_bounds__(256) k_fs_isolated_gas(FsArgs a) {
 
 // the surplus and the interface count of the step; the next list becomes current
 __global__ void k_fs_ledger(FsArgs a) {
+    pdl_enter();
     FsCount* c = a.cnt;
     const int nxt = c->sel ^ 1;
     const long long count = min((long long)c->icount[nxt], a.icap);
@@ -500,6 +510,7 @@ __global__ void k_fs_ledger(FsArgs a) {
 // (k_fs_ledger), as the reference forms addMass once; then the step's conversion flags
 // and claim slots go back to zero
 __global__ void __launch_bounds__(256) k_fs_redistribute(FsArgs a) {
+    pdl_enter();
     const int n0 = cur_count(a);
     const int nc = min(a.cnt->ccount, (int)a.icap), nn = min(a.cnt->ncount, (int)a.icap);
     const uint32_t* list = cur_list(a);
@@ -592,21 +603,22 @@ void launch_fs_step(hb_ctx* c, int cur) {
     const int GL = FS_LIST_GRID;
     // this step's conversion and new-cell counts and its ledger start at zero
     cudaMemsetAsync(&a.cnt->ccount, 0, sizeof(FsCount) - offsetof(FsCount, ccount), s);
-    k_fs_ilist<<<GL, 256, 0, s>>>(a);
-    if (c->P.precision == HB_FP64) k_fs_mass_list<PolF64><<<GL, 256, 0, s>>>(a);
-    else if (c->P.precision == HB_FP32) k_fs_mass_list<PolF32><<<GL, 256, 0, s>>>(a);
-    else k_fs_mass_list<PolF16><<<GL, 256, 0, s>>>(a);
-    k_fs_fluid_mass<<<152 * 8, 256, 0, s>>>(a);
-    k_fs_classify<<<GL, 256, 0, s>>>(a);
-    k_fs_filled_parent<<<GL, 256, 0, s>>>(a);
-    if (c->P.precision == HB_FP64) k_fs_new_from_filled<PolF64><<<GL, 256, 0, s>>>(a);
-    else if (c->P.precision == HB_FP32) k_fs_new_from_filled<PolF32><<<GL, 256, 0, s>>>(a);
-    else k_fs_new_from_filled<PolF16><<<GL, 256, 0, s>>>(a);
-    k_fs_new_from_emptied<<<GL, 256, 0, s>>>(a);
-    k_fs_mutants_to_fluid<<<GL, 256, 0, s>>>(a);
-    k_fs_isolated_gas<<<GL, 256, 0, s>>>(a);
-    k_fs_ledger<<<1, 1, 0, s>>>(a);
-    k_fs_redistribute<<<GL, 256, 0, s>>>(a);
+    // a chain of short list passes: each one scheduled behind the tail of the previous
+    launch_pdl(k_fs_ilist, GL, 256, s, a);
+    if (c->P.precision == HB_FP64) launch_pdl(k_fs_mass_list<PolF64>, GL, 256, s, a);
+    else if (c->P.precision == HB_FP32) launch_pdl(k_fs_mass_list<PolF32>, GL, 256, s, a);
+    else launch_pdl(k_fs_mass_list<PolF16>, GL, 256, s, a);
+    launch_pdl(k_fs_fluid_mass, 152 * 8, 256, s, a);
+    launch_pdl(k_fs_classify, GL, 256, s, a);
+    launch_pdl(k_fs_filled_parent, GL, 256, s, a);
+    if (c->P.precision == HB_FP64) launch_pdl(k_fs_new_from_filled<PolF64>, GL, 256, s, a);
+    else if (c->P.precision == HB_FP32) launch_pdl(k_fs_new_from_filled<PolF32>, GL, 256, s, a);
+    else launch_pdl(k_fs_new_from_filled<PolF16>, GL, 256, s, a);
+    launch_pdl(k_fs_new_from_emptied, GL, 256, s, a);
+    launch_pdl(k_fs_mutants_to_fluid, GL, 256, s, a);
+    launch_pdl(k_fs_isolated_gas, GL, 256, s, a);
+    launch_pdl(k_fs_ledger, 1, 1, s, a);
+    launch_pdl(k_fs_redistribute, GL, 256, s, a);
     launch_refresh_bulk(c, &a.cnt->changed);  // only when a cell's activity changed
 }
 

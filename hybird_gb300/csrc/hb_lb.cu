@@ -555,6 +555,7 @@ __device__ __forceinline__ void bulk_node(const InitArgs& a, const PerFaces& pf,
 }
 
 __global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, unsigned long long* lmask, int* changed) {
+    pdl_enter();
     if (changed && *changed == 0) return;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= a.X) return;
@@ -565,7 +566,10 @@ __global__ void k_bulk(InitArgs a, PerFaces pf, uint8_t* ntype, unsigned long lo
 }
 
 // resets the activity-change counter after the (conditional) refresh has run
-__global__ void k_bulk_done(int* changed) { *changed = 0; }
+__global__ void k_bulk_done(int* changed) {
+    pdl_enter();
+    *changed = 0;
+}
 
 // ---- upload / download ---------------------------------------------------------------
 
@@ -730,9 +734,9 @@ int launch_init_lattice(hb_ctx* c, const double* el_x0, const double* el_r, int 
 
 void launch_refresh_bulk(hb_ctx* c, int* changed) {
     InitArgs a = init_args(c);
-    k_bulk<<<dim3((unsigned)ceil_div(c->X, 128), (unsigned)c->Y, (unsigned)ceil_div(c->Z, BULK_ZC)), 128, 0,
-             c->stream>>>(a, per_faces(c), c->ntype, c->lmask, changed);
-    if (changed) k_bulk_done<<<1, 1, 0, c->stream>>>(changed);
+    launch_pdl(k_bulk, dim3((unsigned)ceil_div(c->X, 128), (unsigned)c->Y, (unsigned)ceil_div(c->Z, BULK_ZC)), 128,
+               c->stream, a, per_faces(c), c->ntype, c->lmask, changed);
+    if (changed) launch_pdl(k_bulk_done, 1, 1, c->stream, changed);
 }
 
 void launch_lb_step(hb_ctx* c, int cur) {
