@@ -1050,7 +1050,6 @@ __device__ double newton_plain(const DemArgs& a, int i, int c, PredBuf pb, doubl
 
 __device__ void predict_one(const DemArgs& a, int i) {  // elmt.cpp:139-177
     const int E = a.E;
-    const double dt = a.dt;
     const double* c = a.gc;
     const V x0 = ld3(a.x0, E, i), x1 = ld3(a.x1, E, i), x2 = ld3(a.x2, E, i), x3 = ld3(a.x3, E, i),
             x4 = ld3(a.x4, E, i), x5 = ld3(a.x5, E, i);
@@ -1118,8 +1117,6 @@ __device__ double correct_one(const DemArgs& a, int i) {  // elmt.cpp:179-254
     const int E = a.E;
     double v2 = 0.0;
     {
-        const double dt = a.dt;
-        const double* c = a.gc;
         const double* c1o = a.gc1;
         const double* c2o = a.gc2;
         const V x2 = ld3(a.x2, E, i);
@@ -1167,7 +1164,6 @@ __device__ double correct_one(const DemArgs& a, int i) {  // elmt.cpp:179-254
 // element's loads overlap instead of waiting on each other
 __device__ __noinline__ double correct_predict_one(const DemArgs& a, int i, PredBuf pb) {
     const int E = a.E;
-    const double dt = a.dt;
     const double* c = a.gc;
     const double* c1o = a.gc1;
     const double* c2o = a.gc2;
