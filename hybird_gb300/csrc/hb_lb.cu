@@ -531,6 +531,8 @@ __device__ __forceinline__ void bulk_node(const InitArgs& a, const PerFaces& pf,
             bulk = false;
             mask = 0x7FFFEu;
         } else {
+            // unrolled: the 18 neighbour bytes are loaded together, not one after another
+#pragma unroll
             for (int j = 1; j < Q; ++j) {
                 int xn = x + cx(j), yn = y + cy(j), zn = z + cz(j);
                 if (xn == 0 && pf.v[0]) xn = a.X - 2; else if (xn == a.X - 1 && pf.v[1]) xn = 1;
@@ -869,6 +871,9 @@ __device__ __forceinline__ void mbb_refill_one(const MbbArgs& a, int k) {
     const int x = (int)(l % a.X), y = (int)((l / a.X) % a.Y), z = (int)(l / ((long long)a.X * a.Y));
     double sum = 0.0;
     int cnt = 0;
+    // unrolled: the 18 neighbours' bytes and densities are loaded together; the sum still
+    // runs in link order
+#pragma unroll
     for (int j = 1; j < Q; ++j) {
         const long long m = (long long)(x + cx(j)) + (long long)a.X * ((long long)(y + cy(j)) + (long long)a.Y * (z + cz(j)));
         const double r = a.rho[m];
@@ -881,6 +886,7 @@ __device__ __forceinline__ void mbb_refill_one(const MbbArgs& a, int k) {
     mbb_velocity(a.parts, (int)a.solid[l], x, y, z, ux, uy, uz);
     const double usq = ux * ux + uy * uy + uz * uz;
     S* f = reinterpret_cast<S*>(a.f);
+#pragma unroll
     for (int j = 0; j < Q; ++j) {
         const double vu = ux * cx(j) + uy * cy(j) + uz * cz(j);
         double v = wgt(j) * rho * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
