@@ -884,20 +884,24 @@ __device__ __forceinline__ void mbb_refill_one(const MbbArgs& a, int k) {
     const double rho = cnt ? sum / (double)cnt : 1.0;
     double ux, uy, uz;
     mbb_velocity(a.parts, (int)a.solid[l], x, y, z, ux, uy, uz);
-    const double usq = ux * ux + uy * uy + uz * uz;
+    // f_eq in the storage policy's arithmetic (double for FP64 populations, float for the
+    // FP32 and FP16 forms, whose stored values carry float precision at most)
+    const T rt = (T)rho, uxt = (T)ux, uyt = (T)uy, uzt = (T)uz;
+    const T usq = uxt * uxt + uyt * uyt + uzt * uzt;
     S* f = reinterpret_cast<S*>(a.f);
 #pragma unroll
     for (int j = 0; j < Q; ++j) {
-        const double vu = ux * cx(j) + uy * cy(j) + uz * cz(j);
-        double v = wgt(j) * rho * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
-        if (P::DEV) v -= wgt(j);
-        P::store(f + (long long)j * a.N + l, (T)v);
+        const T vu = uxt * T(cx(j)) + uyt * T(cy(j)) + uzt * T(cz(j));
+        T v = T(wgt(j)) * rt * (T(1) + T(3) * vu + T(4.5) * vu * vu - T(1.5) * usq);
+        if (P::DEV) v -= T(wgt(j));
+        P::store(f + (long long)j * a.N + l, v);
     }
     a.pop_rho[k] = rho;
 }
 
 template <class P>
 __global__ void k_mbb_refill_gs(MbbArgs a) {
+    pdl_enter();
     const int n = *a.npop;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) mbb_refill_one<P>(a, k);
 }
@@ -906,6 +910,7 @@ __global__ void k_mbb_refill_gs(MbbArgs a) {
 // that node from its neighbours' final state; uncovered nodes take their refill density.
 // Nodes reached from several changed nodes compute the same values.
 __global__ void k_mbb_relink_gs(MbbArgs m, InitArgs a, PerFaces pf, unsigned long long* lmask) {
+    pdl_enter();
     const long long np = *m.npop, nc = *m.nclaim;
     const long long total = (np + nc) * Q;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
@@ -1010,10 +1015,10 @@ void launch_mbb_nodes(hb_ctx* c, int cur) {
     // the lists hold a few thousand entries per step: a fixed grid with grid-stride loops
     // (the launch shape does not depend on the device-side counts)
     const unsigned gp = 152 * 4;
-    if (c->P.precision == HB_FP64) k_mbb_refill_gs<PolF64><<<gp, B, 0, c->stream>>>(m);
-    else if (c->P.precision == HB_FP32) k_mbb_refill_gs<PolF32><<<gp, B, 0, c->stream>>>(m);
-    else k_mbb_refill_gs<PolF16><<<gp, B, 0, c->stream>>>(m);
-    k_mbb_relink_gs<<<gp, B, 0, c->stream>>>(m, init_args(c), per_faces(c), c->lmask);
+    if (c->P.precision == HB_FP64) launch_pdl(k_mbb_refill_gs<PolF64>, gp, B, c->stream, m);
+    else if (c->P.precision == HB_FP32) launch_pdl(k_mbb_refill_gs<PolF32>, gp, B, c->stream, m);
+    else launch_pdl(k_mbb_refill_gs<PolF16>, gp, B, c->stream, m);
+    launch_pdl(k_mbb_relink_gs, gp, B, c->stream, m, init_args(c), per_faces(c), c->lmask);
 }
 
 void launch_mbb_force(hb_ctx* c, int cur) {
