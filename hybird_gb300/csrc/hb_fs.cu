@@ -122,6 +122,12 @@ __device__ __forceinline__ int cur_count(const FsArgs& a) { return (int)min((lon
 
 // append `item` of the lanes with `take` to list[0 .. cap) at *count (warp ballot, one
 // atomic per warp); a full list sets status word 2, bit 8
+// The list passes deal 32-entry chunks of their list over the blocks first (chunk c to
+// block c mod grid), so that a list of 10^4 cells reaches every SM instead of the first
+// few dozen blocks; a whole warp takes each chunk, as the ballots of list_push need.
+__device__ __forceinline__ int chunk_first() { return 32 * (blockIdx.x + gridDim.x * (threadIdx.x >> 5)) + (threadIdx.x & 31); }
+__device__ __forceinline__ int chunk_stride() { return 32 * gridDim.x * (blockDim.x >> 5); }
+
 __device__ __forceinline__ void list_push(const FsArgs& a, uint32_t* list, int* count, bool take, uint32_t item) {
     const unsigned warp = __activemask();
     const unsigned b = __ballot_sync(warp, take);
@@ -212,7 +218,7 @@ __global__ void __launch_bounds__(256) k_fs_mass_list(FsArgs a) {
     const int n = cur_count(a);
     const uint32_t* list = cur_list(a);
     const bool first = a.cnt->first != 0;
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x) {
+    for (int w = chunk_first(); w < n; w += chunk_stride()) {
         const Node nd = node_at(a, list[w]);
         const long long i = nd.i;
         const double mi = a.mass[i];
@@ -245,7 +251,8 @@ __global__ void __launch_bounds__(256) k_fs_mass_list(FsArgs a) {
                     diff = fval<P>(a, opp(j), i) - fval<P>(a, j, src);
                 }
             }
-            dm += 1.0 * av * diff;
+            if (t == HB_T_FLUID) dm += diff;  // av = 1: the product 1.0 * av * diff is diff
+            else dm += 1.0 * av * diff;
         }
         a.mass2[i] = mi + dm;
     }
@@ -278,7 +285,7 @@ __global__ void __launch_bounds__(256) k_fs_classify(FsArgs a) {
     const int n = cur_count(a);
     const uint32_t* list = cur_list(a);
     const int n_up = (n + 31) / 32 * 32;
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n_up; w += gridDim.x * blockDim.x) {
+    for (int w = chunk_first(); w < n_up; w += chunk_stride()) {
         bool conv = false;
         uint32_t iu = 0u;
         if (w < n) {
@@ -309,7 +316,7 @@ __global__ void __launch_bounds__(256) k_fs_classify(FsArgs a) {
 __global__ void __launch_bounds__(256) k_fs_filled_parent(FsArgs a) {
     pdl_enter();
     const int n = min(a.cnt->ccount, (int)a.icap);
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x) {
+    for (int w = chunk_first(); w < n; w += chunk_stride()) {
         const uint32_t m = a.clist[w];
         if (!(a.flag[m] & FS_FILLED)) continue;
         const Node nd = node_at(a, m);
@@ -329,7 +336,7 @@ __global__ void __launch_bounds__(256) k_fs_new_from_filled(FsArgs a) {
     pdl_enter();
     const int n = min(a.cnt->ccount, (int)a.icap);
     const int n_up = (n + 31) / 32 * 32;
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n_up; w += gridDim.x * blockDim.x) {
+    for (int w = chunk_first(); w < n_up; w += chunk_stride()) {
         const uint32_t m = w < n ? a.clist[w] : 0u;
         const bool filled = w < n && (a.flag[m] & FS_FILLED);
         const Node nd = node_at(a, m);
@@ -383,7 +390,7 @@ __global__ void __launch_bounds__(256) k_fs_new_from_emptied(FsArgs a) {
     pdl_enter();
     const int n = min(a.cnt->ccount, (int)a.icap);
     const int n_up = (n + 31) / 32 * 32;
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n_up; w += gridDim.x * blockDim.x) {
+    for (int w = chunk_first(); w < n_up; w += chunk_stride()) {
         const uint32_t m = w < n ? a.clist[w] : 0u;
         const bool emptied = w < n && (a.flag[m] & FS_EMPTIED);
         const Node nd = node_at(a, m);
@@ -428,7 +435,7 @@ __global__ void __launch_bounds__(256) k_fs_mutants_to_fluid(FsArgs a) {
     const int nc = min(a.cnt->ccount, (int)a.icap);
     const int n0 = cur_count(a), nn = min(a.cnt->ncount, (int)a.icap);
     const int total = nc + n0 + nn;
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < total; w += gridDim.x * blockDim.x) {
+    for (int w = chunk_first(); w < total; w += chunk_stride()) {
         if (w < nc) {
             const uint32_t i = a.clist[w];
             const uint8_t fl = a.flag[i];
@@ -443,9 +450,11 @@ __global__ void __launch_bounds__(256) k_fs_mutants_to_fluid(FsArgs a) {
         uint32_t iu;
         if (!interface_cell(a, w - nc, n0, iu)) continue;
         const Node nd = node_at(a, iu);
+        // all 18 neighbour bytes at once (no early exit: the loads overlap); concurrent
+        // conversions in this pass turn interface cells into fluid, never into gas
         bool gas = false;
-        for (int j = 1; j < Q && !gas; ++j)
-            if (code_of(a, fs_link(a, nd, j)) == HB_T_GAS) gas = true;
+#pragma unroll
+        for (int j = 1; j < Q; ++j) gas |= code_of(a, fs_link(a, nd, j)) == HB_T_GAS;
         if (!gas) {
             ledger_add(a, a.mass[iu] - a.rho[iu]);
             a.mass[iu] = a.rho[iu];
@@ -463,14 +472,16 @@ __global__ void __launch_bounds__(256) k_fs_isolated_gas(FsArgs a) {
     const int t_up = (total + 31) / 32 * 32;
     uint32_t* next = next_list(a);
     int* ncount = &a.cnt->icount[a.cnt->sel ^ 1];
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < t_up; w += gridDim.x * blockDim.x) {
+    for (int w = chunk_first(); w < t_up; w += chunk_stride()) {
         uint32_t iu = 0u;
         bool keep = false;
         if (w < total && interface_cell(a, w, n0, iu) && (a.ntype[iu] & HB_TYPE_MASK) == HB_T_INTERFACE) {
             const Node nd = node_at(a, iu);
+            // all 18 neighbour bytes at once (no early exit: the loads overlap); concurrent
+            // conversions in this pass turn interface cells into gas, never into fluid
             bool fluid = false;
-            for (int j = 1; j < Q && !fluid; ++j)
-                if (code_of(a, fs_link(a, nd, j)) == HB_T_FLUID) fluid = true;
+#pragma unroll
+            for (int j = 1; j < Q; ++j) fluid |= code_of(a, fs_link(a, nd, j)) == HB_T_FLUID;
             if (!fluid) {
                 ledger_add(a, a.mass[iu]);
                 a.ntype[iu] = (a.ntype[iu] & ~HB_TYPE_MASK) | HB_T_GAS;
@@ -515,7 +526,7 @@ __global__ void __launch_bounds__(256) k_fs_redistribute(FsArgs a) {
     const int nc = min(a.cnt->ccount, (int)a.icap), nn = min(a.cnt->ncount, (int)a.icap);
     const uint32_t* list = cur_list(a);
     const double add = a.scal[2];
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n0 + nc + nn; w += gridDim.x * blockDim.x) {
+    for (int w = chunk_first(); w < n0 + nc + nn; w += chunk_stride()) {
         if (w < n0) {
             a.mass[list[w]] += add;
         } else if (w < n0 + nc) {
