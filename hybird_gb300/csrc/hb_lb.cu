@@ -903,7 +903,9 @@ template <class P>
 __global__ void k_mbb_refill_gs(MbbArgs a) {
     pdl_enter();
     const int n = *a.npop;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) mbb_refill_one<P>(a, k);
+    // consecutive entries to different blocks: a list of a few hundred nodes reaches
+    // every SM (its FP64 work would otherwise queue on the first two)
+    for (int k = blockIdx.x + gridDim.x * threadIdx.x; k < n; k += gridDim.x * blockDim.x) mbb_refill_one<P>(a, k);
 }
 
 // One thread per (changed node, node or one of its 18 links): the bulk bit and link mask of
@@ -913,7 +915,7 @@ __global__ void k_mbb_relink_gs(MbbArgs m, InitArgs a, PerFaces pf, unsigned lon
     pdl_enter();
     const long long np = *m.npop, nc = *m.nclaim;
     const long long total = (np + nc) * Q;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+    for (long long t = blockIdx.x + (long long)gridDim.x * threadIdx.x; t < total;  // spread over the blocks
          t += (long long)gridDim.x * blockDim.x) {
         const long long e = t / Q;
         const int j = (int)(t - e * Q);
