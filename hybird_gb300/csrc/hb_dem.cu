@@ -1614,7 +1614,7 @@ __device__ __forceinline__ void commit_when_last(const CoupleArgs& a, bool wrote
 // item, instead of each lane walking its own mix of node kinds.  A node that pops joins
 // the claim queue when a neighbour carries the flag.  Rows near a periodic face, or of a
 // length that is not a multiple of 4, take the general per-node rules.
-__global__ void __launch_bounds__(128) k_mask(CoupleArgs a) {
+__global__ void __launch_bounds__(128, 12) k_mask(CoupleArgs a) {
     __shared__ uint32_t s_pop[4][128];    // x | node byte << 16 | neighbour flags << 24
     __shared__ uint32_t s_psk[4][128];    // the particle of a queued particle node
     __shared__ uint32_t s_claim[4][128];  // x | neighbour flags << 16
