@@ -126,6 +126,53 @@ def test_dem_matches_reference_fixture(name, early_steps):
     g.close()
 
 
+def _kissing_cluster():
+    """A sphere with twelve neighbours in the cuboctahedral (kissing) arrangement, every
+    neighbour pressed 0.05 into it and into its four nearest neighbours, the lowest four
+    also 0.05 into the floor: the centre has twelve contacts (more than the eight lanes
+    of its element group, so its contacts take two rounds), the others four to six plus,
+    for four of them, the wall."""
+    r, gap = 3.0, 0.05
+    d = 2 * r - gap
+    dirs = []
+    for a, b in ((0, 1), (0, 2), (1, 2)):
+        for sa in (-1, 1):
+            for sb in (-1, 1):
+                v = np.zeros(3)
+                v[a], v[b] = sa, sb
+                dirs.append(v / np.sqrt(2.0))
+    zc = 0.5 + r - gap + d / np.sqrt(2.0)
+    centre = np.array([12.0, 12.0, zc])
+    spheres = [np.r_[centre, r]] + [np.r_[centre + d * v, r] for v in dirs]
+    return np.array(spheres)
+
+
+def test_dem_contacts_beyond_eight_per_element_fp64_vs_oracle():
+    """The contact path when an element has more contacts than its group has lanes and
+    when the wall shares a lane with particle contacts, against the FP64 oracle (the
+    reference's contact order) over the first cycles, before the summation-order
+    differences of stiff contacts grow."""
+    spheres = _kissing_cluster()
+    p = abi.make_params((24, 24, 24), (7,) * 6, init_visc=0.1, lbF=(0, 0, -1e-5), multi_step=10,
+                        collision=abi.HB_BGK)
+    g = _gpu()(p, spheres)
+    o = OracleSim(p, spheres, threads=4)
+    # the overlaps push the cluster apart within the first cycle's ten substeps; the floor
+    # enters at the first neighbour rebuild, during the second cycle
+    for c, n in enumerate((1, 1, 2)):
+        g.cycle(n)
+        o.cycle(n)
+        ge, oe = g.elements(), o.elements()
+        if c == 0:
+            assert np.abs(oe["x1"]).max() > 0.01  # the contact forces acted
+        for k in ("x0", "x1"):
+            assert rel_linf(ge[k], oe[k]) <= 1e-9, (k, rel_linf(ge[k], oe[k]))
+        # the arrangement is symmetric: spins are rounding noise (~1e-15) on both sides
+        assert np.abs(ge["w"] - oe["w"]).max() <= 1e-12
+    g.close()
+    o.close()
+
+
 def _channel(shape=(64, 32, 32), precision=abi.HB_FP64, collision=abi.HB_BGK, tau=0.8, magic=3 / 16):
     return abi.make_params(shape, (4, 4, 7, 7, 4, 4), init_visc=(tau - 0.5) / 3.0, lbF=(1e-6, 0, 0),
                            precision=precision, collision=collision, trt_magic=magic)
